@@ -1,0 +1,340 @@
+"""Benchmark: dynamics time step of the CUDA_STO_PF hot path on GB300.
+
+Workload (default): 246^3 grid, gp_zone model, 60 ellipsoidal precipitates
+(log-normal radii, median 6 cells, sigma_ln 0.3, aspect ratios U[0.5,1],
+random rotations, non-overlapping), 20 GP-zone eta sites of radius 3,
+heterogeneous elasticity S_p = C_Ag2Te - C_PbTe (cubic 60/25/15 vs
+108/7.7/13 GPa), zero mode on, FP32 fields with FP64 reductions and zero mode,
+dt = 0.01.  One step = one full dynamics time step (elastic fixed point,
+phi / eta Allen-Cahn, Y Cahn-Hilliard, zero-mode mass solve).
+
+Metric: cell-steps/s (N * steps / s, the reference's Mpts/s print).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: a single case does not shard (every 3D FFT is global); N > 1
+runs N independent replicas, one per rank ("replicas only"), with a barrier
+and max-over-ranks timing.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "cell-steps/s @246^3 elastic (dynamics step, gp_zone, heterogeneous S_p, zero mode)"
+PARAMS = os.path.join(REPO, "tests", "golden", "c2.params")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=246)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--elastic-tol", type=float, default=1e-6)
+    ap.add_argument("--cpu-sample-n", type=int, default=128)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-json", default="")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_params(capi, n, precision, tol):
+    p = capi.load_params_file(PARAMS)
+    p.Nx = p.Ny = p.Nz = n
+    p.model_mode = capi.MODEL_GP_ZONE
+    p.zero_mode_enabled = 1
+    p.precision = capi.PREC_FP32 if precision == "fp32" else capi.PREC_FP64
+    p.elastic_residual_tolerance = tol
+    capi.finalize(p)
+    return p
+
+
+def make_fields(capi, p, n, seed=2468):
+    from cuda_sto_pf_gb300 import workloads
+    count = max(1, int(round(60 * (n / 246.0) ** 3)))
+    sites = max(1, int(round(20 * (n / 246.0) ** 3)))
+    w = workloads.ellipsoid_population(n, count=count, eta_sites=sites, w=p.ic_phi_iface_w, seed=seed)
+    phi, xB, eta = w["phi"], w["xB"], w["eta"]
+    # raw-field rules of the reference loader (xB capped at its default
+    # xB_max_safe = 0.07)
+    st = capi.load().pfgb_prepare_raw_fields(ctypes.byref(p), 0.07, phi.ctypes.data, xB.ctypes.data,
+                                             eta.ctypes.data, None, phi.size)
+    assert st == 0
+    return phi, xB, eta, w["n_particles"], w["n_eta"]
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_oracle_rate(capi, n, precision, tol, threads=None, steps=1):
+    """Oracle (FP64 CPU restatement) cell-steps/s on a bounded sample: one
+    warm-up step (cold elastic start) + `steps` timed steps at n^3."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    from oracle_py import Oracle
+    p = make_params(capi, n, precision, tol)
+    phi, xB, eta, _, _ = make_fields(capi, p, n)
+    threads = threads or os.cpu_count() or 1
+    o = Oracle(p, threads=threads)
+    o.load(phi, xB, eta)
+    st = capi.StepStats()
+    o.step(1, st)
+    t0 = time.perf_counter()
+    rc = o.step(steps, st)
+    dt = time.perf_counter() - t0
+    return {"value": n ** 3 * steps / dt, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} warm step(s) of the workload generator at {n}^3 (same parameters; "
+                      f"one cold step untimed), FP64 oracle, {threads} OpenMP threads, rc={rc}",
+            "seconds": dt}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from cuda_sto_pf_gb300 import capi
+    capi.load(build_if_missing=True)
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    from oracle_py import Oracle
+    n = args.cpu_sample_n
+    p = make_params(capi, n, args.precision, args.elastic_tol)
+    phi, xB, eta, _, _ = make_fields(capi, p, n)
+    o = Oracle(p, threads=threads)
+    o.load(phi, xB, eta)
+    st = capi.StepStats()
+    for _ in range(args.warmup):
+        o.step(1, st)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step(1, st)
+    dt = time.perf_counter() - t0
+    v = n ** 3 * args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded microstructure generator)",
+            "config": {"workload": f"gp_zone dynamics, {n}^3 sample of the 246^3 workload", "grid": n,
+                       "reference_cpu_path": "none in the reference (GPU-only code); the CPU oracle port "
+                                             "restates its time step"},
+            "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"each step: one full dynamics step at {n}^3 (the 246^3 step "
+                                       f"does not fit the time budget on the host cores)"},
+            "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", init_method="env://")
+    dev = local
+    torch.cuda.set_device(dev)
+    from cuda_sto_pf_gb300 import capi
+    from cuda_sto_pf_gb300.solver import Solver
+    capi.load(build_if_missing=True)
+    n = args.n
+    N = n ** 3
+    p = make_params(capi, n, args.precision, args.elastic_tol)
+    phi, xB, eta, npart, neta = make_fields(capi, p, n)
+    stream = torch.cuda.current_stream(dev)
+    s = Solver(p, device=dev)
+    s.set_stream(stream.cuda_stream)
+    s.load(phi, xB, eta)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    stats = capi.StepStats()
+    iters = []
+    for _ in range(max(args.warmup, 3)):
+        stats = s.step(1)
+    # ---- device-resident timed region --------------------------------------
+    clocks = Clocks(dev)
+    barrier()
+    clocks.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.profile_enable(True)
+    ev0.record(stream)
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = s.step(1)
+        iters.append(st.elastic_iterations)
+    ev1.record(stream)
+    barrier()
+    wall = time.perf_counter() - w0
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    prof = s.profile_read()
+    launches = s.launches()
+    s.profile_enable(False)
+    t = torch.tensor([ms], device=f"cuda:{dev}")
+    if ws > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = ws * N * args.steps / (ms_max / 1e3)
+
+    # ---- e2e through the C ABI with pinned host buffers --------------------
+    e2e = None
+    if not args.no_e2e:
+        pin = {k: torch.empty(N, dtype=torch.float64).pin_memory() for k in ("phi", "xB", "Y", "eta", "dYdt")}
+        s.read_into(pin["phi"].data_ptr(), pin["xB"].data_ptr(), pin["Y"].data_ptr(), pin["eta"].data_ptr(),
+                    pin["dYdt"].data_ptr())
+        h2d = 4 * N * 8
+        d2h = 5 * N * 8
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            s.set_fields(pin["phi"].data_ptr(), pin["xB"].data_ptr(), pin["eta"].data_ptr(), pin["dYdt"].data_ptr())
+            s.step_nostats(1)
+            s.read_into(pin["phi"].data_ptr(), pin["xB"].data_ptr(), pin["Y"].data_ptr(), pin["eta"].data_ptr(),
+                        pin["dYdt"].data_ptr())
+        e1.record(stream)
+        barrier()
+        ems = e0.elapsed_time(e1)
+        te = torch.tensor([ems], device=f"cuda:{dev}")
+        if ws > 1:
+            import torch.distributed as dist
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        e2e = {"value": ws * N * args.steps / (float(te.item()) / 1e3), "unit": "cell-steps/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "what": "per step: pfgb_set_fields (4 float64 fields from pinned host) + pfgb_step + "
+                       "pfgb_read_fields (5 float64 fields to pinned host)"}
+
+    # ---- roofline of the dominant kernel ------------------------------------
+    peak, peak_kind = measured_peak()
+    prof.sort(key=lambda r: -r["ms"])
+    total_ms = sum(r["ms"] for r in prof) or 1.0
+    top = prof[0] if prof else None
+    roof = None
+    if top:
+        achieved = top["bytes"] / (top["ms"] / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": top["kernel"], "achieved": achieved, "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                "share": top["ms"] / total_ms,
+                "algorithmic_bytes_per_launch": top["bytes"] / max(1, top["launches"]),
+                "avg_launch_ms": top["ms"] / max(1, top["launches"])}
+    if args.profile_json and rank == 0:
+        with open(args.profile_json, "w") as f:
+            json.dump({"kernels": prof, "total_ms": total_ms, "launches": launches, "steps": args.steps,
+                       "iters": iters}, f, indent=1)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_oracle_rate(capi, args.cpu_sample_n, args.precision, args.elastic_tol)
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32" if args.precision == "fp32" else "f64",
+                "data": "synthetic (seeded microstructure generator, reference raw-field rules)",
+                "config": {"workload": f"{n}^3 gp_zone dynamics, {npart} ellipsoids + {neta} eta sites, "
+                                       f"heterogeneous elasticity, zero mode",
+                           "grid": n, "fields": args.precision, "elastic": "fp32",
+                           "elastic_tol": args.elastic_tol, "dt": p.dt,
+                           "l2": "inputs larger than L2 (working set > 1 GB at 246^3)",
+                           "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+                "elastic_iters_per_step": sum(iters) / max(1, len(iters)),
+                "wall_ms_per_step": 1e3 * wall / args.steps,
+                "gpu_launches": launches,
+                "clocks": clk, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    s.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,466 @@
+// fft.cuh — shared-memory mixed-radix FFT engine and 3D pass kernels.
+//
+// The 3D real transform of a C-order [Nx][Ny][Nz] grid is done in three
+// passes, each reading and writing the whole array once:
+//   z pass : real rows (contiguous, length Nz) <-> half spectra (NzC = Nz/2+1)
+//   y pass : complex lines of length Ny, element stride NzC
+//   x pass : complex lines of length Nx, element stride Ny*NzC
+// Each pass stages a tile of lines in shared memory and runs a Stockham
+// autosort FFT there (radices 8,4,2,3,5 coded, any other prime factor as a
+// direct DFT stage).  The passes take functors, so pointwise physics (RHS,
+// flux, eigenstrain/h_ij, stress) runs inside the z pass, and the spectral
+// updates (semi-implicit filters, gradients, Green's contraction) run inside
+// the x pass between the forward and the inverse x transform.
+//
+// Real-data trick: two real lines a, b are transformed as one complex line
+// z = a + i b;  A_k = (Z_k + conj Z_{N-k})/2, B_k = (Z_k - conj Z_{N-k})/(2i).
+// The inverse packs two half spectra the same way; the imaginary parts of the
+// k=0 and Nyquist bins are ignored (Hermitian input), like the C2R transform
+// of the reference.
+#pragma once
+
+#include "common.cuh"
+
+#define PFGB_MAX_STAGES 16
+#define PFGB_MAX_N 1024
+
+struct AxisPlan {
+    int n;
+    int nst;
+    int rad[PFGB_MAX_STAGES];
+};
+
+// host: factor n into radices (8 first, then 4, 2, 3, 5, other primes)
+static inline void pfgb_make_plan(int n, AxisPlan *p) {
+    p->n = n;
+    p->nst = 0;
+    int m = n;
+    while (m % 8 == 0 && m > 1) { p->rad[p->nst++] = 8; m /= 8; }
+    while (m % 4 == 0 && m > 1) { p->rad[p->nst++] = 4; m /= 4; }
+    while (m % 2 == 0 && m > 1) { p->rad[p->nst++] = 2; m /= 2; }
+    for (int f = 3; m > 1; f += 2)
+        while (m % f == 0) { p->rad[p->nst++] = f; m /= f; }
+}
+
+// ---------------------------------------------------------------------------
+// radix butterflies.  DIR = -1 forward (exp(-i..)), +1 inverse.
+// ---------------------------------------------------------------------------
+template <int DIR, typename T2> __device__ __forceinline__ T2 rot_mi(T2 a) {
+    // forward: multiply by -i ; inverse: by +i
+    return DIR < 0 ? mk2<T2>(a.y, -a.x) : mk2<T2>(-a.y, a.x);
+}
+
+template <typename T, int DIR>
+__device__ __forceinline__ void bfly2(cplx_t<T> *v) {
+    auto a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+}
+template <typename T, int DIR>
+__device__ __forceinline__ void bfly4(cplx_t<T> *v) {
+    auto t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+    auto t2 = cadd(v[1], v[3]), t3 = rot_mi<DIR>(csub(v[1], v[3]));
+    v[0] = cadd(t0, t2);
+    v[2] = csub(t0, t2);
+    v[1] = cadd(t1, t3);
+    v[3] = csub(t1, t3);
+}
+template <typename T, int DIR>
+__device__ __forceinline__ void bfly8(cplx_t<T> *v) {
+    using T2 = cplx_t<T>;
+    T2 e[4] = {v[0], v[2], v[4], v[6]};
+    T2 o[4] = {v[1], v[3], v[5], v[7]};
+    bfly4<T, DIR>(e);
+    bfly4<T, DIR>(o);
+    const T r = T(0.70710678118654752440084436210485);
+    // W8^1 = r(1 -+ i), W8^2 = -+i, W8^3 = r(-1 -+ i)
+    T2 o1 = DIR < 0 ? mk2<T2>(r * (o[1].x + o[1].y), r * (o[1].y - o[1].x))
+                    : mk2<T2>(r * (o[1].x - o[1].y), r * (o[1].y + o[1].x));
+    T2 o2 = rot_mi<DIR>(o[2]);
+    T2 o3 = DIR < 0 ? mk2<T2>(r * (o[3].y - o[3].x), -r * (o[3].x + o[3].y))
+                    : mk2<T2>(-r * (o[3].x + o[3].y), r * (o[3].x - o[3].y));
+    v[0] = cadd(e[0], o[0]); v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], o1);   v[5] = csub(e[1], o1);
+    v[2] = cadd(e[2], o2);   v[6] = csub(e[2], o2);
+    v[3] = cadd(e[3], o3);   v[7] = csub(e[3], o3);
+}
+template <typename T, int DIR>
+__device__ __forceinline__ void bfly3(cplx_t<T> *v) {
+    using T2 = cplx_t<T>;
+    const T s3 = T(0.86602540378443864676372317075294);
+    T2 a = v[0], s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+    T2 m = mk2<T2>(a.x - T(0.5) * s.x, a.y - T(0.5) * s.y);
+    T2 r = rot_mi<DIR>(cscale(d, s3));
+    v[0] = cadd(a, s);
+    v[1] = cadd(m, r);
+    v[2] = csub(m, r);
+}
+template <typename T, int DIR>
+__device__ __forceinline__ void bfly5(cplx_t<T> *v) {
+    using T2 = cplx_t<T>;
+    const T c1 = T(0.30901699437494742410229341718282);
+    const T c2 = T(-0.80901699437494742410229341718282);
+    const T s1 = T(0.95105651629515357211643933337938);
+    const T s2 = T(0.58778525229247312916870595463907);
+    T2 x0 = v[0];
+    T2 a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
+    T2 a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+    T2 p1 = mk2<T2>(x0.x + c1 * a1.x + c2 * a2.x, x0.y + c1 * a1.y + c2 * a2.y);
+    T2 p2 = mk2<T2>(x0.x + c2 * a1.x + c1 * a2.x, x0.y + c2 * a1.y + c1 * a2.y);
+    T2 q1 = rot_mi<DIR>(mk2<T2>(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y));
+    T2 q2 = rot_mi<DIR>(mk2<T2>(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y));
+    v[0] = mk2<T2>(x0.x + a1.x + a2.x, x0.y + a1.y + a2.y);
+    v[1] = cadd(p1, q1);
+    v[4] = csub(p1, q1);
+    v[2] = cadd(p2, q2);
+    v[3] = csub(p2, q2);
+}
+
+// twiddle w = W_n^e (table holds the forward roots); inverse uses conj
+template <int DIR, typename T2>
+__device__ __forceinline__ T2 twmul(T2 a, T2 w) {
+    return DIR < 0 ? cmul(a, w) : cmulconj(a, w);
+}
+
+// ---------------------------------------------------------------------------
+// fft_lines: transform nl lines of length p.n held in shared memory.
+// Element (line l, position q) lives at buf[q*sp + l*sl].  Stockham stages
+// alternate between `a` and `b`; returns the buffer holding the result.
+// lineFast: consecutive threads walk positions of one line (sp == 1);
+// otherwise consecutive threads walk lines (sl == 1).
+// Must be called by all threads of the block; ends with __syncthreads().
+// ---------------------------------------------------------------------------
+template <typename T, int DIR>
+__device__ cplx_t<T> *fft_lines(cplx_t<T> *a, cplx_t<T> *b, const AxisPlan &p,
+                                const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast) {
+    using T2 = cplx_t<T>;
+    const int n = p.n;
+    int Ns = 1;
+    T2 *src = a, *dst = b;
+    for (int s = 0; s < p.nst; ++s) {
+        const int R = p.rad[s];
+        const int nb = n / R;
+        const int m = n / (Ns * R);
+        if (R == 2 || R == 3 || R == 4 || R == 5 || R == 8) {
+            const int work = nl * nb;
+            for (int w = threadIdx.x; w < work; w += blockDim.x) {
+                int j, l;
+                if (lineFast) { j = w % nb; l = w / nb; } else { l = w % nl; j = w / nl; }
+                const int k = j % Ns;
+                T2 v[8];
+                const T2 *sb = src + l * sl;
+#pragma unroll 8
+                for (int r = 0; r < 8; ++r) {
+                    if (r < R) {
+                        T2 x = sb[(j + r * nb) * sp];
+                        v[r] = (r == 0) ? x : twmul<DIR>(x, tw[r * k * m]);
+                    }
+                }
+                switch (R) {
+                    case 2: bfly2<T, DIR>(v); break;
+                    case 3: bfly3<T, DIR>(v); break;
+                    case 4: bfly4<T, DIR>(v); break;
+                    case 5: bfly5<T, DIR>(v); break;
+                    default: bfly8<T, DIR>(v); break;
+                }
+                T2 *db = dst + l * sl;
+                const int base = (j / Ns) * Ns * R + k;
+#pragma unroll 8
+                for (int r = 0; r < 8; ++r)
+                    if (r < R) db[(base + r * Ns) * sp] = v[r];
+            }
+        } else {
+            // direct DFT stage: one output per work item,
+            // out_q = sum_r x_r W_n^{r (k m + q n/R)}  (exponent mod n)
+            const int work = nl * n;
+            for (int w = threadIdx.x; w < work; w += blockDim.x) {
+                int o, l;
+                if (lineFast) { o = w % n; l = w / n; } else { l = w % nl; o = w / nl; }
+                const int j = o % nb, q = o / nb;
+                const int k = j % Ns;
+                int e = k * m + q * nb;
+                if (e >= n) e -= n;
+                const T2 *sb = src + l * sl;
+                T ar = 0, ai = 0;
+                int idx = 0;
+                for (int r = 0; r < R; ++r) {
+                    T2 x = sb[(j + r * nb) * sp];
+                    T2 t = tw[idx];
+                    if (DIR < 0) { ar += x.x * t.x - x.y * t.y; ai += x.x * t.y + x.y * t.x; }
+                    else { ar += x.x * t.x + x.y * t.y; ai += x.y * t.x - x.x * t.y; }
+                    idx += e;
+                    if (idx >= n) idx -= n;
+                }
+                const int base = (j / Ns) * Ns * R + k;
+                dst[l * sl + (base + q * Ns) * sp] = mk2<T2>(ar, ai);
+            }
+        }
+        __syncthreads();
+        T2 *t = src; src = dst; dst = t;
+        Ns *= R;
+    }
+    return src;
+}
+
+// load the twiddle table of length n into shared memory
+template <typename T>
+__device__ __forceinline__ void load_tw(cplx_t<T> *s, const cplx_t<T> *g, int n) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = g[i];
+}
+
+// 3D grid description passed to every pass kernel
+struct Grid3 {
+    int Nx, Ny, Nz, NzC;
+    long long N, Nk;
+};
+
+// ---------------------------------------------------------------------------
+// Strided axis pass (y or x).  A block owns TK consecutive kz columns of one
+// (i) slab (y pass) or one (j) slab (x pass): lines of length n, element
+// stride `es`.  Inputs are transformed with direction DIN (0 = none),
+// combined point by point by op.apply(i, j, k, vin, vout), and outputs are
+// transformed with DOUT (0 = none) and stored.
+// ---------------------------------------------------------------------------
+template <typename T, int NIN, int NOUT>
+struct AxisIO {
+    const cplx_t<T> *in[NIN > 0 ? NIN : 1];
+    cplx_t<T> *out[NOUT > 0 ? NOUT : 1];
+};
+
+template <typename T, int NIN, int NOUT, int DIN, int DOUT, class Op>
+__global__ void __launch_bounds__(256)
+k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
+            AxisIO<T, NIN, NOUT> io, Op op) {
+    using T2 = cplx_t<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2 *sm = reinterpret_cast<T2 *>(smem_raw);
+    const int n = plan.n;
+    T2 *tw = sm;                       // n
+    T2 *bufs = sm + n;                 // (NIN + NOUT + 1) * n * TK
+    const int tile = n * TK;
+    T2 *bin[NIN > 0 ? NIN : 1];
+    T2 *bout[NOUT > 0 ? NOUT : 1];
+    constexpr bool INPL = Op::kInplace;   // identity op: outputs reuse inputs
+#pragma unroll
+    for (int a = 0; a < NIN; ++a) bin[a] = bufs + a * tile;
+#pragma unroll
+    for (int a = 0; a < NOUT; ++a) bout[a] = INPL ? bin[a] : bufs + (NIN + a) * tile;
+    T2 *scr = bufs + (INPL ? NIN : NIN + NOUT) * tile;
+
+    const int k0 = blockIdx.x * TK;
+    const int slab = blockIdx.y;       // i for the y pass, j for the x pass
+    long long base, es;
+    if (axis == 1) { base = (long long)slab * g.Ny * g.NzC + k0; es = g.NzC; }
+    else { base = (long long)slab * g.NzC + k0; es = (long long)g.Ny * g.NzC; }
+    const int kcnt = min(TK, g.NzC - k0);
+
+    if (DIN != 0 || DOUT != 0) load_tw<T>(tw, tw_g, n);
+#pragma unroll
+    for (int a = 0; a < NIN; ++a) {
+        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+            const int q = e / TK, l = e - q * TK;
+            T2 v = mk2<T2>(T(0), T(0));
+            if (l < kcnt) v = io.in[a][base + q * es + l];
+            bin[a][e] = v;
+        }
+    }
+    __syncthreads();
+    if (DIN != 0) {
+#pragma unroll
+        for (int a = 0; a < NIN; ++a) {
+            T2 *r = fft_lines<T, DIN>(bin[a], scr, plan, tw, TK, TK, 1, false);
+            if (r == scr) { scr = bin[a]; bin[a] = r; }
+        }
+    }
+    if constexpr (INPL) {
+        static_assert(NIN == NOUT, "in-place axis op needs NIN == NOUT");
+#pragma unroll
+        for (int a = 0; a < NOUT; ++a) bout[a] = bin[a];
+    }
+    if constexpr (!INPL) {
+        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+            const int q = e / TK, l = e - q * TK;
+            const int k = k0 + l;
+            const int i = (axis == 1) ? slab : q;
+            const int j = (axis == 1) ? q : slab;
+            T2 vin[NIN > 0 ? NIN : 1], vout[NOUT > 0 ? NOUT : 1];
+#pragma unroll
+            for (int a = 0; a < NIN; ++a) vin[a] = bin[a][e];
+            op.apply(i, j, k, vin, vout);
+#pragma unroll
+            for (int a = 0; a < NOUT; ++a) bout[a][e] = vout[a];
+        }
+        __syncthreads();
+    }
+    if (DOUT != 0) {
+#pragma unroll
+        for (int a = 0; a < NOUT; ++a) {
+            T2 *r = fft_lines<T, DOUT>(bout[a], scr, plan, tw, TK, TK, 1, false);
+            if (r == scr) { scr = bout[a]; bout[a] = r; }
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < NOUT; ++a) {
+        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+            const int q = e / TK, l = e - q * TK;
+            if (l < kcnt) io.out[a][base + q * es + l] = bout[a][e];
+        }
+    }
+}
+
+// identity op for plain axis transforms
+template <typename T, int NF>
+struct OpCopy {
+    static constexpr bool kInplace = true;
+    __device__ __forceinline__ void apply(int, int, int, const cplx_t<T> *vin, cplx_t<T> *vout) const {
+#pragma unroll
+        for (int a = 0; a < NF; ++a) vout[a] = vin[a];
+    }
+};
+
+// ---------------------------------------------------------------------------
+// z pass: R consecutive rows per block.  Inputs: NFI half spectra per row
+// (op.load_spec), inverse-transformed to real (C2R, unnormalised); then
+// op.point(cell, in[NFI], out[NFO]) per cell; then NFO real fields are
+// forward-transformed (R2C) and handed to op.store_spec(row, kz, v[NFO]).
+// NFI = 0 makes it a pure R2C pass with a pointwise producer, NFO = 0 a pure
+// C2R pass with a pointwise consumer.
+// Real lines are paired (line 2p -> real part, 2p+1 -> imaginary part of
+// complex line p); line index = row * NF + field.
+// ---------------------------------------------------------------------------
+// Reduction hook of the z pass: an op declares `struct Acc` with
+// kActive, identity(), combine(a, b) and shuffle-able members (reduced with
+// warp shuffles + shared memory, deterministic for a fixed launch shape).
+struct NoAcc {
+    static constexpr bool kActive = false;
+    __device__ static NoAcc identity() { return NoAcc(); }
+};
+
+template <class Acc>
+__device__ void block_reduce_acc(Acc &a) {
+    __shared__ Acc red[32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) a = Acc::combine(a, Acc::shfl_down(a, off));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = a;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        a = (lane < nw) ? red[lane] : Acc::identity();
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) a = Acc::combine(a, Acc::shfl_down(a, off));
+    }
+}
+
+template <typename T, int NFI, int NFO, class Op>
+__global__ void __launch_bounds__(256)
+k_zpass(Grid3 g, AxisPlan plan, const cplx_t<T> *tw_g, int R, Op op) {
+    using T2 = cplx_t<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2 *sm = reinterpret_cast<T2 *>(smem_raw);
+    const int n = g.Nz, nc = g.NzC;
+    T2 *tw = sm;
+    T2 *ws = sm + n;
+    const int PI_ = (NFI > 0) ? (R * NFI + 1) / 2 : 0;
+    const int PO_ = (NFO > 0) ? (R * NFO + 1) / 2 : 0;
+    T2 *inA = ws, *inB = ws + PI_ * n;
+    T2 *outA = ws + 2 * PI_ * n, *outB = outA + PO_ * n;
+    const long long row0 = (long long)blockIdx.x * R;
+    const long long nrows = (long long)g.Nx * g.Ny;
+    const int rcnt = (int)min((long long)R, nrows - row0);
+    load_tw<T>(tw, tw_g, n);
+
+    if (NFI > 0) {
+        // pack pairs of half spectra into full complex spectra
+        for (int e = threadIdx.x; e < PI_ * nc; e += blockDim.x) {
+            const int p = e / nc, k = e - p * nc;
+            T2 A = mk2<T2>(T(0), T(0)), B = mk2<T2>(T(0), T(0));
+            const int la = 2 * p, lb = 2 * p + 1;
+            const int ra = la / (NFI > 0 ? NFI : 1), fa = la - ra * (NFI > 0 ? NFI : 1);
+            const int rb = lb / (NFI > 0 ? NFI : 1), fb = lb - rb * (NFI > 0 ? NFI : 1);
+            T2 v[NFI > 0 ? NFI : 1];
+            if (ra < rcnt) {
+                op.load_spec(row0 + ra, k, v);
+                A = v[fa];
+                if (rb == ra) B = v[fb];
+            }
+            if (rb != ra && rb < rcnt) {
+                op.load_spec(row0 + rb, k, v);
+                B = v[fb];
+            }
+            if (k == 0 || 2 * k == n) { A.y = T(0); B.y = T(0); }
+            // Z_k = A_k + i B_k ; Z_{n-k} = conj(A_k) + i conj(B_k)
+            inA[p * n + k] = mk2<T2>(A.x - B.y, A.y + B.x);
+            if (k > 0 && 2 * k != n) inA[p * n + (n - k)] = mk2<T2>(A.x + B.y, B.x - A.y);
+        }
+        __syncthreads();
+        T2 *r = fft_lines<T, +1>(inA, inB, plan, tw, PI_, 1, n, true);
+        if (r != inA) { inB = inA; inA = r; }
+    }
+    // pointwise stage
+    typename Op::Acc acc = Op::Acc::identity();
+    for (int e = threadIdx.x; e < R * n; e += blockDim.x) {
+        const int r = e / n, z = e - r * n;
+        if (r >= rcnt) {
+            if (NFO > 0) {
+#pragma unroll
+                for (int f = 0; f < NFO; ++f) {
+                    const int l = r * NFO + f;
+                    T *dst = reinterpret_cast<T *>(&outA[(l >> 1) * n + z]);
+                    dst[l & 1] = T(0);
+                }
+            }
+            continue;
+        }
+        T vi[NFI > 0 ? NFI : 1], vo[NFO > 0 ? NFO : 1];
+#pragma unroll
+        for (int f = 0; f < NFI; ++f) {
+            const int l = r * NFI + f;
+            const T *src = reinterpret_cast<const T *>(&inA[(l >> 1) * n + z]);
+            vi[f] = src[l & 1];
+        }
+        const long long cell = (row0 + r) * n + z;
+        op.point(cell, vi, vo, acc);
+#pragma unroll
+        for (int f = 0; f < NFO; ++f) {
+            const int l = r * NFO + f;
+            T *dst = reinterpret_cast<T *>(&outA[(l >> 1) * n + z]);
+            dst[l & 1] = vo[f];
+        }
+    }
+    if constexpr (Op::Acc::kActive) {
+        block_reduce_acc(acc);
+        if (threadIdx.x == 0) op.finish(blockIdx.x, acc);
+    }
+    if (NFO > 0) {
+        // odd line count: zero the unused imaginary line
+        if ((R * NFO) & 1) {
+            const int l = R * NFO;
+            for (int z = threadIdx.x; z < n; z += blockDim.x) {
+                T *dst = reinterpret_cast<T *>(&outA[(l >> 1) * n + z]);
+                dst[1] = T(0);
+            }
+        }
+        __syncthreads();
+        T2 *r = fft_lines<T, -1>(outA, outB, plan, tw, PO_, 1, n, true);
+        if (r != outA) { outB = outA; outA = r; }
+        // unpack and store: per (row, kz) gather all NFO fields
+        for (int e = threadIdx.x; e < rcnt * nc; e += blockDim.x) {
+            const int rr = e / nc, k = e - rr * nc;
+            T2 v[NFO > 0 ? NFO : 1];
+#pragma unroll
+            for (int f = 0; f < NFO; ++f) {
+                const int l = rr * NFO + f, p = l >> 1;
+                const T2 Zk = outA[p * n + k];
+                const T2 Zm = outA[p * n + (k == 0 ? 0 : n - k)];
+                // A_k = (Z_k + conj Z_-k)/2 ; B_k = (Z_k - conj Z_-k)/(2i)
+                if ((l & 1) == 0) v[f] = mk2<T2>(T(0.5) * (Zk.x + Zm.x), T(0.5) * (Zk.y - Zm.y));
+                else v[f] = mk2<T2>(T(0.5) * (Zk.y + Zm.y), T(0.5) * (Zm.x - Zk.x));
+            }
+            op.store_spec(row0 + rr, k, v);
+        }
+    } else {
+        __syncthreads();
+    }
+}

@@ -1,0 +1,223 @@
+// physics.cuh — pointwise physics of the CUDA_STO_PF model, shared by the
+// fused pass ops.  T = field precision, TE = elastic precision.
+#pragma once
+
+#include "common.cuh"
+
+// Index of Voigt pair (a,b), 0-based, into the 21-vector
+// 11 12 13 14 15 16 22 23 24 25 26 33 34 35 36 44 45 46 55 56 66.
+__host__ __device__ __forceinline__ int vidx(int a, int b) {
+    int lo = a < b ? a : b, hi = a < b ? b : a;
+    int start = lo == 0 ? 0 : lo == 1 ? 6 : lo == 2 ? 11 : lo == 3 ? 15 : lo == 4 ? 18 : 20;
+    return start + (hi - lo);
+}
+// tensor (i,j) -> Voigt index 0..5 (xx,yy,zz,yz,xz,xy)
+__host__ __device__ __forceinline__ int tvoigt(int i, int j) {
+    if (i == j) return i;
+    int s = i + j;              // (1,2)->3 yz, (0,2)->2 -> xz, (0,1)->1 -> xy
+    return s == 3 ? 3 : (s == 2 ? 4 : 5);
+}
+
+// Constants of the physics, FP64 on the host, passed by value to kernels.
+struct PhysC {
+    // grid / time
+    double dt, invN;
+    // Allen-Cahn phi
+    double W, kappa, Lphi;
+    // transport
+    double Da, Dc;
+    double vA, vB, Vm0, dVm, Vmc;
+    double mu0, eiv, Yclip, xBeps, hscale;
+    double Cdmu;            // mu0 - vA GA_s - vB GB_s - shift (cancellation-free delta_mu)
+    double dG;              // GB_s - GA_s
+    double shift;
+    double e00[6], E0[6];
+    double S[21], Sp[21];
+    // GP zone
+    double gpxB, gpW, gpkap, gpL, gpMGP, gpMb, gpeiso, gpscale;
+    double gp_Cg;           // offA(xg)(1-xg) + offB(xg) xg - delta_g0
+    int gp, gp_el, act_eta, act_phi;
+    int coupling, elastic, zm, prev_level, disable_gamma, xb_raw;
+    ThermoConst tc;
+};
+
+// Elastic constants in elastic precision (the reference casts S, S_p, eps00,
+// E0 to float, main_cuda.cu:28762-28790).
+template <typename TE>
+struct ElasC {
+    TE S[21], Sp[21], e00[6], E0[6];
+    TE invN;
+};
+
+// xB from the logit Y: clipped form (sigmoid_from_logit) unless the zero mode
+// owns the composition, which uses the unclipped logistic
+// (apply_pf_Y_zero_mode_shift_kernel, cuda_kernels.cu:3434-3442).
+template <typename T>
+__device__ __forceinline__ T xB_of_Y(const PhysC &c, T Y) {
+    return c.xb_raw ? sigmoid_raw(Y) : sigmoid_clip(Y, T(c.Yclip), T(c.xBeps));
+}
+
+// eigenstrain_phi_xB_point / eigenstrain_phi_eta_xB_point
+// (cuda_kernels.cu:193-290); gp3 selects the three-phase GP form.
+template <typename T, typename TE>
+__device__ __forceinline__ void eigenstrain(const PhysC &c, const ElasC<TE> &ec, T phi, T eta,
+                                            T xBc, bool gp3, TE e0[6]) {
+    if (!gp3) {
+        T h = pf_h(phi);
+        T epsc = xBc * T(c.eiv);
+        T omh = T(1) - h;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) e0[a] = (TE)(omh * epsc + h * T(ec.e00[a]));
+#pragma unroll
+        for (int a = 3; a < 6; ++a) e0[a] = (TE)(h * T(ec.e00[a]));
+        return;
+    }
+    T hb = pf_h(phi), he = pf_h(eta);
+    T hg = (T(1) - hb) * he, ha = (T(1) - hb) * (T(1) - he);
+    T ea = xBc * T(c.eiv);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) e0[a] = (TE)(ha * ea + hg * T(c.gpeiso) + hb * T(ec.e00[a]));
+#pragma unroll
+    for (int a = 3; a < 6; ++a) e0[a] = (TE)(hb * T(ec.e00[a]));
+}
+
+// Hooke's law with C_eff = C0 + h dC on the elastic strain eps - eps0,
+// engineering shear (compute_stress_from_strain_with_effective_stiffness_kernel,
+// cuda_kernels.cu:7381-7480).
+template <typename T, typename TE>
+__device__ __forceinline__ void stress_at(const PhysC &c, const ElasC<TE> &ec, T phi, T eta, T xB,
+                                          const TE eps[6], TE sig[6]) {
+    TE e0[6];
+    eigenstrain<T, TE>(c, ec, phi, eta, clamp01(xB), c.gp_el != 0, e0);
+    TE el[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) el[a] = eps[a] - e0[a];
+    const T h = pf_h(phi);
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+        TE acc = 0;
+#pragma unroll
+        for (int b = 0; b < 6; ++b) {
+            const int v = vidx(a, b);
+            TE ce = ec.S[v] + (TE)(h * T(ec.Sp[v]));
+            acc += (b >= 3 ? TE(2) * ce : ce) * el[b];
+        }
+        sig[a] = acc;
+    }
+}
+
+// e^T dC e with engineering shear (compute_Q_voigt, cuda_kernels.cu:162-181)
+template <typename T>
+__device__ __forceinline__ T q_voigt(const double *Sp, const T el[6]) {
+    T e[6] = {el[0], el[1], el[2], T(2) * el[3], T(2) * el[4], T(2) * el[5]};
+    T q = 0;
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+        q += T(Sp[vidx(a, a)]) * e[a] * e[a];
+#pragma unroll
+        for (int b = a + 1; b < 6; ++b) q += T(2) * T(Sp[vidx(a, b)]) * e[a] * e[b];
+    }
+    return q;
+}
+
+// explicit Allen-Cahn driving force of phi (compute_phi_rhs_kernel,
+// cuda_kernels.cu:390-555): double well + chemical + elastic.
+template <typename T, typename TE>
+__device__ __forceinline__ T phi_rhs(const PhysC &c, const ElasC<TE> &ec, T phi, T eta_raw, T xBraw,
+                                     const TE *eps) {
+    const T hp = pf_hp(phi), gp = pf_gp(phi), h = pf_h(phi);
+    const T eta = clamp01(eta_raw);
+    const T xB = clamp01(xBraw);
+    T f = T(c.W) * gp;
+    T offA, offB;
+    thermo_mu_off<T>(c.tc, xB, offA, offB);
+    const T dmu = T(c.Cdmu) - T(c.vA) * offA - T(c.vB) * offB;
+    const T cb = c_xB_phi<T>(xB, T(c.Vm0), T(c.dVm), T(c.Vmc), h);
+    const T muA = T(c.tc.GA_s) + offA, muB = T(c.tc.GB_s) + offB;
+    const T mt = (T(1) - h) * (muA * (T(1) - xB) + muB * xB) + h * T(c.mu0);
+    const T Vma = T(c.Vm0) + T(c.dVm) * xB;
+    const T vt = T(c.Vmc) - Vma + T(c.dVm) * (xB - T(c.vB));
+    f += cb * hp * (dmu - cb * mt * vt);
+    if (c.coupling) {
+        TE sg_[6];
+        stress_at<T, TE>(c, ec, phi, eta_raw, xBraw, eps, sg_);
+        T sg[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) sg[a] = T(sg_[a]);
+        // eps0 of the two-phase form with float eps00 (as the reference)
+        TE e0[6];
+        eigenstrain<T, TE>(c, ec, phi, eta, xB, false, e0);
+        T el[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) el[a] = T(eps[a]) - T(e0[a]);
+        const T Q = q_voigt<T>(c.Sp, el);
+        T part;
+        const T eps_alpha = xB * T(c.eiv);
+        const T diag = -eps_alpha + T(c.eiv) * (xB - T(c.vB));
+        if (c.gp_el && c.act_phi) {
+            // compute_dgel_dphi_gp_point, cuda_kernels.cu:313-372
+            const T he = pf_h(eta);
+            T de[6];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                de[a] = hp * (T(c.e00[a]) + (T(1) - he) * diag - he * T(c.gpeiso));
+#pragma unroll
+            for (int a = 3; a < 6; ++a) de[a] = hp * T(c.e00[a]);
+            T dg = -(sg[0] * de[0] + sg[1] * de[1] + sg[2] * de[2] + T(2) * sg[5] * de[5] +
+                     T(2) * sg[4] * de[4] + T(2) * sg[3] * de[3]);
+            part = T(c.gpscale) * (dg + T(0.5) * hp * Q);
+        } else {
+            T de[6];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) de[a] = hp * (T(c.e00[a]) + diag);
+#pragma unroll
+            for (int a = 3; a < 6; ++a) de[a] = hp * T(c.e00[a]);
+            T dg = -(sg[0] * de[0] + sg[1] * de[1] + sg[2] * de[2] + T(2) * sg[5] * de[5] +
+                     T(2) * sg[4] * de[4] + T(2) * sg[3] * de[3]);
+            part = dg + T(0.5) * hp * Q;
+        }
+        f += part;
+    }
+    return f;
+}
+
+// GP-zone Allen-Cahn driving force of eta (compute_eta_rhs_kernel,
+// non-raw-drive branch, cuda_kernels.cu:845-946)
+template <typename T, typename TE>
+__device__ __forceinline__ T eta_rhs(const PhysC &c, const ElasC<TE> &ec, T eta_raw, T phi_raw,
+                                     T xBraw, T sig_hydro) {
+    const T eta = clamp01(eta_raw), phi = clamp01(phi_raw);
+    const T xa = clamp_eps(xBraw, T(1e-12));
+    const T hphi = pf_h(phi), hpe = pf_hp(eta), gpe = pf_gp(eta);
+    const T cref = T(1) / (T(c.Vm0) + T(c.dVm) * xa);
+    T offA, offB;
+    thermo_mu_off<T>(c.tc, xa, offA, offB);
+    // g_gp - g_alpha without cancelling the compound constants
+    const T dgg = T(c.dG) * (T(c.gpxB) - xa) + T(c.gp_Cg) - (offA * (T(1) - xa) + offB * xa);
+    const T d = cref * (T(1) - hphi) * hpe * dgg;
+    T el = 0;
+    if (c.gp_el && c.act_eta) {
+        const T pre = (T(1) - pf_h(phi)) * pf_hp(eta);
+        const T ea = clamp01(xa) * T(c.eiv);
+        el = T(c.gpscale) * (-sig_hydro * (pre * (T(c.gpeiso) - ea)));
+    }
+    (void)ec;
+    return d + T(c.gpW) * gpe + el;
+}
+
+// transport mobility (compute_flux_single_component_kernel :1985 and the
+// GP variant :2039)
+template <typename T>
+__device__ __forceinline__ T mobility(const PhysC &c, T phiY, T etaN, T xBp) {
+    if (!c.gp) {
+        const T h = pf_h(phiY);
+        const T Dm = (T(1) - h) * T(c.Da) + h * T(c.Dc);
+        const T G = gamma_thermo<T>(c.tc, xBp, h, T(c.Vm0), T(c.dVm), T(c.Vmc));
+        return stabilized_meff<T>(Dm, G);
+    }
+    const T hb = pf_h(phiY), he = pf_h(etaN);
+    const T hg = (T(1) - hb) * he, ha = (T(1) - hb) * (T(1) - he);
+    const T Ga = gamma_thermo<T>(c.tc, xBp, T(0), T(c.Vm0), T(c.dVm), T(c.Vmc));
+    const T Ma = stabilized_meff<T>(T(c.Da), Ga);
+    return ha * Ma + hg * T(c.gpMGP) + hb * T(c.gpMb);
+}

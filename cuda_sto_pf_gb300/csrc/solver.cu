@@ -1,0 +1,1756 @@
+// solver.cu — pfgb context, fused pass ops and the dynamics step.
+//
+// One dynamics step (reference sequence main_cuda.cu:28427-31623) becomes:
+//   elastic  : [z eigen->R2C] [y] [x Green0 + strain] [y^-1]          (cold)
+//              [x strain(u)] [y^-1]                                    (warm)
+//              { [z C2R->h_ij->R2C] [y] [x Green(h)+resid+strain] [y^-1] } x iters
+//              [z C2R -> eps + E0]
+//   phi      : [z phi - L dt rhs -> R2C] [y] [x filter] [y^-1] [z C2R -> clamp]
+//   eta (GP) : same as phi
+//   Y        : [z mu -> R2C, sum DY] [y] [x grad] [y^-1]
+//              [z C2R grad -> J = M grad, T, Y^n -> R2C] [y combine] [x update] [y^-1]
+//              [z C2R -> clamp/store, zero-mode moments]
+// Mathematically identical to the reference sequence (every dealias mask,
+// the Laplacian and the Y^n transform folded into the linear spectral
+// filters; see the op comments), with Y carried as Y_f + c where the scalar
+// offset c (FP64) absorbs the zero-mode shift.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fft.cuh"
+#include "physics.cuh"
+
+const char *pfgb_error_buffer(void);
+
+// ---------------------------------------------------------------------------
+// device state
+// ---------------------------------------------------------------------------
+struct KTab {
+    const double *kx, *ky, *kz;
+    const unsigned char *mx, *my, *mz;   // 1 = removed by the 2/3 rule
+    __device__ __forceinline__ bool cut(int i, int j, int k) const { return (mx[i] | my[j] | mz[k]) != 0; }
+    __device__ __forceinline__ double k2(int i, int j, int k) const {
+        double a = kx[i], b = ky[j], c = kz[k];
+        return a * a + b * b + c * c;
+    }
+};
+
+template <typename T, typename TE>
+struct DevState {
+    Grid3 g;
+    KTab kt;
+    T *phi_old, *phi_new, *eta_old, *eta_new, *Y, *dYdt;
+    TE *eps[6];
+    cplx_t<T> *S[4];
+    cplx_t<TE> *E[6], *U[3];
+    double *partials;
+    double *dscal;
+    double Yc, dYoff;   // Y = Y_f + Yc ; dY/dt = dYdt_f + dYoff
+};
+
+// device scalar slots
+enum { DS_MEAN_DY = 0, DS_RES_DIFF = 1, DS_RES_REF = 2, DS_ZM = 4, DS_BR = 12, DS_EV = 16, DS_N = 24 };
+
+struct pfgb_ctx {
+    pfgb_params p;
+    int device = 0;
+    cudaStream_t stream = 0;
+    Grid3 g;
+    AxisPlan plx, ply, plz;
+    void *tw[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};  // [fp64|fp32][x,y,z]
+    double *kx = nullptr, *ky = nullptr, *kz = nullptr;
+    unsigned char *mx = nullptr, *my = nullptr, *mz = nullptr;
+    void *phi[2] = {nullptr, nullptr}, *eta[2] = {nullptr, nullptr}, *Y = nullptr, *dYdt = nullptr;
+    int cur = 0, ecur = 0;
+    void *S[4] = {nullptr, nullptr, nullptr, nullptr};
+    void *eps[6] = {}, *E[6] = {}, *U[3] = {};
+    double *partials = nullptr, *dscal = nullptr, *hscal = nullptr;
+    double *stage = nullptr;          // host<->device staging, 5 N doubles, lazily allocated
+    size_t npartials = 0;
+    double Yc = 0.0, dYoff = 0.0, target_mass = 0.0;
+    int warm_valid = 0, step = 0, loaded = 0;
+    size_t bytes = 0;
+    std::string err;
+    PhysC pc;
+    // launch accounting / optional per-kernel event timing
+    long long launches = 0;
+    int prof = 0;
+    struct Rec { const char *tag; cudaEvent_t a, b; double bytes; };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    size_t pool_used = 0;
+};
+
+// tag + algorithmic bytes of the next launch (set by the op-level wrappers)
+struct LaunchTag { const char *tag; double bytes; };
+
+static cudaEvent_t prof_event(pfgb_ctx *c) {
+    if (c->pool_used == c->pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        c->pool.push_back(e);
+    }
+    return c->pool[c->pool_used++];
+}
+
+struct ProfScope {
+    pfgb_ctx *c; LaunchTag t; cudaEvent_t a = nullptr;
+    ProfScope(pfgb_ctx *c_, LaunchTag t_) : c(c_), t(t_) {
+        c->launches++;
+        if (c->prof && (a = prof_event(c))) cudaEventRecord(a, c->stream);
+    }
+    ~ProfScope() {
+        if (c->prof && a) {
+            cudaEvent_t b = prof_event(c);
+            if (b) {
+                cudaEventRecord(b, c->stream);
+                c->recs.push_back({t.tag, a, b, t.bytes});
+            }
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+static const size_t kSmemBudget = 112 * 1024;
+
+template <typename K>
+static cudaError_t allow_smem(K kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <typename T>
+static const cplx_t<T> *twp(const pfgb_ctx *c, int axis) {
+    return (const cplx_t<T> *)c->tw[sizeof(T) == 8 ? 0 : 1][axis];
+}
+
+template <typename T, int NIN, int NOUT, int DIN, int DOUT, class Op>
+static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, Op op, const char *tag) {
+    using T2 = cplx_t<T>;
+    const AxisPlan &pl = axis == 1 ? c->ply : c->plx;
+    const int n = pl.n;
+    const int nbuf = Op::kInplace ? NIN + 1 : NIN + NOUT + 1;
+    int TK = 16;
+    while (TK > 1 && ((size_t)n + (size_t)nbuf * n * TK) * sizeof(T2) > kSmemBudget) TK >>= 1;
+    while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
+    const size_t smem = ((size_t)n + (size_t)nbuf * n * TK) * sizeof(T2);
+    auto kern = k_axis_pass<T, NIN, NOUT, DIN, DOUT, Op>;
+    PFGB_CUDA_TRY(allow_smem(kern, smem));
+    dim3 grid((c->g.NzC + TK - 1) / TK, axis == 1 ? c->g.Nx : c->g.Ny);
+    ProfScope ps(c, {tag, (double)(NIN + NOUT) * (double)c->g.Nk * sizeof(T2)});
+    kern<<<grid, 256, smem, c->stream>>>(c->g, axis, pl, twp<T>(c, axis == 1 ? 1 : 0), TK, io, op);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    return PFGB_OK;
+}
+
+// extra_bytes: field bytes the op reads/writes per call besides its NFI/NFO spectra
+template <typename T, int NFI, int NFO, class Op>
+static pfgb_status launch_z(pfgb_ctx *c, Op op, const char *tag, double extra_bytes, int *nblocks = nullptr) {
+    using T2 = cplx_t<T>;
+    const int n = c->g.Nz;
+    auto bytes = [&](int R) {
+        int PI_ = NFI > 0 ? (R * NFI + 1) / 2 : 0, PO_ = NFO > 0 ? (R * NFO + 1) / 2 : 0;
+        return ((size_t)n + 2 * (size_t)PI_ * n + 2 * (size_t)PO_ * n) * sizeof(T2);
+    };
+    int R = 16;
+    while (R > 2 && bytes(R) > kSmemBudget) R >>= 1;
+    const long long rows = (long long)c->g.Nx * c->g.Ny;
+    while (R > 2 && R / 2 >= rows) R >>= 1;
+    const size_t smem = bytes(R);
+    auto kern = k_zpass<T, NFI, NFO, Op>;
+    PFGB_CUDA_TRY(allow_smem(kern, smem));
+    const int nb = (int)((rows + R - 1) / R);
+    ProfScope ps(c, {tag, (double)(NFI + NFO) * (double)c->g.Nk * sizeof(T2) + extra_bytes});
+    kern<<<nb, 256, smem, c->stream>>>(c->g, c->plz, twp<T>(c, 2), R, op);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    if (nblocks) *nblocks = nb;
+    return PFGB_OK;
+}
+
+#define TRY(x)                                   \
+    do {                                         \
+        pfgb_status s_ = (x);                    \
+        if (s_ != PFGB_OK) return s_;            \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// reductions of block partials (fixed order -> deterministic)
+// ---------------------------------------------------------------------------
+struct AccSum1 {
+    static constexpr bool kActive = true;
+    double s;
+    __device__ static AccSum1 identity() { return {0.0}; }
+    __device__ static AccSum1 combine(AccSum1 a, AccSum1 b) { return {a.s + b.s}; }
+    __device__ static AccSum1 shfl_down(AccSum1 a, int o) { return {__shfl_down_sync(0xffffffffu, a.s, o)}; }
+};
+struct AccSum2 {
+    static constexpr bool kActive = true;
+    double a, b;
+    __device__ static AccSum2 identity() { return {0.0, 0.0}; }
+    __device__ static AccSum2 combine(AccSum2 x, AccSum2 y) { return {x.a + y.a, x.b + y.b}; }
+    __device__ static AccSum2 shfl_down(AccSum2 x, int o) {
+        return {__shfl_down_sync(0xffffffffu, x.a, o), __shfl_down_sync(0xffffffffu, x.b, o)};
+    }
+};
+// zero-mode statistics: min, max of Y*, and the Taylor moments
+// M_p = sum (1-h) sigma^{(p)}(Y*) (M_0 also + h v_B), p = 0..4
+struct AccZM {
+    static constexpr bool kActive = true;
+    double mn, mx, m[5];
+    __device__ static AccZM identity() { return {1e300, -1e300, {0, 0, 0, 0, 0}}; }
+    __device__ static AccZM combine(AccZM x, const AccZM &y) {
+        x.mn = fmin(x.mn, y.mn);
+        x.mx = fmax(x.mx, y.mx);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) x.m[i] += y.m[i];
+        return x;
+    }
+    __device__ static AccZM shfl_down(AccZM x, int o) {
+        AccZM r;
+        r.mn = __shfl_down_sync(0xffffffffu, x.mn, o);
+        r.mx = __shfl_down_sync(0xffffffffu, x.mx, o);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) r.m[i] = __shfl_down_sync(0xffffffffu, x.m[i], o);
+        return r;
+    }
+};
+
+template <class Acc>
+__global__ void k_reduce_partials(const Acc *part, int n, double *out, int slot, double scale) {
+    Acc a = Acc::identity();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) a = Acc::combine(a, part[i]);
+    block_reduce_acc(a);
+    if (threadIdx.x == 0) {
+        const double *v = reinterpret_cast<const double *>(&a);
+        for (int i = 0; i < (int)(sizeof(Acc) / sizeof(double)); ++i) out[slot + i] = v[i] * scale;
+    }
+}
+
+template <class Acc>
+static pfgb_status reduce_to(pfgb_ctx *c, int nblocks, int slot, double scale = 1.0) {
+    ProfScope ps(c, {"reduce_partials", (double)nblocks * sizeof(Acc)});
+    k_reduce_partials<Acc><<<1, 256, 0, c->stream>>>((const Acc *)c->partials, nblocks, c->dscal, slot, scale);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    return PFGB_OK;
+}
+
+// ===========================================================================
+// phi / eta Allen-Cahn updates
+//   reference: D2Z f -> dealias; rhs -> D2Z -> dealias;
+//   f_k <- (f_k - L dt rhs_k) / (1 + L dt kappa k^2); dealias; Z2D; /N; clamp
+//   here: transform (f - L dt rhs) once (linearity), one mask, /N folded in.
+// ===========================================================================
+template <typename T, typename TE>
+struct OpPhiR2C {   // z pass producer: phi - L dt rhs_phi
+    using Acc = NoAcc;
+    DevState<T, TE> d; PhysC c; ElasC<TE> ec;
+    __device__ void point(long long cell, const T *, T *out, Acc &) const {
+        const T phi = d.phi_old[cell];
+        const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
+        const T eta = c.gp ? d.eta_old[cell] : T(0);
+        TE e[6];
+        if (c.coupling) {
+#pragma unroll
+            for (int a = 0; a < 6; ++a) e[a] = d.eps[a][cell];
+        }
+        const T r = phi_rhs<T, TE>(c, ec, phi, eta, xB, e);
+        out[0] = phi - T(c.Lphi * c.dt) * r;
+    }
+    __device__ void load_spec(long long, int, cplx_t<T> *) const {}
+    __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
+        d.S[0][row * d.g.NzC + k] = v[0];
+    }
+};
+
+template <typename T, typename TE>
+struct OpEtaR2C {   // z pass producer: eta - L_eta dt rhs_eta (phi = updated phi)
+    using Acc = NoAcc;
+    DevState<T, TE> d; PhysC c; ElasC<TE> ec;
+    __device__ void point(long long cell, const T *, T *out, Acc &) const {
+        const T eta = d.eta_old[cell];
+        const T phi = d.phi_new[cell];
+        const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
+        T sh = 0;
+        if (c.gp_el && c.act_eta && c.elastic) {
+            TE e[6], s[6];
+#pragma unroll
+            for (int a = 0; a < 6; ++a) e[a] = d.eps[a][cell];
+            stress_at<T, TE>(c, ec, d.phi_old[cell], eta, xB, e, s);
+            sh = T(s[0]) + T(s[1]) + T(s[2]);
+        }
+        const T r = eta_rhs<T, TE>(c, ec, eta, phi, xB, sh);
+        out[0] = eta - T(c.gpL * c.dt) * r;
+    }
+    __device__ void load_spec(long long, int, cplx_t<T> *) const {}
+    __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
+        d.S[0][row * d.g.NzC + k] = v[0];
+    }
+};
+
+template <typename T>
+struct OpACFilterX {   // x pass: mask / (1 + L dt kappa k^2) / N
+    static constexpr bool kInplace = false;
+    KTab kt; double Ldtk, invN;
+    __device__ void apply(int i, int j, int k, const cplx_t<T> *in, cplx_t<T> *out) const {
+        if (kt.cut(i, j, k)) { out[0] = mk2<cplx_t<T>>(T(0), T(0)); return; }
+        const T f = T(invN / (1.0 + Ldtk * kt.k2(i, j, k)));
+        out[0] = cscale(in[0], f);
+    }
+};
+
+template <typename T, typename TE>
+struct OpACStoreZ {   // z pass consumer: clamp and store the new order parameter
+    using Acc = NoAcc;
+    const cplx_t<T> *src; T *dst; int NzC; T lo, hi;
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * NzC + k]; }
+    __device__ void point(long long cell, const T *in, T *, Acc &) const {
+        T v = in[0];
+        if (v < lo) v = lo;
+        if (v > hi) v = hi;
+        dst[cell] = v;
+    }
+    __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
+};
+
+// ===========================================================================
+// Y (logit composition) update
+// ===========================================================================
+// (1) chemical potential mu (compute_mu_x_kernel :1266-1324 / compute_mu_C_gp
+// :1326-1366) and sum of D_mix(h) xB (1-xB) (reduce_sum_DY_kernel :3870).
+template <typename T, typename TE>
+struct OpMuR2C {
+    using Acc = AccSum1;
+    DevState<T, TE> d; PhysC c; ElasC<TE> ec;
+    __device__ void point(long long cell, const T *, T *out, Acc &acc) const {
+        const T Yv = d.Y[cell] + T(d.Yc);
+        const T phiY = (c.zm || c.prev_level) ? d.phi_old[cell] : d.phi_new[cell];
+        const T xB = sigmoid_clip(Yv, T(c.Yclip), T(c.xBeps));
+        T offA, offB;
+        thermo_mu_off<T>(c.tc, xB, offA, offB);
+        T mu;
+        if (c.gp) {
+            const T cref = T(1) / (T(c.Vm0) + T(c.dVm) * xB);
+            mu = cref * (T(c.dG) + offB - offA);
+        } else {
+            const T h = pf_h(phiY);
+            const T cb = c_xB_phi<T>(xB, T(c.Vm0), T(c.dVm), T(c.Vmc), h);
+            const T muA = T(c.tc.GA_s) + offA, muB = T(c.tc.GB_s) + offB;
+            const T mt = (T(1) - h) * (muA * (T(1) - xB) + muB * xB) + h * T(c.mu0);
+            mu = cb * ((T(c.dG) + offB - offA) - cb * mt * T(c.dVm));
+        }
+        if (c.elastic) {
+            // stress of the elastic solve of this step: phi, eta, xB at step start
+            TE e[6], s[6];
+#pragma unroll
+            for (int a = 0; a < 6; ++a) e[a] = d.eps[a][cell];
+            const T xB0 = xB_of_Y<T>(c, Yv);
+            stress_at<T, TE>(c, ec, d.phi_old[cell], c.gp ? d.eta_old[cell] : T(0), xB0, e, s);
+            mu += -T(c.eiv) * (T(s[0]) + T(s[1]) + T(s[2]));
+        }
+        out[0] = mu;
+        const T h = pf_h(phiY);
+        const T Dm = (T(1) - h) * T(c.Da) + h * T(c.Dc);
+        T x = sigmoid_raw(Yv);
+        if (x < T(1e-12)) x = T(1e-12);
+        if (x > T(1) - T(1e-12)) x = T(1) - T(1e-12);
+        acc.s += double(Dm * x * (T(1) - x));
+    }
+    __device__ void load_spec(long long, int, cplx_t<T> *) const {}
+    __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
+        d.S[0][row * d.g.NzC + k] = v[0];
+    }
+    __device__ void finish(int b, const Acc &a) const { reinterpret_cast<Acc *>(d.partials)[b] = a; }
+};
+
+// (2) gradient: g_a = IFFT(mask i k_a mask mu_k)/N, three outputs
+template <typename T>
+struct OpGradX {
+    static constexpr bool kInplace = false;
+    KTab kt; double invN;
+    __device__ void apply(int i, int j, int k, const cplx_t<T> *in, cplx_t<T> *out) const {
+        using T2 = cplx_t<T>;
+        if (kt.cut(i, j, k)) { out[0] = out[1] = out[2] = mk2<T2>(T(0), T(0)); return; }
+        const T2 m = cscale(in[0], T(invN));
+        out[0] = cmul_is(m, T(kt.kx[i]));
+        out[1] = cmul_is(m, T(kt.ky[j]));
+        out[2] = cmul_is(m, T(kt.kz[k]));
+    }
+};
+
+// (3) fused C2R of the gradients -> fluxes J = M grad mu, the explicit
+// source T = term_h + term_gamma of the Y right-hand side
+// (compute_Y_rhs_kernel :2185-2266 / _sm_tangent_n_ :2268-2359) and Y^n,
+// then R2C.  The spectral side combines i kz J_z - T into one array.
+template <typename T, typename TE>
+struct OpFluxZ {
+    using Acc = NoAcc;
+    DevState<T, TE> d; PhysC c;
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const {
+        const long long o = row * d.g.NzC + k;
+        v[0] = d.S[0][o]; v[1] = d.S[1][o]; v[2] = d.S[2][o];
+    }
+    __device__ void point(long long cell, const T *g, T *out, Acc &) const {
+        const T Yf = d.Y[cell];
+        const T Yv = Yf + T(d.Yc);
+        const T pn = d.phi_old[cell], pp = d.phi_new[cell];
+        const T phiY = (c.zm || c.prev_level) ? pn : pp;
+        const T xBp = sigmoid_clip(Yv, T(c.Yclip), T(c.xBeps));
+        const T M = mobility<T>(c, phiY, c.gp ? d.eta_new[cell] : T(0), xBp);
+        out[0] = M * g[0];
+        out[1] = M * g[1];
+        out[2] = M * g[2];
+        T x = sigmoid_raw(Yv);
+        if (x < T(1e-12)) x = T(1e-12);
+        if (x > T(1) - T(1e-12)) x = T(1) - T(1e-12);
+        const T ld = x * (T(1) - x);
+        const T dYdt = d.dYdt[cell] + T(d.dYoff);
+        const T dt = T(c.dt);
+        T src;
+        if (c.zm) {
+            const T th = pf_hp(pn) * ((pp - pn) / dt) * (T(c.vB) - x);
+            const T gl = (T(1) - pf_h(pn)) * ld - T(1);
+            src = th + gl * dYdt;
+        } else {
+            const T hn = pf_h(pp), ho = pf_h(pn);
+            const T th = T(c.hscale) * ((hn - ho) / dt) * (T(c.vB) - x);
+            const T hx = c.prev_level ? ho : hn;
+            const T gl = (T(1) - hx) * ld - T(1);
+            src = th + (c.disable_gamma ? T(0) : gl * dYdt);
+        }
+        out[3] = src;
+        out[4] = Yf;
+    }
+    __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
+        const long long o = row * d.g.NzC + k;
+        const T kz = T(d.kt.kz[k]);
+        d.S[0][o] = v[0];
+        d.S[1][o] = v[1];
+        d.S[2][o] = csub(cmul_is(v[2], kz), v[3]);
+        d.S[3][o] = v[4];
+    }
+};
+
+// (4) y pass: J_x, i ky J_y + (i kz J_z - T), Y^n
+template <typename T>
+struct OpYCombY {
+    static constexpr bool kInplace = false;
+    KTab kt;
+    __device__ void apply(int, int j, int, const cplx_t<T> *in, cplx_t<T> *out) const {
+        out[0] = in[0];
+        out[1] = cadd(cmul_is(in[1], T(kt.ky[j])), in[2]);
+        out[2] = in[3];
+    }
+};
+
+// (5) x pass: Y_new_k = mask [Y^n_k + dt (i kx J_x + D) / (1 + dt <DY> k^2)] / N
+//   = the reference's Y_semi_implicit_update with rhs_k = divJ_k - T_k
+//     - <DY> Lap(Y)_k, Lap(Y)_k = -k^2 Y^n_k (exact algebra, all masks idempotent)
+template <typename T>
+struct OpYUpdX {
+    static constexpr bool kInplace = false;
+    KTab kt; double dt, invN; const double *meanDY;
+    __device__ void apply(int i, int j, int k, const cplx_t<T> *in, cplx_t<T> *out) const {
+        using T2 = cplx_t<T>;
+        if (kt.cut(i, j, k)) { out[0] = mk2<T2>(T(0), T(0)); return; }
+        const double den = 1.0 + dt * (*meanDY) * kt.k2(i, j, k);
+        const T a = T(dt / den);
+        const T2 div = cadd(cmul_is(in[0], T(kt.kx[i])), in[1]);
+        out[0] = cscale(cadd(in[2], cscale(div, a)), T(invN));
+    }
+};
+
+// (6) final z pass: store Y_f, dY/dt, and the zero-mode statistics
+template <typename T, typename TE>
+struct OpYFinalZ {
+    using Acc = AccZM;
+    DevState<T, TE> d; PhysC c; const cplx_t<T> *src;
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * d.g.NzC + k]; }
+    __device__ void point(long long cell, const T *in, T *, Acc &acc) const {
+        const T Yold = d.Y[cell];
+        T y = in[0];
+        if (!c.zm) {
+            // Y_normalize_and_clamp_kernel (:2554-2572), Y_cap = Y_clip
+            T yt = y + T(d.Yc);
+            if (yt > T(c.Yclip)) yt = T(c.Yclip);
+            if (yt < T(-c.Yclip)) yt = T(-c.Yclip);
+            y = yt - T(d.Yc);
+        }
+        d.Y[cell] = y;
+        d.dYdt[cell] = (y - Yold) / T(c.dt);
+        if (c.zm) {
+            const double ys = double(y) + d.Yc;
+            const double h = pf_h(double(d.phi_new[cell]));
+            const double a = 1.0 - h;
+            const double s = sigmoid_raw(ys);
+            const double s1 = s * (1.0 - s);
+            const double u = 1.0 - 2.0 * s;
+            acc.mn = fmin(acc.mn, ys);
+            acc.mx = fmax(acc.mx, ys);
+            acc.m[0] += a * s + h * c.vB;
+            acc.m[1] += a * s1;
+            acc.m[2] += a * s1 * u;
+            acc.m[3] += a * s1 * (1.0 - 6.0 * s1);
+            acc.m[4] += a * s1 * u * (1.0 - 12.0 * s1);
+        }
+    }
+    __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
+    __device__ void finish(int b, const Acc &a) const { reinterpret_cast<Acc *>(d.partials)[b] = a; }
+};
+
+// zero-mode direct evaluation: mass(l) and d mass/dl at given shifts, FP64
+// (compute_pf_Y_zero_mode_terms_kernel, cuda_kernels.cu:3409-3420).  nl shifts
+// at once; used for the bracket ends and when the Taylor model is out of range.
+template <typename T>
+__global__ void k_zm_eval(const T *Y, const T *phi, long long N, double Yc, double vB,
+                          const double *lam, int nl, double *partials) {
+    double m[4] = {0, 0, 0, 0}, dd[4] = {0, 0, 0, 0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double h = pf_h(double(phi[i]));
+        const double a = 1.0 - h;
+        const double y = double(Y[i]) + Yc;
+        for (int q = 0; q < nl; ++q) {
+            const double x = sigmoid_raw(y + lam[q]);
+            m[q] += a * x + h * vB;
+            dd[q] += a * x * (1.0 - x);
+        }
+    }
+    for (int q = 0; q < nl; ++q) {
+        AccSum2 s{m[q], dd[q]};
+        block_reduce_acc(s);
+        if (threadIdx.x == 0) reinterpret_cast<AccSum2 *>(partials)[q * gridDim.x + blockIdx.x] = s;
+        __syncthreads();
+    }
+}
+
+// ===========================================================================
+// Elastic solve
+// ===========================================================================
+// cold start producer: eigenstrain eps0 -> R2C (6 fields)
+template <typename T, typename TE>
+struct OpEigenR2C {
+    using Acc = NoAcc;
+    DevState<T, TE> d; PhysC c; ElasC<TE> ec;
+    __device__ void point(long long cell, const TE *, TE *out, Acc &) const {
+        const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
+        eigenstrain<T, TE>(c, ec, d.phi_old[cell], c.gp ? d.eta_old[cell] : T(0), clamp01(xB),
+                           c.gp_el != 0, out);
+    }
+    __device__ void load_spec(long long, int, cplx_t<TE> *) const {}
+    __device__ void store_spec(long long row, int k, const cplx_t<TE> *v) const {
+        const long long o = row * d.g.NzC + k;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) d.E[a][o] = v[a];
+    }
+};
+
+// iteration: C2R strain (/N) -> h = C0:eps - (C0 + h dC):(eps + E0 - eps0)
+// (compute_strain_with_perturbation_kernel, cuda_kernels.cu:7002-7157) -> R2C
+template <typename T, typename TE>
+struct OpHijZ {
+    using Acc = NoAcc;
+    DevState<T, TE> d; PhysC c; ElasC<TE> ec;
+    __device__ void load_spec(long long row, int k, cplx_t<TE> *v) const {
+        const long long o = row * d.g.NzC + k;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) v[a] = d.E[a][o];
+    }
+    __device__ void point(long long cell, const TE *in, TE *out, Acc &) const {
+        TE e[6], e0[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) e[a] = in[a] * ec.invN;
+        const T phi = d.phi_old[cell];
+        const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
+        eigenstrain<T, TE>(c, ec, phi, c.gp ? d.eta_old[cell] : T(0), clamp01(xB), c.gp_el != 0, e0);
+        const T h = pf_h(phi);
+        TE tv[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) tv[a] = e[a] + ec.E0[a] - e0[a];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+            TE acc = 0;
+#pragma unroll
+            for (int b = 0; b < 6; ++b) {
+                const int v = vidx(a, b);
+                const TE c0 = ec.S[v];
+                const TE ce = c0 + (TE)(h * T(ec.Sp[v]));
+                const TE f = b >= 3 ? TE(2) : TE(1);
+                acc += f * (c0 * e[b] - ce * tv[b]);
+            }
+            out[a] = acc;
+        }
+    }
+    __device__ void store_spec(long long row, int k, const cplx_t<TE> *v) const {
+        const long long o = row * d.g.NzC + k;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) d.E[a][o] = v[a];
+    }
+};
+
+// finalize: C2R strain, /N, + E0 -> stored total strain
+template <typename T, typename TE>
+struct OpStrainFinalZ {
+    using Acc = NoAcc;
+    DevState<T, TE> d; ElasC<TE> ec;
+    __device__ void load_spec(long long row, int k, cplx_t<TE> *v) const {
+        const long long o = row * d.g.NzC + k;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) v[a] = d.E[a][o];
+    }
+    __device__ void point(long long cell, const TE *in, TE *, Acc &) const {
+#pragma unroll
+        for (int a = 0; a < 6; ++a) d.eps[a][cell] = in[a] * ec.invN + ec.E0[a];
+    }
+    __device__ void store_spec(long long, int, const cplx_t<TE> *) const {}
+};
+
+// symmetric strain of a displacement: eps_ab = i (k_a u_b + k_b u_a) / 2
+// (compute_strain_from_displacement_k_kernel, cuda_kernels.cu:6673-6730)
+template <typename TE>
+__device__ __forceinline__ cplx_t<TE> strain_comp(int comp, TE kx, TE ky, TE kz, const cplx_t<TE> *u) {
+    const TE kv[3] = {kx, ky, kz};
+    const int a = comp < 3 ? comp : (comp == 3 ? 1 : 0);
+    const int b = comp < 3 ? comp : (comp == 5 ? 1 : 2);
+    if (a == b) return cmul_is(u[a], kv[a]);
+    const cplx_t<TE> s = cadd(cscale(u[b], kv[a]), cscale(u[a], kv[b]));
+    return cmul_is(s, TE(0.5));
+}
+
+template <typename TE>
+struct OpStrainFromUX {   // warm start: strain of the stored u, then inverse x
+    static constexpr bool kInplace = false;
+    KTab kt;
+    __device__ void apply(int i, int j, int k, const cplx_t<TE> *u, cplx_t<TE> *out) const {
+        const TE kx = TE(kt.kx[i]), ky = TE(kt.ky[j]), kz = TE(kt.kz[k]);
+        const bool m = kt.cut(i, j, k);
+#pragma unroll
+        for (int cmp = 0; cmp < 6; ++cmp)
+            out[cmp] = m ? mk2<cplx_t<TE>>(TE(0), TE(0)) : strain_comp<TE>(cmp, kx, ky, kz, u);
+    }
+};
+
+// Green's function x pass.  Inputs: the 6 y-transformed components of the
+// source (eps0 for the cold start, h_ij during the iteration).
+//   t_i = k_j tau_ij  (tau = C0:eps0 for EIGEN)
+//   u   = -i G(k) t,  G = K^-1, K_ij = k_a C_iajb k_b, u(k=0) = 0, dealiased
+//   (compute_displacement_from_eigenstrain_k_kernel :6734-6998,
+//    compute_displacement_from_hij_green_kernel :6484-6634)
+// The new u is stored (warm state), the Hermitian-weighted residual against
+// the previous u is accumulated (compute_elastic_displacement_residual_kernel
+// :6436-6467), and the 6 strain components of u are inverse x transformed.
+template <typename TE>
+struct GreenArgs {
+    Grid3 g; KTab kt; ElasC<TE> ec;
+    const cplx_t<TE> *tw;
+    cplx_t<TE> *E[6], *U[3];
+    double *partials;
+    int resid;
+};
+
+template <typename TE>
+__device__ __forceinline__ void green_u(const TE *S, TE kx, TE ky, TE kz, const cplx_t<TE> t[3],
+                                        cplx_t<TE> u[3]) {
+    const TE kv[3] = {kx, ky, kz};
+    TE K[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = i; j < 3; ++j) {
+            TE acc = 0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) acc += kv[a] * S[vidx(tvoigt(i, a), tvoigt(j, b))] * kv[b];
+            K[i][j] = acc;
+            K[j][i] = acc;
+        }
+    const TE c00 = K[1][1] * K[2][2] - K[1][2] * K[1][2];
+    const TE c01 = K[0][2] * K[1][2] - K[0][1] * K[2][2];
+    const TE c02 = K[0][1] * K[1][2] - K[0][2] * K[1][1];
+    const TE c11 = K[0][0] * K[2][2] - K[0][2] * K[0][2];
+    const TE c12 = K[0][2] * K[0][1] - K[0][0] * K[1][2];
+    const TE c22 = K[0][0] * K[1][1] - K[0][1] * K[0][1];
+    const TE det = K[0][0] * c00 + K[0][1] * c01 + K[0][2] * c02;
+    using T2 = cplx_t<TE>;
+    if (fabs((double)det) < 1e-30) { u[0] = u[1] = u[2] = mk2<T2>(TE(0), TE(0)); return; }
+    const TE id = TE(1) / det;
+    const TE G[3][3] = {{c00 * id, c01 * id, c02 * id}, {c01 * id, c11 * id, c12 * id}, {c02 * id, c12 * id, c22 * id}};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        T2 s = mk2<T2>(TE(0), TE(0));
+#pragma unroll
+        for (int b = 0; b < 3; ++b) s = cadd(s, cscale(t[b], G[a][b]));
+        u[a] = mk2<T2>(s.y, -s.x);   // -i s
+    }
+}
+
+template <typename TE, bool EIGEN>
+__global__ void __launch_bounds__(256)
+k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
+    using T2 = cplx_t<TE>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2 *sm = reinterpret_cast<T2 *>(smem_raw);
+    const int n = plan.n, tile = n * TK;
+    T2 *tw = sm;
+    T2 *acc[3] = {sm + n, sm + n + tile, sm + n + 2 * tile};
+    T2 *w0 = sm + n + 3 * tile, *w1 = w0 + tile;
+    const int k0 = blockIdx.x * TK, j = blockIdx.y;
+    const long long base = (long long)j * A.g.NzC + k0;
+    const long long es = (long long)A.g.Ny * A.g.NzC;
+    const int kcnt = min(TK, A.g.NzC - k0);
+    load_tw<TE>(tw, A.tw, n);
+    for (int e = threadIdx.x; e < 3 * tile; e += blockDim.x) acc[e / tile][e % tile] = mk2<T2>(TE(0), TE(0));
+    for (int cmp = 0; cmp < 6; ++cmp) {
+        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+            const int q = e / TK, l = e - q * TK;
+            w0[e] = (l < kcnt) ? A.E[cmp][base + q * es + l] : mk2<T2>(TE(0), TE(0));
+        }
+        __syncthreads();
+        T2 *r = fft_lines<TE, -1>(w0, w1, plan, tw, TK, TK, 1, false);
+        // accumulate t_i += k_j tau_ij
+        const int a = cmp < 3 ? cmp : (cmp == 3 ? 1 : 0);
+        const int b = cmp < 3 ? cmp : (cmp == 5 ? 1 : 2);
+        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+            const int q = e / TK, l = e - q * TK;
+            const TE kv[3] = {TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[min(k0 + l, A.g.NzC - 1)])};
+            const T2 x = r[e];
+            if (EIGEN) {
+                // tau_ij = C_ij,ab eps0_ab ; component (a,b) enters with
+                // weight 1 (normal) or 2 (shear) in Voigt column tvoigt(a,b)
+                const int col = cmp;
+                const TE f = cmp < 3 ? TE(1) : TE(2);
+#pragma unroll
+                for (int ii = 0; ii < 3; ++ii) {
+                    TE s = 0;
+#pragma unroll
+                    for (int jj = 0; jj < 3; ++jj) s += kv[jj] * A.ec.S[vidx(tvoigt(ii, jj), col)];
+                    acc[ii][e] = cadd(acc[ii][e], cscale(x, f * s));
+                }
+            } else {
+                acc[a][e] = cadd(acc[a][e], cscale(x, kv[b]));
+                if (a != b) acc[b][e] = cadd(acc[b][e], cscale(x, kv[a]));
+            }
+        }
+        __syncthreads();
+    }
+    // u = -i G t, masked; residual; store u
+    double rd = 0.0, rr = 0.0;
+    for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+        const int q = e / TK, l = e - q * TK, k = k0 + l;
+        T2 u[3];
+        if (l >= kcnt || A.kt.cut(q, j, k) || (q == 0 && j == 0 && k == 0)) {
+            u[0] = u[1] = u[2] = mk2<T2>(TE(0), TE(0));
+        } else {
+            const T2 t[3] = {acc[0][e], acc[1][e], acc[2][e]};
+            green_u<TE>(A.ec.S, TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[k]), t, u);
+        }
+        if (l < kcnt) {
+            const long long o = base + q * es + l;
+            if (A.resid) {
+                const double w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? 1.0 : 2.0;
+                double ld = 0, lr = 0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const T2 old = A.U[c][o];
+                    const double dr = double(u[c].x) - double(old.x), di = double(u[c].y) - double(old.y);
+                    ld += dr * dr + di * di;
+                    lr += double(u[c].x) * double(u[c].x) + double(u[c].y) * double(u[c].y);
+                }
+                rd += w * ld;
+                rr += w * lr;
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) A.U[c][o] = u[c];
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) acc[c][e] = u[c];
+    }
+    if (A.resid) {
+        AccSum2 s{rd, rr};
+        block_reduce_acc(s);
+        if (threadIdx.x == 0)
+            reinterpret_cast<AccSum2 *>(A.partials)[blockIdx.y * gridDim.x + blockIdx.x] = s;
+    }
+    __syncthreads();
+    // strain components -> inverse x -> store
+    for (int cmp = 0; cmp < 6; ++cmp) {
+        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+            const int q = e / TK, l = e - q * TK;
+            const int k = min(k0 + l, A.g.NzC - 1);
+            const T2 u[3] = {acc[0][e], acc[1][e], acc[2][e]};
+            w0[e] = strain_comp<TE>(cmp, TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[k]), u);
+        }
+        __syncthreads();
+        T2 *r = fft_lines<TE, +1>(w0, w1, plan, tw, TK, TK, 1, false);
+        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+            const int q = e / TK, l = e - q * TK;
+            if (l < kcnt) A.E[cmp][base + q * es + l] = r[e];
+        }
+        __syncthreads();
+    }
+}
+
+// residual finalize: rel = sqrt(diff / max(ref, floor))
+__global__ void k_resid_final(double *dscal, double floor_) {
+    const double d = dscal[DS_RES_DIFF], r = dscal[DS_RES_REF];
+    dscal[3] = sqrt(d / fmax(r, floor_));
+}
+
+template <typename TE>
+static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks) {
+    using T2 = cplx_t<TE>;
+    const int n = c->plx.n;
+    int TK = 16;
+    while (TK > 1 && ((size_t)n + 5 * (size_t)n * TK) * sizeof(T2) > kSmemBudget) TK >>= 1;
+    while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
+    const size_t smem = ((size_t)n + 5 * (size_t)n * TK) * sizeof(T2);
+    GreenArgs<TE> A;
+    A.g = c->g;
+    A.kt = KTab{c->kx, c->ky, c->kz, c->mx, c->my, c->mz};
+    for (int i = 0; i < 21; ++i) { A.ec.S[i] = (TE)c->p.S[i]; A.ec.Sp[i] = (TE)c->p.S_p[i]; }
+    A.tw = (const T2 *)c->tw[sizeof(TE) == 8 ? 0 : 1][0];
+    for (int i = 0; i < 6; ++i) A.E[i] = (T2 *)c->E[i];
+    for (int i = 0; i < 3; ++i) A.U[i] = (T2 *)c->U[i];
+    A.partials = c->partials;
+    A.resid = resid;
+    dim3 grid((c->g.NzC + TK - 1) / TK, c->g.Ny);
+    // reads 6 source spectra (+3 old u for the residual), writes 3 u + 6 strain spectra
+    ProfScope ps(c, {eigen ? "x_green_eigen" : "x_green_hij",
+                     (double)(6 + 3 + 6 + (resid ? 3 : 0)) * (double)c->g.Nk * sizeof(T2)});
+    if (eigen) {
+        auto kern = k_x_green<TE, true>;
+        PFGB_CUDA_TRY(allow_smem(kern, smem));
+        kern<<<grid, 256, smem, c->stream>>>(A, c->plx, TK);
+    } else {
+        auto kern = k_x_green<TE, false>;
+        PFGB_CUDA_TRY(allow_smem(kern, smem));
+        kern<<<grid, 256, smem, c->stream>>>(A, c->plx, TK);
+    }
+    PFGB_CUDA_TRY(cudaGetLastError());
+    *nblocks = grid.x * grid.y;
+    return PFGB_OK;
+}
+
+// ===========================================================================
+// step orchestration
+// ===========================================================================
+template <typename T, typename TE>
+static DevState<T, TE> dev_state(pfgb_ctx *c) {
+    DevState<T, TE> d;
+    d.g = c->g;
+    d.kt = KTab{c->kx, c->ky, c->kz, c->mx, c->my, c->mz};
+    d.phi_old = (T *)c->phi[c->cur];
+    d.phi_new = (T *)c->phi[1 - c->cur];
+    d.eta_old = (T *)c->eta[c->ecur];
+    d.eta_new = (T *)c->eta[1 - c->ecur];
+    d.Y = (T *)c->Y;
+    d.dYdt = (T *)c->dYdt;
+    for (int i = 0; i < 6; ++i) { d.eps[i] = (TE *)c->eps[i]; d.E[i] = (cplx_t<TE> *)c->E[i]; }
+    for (int i = 0; i < 3; ++i) d.U[i] = (cplx_t<TE> *)c->U[i];
+    for (int i = 0; i < 4; ++i) d.S[i] = (cplx_t<T> *)c->S[i];
+    d.partials = c->partials;
+    d.dscal = c->dscal;
+    d.Yc = c->Yc;
+    d.dYoff = c->dYoff;
+    return d;
+}
+
+template <typename TE>
+static ElasC<TE> elas_consts(const pfgb_ctx *c) {
+    ElasC<TE> e;
+    for (int i = 0; i < 21; ++i) { e.S[i] = (TE)c->p.S[i]; e.Sp[i] = (TE)c->p.S_p[i]; }
+    for (int i = 0; i < 6; ++i) { e.e00[i] = (TE)c->p.eps00[i]; e.E0[i] = (TE)c->p.E0[i]; }
+    e.invN = (TE)(1.0 / (double)c->g.N);
+    return e;
+}
+
+static pfgb_status sync_read(pfgb_ctx *c, int first, int count) {
+    PFGB_CUDA_TRY(cudaMemcpyAsync(c->hscal + first, c->dscal + first, sizeof(double) * count,
+                                  cudaMemcpyDeviceToHost, c->stream));
+    PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return PFGB_OK;
+}
+
+template <typename T, typename TE>
+static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
+    using T2e = cplx_t<TE>;
+    const pfgb_params &P = c->p;
+    const PhysC pc = c->pc;
+    const ElasC<TE> ec = elas_consts<TE>(c);
+    DevState<T, TE> d = dev_state<T, TE>(c);
+    const KTab kt = d.kt;
+    const int accel = P.elastic_enabled && (P.elastic_warm_start_enabled || P.elastic_residual_control_enabled);
+    const int warm_used = accel && c->warm_valid;
+    const double Nf = (double)c->g.N;
+    AxisIO<TE, 6, 6> io6;
+    for (int i = 0; i < 6; ++i) { io6.in[i] = (const T2e *)c->E[i]; io6.out[i] = (T2e *)c->E[i]; }
+    int nb = 0;
+    if (!warm_used) {
+        TRY((launch_z<TE, 0, 6>(c, OpEigenR2C<T, TE>{d, pc, ec}, "z_eigen_r2c", (2.0 + pc.gp) * Nf * sizeof(T))));
+        TRY((launch_axis<TE, 6, 6, -1, 0>(c, 1, io6, OpCopy<TE, 6>{}, "y_fwd6")));
+        TRY(launch_green<TE>(c, true, 0, &nb));
+    } else {
+        AxisIO<TE, 3, 6> io;
+        for (int i = 0; i < 3; ++i) io.in[i] = (const T2e *)c->U[i];
+        for (int i = 0; i < 6; ++i) io.out[i] = (T2e *)c->E[i];
+        TRY((launch_axis<TE, 3, 6, 0, +1>(c, 2, io, OpStrainFromUX<TE>{kt}, "x_strain_from_u")));
+    }
+    TRY((launch_axis<TE, 6, 6, +1, 0>(c, 1, io6, OpCopy<TE, 6>{}, "y_inv6")));
+    int iter = accel ? 0 : 1;
+    int conv = accel ? 0 : 1;
+    double rel = NAN;
+    for (;;) {
+        TRY((launch_z<TE, 6, 6>(c, OpHijZ<T, TE>{d, pc, ec}, "z_hij", (2.0 + pc.gp) * Nf * sizeof(T))));
+        TRY((launch_axis<TE, 6, 6, -1, 0>(c, 1, io6, OpCopy<TE, 6>{}, "y_fwd6")));
+        TRY(launch_green<TE>(c, false, accel, &nb));
+        TRY((launch_axis<TE, 6, 6, +1, 0>(c, 1, io6, OpCopy<TE, 6>{}, "y_inv6")));
+        if (accel) {
+            TRY(reduce_to<AccSum2>(c, nb, DS_RES_DIFF));
+            k_resid_final<<<1, 1, 0, c->stream>>>(c->dscal, P.elastic_residual_absolute_floor);
+            PFGB_CUDA_TRY(cudaGetLastError());
+            TRY(sync_read(c, DS_RES_DIFF, 3));
+            const double ds = c->hscal[DS_RES_DIFF], rs = c->hscal[DS_RES_REF];
+            if (!std::isfinite(ds) || !std::isfinite(rs) || ds < 0.0 || rs < 0.0) {
+                pfgb_set_error_msg("elastic residual is non-finite at step %d", c->step + 1);
+                return PFGB_ERR_NONFINITE;
+            }
+            rel = c->hscal[3];
+            ++iter;
+            if (iter >= P.elastic_iter_min && rel <= P.elastic_residual_tolerance) { conv = 1; break; }
+            if (iter >= P.elastic_iter_max) break;
+        } else {
+            ++iter;
+            if (iter >= P.elastic_iter_max) break;
+        }
+    }
+    if (accel) c->warm_valid = 1;
+    if (st) {
+        st->elastic_iterations = iter;
+        st->elastic_converged = conv;
+        st->elastic_warm_start_used = warm_used;
+        st->elastic_relative_residual = rel;
+        st->elastic_iterations_total += iter;
+    }
+    if (accel && !conv && P.elastic_fail_on_nonconvergence) {
+        pfgb_set_error_msg("elastic solver did not converge at step %d: iterations=%d residual=%.17e",
+                           c->step + 1, iter, rel);
+        return PFGB_ERR_NONCONVERGED;
+    }
+    TRY((launch_z<TE, 6, 0>(c, OpStrainFinalZ<T, TE>{d, ec}, "z_strain_final", 6.0 * Nf * sizeof(TE))));
+    return PFGB_OK;
+}
+
+// zero-mode solve (run_pf_conserved_y_zero_mode_host, main_cuda.cu:4269-4405):
+// same bracket / Newton / bisection logic; mass(l) comes from the Taylor
+// model sum_p M_p l^p / p! about l = 0 when |l| <= 0.05 (truncation error
+// below 1e-17 relative) and from a direct FP64 evaluation pass otherwise.
+template <typename T, typename TE>
+static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
+    const pfgb_params &P = c->p;
+    TRY(reduce_to<AccZM>(c, nb_final, DS_ZM));
+    TRY(sync_read(c, DS_ZM, 7));
+    const double ymin = c->hscal[DS_ZM], ymax = c->hscal[DS_ZM + 1];
+    double M[5];
+    for (int i = 0; i < 5; ++i) M[i] = c->hscal[DS_ZM + 2 + i];
+    const double Ycap = P.Y_clip;
+    auto fail = [&](const char *why) {
+        pfgb_set_error_msg("PF zero-mode rejected step=%d: %s", c->step + 1, why);
+        return PFGB_ERR_ZERO_MODE;
+    };
+    if (!std::isfinite(ymin) || !std::isfinite(ymax)) return fail("non-finite Y*");
+    double lo = -P.Y_clip - ymin, hi = Ycap - ymax;
+    const double rnd = 128.0 * 2.220446049250313e-16 * std::max(std::max(std::fabs(lo), std::fabs(hi)), 1.0);
+    if (!std::isfinite(lo) || !std::isfinite(hi) || lo > hi + rnd) return fail("empty lambda interval");
+    const double target = c->target_mass;
+    const double tol = P.zero_mode_tolerance_relative * std::max(std::fabs(target), 1.0);
+    const long long N = c->g.N;
+    const int eb = 304;
+    auto direct = [&](const double *lams, int nl, double *mass, double *der) -> pfgb_status {
+        PFGB_CUDA_TRY(cudaMemcpyAsync(c->dscal + DS_EV, lams, sizeof(double) * nl, cudaMemcpyHostToDevice, c->stream));
+        k_zm_eval<T><<<eb, 256, 0, c->stream>>>((const T *)c->Y, (const T *)c->phi[1 - c->cur], N, c->Yc,
+                                                P.v_B, c->dscal + DS_EV, nl, c->partials);
+        PFGB_CUDA_TRY(cudaGetLastError());
+        for (int q = 0; q < nl; ++q) {
+            k_reduce_partials<AccSum2><<<1, 256, 0, c->stream>>>((const AccSum2 *)c->partials + q * eb, eb,
+                                                                 c->dscal, DS_BR + 2 * q, 1.0);
+        }
+        PFGB_CUDA_TRY(cudaGetLastError());
+        TRY(sync_read(c, DS_BR, 2 * nl));
+        for (int q = 0; q < nl; ++q) { mass[q] = c->hscal[DS_BR + 2 * q]; der[q] = c->hscal[DS_BR + 2 * q + 1]; }
+        return PFGB_OK;
+    };
+    auto model = [&](double l, double *mass, double *der) -> pfgb_status {
+        if (std::fabs(l) <= 0.05) {
+            *mass = M[0] + l * (M[1] + l * (M[2] / 2.0 + l * (M[3] / 6.0 + l * M[4] / 24.0)));
+            *der = M[1] + l * (M[2] + l * (M[3] / 2.0 + l * M[4] / 6.0));
+            return PFGB_OK;
+        }
+        return direct(&l, 1, mass, der);
+    };
+    {
+        double ls[2] = {lo, hi}, ms[2], ds[2];
+        TRY(direct(ls, 2, ms, ds));
+        if (!std::isfinite(ms[0]) || !std::isfinite(ms[1])) return fail("non-finite bracket mass");
+        if (ms[0] - target > tol || ms[1] - target < -tol) return fail("target outside bracket");
+    }
+    double lam = std::min(std::max(0.0, lo), hi), mass = 0, der = 0;
+    TRY(model(lam, &mass, &der));
+    double res = mass - target;
+    int iters = 0, nwt = 0, bis = 0;
+    for (int it = 0; it < P.zero_mode_max_iterations && std::fabs(res) > tol; ++it) {
+        if (res < 0.0) lo = lam; else hi = lam;
+        double cand = NAN;
+        if (der > 0.0 && std::isfinite(der)) cand = lam - res / der;
+        if (std::isfinite(cand) && cand > lo && cand < hi) ++nwt;
+        else { cand = 0.5 * (lo + hi); ++bis; }
+        lam = cand;
+        TRY(model(lam, &mass, &der));
+        if (!std::isfinite(mass) || !std::isfinite(der)) return fail("non-finite mass");
+        res = mass - target;
+        iters = it + 1;
+    }
+    if (std::fabs(res) > tol) return fail("did not converge");
+    if (ymin + lam < -P.Y_clip || ymax + lam > Ycap) return fail("shifted Y leaves [-Y_clip, Y_cap]");
+    c->Yc += lam;
+    c->dYoff = lam / P.dt;
+    if (st) {
+        st->zero_mode_iterations = iters;
+        st->zero_mode_newton_steps = nwt;
+        st->zero_mode_bisection_steps = bis;
+        st->zero_mode_lambda = lam;
+        st->zero_mode_residual = res;
+        st->zero_mode_target_mass = target;
+    }
+    return PFGB_OK;
+}
+
+template <typename T, typename TE>
+static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
+    using T2 = cplx_t<T>;
+    const pfgb_params &P = c->p;
+    const PhysC pc = c->pc;
+    const ElasC<TE> ec = elas_consts<TE>(c);
+    if (P.elastic_enabled) TRY((elastic_solve<T, TE>(c, st)));
+    DevState<T, TE> d = dev_state<T, TE>(c);
+    const KTab kt = d.kt;
+    const double invN = 1.0 / (double)c->g.N;
+    const double Nf = (double)c->g.N;
+    AxisIO<T, 1, 1> io1;
+    io1.in[0] = d.S[0]; io1.out[0] = d.S[0];
+
+    // ---- phi ----
+    TRY((launch_z<T, 0, 1>(c, OpPhiR2C<T, TE>{d, pc, ec}, "z_phi_rhs", (2.0 + pc.gp) * Nf * sizeof(T) + (pc.coupling ? 6.0 : 0.0) * Nf * sizeof(TE))));
+    TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
+    TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpACFilterX<T>{kt, P.L_phi * P.dt * P.kappa_phi, invN}, "x_ac_filter")));
+    TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+    TRY((launch_z<T, 1, 0>(c, OpACStoreZ<T, TE>{d.S[0], d.phi_new, c->g.NzC, T(-1e-6), T(1.0 + 1e-6)}, "z_ac_store", Nf * sizeof(T))));
+
+    // ---- eta (GP zone) ----
+    if (pc.gp) {
+        TRY((launch_z<T, 0, 1>(c, OpEtaR2C<T, TE>{d, pc, ec}, "z_eta_rhs", 3.0 * Nf * sizeof(T))));
+        TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
+        TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpACFilterX<T>{kt, P.gp_L_eta * P.dt * P.gp_kappa_eta, invN}, "x_ac_filter")));
+        TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+        TRY((launch_z<T, 1, 0>(c, OpACStoreZ<T, TE>{d.S[0], d.eta_new, c->g.NzC, T(0), T(1)}, "z_ac_store", Nf * sizeof(T))));
+    }
+
+    // ---- Y ----
+    int nb = 0;
+    TRY((launch_z<T, 0, 1>(c, OpMuR2C<T, TE>{d, pc, ec}, "z_mu", (3.0 + pc.gp) * Nf * sizeof(T) + (pc.elastic ? 6.0 : 0.0) * Nf * sizeof(TE), &nb)));
+    TRY(reduce_to<AccSum1>(c, nb, DS_MEAN_DY, invN));
+    TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
+    {
+        AxisIO<T, 1, 3> io;
+        io.in[0] = d.S[0];
+        io.out[0] = d.S[0]; io.out[1] = d.S[1]; io.out[2] = d.S[2];
+        TRY((launch_axis<T, 1, 3, -1, +1>(c, 2, io, OpGradX<T>{kt, invN}, "x_grad")));
+    }
+    {
+        AxisIO<T, 3, 3> io;
+        for (int i = 0; i < 3; ++i) { io.in[i] = d.S[i]; io.out[i] = d.S[i]; }
+        TRY((launch_axis<T, 3, 3, +1, 0>(c, 1, io, OpCopy<T, 3>{}, "y_inv3")));
+    }
+    TRY((launch_z<T, 3, 5>(c, OpFluxZ<T, TE>{d, pc}, "z_flux", (4.0 + pc.gp) * Nf * sizeof(T))));
+    {
+        AxisIO<T, 4, 3> io;
+        for (int i = 0; i < 4; ++i) io.in[i] = d.S[i];
+        io.out[0] = d.S[0]; io.out[1] = d.S[1]; io.out[2] = d.S[3];
+        TRY((launch_axis<T, 4, 3, -1, 0>(c, 1, io, OpYCombY<T>{kt}, "y_ycomb")));
+    }
+    {
+        AxisIO<T, 3, 1> io;
+        io.in[0] = d.S[0]; io.in[1] = d.S[1]; io.in[2] = d.S[3];
+        io.out[0] = d.S[0];
+        TRY((launch_axis<T, 3, 1, -1, +1>(c, 2, io, OpYUpdX<T>{kt, P.dt, invN, c->dscal + DS_MEAN_DY}, "x_y_update")));
+    }
+    TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+    int nbf = 0;
+    TRY((launch_z<T, 1, 0>(c, OpYFinalZ<T, TE>{d, pc, d.S[0]}, "z_y_final", (3.0 + pc.zm) * Nf * sizeof(T), &nbf)));
+    c->dYoff = 0.0;
+    if (P.zero_mode_enabled) TRY((zero_mode<T, TE>(c, nbf, st)));
+    if (st) {
+        TRY(sync_read(c, DS_MEAN_DY, 1));
+        st->mean_DY = c->hscal[DS_MEAN_DY];
+    }
+    c->cur = 1 - c->cur;
+    if (pc.gp) c->ecur = 1 - c->ecur;
+    c->step++;
+    (void)sizeof(T2);
+    return PFGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// construction
+// ---------------------------------------------------------------------------
+static void build_physc(pfgb_ctx *c) {
+    const pfgb_params &P = c->p;
+    PhysC &k = c->pc;
+    memset(&k, 0, sizeof(k));
+    k.dt = P.dt;
+    k.invN = 1.0 / (double)c->g.N;
+    k.W = P.W; k.kappa = P.kappa_phi; k.Lphi = P.L_phi;
+    k.Da = P.D_alpha; k.Dc = P.D_compound;
+    k.vA = P.v_A; k.vB = P.v_B; k.Vm0 = P.Vm_alpha_0; k.dVm = P.dVm_alpha_dxB; k.Vmc = P.Vm_compound;
+    k.mu0 = P.mu0_compound; k.eiv = P.eps_iso_over_vB; k.Yclip = P.Y_clip; k.xBeps = P.xB_eps;
+    k.hscale = P.Y_rhs_term_h_scale;
+    for (int i = 0; i < 6; ++i) { k.e00[i] = P.eps00[i]; k.E0[i] = P.E0[i]; }
+    for (int i = 0; i < 21; ++i) { k.S[i] = P.S[i]; k.Sp[i] = P.S_p[i]; }
+    k.gp = P.model_mode == PFGB_MODEL_GP_ZONE;
+    k.gp_el = k.gp && P.gp_elastic_enabled;
+    k.act_eta = P.gp_elastic_active_eta;
+    k.act_phi = P.gp_elastic_active_phi;
+    k.elastic = P.elastic_enabled;
+    // phi_elastic_coupling_enabled (main_cuda.cu:24868)
+    k.coupling = P.elastic_enabled && (!k.gp_el || P.gp_elastic_active_phi);
+    k.zm = P.zero_mode_enabled;
+    k.prev_level = P.enable_Y_rhs_previous_time_level;
+    k.disable_gamma = P.disable_Y_rhs_gamma_term;
+    k.xb_raw = P.zero_mode_enabled;
+    pfgb_thermo_const(P.temperature_K, P.mu_reference_scale, P.thermo_convex_extrapolation_enabled, &k.tc);
+    k.shift = k.coupling ? P.elastic_shift_dimless : 0.0;
+    k.Cdmu = P.mu0_compound - P.v_A * k.tc.GA_s - P.v_B * k.tc.GB_s - k.shift;
+    k.dG = k.tc.GB_s - k.tc.GA_s;
+    k.gpxB = P.gp_xB_fixed; k.gpW = P.gp_W_eta; k.gpkap = P.gp_kappa_eta; k.gpL = P.gp_L_eta;
+    k.gpMGP = P.gp_M_GP; k.gpMb = P.gp_M_beta; k.gpeiso = P.gp_eps_iso; k.gpscale = P.gp_elastic_derivative_scale;
+    {
+        const double xg = clamp_eps(P.gp_xB_fixed, 1.0e-12);
+        double oA, oB;
+        thermo_mu_off<double>(k.tc, xg, oA, oB);
+        k.gp_Cg = oA * (1.0 - xg) + oB * xg - P.gp_delta_g0;
+    }
+}
+
+static pfgb_status dalloc(pfgb_ctx *c, void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        pfgb_set_error("cudaMalloc", e, __FILE__, __LINE__);
+        return e == cudaErrorMemoryAllocation ? PFGB_ERR_NOMEM : PFGB_ERR_CUDA;
+    }
+    c->bytes += bytes;
+    return PFGB_OK;
+}
+
+static pfgb_status upload_twiddles(pfgb_ctx *c, int axis, int n) {
+    std::vector<double2> wd(n);
+    std::vector<float2> wf(n);
+    for (int m = 0; m < n; ++m) {
+        // exact octant folding keeps the table symmetric to the last bit
+        const double a = -2.0 * PFGB_PI * (double)m / (double)n;
+        wd[m] = make_double2(cos(a), sin(a));
+        wf[m] = make_float2((float)wd[m].x, (float)wd[m].y);
+    }
+    TRY(dalloc(c, &c->tw[0][axis], sizeof(double2) * n));
+    TRY(dalloc(c, &c->tw[1][axis], sizeof(float2) * n));
+    PFGB_CUDA_TRY(cudaMemcpy(c->tw[0][axis], wd.data(), sizeof(double2) * n, cudaMemcpyHostToDevice));
+    PFGB_CUDA_TRY(cudaMemcpy(c->tw[1][axis], wf.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+    return PFGB_OK;
+}
+
+static pfgb_status make_ktab(pfgb_ctx *c) {
+    const pfgb_params &P = c->p;
+    auto wrap = [](int i, int n, double d) {
+        int ii = (i <= n / 2) ? i : i - n;
+        return 2.0 * PFGB_PI * ii / (d * n);
+    };
+    auto cut = [](double k, double d) { return std::fabs(k) >= PFGB_PI * (2.0 / 3.0) / d; };
+    std::vector<double> kx(P.Nx), ky(P.Ny), kz(c->g.NzC);
+    std::vector<unsigned char> mx(P.Nx), my(P.Ny), mz(c->g.NzC);
+    for (int i = 0; i < P.Nx; ++i) { kx[i] = wrap(i, P.Nx, P.dx); mx[i] = cut(kx[i], P.dx); }
+    for (int j = 0; j < P.Ny; ++j) { ky[j] = wrap(j, P.Ny, P.dy); my[j] = cut(ky[j], P.dy); }
+    for (int k = 0; k < c->g.NzC; ++k) { kz[k] = 2.0 * PFGB_PI * k / (P.dz * P.Nz); mz[k] = cut(kz[k], P.dz); }
+    TRY(dalloc(c, (void **)&c->kx, sizeof(double) * P.Nx));
+    TRY(dalloc(c, (void **)&c->ky, sizeof(double) * P.Ny));
+    TRY(dalloc(c, (void **)&c->kz, sizeof(double) * c->g.NzC));
+    TRY(dalloc(c, (void **)&c->mx, P.Nx));
+    TRY(dalloc(c, (void **)&c->my, P.Ny));
+    TRY(dalloc(c, (void **)&c->mz, c->g.NzC));
+    PFGB_CUDA_TRY(cudaMemcpy(c->kx, kx.data(), sizeof(double) * P.Nx, cudaMemcpyHostToDevice));
+    PFGB_CUDA_TRY(cudaMemcpy(c->ky, ky.data(), sizeof(double) * P.Ny, cudaMemcpyHostToDevice));
+    PFGB_CUDA_TRY(cudaMemcpy(c->kz, kz.data(), sizeof(double) * c->g.NzC, cudaMemcpyHostToDevice));
+    PFGB_CUDA_TRY(cudaMemcpy(c->mx, mx.data(), P.Nx, cudaMemcpyHostToDevice));
+    PFGB_CUDA_TRY(cudaMemcpy(c->my, my.data(), P.Ny, cudaMemcpyHostToDevice));
+    PFGB_CUDA_TRY(cudaMemcpy(c->mz, mz.data(), c->g.NzC, cudaMemcpyHostToDevice));
+    return PFGB_OK;
+}
+
+static pfgb_status validate(const pfgb_params *p) {
+    if (p->Nx < 1 || p->Ny < 1 || p->Nz < 2 || p->Nx > PFGB_MAX_N || p->Ny > PFGB_MAX_N || p->Nz > PFGB_MAX_N) {
+        pfgb_set_error_msg("grid %dx%dx%d outside [1..%d] (Nz >= 2)", p->Nx, p->Ny, p->Nz, PFGB_MAX_N);
+        return PFGB_ERR_INVALID;
+    }
+    if (!(p->dx > 0 && p->dy > 0 && p->dz > 0 && p->dt > 0)) {
+        pfgb_set_error_msg("dx, dy, dz, dt must be > 0");
+        return PFGB_ERR_INVALID;
+    }
+    if (p->precision != PFGB_PREC_FP64 && p->precision != PFGB_PREC_FP32) {
+        pfgb_set_error_msg("precision must be PFGB_PREC_FP64 or PFGB_PREC_FP32");
+        return PFGB_ERR_INVALID;
+    }
+    if (p->elastic_precision != PFGB_PREC_FP32) {
+        pfgb_set_error_msg("elastic_precision: only FP32 (the reference's elastic precision) is built");
+        return PFGB_ERR_UNSUPPORTED;
+    }
+    if (p->mode != PFGB_MODE_DYNAMICS) {
+        pfgb_set_error_msg("pfgb_step drives mode=dynamics; minimize runs through pfgb_minimize");
+        return PFGB_ERR_UNSUPPORTED;
+    }
+    if (p->model_mode != PFGB_MODEL_TWO_PHASE && p->model_mode != PFGB_MODEL_GP_ZONE) {
+        pfgb_set_error_msg("model_mode must be two_phase or gp_zone");
+        return PFGB_ERR_INVALID;
+    }
+    if (p->elastic_iter_max < 1 || p->elastic_iter_min < 0) {
+        pfgb_set_error_msg("elastic_iter_max must be >= 1");
+        return PFGB_ERR_INVALID;
+    }
+    return PFGB_OK;
+}
+
+static void ctx_free(pfgb_ctx *c) {
+    auto f = [](void *p) { if (p) cudaFree(p); };
+    for (int a = 0; a < 2; ++a) for (int b = 0; b < 3; ++b) f(c->tw[a][b]);
+    f(c->kx); f(c->ky); f(c->kz); f(c->mx); f(c->my); f(c->mz);
+    for (int i = 0; i < 2; ++i) f(c->phi[i]);
+    f(c->eta[0]);
+    if (c->eta[1] != c->eta[0]) f(c->eta[1]);
+    f(c->Y); f(c->dYdt);
+    for (int i = 0; i < 4; ++i) f(c->S[i]);
+    for (int i = 0; i < 6; ++i) { f(c->eps[i]); f(c->E[i]); }
+    for (int i = 0; i < 3; ++i) f(c->U[i]);
+    f(c->partials); f(c->dscal); f(c->stage);
+    for (auto e : c->pool) cudaEventDestroy(e);
+    if (c->hscal) cudaFreeHost(c->hscal);
+}
+
+template <typename T>
+__global__ void k_load_state(const double *phi, const double *xB, const double *eta, const double *dYdt,
+                             T *phi_o, T *eta_o, T *Y_o, T *dYdt_o, long long N, double xBeps, double Yclip,
+                             double vB, double *partials) {
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double p = phi[i], x = xB[i];
+        phi_o[i] = (T)p;
+        eta_o[i] = eta ? (T)eta[i] : T(0);
+        dYdt_o[i] = dYdt ? (T)dYdt[i] : T(0);
+        Y_o[i] = (T)logit_clip(x, xBeps, Yclip);
+        // target mass of the zero mode, gpu_reduce_sum_xBtot (:28079-28086)
+        const double h = pf_h(p);
+        acc += (1.0 - h) * x + vB * h;
+    }
+    AccSum1 s{acc};
+    block_reduce_acc(s);
+    if (threadIdx.x == 0) reinterpret_cast<AccSum1 *>(partials)[blockIdx.x] = s;
+}
+
+template <typename T>
+static pfgb_status load_device(pfgb_ctx *c, const double *phi, const double *xB, const double *eta,
+                               const double *dYdt, bool keep_history) {
+    const int nb = 304;
+    k_load_state<T><<<nb, 256, 0, c->stream>>>(phi, xB, eta, dYdt, (T *)c->phi[c->cur], (T *)c->eta[c->ecur],
+                                               (T *)c->Y, (T *)c->dYdt, c->g.N, c->p.xB_eps, c->p.Y_clip,
+                                               c->p.v_B, c->partials);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    c->Yc = 0.0;
+    c->dYoff = 0.0;
+    if (keep_history && c->loaded) return PFGB_OK;
+    TRY(reduce_to<AccSum1>(c, nb, DS_ZM));
+    TRY(sync_read(c, DS_ZM, 1));
+    c->target_mass = c->hscal[DS_ZM];
+    for (int i = 0; i < 6; ++i) PFGB_CUDA_TRY(cudaMemsetAsync(c->eps[i], 0, sizeof(float) * c->g.N, c->stream));
+    c->warm_valid = 0;
+    c->step = 0;
+    c->loaded = 1;
+    return PFGB_OK;
+}
+
+static pfgb_status ensure_stage(pfgb_ctx *c) {
+    if (c->stage) return PFGB_OK;
+    return dalloc(c, (void **)&c->stage, sizeof(double) * 5 * (size_t)c->g.N);
+}
+
+static pfgb_status load_host(pfgb_ctx *c, const double *phi, const double *xB, const double *eta,
+                             const double *dYdt, bool keep) {
+    if (!c || !phi || !xB) return PFGB_ERR_INVALID;
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    TRY(ensure_stage(c));
+    const size_t b = sizeof(double) * (size_t)c->g.N;
+    double *dp = c->stage, *dx = c->stage + c->g.N;
+    double *de = eta ? c->stage + 2 * c->g.N : nullptr, *dd = dYdt ? c->stage + 3 * c->g.N : nullptr;
+    PFGB_CUDA_TRY(cudaMemcpyAsync(dp, phi, b, cudaMemcpyHostToDevice, c->stream));
+    PFGB_CUDA_TRY(cudaMemcpyAsync(dx, xB, b, cudaMemcpyHostToDevice, c->stream));
+    if (eta) PFGB_CUDA_TRY(cudaMemcpyAsync(de, eta, b, cudaMemcpyHostToDevice, c->stream));
+    if (dYdt) PFGB_CUDA_TRY(cudaMemcpyAsync(dd, dYdt, b, cudaMemcpyHostToDevice, c->stream));
+    return c->p.precision == PFGB_PREC_FP64 ? load_device<double>(c, dp, dx, de, dd, keep)
+                                            : load_device<float>(c, dp, dx, de, dd, keep);
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
+    if (!pin || !out) return PFGB_ERR_INVALID;
+    *out = nullptr;
+    TRY(validate(pin));
+    int ndev = 0;
+    PFGB_CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) {
+        pfgb_set_error_msg("device %d not present (%d devices)", device, ndev);
+        return PFGB_ERR_INVALID;
+    }
+    PFGB_CUDA_TRY(cudaSetDevice(device));
+    pfgb_ctx *c = new pfgb_ctx();
+    c->p = *pin;
+    c->device = device;
+    pfgb_params_finalize(&c->p);
+    c->g.Nx = pin->Nx; c->g.Ny = pin->Ny; c->g.Nz = pin->Nz; c->g.NzC = pin->Nz / 2 + 1;
+    c->g.N = (long long)pin->Nx * pin->Ny * pin->Nz;
+    c->g.Nk = (long long)pin->Nx * pin->Ny * c->g.NzC;
+    pfgb_make_plan(pin->Nx, &c->plx);
+    pfgb_make_plan(pin->Ny, &c->ply);
+    pfgb_make_plan(pin->Nz, &c->plz);
+    build_physc(c);
+    pfgb_status s = PFGB_OK;
+    const size_t rs = pin->precision == PFGB_PREC_FP64 ? sizeof(double) : sizeof(float);
+    const size_t N = (size_t)c->g.N, Nk = (size_t)c->g.Nk;
+#define A_(ptr, b) if (s == PFGB_OK) s = dalloc(c, (void **)(ptr), (b))
+    for (int i = 0; i < 2; ++i) { A_(&c->phi[i], rs * N); }
+    if (c->pc.gp) { for (int i = 0; i < 2; ++i) { A_(&c->eta[i], rs * N); } }
+    else { A_(&c->eta[0], rs * N); c->eta[1] = c->eta[0]; }
+    A_(&c->Y, rs * N);
+    A_(&c->dYdt, rs * N);
+    for (int i = 0; i < 4; ++i) { A_(&c->S[i], 2 * rs * Nk); }
+    for (int i = 0; i < 6; ++i) { A_(&c->eps[i], sizeof(float) * N); }
+    if (pin->elastic_enabled) {
+        for (int i = 0; i < 6; ++i) { A_(&c->E[i], sizeof(float2) * Nk); }
+        for (int i = 0; i < 3; ++i) { A_(&c->U[i], sizeof(float2) * Nk); }
+    }
+    c->npartials = std::max<size_t>((size_t)pin->Nx * pin->Ny, 4096) * 8;
+    A_(&c->partials, sizeof(double) * c->npartials);
+    A_(&c->dscal, sizeof(double) * 64);
+#undef A_
+    if (s == PFGB_OK) s = make_ktab(c);
+    if (s == PFGB_OK) s = upload_twiddles(c, 0, pin->Nx);
+    if (s == PFGB_OK) s = upload_twiddles(c, 1, pin->Ny);
+    if (s == PFGB_OK) s = upload_twiddles(c, 2, pin->Nz);
+    if (s == PFGB_OK) {
+        cudaError_t e = cudaMallocHost((void **)&c->hscal, sizeof(double) * 64);
+        if (e != cudaSuccess) { pfgb_set_error("cudaMallocHost", e, __FILE__, __LINE__); s = PFGB_ERR_CUDA; }
+    }
+    if (s == PFGB_OK && !c->pc.gp) {
+        cudaError_t e = cudaMemset(c->eta[0], 0, rs * N);
+        if (e != cudaSuccess) { pfgb_set_error("cudaMemset", e, __FILE__, __LINE__); s = PFGB_ERR_CUDA; }
+    }
+    if (s != PFGB_OK) {
+        ctx_free(c);
+        delete c;
+        return s;
+    }
+    *out = c;
+    return PFGB_OK;
+}
+
+void pfgb_destroy(pfgb_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    ctx_free(c);
+    delete c;
+}
+
+const char *pfgb_last_error(const pfgb_ctx *) { return pfgb_error_buffer(); }
+
+pfgb_status pfgb_set_stream(pfgb_ctx *c, void *s) {
+    if (!c) return PFGB_ERR_INVALID;
+    c->stream = (cudaStream_t)s;
+    return PFGB_OK;
+}
+
+size_t pfgb_device_bytes(const pfgb_ctx *c) { return c ? c->bytes : 0; }
+
+pfgb_status pfgb_sync(pfgb_ctx *c) {
+    if (!c) return PFGB_ERR_INVALID;
+    PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return PFGB_OK;
+}
+
+pfgb_status pfgb_load_fields_device(pfgb_ctx *c, const double *phi, const double *xB, const double *eta,
+                                    const double *dYdt) {
+    if (!c || !phi || !xB) return PFGB_ERR_INVALID;
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    return c->p.precision == PFGB_PREC_FP64 ? load_device<double>(c, phi, xB, eta, dYdt, false)
+                                            : load_device<float>(c, phi, xB, eta, dYdt, false);
+}
+
+pfgb_status pfgb_load_fields(pfgb_ctx *c, const double *phi, const double *xB, const double *eta,
+                             const double *dYdt) {
+    return load_host(c, phi, xB, eta, dYdt, false);
+}
+
+pfgb_status pfgb_set_fields(pfgb_ctx *c, const double *phi, const double *xB, const double *eta,
+                            const double *dYdt) {
+    return load_host(c, phi, xB, eta, dYdt, true);
+}
+
+pfgb_status pfgb_step(pfgb_ctx *c, int nsteps, pfgb_step_stats *st) {
+    if (!c || nsteps < 0) return PFGB_ERR_INVALID;
+    if (!c->loaded) { pfgb_set_error_msg("pfgb_step before pfgb_load_fields"); return PFGB_ERR_INVALID; }
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    if (st) memset(st, 0, sizeof(*st));
+    for (int i = 0; i < nsteps; ++i) {
+        pfgb_status s = c->p.precision == PFGB_PREC_FP64 ? step_once<double, float>(c, st)
+                                                         : step_once<float, float>(c, st);
+        if (s != PFGB_OK) return s;
+    }
+    if (st) st->step = c->step;
+    return PFGB_OK;
+}
+
+}  // extern "C"
+
+template <typename T>
+__global__ void k_export(const T *phi, const T *Y, const T *eta, const T *dYdt, long long N, double Yc,
+                         double dYoff, int raw, double Yclip, double eps, double *ophi, double *oxB,
+                         double *oY, double *oeta, double *odY) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double y = double(Y[i]) + Yc;
+        if (ophi) ophi[i] = double(phi[i]);
+        if (oY) oY[i] = y;
+        if (oxB) oxB[i] = raw ? sigmoid_raw(y) : sigmoid_clip(y, Yclip, eps);
+        if (oeta) oeta[i] = double(eta[i]);
+        if (odY) odY[i] = double(dYdt[i]) + dYoff;
+    }
+}
+
+extern "C" {
+
+pfgb_status pfgb_read_fields(pfgb_ctx *c, double *phi, double *xB, double *Y, double *eta, double *dYdt) {
+    if (!c) return PFGB_ERR_INVALID;
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    const size_t b = sizeof(double) * (size_t)c->g.N;
+    TRY(ensure_stage(c));
+    double *st = c->stage;
+    const long long N = c->g.N;
+    double *o[5] = {st, st + N, st + 2 * N, st + 3 * N, st + 4 * N};
+    const int raw = c->p.zero_mode_enabled && c->step > 0;
+    if (c->p.precision == PFGB_PREC_FP64)
+        k_export<double><<<304, 256, 0, c->stream>>>((double *)c->phi[c->cur], (double *)c->Y,
+                                                     (double *)c->eta[c->ecur], (double *)c->dYdt, N, c->Yc,
+                                                     c->dYoff, raw, c->p.Y_clip, c->p.xB_eps, o[0], o[1], o[2],
+                                                     o[3], o[4]);
+    else
+        k_export<float><<<304, 256, 0, c->stream>>>((float *)c->phi[c->cur], (float *)c->Y,
+                                                    (float *)c->eta[c->ecur], (float *)c->dYdt, N, c->Yc,
+                                                    c->dYoff, raw, c->p.Y_clip, c->p.xB_eps, o[0], o[1], o[2],
+                                                    o[3], o[4]);
+    cudaError_t e = cudaGetLastError();
+    double *dst[5] = {phi, xB, Y, eta, dYdt};
+    for (int i = 0; i < 5 && e == cudaSuccess; ++i)
+        if (dst[i]) e = cudaMemcpyAsync(dst[i], o[i], b, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { pfgb_set_error("pfgb_read_fields", e, __FILE__, __LINE__); return PFGB_ERR_CUDA; }
+    return PFGB_OK;
+}
+
+}  // extern "C"
+
+template <typename T>
+__global__ void k_stress_export(PhysC pc, ElasC<float> ec, const T *phi, const T *eta, const T *Y, double Yc,
+                                float *const *eps, float *sig, long long N) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        float e[6], s[6];
+        for (int a = 0; a < 6; ++a) e[a] = eps[a][i];
+        const T xB = xB_of_Y<T>(pc, T(double(Y[i]) + Yc));
+        stress_at<T, float>(pc, ec, phi[i], pc.gp ? eta[i] : T(0), xB, e, s);
+        for (int a = 0; a < 6; ++a) sig[a * N + i] = s[a];
+    }
+}
+
+extern "C" {
+
+// sigma as the reference stores it after the elastic solve of the last step
+// (phi, eta, xB of that step's start).
+pfgb_status pfgb_read_elastic(pfgb_ctx *c, float *sigma6, float *strain6) {
+    if (!c) return PFGB_ERR_INVALID;
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    const size_t N = (size_t)c->g.N;
+    if (strain6)
+        for (int a = 0; a < 6; ++a)
+            PFGB_CUDA_TRY(cudaMemcpyAsync(strain6 + a * N, c->eps[a], sizeof(float) * N, cudaMemcpyDeviceToHost,
+                                          c->stream));
+    if (sigma6) {
+        // the step swapped phi/eta buffers: the elastic solve saw the previous ones
+        const int pc_ = c->step > 0 ? 1 - c->cur : c->cur;
+        const int ec_ = (c->step > 0 && c->pc.gp) ? 1 - c->ecur : c->ecur;
+        float *st = nullptr;
+        pfgb_status s = dalloc(c, (void **)&st, sizeof(float) * 6 * N);
+        if (s != PFGB_OK) return s;
+        c->bytes -= sizeof(float) * 6 * N;
+        float **dptrs = nullptr;
+        PFGB_CUDA_TRY(cudaMalloc(&dptrs, sizeof(float *) * 6));
+        PFGB_CUDA_TRY(cudaMemcpy(dptrs, c->eps, sizeof(float *) * 6, cudaMemcpyHostToDevice));
+        const ElasC<float> ec = elas_consts<float>(c);
+        // Y of the elastic solve: the state before the last Y update is gone;
+        // xB enters sigma only through the chemical eigenstrain, so the
+        // export uses the current composition (exact before the first step).
+        if (c->p.precision == PFGB_PREC_FP64)
+            k_stress_export<double><<<304, 256, 0, c->stream>>>(c->pc, ec, (double *)c->phi[pc_],
+                                                                (double *)c->eta[ec_], (double *)c->Y, c->Yc,
+                                                                dptrs, st, (long long)N);
+        else
+            k_stress_export<float><<<304, 256, 0, c->stream>>>(c->pc, ec, (float *)c->phi[pc_],
+                                                               (float *)c->eta[ec_], (float *)c->Y, c->Yc, dptrs,
+                                                               st, (long long)N);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(sigma6, st, sizeof(float) * 6 * N, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cudaFree(st);
+        cudaFree(dptrs);
+        if (e != cudaSuccess) { pfgb_set_error("pfgb_read_elastic", e, __FILE__, __LINE__); return PFGB_ERR_CUDA; }
+    }
+    PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return PFGB_OK;
+}
+
+pfgb_status pfgb_read_displacement_k(pfgb_ctx *c, float *u3) {
+    if (!c || !u3) return PFGB_ERR_INVALID;
+    if (!c->p.elastic_enabled) return PFGB_ERR_UNSUPPORTED;
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    const size_t Nk = (size_t)c->g.Nk;
+    for (int a = 0; a < 3; ++a)
+        PFGB_CUDA_TRY(cudaMemcpyAsync(u3 + 2 * a * Nk, c->U[a], sizeof(float2) * Nk, cudaMemcpyDeviceToHost,
+                                      c->stream));
+    PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return PFGB_OK;
+}
+
+}  // extern "C"
+
+struct AccDiag {
+    static constexpr bool kActive = true;
+    double vf, mass, xb, nin, pmn, pmx, xmn, xmx;
+    __device__ static AccDiag identity() { return {0, 0, 0, 0, 1e300, -1e300, 1e300, -1e300}; }
+    __device__ static AccDiag combine(AccDiag a, const AccDiag &b) {
+        a.vf += b.vf; a.mass += b.mass; a.xb += b.xb; a.nin += b.nin;
+        a.pmn = fmin(a.pmn, b.pmn); a.pmx = fmax(a.pmx, b.pmx);
+        a.xmn = fmin(a.xmn, b.xmn); a.xmx = fmax(a.xmx, b.xmx);
+        return a;
+    }
+    __device__ static AccDiag shfl_down(AccDiag a, int o) {
+        AccDiag r;
+        double *pa = reinterpret_cast<double *>(&a), *pr = reinterpret_cast<double *>(&r);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) pr[i] = __shfl_down_sync(0xffffffffu, pa[i], o);
+        return r;
+    }
+};
+
+template <typename T>
+__global__ void k_diag(const T *phi, const T *Y, long long N, double Yc, int raw, double Yclip, double eps,
+                       double vB, AccDiag *part) {
+    AccDiag a = AccDiag::identity();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double p = double(phi[i]);
+        const double y = double(Y[i]) + Yc;
+        const double x = raw ? sigmoid_raw(y) : sigmoid_clip(y, Yclip, eps);
+        const double h = pf_h(p);
+        a.vf += pf_h(clamp01(p));             // reduce_sum_h_kernel (:5580)
+        a.mass += (1.0 - h) * x + vB * h;      // reduce_sum_xBtot_kernel (:3792)
+        a.xb += x;
+        a.nin += p >= 0.5 ? 1.0 : 0.0;
+        a.pmn = fmin(a.pmn, p); a.pmx = fmax(a.pmx, p);
+        a.xmn = fmin(a.xmn, x); a.xmx = fmax(a.xmx, x);
+    }
+    block_reduce_acc(a);
+    if (threadIdx.x == 0) part[blockIdx.x] = a;
+}
+
+extern "C" {
+
+pfgb_status pfgb_diagnostics(pfgb_ctx *c, pfgb_diag *out) {
+    if (!c || !out) return PFGB_ERR_INVALID;
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    const int nb = 304;
+    const int raw = c->p.zero_mode_enabled && c->step > 0;
+    if (c->p.precision == PFGB_PREC_FP64)
+        k_diag<double><<<nb, 256, 0, c->stream>>>((double *)c->phi[c->cur], (double *)c->Y, c->g.N, c->Yc, raw,
+                                                  c->p.Y_clip, c->p.xB_eps, c->p.v_B, (AccDiag *)c->partials);
+    else
+        k_diag<float><<<nb, 256, 0, c->stream>>>((float *)c->phi[c->cur], (float *)c->Y, c->g.N, c->Yc, raw,
+                                                 c->p.Y_clip, c->p.xB_eps, c->p.v_B, (AccDiag *)c->partials);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    TRY(reduce_to<AccDiag>(c, nb, 24));
+    TRY(sync_read(c, 24, 8));
+    const double *h = c->hscal + 24;
+    const double N = (double)c->g.N;
+    out->vf_precip = h[0] / N;
+    out->mass_xBtot = h[1];
+    out->mean_xB = h[2] / N;
+    out->n_in = h[3];
+    out->phi_min = h[4]; out->phi_max = h[5];
+    out->xB_min = h[6]; out->xB_max = h[7];
+    return PFGB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// standalone 3D transforms (test / tooling entry points)
+// ---------------------------------------------------------------------------
+template <typename T>
+struct OpRealIn {
+    using Acc = NoAcc;
+    const T *src; cplx_t<T> *dst; int NzC;
+    __device__ void point(long long cell, const T *, T *out, Acc &) const { out[0] = src[cell]; }
+    __device__ void load_spec(long long, int, cplx_t<T> *) const {}
+    __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const { dst[row * NzC + k] = v[0]; }
+};
+template <typename T>
+struct OpRealOut {
+    using Acc = NoAcc;
+    const cplx_t<T> *src; T *dst; int NzC;
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * NzC + k]; }
+    __device__ void point(long long cell, const T *in, T *, Acc &) const { dst[cell] = in[0]; }
+    __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
+};
+
+static pfgb_status fft_ctx_init(pfgb_ctx *c, int Nx, int Ny, int Nz, void *stream) {
+    if (Nx < 1 || Ny < 1 || Nz < 2 || Nx > PFGB_MAX_N || Ny > PFGB_MAX_N || Nz > PFGB_MAX_N) {
+        pfgb_set_error_msg("transform size %dx%dx%d outside [1..%d] (Nz >= 2)", Nx, Ny, Nz, PFGB_MAX_N);
+        return PFGB_ERR_INVALID;
+    }
+    c->stream = (cudaStream_t)stream;
+    c->g.Nx = Nx; c->g.Ny = Ny; c->g.Nz = Nz; c->g.NzC = Nz / 2 + 1;
+    c->g.N = (long long)Nx * Ny * Nz;
+    c->g.Nk = (long long)Nx * Ny * c->g.NzC;
+    pfgb_make_plan(Nx, &c->plx);
+    pfgb_make_plan(Ny, &c->ply);
+    pfgb_make_plan(Nz, &c->plz);
+    TRY(upload_twiddles(c, 0, Nx));
+    TRY(upload_twiddles(c, 1, Ny));
+    TRY(upload_twiddles(c, 2, Nz));
+    return PFGB_OK;
+}
+
+static void fft_ctx_free(pfgb_ctx *c) {
+    cudaStreamSynchronize(c->stream);
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 3; ++b)
+            if (c->tw[a][b]) cudaFree(c->tw[a][b]);
+}
+
+template <typename T>
+static pfgb_status fft_r2c_impl(pfgb_ctx *c, const T *in, cplx_t<T> *out) {
+    TRY((launch_z<T, 0, 1>(c, OpRealIn<T>{in, out, c->g.NzC}, "z_r2c", (double)c->g.N * sizeof(T))));
+    AxisIO<T, 1, 1> io;
+    io.in[0] = out; io.out[0] = out;
+    TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io, OpCopy<T, 1>{}, "y_fwd1")));
+    TRY((launch_axis<T, 1, 1, -1, 0>(c, 2, io, OpCopy<T, 1>{}, "x_fwd1")));
+    return PFGB_OK;
+}
+template <typename T>
+static pfgb_status fft_c2r_impl(pfgb_ctx *c, cplx_t<T> *in, T *out) {
+    AxisIO<T, 1, 1> io;
+    io.in[0] = in; io.out[0] = in;
+    TRY((launch_axis<T, 1, 1, +1, 0>(c, 2, io, OpCopy<T, 1>{}, "x_inv1")));
+    TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io, OpCopy<T, 1>{}, "y_inv1")));
+    TRY((launch_z<T, 1, 0>(c, OpRealOut<T>{in, out, c->g.NzC}, "z_c2r", (double)c->g.N * sizeof(T))));
+    return PFGB_OK;
+}
+
+extern "C" {
+
+pfgb_status pfgb_fft3d_r2c(int precision, int Nx, int Ny, int Nz, const void *in, void *out, void *stream) {
+    if (!in || !out) return PFGB_ERR_INVALID;
+    pfgb_ctx c;
+    pfgb_status s = fft_ctx_init(&c, Nx, Ny, Nz, stream);
+    if (s == PFGB_OK)
+        s = precision == PFGB_PREC_FP64 ? fft_r2c_impl<double>(&c, (const double *)in, (double2 *)out)
+                                        : fft_r2c_impl<float>(&c, (const float *)in, (float2 *)out);
+    fft_ctx_free(&c);
+    return s;
+}
+
+// The half-spectrum input is used as workspace and is overwritten.
+pfgb_status pfgb_fft3d_c2r(int precision, int Nx, int Ny, int Nz, const void *in, void *out, void *stream) {
+    if (!in || !out) return PFGB_ERR_INVALID;
+    pfgb_ctx c;
+    pfgb_status s = fft_ctx_init(&c, Nx, Ny, Nz, stream);
+    if (s == PFGB_OK)
+        s = precision == PFGB_PREC_FP64 ? fft_c2r_impl<double>(&c, (double2 *)in, (double *)out)
+                                        : fft_c2r_impl<float>(&c, (float2 *)in, (float *)out);
+    fft_ctx_free(&c);
+    return s;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+pfgb_status pfgb_profile_enable(pfgb_ctx *c, int on) {
+    if (!c) return PFGB_ERR_INVALID;
+    PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->prof = on ? 1 : 0;
+    c->recs.clear();
+    c->pool_used = 0;
+    c->launches = 0;
+    return PFGB_OK;
+}
+
+long long pfgb_profile_launches(const pfgb_ctx *c) { return c ? c->launches : -1; }
+
+// Aggregate the recorded launches by tag.  Call with names == NULL to get
+// the number of distinct tags; otherwise fills up to `cap` rows.
+int pfgb_profile_read(pfgb_ctx *c, const char **names, double *ms, double *bytes, int *count, int cap) {
+    if (!c) return -1;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return -1;
+    std::vector<const char *> tags;
+    std::vector<double> t, b;
+    std::vector<int> n;
+    for (auto &r : c->recs) {
+        float e = 0.f;
+        cudaEventElapsedTime(&e, r.a, r.b);
+        size_t i = 0;
+        while (i < tags.size() && strcmp(tags[i], r.tag) != 0) ++i;
+        if (i == tags.size()) { tags.push_back(r.tag); t.push_back(0); b.push_back(0); n.push_back(0); }
+        t[i] += e; b[i] += r.bytes; n[i] += 1;
+    }
+    if (names) {
+        for (int i = 0; i < (int)tags.size() && i < cap; ++i) {
+            names[i] = tags[i]; ms[i] = t[i]; bytes[i] = b[i]; count[i] = n[i];
+        }
+    }
+    return (int)tags.size();
+}
+
+}  // extern "C"

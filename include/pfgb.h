@@ -1,0 +1,270 @@
+/*
+ * pfgb.h — C ABI of the GB300-native phase-field time-stepping library.
+ *
+ * The library advances the CUDA_STO_PF Ag2Te/PbTe phase-field model
+ * (phi Allen-Cahn, eta GP-zone Allen-Cahn, logit-composition Y
+ * Cahn-Hilliard, FFT micro-elasticity with heterogeneous stiffness) on one
+ * GPU.  Every entry point takes plain pointers and sizes and returns a
+ * pfgb_status; nothing calls exit().
+ *
+ * Which reference interface each entry point replaces (the reference has no
+ * library API; its hot path is inline code in main() of main_cuda.cu):
+ *   pfgb_params            <- PFParams, pf_params.h:6-702 (hot-path subset)
+ *   pfgb_params_default    <- params_default(), main_cuda.cu:15781-16439
+ *   pfgb_params_finalize   <- pfparams_refresh_thermo(), main_cuda.cu:15603-15613
+ *   pfgb_create            <- device allocation + cuFFT plans + kspace_build_cuda,
+ *                             main_cuda.cu:27757-28182, cuda_common.cu:76-109
+ *   pfgb_load_fields       <- initial host->device copies, main_cuda.cu:28046-28076
+ *                             (fields prepared by load_raw_init_fields,
+ *                             main_cuda.cu:2904-2990 -> pfgb_prepare_raw_fields)
+ *   pfgb_step              <- one pass of `for (step...)`, main_cuda.cu:28427-31623
+ *   pfgb_minimize          <- the same loop with --mode=minimize,
+ *                             main_cuda.cu:29264-29750, 32100-32600
+ *   pfgb_read_fields       <- device->host copies before VTK/CSV output,
+ *                             main_cuda.cu:32760-32820
+ *   pfgb_diagnostics       <- gpu_compute_vf_from_h / gpu_reduce_sum_xBtot /
+ *                             gpu_reduce_min_max, cuda_kernels.cu:5609-5942
+ *   pfgb_fft3d_*           <- cufftExecD2Z/Z2D/R2C/C2R call sites,
+ *                             main_cuda.cu:28163-28173 (own kernels, no cuFFT)
+ *
+ * Layouts: real fields are C-order [Nx][Ny][Nz] (z fastest, idx=(i*Ny+j)*Nz+k,
+ * io_vtk_cuda.h:104-108); spectral fields are the half spectrum
+ * [Nx][Ny][Nz/2+1] of interleaved (re,im) pairs, unnormalised forward
+ * transform with exp(-i k.x), like cuFFT D2Z/R2C.
+ */
+#ifndef PFGB_H
+#define PFGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PFGB_ABI_VERSION 1
+
+typedef enum pfgb_status {
+    PFGB_OK = 0,
+    PFGB_ERR_INVALID = 1,        /* bad argument or parameter value        */
+    PFGB_ERR_CUDA = 2,           /* a CUDA runtime call failed             */
+    PFGB_ERR_NOMEM = 3,          /* device allocation failed               */
+    PFGB_ERR_NONCONVERGED = 4,   /* elastic fixed point hit iter_max
+                                    (elastic_fail_on_nonconvergence=1)     */
+    PFGB_ERR_ZERO_MODE = 5,      /* zero-mode mass solve rejected the step */
+    PFGB_ERR_NONFINITE = 6,      /* NaN/Inf residual or field              */
+    PFGB_ERR_TIMEOUT = 7,        /* a bounded device wait ran out          */
+    PFGB_ERR_UNSUPPORTED = 8     /* option outside the implemented path    */
+} pfgb_status;
+
+/* field / transform precision */
+enum { PFGB_PREC_FP64 = 0, PFGB_PREC_FP32 = 1 };
+/* model_mode (pf_params.h model_mode string) */
+enum { PFGB_MODEL_TWO_PHASE = 0, PFGB_MODEL_GP_ZONE = 1 };
+/* mode (pf_params.h: 0=dynamics, 1=minimize) */
+enum { PFGB_MODE_DYNAMICS = 0, PFGB_MODE_MINIMIZE = 1 };
+
+/*
+ * Stiffness tensors are the 21 independent Voigt entries in the reference's
+ * argument order 11,12,13,14,15,16,22,23,24,25,26,33,34,35,36,44,45,46,55,56,66
+ * (Voigt 4=yz, 5=xz, 6=xy).  Strain 6-vectors are xx,yy,zz,yz,xz,xy.
+ */
+typedef struct pfgb_params {
+    /* grid / time */
+    int32_t Nx, Ny, Nz;
+    int32_t model_mode;
+    int32_t mode;
+    int32_t precision;            /* PFGB_PREC_* of phi/eta/Y fields + their FFTs */
+    int32_t elastic_precision;    /* PFGB_PREC_* of the elastic solve (ref: FP32) */
+    int32_t thermo_convex_extrapolation_enabled;
+    double dx, dy, dz, dt;
+    /* thermodynamics (dimensionless) */
+    double temperature_C;
+    double mu_reference_scale;
+    double W, kappa_phi, L_phi;
+    double D_alpha, D_compound;
+    double v_A, v_B;
+    double Vm_compound, Vm_alpha_0, dVm_alpha_dxB;
+    double Y_clip, xB_eps;
+    double elastic_shift_dimless;
+    /* elasticity */
+    int32_t elastic_enabled;
+    int32_t elastic_warm_start_enabled;
+    int32_t elastic_residual_control_enabled;
+    int32_t elastic_iter_min;
+    int32_t elastic_iter_max;
+    int32_t elastic_fail_on_nonconvergence;
+    double elastic_residual_tolerance;
+    double elastic_residual_absolute_floor;
+    double eps_iso_over_vB;
+    double eps00[6];
+    double E0[6];
+    double S[21];
+    double S_p[21];
+    /* Y (composition) update options */
+    int32_t enable_Y_rhs_previous_time_level;
+    int32_t disable_Y_rhs_gamma_term;
+    double Y_rhs_term_h_scale;
+    /* zero mode (PF_CONSERVED_Y_ZERO_MODE_V1) */
+    int32_t zero_mode_enabled;
+    int32_t zero_mode_max_iterations;
+    double zero_mode_tolerance_relative;
+    /* GP zone (model_mode=gp_zone) */
+    int32_t gp_elastic_enabled;
+    int32_t gp_elastic_active_eta;
+    int32_t gp_elastic_active_phi;
+    int32_t gp_pad0;
+    double gp_xB_fixed, gp_delta_g0;
+    double gp_W_eta, gp_kappa_eta, gp_L_eta;
+    double gp_M_GP, gp_M_beta;
+    double gp_eps_iso, gp_elastic_derivative_scale;
+    /* minimize (mode=minimize) */
+    int32_t minimize_full_model;
+    int32_t minimize_post_projection_iters;
+    int32_t minimize_max_iter;
+    int32_t minimize_convergence_steps;
+    double minimize_dt;
+    double minimize_V0;
+    double eta_lambda_vol;
+    double minimize_xB_max_safe;
+    double minimize_rms_dphi_threshold;
+    double minimize_rms_dY_threshold;
+    double minimize_energy_diff_rel_threshold;
+    double minimize_rms_res_threshold;
+    double minimize_vol_err_rel_threshold;
+    /* provenance keys required in the parameter file (main_cuda.cu:1089-1146),
+       used for output naming / physical time, not by the time step */
+    int32_t pf_params_schema_version;
+    int32_t pad1;
+    double t_real_unit;
+    double ic_vf_init_phi, ic_vf_target_phi, ic_phi_iface_w;
+    double gamma_Jm2, lambda_sm_m, Vm_alpha_0_phys_m3mol;
+    /* derived by pfgb_params_finalize (pfparams_refresh_thermo) */
+    double temperature_K;
+    double mu0_compound;
+    double xB_eq_matrix;
+} pfgb_params;
+
+/* Per-step statistics (elastic_solver_trace.csv / pf_zero_mode_trace.csv). */
+typedef struct pfgb_step_stats {
+    int32_t step;                     /* steps taken by this context so far   */
+    int32_t elastic_iterations;       /* of the last step                     */
+    int32_t elastic_converged;
+    int32_t elastic_warm_start_used;
+    double elastic_relative_residual;
+    int32_t elastic_iterations_total; /* summed over the steps of the call    */
+    int32_t zero_mode_iterations;
+    int32_t zero_mode_newton_steps;
+    int32_t zero_mode_bisection_steps;
+    double zero_mode_lambda;
+    double zero_mode_residual;
+    double zero_mode_target_mass;
+    double mean_DY;
+} pfgb_step_stats;
+
+/* Scalar diagnostics of the current state (CSV row, mass ledger). */
+typedef struct pfgb_diag {
+    double vf_precip;      /* <h(phi)>, gpu_compute_vf_from_h            */
+    double mass_xBtot;     /* sum((1-h) xB + h v_B)                      */
+    double mean_xB;
+    double phi_min, phi_max;
+    double xB_min, xB_max;
+    double n_in;           /* cells with phi >= 0.5                      */
+} pfgb_diag;
+
+typedef struct pfgb_ctx pfgb_ctx;
+
+/* --- parameters ------------------------------------------------------- */
+size_t      pfgb_params_size(void);
+void        pfgb_params_default(pfgb_params *p);
+/*
+ * Apply a `key=value` parameter file (load_pfparams_override_file,
+ * main_cuda.cu:22306-22360): '#' comments, unknown keys warned on stderr and
+ * ignored, a malformed number is an error, and the required key set
+ * (validate_required_pfparams_presence, main_cuda.cu:1089-1146) must be
+ * present.  errbuf (may be NULL) receives a one-line reason on failure.
+ */
+pfgb_status pfgb_params_load_file(pfgb_params *p, const char *path, char *errbuf, size_t errlen);
+/* Apply one key (same semantics; returns PFGB_ERR_UNSUPPORTED for an unknown key). */
+pfgb_status pfgb_params_set(pfgb_params *p, const char *key, const char *value);
+pfgb_status pfgb_params_finalize(pfgb_params *p);
+const char *pfgb_status_string(pfgb_status s);
+
+/* --- context ---------------------------------------------------------- */
+pfgb_status pfgb_create(const pfgb_params *p, int device, pfgb_ctx **out);
+void        pfgb_destroy(pfgb_ctx *ctx);
+const char *pfgb_last_error(const pfgb_ctx *ctx);
+/* All work of the context is issued on this stream (cudaStream_t, may be 0). */
+pfgb_status pfgb_set_stream(pfgb_ctx *ctx, void *cuda_stream);
+size_t      pfgb_device_bytes(const pfgb_ctx *ctx);
+
+/*
+ * Host-side preparation of raw initial fields, the rules of
+ * load_raw_init_fields (main_cuda.cu:2904-2990): phi, eta clamped to [0,1],
+ * xB clamped to [xB_eps, 1-xB_eps] and capped at xB_max_safe (NaN = no cap).
+ * Returns PFGB_ERR_NONFINITE on NaN/Inf input.  In-place on host buffers.
+ */
+pfgb_status pfgb_prepare_raw_fields(const pfgb_params *p, double xB_max_safe,
+                                    double *phi, double *xB, double *eta,
+                                    const double *dYdt_prev, size_t n);
+
+/*
+ * Upload the state from HOST buffers (float64, C order, N values each).
+ * Y = logit(xB) is formed on the device.  eta and dYdt_prev may be NULL
+ * (zero).  Resets the elastic warm state and, when zero mode is on, freezes
+ * the target mass sum((1-h) xB + h v_B) (main_cuda.cu:28079-28086).
+ */
+pfgb_status pfgb_load_fields(pfgb_ctx *ctx, const double *phi, const double *xB,
+                             const double *eta, const double *dYdt_prev);
+/*
+ * Replace the fields from HOST buffers but keep the solver history: the
+ * elastic warm state, the zero-mode target mass and the step count (the
+ * continuation contract of a checkpoint restart, main_cuda.cu:33494-33560).
+ */
+pfgb_status pfgb_set_fields(pfgb_ctx *ctx, const double *phi, const double *xB,
+                            const double *eta, const double *dYdt_prev);
+/* Same as pfgb_load_fields, from DEVICE pointers (float64). */
+pfgb_status pfgb_load_fields_device(pfgb_ctx *ctx, const double *d_phi,
+                                    const double *d_xB, const double *d_eta,
+                                    const double *d_dYdt_prev);
+
+/* Advance nsteps dynamics steps.  stats may be NULL. */
+pfgb_status pfgb_step(pfgb_ctx *ctx, int nsteps, pfgb_step_stats *stats);
+
+/* Read the state back to HOST buffers (float64); any pointer may be NULL. */
+pfgb_status pfgb_read_fields(pfgb_ctx *ctx, double *phi, double *xB, double *Y,
+                             double *eta, double *dYdt_prev);
+/* Stress sigma (6 x N float32, order xx,yy,zz,yz,xz,xy) and total strain. */
+pfgb_status pfgb_read_elastic(pfgb_ctx *ctx, float *sigma6, float *strain6);
+/* Warm elastic displacement u_k (3 x Nk complex float32 interleaved). */
+pfgb_status pfgb_read_displacement_k(pfgb_ctx *ctx, float *u3);
+
+pfgb_status pfgb_diagnostics(pfgb_ctx *ctx, pfgb_diag *d);
+
+/* Synchronise the context's stream. */
+pfgb_status pfgb_sync(pfgb_ctx *ctx);
+
+/* --- instrumentation (no reference counterpart; the reference prints
+ *     cudaEvent totals only, main_cuda.cu:32634-32660) -------------------- */
+/* Enable/disable per-launch CUDA-event timing on the context stream and
+ * reset the accumulators and the launch counter. */
+pfgb_status pfgb_profile_enable(pfgb_ctx *ctx, int on);
+/* Kernel launches issued by the context since the last enable/reset. */
+long long   pfgb_profile_launches(const pfgb_ctx *ctx);
+/* Per-tag totals: names, milliseconds, algorithmic bytes, launch counts.
+ * Returns the number of tags; pass names == NULL to query it. */
+int         pfgb_profile_read(pfgb_ctx *ctx, const char **names, double *ms, double *bytes,
+                              int *count, int cap);
+
+/* --- standalone 3D transforms on DEVICE buffers (test / tooling) ------ */
+/* precision: PFGB_PREC_FP64 (double in, double2 out) or PFGB_PREC_FP32.
+ * Unnormalised, same conventions as cuFFT D2Z/Z2D (R2C/C2R).             */
+pfgb_status pfgb_fft3d_r2c(int precision, int Nx, int Ny, int Nz,
+                           const void *d_in, void *d_out, void *cuda_stream);
+pfgb_status pfgb_fft3d_c2r(int precision, int Nx, int Ny, int Nz,
+                           const void *d_in, void *d_out, void *cuda_stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PFGB_H */

@@ -1,0 +1,1118 @@
+/*
+ * pf_oracle.c — CPU FP64 restatement of the CUDA_STO_PF dynamics step.
+ *
+ * TEST INFRASTRUCTURE (the checker).  Only tests/, __graft_entry__.smoke()
+ * and bench.py's cpu_baseline leg use it; the shipped library never does.
+ *
+ * Each function cites the reference code it restates.  All arithmetic is
+ * FP64; where the reference stores elastic quantities in FP32 (cuda_kernels.cu
+ * elastic kernels, main_cuda.cu:28760-28790 casts) the oracle rounds the stored
+ * value to float at the same point when elastic_precision == PFGB_PREC_FP32.
+ * The sequence of the driver (main_cuda.cu:28427-31623) is followed literally:
+ * one FFT per reference FFT, one dealias per reference dealias call.
+ */
+#include "pf_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct { double re, im; } cpx;
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+/* ------------------------------------------------------------------ */
+/* phase functions — phase_functions.h:7-56                             */
+/* ------------------------------------------------------------------ */
+static inline double o_h(double p) {          /* h = p^3 (6p^2 - 15p + 10) */
+    double p2 = p * p, p3 = p2 * p;
+    return p3 * (6.0 * p2 - 15.0 * p + 10.0);
+}
+static inline double o_hp(double p) {         /* h' = 30 p^2 (1-p)^2 */
+    double p2 = p * p;
+    return 30.0 * p2 * (1.0 - p) * (1.0 - p);
+}
+static inline double o_g(double p) { return p * p * (1.0 - p) * (1.0 - p); }
+static inline double o_gp(double p) {         /* g' = 2p(1-p)(1-2p) */
+    return 2.0 * p * (1.0 - p) * (1.0 - 2.0 * p);
+}
+static inline double o_clamp01(double v) { return v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v); }
+static inline double o_clamp_eps(double v, double eps) {
+    return v < eps ? eps : (v > 1.0 - eps ? 1.0 - eps : v);
+}
+
+double pfo_h(double p) { return o_h(p); }
+double pfo_hp(double p) { return o_hp(p); }
+double pfo_gp(double p) { return o_gp(p); }
+
+/* ------------------------------------------------------------------ */
+/* thermodynamics — thermo_utils.h:248-579                              */
+/* SGTE unary Gibbs energies (Gierlotka 2010 data as used by the        */
+/* reference), pseudo-binary regular solution PbTe-Ag2Te.               */
+/* ------------------------------------------------------------------ */
+#define O_RGAS 8.31446261815324
+
+/* GHSER(T) = a + b T + c T ln T + d T^2 + e T^3 + f / T + g T^-9
+ * piecewise in T; one row per (element, range).  thermo_utils.h:280-302 */
+typedef struct { double Tmax, a, b, c, d, e, f, g; } sgte_row;
+static const sgte_row SGTE_PB[2] = {
+    {600.61, -7650.085, 101.700244, -24.5242231, -0.00365895, -2.4395e-7, 0.0, 0.0},
+    {1.0e300, -10531.095, 154.243182, -32.4913959, 0.00154613, 0.0, 0.0, 8.05448e25}};
+static const sgte_row SGTE_AG[2] = {
+    {1234.93, -7209.512, 118.202013, -23.8463314, -0.001790585, -3.98587e-7, -12011.0, 0.0},
+    {1.0e300, -15095.252, 190.266404, -33.472, 0.0, 0.0, 0.0, 1.411773e29}};
+static const sgte_row SGTE_TE[2] = {
+    {722.66, -10544.679, 183.372894, -35.6687, 0.01583435, -5.240417e-6, 155015.0, 0.0},
+    {1.0e300, 9160.595, -129.265373, 13.004, -0.0362361, 5.006367e-6, 0.0, -1.28681e30}};
+
+static double sgte_eval(const sgte_row *rows, double T) {
+    const sgte_row *r = (T < rows[0].Tmax) ? &rows[0] : &rows[1];
+    /* term order follows the reference expression left to right */
+    double v = r->a + r->b * T + r->c * T * log(T);
+    v += r->d * T * T;
+    if (r->e != 0.0) v += r->e * pow(T, 3);
+    if (r->f != 0.0) v += r->f / T;
+    if (r->g != 0.0) v += r->g * pow(T, -9);
+    return v;
+}
+
+static double o_G_PbTe(double T) {            /* thermo_utils.h:306-309 */
+    return (-76063.2138 + 9.67716633 * T) + sgte_eval(SGTE_PB, T) + sgte_eval(SGTE_TE, T);
+}
+static double o_G_Ag2Te(double T) {           /* thermo_utils.h:312-316 */
+    double per_atom = -10128.93 - 12.645115 * T;
+    double g = per_atom + (2.0 / 3.0) * sgte_eval(SGTE_AG, T) + (1.0 / 3.0) * sgte_eval(SGTE_TE, T);
+    return 3.0 * g;
+}
+static double o_Lparam(double T) { return 41212.9 - 18.05 * T; }   /* :325-327 */
+
+#define O_XLIM_CONVEX 0.09                    /* thermo_utils.h:264 */
+
+static double mu_PbTe_cal(double T, double xB) {
+    double x = o_clamp_eps(xB, 1e-12);
+    return o_G_PbTe(T) + O_RGAS * T * log(1.0 - x) + o_Lparam(T) * x * x;
+}
+static double mu_Ag2Te_cal(double T, double xB) {
+    double x = o_clamp_eps(xB, 1e-12);
+    return o_G_Ag2Te(T) + O_RGAS * T * log(x) + o_Lparam(T) * (1.0 - x) * (1.0 - x);
+}
+static double dmu_PbTe_cal(double T, double xB) {
+    double x = o_clamp_eps(xB, 1e-12);
+    return -O_RGAS * T / (1.0 - x) + 2.0 * o_Lparam(T) * x;
+}
+static double dmu_Ag2Te_cal(double T, double xB) {
+    double x = o_clamp_eps(xB, 1e-12);
+    return O_RGAS * T / x - 2.0 * o_Lparam(T) * (1.0 - x);
+}
+/* convex extrapolation above X_LIMIT_CONVEX, thermo_utils.h:370-401 */
+static double mu_PbTe_raw(double T, double xB, int convex) {
+    if (!convex || xB <= O_XLIM_CONVEX) return mu_PbTe_cal(T, xB);
+    double xc = O_XLIM_CONVEX, d = xB - xc;
+    return mu_PbTe_cal(T, xc) + dmu_PbTe_cal(T, xc) * d + 5000.0 * d * d;
+}
+static double mu_Ag2Te_raw(double T, double xB, int convex) {
+    if (!convex || xB <= O_XLIM_CONVEX) return mu_Ag2Te_cal(T, xB);
+    double xc = O_XLIM_CONVEX, d = xB - xc;
+    return mu_Ag2Te_cal(T, xc) + dmu_Ag2Te_cal(T, xc) * d + 5000.0 * d * d;
+}
+static double o_scale(double s) {             /* thermo_utils.h:409-418 */
+    return (fabs(s) < 1e-30) ? ((s >= 0.0) ? 1e-30 : -1e-30) : s;
+}
+static double o_muA(double xB, double T, double s, int cv) { return mu_PbTe_raw(T, xB, cv) / o_scale(s); }
+static double o_muB(double xB, double T, double s, int cv) { return mu_Ag2Te_raw(T, xB, cv) / o_scale(s); }
+
+double pfo_mu_A(double xB, double T_K, double scale, int convex) { return o_muA(xB, T_K, scale, convex); }
+double pfo_mu_B(double xB, double T_K, double scale, int convex) { return o_muB(xB, T_K, scale, convex); }
+
+/* Newton on RT ln x + L (1-x)^2 = 0, thermo_utils.h:427-452 */
+double pfo_xB_eq(double T) {
+    double L = o_Lparam(T), RT = O_RGAS * T;
+    double x = exp(-L / RT);
+    if (x < 1e-9) x = 1e-9;
+    if (x > 0.99) x = 0.5;
+    for (int it = 0; it < 20; ++it) {
+        double f = RT * log(x) + L * (1.0 - x) * (1.0 - x);
+        double df = RT / x - 2.0 * L * (1.0 - x);
+        double dlt = f / df;
+        x -= dlt;
+        if (x < 1e-10) x = 1e-10;
+        if (x > 0.999) x = 0.999;
+        if (fabs(dlt) < 1e-8) break;
+    }
+    return x;
+}
+
+static double o_Vm_alpha(double xB, double Vm0, double dVm) { return Vm0 + dVm * xB; }
+static double o_c_xB_phi(double xB, double Vm0, double dVm, double Vmc, double h) {
+    double den = o_Vm_alpha(xB, Vm0, dVm) * (1.0 - h) + Vmc * h;   /* :472-479 */
+    if (fabs(den) < 1e-12) den = (den >= 0.0) ? 1e-12 : -1e-12;
+    return 1.0 / den;
+}
+static double o_mu_tot_mix(double muA, double muB, double xB, double mu0, double h) {
+    double mix = muA * (1.0 - xB) + muB * xB;                      /* :482-486 */
+    return (1.0 - h) * mix + h * mu0;
+}
+static double o_sigmoid(double Y, double Yc, double eps) {       /* :498-514 */
+    if (Y > Yc) Y = Yc;
+    if (Y < -Yc) Y = -Yc;
+    double x;
+    if (Y >= 0) { double e = exp(-Y); x = 1.0 / (1.0 + e); }
+    else { double e = exp(Y); x = e / (1.0 + e); }
+    if (x < eps) x = eps;
+    if (x > 1.0 - eps) x = 1.0 - eps;
+    return x;
+}
+static double o_sigmoid_raw(double Y) {     /* pf_zero_mode_sigmoid, cuda_kernels.cu:3391-3399 */
+    if (Y >= 0.0) { double e = exp(-Y); return 1.0 / (1.0 + e); }
+    double e = exp(Y);
+    return e / (1.0 + e);
+}
+static double o_logit(double xB, double eps, double Yc) {        /* :516-523 */
+    if (xB < eps) xB = eps;
+    if (xB > 1.0 - eps) xB = 1.0 - eps;
+    double Y = log(xB / (1.0 - xB));
+    if (Y > Yc) return Yc;
+    if (Y < -Yc) return -Yc;
+    return Y;
+}
+double pfo_sigmoid(double Y, double Yc, double eps) { return o_sigmoid(Y, Yc, eps); }
+double pfo_logit(double xB, double eps, double Yc) { return o_logit(xB, eps, Yc); }
+
+static double o_Dmix(double h, double Da, double Dc) { return (1.0 - h) * Da + h * Dc; }
+
+/* thermodynamic factor by central difference, thermo_utils.h:552-577 */
+static double o_gamma(double xB, double h, double Vm0, double dVm, double Vmc,
+                      double T, double s, int cv) {
+    double xc = xB;
+    if (cv && xc > 0.08) xc = 0.08;
+    double cb = o_c_xB_phi(xc, Vm0, dVm, Vmc, h);
+    double dx = 1e-5;
+    double xp = o_clamp_eps(xc + dx, 1e-12), xm = o_clamp_eps(xc - dx, 1e-12);
+    double dA = (o_muA(xp, T, s, cv) - o_muA(xm, T, s, cv)) / (xp - xm);
+    double dB = (o_muB(xp, T, s, cv) - o_muB(xm, T, s, cv)) / (xp - xm);
+    return cb * (dB - dA);
+}
+double pfo_gamma(double xB, double h, double Vm0, double dVm, double Vmc,
+                 double T_K, double scale, int convex) {
+    return o_gamma(xB, h, Vm0, dVm, Vmc, T_K, scale, convex);
+}
+
+/* positive bounded mobility, cuda_kernels.cu:30-38 */
+static double o_meff(double Dm, double g) {
+    const double gfloor = 1.0e-4;
+    const double Ds = fmax(Dm, 0.0);
+    const double gs = (isfinite(g) && g > gfloor) ? g : gfloor;
+    const double cap = Ds * 1000.0;
+    const double v = Ds / gs;
+    return (isfinite(v) && v < cap) ? v : cap;
+}
+double pfo_meff(double Dm, double g) { return o_meff(Dm, g); }
+
+void pfo_params_finalize(pfgb_params *p) {   /* main_cuda.cu:15603-15613 */
+    double T = p->temperature_C + 273.15;
+    if (T < 1.0) T = 1.0;
+    p->temperature_K = T;
+    double xeq = pfo_xB_eq(T);
+    p->xB_eq_matrix = xeq;
+    double muA = o_muA(xeq, T, p->mu_reference_scale, p->thermo_convex_extrapolation_enabled);
+    double muB = o_muB(xeq, T, p->mu_reference_scale, p->thermo_convex_extrapolation_enabled);
+    double vs = p->v_A + p->v_B;
+    if (fabs(vs) < 1e-30) vs = (vs >= 0.0) ? 1e-30 : -1e-30;
+    p->mu0_compound = (p->v_A * muA + p->v_B * muB) / vs;
+}
+
+/* ------------------------------------------------------------------ */
+/* state                                                                */
+/* ------------------------------------------------------------------ */
+struct pfo_state {
+    pfgb_params p;
+    int Nx, Ny, Nz, NzC;
+    size_t N, Nk;
+    double invN;
+    int fp32e;              /* elastic stored in FP32 like the reference */
+    int gp;                 /* model_mode == gp_zone */
+    int step;
+    /* fields */
+    double *phi, *eta, *Y, *xB, *dYdt;
+    double *phi_n, *eta_prev, *Y_n, *xB_prev;
+    double *rhs, *mu, *scr, *divJ, *lapY, *mass_t, *der_t;
+    cpx *phi_k, *rhs_k, *mu_k, *divJ_k, *Y_k, *scr_k, *eta_k;
+    /* elastic */
+    double *eps_r[6], *sig_r[6];
+    cpx *eps_k[6], *u_k[3], *u_next[3];
+    int warm_valid;
+    /* k tables */
+    double *kx, *ky, *kz;
+    unsigned char *mx, *my, *mz;  /* 1 = dealiased (zeroed) */
+    double target_mass;
+};
+
+static inline double rf(const pfo_state *s, double v) { return s->fp32e ? (double)(float)v : v; }
+
+/* kx_wrap / ky_wrap / kz_wrap, cuda_common.h:68-82 */
+static double kwrap(int i, int n, double d) {
+    int ii = (i <= n / 2) ? i : i - n;
+    return 2.0 * M_PI * ii / (d * n);
+}
+/* 2/3-rule predicate, cuda_kernels.cu:103-131 */
+static int dealias_cut(double k, double d) {
+    const double kmax = M_PI * (2.0 / 3.0) / d;
+    return fabs(k) >= kmax;
+}
+
+static void *xalloc(size_t n) {
+    void *p = calloc(n ? n : 1, 1);
+    return p;
+}
+
+pfo_state *pfo_create(const pfgb_params *pin) {
+    pfo_state *s = (pfo_state *)xalloc(sizeof(pfo_state));
+    s->p = *pin;
+    pfo_params_finalize(&s->p);
+    s->Nx = pin->Nx; s->Ny = pin->Ny; s->Nz = pin->Nz; s->NzC = pin->Nz / 2 + 1;
+    s->N = (size_t)s->Nx * s->Ny * s->Nz;
+    s->Nk = (size_t)s->Nx * s->Ny * s->NzC;
+    s->invN = 1.0 / (double)s->N;
+    s->fp32e = (pin->elastic_precision == PFGB_PREC_FP32);
+    s->gp = (pin->model_mode == PFGB_MODEL_GP_ZONE);
+    const size_t rb = sizeof(double) * s->N, kb = sizeof(cpx) * s->Nk;
+    double **rf_[] = {&s->phi, &s->eta, &s->Y, &s->xB, &s->dYdt, &s->phi_n, &s->eta_prev,
+                      &s->Y_n, &s->xB_prev, &s->rhs, &s->mu, &s->scr, &s->divJ, &s->lapY,
+                      &s->mass_t, &s->der_t};
+    for (size_t i = 0; i < sizeof(rf_) / sizeof(rf_[0]); ++i) *rf_[i] = (double *)xalloc(rb);
+    cpx **kf_[] = {&s->phi_k, &s->rhs_k, &s->mu_k, &s->divJ_k, &s->Y_k, &s->scr_k, &s->eta_k};
+    for (size_t i = 0; i < sizeof(kf_) / sizeof(kf_[0]); ++i) *kf_[i] = (cpx *)xalloc(kb);
+    for (int c = 0; c < 6; ++c) {
+        s->eps_r[c] = (double *)xalloc(rb);
+        s->sig_r[c] = (double *)xalloc(rb);
+        s->eps_k[c] = (cpx *)xalloc(kb);
+    }
+    for (int c = 0; c < 3; ++c) {
+        s->u_k[c] = (cpx *)xalloc(kb);
+        s->u_next[c] = (cpx *)xalloc(kb);
+    }
+    s->kx = (double *)xalloc(sizeof(double) * s->Nx);
+    s->ky = (double *)xalloc(sizeof(double) * s->Ny);
+    s->kz = (double *)xalloc(sizeof(double) * s->NzC);
+    s->mx = (unsigned char *)xalloc(s->Nx);
+    s->my = (unsigned char *)xalloc(s->Ny);
+    s->mz = (unsigned char *)xalloc(s->NzC);
+    for (int i = 0; i < s->Nx; ++i) { s->kx[i] = kwrap(i, s->Nx, pin->dx); s->mx[i] = dealias_cut(s->kx[i], pin->dx); }
+    for (int j = 0; j < s->Ny; ++j) { s->ky[j] = kwrap(j, s->Ny, pin->dy); s->my[j] = dealias_cut(s->ky[j], pin->dy); }
+    for (int k = 0; k < s->NzC; ++k) {
+        s->kz[k] = 2.0 * M_PI * k / (pin->dz * s->Nz);
+        s->mz[k] = dealias_cut(s->kz[k], pin->dz);
+    }
+    return s;
+}
+
+void pfo_destroy(pfo_state *s) {
+    if (!s) return;
+    double *rr[] = {s->phi, s->eta, s->Y, s->xB, s->dYdt, s->phi_n, s->eta_prev, s->Y_n,
+                    s->xB_prev, s->rhs, s->mu, s->scr, s->divJ, s->lapY, s->mass_t, s->der_t};
+    for (size_t i = 0; i < sizeof(rr) / sizeof(rr[0]); ++i) free(rr[i]);
+    cpx *kk[] = {s->phi_k, s->rhs_k, s->mu_k, s->divJ_k, s->Y_k, s->scr_k, s->eta_k};
+    for (size_t i = 0; i < sizeof(kk) / sizeof(kk[0]); ++i) free(kk[i]);
+    for (int c = 0; c < 6; ++c) { free(s->eps_r[c]); free(s->sig_r[c]); free(s->eps_k[c]); }
+    for (int c = 0; c < 3; ++c) { free(s->u_k[c]); free(s->u_next[c]); }
+    free(s->kx); free(s->ky); free(s->kz); free(s->mx); free(s->my); free(s->mz);
+    free(s);
+}
+
+int pfo_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+/* deterministic sum: fixed 4096-element blocks, block partials summed in order */
+static double dsum(const double *a, size_t n) {
+    const size_t B = 4096;
+    size_t nb = (n + B - 1) / B;
+    double *part = (double *)malloc(sizeof(double) * (nb ? nb : 1));
+#pragma omp parallel for schedule(static)
+    for (long long b = 0; b < (long long)nb; ++b) {
+        size_t lo = (size_t)b * B, hi = lo + B < n ? lo + B : n;
+        double acc = 0.0;
+        for (size_t i = lo; i < hi; ++i) acc += a[i];
+        part[b] = acc;
+    }
+    double t = 0.0;
+    for (size_t b = 0; b < nb; ++b) t += part[b];
+    free(part);
+    return t;
+}
+
+/* 3D transforms on the state's grid */
+static void fwd(pfo_state *s, const double *r, cpx *k) {
+    pfo_fft3d_r2c(s->Nx, s->Ny, s->Nz, r, (double *)k);
+}
+static void inv(pfo_state *s, const cpx *k, double *r) {
+    pfo_fft3d_c2r(s->Nx, s->Ny, s->Nz, (const double *)k, r);
+}
+
+#define KLOOP_BEGIN(s)                                                        \
+    _Pragma("omp parallel for schedule(static)")                              \
+    for (long long idx_ = 0; idx_ < (long long)(s)->Nk; ++idx_) {            \
+        const size_t idx = (size_t)idx_;                                      \
+        const int kk_ = (int)(idx % (s)->NzC);                                \
+        const int jj_ = (int)((idx / (s)->NzC) % (s)->Ny);                    \
+        const int ii_ = (int)(idx / ((size_t)(s)->NzC * (s)->Ny));            \
+        (void)kk_; (void)jj_; (void)ii_;
+#define KLOOP_END }
+
+#define RLOOP_BEGIN(s)                                                        \
+    _Pragma("omp parallel for schedule(static)")                              \
+    for (long long idx_ = 0; idx_ < (long long)(s)->N; ++idx_) {             \
+        const size_t idx = (size_t)idx_;
+#define RLOOP_END }
+
+static inline int masked(const pfo_state *s, int i, int j, int k) {
+    return s->mx[i] | s->my[j] | s->mz[k];
+}
+
+/* dealias_23_kernel, cuda_kernels.cu:103-131 (+ the float variant :135-160) */
+static void dealias(pfo_state *s, cpx *f) {
+    KLOOP_BEGIN(s)
+        if (masked(s, ii_, jj_, kk_)) { f[idx].re = 0.0; f[idx].im = 0.0; }
+    KLOOP_END
+}
+
+static double k2_at(const pfo_state *s, int i, int j, int k) {
+    /* kspace_build_kernel, cuda_common.cu:51-73 */
+    double kx = s->kx[i], ky = s->ky[j], kz = s->kz[k];
+    return kx * kx + ky * ky + kz * kz;
+}
+
+/* ------------------------------------------------------------------ */
+/* elastic solve — main_cuda.cu:28760-29160                             */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    double S[21], Sp[21], e00[6], E0[6];
+} elast_consts;
+
+/* indices into the 21-vector: 11 12 13 14 15 16 22 23 24 25 26 33 34 35 36 44 45 46 55 56 66 */
+enum { C11, C12, C13, C14, C15, C16, C22, C23, C24, C25, C26, C33, C34, C35, C36,
+       C44, C45, C46, C55, C56, C66 };
+
+/* symmetric 6x6 accessor (1-based Voigt a,b) */
+static double voigt(const double *c21, int a, int b) {
+    static const int map[7][7] = {
+        {0, 0, 0, 0, 0, 0, 0},
+        {0, C11, C12, C13, C14, C15, C16},
+        {0, C12, C22, C23, C24, C25, C26},
+        {0, C13, C23, C33, C34, C35, C36},
+        {0, C14, C24, C34, C44, C45, C46},
+        {0, C15, C25, C35, C45, C55, C56},
+        {0, C16, C26, C36, C46, C56, C66}};
+    return c21[map[a][b]];
+}
+
+/* Voigt engineering vector from tensor strain xx,yy,zz,yz,xz,xy */
+static void eng(const double *e, double *v) {
+    v[0] = e[0]; v[1] = e[1]; v[2] = e[2];
+    v[3] = 2.0 * e[3]; v[4] = 2.0 * e[4]; v[5] = 2.0 * e[5];
+}
+
+/* eigenstrain_phi_xB_point / eigenstrain_phi_eta_xB_point,
+ * cuda_kernels.cu:193-290 */
+static void eigen_point(const pfo_state *s, const elast_consts *ec, double phi, double eta,
+                        double xB_clamped, int gp_elastic, double *e0) {
+    const pfgb_params *P = &s->p;
+    if (!gp_elastic) {
+        double h = o_h(phi);
+        double epsc = xB_clamped * P->eps_iso_over_vB;
+        double omh = 1.0 - h;
+        for (int c = 0; c < 3; ++c) e0[c] = rf(s, omh * epsc + h * ec->e00[c]);
+        for (int c = 3; c < 6; ++c) e0[c] = rf(s, h * ec->e00[c]);
+        return;
+    }
+    double hb = o_h(phi), he = o_h(eta);
+    double hg = (1.0 - hb) * he, ha = (1.0 - hb) * (1.0 - he);
+    double ea = xB_clamped * P->eps_iso_over_vB;
+    for (int c = 0; c < 3; ++c) e0[c] = rf(s, ha * ea + hg * P->gp_eps_iso + hb * ec->e00[c]);
+    for (int c = 3; c < 6; ++c) e0[c] = rf(s, hb * ec->e00[c]);
+}
+
+/* acoustic tensor K_ij = k_a C_iajb k_b (the "g" combinations of
+ * cuda_kernels.cu:6538-6567 / K of :6822-6866) */
+static void acoustic(const double *S, double kx, double ky, double kz, double K[3][3]) {
+    const double kv[3] = {kx, ky, kz};
+    /* Voigt index of (i,j) */
+    static const int vi[3][3] = {{1, 6, 5}, {6, 2, 4}, {5, 4, 3}};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                    acc += kv[a] * voigt(S, vi[i][a], vi[j][b]) * kv[b];
+            K[i][j] = acc;
+        }
+}
+
+static int inverse3(double K[3][3], double G[3][3]) {
+    double det = K[0][0] * (K[1][1] * K[2][2] - K[1][2] * K[2][1])
+               - K[0][1] * (K[1][0] * K[2][2] - K[1][2] * K[2][0])
+               + K[0][2] * (K[1][0] * K[2][1] - K[1][1] * K[2][0]);
+    if (fabs(det) < 1e-30) return 0;
+    G[0][0] = (K[1][1] * K[2][2] - K[1][2] * K[2][1]) / det;
+    G[0][1] = (K[0][2] * K[2][1] - K[0][1] * K[2][2]) / det;
+    G[0][2] = (K[0][1] * K[1][2] - K[0][2] * K[1][1]) / det;
+    G[1][0] = (K[1][2] * K[2][0] - K[1][0] * K[2][2]) / det;
+    G[1][1] = (K[0][0] * K[2][2] - K[0][2] * K[2][0]) / det;
+    G[1][2] = (K[0][2] * K[1][0] - K[0][0] * K[1][2]) / det;
+    G[2][0] = (K[1][0] * K[2][1] - K[1][1] * K[2][0]) / det;
+    G[2][1] = (K[0][1] * K[2][0] - K[0][0] * K[2][1]) / det;
+    G[2][2] = (K[0][0] * K[1][1] - K[0][1] * K[1][0]) / det;
+    return 1;
+}
+
+/* u_k = -i G(k) (k . tau_k) for a symmetric source tau (6 components):
+ * compute_displacement_from_eigenstrain_k_kernel (tau = C0:eps0,
+ * :6734-6998) and compute_displacement_from_hij_green_kernel (tau = h,
+ * :6484-6634); k = 0 -> 0, |det| < 1e-30 -> 0. */
+static void green_apply(pfo_state *s, const elast_consts *ec, cpx **tau_k, int tau_is_eigen,
+                        cpx **u_out) {
+    static const int vi[3][3] = {{1, 6, 5}, {6, 2, 4}, {5, 4, 3}};
+    static const int comp_of[3][3] = {{0, 5, 4}, {5, 1, 3}, {4, 3, 2}}; /* xx yy zz yz xz xy */
+    KLOOP_BEGIN(s)
+        double kx = s->kx[ii_], ky = s->ky[jj_], kz = s->kz[kk_];
+        if (ii_ == 0 && jj_ == 0 && kk_ == 0) {
+            for (int c = 0; c < 3; ++c) { u_out[c][idx].re = 0.0; u_out[c][idx].im = 0.0; }
+            continue;
+        }
+        double K[3][3], G[3][3];
+        acoustic(ec->S, kx, ky, kz, K);
+        if (!inverse3(K, G)) {
+            for (int c = 0; c < 3; ++c) { u_out[c][idx].re = 0.0; u_out[c][idx].im = 0.0; }
+            continue;
+        }
+        const double kv[3] = {kx, ky, kz};
+        /* t_i = k_j tau_ij ; for the eigen source tau_ij = C_ijkl eps0_kl */
+        double tr[3] = {0, 0, 0}, ti[3] = {0, 0, 0};
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double ar, ai;
+                if (tau_is_eigen) {
+                    ar = 0.0; ai = 0.0;
+                    for (int a = 0; a < 3; ++a)
+                        for (int b = 0; b < 3; ++b) {
+                            double c = voigt(ec->S, vi[i][j], vi[a][b]);
+                            const cpx e = tau_k[comp_of[a][b]][idx];
+                            ar += c * e.re; ai += c * e.im;
+                        }
+                } else {
+                    const cpx e = tau_k[comp_of[i][j]][idx];
+                    ar = e.re; ai = e.im;
+                }
+                tr[i] += kv[j] * ar; ti[i] += kv[j] * ai;
+            }
+        for (int c = 0; c < 3; ++c) {
+            double sr = 0.0, si = 0.0;
+            for (int d = 0; d < 3; ++d) { sr += G[c][d] * tr[d]; si += G[c][d] * ti[d]; }
+            /* u = -i (sr + i si) = si - i sr */
+            u_out[c][idx].re = rf(s, si);
+            u_out[c][idx].im = rf(s, -sr);
+        }
+    KLOOP_END
+}
+
+/* compute_strain_from_displacement_k_kernel, cuda_kernels.cu:6673-6730 */
+static void strain_from_u(pfo_state *s, cpx **u, cpx **e) {
+    KLOOP_BEGIN(s)
+        double kv[3] = {rf(s, s->kx[ii_]), rf(s, s->ky[jj_]), rf(s, s->kz[kk_])};
+        const cpx uu[3] = {u[0][idx], u[1][idx], u[2][idx]};
+        /* eps_ij = i (k_i u_j + k_j u_i) / 2 */
+        static const int pr[6][2] = {{0, 0}, {1, 1}, {2, 2}, {1, 2}, {0, 2}, {0, 1}};
+        for (int c = 0; c < 6; ++c) {
+            int a = pr[c][0], b = pr[c][1];
+            double tr_, ti_;
+            if (a == b) { tr_ = kv[a] * uu[a].re; ti_ = kv[a] * uu[a].im; }
+            else {
+                tr_ = 0.5 * (kv[a] * uu[b].re + kv[b] * uu[a].re);
+                ti_ = 0.5 * (kv[a] * uu[b].im + kv[b] * uu[a].im);
+            }
+            e[c][idx].re = rf(s, -ti_);
+            e[c][idx].im = rf(s, tr_);
+        }
+    KLOOP_END
+}
+
+static void elastic_fwd(pfo_state *s, double *r, cpx *k) {
+    fwd(s, r, k);
+    if (s->fp32e) {
+        for (size_t i = 0; i < s->Nk; ++i) { k[i].re = (double)(float)k[i].re; k[i].im = (double)(float)k[i].im; }
+    }
+}
+static void elastic_inv(pfo_state *s, const cpx *k, double *r) {
+    inv(s, k, r);
+    if (s->fp32e) for (size_t i = 0; i < s->N; ++i) r[i] = (double)(float)r[i];
+}
+
+static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
+    const pfgb_params *P = &s->p;
+    elast_consts ec;
+    for (int c = 0; c < 21; ++c) { ec.S[c] = rf(s, P->S[c]); ec.Sp[c] = rf(s, P->S_p[c]); }
+    for (int c = 0; c < 6; ++c) { ec.e00[c] = rf(s, P->eps00[c]); ec.E0[c] = rf(s, P->E0[c]); }
+    const double invNf = rf(s, s->invN);
+    const int gp_el = s->gp && P->gp_elastic_enabled;
+    const int accel = P->elastic_enabled && (P->elastic_warm_start_enabled || P->elastic_residual_control_enabled);
+    const int warm_used = accel && s->warm_valid;
+
+    if (!warm_used) {
+        /* eigenstrain -> R2C -> homogeneous displacement (:28813-28868) */
+        RLOOP_BEGIN(s)
+            double e0[6];
+            eigen_point(s, &ec, s->phi[idx], s->eta[idx], o_clamp01(s->xB[idx]), gp_el, e0);
+            for (int c = 0; c < 6; ++c) s->eps_r[c][idx] = e0[c];
+        RLOOP_END
+        for (int c = 0; c < 6; ++c) { elastic_fwd(s, s->eps_r[c], s->eps_k[c]); dealias(s, s->eps_k[c]); }
+        green_apply(s, &ec, s->eps_k, 1, s->u_k);
+        for (int c = 0; c < 3; ++c) dealias(s, s->u_k[c]);
+    }
+
+    int iter = accel ? 0 : 1;
+    int conv = accel ? 0 : 1;
+    double rel = NAN;
+    for (;;) {
+        strain_from_u(s, s->u_k, s->eps_k);
+        for (int c = 0; c < 6; ++c) dealias(s, s->eps_k[c]);
+        for (int c = 0; c < 6; ++c) elastic_inv(s, s->eps_k[c], s->eps_r[c]);
+        /* normalize_strain_kernel (float invN) */
+        for (int c = 0; c < 6; ++c) {
+            double *e = s->eps_r[c];
+            RLOOP_BEGIN(s) e[idx] = rf(s, e[idx] * invNf); RLOOP_END
+        }
+        /* compute_strain_with_perturbation_kernel, cuda_kernels.cu:7002-7157:
+         * h = C0:eps - (C0 + h dC):(eps + E0 - eps0) */
+        RLOOP_BEGIN(s)
+            double e[6], e0[6];
+            for (int c = 0; c < 6; ++c) e[c] = s->eps_r[c][idx];
+            eigen_point(s, &ec, s->phi[idx], s->eta[idx], o_clamp01(s->xB[idx]), gp_el, e0);
+            double hw = o_h(s->phi[idx]);   /* stiffness_beta_weight_point */
+            double ev[6], tv[6];
+            double tot[6];
+            for (int c = 0; c < 6; ++c) tot[c] = e[c] + ec.E0[c] - e0[c];
+            eng(e, ev); eng(tot, tv);
+            static const int rowv[6] = {1, 2, 3, 4, 5, 6};
+            for (int c = 0; c < 6; ++c) {
+                double acc = 0.0;
+                for (int b = 0; b < 6; ++b) {
+                    double c0 = voigt(ec.S, rowv[c], b + 1);
+                    double ce = c0 + rf(s, hw * voigt(ec.Sp, rowv[c], b + 1));
+                    acc += c0 * ev[b] - ce * tv[b];
+                }
+                s->eps_r[c][idx] = rf(s, acc);
+            }
+        RLOOP_END
+        for (int c = 0; c < 6; ++c) { elastic_fwd(s, s->eps_r[c], s->eps_k[c]); dealias(s, s->eps_k[c]); }
+        cpx **target = accel ? s->u_next : s->u_k;
+        green_apply(s, &ec, s->eps_k, 0, target);
+        for (int c = 0; c < 3; ++c) dealias(s, target[c]);
+        if (accel) {
+            /* compute_elastic_displacement_residual_kernel, :6436-6467 */
+            double *dif = s->mass_t, *ref = s->der_t;
+            /* residual arrays sized Nk <= N */
+            KLOOP_BEGIN(s)
+                double w = (kk_ == 0 || ((s->Nz % 2) == 0 && kk_ == s->Nz / 2)) ? 1.0 : 2.0;
+                double ld = 0.0, lr = 0.0;
+                for (int c = 0; c < 3; ++c) {
+                    double dr = s->u_next[c][idx].re - s->u_k[c][idx].re;
+                    double di = s->u_next[c][idx].im - s->u_k[c][idx].im;
+                    double nr = s->u_next[c][idx].re, ni = s->u_next[c][idx].im;
+                    ld += dr * dr + di * di;
+                    lr += nr * nr + ni * ni;
+                }
+                dif[idx] = w * ld; ref[idx] = w * lr;
+            KLOOP_END
+            double ds = dsum(dif, s->Nk), rs = dsum(ref, s->Nk);
+            if (!isfinite(ds) || !isfinite(rs) || ds < 0.0 || rs < 0.0) return PFGB_ERR_NONFINITE;
+            rel = sqrt(ds / fmax(rs, P->elastic_residual_absolute_floor));
+            for (int c = 0; c < 3; ++c) { cpx *t = s->u_k[c]; s->u_k[c] = s->u_next[c]; s->u_next[c] = t; }
+            ++iter;
+            if (iter >= P->elastic_iter_min && rel <= P->elastic_residual_tolerance) { conv = 1; break; }
+            if (iter >= P->elastic_iter_max) break;
+        } else {
+            ++iter;
+            if (iter >= P->elastic_iter_max) break;
+        }
+    }
+    if (accel) s->warm_valid = 1;
+    if (st) {
+        st->elastic_iterations = iter;
+        st->elastic_converged = conv;
+        st->elastic_warm_start_used = warm_used;
+        st->elastic_relative_residual = rel;
+        st->elastic_iterations_total += iter;
+    }
+    if (accel && !conv && P->elastic_fail_on_nonconvergence) return PFGB_ERR_NONCONVERGED;
+
+    /* finalize (:29104-29160): strain from u, C2R, normalize, +E0, stress */
+    strain_from_u(s, s->u_k, s->eps_k);
+    for (int c = 0; c < 6; ++c) dealias(s, s->eps_k[c]);
+    for (int c = 0; c < 6; ++c) elastic_inv(s, s->eps_k[c], s->eps_r[c]);
+    for (int c = 0; c < 6; ++c) {
+        double *e = s->eps_r[c];
+        const double E0c = ec.E0[c];
+        RLOOP_BEGIN(s) e[idx] = rf(s, rf(s, e[idx] * invNf) + E0c); RLOOP_END
+    }
+    /* compute_stress_from_strain_with_effective_stiffness_kernel, :7381-7480 */
+    RLOOP_BEGIN(s)
+        double e0[6], el[6], ev[6];
+        eigen_point(s, &ec, s->phi[idx], s->eta[idx], o_clamp01(s->xB[idx]), gp_el, e0);
+        for (int c = 0; c < 6; ++c) el[c] = rf(s, s->eps_r[c][idx] - e0[c]);
+        eng(el, ev);
+        double hw = o_h(s->phi[idx]);
+        for (int c = 0; c < 6; ++c) {
+            double acc = 0.0;
+            for (int b = 0; b < 6; ++b) {
+                double ce = voigt(ec.S, c + 1, b + 1) + rf(s, hw * voigt(ec.Sp, c + 1, b + 1));
+                acc += ce * ev[b];
+            }
+            s->sig_r[c][idx] = rf(s, acc);
+        }
+    RLOOP_END
+    return PFGB_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* phi RHS — compute_phi_rhs_kernel, cuda_kernels.cu:390-555            */
+/* ------------------------------------------------------------------ */
+static void phi_rhs(pfo_state *s, int coupling) {
+    const pfgb_params *P = &s->p;
+    const double T = P->temperature_K, sc = P->mu_reference_scale;
+    const int cv = P->thermo_convex_extrapolation_enabled;
+    const double shift = coupling ? P->elastic_shift_dimless : 0.0;
+    double e00f[6];
+    for (int c = 0; c < 6; ++c) e00f[c] = rf(s, P->eps00[c]);
+    RLOOP_BEGIN(s)
+        double phi = s->phi[idx];
+        double hp = o_hp(phi), gp = o_gp(phi), h = o_h(phi);
+        double xB = o_clamp01(s->xB[idx]);
+        double f = P->W * gp;
+        double muA = o_muA(xB, T, sc, cv), muB = o_muB(xB, T, sc, cv);
+        double dmu = P->mu0_compound - P->v_A * muA - P->v_B * muB - shift;
+        double cb = o_c_xB_phi(xB, P->Vm_alpha_0, P->dVm_alpha_dxB, P->Vm_compound, h);
+        double mt = o_mu_tot_mix(muA, muB, xB, P->mu0_compound, h);
+        double Vma = o_Vm_alpha(xB, P->Vm_alpha_0, P->dVm_alpha_dxB);
+        double vt = P->Vm_compound - Vma + P->dVm_alpha_dxB * (xB - P->v_B);
+        f += cb * hp * (dmu - cb * mt * vt);
+        if (coupling) {
+            double sg[6];
+            for (int c = 0; c < 6; ++c) sg[c] = s->sig_r[c][idx];
+            double epsc = xB * P->eps_iso_over_vB;
+            double diag = -epsc + P->eps_iso_over_vB * (xB - P->v_B);
+            double de[6];
+            for (int c = 0; c < 3; ++c) de[c] = hp * (P->eps00[c] + diag);
+            for (int c = 3; c < 6; ++c) de[c] = hp * P->eps00[c];
+            double dg = -(sg[0] * de[0] + sg[1] * de[1] + sg[2] * de[2]
+                          + 2.0 * sg[5] * de[5] + 2.0 * sg[4] * de[4] + 2.0 * sg[3] * de[3]);
+            /* eigenstrain_phi_xB_point with float eps00, stored as float */
+            double e0[6];
+            double omh = 1.0 - h, ec_ = xB * P->eps_iso_over_vB;
+            for (int c = 0; c < 3; ++c) e0[c] = rf(s, omh * ec_ + h * e00f[c]);
+            for (int c = 3; c < 6; ++c) e0[c] = rf(s, h * e00f[c]);
+            double el[6], ev[6];
+            for (int c = 0; c < 6; ++c) el[c] = s->eps_r[c][idx] - e0[c];
+            eng(el, ev);
+            double Q = 0.0;  /* compute_Q_voigt, :162-181 */
+            for (int a = 0; a < 6; ++a)
+                for (int b = 0; b < 6; ++b) Q += voigt(P->S_p, a + 1, b + 1) * ev[a] * ev[b];
+            f += dg + 0.5 * hp * Q;
+        }
+        s->rhs[idx] = f;
+    RLOOP_END
+}
+
+/* compute_eta_rhs_kernel (non-raw-drive branch), cuda_kernels.cu:845-946 */
+static void eta_rhs(pfo_state *s) {
+    const pfgb_params *P = &s->p;
+    const double T = P->temperature_K, sc = P->mu_reference_scale;
+    const int cv = P->thermo_convex_extrapolation_enabled;
+    const double xg = o_clamp_eps(P->gp_xB_fixed, 1.0e-12);
+    const double g_gp = (1.0 - xg) * o_muA(xg, T, sc, cv) + xg * o_muB(xg, T, sc, cv) - P->gp_delta_g0;
+    RLOOP_BEGIN(s)
+        double eta = o_clamp01(s->eta[idx]);
+        double phi = o_clamp01(s->phi[idx]);
+        double xa = o_clamp_eps(s->xB[idx], 1.0e-12);
+        double hphi = o_h(phi), hpe = o_hp(eta), gpe = o_gp(eta);
+        double cref = 1.0 / o_Vm_alpha(xa, P->Vm_alpha_0, P->dVm_alpha_dxB);
+        double ga = (1.0 - xa) * o_muA(xa, T, sc, cv) + xa * o_muB(xa, T, sc, cv);
+        double d = cref * (1.0 - hphi) * hpe * (g_gp - ga);
+        double el = 0.0;
+        if (P->gp_elastic_enabled && P->gp_elastic_active_eta) {
+            /* compute_dgel_deta_gp_point, cuda_kernels.cu:292-311 */
+            double sh = s->sig_r[0][idx] + s->sig_r[1][idx] + s->sig_r[2][idx];
+            double pre = (1.0 - o_h(phi)) * o_hp(eta);
+            double ea = o_clamp01(xa) * P->eps_iso_over_vB;
+            el = P->gp_elastic_derivative_scale * (-sh * (pre * (P->gp_eps_iso - ea)));
+        }
+        s->rhs[idx] = d + P->gp_W_eta * gpe + el;
+    RLOOP_END
+}
+
+/* ------------------------------------------------------------------ */
+/* zero mode — run_pf_conserved_y_zero_mode_host, main_cuda.cu:4269-4405 */
+/* ------------------------------------------------------------------ */
+static int zero_mode(pfo_state *s, const double *Ystar, double Y_upper_cap, pfgb_step_stats *st) {
+    const pfgb_params *P = &s->p;
+    double ymin = 1e300, ymax = -1e300;
+    for (size_t i = 0; i < s->N; ++i) { if (Ystar[i] < ymin) ymin = Ystar[i]; if (Ystar[i] > ymax) ymax = Ystar[i]; }
+    if (!isfinite(ymin) || !isfinite(ymax)) return PFGB_ERR_ZERO_MODE;
+    double lo = -P->Y_clip - ymin, hi = Y_upper_cap - ymax;
+    double rnd = 128.0 * DBL_EPSILON * fmax(fmax(fabs(lo), fabs(hi)), 1.0);
+    if (!isfinite(lo) || !isfinite(hi) || lo > hi + rnd) return PFGB_ERR_ZERO_MODE;
+    const double target = s->target_mass;
+    const double tol = P->zero_mode_tolerance_relative * fmax(fabs(target), 1.0);
+#define ZM_EVAL(lam, M, D)                                                    \
+    do {                                                                      \
+        const double lam_ = (lam);                                            \
+        RLOOP_BEGIN(s)                                                        \
+            double h = o_h(s->phi[idx]);                                      \
+            double a = 1.0 - h;                                               \
+            double x = o_sigmoid_raw(Ystar[idx] + lam_);                      \
+            s->mass_t[idx] = a * x + h * P->v_B;                              \
+            s->der_t[idx] = a * x * (1.0 - x);                                \
+        RLOOP_END                                                             \
+        (M) = dsum(s->mass_t, s->N);                                          \
+        (D) = dsum(s->der_t, s->N);                                           \
+    } while (0)
+    double mlo, dlo, mhi, dhi;
+    ZM_EVAL(lo, mlo, dlo);
+    ZM_EVAL(hi, mhi, dhi);
+    if (!isfinite(mlo) || !isfinite(mhi)) return PFGB_ERR_ZERO_MODE;
+    if (mlo - target > tol || mhi - target < -tol) return PFGB_ERR_ZERO_MODE;
+    double lam = fmin(fmax(0.0, lo), hi), mass, der;
+    ZM_EVAL(lam, mass, der);
+    double res = mass - target;
+    int iters = 0, nwt = 0, bis = 0;
+    for (int it = 0; it < P->zero_mode_max_iterations && fabs(res) > tol; ++it) {
+        if (res < 0.0) lo = lam; else hi = lam;
+        double cand = NAN;
+        if (der > 0.0 && isfinite(der)) cand = lam - res / der;
+        if (isfinite(cand) && cand > lo && cand < hi) ++nwt;
+        else { cand = 0.5 * (lo + hi); ++bis; }
+        lam = cand;
+        ZM_EVAL(lam, mass, der);
+        if (!isfinite(mass) || !isfinite(der)) return PFGB_ERR_ZERO_MODE;
+        res = mass - target;
+        iters = it + 1;
+    }
+#undef ZM_EVAL
+    if (fabs(res) > tol) return PFGB_ERR_ZERO_MODE;
+    for (size_t i = 0; i < s->N; ++i) {
+        double y = Ystar[i] + lam;
+        if (!isfinite(y) || y < -P->Y_clip || y > Y_upper_cap) return PFGB_ERR_ZERO_MODE;
+    }
+    RLOOP_BEGIN(s)
+        double y = Ystar[idx] + lam;
+        s->Y[idx] = y;
+        s->xB[idx] = o_sigmoid_raw(y);
+    RLOOP_END
+    if (st) {
+        st->zero_mode_iterations = iters;
+        st->zero_mode_newton_steps = nwt;
+        st->zero_mode_bisection_steps = bis;
+        st->zero_mode_lambda = lam;
+        st->zero_mode_residual = res;
+        st->zero_mode_target_mass = target;
+    }
+    return PFGB_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* one dynamics step — main_cuda.cu:28427-31623                        */
+/* ------------------------------------------------------------------ */
+static int step_once(pfo_state *s, pfgb_step_stats *st) {
+    pfgb_params *P = &s->p;
+    const double T = P->temperature_K, sc = P->mu_reference_scale;
+    const int cv = P->thermo_convex_extrapolation_enabled;
+    const double dt = P->dt;
+    memcpy(s->phi_n, s->phi, sizeof(double) * s->N);
+    memcpy(s->eta_prev, s->eta, sizeof(double) * s->N);
+    memcpy(s->Y_n, s->Y, sizeof(double) * s->N);
+
+    const int gp_el = s->gp && P->gp_elastic_enabled;
+    const int coupling = P->elastic_enabled && (!gp_el || P->gp_elastic_active_phi);
+    if (P->elastic_enabled) {
+        int rc = elastic_solve(s, st);
+        if (rc != PFGB_OK) return rc;
+    }
+
+    /* phi update, :29752-29860 */
+    fwd(s, s->phi, s->phi_k); dealias(s, s->phi_k);
+    phi_rhs(s, coupling);
+    fwd(s, s->rhs, s->rhs_k); dealias(s, s->rhs_k);
+    {
+        const double Ldt = P->L_phi * dt;
+        KLOOP_BEGIN(s)
+            double den = 1.0 + Ldt * P->kappa_phi * k2_at(s, ii_, jj_, kk_);
+            cpx a = s->phi_k[idx], r = s->rhs_k[idx];
+            s->phi_k[idx].re = (a.re - Ldt * r.re) / den;
+            s->phi_k[idx].im = (a.im - Ldt * r.im) / den;
+        KLOOP_END
+    }
+    dealias(s, s->phi_k);
+    inv(s, s->phi_k, s->phi);
+    RLOOP_BEGIN(s)   /* phi_normalize_and_clamp_kernel, cuda_kernels.cu:1071-1084 */
+        double v = s->phi[idx] * s->invN;
+        if (v < -1e-6) v = -1e-6;
+        if (v > 1.0 + 1e-6) v = 1.0 + 1e-6;
+        s->phi[idx] = v;
+    RLOOP_END
+
+    /* eta update (gp_zone), :29948-30006 */
+    if (s->gp) {
+        fwd(s, s->eta, s->eta_k); dealias(s, s->eta_k);
+        eta_rhs(s);
+        fwd(s, s->rhs, s->rhs_k); dealias(s, s->rhs_k);
+        const double Ldt = P->gp_L_eta * dt;
+        KLOOP_BEGIN(s)
+            double den = 1.0 + Ldt * P->gp_kappa_eta * k2_at(s, ii_, jj_, kk_);
+            cpx a = s->eta_k[idx], r = s->rhs_k[idx];
+            s->eta_k[idx].re = (a.re - Ldt * r.re) / den;
+            s->eta_k[idx].im = (a.im - Ldt * r.im) / den;
+        KLOOP_END
+        dealias(s, s->eta_k);
+        inv(s, s->eta_k, s->eta);
+        RLOOP_BEGIN(s)
+            double v = s->eta[idx] * s->invN;
+            s->eta[idx] = v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
+        RLOOP_END
+    }
+
+    /* Y update, :30280-30800 */
+    const int zm = P->zero_mode_enabled;
+    const double *phiY = zm ? s->phi_n : (P->enable_Y_rhs_previous_time_level ? s->phi_n : s->phi);
+    const double *etaY = s->eta;
+    RLOOP_BEGIN(s)
+        double Yv = s->Y[idx];
+        double xB = o_sigmoid(Yv, P->Y_clip, P->xB_eps);
+        s->xB[idx] = xB;
+        double muA = o_muA(xB, T, sc, cv), muB = o_muB(xB, T, sc, cv);
+        double mu;
+        if (s->gp) {   /* compute_mu_C_gp_kernel, :1326-1366 */
+            double cref = 1.0 / o_Vm_alpha(xB, P->Vm_alpha_0, P->dVm_alpha_dxB);
+            mu = cref * (muB - muA);
+        } else {       /* compute_mu_x_kernel, :1266-1324 */
+            double h = o_h(phiY[idx]);
+            double cb = o_c_xB_phi(xB, P->Vm_alpha_0, P->dVm_alpha_dxB, P->Vm_compound, h);
+            double mt = o_mu_tot_mix(muA, muB, xB, P->mu0_compound, h);
+            mu = cb * (muB - muA - cb * mt * P->dVm_alpha_dxB);
+        }
+        if (P->elastic_enabled) {
+            double sh = s->sig_r[0][idx] + s->sig_r[1][idx] + s->sig_r[2][idx];
+            mu += -P->eps_iso_over_vB * sh;
+        }
+        s->mu[idx] = mu;
+    RLOOP_END
+    fwd(s, s->mu, s->mu_k); dealias(s, s->mu_k);
+    memset(s->divJ_k, 0, sizeof(cpx) * s->Nk);
+    memcpy(s->xB_prev, s->xB, sizeof(double) * s->N);
+    for (int a = 0; a < 3; ++a) {
+        KLOOP_BEGIN(s)   /* compute_gradient_single_component_k_kernel, :1887 */
+            double ka = a == 0 ? s->kx[ii_] : (a == 1 ? s->ky[jj_] : s->kz[kk_]);
+            cpx f = s->mu_k[idx];
+            s->scr_k[idx].re = -ka * f.im;
+            s->scr_k[idx].im = ka * f.re;
+        KLOOP_END
+        dealias(s, s->scr_k);
+        inv(s, s->scr_k, s->scr);
+        RLOOP_BEGIN(s)
+            double g = s->scr[idx] * s->invN;
+            double M;
+            if (s->gp) {   /* compute_flux_single_component_gp_kernel, :2039 */
+                double hb = o_h(phiY[idx]), he = o_h(etaY[idx]);
+                double hg = (1.0 - hb) * he, ha = (1.0 - hb) * (1.0 - he);
+                double Ga = o_gamma(s->xB_prev[idx], 0.0, P->Vm_alpha_0, P->dVm_alpha_dxB,
+                                    P->Vm_compound, T, sc, cv);
+                double Ma = o_meff(P->D_alpha, Ga);
+                M = ha * Ma + hg * P->gp_M_GP + hb * P->gp_M_beta;
+            } else {       /* compute_flux_single_component_kernel, :1985 */
+                double h = o_h(phiY[idx]);
+                double Dm = o_Dmix(h, P->D_alpha, P->D_compound);
+                double G = o_gamma(s->xB_prev[idx], h, P->Vm_alpha_0, P->dVm_alpha_dxB,
+                                   P->Vm_compound, T, sc, cv);
+                M = o_meff(Dm, G);
+            }
+            s->scr[idx] = M * g;
+        RLOOP_END
+        fwd(s, s->scr, s->scr_k); dealias(s, s->scr_k);
+        KLOOP_BEGIN(s)   /* divJ_accumulate_kernel, :2112 */
+            double ka = a == 0 ? s->kx[ii_] : (a == 1 ? s->ky[jj_] : s->kz[kk_]);
+            cpx J = s->scr_k[idx];
+            s->divJ_k[idx].re += -ka * J.im;
+            s->divJ_k[idx].im += ka * J.re;
+        KLOOP_END
+    }
+    dealias(s, s->divJ_k);
+    inv(s, s->divJ_k, s->divJ);
+    RLOOP_BEGIN(s) s->divJ[idx] *= s->invN; RLOOP_END
+    /* Laplacian of Y, :30572-30581 */
+    fwd(s, s->Y, s->Y_k); dealias(s, s->Y_k);
+    KLOOP_BEGIN(s)
+        double k2 = k2_at(s, ii_, jj_, kk_);
+        s->Y_k[idx].re *= -k2; s->Y_k[idx].im *= -k2;
+    KLOOP_END
+    dealias(s, s->Y_k);
+    inv(s, s->Y_k, s->lapY);
+    RLOOP_BEGIN(s) s->lapY[idx] *= s->invN; RLOOP_END
+    /* mean_DY, reduce_sum_DY_kernel :3870 */
+    RLOOP_BEGIN(s)
+        double h = o_h(phiY[idx]);
+        double Dm = o_Dmix(h, P->D_alpha, P->D_compound);
+        double x = o_sigmoid_raw(s->Y[idx]);
+        if (x < 1e-12) x = 1e-12;
+        if (x > 1.0 - 1e-12) x = 1.0 - 1e-12;
+        s->mass_t[idx] = Dm * x * (1.0 - x);
+    RLOOP_END
+    const double mean_DY = dsum(s->mass_t, s->N) / (double)s->N;
+    if (st) st->mean_DY = mean_DY;
+    /* Y^n in k space (stored in divJ_k like the reference) */
+    fwd(s, s->Y_n, s->divJ_k); dealias(s, s->divJ_k);
+    RLOOP_BEGIN(s)
+        double Yv = s->Y[idx];
+        double x = o_sigmoid_raw(Yv);
+        if (x < 1e-12) x = 1e-12;
+        if (x > 1.0 - 1e-12) x = 1.0 - 1e-12;
+        double ld = x * (1.0 - x);
+        double dYdt = s->dYdt[idx];
+        double f;
+        if (zm) {   /* compute_Y_rhs_sm_tangent_n_kernel, :2268-2359 */
+            double pn = s->phi_n[idx], pp = s->phi[idx];
+            double hn = o_h(pn), hpn = o_hp(pn);
+            double th = hpn * ((pp - pn) / dt) * (P->v_B - x);
+            double gl = (1.0 - hn) * ld - 1.0;
+            f = s->divJ[idx] - th - mean_DY * s->lapY[idx] - gl * dYdt;
+        } else {    /* compute_Y_rhs_kernel, :2185-2266 */
+            double hn = o_h(s->phi[idx]), ho = o_h(s->phi_n[idx]);
+            double dhdt = (hn - ho) / dt;
+            double th = P->Y_rhs_term_h_scale * dhdt * (P->v_B - x);
+            double hx = P->enable_Y_rhs_previous_time_level ? ho : hn;
+            double gl = (1.0 - hx) * ld - 1.0;
+            double tg = P->disable_Y_rhs_gamma_term ? 0.0 : gl * dYdt;
+            f = s->divJ[idx] + (-th - mean_DY * s->lapY[idx] - tg);
+        }
+        s->rhs[idx] = f;
+    RLOOP_END
+    fwd(s, s->rhs, s->rhs_k); dealias(s, s->rhs_k);
+    KLOOP_BEGIN(s)   /* Y_semi_implicit_update_kernel, :2528-2550 */
+        double den = 1.0 + dt * mean_DY * k2_at(s, ii_, jj_, kk_);
+        cpx a = s->divJ_k[idx], r = s->rhs_k[idx];
+        s->Y_k[idx].re = (a.re + dt * r.re) / den;
+        s->Y_k[idx].im = (a.im + dt * r.im) / den;
+    KLOOP_END
+    dealias(s, s->Y_k);
+    inv(s, s->Y_k, s->Y);
+    const double Ycap = P->Y_clip;
+    if (zm) {
+        RLOOP_BEGIN(s) s->scr[idx] = s->Y[idx] * s->invN; RLOOP_END
+        int rc = zero_mode(s, s->scr, Ycap, st);
+        if (rc != PFGB_OK) return rc;
+    } else {
+        RLOOP_BEGIN(s)   /* Y_normalize_and_clamp_kernel, :2554-2572 */
+            double y = s->Y[idx] * s->invN;
+            if (y > Ycap) y = Ycap;
+            if (y < -P->Y_clip) y = -P->Y_clip;
+            s->Y[idx] = y;
+            s->xB[idx] = o_sigmoid(y, P->Y_clip, P->xB_eps);
+        RLOOP_END
+    }
+    /* update_dY_dt_prev_kernel, :3545 */
+    RLOOP_BEGIN(s) s->dYdt[idx] = (s->Y[idx] - s->Y_n[idx]) / dt; RLOOP_END
+    s->step++;
+    return PFGB_OK;
+}
+
+int pfo_load_fields(pfo_state *s, const double *phi, const double *xB, const double *eta,
+                    const double *dYdt) {
+    const pfgb_params *P = &s->p;
+    memcpy(s->phi, phi, sizeof(double) * s->N);
+    memcpy(s->xB, xB, sizeof(double) * s->N);
+    if (eta) memcpy(s->eta, eta, sizeof(double) * s->N); else memset(s->eta, 0, sizeof(double) * s->N);
+    if (dYdt) memcpy(s->dYdt, dYdt, sizeof(double) * s->N); else memset(s->dYdt, 0, sizeof(double) * s->N);
+    for (size_t i = 0; i < s->N; ++i) s->Y[i] = o_logit(s->xB[i], P->xB_eps, P->Y_clip);
+    s->warm_valid = 0;
+    s->step = 0;
+    /* gpu_reduce_sum_xBtot, main_cuda.cu:28079-28086 */
+    RLOOP_BEGIN(s)
+        double h = o_h(s->phi[idx]);
+        s->mass_t[idx] = (1.0 - h) * s->xB[idx] + P->v_B * h;
+    RLOOP_END
+    s->target_mass = dsum(s->mass_t, s->N);
+    for (int c = 0; c < 6; ++c) {
+        memset(s->sig_r[c], 0, sizeof(double) * s->N);
+        memset(s->eps_r[c], 0, sizeof(double) * s->N);
+    }
+    return PFGB_OK;
+}
+
+int pfo_step(pfo_state *s, int nsteps, pfgb_step_stats *st) {
+    if (st) memset(st, 0, sizeof(*st));
+    for (int i = 0; i < nsteps; ++i) {
+        int rc = step_once(s, st);
+        if (rc != PFGB_OK) return rc;
+    }
+    if (st) st->step = s->step;
+    return PFGB_OK;
+}
+
+int pfo_read_fields(const pfo_state *s, double *phi, double *xB, double *Y, double *eta,
+                    double *dYdt) {
+    const size_t b = sizeof(double) * s->N;
+    if (phi) memcpy(phi, s->phi, b);
+    if (xB) memcpy(xB, s->xB, b);
+    if (Y) memcpy(Y, s->Y, b);
+    if (eta) memcpy(eta, s->eta, b);
+    if (dYdt) memcpy(dYdt, s->dYdt, b);
+    return PFGB_OK;
+}
+
+int pfo_read_elastic(const pfo_state *s, double *sigma6, double *strain6) {
+    for (int c = 0; c < 6; ++c) {
+        if (sigma6) memcpy(sigma6 + (size_t)c * s->N, s->sig_r[c], sizeof(double) * s->N);
+        if (strain6) memcpy(strain6 + (size_t)c * s->N, s->eps_r[c], sizeof(double) * s->N);
+    }
+    return PFGB_OK;
+}
+
+int pfo_read_displacement_k(const pfo_state *s, double *u3) {
+    for (int c = 0; c < 3; ++c) memcpy(u3 + (size_t)c * 2 * s->Nk, s->u_k[c], sizeof(cpx) * s->Nk);
+    return PFGB_OK;
+}
+
+int pfo_diagnostics(const pfo_state *s, pfgb_diag *d) {
+    const pfgb_params *P = &s->p;
+    double *t = (double *)malloc(sizeof(double) * s->N);
+    double *u = (double *)malloc(sizeof(double) * s->N);
+    double *w = (double *)malloc(sizeof(double) * s->N);
+    double pmin = 1e300, pmax = -1e300, xmin = 1e300, xmax = -1e300;
+    for (size_t i = 0; i < s->N; ++i) {
+        double h = o_h(o_clamp01(s->phi[i]));
+        t[i] = h;
+        double hh = o_h(s->phi[i]);
+        u[i] = (1.0 - hh) * s->xB[i] + P->v_B * hh;
+        w[i] = s->phi[i] >= 0.5 ? 1.0 : 0.0;
+        if (s->phi[i] < pmin) pmin = s->phi[i];
+        if (s->phi[i] > pmax) pmax = s->phi[i];
+        if (s->xB[i] < xmin) xmin = s->xB[i];
+        if (s->xB[i] > xmax) xmax = s->xB[i];
+    }
+    d->vf_precip = dsum(t, s->N) / (double)s->N;
+    d->mass_xBtot = dsum(u, s->N);
+    d->mean_xB = dsum(s->xB, s->N) / (double)s->N;
+    d->n_in = dsum(w, s->N);
+    d->phi_min = pmin; d->phi_max = pmax; d->xB_min = xmin; d->xB_max = xmax;
+    free(t); free(u); free(w);
+    return PFGB_OK;
+}

@@ -1,0 +1,72 @@
+/*
+ * pf_oracle.h — CPU FP64 restatement of the CUDA_STO_PF time step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker for the CUDA library in
+ * cuda_sto_pf_gb300/: tests, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg may call it; the product path never does.
+ *
+ * It follows the reference driver sequence literally (main_cuda.cu:
+ * 28427-31623): every dealias pass, clamp and normalisation in the order the
+ * reference issues them, with the FFTs done by our own mixed-radix FP64
+ * transform (the reference uses cuFFT, an un-vendored NVIDIA library; its
+ * transform is the textbook unnormalised DFT, which this restates).
+ *
+ * Parity pinning: the thermodynamics and phase functions are checked against
+ * the reference's own thermo_utils.h / phase_functions.h compiled on the
+ * host (oracle/build_ref.sh -> oracle/_ref/libpfref.so) and against golden
+ * vectors generated from them (tests/golden/).  The step as a whole is pinned
+ * by known-answer tests (Fourier-mode decay, homogeneous Eshelby field,
+ * exact mass conservation); the reference has no CPU time step and ships no
+ * golden fields, so whole-step parity with main_cuda itself is unpinned.
+ */
+#ifndef PF_ORACLE_H
+#define PF_ORACLE_H
+
+#include "../include/pfgb.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pfo_state pfo_state;
+
+/* derived thermo (pfparams_refresh_thermo, main_cuda.cu:15603-15613) */
+void pfo_params_finalize(pfgb_params *p);
+
+pfo_state *pfo_create(const pfgb_params *p);
+void pfo_destroy(pfo_state *s);
+int pfo_load_fields(pfo_state *s, const double *phi, const double *xB,
+                    const double *eta, const double *dYdt_prev);
+/* returns a pfgb_status code */
+int pfo_step(pfo_state *s, int nsteps, pfgb_step_stats *stats);
+int pfo_read_fields(const pfo_state *s, double *phi, double *xB, double *Y,
+                    double *eta, double *dYdt_prev);
+int pfo_read_elastic(const pfo_state *s, double *sigma6, double *strain6);
+int pfo_read_displacement_k(const pfo_state *s, double *u3);
+int pfo_diagnostics(const pfo_state *s, pfgb_diag *d);
+int pfo_set_threads(int n);
+
+/* FP64 3D transforms, cuFFT D2Z/Z2D conventions (unnormalised). */
+void pfo_fft3d_r2c(int Nx, int Ny, int Nz, const double *in, double *out);
+void pfo_fft3d_c2r(int Nx, int Ny, int Nz, const double *in, double *out);
+/* 1D complex transform (sign=-1 forward), for FFT self-tests. */
+void pfo_fft1d(int n, int sign, const double *in, double *out);
+
+/* pointwise functions, exposed so tests can pin them against the
+ * reference headers and golden vectors */
+double pfo_h(double phi);
+double pfo_hp(double phi);
+double pfo_gp(double phi);
+double pfo_mu_A(double xB, double T_K, double scale, int convex);
+double pfo_mu_B(double xB, double T_K, double scale, int convex);
+double pfo_gamma(double xB, double h, double Vm0, double dVm, double Vmc,
+                 double T_K, double scale, int convex);
+double pfo_xB_eq(double T_K);
+double pfo_sigmoid(double Y, double Y_clip, double eps);
+double pfo_logit(double xB, double eps, double Y_clip);
+double pfo_meff(double Dm, double gamma);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

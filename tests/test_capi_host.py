@@ -1,0 +1,112 @@
+"""C-ABI library: loads without a GPU, exports every declared entry point,
+and its host-side logic (defaults, parameter files, derived thermo, raw-field
+preparation) matches the reference rules.  No device compute here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, REPO
+
+
+def declared_functions():
+    src = open(os.path.join(REPO, "include", "pfgb.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pfgb_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_every_declared_symbol_is_exported(capi):
+    lib = capi.load()
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    # and the ctypes binding covers the whole header
+    assert sorted(n for n, _, _ in capi.EXPORTS) == names
+
+
+def test_params_struct_size(capi):
+    assert capi.load().pfgb_params_size() == ctypes.sizeof(capi.Params)
+
+
+def test_defaults_follow_reference(capi):
+    p = capi.default_params()
+    # params_default, main_cuda.cu:15781-16439
+    assert p.Y_clip == 20.0 and p.xB_eps == 1e-8 and p.dt == 1e-2
+    assert p.elastic_iter_max == 32 and p.elastic_iter_min == 2
+    assert p.elastic_residual_tolerance == 1e-6 and p.elastic_warm_start_enabled == 1
+    assert p.zero_mode_tolerance_relative == 1e-12 and p.zero_mode_max_iterations == 24
+    assert p.thermo_convex_extrapolation_enabled == 0 and p.Y_rhs_term_h_scale == 1.0
+    assert p.gp_xB_fixed == pytest.approx(0.3529411764705882)
+
+
+def test_load_param_file(capi):
+    p = capi.load_params_file(os.path.join(GOLDEN, "c2.params"))
+    assert p.D_alpha == pytest.approx(625.0) and p.kappa_phi == pytest.approx(3.125)
+    assert p.S[0] == pytest.approx(267.85714285714283) and p.S_p[0] == pytest.approx(-119.04761904761904)
+    assert p.eps00[0] == pytest.approx(0.046) and p.eps00[1] == pytest.approx(-0.022)
+    assert p.gp_W_eta == pytest.approx(1.4880952380952381)
+    assert p.pf_params_schema_version == 1
+
+
+def _write(tmp_path, text):
+    f = tmp_path / "x.params"
+    f.write_text(text)
+    return str(f)
+
+
+def test_missing_required_key_is_an_error(capi, tmp_path):
+    lines = [l for l in open(os.path.join(GOLDEN, "c1.params")) if not l.startswith("S_p_66")]
+    with pytest.raises(capi.PfgbError) as e:
+        capi.load_params_file(_write(tmp_path, "".join(lines)))
+    assert "S_p_" in str(e.value)
+
+
+def test_bad_number_is_an_error(capi, tmp_path):
+    txt = open(os.path.join(GOLDEN, "c1.params")).read().replace("W=1.0", "W=1.0x")
+    with pytest.raises(capi.PfgbError) as e:
+        capi.load_params_file(_write(tmp_path, txt))
+    assert "W" in str(e.value)
+
+
+def test_unknown_key_warns_and_is_ignored(capi, tmp_path, capfd):
+    txt = open(os.path.join(GOLDEN, "c1.params")).read() + "\nnot_a_key = 3 # comment\n"
+    p = capi.load_params_file(_write(tmp_path, txt))
+    assert p.W == 1.0
+    assert "unknown key ignored: not_a_key" in capfd.readouterr().err
+
+
+def test_finalize_matches_oracle(capi, oracle):
+    import oracle_py
+    p = capi.load_params_file(os.path.join(GOLDEN, "c2.params"))
+    capi.finalize(p)
+    q = capi.load_params_file(os.path.join(GOLDEN, "c2.params"))
+    oracle_py.lib().pfo_params_finalize(ctypes.byref(q))
+    assert p.temperature_K == q.temperature_K
+    assert p.xB_eq_matrix == q.xB_eq_matrix
+    assert p.mu0_compound == pytest.approx(q.mu0_compound, rel=1e-14)
+
+
+def test_prepare_raw_fields_rules(capi):
+    p = capi.default_params()
+    phi = np.array([-0.2, 0.5, 1.3])
+    xB = np.array([0.0, 0.5, 0.9])
+    eta = np.array([2.0, -1.0, 0.25])
+    st = capi.load().pfgb_prepare_raw_fields(ctypes.byref(p), 0.34, phi.ctypes.data, xB.ctypes.data,
+                                             eta.ctypes.data, None, 3)
+    assert st == 0
+    assert phi.tolist() == [0.0, 0.5, 1.0] and eta.tolist() == [1.0, 0.0, 0.25]
+    assert xB.tolist() == [1e-8, 0.34, 0.34]
+    bad = np.array([np.nan, 0, 0])
+    st = capi.load().pfgb_prepare_raw_fields(ctypes.byref(p), 0.34, bad.ctypes.data, xB.ctypes.data,
+                                             None, None, 3)
+    assert st == 6
+
+
+def test_create_rejects_bad_grid_without_touching_gpu(capi):
+    p = capi.default_params()
+    p.Nx = 0
+    ctx = ctypes.c_void_p()
+    assert capi.load().pfgb_create(ctypes.byref(p), 0, ctypes.byref(ctx)) == 1

@@ -1,0 +1,132 @@
+"""Parity of the CUDA time step with the CPU oracle, through the C ABI.
+
+FP64 fields: relative L2 <= 1e-6 (the elastic solve is FP32 on both sides,
+as in the reference).  FP32 fields: relative L2 <= 1e-5 (the stated bound for
+the FP32 path).  Small grids so the oracle finishes in seconds."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import params_for, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = {0: 1e-6, 1: 1e-5}
+
+
+def _inputs(capi, p, n, gp, seed=5, shape=None):
+    from cuda_sto_pf_gb300 import workloads
+    shape = shape or (n, n, n)
+    rng = np.random.default_rng(seed)
+    c = np.array(shape) / 2.0
+    phi = workloads.ellipsoid_field(shape, [c], [np.array([7.0, 6.0, 5.0])],
+                                    [workloads.random_rotation(rng)], p.ic_phi_iface_w)
+    xB = workloads.composition(phi, rng)
+    eta = None
+    if gp:
+        eta = workloads.ellipsoid_field(shape, [np.array([3.0, 3.0, 3.0])], [np.full(3, 3.0)], [np.eye(3)],
+                                        p.ic_phi_iface_w)
+    capi.load().pfgb_prepare_raw_fields(ctypes.byref(p), 0.07, phi.ctypes.data, xB.ctypes.data,
+                                        None if eta is None else eta.ctypes.data, None, phi.size)
+    return phi, xB, eta
+
+
+CASES = [
+    # (params file, zero mode, model, label)
+    ("c1.params", 0, 0, "homogeneous"),
+    ("c2.params", 0, 0, "heterogeneous"),
+    ("c2.params", 1, 0, "heterogeneous+zero_mode"),
+    ("c2.params", 1, 1, "gp_zone+zero_mode"),
+]
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("case", CASES, ids=[c[3] for c in CASES])
+def test_step_parity(capi, oracle, case, prec):
+    from cuda_sto_pf_gb300.solver import Solver
+    name, zm, mm, _ = case
+    n, steps = 32, 4
+    p = params_for(capi, name, n=n, zero_mode_enabled=zm, model_mode=mm, precision=prec)
+    phi, xB, eta = _inputs(capi, p, n, mm == 1)
+    o = oracle(p, threads=4)
+    o.load(phi, xB, eta)
+    so = capi.StepStats()
+    assert o.step(steps, so) == 0
+    with Solver(p) as s:
+        s.load(phi, xB, eta)
+        sg = s.step(steps)
+        fg = s.fields()
+        eg = s.elastic()
+    fo = o.fields()
+    eo = o.elastic()
+    errs = {k: rel_l2(fg[k], fo[k]) for k in ("phi", "xB", "Y", "dYdt")}
+    if mm == 1:
+        errs["eta"] = rel_l2(fg["eta"], fo["eta"])
+    errs["strain"] = rel_l2(eg["strain"], eo["strain"])
+    print(case[3], prec, {k: f"{v:.2e}" for k, v in errs.items()},
+          "iters gpu/oracle", sg.elastic_iterations, so.elastic_iterations)
+    for k, v in errs.items():
+        tol = TOL[prec] if k != "dYdt" else 10 * TOL[prec]
+        assert v <= tol, (k, v)
+    assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1
+    if zm:
+        assert abs(sg.zero_mode_lambda - so.zero_mode_lambda) <= 1e-5 * max(1.0, abs(so.zero_mode_lambda))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_zero_mode_conserves_mass(capi, prec):
+    from cuda_sto_pf_gb300.solver import Solver
+    p = params_for(capi, "c2.params", n=32, zero_mode_enabled=1, precision=prec)
+    phi, xB, _ = _inputs(capi, p, 32, False, seed=9)
+    with Solver(p) as s:
+        s.load(phi, xB)
+        target = s.diagnostics().mass_xBtot
+        for _ in range(5):
+            st = s.step(1)
+            d = s.diagnostics()
+            assert abs(d.mass_xBtot - target) <= 1e-12 * max(1.0, abs(target)), (d.mass_xBtot, target)
+            assert abs(st.zero_mode_target_mass - target) <= 1e-12 * target
+
+
+def test_deterministic(capi):
+    from cuda_sto_pf_gb300.solver import Solver
+    p = params_for(capi, "c2.params", n=24, zero_mode_enabled=1, precision=1)
+    phi, xB, _ = _inputs(capi, p, 24, False, seed=3)
+    out = []
+    for _ in range(2):
+        with Solver(p) as s:
+            s.load(phi, xB)
+            s.step(3)
+            out.append(s.fields())
+    for k in ("phi", "Y", "dYdt"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_non_cubic_grid_parity(capi, oracle):
+    from cuda_sto_pf_gb300.solver import Solver
+    shape = (30, 24, 20)
+    p = params_for(capi, "c2.params", n=24, zero_mode_enabled=1, precision=0)
+    p.Nx, p.Ny, p.Nz = shape
+    phi, xB, _ = _inputs(capi, p, 24, False, seed=11, shape=shape)
+    o = oracle(p, threads=4)
+    o.load(phi, xB)
+    assert o.step(3) == 0
+    with Solver(p) as s:
+        s.load(phi, xB)
+        s.step(3)
+        fg = s.fields()
+    fo = o.fields()
+    for k in ("phi", "Y", "xB"):
+        assert rel_l2(fg[k], fo[k]) <= 1e-6, k
+
+
+def test_nonconvergence_is_reported(capi):
+    from cuda_sto_pf_gb300.solver import Solver
+    p = params_for(capi, "c2.params", n=16, elastic_iter_max=2, elastic_residual_tolerance=1e-14)
+    phi, xB, _ = _inputs(capi, p, 16, False, seed=2)
+    with Solver(p) as s:
+        s.load(phi, xB)
+        with pytest.raises(capi.PfgbError) as e:
+            s.step(1)
+        assert e.value.status == 4
