@@ -946,14 +946,17 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
 }
 
 // zero-mode solve (run_pf_conserved_y_zero_mode_host, main_cuda.cu:4269-4405):
-// same bracket / Newton / bisection logic; mass(l) comes from the Taylor
-// model sum_p M_p l^p / p! about l = 0 when |l| <= 0.05 (truncation error
-// below 1e-17 relative) and from a direct FP64 evaluation pass otherwise.
+// the same bracket check and Newton / bisection iteration on
+// F(l) = sum((1-h) sigmoid(Y* + l) + h v_B) - target.  The Newton iterates
+// are first taken on the quartic Taylor model of F about l = 0 (moments
+// accumulated by the final Y pass, no extra pass); the iteration is then
+// continued on FP64 direct evaluations until |F| <= tol, so convergence is
+// always decided on the exact sum, as in the reference.
 template <typename T, typename TE>
 static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     const pfgb_params &P = c->p;
     TRY(reduce_to<AccZM>(c, nb_final, DS_ZM));
-    TRY(sync_read(c, DS_ZM, 7));
+    TRY(sync_read(c, DS_MEAN_DY, DS_ZM + 7));   // mean_DY rides along
     const double ymin = c->hscal[DS_ZM], ymax = c->hscal[DS_ZM + 1];
     double M[5];
     for (int i = 0; i < 5; ++i) M[i] = c->hscal[DS_ZM + 2 + i];
@@ -972,10 +975,14 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     const int eb = 304;
     auto direct = [&](const double *lams, int nl, double *mass, double *der) -> pfgb_status {
         PFGB_CUDA_TRY(cudaMemcpyAsync(c->dscal + DS_EV, lams, sizeof(double) * nl, cudaMemcpyHostToDevice, c->stream));
-        k_zm_eval<T><<<eb, 256, 0, c->stream>>>((const T *)c->Y, (const T *)c->phi[1 - c->cur], N, c->Yc,
-                                                P.v_B, c->dscal + DS_EV, nl, c->partials);
+        {
+            ProfScope ps(c, {"zero_mode_eval", (double)N * 2.0 * sizeof(T)});
+            k_zm_eval<T><<<eb, 256, 0, c->stream>>>((const T *)c->Y, (const T *)c->phi[1 - c->cur], N, c->Yc,
+                                                    P.v_B, c->dscal + DS_EV, nl, c->partials);
+        }
         PFGB_CUDA_TRY(cudaGetLastError());
         for (int q = 0; q < nl; ++q) {
+            ProfScope ps(c, {"reduce_partials", (double)eb * sizeof(AccSum2)});
             k_reduce_partials<AccSum2><<<1, 256, 0, c->stream>>>((const AccSum2 *)c->partials + q * eb, eb,
                                                                  c->dscal, DS_BR + 2 * q, 1.0);
         }
@@ -984,32 +991,48 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
         for (int q = 0; q < nl; ++q) { mass[q] = c->hscal[DS_BR + 2 * q]; der[q] = c->hscal[DS_BR + 2 * q + 1]; }
         return PFGB_OK;
     };
-    auto model = [&](double l, double *mass, double *der) -> pfgb_status {
-        if (std::fabs(l) <= 0.05) {
-            *mass = M[0] + l * (M[1] + l * (M[2] / 2.0 + l * (M[3] / 6.0 + l * M[4] / 24.0)));
-            *der = M[1] + l * (M[2] + l * (M[3] / 2.0 + l * M[4] / 6.0));
-            return PFGB_OK;
-        }
-        return direct(&l, 1, mass, der);
-    };
     {
         double ls[2] = {lo, hi}, ms[2], ds[2];
         TRY(direct(ls, 2, ms, ds));
         if (!std::isfinite(ms[0]) || !std::isfinite(ms[1])) return fail("non-finite bracket mass");
         if (ms[0] - target > tol || ms[1] - target < -tol) return fail("target outside bracket");
     }
-    double lam = std::min(std::max(0.0, lo), hi), mass = 0, der = 0;
-    TRY(model(lam, &mass, &der));
-    double res = mass - target;
     int iters = 0, nwt = 0, bis = 0;
-    for (int it = 0; it < P.zero_mode_max_iterations && std::fabs(res) > tol; ++it) {
+    // one safeguarded Newton / bisection update (same rule as the reference)
+    auto update = [&](double &lam, double res, double der) {
         if (res < 0.0) lo = lam; else hi = lam;
         double cand = NAN;
         if (der > 0.0 && std::isfinite(der)) cand = lam - res / der;
         if (std::isfinite(cand) && cand > lo && cand < hi) ++nwt;
         else { cand = 0.5 * (lo + hi); ++bis; }
         lam = cand;
-        TRY(model(lam, &mass, &der));
+    };
+    double lam = std::min(std::max(0.0, lo), hi);
+    // predictor on the Taylor model (valid near l = 0)
+    auto model = [&](double l, double *mass, double *der) {
+        *mass = M[0] + l * (M[1] + l * (M[2] / 2.0 + l * (M[3] / 6.0 + l * M[4] / 24.0)));
+        *der = M[1] + l * (M[2] + l * (M[3] / 2.0 + l * M[4] / 6.0));
+    };
+    {
+        const double slo = lo, shi = hi;
+        double l = lam, m, d;
+        model(l, &m, &d);
+        for (int k = 0; k < 30 && std::fabs(m - target) > 0.01 * tol && std::fabs(l) <= 0.25; ++k) {
+            if (!(d > 0.0)) break;
+            const double nl_ = l - (m - target) / d;
+            if (!(nl_ > slo && nl_ < shi)) break;
+            l = nl_;
+            model(l, &m, &d);
+        }
+        if (std::isfinite(l) && l > slo && l < shi && std::fabs(l) <= 0.25) lam = l;
+        lo = slo; hi = shi;
+    }
+    double mass = 0, der = 0;
+    TRY(direct(&lam, 1, &mass, &der));
+    double res = mass - target;
+    for (int it = 0; it < P.zero_mode_max_iterations && std::fabs(res) > tol; ++it) {
+        update(lam, res, der);
+        TRY(direct(&lam, 1, &mass, &der));
         if (!std::isfinite(mass) || !std::isfinite(der)) return fail("non-finite mass");
         res = mass - target;
         iters = it + 1;
@@ -1094,7 +1117,7 @@ static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
     c->dYoff = 0.0;
     if (P.zero_mode_enabled) TRY((zero_mode<T, TE>(c, nbf, st)));
     if (st) {
-        TRY(sync_read(c, DS_MEAN_DY, 1));
+        if (!P.zero_mode_enabled) TRY(sync_read(c, DS_MEAN_DY, 1));
         st->mean_DY = c->hscal[DS_MEAN_DY];
     }
     c->cur = 1 - c->cur;
