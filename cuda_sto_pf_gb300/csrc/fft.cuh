@@ -20,26 +20,67 @@
 #pragma once
 
 #include "common.cuh"
+#include "rader41.cuh"
 
 #define PFGB_MAX_STAGES 16
 #define PFGB_MAX_N 1024
 
+// Division by a run-time constant d via a multiply-high (round-up method):
+// valid for every 32-bit dividend.
+struct FastDiv {
+    unsigned M;
+    int L;
+    unsigned d;
+    __host__ void init(unsigned dd) {
+        d = dd;
+        if (d <= 1) { M = 0; L = 0; return; }
+        L = 0;
+        while ((1u << L) < d) ++L;
+        M = (unsigned)((((unsigned long long)1 << 32) * ((1ull << L) - d)) / d + 1);
+    }
+    __device__ __forceinline__ unsigned div(unsigned x) const {
+        if (d <= 1) return x;
+        const unsigned t = __umulhi(M, x);
+        return (t + ((x - t) >> 1)) >> (L - 1);
+    }
+};
+
+struct StagePlan {
+    int R, Ns, nb, m;          // radix, span so far, butterflies per line, twiddle stride
+    FastDiv fNs, fnb;
+};
+
 struct AxisPlan {
     int n;
     int nst;
-    int rad[PFGB_MAX_STAGES];
+    StagePlan st[PFGB_MAX_STAGES];
 };
 
-// host: factor n into radices (8 first, then 4, 2, 3, 5, other primes)
+// host: factor n into stages.  A radix-41 factor goes first (its Rader stage
+// then needs no input twiddles), then 8, 6, 4, 2, 3, 5, 7, other primes.
 static inline void pfgb_make_plan(int n, AxisPlan *p) {
     p->n = n;
     p->nst = 0;
+    int rad[PFGB_MAX_STAGES], nr = 0;
     int m = n;
-    while (m % 8 == 0 && m > 1) { p->rad[p->nst++] = 8; m /= 8; }
-    while (m % 4 == 0 && m > 1) { p->rad[p->nst++] = 4; m /= 4; }
-    while (m % 2 == 0 && m > 1) { p->rad[p->nst++] = 2; m /= 2; }
+    while (m % 41 == 0 && m > 1) { rad[nr++] = 41; m /= 41; }
+    while (m % 8 == 0 && m > 1) { rad[nr++] = 8; m /= 8; }
+    while (m % 6 == 0 && m > 1) { rad[nr++] = 6; m /= 6; }
+    while (m % 4 == 0 && m > 1) { rad[nr++] = 4; m /= 4; }
+    while (m % 2 == 0 && m > 1) { rad[nr++] = 2; m /= 2; }
     for (int f = 3; m > 1; f += 2)
-        while (m % f == 0) { p->rad[p->nst++] = f; m /= f; }
+        while (m % f == 0) { rad[nr++] = f; m /= f; }
+    int Ns = 1;
+    for (int s = 0; s < nr; ++s) {
+        StagePlan &st = p->st[p->nst++];
+        st.R = rad[s];
+        st.Ns = Ns;
+        st.nb = n / rad[s];
+        st.m = n / (Ns * rad[s]);
+        st.fNs.init((unsigned)Ns);
+        st.fnb.init((unsigned)st.nb);
+        Ns *= rad[s];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -122,82 +163,231 @@ __device__ __forceinline__ T2 twmul(T2 a, T2 w) {
     return DIR < 0 ? cmul(a, w) : cmulconj(a, w);
 }
 
+template <typename T, int DIR>
+__device__ __forceinline__ void bfly6(cplx_t<T> *v) {
+    // 6 = 2 x 3: E = DFT3(x0,x2,x4), O = DFT3(x1,x3,x5), X_k = E_k + W6^k O_k
+    using T2 = cplx_t<T>;
+    T2 e[3] = {v[0], v[2], v[4]}, o[3] = {v[1], v[3], v[5]};
+    bfly3<T, DIR>(e);
+    bfly3<T, DIR>(o);
+    const T h = T(0.5), s3 = T(0.86602540378443864676372317075294);
+    // W6^1 = (1/2, -+ s3), W6^2 = (-1/2, -+ s3)
+    const T sg = DIR < 0 ? -s3 : s3;
+    T2 o1 = mk2<T2>(h * o[1].x - sg * o[1].y, h * o[1].y + sg * o[1].x);
+    T2 o2 = mk2<T2>(-h * o[2].x - sg * o[2].y, -h * o[2].y + sg * o[2].x);
+    v[0] = cadd(e[0], o[0]); v[3] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], o1);   v[4] = csub(e[1], o1);
+    v[2] = cadd(e[2], o2);   v[5] = csub(e[2], o2);
+}
+
+// ---------------------------------------------------------------------------
+// Radix-41 stage by Rader's algorithm, 8 lanes per 41-point DFT.
+//   X_0 = sum x ;  X_{7^q} = x_0 + (a (*) b)_q,  a_p = x_{6^p}  (mod 41)
+// The length-40 cyclic convolution is IFFT40(FFT40(a) . B) with
+// B = FFT40(b)/40 (rader41.cuh).  FFT40 = 5 x 8: lane t (0..7) owns
+// a[t + 8m], m = 0..4, does the 5-point DFTs in registers, the W40^{t k1}
+// twiddles, and the 8-point DFTs run across the 8 lanes with shuffles
+// (decimation in frequency forward -> bit-reversed lanes, decimation in time
+// inverse -> natural lanes).  Index maps: 6^(t+8m) = 6^t 10^m, 7^(t+8m) =
+// 7^t 37^m (mod 41).
+// ---------------------------------------------------------------------------
+template <typename T> struct RaderTab;
+template <> struct RaderTab<float> {
+    static __device__ __forceinline__ float2 B(int dir, int k) { return dir < 0 ? c_rader41_BF_f[k] : c_rader41_BI_f[k]; }
+};
+template <> struct RaderTab<double> {
+    static __device__ __forceinline__ double2 B(int dir, int k) { return dir < 0 ? c_rader41_BF_d[k] : c_rader41_BI_d[k]; }
+};
+
+template <typename T2>
+__device__ __forceinline__ T2 shfl_x(T2 v, int m, unsigned mask) {
+    v.x = __shfl_xor_sync(mask, v.x, m, 8);
+    v.y = __shfl_xor_sync(mask, v.y, m, 8);
+    return v;
+}
+
+template <typename T, int DIR>
+__device__ void stage_rader41(const cplx_t<T> *src, cplx_t<T> *dst, const StagePlan &st,
+                              const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast, int lgnl) {
+    using T2 = cplx_t<T>;
+    const int nb = st.nb, Ns = st.Ns, m = st.m;
+    const int t = threadIdx.x & 7;
+    const int group = threadIdx.x >> 3, ngroups = blockDim.x >> 3;
+    const unsigned gmask = 0xffu << (threadIdx.x & 24);
+    const int brt = ((t & 1) << 2) | (t & 2) | ((t & 4) >> 2);
+    // per-lane constants: W40^{t k1}, B[k1 + 5 br(t)], cross-lane twiddles
+    T2 W[5], Bk[5];
+#pragma unroll
+    for (int k1 = 0; k1 < 5; ++k1) {
+        T sn, cs;
+        if constexpr (sizeof(T) == 4) sincospif(-2.0f * (float)(t * k1) / 40.0f, &sn, &cs);
+        else sincospi(-2.0 * (double)(t * k1) / 40.0, &sn, &cs);
+        W[k1] = mk2<T2>(cs, sn);
+        Bk[k1] = RaderTab<T>::B(DIR, k1 + 5 * brt);
+    }
+    const T r = T(0.70710678118654752440084436210485);
+    const int p4 = t & 3, p2 = t & 1;
+    // forward DIF: span 4 -> W8^{p4}, span 2 -> W4^{p2} (exp(-i..))
+    const T2 f4 = p4 == 0 ? mk2<T2>(T(1), T(0)) : p4 == 1 ? mk2<T2>(r, -r) : p4 == 2 ? mk2<T2>(T(0), T(-1)) : mk2<T2>(-r, -r);
+    const T2 f2 = p2 == 0 ? mk2<T2>(T(1), T(0)) : mk2<T2>(T(0), T(-1));
+    int g6 = 1, g7 = 1;
+    for (int i = 0; i < t; ++i) { g6 = (g6 * 6) % 41; g7 = (g7 * 7) % 41; }
+    const int items = nl * nb;
+    for (int it = group; it < items; it += ngroups) {
+        int j, l;
+        if (lineFast) { l = (int)st.fnb.div((unsigned)it); j = it - l * nb; }
+        else { l = it & (nl - 1); j = it >> lgnl; }
+        const int jq = (int)st.fNs.div((unsigned)j);
+        const int k = j - jq * Ns;
+        const T2 *sb = src + l * sl;
+        T2 v[5];
+        int n = g6;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            T2 x = sb[(j + n * nb) * sp];
+            if (Ns > 1) x = twmul<DIR>(x, tw[n * k * m]);
+            v[q] = x;
+            n = (n * 10) % 41;
+        }
+        const T2 x0 = sb[j * sp];
+        // X_0 = x_0 + sum over the 40 permuted inputs
+        T2 s = cadd(cadd(cadd(v[0], v[1]), cadd(v[2], v[3])), v[4]);
+        s = cadd(s, shfl_x(s, 1, gmask));
+        s = cadd(s, shfl_x(s, 2, gmask));
+        s = cadd(s, shfl_x(s, 4, gmask));
+        // forward FFT40 of a: in-lane DFT5, twiddle, cross-lane DFT8 (DIF)
+        bfly5<T, -1>(v);
+#pragma unroll
+        for (int q = 1; q < 5; ++q) v[q] = cmul(v[q], W[q]);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            T2 u = shfl_x(v[q], 4, gmask);
+            v[q] = (t & 4) ? cmul(csub(u, v[q]), f4) : cadd(v[q], u);
+            u = shfl_x(v[q], 2, gmask);
+            v[q] = (t & 2) ? cmul(csub(u, v[q]), f2) : cadd(v[q], u);
+            u = shfl_x(v[q], 1, gmask);
+            v[q] = (t & 1) ? csub(u, v[q]) : cadd(v[q], u);
+            v[q] = cmul(v[q], Bk[q]);
+            // inverse cross-lane DFT8 (DIT, bit-reversed in, natural out)
+            u = shfl_x(v[q], 1, gmask);
+            v[q] = (t & 1) ? csub(u, v[q]) : cadd(v[q], u);
+            u = shfl_x(v[q], 2, gmask);
+            v[q] = (t & 2) ? csub(u, cmulconj(v[q], f2)) : cadd(v[q], cmulconj(u, f2));
+            u = shfl_x(v[q], 4, gmask);
+            v[q] = (t & 4) ? csub(u, cmulconj(v[q], f4)) : cadd(v[q], cmulconj(u, f4));
+        }
+#pragma unroll
+        for (int q = 1; q < 5; ++q) v[q] = cmulconj(v[q], W[q]);
+        bfly5<T, +1>(v);
+        // outputs X[7^(t+8m)] = x0 + c[t+8m]
+        T2 *db = dst + l * sl;
+        const int base = jq * Ns * 41 + k;
+        int o = g7;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            db[(base + o * Ns) * sp] = cadd(x0, v[q]);
+            o = (o * 37) % 41;
+        }
+        if (t == 0) db[base * sp] = cadd(x0, s);
+    }
+}
+
+// one Stockham stage of compile-time radix R: each work item is one
+// butterfly (R inputs twiddled, R-point DFT in registers, R outputs)
+template <typename T, int DIR, int R>
+__device__ __forceinline__ void stage_bfly(const cplx_t<T> *src, cplx_t<T> *dst, const StagePlan &st,
+                                           const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast,
+                                           int lgnl) {
+    using T2 = cplx_t<T>;
+    const int nb = st.nb, Ns = st.Ns, m = st.m;
+    const int work = nl * nb;
+    for (int w = threadIdx.x; w < work; w += blockDim.x) {
+        int j, l;
+        if (lineFast) { l = (int)st.fnb.div((unsigned)w); j = w - l * nb; }
+        else { l = w & (nl - 1); j = w >> lgnl; }
+        const int jq = (int)st.fNs.div((unsigned)j);
+        const int k = j - jq * Ns;
+        T2 v[R];
+        const T2 *sb = src + l * sl;
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = sb[(j + r * nb) * sp];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[r] = twmul<DIR>(v[r], tw[r * k * m]);
+        }
+        if constexpr (R == 2) bfly2<T, DIR>(v);
+        else if constexpr (R == 3) bfly3<T, DIR>(v);
+        else if constexpr (R == 4) bfly4<T, DIR>(v);
+        else if constexpr (R == 5) bfly5<T, DIR>(v);
+        else if constexpr (R == 6) bfly6<T, DIR>(v);
+        else bfly8<T, DIR>(v);
+        T2 *db = dst + l * sl;
+        const int base = jq * Ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) db[(base + r * Ns) * sp] = v[r];
+    }
+}
+
+// direct DFT stage for any other radix: one output per work item,
+// out_q = sum_r x_r W_n^{r (k m + q n/R)}  (exponent mod n)
+template <typename T, int DIR>
+__device__ void stage_direct(const cplx_t<T> *src, cplx_t<T> *dst, const StagePlan &st, int n,
+                             const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast, int lgnl) {
+    using T2 = cplx_t<T>;
+    const int R = st.R, nb = st.nb, Ns = st.Ns, m = st.m;
+    const int work = nl * n;
+    for (int w = threadIdx.x; w < work; w += blockDim.x) {
+        int o, l;
+        if (lineFast) { l = w / n; o = w - l * n; } else { l = w & (nl - 1); o = w >> lgnl; }
+        const int q = (int)st.fnb.div((unsigned)o);
+        const int j = o - q * nb;
+        const int jq = (int)st.fNs.div((unsigned)j);
+        const int k = j - jq * Ns;
+        int e = k * m + q * nb;
+        if (e >= n) e -= n;
+        const T2 *sb = src + l * sl;
+        T ar = 0, ai = 0;
+        int idx = 0;
+        for (int r = 0; r < R; ++r) {
+            T2 x = sb[(j + r * nb) * sp];
+            T2 t = tw[idx];
+            if (DIR < 0) { ar += x.x * t.x - x.y * t.y; ai += x.x * t.y + x.y * t.x; }
+            else { ar += x.x * t.x + x.y * t.y; ai += x.y * t.x - x.x * t.y; }
+            idx += e;
+            if (idx >= n) idx -= n;
+        }
+        dst[l * sl + (jq * Ns * R + k + q * Ns) * sp] = mk2<T2>(ar, ai);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // fft_lines: transform nl lines of length p.n held in shared memory.
 // Element (line l, position q) lives at buf[q*sp + l*sl].  Stockham stages
 // alternate between `a` and `b`; returns the buffer holding the result.
-// lineFast: consecutive threads walk positions of one line (sp == 1);
-// otherwise consecutive threads walk lines (sl == 1).
+// lineFast: consecutive threads walk butterflies of one line (sp == 1);
+// otherwise consecutive threads walk lines (sl == 1, nl a power of two).
 // Must be called by all threads of the block; ends with __syncthreads().
 // ---------------------------------------------------------------------------
 template <typename T, int DIR>
-__device__ cplx_t<T> *fft_lines(cplx_t<T> *a, cplx_t<T> *b, const AxisPlan &p,
-                                const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast) {
+__device__ __noinline__ cplx_t<T> *fft_lines(cplx_t<T> *a, cplx_t<T> *b, const AxisPlan &p,
+                                             const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast) {
     using T2 = cplx_t<T>;
-    const int n = p.n;
-    int Ns = 1;
+    const int lgnl = lineFast ? 0 : (__ffs(nl) - 1);
     T2 *src = a, *dst = b;
     for (int s = 0; s < p.nst; ++s) {
-        const int R = p.rad[s];
-        const int nb = n / R;
-        const int m = n / (Ns * R);
-        if (R == 2 || R == 3 || R == 4 || R == 5 || R == 8) {
-            const int work = nl * nb;
-            for (int w = threadIdx.x; w < work; w += blockDim.x) {
-                int j, l;
-                if (lineFast) { j = w % nb; l = w / nb; } else { l = w % nl; j = w / nl; }
-                const int k = j % Ns;
-                T2 v[8];
-                const T2 *sb = src + l * sl;
-#pragma unroll 8
-                for (int r = 0; r < 8; ++r) {
-                    if (r < R) {
-                        T2 x = sb[(j + r * nb) * sp];
-                        v[r] = (r == 0) ? x : twmul<DIR>(x, tw[r * k * m]);
-                    }
-                }
-                switch (R) {
-                    case 2: bfly2<T, DIR>(v); break;
-                    case 3: bfly3<T, DIR>(v); break;
-                    case 4: bfly4<T, DIR>(v); break;
-                    case 5: bfly5<T, DIR>(v); break;
-                    default: bfly8<T, DIR>(v); break;
-                }
-                T2 *db = dst + l * sl;
-                const int base = (j / Ns) * Ns * R + k;
-#pragma unroll 8
-                for (int r = 0; r < 8; ++r)
-                    if (r < R) db[(base + r * Ns) * sp] = v[r];
-            }
-        } else {
-            // direct DFT stage: one output per work item,
-            // out_q = sum_r x_r W_n^{r (k m + q n/R)}  (exponent mod n)
-            const int work = nl * n;
-            for (int w = threadIdx.x; w < work; w += blockDim.x) {
-                int o, l;
-                if (lineFast) { o = w % n; l = w / n; } else { l = w % nl; o = w / nl; }
-                const int j = o % nb, q = o / nb;
-                const int k = j % Ns;
-                int e = k * m + q * nb;
-                if (e >= n) e -= n;
-                const T2 *sb = src + l * sl;
-                T ar = 0, ai = 0;
-                int idx = 0;
-                for (int r = 0; r < R; ++r) {
-                    T2 x = sb[(j + r * nb) * sp];
-                    T2 t = tw[idx];
-                    if (DIR < 0) { ar += x.x * t.x - x.y * t.y; ai += x.x * t.y + x.y * t.x; }
-                    else { ar += x.x * t.x + x.y * t.y; ai += x.y * t.x - x.x * t.y; }
-                    idx += e;
-                    if (idx >= n) idx -= n;
-                }
-                const int base = (j / Ns) * Ns * R + k;
-                dst[l * sl + (base + q * Ns) * sp] = mk2<T2>(ar, ai);
-            }
+        const StagePlan &st = p.st[s];
+        switch (st.R) {
+            case 2: stage_bfly<T, DIR, 2>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
+            case 3: stage_bfly<T, DIR, 3>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
+            case 4: stage_bfly<T, DIR, 4>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
+            case 5: stage_bfly<T, DIR, 5>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
+            case 6: stage_bfly<T, DIR, 6>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
+            case 8: stage_bfly<T, DIR, 8>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
+            case 41: stage_rader41<T, DIR>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
+            default: stage_direct<T, DIR>(src, dst, st, p.n, tw, nl, sp, sl, lineFast, lgnl); break;
         }
         __syncthreads();
         T2 *t = src; src = dst; dst = t;
-        Ns *= R;
     }
     return src;
 }

@@ -483,19 +483,22 @@ struct OpYFinalZ {
         d.Y[cell] = y;
         d.dYdt[cell] = (y - Yold) / T(c.dt);
         if (c.zm) {
+            // exact min / max of Y* (they fix the lambda bracket); the Taylor
+            // moments feed only the Newton predictor, so field precision is
+            // enough for them
             const double ys = double(y) + d.Yc;
-            const double h = pf_h(double(d.phi_new[cell]));
-            const double a = 1.0 - h;
-            const double s = sigmoid_raw(ys);
-            const double s1 = s * (1.0 - s);
-            const double u = 1.0 - 2.0 * s;
             acc.mn = fmin(acc.mn, ys);
             acc.mx = fmax(acc.mx, ys);
-            acc.m[0] += a * s + h * c.vB;
-            acc.m[1] += a * s1;
-            acc.m[2] += a * s1 * u;
-            acc.m[3] += a * s1 * (1.0 - 6.0 * s1);
-            acc.m[4] += a * s1 * u * (1.0 - 12.0 * s1);
+            const T h = pf_h(d.phi_new[cell]);
+            const T a = T(1) - h;
+            const T s = sigmoid_raw(T(ys));
+            const T s1 = s * (T(1) - s);
+            const T u = T(1) - T(2) * s;
+            acc.m[0] += double(a * s + h * T(c.vB));
+            acc.m[1] += double(a * s1);
+            acc.m[2] += double(a * s1 * u);
+            acc.m[3] += double(a * s1 * (T(1) - T(6) * s1));
+            acc.m[4] += double(a * s1 * u * (T(1) - T(12) * s1));
         }
     }
     __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
@@ -505,19 +508,21 @@ struct OpYFinalZ {
 // zero-mode direct evaluation: mass(l) and d mass/dl at given shifts, FP64
 // (compute_pf_Y_zero_mode_terms_kernel, cuda_kernels.cu:3409-3420).  nl shifts
 // at once; used for the bracket ends and when the Taylor model is out of range.
-template <typename T>
+// TV = evaluation precision: double for every convergence decision; the
+// field precision for the bracket-end check, whose margin is then verified
+template <typename T, typename TV>
 __global__ void k_zm_eval(const T *Y, const T *phi, long long N, double Yc, double vB,
                           const double *lam, int nl, double *partials) {
     double m[4] = {0, 0, 0, 0}, dd[4] = {0, 0, 0, 0};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
          i += (long long)gridDim.x * blockDim.x) {
-        const double h = pf_h(double(phi[i]));
-        const double a = 1.0 - h;
+        const TV h = pf_h(TV(phi[i]));
+        const TV a = TV(1) - h;
         const double y = double(Y[i]) + Yc;
         for (int q = 0; q < nl; ++q) {
-            const double x = sigmoid_raw(y + lam[q]);
-            m[q] += a * x + h * vB;
-            dd[q] += a * x * (1.0 - x);
+            const TV x = sigmoid_raw(TV(y + lam[q]));
+            m[q] += double(a * x + h * TV(vB));
+            dd[q] += double(a * x * (TV(1) - x));
         }
     }
     for (int q = 0; q < nl; ++q) {
@@ -973,12 +978,16 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     const double tol = P.zero_mode_tolerance_relative * std::max(std::fabs(target), 1.0);
     const long long N = c->g.N;
     const int eb = 304;
-    auto direct = [&](const double *lams, int nl, double *mass, double *der) -> pfgb_status {
+    auto direct = [&](const double *lams, int nl, double *mass, double *der, bool exact = true) -> pfgb_status {
         PFGB_CUDA_TRY(cudaMemcpyAsync(c->dscal + DS_EV, lams, sizeof(double) * nl, cudaMemcpyHostToDevice, c->stream));
         {
             ProfScope ps(c, {"zero_mode_eval", (double)N * 2.0 * sizeof(T)});
-            k_zm_eval<T><<<eb, 256, 0, c->stream>>>((const T *)c->Y, (const T *)c->phi[1 - c->cur], N, c->Yc,
-                                                    P.v_B, c->dscal + DS_EV, nl, c->partials);
+            if (exact)
+                k_zm_eval<T, double><<<eb, 256, 0, c->stream>>>((const T *)c->Y, (const T *)c->phi[1 - c->cur], N,
+                                                                c->Yc, P.v_B, c->dscal + DS_EV, nl, c->partials);
+            else
+                k_zm_eval<T, T><<<eb, 256, 0, c->stream>>>((const T *)c->Y, (const T *)c->phi[1 - c->cur], N,
+                                                           c->Yc, P.v_B, c->dscal + DS_EV, nl, c->partials);
         }
         PFGB_CUDA_TRY(cudaGetLastError());
         for (int q = 0; q < nl; ++q) {
@@ -992,8 +1001,17 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
         return PFGB_OK;
     };
     {
+        // bracket ends: evaluated in field precision; an FP64 re-evaluation is
+        // taken only when the FP32 value is within 1e-5 of the decision limit
         double ls[2] = {lo, hi}, ms[2], ds[2];
-        TRY(direct(ls, 2, ms, ds));
+        const bool fp32 = sizeof(T) == 4;
+        TRY(direct(ls, 2, ms, ds, !fp32));
+        if (fp32) {
+            const double margin = 1e-5 * std::max(std::fabs(target), 1.0);
+            if (!std::isfinite(ms[0]) || !std::isfinite(ms[1]) || std::fabs(ms[0] - target - tol) < margin ||
+                std::fabs(ms[1] - target + tol) < margin)
+                TRY(direct(ls, 2, ms, ds, true));
+        }
         if (!std::isfinite(ms[0]) || !std::isfinite(ms[1])) return fail("non-finite bracket mass");
         if (ms[0] - target > tol || ms[1] - target < -tol) return fail("target outside bracket");
     }
