@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=246)
+    ap.add_argument("--shape", default="", help="Nx,Ny,Nz (profiling cases; default n^3)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--elastic-tol", type=float, default=1e-6)
     ap.add_argument("--cpu-sample-n", type=int, default=128)
@@ -59,9 +60,9 @@ def dist_env():
     return ws, rank, local
 
 
-def make_params(capi, n, precision, tol):
+def make_params(capi, n, precision, tol, shape=None):
     p = capi.load_params_file(PARAMS)
-    p.Nx = p.Ny = p.Nz = n
+    p.Nx, p.Ny, p.Nz = shape if shape else (n, n, n)
     p.model_mode = capi.MODEL_GP_ZONE
     p.zero_mode_enabled = 1
     p.precision = capi.PREC_FP32 if precision == "fp32" else capi.PREC_FP64
@@ -72,9 +73,12 @@ def make_params(capi, n, precision, tol):
 
 def make_fields(capi, p, n, seed=2468):
     from cuda_sto_pf_gb300 import workloads
-    count = max(1, int(round(60 * (n / 246.0) ** 3)))
-    sites = max(1, int(round(20 * (n / 246.0) ** 3)))
-    w = workloads.ellipsoid_population(n, count=count, eta_sites=sites, w=p.ic_phi_iface_w, seed=seed)
+    shape = (p.Nx, p.Ny, p.Nz)
+    frac = shape[0] * shape[1] * shape[2] / 246.0 ** 3
+    count = max(1, int(round(60 * frac)))
+    sites = max(1, int(round(20 * frac)))
+    w = workloads.ellipsoid_population(n, count=count, eta_sites=sites, w=p.ic_phi_iface_w, seed=seed,
+                                       shape=shape)
     phi, xB, eta = w["phi"], w["xB"], w["eta"]
     # raw-field rules of the reference loader (xB capped at its default
     # xB_max_safe = 0.07)
@@ -205,8 +209,9 @@ def run_ours(args):
     from cuda_sto_pf_gb300.solver import Solver
     capi.load(build_if_missing=True)
     n = args.n
-    N = n ** 3
-    p = make_params(capi, n, args.precision, args.elastic_tol)
+    shape = tuple(int(x) for x in args.shape.split(",")) if args.shape else (n, n, n)
+    N = shape[0] * shape[1] * shape[2]
+    p = make_params(capi, n, args.precision, args.elastic_tol, shape)
     phi, xB, eta, npart, neta = make_fields(capi, p, n)
     stream = torch.cuda.current_stream(dev)
     s = Solver(p, device=dev)
@@ -316,7 +321,7 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32" if args.precision == "fp32" else "f64",
                 "data": "synthetic (seeded microstructure generator, reference raw-field rules)",
-                "config": {"workload": f"{n}^3 gp_zone dynamics, {npart} ellipsoids + {neta} eta sites, "
+                "config": {"workload": f"{'x'.join(map(str, shape))} gp_zone dynamics, {npart} ellipsoids + {neta} eta sites, "
                                        f"heterogeneous elasticity, zero mode",
                            "grid": n, "fields": args.precision, "elastic": "fp32",
                            "elastic_tol": args.elastic_tol, "dt": p.dt,

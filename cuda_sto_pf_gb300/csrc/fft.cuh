@@ -426,8 +426,9 @@ k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
     T2 *sm = reinterpret_cast<T2 *>(smem_raw);
     const int n = plan.n;
     T2 *tw = sm;                       // n
-    T2 *bufs = sm + n;                 // (NIN + NOUT + 1) * n * TK
-    const int tile = n * TK;
+    T2 *bufs = sm + n;                 // (NIN + NOUT + 1) * n * (TK + 1)
+    const int TKP = TK + 1;            // padded row stride: spreads rows over banks
+    const int tile = n * TKP;
     T2 *bin[NIN > 0 ? NIN : 1];
     T2 *bout[NOUT > 0 ? NOUT : 1];
     constexpr bool INPL = Op::kInplace;   // identity op: outputs reuse inputs
@@ -447,18 +448,18 @@ k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
     if (DIN != 0 || DOUT != 0) load_tw<T>(tw, tw_g, n);
 #pragma unroll
     for (int a = 0; a < NIN; ++a) {
-        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+        for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
             const int q = e / TK, l = e - q * TK;
             T2 v = mk2<T2>(T(0), T(0));
             if (l < kcnt) v = io.in[a][base + q * es + l];
-            bin[a][e] = v;
+            bin[a][q * TKP + l] = v;
         }
     }
     __syncthreads();
     if (DIN != 0) {
 #pragma unroll
         for (int a = 0; a < NIN; ++a) {
-            T2 *r = fft_lines<T, DIN>(bin[a], scr, plan, tw, TK, TK, 1, false);
+            T2 *r = fft_lines<T, DIN>(bin[a], scr, plan, tw, TK, TKP, 1, false);
             if (r == scr) { scr = bin[a]; bin[a] = r; }
         }
     }
@@ -468,32 +469,32 @@ k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
         for (int a = 0; a < NOUT; ++a) bout[a] = bin[a];
     }
     if constexpr (!INPL) {
-        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+        for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
             const int q = e / TK, l = e - q * TK;
             const int k = k0 + l;
             const int i = (axis == 1) ? slab : q;
             const int j = (axis == 1) ? q : slab;
             T2 vin[NIN > 0 ? NIN : 1], vout[NOUT > 0 ? NOUT : 1];
 #pragma unroll
-            for (int a = 0; a < NIN; ++a) vin[a] = bin[a][e];
+            for (int a = 0; a < NIN; ++a) vin[a] = bin[a][q * TKP + l];
             op.apply(i, j, k, vin, vout);
 #pragma unroll
-            for (int a = 0; a < NOUT; ++a) bout[a][e] = vout[a];
+            for (int a = 0; a < NOUT; ++a) bout[a][q * TKP + l] = vout[a];
         }
         __syncthreads();
     }
     if (DOUT != 0) {
 #pragma unroll
         for (int a = 0; a < NOUT; ++a) {
-            T2 *r = fft_lines<T, DOUT>(bout[a], scr, plan, tw, TK, TK, 1, false);
+            T2 *r = fft_lines<T, DOUT>(bout[a], scr, plan, tw, TK, TKP, 1, false);
             if (r == scr) { scr = bout[a]; bout[a] = r; }
         }
     }
 #pragma unroll
     for (int a = 0; a < NOUT; ++a) {
-        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+        for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
             const int q = e / TK, l = e - q * TK;
-            if (l < kcnt) io.out[a][base + q * es + l] = bout[a][e];
+            if (l < kcnt) io.out[a][base + q * es + l] = bout[a][q * TKP + l];
         }
     }
 }

@@ -136,9 +136,9 @@ static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, O
     const int n = pl.n;
     const int nbuf = Op::kInplace ? NIN + 1 : NIN + NOUT + 1;
     int TK = 16;
-    while (TK > 1 && ((size_t)n + (size_t)nbuf * n * TK) * sizeof(T2) > kSmemBudget) TK >>= 1;
+    while (TK > 1 && ((size_t)n + (size_t)nbuf * n * (TK + 1)) * sizeof(T2) > kSmemBudget) TK >>= 1;
     while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
-    const size_t smem = ((size_t)n + (size_t)nbuf * n * TK) * sizeof(T2);
+    const size_t smem = ((size_t)n + (size_t)nbuf * n * (TK + 1)) * sizeof(T2);
     auto kern = k_axis_pass<T, NIN, NOUT, DIN, DOUT, Op>;
     PFGB_CUDA_TRY(allow_smem(kern, smem));
     dim3 grid((c->g.NzC + TK - 1) / TK, axis == 1 ? c->g.Nx : c->g.Ny);
@@ -700,7 +700,7 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
     using T2 = cplx_t<TE>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2 *sm = reinterpret_cast<T2 *>(smem_raw);
-    const int n = plan.n, tile = n * TK;
+    const int n = plan.n, TKP = TK + 1, tile = n * TKP;   // padded row stride
     T2 *tw = sm;
     T2 *acc[3] = {sm + n, sm + n + tile, sm + n + 2 * tile};
     T2 *w0 = sm + n + 3 * tile, *w1 = w0 + tile;
@@ -711,17 +711,18 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
     load_tw<TE>(tw, A.tw, n);
     for (int e = threadIdx.x; e < 3 * tile; e += blockDim.x) acc[e / tile][e % tile] = mk2<T2>(TE(0), TE(0));
     for (int cmp = 0; cmp < 6; ++cmp) {
-        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+        for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
             const int q = e / TK, l = e - q * TK;
-            w0[e] = (l < kcnt) ? A.E[cmp][base + q * es + l] : mk2<T2>(TE(0), TE(0));
+            w0[q * TKP + l] = (l < kcnt) ? A.E[cmp][base + q * es + l] : mk2<T2>(TE(0), TE(0));
         }
         __syncthreads();
-        T2 *r = fft_lines<TE, -1>(w0, w1, plan, tw, TK, TK, 1, false);
+        T2 *r = fft_lines<TE, -1>(w0, w1, plan, tw, TK, TKP, 1, false);
         // accumulate t_i += k_j tau_ij
         const int a = cmp < 3 ? cmp : (cmp == 3 ? 1 : 0);
         const int b = cmp < 3 ? cmp : (cmp == 5 ? 1 : 2);
-        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
-            const int q = e / TK, l = e - q * TK;
+        for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
+            const int q = e0 / TK, l = e0 - q * TK;
+            const int e = q * TKP + l;
             const TE kv[3] = {TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[min(k0 + l, A.g.NzC - 1)])};
             const T2 x = r[e];
             if (EIGEN) {
@@ -745,8 +746,9 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
     }
     // u = -i G t, masked; residual; store u
     double rd = 0.0, rr = 0.0;
-    for (int e = threadIdx.x; e < tile; e += blockDim.x) {
-        const int q = e / TK, l = e - q * TK, k = k0 + l;
+    for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
+        const int q = e0 / TK, l = e0 - q * TK, k = k0 + l;
+        const int e = q * TKP + l;
         T2 u[3];
         if (l >= kcnt || A.kt.cut(q, j, k) || (q == 0 && j == 0 && k == 0)) {
             u[0] = u[1] = u[2] = mk2<T2>(TE(0), TE(0));
@@ -784,17 +786,18 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
     __syncthreads();
     // strain components -> inverse x -> store
     for (int cmp = 0; cmp < 6; ++cmp) {
-        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
-            const int q = e / TK, l = e - q * TK;
+        for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
+            const int q = e0 / TK, l = e0 - q * TK;
+            const int e = q * TKP + l;
             const int k = min(k0 + l, A.g.NzC - 1);
             const T2 u[3] = {acc[0][e], acc[1][e], acc[2][e]};
             w0[e] = strain_comp<TE>(cmp, TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[k]), u);
         }
         __syncthreads();
-        T2 *r = fft_lines<TE, +1>(w0, w1, plan, tw, TK, TK, 1, false);
-        for (int e = threadIdx.x; e < tile; e += blockDim.x) {
-            const int q = e / TK, l = e - q * TK;
-            if (l < kcnt) A.E[cmp][base + q * es + l] = r[e];
+        T2 *r = fft_lines<TE, +1>(w0, w1, plan, tw, TK, TKP, 1, false);
+        for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
+            const int q = e0 / TK, l = e0 - q * TK;
+            if (l < kcnt) A.E[cmp][base + q * es + l] = r[q * TKP + l];
         }
         __syncthreads();
     }
@@ -811,9 +814,9 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
     using T2 = cplx_t<TE>;
     const int n = c->plx.n;
     int TK = 16;
-    while (TK > 1 && ((size_t)n + 5 * (size_t)n * TK) * sizeof(T2) > kSmemBudget) TK >>= 1;
+    while (TK > 1 && ((size_t)n + 5 * (size_t)n * (TK + 1)) * sizeof(T2) > kSmemBudget) TK >>= 1;
     while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
-    const size_t smem = ((size_t)n + 5 * (size_t)n * TK) * sizeof(T2);
+    const size_t smem = ((size_t)n + 5 * (size_t)n * (TK + 1)) * sizeof(T2);
     GreenArgs<TE> A;
     A.g = c->g;
     A.kt = KTab{c->kx, c->ky, c->kz, c->mx, c->my, c->mz};

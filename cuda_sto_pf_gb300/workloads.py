@@ -77,21 +77,23 @@ def single_sphere(n=64, radius=8.0, w=2.5, seed=1234):
 
 
 def ellipsoid_population(n=246, count=60, median_r=6.0, sigma_ln=0.3, eta_sites=20, eta_r=3.0,
-                         w=2.5, seed=2468, max_tries=200000):
+                         w=2.5, seed=2468, max_tries=200000, shape=None):
     """Non-overlapping ellipsoids (log-normal radii, aspect ratios U[0.5,1],
-    uniform rotations, rejection placement) plus spherical GP-zone eta seeds."""
+    uniform rotations, rejection placement) plus spherical GP-zone eta seeds.
+    ``shape`` overrides the cubic n^3 grid."""
     rng = np.random.default_rng(seed)
-    shape = (n, n, n)
+    shape = tuple(shape) if shape else (n, n, n)
+    L = np.array(shape, dtype=np.float64)
     centers, radii, rots = [], [], []
     tries = 0
     while len(centers) < count and tries < max_tries:
         tries += 1
         a = median_r * math.exp(sigma_ln * rng.standard_normal())
         R = np.array([a, a * rng.uniform(0.5, 1.0), a * rng.uniform(0.5, 1.0)])
-        c = rng.uniform(0, n, size=3)
+        c = rng.uniform(0, 1, size=3) * L
         ok = True
         for c2, R2 in zip(centers, radii):
-            d = _periodic(c - c2, n)
+            d = _periodic(c - c2, L)
             if np.linalg.norm(d) < R.max() + R2.max() + 2 * w:
                 ok = False
                 break
@@ -105,10 +107,10 @@ def ellipsoid_population(n=246, count=60, median_r=6.0, sigma_ln=0.3, eta_sites=
     tries = 0
     while len(ecs) < eta_sites and tries < max_tries:
         tries += 1
-        c = rng.uniform(0, n, size=3)
-        ok = all(np.linalg.norm(_periodic(c - c2, n)) > R2.max() + eta_r + 2 * w
+        c = rng.uniform(0, 1, size=3) * L
+        ok = all(np.linalg.norm(_periodic(c - c2, L)) > R2.max() + eta_r + 2 * w
                  for c2, R2 in zip(centers, radii))
-        ok = ok and all(np.linalg.norm(_periodic(c - e, n)) > 2 * eta_r + 2 * w for e in ecs)
+        ok = ok and all(np.linalg.norm(_periodic(c - e, L)) > 2 * eta_r + 2 * w for e in ecs)
         if ok:
             ecs.append(c)
     eta = ellipsoid_field(shape, ecs, [np.full(3, eta_r)] * len(ecs), [np.eye(3)] * len(ecs), w)
