@@ -157,6 +157,23 @@ __device__ __forceinline__ void bfly5(cplx_t<T> *v) {
     v[3] = csub(p2, q2);
 }
 
+// Asynchronous global->shared element copy (cp.async, sm_80+): all of a
+// thread's tile loads are in flight at once.  `valid == false` zero-fills
+// (source size 0; the source address is clamped to a valid one).
+template <typename T2>
+__device__ __forceinline__ void cp_async_elem(T2 *smem, const T2 *gmem, bool valid) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (sizeof(T2) == 16) {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 16 : 0));
+    } else {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(valid ? 8 : 0));
+    }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // twiddle w = W_n^e (table holds the forward roots); inverse uses conj
 template <int DIR, typename T2>
 __device__ __forceinline__ T2 twmul(T2 a, T2 w) {
@@ -444,17 +461,19 @@ k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
     if (axis == 1) { base = (long long)slab * g.Ny * g.NzC + k0; es = g.NzC; }
     else { base = (long long)slab * g.NzC + k0; es = (long long)g.Ny * g.NzC; }
     const int kcnt = min(TK, g.NzC - k0);
+    const int lgTK = __ffs(TK) - 1;    // TK is a power of two
 
     if (DIN != 0 || DOUT != 0) load_tw<T>(tw, tw_g, n);
 #pragma unroll
     for (int a = 0; a < NIN; ++a) {
         for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
-            const int q = e / TK, l = e - q * TK;
-            T2 v = mk2<T2>(T(0), T(0));
-            if (l < kcnt) v = io.in[a][base + q * es + l];
-            bin[a][q * TKP + l] = v;
+            const int q = e >> lgTK, l = e & (TK - 1);
+            const bool ok = l < kcnt;
+            cp_async_elem(&bin[a][q * TKP + l], io.in[a] + (ok ? base + q * es + l : base), ok);
         }
     }
+    cp_async_commit();
+    cp_async_wait_all();
     __syncthreads();
     if (DIN != 0) {
 #pragma unroll
@@ -470,7 +489,7 @@ k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
     }
     if constexpr (!INPL) {
         for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
-            const int q = e / TK, l = e - q * TK;
+            const int q = e >> lgTK, l = e & (TK - 1);
             const int k = k0 + l;
             const int i = (axis == 1) ? slab : q;
             const int j = (axis == 1) ? q : slab;
@@ -493,7 +512,7 @@ k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
 #pragma unroll
     for (int a = 0; a < NOUT; ++a) {
         for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
-            const int q = e / TK, l = e - q * TK;
+            const int q = e >> lgTK, l = e & (TK - 1);
             if (l < kcnt) io.out[a][base + q * es + l] = bout[a][q * TKP + l];
         }
     }

@@ -703,38 +703,53 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
     const int n = plan.n, TKP = TK + 1, tile = n * TKP;   // padded row stride
     T2 *tw = sm;
     T2 *acc[3] = {sm + n, sm + n + tile, sm + n + 2 * tile};
-    T2 *w0 = sm + n + 3 * tile, *w1 = w0 + tile;
+    // ld[0..1]: double-buffered component loads; wk: FFT ping-pong partner
+    T2 *ld[2] = {sm + n + 3 * tile, sm + n + 4 * tile};
+    T2 *wk = sm + n + 5 * tile;
     const int k0 = blockIdx.x * TK, j = blockIdx.y;
     const long long base = (long long)j * A.g.NzC + k0;
     const long long es = (long long)A.g.Ny * A.g.NzC;
     const int kcnt = min(TK, A.g.NzC - k0);
+    const int lgTK = __ffs(TK) - 1;
+    auto issue = [&](int cmp, T2 *dst) {
+        for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
+            const int q = e >> lgTK, l = e & (TK - 1);
+            const bool ok = l < kcnt;
+            cp_async_elem(&dst[q * TKP + l], A.E[cmp] + (ok ? base + q * es + l : base), ok);
+        }
+        cp_async_commit();
+    };
+    issue(0, ld[0]);
     load_tw<TE>(tw, A.tw, n);
     for (int e = threadIdx.x; e < 3 * tile; e += blockDim.x) acc[e / tile][e % tile] = mk2<T2>(TE(0), TE(0));
     for (int cmp = 0; cmp < 6; ++cmp) {
-        for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
-            const int q = e / TK, l = e - q * TK;
-            w0[q * TKP + l] = (l < kcnt) ? A.E[cmp][base + q * es + l] : mk2<T2>(TE(0), TE(0));
+        T2 *cur = ld[cmp & 1];
+        if (cmp + 1 < 6) {
+            issue(cmp + 1, ld[(cmp + 1) & 1]);   // prefetch the next component
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         __syncthreads();
-        T2 *r = fft_lines<TE, -1>(w0, w1, plan, tw, TK, TKP, 1, false);
+        T2 *r = fft_lines<TE, -1>(cur, wk, plan, tw, TK, TKP, 1, false);
+        if (r == wk) { wk = cur; ld[cmp & 1] = r; }   // keep three distinct buffers
         // accumulate t_i += k_j tau_ij
         const int a = cmp < 3 ? cmp : (cmp == 3 ? 1 : 0);
         const int b = cmp < 3 ? cmp : (cmp == 5 ? 1 : 2);
         for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
-            const int q = e0 / TK, l = e0 - q * TK;
+            const int q = e0 >> lgTK, l = e0 & (TK - 1);
             const int e = q * TKP + l;
             const TE kv[3] = {TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[min(k0 + l, A.g.NzC - 1)])};
             const T2 x = r[e];
             if (EIGEN) {
                 // tau_ij = C_ij,ab eps0_ab ; component (a,b) enters with
-                // weight 1 (normal) or 2 (shear) in Voigt column tvoigt(a,b)
-                const int col = cmp;
+                // weight 1 (normal) or 2 (shear) in Voigt column cmp
                 const TE f = cmp < 3 ? TE(1) : TE(2);
 #pragma unroll
                 for (int ii = 0; ii < 3; ++ii) {
                     TE s = 0;
 #pragma unroll
-                    for (int jj = 0; jj < 3; ++jj) s += kv[jj] * A.ec.S[vidx(tvoigt(ii, jj), col)];
+                    for (int jj = 0; jj < 3; ++jj) s += kv[jj] * A.ec.S[vidx(tvoigt(ii, jj), cmp)];
                     acc[ii][e] = cadd(acc[ii][e], cscale(x, f * s));
                 }
             } else {
@@ -747,7 +762,7 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
     // u = -i G t, masked; residual; store u
     double rd = 0.0, rr = 0.0;
     for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
-        const int q = e0 / TK, l = e0 - q * TK, k = k0 + l;
+        const int q = e0 >> lgTK, l = e0 & (TK - 1), k = k0 + l;
         const int e = q * TKP + l;
         T2 u[3];
         if (l >= kcnt || A.kt.cut(q, j, k) || (q == 0 && j == 0 && k == 0)) {
@@ -760,15 +775,15 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
             const long long o = base + q * es + l;
             if (A.resid) {
                 const double w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? 1.0 : 2.0;
-                double ld = 0, lr = 0;
+                double ld_ = 0, lr = 0;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const T2 old = A.U[c][o];
                     const double dr = double(u[c].x) - double(old.x), di = double(u[c].y) - double(old.y);
-                    ld += dr * dr + di * di;
+                    ld_ += dr * dr + di * di;
                     lr += double(u[c].x) * double(u[c].x) + double(u[c].y) * double(u[c].y);
                 }
-                rd += w * ld;
+                rd += w * ld_;
                 rr += w * lr;
             }
 #pragma unroll
@@ -785,9 +800,10 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
     }
     __syncthreads();
     // strain components -> inverse x -> store
+    T2 *w0 = ld[0], *w1 = ld[1];
     for (int cmp = 0; cmp < 6; ++cmp) {
         for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
-            const int q = e0 / TK, l = e0 - q * TK;
+            const int q = e0 >> lgTK, l = e0 & (TK - 1);
             const int e = q * TKP + l;
             const int k = min(k0 + l, A.g.NzC - 1);
             const T2 u[3] = {acc[0][e], acc[1][e], acc[2][e]};
@@ -796,7 +812,7 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
         __syncthreads();
         T2 *r = fft_lines<TE, +1>(w0, w1, plan, tw, TK, TKP, 1, false);
         for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
-            const int q = e0 / TK, l = e0 - q * TK;
+            const int q = e0 >> lgTK, l = e0 & (TK - 1);
             if (l < kcnt) A.E[cmp][base + q * es + l] = r[q * TKP + l];
         }
         __syncthreads();
@@ -814,9 +830,9 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
     using T2 = cplx_t<TE>;
     const int n = c->plx.n;
     int TK = 16;
-    while (TK > 1 && ((size_t)n + 5 * (size_t)n * (TK + 1)) * sizeof(T2) > kSmemBudget) TK >>= 1;
+    while (TK > 1 && ((size_t)n + 6 * (size_t)n * (TK + 1)) * sizeof(T2) > kSmemBudget) TK >>= 1;
     while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
-    const size_t smem = ((size_t)n + 5 * (size_t)n * (TK + 1)) * sizeof(T2);
+    const size_t smem = ((size_t)n + 6 * (size_t)n * (TK + 1)) * sizeof(T2);
     GreenArgs<TE> A;
     A.g = c->g;
     A.kt = KTab{c->kx, c->ky, c->kz, c->mx, c->my, c->mz};
