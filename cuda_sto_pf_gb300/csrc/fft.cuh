@@ -232,7 +232,8 @@ __device__ void stage_rader41(const cplx_t<T> *src, cplx_t<T> *dst, const StageP
     const int group = threadIdx.x >> 3, ngroups = blockDim.x >> 3;
     const unsigned gmask = 0xffu << (threadIdx.x & 24);
     const int brt = ((t & 1) << 2) | (t & 2) | ((t & 4) >> 2);
-    // per-lane constants: W40^{t k1}, B[k1 + 5 br(t)], cross-lane twiddles
+    // per-lane constants: W40^{t k1}, B[k1 + 5 br(t)], butterfly signs/twiddles,
+    // and the shared-memory offsets of the lane's 5 inputs and 5 outputs
     T2 W[5], Bk[5];
 #pragma unroll
     for (int k1 = 0; k1 < 5; ++k1) {
@@ -244,11 +245,28 @@ __device__ void stage_rader41(const cplx_t<T> *src, cplx_t<T> *dst, const StageP
     }
     const T r = T(0.70710678118654752440084436210485);
     const int p4 = t & 3, p2 = t & 1;
-    // forward DIF: span 4 -> W8^{p4}, span 2 -> W4^{p2} (exp(-i..))
-    const T2 f4 = p4 == 0 ? mk2<T2>(T(1), T(0)) : p4 == 1 ? mk2<T2>(r, -r) : p4 == 2 ? mk2<T2>(T(0), T(-1)) : mk2<T2>(-r, -r);
-    const T2 f2 = p2 == 0 ? mk2<T2>(T(1), T(0)) : mk2<T2>(T(0), T(-1));
-    int g6 = 1, g7 = 1;
-    for (int i = 0; i < t; ++i) { g6 = (g6 * 6) % 41; g7 = (g7 * 7) % 41; }
+    // forward twiddles of the lane's DIF butterflies (W8^{p4}, W4^{p2}); the
+    // lower lane of a pair uses 1 and sign +1, the upper one f and sign -1
+    const T2 one = mk2<T2>(T(1), T(0));
+    const T2 f4 = p4 == 0 ? one : p4 == 1 ? mk2<T2>(r, -r) : p4 == 2 ? mk2<T2>(T(0), T(-1)) : mk2<T2>(-r, -r);
+    const T2 f2 = p2 == 0 ? one : mk2<T2>(T(0), T(-1));
+    const T s4 = (t & 4) ? T(-1) : T(1), s2 = (t & 2) ? T(-1) : T(1), s1 = (t & 1) ? T(-1) : T(1);
+    const T2 w4 = (t & 4) ? f4 : one, w2 = (t & 2) ? f2 : one;
+    // inverse (DIT) twiddles W8^{+p4}, W4^{+p2} applied by the upper lane
+    const T2 c4 = mk2<T2>(f4.x, -f4.y), c2 = mk2<T2>(f2.x, -f2.y);
+    int inoff[5], nidx[5], outoff[5];
+    {
+        int n = 1, o = 1;
+        for (int i = 0; i < t; ++i) { n = (n * 6) % 41; o = (o * 7) % 41; }
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            nidx[q] = n;
+            inoff[q] = n * nb * sp;
+            outoff[q] = o * Ns * sp;
+            n = (n * 10) % 41;
+            o = (o * 37) % 41;
+        }
+    }
     const int items = nl * nb;
     for (int it = group; it < items; it += ngroups) {
         int j, l;
@@ -256,17 +274,15 @@ __device__ void stage_rader41(const cplx_t<T> *src, cplx_t<T> *dst, const StageP
         else { l = it & (nl - 1); j = it >> lgnl; }
         const int jq = (int)st.fNs.div((unsigned)j);
         const int k = j - jq * Ns;
-        const T2 *sb = src + l * sl;
+        const T2 *sb = src + l * sl + j * sp;
         T2 v[5];
-        int n = g6;
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
-            T2 x = sb[(j + n * nb) * sp];
-            if (Ns > 1) x = twmul<DIR>(x, tw[n * k * m]);
+            T2 x = sb[inoff[q]];
+            if (Ns > 1) x = twmul<DIR>(x, tw[nidx[q] * k * m]);
             v[q] = x;
-            n = (n * 10) % 41;
         }
-        const T2 x0 = sb[j * sp];
+        const T2 x0 = sb[0];
         // X_0 = x_0 + sum over the 40 permuted inputs
         T2 s = cadd(cadd(cadd(v[0], v[1]), cadd(v[2], v[3])), v[4]);
         s = cadd(s, shfl_x(s, 1, gmask));
@@ -278,34 +294,34 @@ __device__ void stage_rader41(const cplx_t<T> *src, cplx_t<T> *dst, const StageP
         for (int q = 1; q < 5; ++q) v[q] = cmul(v[q], W[q]);
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
+            // DIF: lower a + b, upper (a - b) w  ==  (partner + sign * own) * w_lane
             T2 u = shfl_x(v[q], 4, gmask);
-            v[q] = (t & 4) ? cmul(csub(u, v[q]), f4) : cadd(v[q], u);
+            v[q] = cmul(mk2<T2>(u.x + s4 * v[q].x, u.y + s4 * v[q].y), w4);
             u = shfl_x(v[q], 2, gmask);
-            v[q] = (t & 2) ? cmul(csub(u, v[q]), f2) : cadd(v[q], u);
+            v[q] = cmul(mk2<T2>(u.x + s2 * v[q].x, u.y + s2 * v[q].y), w2);
             u = shfl_x(v[q], 1, gmask);
-            v[q] = (t & 1) ? csub(u, v[q]) : cadd(v[q], u);
+            v[q] = mk2<T2>(u.x + s1 * v[q].x, u.y + s1 * v[q].y);
             v[q] = cmul(v[q], Bk[q]);
-            // inverse cross-lane DFT8 (DIT, bit-reversed in, natural out)
-            u = shfl_x(v[q], 1, gmask);
-            v[q] = (t & 1) ? csub(u, v[q]) : cadd(v[q], u);
-            u = shfl_x(v[q], 2, gmask);
-            v[q] = (t & 2) ? csub(u, cmulconj(v[q], f2)) : cadd(v[q], cmulconj(u, f2));
-            u = shfl_x(v[q], 4, gmask);
-            v[q] = (t & 4) ? csub(u, cmulconj(v[q], f4)) : cadd(v[q], cmulconj(u, f4));
+            // inverse DIT (bit-reversed in, natural out): the upper lane sends
+            // w b; lower: a + (w b), upper: a - (w b)
+            T2 sv = v[q];                                  // span 1: w = 1
+            u = shfl_x(sv, 1, gmask);
+            v[q] = (t & 1) ? csub(u, sv) : cadd(v[q], u);
+            sv = (t & 2) ? cmul(v[q], c2) : v[q];
+            u = shfl_x(sv, 2, gmask);
+            v[q] = (t & 2) ? csub(u, sv) : cadd(v[q], u);
+            sv = (t & 4) ? cmul(v[q], c4) : v[q];
+            u = shfl_x(sv, 4, gmask);
+            v[q] = (t & 4) ? csub(u, sv) : cadd(v[q], u);
         }
 #pragma unroll
         for (int q = 1; q < 5; ++q) v[q] = cmulconj(v[q], W[q]);
         bfly5<T, +1>(v);
         // outputs X[7^(t+8m)] = x0 + c[t+8m]
-        T2 *db = dst + l * sl;
-        const int base = jq * Ns * 41 + k;
-        int o = g7;
+        T2 *db = dst + l * sl + (jq * Ns * 41 + k) * sp;
 #pragma unroll
-        for (int q = 0; q < 5; ++q) {
-            db[(base + o * Ns) * sp] = cadd(x0, v[q]);
-            o = (o * 37) % 41;
-        }
-        if (t == 0) db[base * sp] = cadd(x0, s);
+        for (int q = 0; q < 5; ++q) db[outoff[q]] = cadd(x0, v[q]);
+        if (t == 0) db[0] = cadd(x0, s);
     }
 }
 
@@ -581,7 +597,30 @@ k_zpass(Grid3 g, AxisPlan plan, const cplx_t<T> *tw_g, int R, Op op) {
     const int rcnt = (int)min((long long)R, nrows - row0);
     load_tw<T>(tw, tw_g, n);
 
-    if (NFI > 0) {
+    auto pack = [&](int p, int k, T2 A, T2 B) {
+        if (k == 0 || 2 * k == n) { A.y = T(0); B.y = T(0); }
+        // Z_k = A_k + i B_k ; Z_{n-k} = conj(A_k) + i conj(B_k)
+        inA[p * n + k] = mk2<T2>(A.x - B.y, A.y + B.x);
+        if (k > 0 && 2 * k != n) inA[p * n + (n - k)] = mk2<T2>(A.x + B.y, B.x - A.y);
+    };
+    if (NFI > 0 && (NFI % 2) == 0) {
+        // even field count: the pairs of a row are (f0,f1), (f2,f3), ...;
+        // each (row, k) is loaded once
+        for (int e = threadIdx.x; e < R * nc; e += blockDim.x) {
+            const int rr = e / nc, k = e - rr * nc;
+            T2 v[NFI > 0 ? NFI : 1];
+            if (rr < rcnt) op.load_spec(row0 + rr, k, v);
+            else {
+#pragma unroll
+                for (int f = 0; f < NFI; ++f) v[f] = mk2<T2>(T(0), T(0));
+            }
+#pragma unroll
+            for (int f = 0; f < NFI / 2; ++f) pack(rr * (NFI / 2) + f, k, v[2 * f], v[2 * f + 1]);
+        }
+        __syncthreads();
+        T2 *r = fft_lines<T, +1>(inA, inB, plan, tw, PI_, 1, n, true);
+        if (r != inA) { inB = inA; inA = r; }
+    } else if (NFI > 0) {
         // pack pairs of half spectra into full complex spectra
         for (int e = threadIdx.x; e < PI_ * nc; e += blockDim.x) {
             const int p = e / nc, k = e - p * nc;
@@ -599,10 +638,7 @@ k_zpass(Grid3 g, AxisPlan plan, const cplx_t<T> *tw_g, int R, Op op) {
                 op.load_spec(row0 + rb, k, v);
                 B = v[fb];
             }
-            if (k == 0 || 2 * k == n) { A.y = T(0); B.y = T(0); }
-            // Z_k = A_k + i B_k ; Z_{n-k} = conj(A_k) + i conj(B_k)
-            inA[p * n + k] = mk2<T2>(A.x - B.y, A.y + B.x);
-            if (k > 0 && 2 * k != n) inA[p * n + (n - k)] = mk2<T2>(A.x + B.y, B.x - A.y);
+            pack(p, k, A, B);
         }
         __syncthreads();
         T2 *r = fft_lines<T, +1>(inA, inB, plan, tw, PI_, 1, n, true);
