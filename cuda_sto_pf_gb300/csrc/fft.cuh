@@ -228,6 +228,7 @@ __device__ void stage_rader41(const cplx_t<T> *src, cplx_t<T> *dst, const StageP
                               const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast, int lgnl) {
     using T2 = cplx_t<T>;
     const int nb = st.nb, Ns = st.Ns, m = st.m;
+    const FastDiv fnb = st.fnb, fNs = st.fNs;     // register copies
     const int t = threadIdx.x & 7;
     const int group = threadIdx.x >> 3, ngroups = blockDim.x >> 3;
     const unsigned gmask = 0xffu << (threadIdx.x & 24);
@@ -270,9 +271,9 @@ __device__ void stage_rader41(const cplx_t<T> *src, cplx_t<T> *dst, const StageP
     const int items = nl * nb;
     for (int it = group; it < items; it += ngroups) {
         int j, l;
-        if (lineFast) { l = (int)st.fnb.div((unsigned)it); j = it - l * nb; }
+        if (lineFast) { l = (int)fnb.div((unsigned)it); j = it - l * nb; }
         else { l = it & (nl - 1); j = it >> lgnl; }
-        const int jq = (int)st.fNs.div((unsigned)j);
+        const int jq = (int)fNs.div((unsigned)j);
         const int k = j - jq * Ns;
         const T2 *sb = src + l * sl + j * sp;
         T2 v[5];
@@ -333,12 +334,13 @@ __device__ __forceinline__ void stage_bfly(const cplx_t<T> *src, cplx_t<T> *dst,
                                            int lgnl) {
     using T2 = cplx_t<T>;
     const int nb = st.nb, Ns = st.Ns, m = st.m;
+    const FastDiv fnb = st.fnb, fNs = st.fNs;     // register copies
     const int work = nl * nb;
     for (int w = threadIdx.x; w < work; w += blockDim.x) {
         int j, l;
-        if (lineFast) { l = (int)st.fnb.div((unsigned)w); j = w - l * nb; }
+        if (lineFast) { l = (int)fnb.div((unsigned)w); j = w - l * nb; }
         else { l = w & (nl - 1); j = w >> lgnl; }
-        const int jq = (int)st.fNs.div((unsigned)j);
+        const int jq = (int)fNs.div((unsigned)j);
         const int k = j - jq * Ns;
         T2 v[R];
         const T2 *sb = src + l * sl;
@@ -368,13 +370,14 @@ __device__ void stage_direct(const cplx_t<T> *src, cplx_t<T> *dst, const StagePl
                              const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast, int lgnl) {
     using T2 = cplx_t<T>;
     const int R = st.R, nb = st.nb, Ns = st.Ns, m = st.m;
+    const FastDiv fnb = st.fnb, fNs = st.fNs;
     const int work = nl * n;
     for (int w = threadIdx.x; w < work; w += blockDim.x) {
         int o, l;
         if (lineFast) { l = w / n; o = w - l * n; } else { l = w & (nl - 1); o = w >> lgnl; }
-        const int q = (int)st.fnb.div((unsigned)o);
+        const int q = (int)fnb.div((unsigned)o);
         const int j = o - q * nb;
-        const int jq = (int)st.fNs.div((unsigned)j);
+        const int jq = (int)fNs.div((unsigned)j);
         const int k = j - jq * Ns;
         int e = k * m + q * nb;
         if (e >= n) e -= n;
@@ -402,13 +405,13 @@ __device__ void stage_direct(const cplx_t<T> *src, cplx_t<T> *dst, const StagePl
 // Must be called by all threads of the block; ends with __syncthreads().
 // ---------------------------------------------------------------------------
 template <typename T, int DIR>
-__device__ __noinline__ cplx_t<T> *fft_lines(cplx_t<T> *a, cplx_t<T> *b, const AxisPlan &p,
-                                             const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast) {
+__device__ __forceinline__ cplx_t<T> *fft_lines(cplx_t<T> *a, cplx_t<T> *b, const AxisPlan &p,
+                                                const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast) {
     using T2 = cplx_t<T>;
     const int lgnl = lineFast ? 0 : (__ffs(nl) - 1);
     T2 *src = a, *dst = b;
     for (int s = 0; s < p.nst; ++s) {
-        const StagePlan &st = p.st[s];
+        const StagePlan st = p.st[s];
         switch (st.R) {
             case 2: stage_bfly<T, DIR, 2>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
             case 3: stage_bfly<T, DIR, 3>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
