@@ -31,7 +31,7 @@ struct FastDiv {
     unsigned M;
     int L;
     unsigned d;
-    __host__ void init(unsigned dd) {
+    __host__ __device__ void init(unsigned dd) {
         d = dd;
         if (d <= 1) { M = 0; L = 0; return; }
         L = 0;
@@ -225,7 +225,7 @@ __device__ __forceinline__ T2 shfl_x(T2 v, int m, unsigned mask) {
 
 template <typename T, int DIR>
 __device__ void stage_rader41(const cplx_t<T> *src, cplx_t<T> *dst, const StagePlan &st,
-                              const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast, int lgnl) {
+                              const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast, const FastDiv &fnl) {
     using T2 = cplx_t<T>;
     const int nb = st.nb, Ns = st.Ns, m = st.m;
     const FastDiv fnb = st.fnb, fNs = st.fNs;     // register copies
@@ -272,7 +272,7 @@ __device__ void stage_rader41(const cplx_t<T> *src, cplx_t<T> *dst, const StageP
     for (int it = group; it < items; it += ngroups) {
         int j, l;
         if (lineFast) { l = (int)fnb.div((unsigned)it); j = it - l * nb; }
-        else { l = it & (nl - 1); j = it >> lgnl; }
+        else { j = (int)fnl.div((unsigned)it); l = it - j * nl; }
         const int jq = (int)fNs.div((unsigned)j);
         const int k = j - jq * Ns;
         const T2 *sb = src + l * sl + j * sp;
@@ -331,7 +331,7 @@ __device__ void stage_rader41(const cplx_t<T> *src, cplx_t<T> *dst, const StageP
 template <typename T, int DIR, int R>
 __device__ __forceinline__ void stage_bfly(const cplx_t<T> *src, cplx_t<T> *dst, const StagePlan &st,
                                            const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast,
-                                           int lgnl) {
+                                           const FastDiv &fnl) {
     using T2 = cplx_t<T>;
     const int nb = st.nb, Ns = st.Ns, m = st.m;
     const FastDiv fnb = st.fnb, fNs = st.fNs;     // register copies
@@ -339,7 +339,7 @@ __device__ __forceinline__ void stage_bfly(const cplx_t<T> *src, cplx_t<T> *dst,
     for (int w = threadIdx.x; w < work; w += blockDim.x) {
         int j, l;
         if (lineFast) { l = (int)fnb.div((unsigned)w); j = w - l * nb; }
-        else { l = w & (nl - 1); j = w >> lgnl; }
+        else { j = (int)fnl.div((unsigned)w); l = w - j * nl; }
         const int jq = (int)fNs.div((unsigned)j);
         const int k = j - jq * Ns;
         T2 v[R];
@@ -367,14 +367,14 @@ __device__ __forceinline__ void stage_bfly(const cplx_t<T> *src, cplx_t<T> *dst,
 // out_q = sum_r x_r W_n^{r (k m + q n/R)}  (exponent mod n)
 template <typename T, int DIR>
 __device__ void stage_direct(const cplx_t<T> *src, cplx_t<T> *dst, const StagePlan &st, int n,
-                             const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast, int lgnl) {
+                             const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast, const FastDiv &fnl) {
     using T2 = cplx_t<T>;
     const int R = st.R, nb = st.nb, Ns = st.Ns, m = st.m;
     const FastDiv fnb = st.fnb, fNs = st.fNs;
     const int work = nl * n;
     for (int w = threadIdx.x; w < work; w += blockDim.x) {
         int o, l;
-        if (lineFast) { l = w / n; o = w - l * n; } else { l = w & (nl - 1); o = w >> lgnl; }
+        if (lineFast) { l = w / n; o = w - l * n; } else { o = (int)fnl.div((unsigned)w); l = w - o * nl; }
         const int q = (int)fnb.div((unsigned)o);
         const int j = o - q * nb;
         const int jq = (int)fNs.div((unsigned)j);
@@ -401,26 +401,27 @@ __device__ void stage_direct(const cplx_t<T> *src, cplx_t<T> *dst, const StagePl
 // Element (line l, position q) lives at buf[q*sp + l*sl].  Stockham stages
 // alternate between `a` and `b`; returns the buffer holding the result.
 // lineFast: consecutive threads walk butterflies of one line (sp == 1);
-// otherwise consecutive threads walk lines (sl == 1, nl a power of two).
+// otherwise consecutive threads walk lines (sl == 1).
 // Must be called by all threads of the block; ends with __syncthreads().
 // ---------------------------------------------------------------------------
 template <typename T, int DIR>
 __device__ __forceinline__ cplx_t<T> *fft_lines(cplx_t<T> *a, cplx_t<T> *b, const AxisPlan &p,
                                                 const cplx_t<T> *tw, int nl, int sp, int sl, bool lineFast) {
     using T2 = cplx_t<T>;
-    const int lgnl = lineFast ? 0 : (__ffs(nl) - 1);
+    FastDiv fnl;
+    fnl.init((unsigned)nl);
     T2 *src = a, *dst = b;
     for (int s = 0; s < p.nst; ++s) {
         const StagePlan st = p.st[s];
         switch (st.R) {
-            case 2: stage_bfly<T, DIR, 2>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
-            case 3: stage_bfly<T, DIR, 3>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
-            case 4: stage_bfly<T, DIR, 4>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
-            case 5: stage_bfly<T, DIR, 5>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
-            case 6: stage_bfly<T, DIR, 6>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
-            case 8: stage_bfly<T, DIR, 8>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
-            case 41: stage_rader41<T, DIR>(src, dst, st, tw, nl, sp, sl, lineFast, lgnl); break;
-            default: stage_direct<T, DIR>(src, dst, st, p.n, tw, nl, sp, sl, lineFast, lgnl); break;
+            case 2: stage_bfly<T, DIR, 2>(src, dst, st, tw, nl, sp, sl, lineFast, fnl); break;
+            case 3: stage_bfly<T, DIR, 3>(src, dst, st, tw, nl, sp, sl, lineFast, fnl); break;
+            case 4: stage_bfly<T, DIR, 4>(src, dst, st, tw, nl, sp, sl, lineFast, fnl); break;
+            case 5: stage_bfly<T, DIR, 5>(src, dst, st, tw, nl, sp, sl, lineFast, fnl); break;
+            case 6: stage_bfly<T, DIR, 6>(src, dst, st, tw, nl, sp, sl, lineFast, fnl); break;
+            case 8: stage_bfly<T, DIR, 8>(src, dst, st, tw, nl, sp, sl, lineFast, fnl); break;
+            case 41: stage_rader41<T, DIR>(src, dst, st, tw, nl, sp, sl, lineFast, fnl); break;
+            default: stage_direct<T, DIR>(src, dst, st, p.n, tw, nl, sp, sl, lineFast, fnl); break;
         }
         __syncthreads();
         T2 *t = src; src = dst; dst = t;
@@ -443,15 +444,19 @@ struct Grid3 {
 // ---------------------------------------------------------------------------
 // Strided axis pass (y or x).  A block owns TK consecutive kz columns of one
 // (i) slab (y pass) or one (j) slab (x pass): lines of length n, element
-// stride `es`.  Inputs are transformed with direction DIN (0 = none),
-// combined point by point by op.apply(i, j, k, vin, vout), and outputs are
-// transformed with DOUT (0 = none) and stored.
+// stride `es`.  All NIN arrays of the tile sit interleaved in one shared
+// buffer (row q holds NIN*TK values, array-major, padded by one) and are
+// transformed together by a single batched FFT with direction DIN (0 =
+// none); op.apply(i, j, k, vin, vout) combines them point by point; the NOUT
+// outputs are transformed together with DOUT (0 = none) and stored.
 // ---------------------------------------------------------------------------
 template <typename T, int NIN, int NOUT>
 struct AxisIO {
     const cplx_t<T> *in[NIN > 0 ? NIN : 1];
     cplx_t<T> *out[NOUT > 0 ? NOUT : 1];
 };
+
+template <int NIN, int NOUT> constexpr int axis_width() { return NIN > NOUT ? NIN : NOUT; }
 
 template <typename T, int NIN, int NOUT, int DIN, int DOUT, class Op>
 __global__ void __launch_bounds__(256)
@@ -460,19 +465,13 @@ k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
     using T2 = cplx_t<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2 *sm = reinterpret_cast<T2 *>(smem_raw);
+    constexpr int NW = axis_width<NIN, NOUT>();
     const int n = plan.n;
-    T2 *tw = sm;                       // n
-    T2 *bufs = sm + n;                 // (NIN + NOUT + 1) * n * (TK + 1)
-    const int TKP = TK + 1;            // padded row stride: spreads rows over banks
-    const int tile = n * TKP;
-    T2 *bin[NIN > 0 ? NIN : 1];
-    T2 *bout[NOUT > 0 ? NOUT : 1];
-    constexpr bool INPL = Op::kInplace;   // identity op: outputs reuse inputs
-#pragma unroll
-    for (int a = 0; a < NIN; ++a) bin[a] = bufs + a * tile;
-#pragma unroll
-    for (int a = 0; a < NOUT; ++a) bout[a] = INPL ? bin[a] : bufs + (NIN + a) * tile;
-    T2 *scr = bufs + (INPL ? NIN : NIN + NOUT) * tile;
+    const int SPI = NIN * TK + 1, SPO = NOUT * TK + 1;   // padded row strides
+    const int buf = n * (NW * TK + 1);
+    T2 *tw = sm;
+    T2 *A = sm + n, *B = A + buf;
+    constexpr bool INPL = Op::kInplace;   // identity op: outputs are the inputs
 
     const int k0 = blockIdx.x * TK;
     const int slab = blockIdx.y;       // i for the y pass, j for the x pass
@@ -488,24 +487,18 @@ k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
         for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
             const int q = e >> lgTK, l = e & (TK - 1);
             const bool ok = l < kcnt;
-            cp_async_elem(&bin[a][q * TKP + l], io.in[a] + (ok ? base + q * es + l : base), ok);
+            cp_async_elem(&A[q * SPI + a * TK + l], io.in[a] + (ok ? base + q * es + l : base), ok);
         }
     }
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
+    T2 *cur = A, *oth = B;
     if (DIN != 0) {
-#pragma unroll
-        for (int a = 0; a < NIN; ++a) {
-            T2 *r = fft_lines<T, DIN>(bin[a], scr, plan, tw, TK, TKP, 1, false);
-            if (r == scr) { scr = bin[a]; bin[a] = r; }
-        }
+        T2 *r = fft_lines<T, DIN>(cur, oth, plan, tw, NIN * TK, SPI, 1, false);
+        if (r != cur) { oth = cur; cur = r; }
     }
-    if constexpr (INPL) {
-        static_assert(NIN == NOUT, "in-place axis op needs NIN == NOUT");
-#pragma unroll
-        for (int a = 0; a < NOUT; ++a) bout[a] = bin[a];
-    }
+    int SP = SPI;
     if constexpr (!INPL) {
         for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
             const int q = e >> lgTK, l = e & (TK - 1);
@@ -514,25 +507,24 @@ k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
             const int j = (axis == 1) ? q : slab;
             T2 vin[NIN > 0 ? NIN : 1], vout[NOUT > 0 ? NOUT : 1];
 #pragma unroll
-            for (int a = 0; a < NIN; ++a) vin[a] = bin[a][q * TKP + l];
+            for (int a = 0; a < NIN; ++a) vin[a] = cur[q * SPI + a * TK + l];
             op.apply(i, j, k, vin, vout);
 #pragma unroll
-            for (int a = 0; a < NOUT; ++a) bout[a][q * TKP + l] = vout[a];
+            for (int a = 0; a < NOUT; ++a) oth[q * SPO + a * TK + l] = vout[a];
         }
         __syncthreads();
+        T2 *t = cur; cur = oth; oth = t;
+        SP = SPO;
     }
     if (DOUT != 0) {
-#pragma unroll
-        for (int a = 0; a < NOUT; ++a) {
-            T2 *r = fft_lines<T, DOUT>(bout[a], scr, plan, tw, TK, TKP, 1, false);
-            if (r == scr) { scr = bout[a]; bout[a] = r; }
-        }
+        T2 *r = fft_lines<T, DOUT>(cur, oth, plan, tw, NOUT * TK, SP, 1, false);
+        if (r != cur) { oth = cur; cur = r; }
     }
 #pragma unroll
     for (int a = 0; a < NOUT; ++a) {
         for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
             const int q = e >> lgTK, l = e & (TK - 1);
-            if (l < kcnt) io.out[a][base + q * es + l] = bout[a][q * TKP + l];
+            if (l < kcnt) io.out[a][base + q * es + l] = cur[q * SP + a * TK + l];
         }
     }
 }

@@ -134,11 +134,12 @@ static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, O
     using T2 = cplx_t<T>;
     const AxisPlan &pl = axis == 1 ? c->ply : c->plx;
     const int n = pl.n;
-    const int nbuf = Op::kInplace ? NIN + 1 : NIN + NOUT + 1;
+    constexpr int NW = axis_width<NIN, NOUT>();
+    auto bytes = [&](int tk) { return ((size_t)n + 2 * (size_t)n * (NW * tk + 1)) * sizeof(T2); };
     int TK = 16;
-    while (TK > 1 && ((size_t)n + (size_t)nbuf * n * (TK + 1)) * sizeof(T2) > kSmemBudget) TK >>= 1;
+    while (TK > 1 && bytes(TK) > kSmemBudget) TK >>= 1;
     while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
-    const size_t smem = ((size_t)n + (size_t)nbuf * n * (TK + 1)) * sizeof(T2);
+    const size_t smem = bytes(TK);
     auto kern = k_axis_pass<T, NIN, NOUT, DIN, DOUT, Op>;
     PFGB_CUDA_TRY(allow_smem(kern, smem));
     dim3 grid((c->g.NzC + TK - 1) / TK, axis == 1 ? c->g.Nx : c->g.Ny);
@@ -700,76 +701,65 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
     using T2 = cplx_t<TE>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2 *sm = reinterpret_cast<T2 *>(smem_raw);
-    const int n = plan.n, TKP = TK + 1, tile = n * TKP;   // padded row stride
+    const int n = plan.n, SP = 6 * TK + 1;   // six components interleaved per row
     T2 *tw = sm;
-    T2 *acc[3] = {sm + n, sm + n + tile, sm + n + 2 * tile};
-    // ld[0..1]: double-buffered component loads; wk: FFT ping-pong partner
-    T2 *ld[2] = {sm + n + 3 * tile, sm + n + 4 * tile};
-    T2 *wk = sm + n + 5 * tile;
+    T2 *X = sm + n, *Yb = X + n * SP;
     const int k0 = blockIdx.x * TK, j = blockIdx.y;
     const long long base = (long long)j * A.g.NzC + k0;
     const long long es = (long long)A.g.Ny * A.g.NzC;
     const int kcnt = min(TK, A.g.NzC - k0);
     const int lgTK = __ffs(TK) - 1;
-    auto issue = [&](int cmp, T2 *dst) {
+#pragma unroll
+    for (int cmp = 0; cmp < 6; ++cmp) {
         for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
             const int q = e >> lgTK, l = e & (TK - 1);
             const bool ok = l < kcnt;
-            cp_async_elem(&dst[q * TKP + l], A.E[cmp] + (ok ? base + q * es + l : base), ok);
+            cp_async_elem(&X[q * SP + cmp * TK + l], A.E[cmp] + (ok ? base + q * es + l : base), ok);
         }
-        cp_async_commit();
-    };
-    issue(0, ld[0]);
+    }
+    cp_async_commit();
     load_tw<TE>(tw, A.tw, n);
-    for (int e = threadIdx.x; e < 3 * tile; e += blockDim.x) acc[e / tile][e % tile] = mk2<T2>(TE(0), TE(0));
-    for (int cmp = 0; cmp < 6; ++cmp) {
-        T2 *cur = ld[cmp & 1];
-        if (cmp + 1 < 6) {
-            issue(cmp + 1, ld[(cmp + 1) & 1]);   // prefetch the next component
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
-        __syncthreads();
-        T2 *r = fft_lines<TE, -1>(cur, wk, plan, tw, TK, TKP, 1, false);
-        if (r == wk) { wk = cur; ld[cmp & 1] = r; }   // keep three distinct buffers
-        // accumulate t_i += k_j tau_ij
-        const int a = cmp < 3 ? cmp : (cmp == 3 ? 1 : 0);
-        const int b = cmp < 3 ? cmp : (cmp == 5 ? 1 : 2);
-        for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
-            const int q = e0 >> lgTK, l = e0 & (TK - 1);
-            const int e = q * TKP + l;
-            const TE kv[3] = {TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[min(k0 + l, A.g.NzC - 1)])};
-            const T2 x = r[e];
-            if (EIGEN) {
-                // tau_ij = C_ij,ab eps0_ab ; component (a,b) enters with
-                // weight 1 (normal) or 2 (shear) in Voigt column cmp
-                const TE f = cmp < 3 ? TE(1) : TE(2);
+    cp_async_wait_all();
+    __syncthreads();
+    T2 *cur = fft_lines<TE, -1>(X, Yb, plan, tw, 6 * TK, SP, 1, false);
+    T2 *oth = (cur == X) ? Yb : X;
+    // per point: t_i = k_j tau_ij, u = -i G t (masked), residual, u stored,
+    // then the six strain components of u into the other buffer
+    double rd = 0.0, rr = 0.0;
+    for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
+        const int q = e >> lgTK, l = e & (TK - 1), k = k0 + l;
+        const int kk = min(k, A.g.NzC - 1);
+        const TE kv[3] = {TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[kk])};
+        T2 x[6];
 #pragma unroll
-                for (int ii = 0; ii < 3; ++ii) {
+        for (int c = 0; c < 6; ++c) x[c] = cur[q * SP + c * TK + l];
+        T2 t[3];
+        if (EIGEN) {
+            // tau_ij = C_ij,ab eps0_ab: component c enters with weight 1
+            // (normal) or 2 (shear) in Voigt column c
+#pragma unroll
+            for (int ii = 0; ii < 3; ++ii) {
+                T2 acc = mk2<T2>(TE(0), TE(0));
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
                     TE s = 0;
 #pragma unroll
-                    for (int jj = 0; jj < 3; ++jj) s += kv[jj] * A.ec.S[vidx(tvoigt(ii, jj), cmp)];
-                    acc[ii][e] = cadd(acc[ii][e], cscale(x, f * s));
+                    for (int jj = 0; jj < 3; ++jj) s += kv[jj] * A.ec.S[vidx(tvoigt(ii, jj), c)];
+                    acc = cadd(acc, cscale(x[c], (c < 3 ? TE(1) : TE(2)) * s));
                 }
-            } else {
-                acc[a][e] = cadd(acc[a][e], cscale(x, kv[b]));
-                if (a != b) acc[b][e] = cadd(acc[b][e], cscale(x, kv[a]));
+                t[ii] = acc;
             }
+        } else {
+            // symmetric h (xx, yy, zz, yz, xz, xy): t_i = k_x h_xi + k_y h_yi + k_z h_zi
+            t[0] = cadd(cadd(cscale(x[0], kv[0]), cscale(x[5], kv[1])), cscale(x[4], kv[2]));
+            t[1] = cadd(cadd(cscale(x[5], kv[0]), cscale(x[1], kv[1])), cscale(x[3], kv[2]));
+            t[2] = cadd(cadd(cscale(x[4], kv[0]), cscale(x[3], kv[1])), cscale(x[2], kv[2]));
         }
-        __syncthreads();
-    }
-    // u = -i G t, masked; residual; store u
-    double rd = 0.0, rr = 0.0;
-    for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
-        const int q = e0 >> lgTK, l = e0 & (TK - 1), k = k0 + l;
-        const int e = q * TKP + l;
         T2 u[3];
         if (l >= kcnt || A.kt.cut(q, j, k) || (q == 0 && j == 0 && k == 0)) {
             u[0] = u[1] = u[2] = mk2<T2>(TE(0), TE(0));
         } else {
-            const T2 t[3] = {acc[0][e], acc[1][e], acc[2][e]};
-            green_u<TE>(A.ec.S, TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[k]), t, u);
+            green_u<TE>(A.ec.S, kv[0], kv[1], kv[2], t, u);
         }
         if (l < kcnt) {
             const long long o = base + q * es + l;
@@ -790,7 +780,7 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
             for (int c = 0; c < 3; ++c) A.U[c][o] = u[c];
         }
 #pragma unroll
-        for (int c = 0; c < 3; ++c) acc[c][e] = u[c];
+        for (int c = 0; c < 6; ++c) oth[q * SP + c * TK + l] = strain_comp<TE>(c, kv[0], kv[1], kv[2], u);
     }
     if (A.resid) {
         AccSum2 s{rd, rr};
@@ -799,23 +789,13 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
             reinterpret_cast<AccSum2 *>(A.partials)[blockIdx.y * gridDim.x + blockIdx.x] = s;
     }
     __syncthreads();
-    // strain components -> inverse x -> store
-    T2 *w0 = ld[0], *w1 = ld[1];
+    T2 *r = fft_lines<TE, +1>(oth, cur, plan, tw, 6 * TK, SP, 1, false);
+#pragma unroll
     for (int cmp = 0; cmp < 6; ++cmp) {
-        for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
-            const int q = e0 >> lgTK, l = e0 & (TK - 1);
-            const int e = q * TKP + l;
-            const int k = min(k0 + l, A.g.NzC - 1);
-            const T2 u[3] = {acc[0][e], acc[1][e], acc[2][e]};
-            w0[e] = strain_comp<TE>(cmp, TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[k]), u);
+        for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
+            const int q = e >> lgTK, l = e & (TK - 1);
+            if (l < kcnt) A.E[cmp][base + q * es + l] = r[q * SP + cmp * TK + l];
         }
-        __syncthreads();
-        T2 *r = fft_lines<TE, +1>(w0, w1, plan, tw, TK, TKP, 1, false);
-        for (int e0 = threadIdx.x; e0 < n * TK; e0 += blockDim.x) {
-            const int q = e0 >> lgTK, l = e0 & (TK - 1);
-            if (l < kcnt) A.E[cmp][base + q * es + l] = r[q * TKP + l];
-        }
-        __syncthreads();
     }
 }
 
@@ -829,10 +809,11 @@ template <typename TE>
 static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks) {
     using T2 = cplx_t<TE>;
     const int n = c->plx.n;
+    auto bytes = [&](int tk) { return ((size_t)n + 2 * (size_t)n * (6 * tk + 1)) * sizeof(T2); };
     int TK = 16;
-    while (TK > 1 && ((size_t)n + 6 * (size_t)n * (TK + 1)) * sizeof(T2) > kSmemBudget) TK >>= 1;
+    while (TK > 1 && bytes(TK) > kSmemBudget) TK >>= 1;
     while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
-    const size_t smem = ((size_t)n + 6 * (size_t)n * (TK + 1)) * sizeof(T2);
+    const size_t smem = bytes(TK);
     GreenArgs<TE> A;
     A.g = c->g;
     A.kt = KTab{c->kx, c->ky, c->kz, c->mx, c->my, c->mz};
