@@ -585,8 +585,11 @@ k_zpass(Grid3 g, AxisPlan plan, const cplx_t<T> *tw_g, int R, Op op) {
     T2 *ws = sm + n;
     const int PI_ = (NFI > 0) ? (R * NFI + 1) / 2 : 0;
     const int PO_ = (NFO > 0) ? (R * NFO + 1) / 2 : 0;
+    // NFI == NFO: the pointwise stage runs in place on the C2R result (same
+    // line layout), so two buffers suffice
+    constexpr bool SAME = (NFI == NFO);
     T2 *inA = ws, *inB = ws + PI_ * n;
-    T2 *outA = ws + 2 * PI_ * n, *outB = outA + PO_ * n;
+    T2 *outA = SAME ? nullptr : ws + 2 * PI_ * n, *outB = SAME ? nullptr : outA + PO_ * n;
     const long long row0 = (long long)blockIdx.x * R;
     const long long nrows = (long long)g.Nx * g.Ny;
     const int rcnt = (int)min((long long)R, nrows - row0);
@@ -639,6 +642,7 @@ k_zpass(Grid3 g, AxisPlan plan, const cplx_t<T> *tw_g, int R, Op op) {
         T2 *r = fft_lines<T, +1>(inA, inB, plan, tw, PI_, 1, n, true);
         if (r != inA) { inB = inA; inA = r; }
     }
+    if constexpr (SAME) { outA = inA; outB = inB; }
     // pointwise stage
     typename Op::Acc acc = Op::Acc::identity();
     for (int e = threadIdx.x; e < R * n; e += blockDim.x) {

@@ -71,6 +71,7 @@ struct pfgb_ctx {
     double *stage = nullptr;          // host<->device staging, 5 N doubles, lazily allocated
     size_t npartials = 0;
     double Yc = 0.0, dYoff = 0.0, target_mass = 0.0;
+    double sum_alpha = 0.0;   // sum (1 - h) of the last phi (zero-mode curvature bound)
     int warm_valid = 0, step = 0, loaded = 0;
     size_t bytes = 0;
     std::string err;
@@ -156,9 +157,10 @@ static pfgb_status launch_z(pfgb_ctx *c, Op op, const char *tag, double extra_by
     const int n = c->g.Nz;
     auto bytes = [&](int R) {
         int PI_ = NFI > 0 ? (R * NFI + 1) / 2 : 0, PO_ = NFO > 0 ? (R * NFO + 1) / 2 : 0;
+        if (NFI == NFO) PO_ = 0;   // in-place pointwise stage
         return ((size_t)n + 2 * (size_t)PI_ * n + 2 * (size_t)PO_ * n) * sizeof(T2);
     };
-    int R = 16;
+    int R = 64;
     while (R > 2 && bytes(R) > kSmemBudget) R >>= 1;
     const long long rows = (long long)c->g.Nx * c->g.Ny;
     while (R > 2 && R / 2 >= rows) R >>= 1;
@@ -200,15 +202,16 @@ struct AccSum2 {
 };
 // zero-mode statistics: min, max of Y*, and the Taylor moments
 // M_p = sum (1-h) sigma^{(p)}(Y*) (M_0 also + h v_B), p = 0..4
+// (m[5] = sum |1 - h|, the curvature bound of the zero-mode certification)
 struct AccZM {
     static constexpr bool kActive = true;
-    double mn, mx, m[5];
-    __device__ static AccZM identity() { return {1e300, -1e300, {0, 0, 0, 0, 0}}; }
+    double mn, mx, m[6];
+    __device__ static AccZM identity() { return {1e300, -1e300, {0, 0, 0, 0, 0, 0}}; }
     __device__ static AccZM combine(AccZM x, const AccZM &y) {
         x.mn = fmin(x.mn, y.mn);
         x.mx = fmax(x.mx, y.mx);
 #pragma unroll
-        for (int i = 0; i < 5; ++i) x.m[i] += y.m[i];
+        for (int i = 0; i < 6; ++i) x.m[i] += y.m[i];
         return x;
     }
     __device__ static AccZM shfl_down(AccZM x, int o) {
@@ -216,7 +219,7 @@ struct AccZM {
         r.mn = __shfl_down_sync(0xffffffffu, x.mn, o);
         r.mx = __shfl_down_sync(0xffffffffu, x.mx, o);
 #pragma unroll
-        for (int i = 0; i < 5; ++i) r.m[i] = __shfl_down_sync(0xffffffffu, x.m[i], o);
+        for (int i = 0; i < 6; ++i) r.m[i] = __shfl_down_sync(0xffffffffu, x.m[i], o);
         return r;
     }
 };
@@ -500,6 +503,7 @@ struct OpYFinalZ {
             acc.m[2] += double(a * s1 * u);
             acc.m[3] += double(a * s1 * (T(1) - T(6) * s1));
             acc.m[4] += double(a * s1 * u * (T(1) - T(12) * s1));
+            acc.m[5] += fabs(1.0 - pf_h(double(d.phi_new[cell])));
         }
     }
     __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
@@ -961,10 +965,11 @@ template <typename T, typename TE>
 static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     const pfgb_params &P = c->p;
     TRY(reduce_to<AccZM>(c, nb_final, DS_ZM));
-    TRY(sync_read(c, DS_MEAN_DY, DS_ZM + 7));   // mean_DY rides along
+    TRY(sync_read(c, DS_MEAN_DY, DS_ZM + 8));   // mean_DY rides along
     const double ymin = c->hscal[DS_ZM], ymax = c->hscal[DS_ZM + 1];
     double M[5];
     for (int i = 0; i < 5; ++i) M[i] = c->hscal[DS_ZM + 2 + i];
+    c->sum_alpha = c->hscal[DS_ZM + 7] * (1.0 + 1e-6);
     const double Ycap = P.Y_clip;
     auto fail = [&](const char *why) {
         pfgb_set_error_msg("PF zero-mode rejected step=%d: %s", c->step + 1, why);
@@ -1048,13 +1053,29 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     double mass = 0, der = 0;
     TRY(direct(&lam, 1, &mass, &der));
     double res = mass - target;
+    // |F''(l)| = |sum (1-h) sigma''| <= sum(1-h) / (6 sqrt 3): after a Newton
+    // step of length d from an exactly evaluated point, |F| <= K2 d^2 / 2
+    // (+ the rounding of the evaluated sum).  When that bound is below tol
+    // the step is accepted without another full-grid evaluation.
+    const double K2 = M[1] > 0.0 ? c->sum_alpha / (6.0 * 1.7320508075688772) : INFINITY;
+    bool certified = false;
     for (int it = 0; it < P.zero_mode_max_iterations && std::fabs(res) > tol; ++it) {
+        const double l0 = lam;
         update(lam, res, der);
+        iters = it + 1;
+        const double d = lam - l0;
+        const double bound = 0.5 * K2 * d * d + 1e-14 * std::fabs(target);
+        if (std::isfinite(bound) && bound <= tol && std::isfinite(der) && der > 0.0 &&
+            std::fabs(res / der - (l0 - lam)) <= 1e-15 * (std::fabs(l0) + 1.0) + std::fabs(d) * 1e-12) {
+            res = bound;            // reported residual: the certified bound
+            certified = true;
+            break;
+        }
         TRY(direct(&lam, 1, &mass, &der));
         if (!std::isfinite(mass) || !std::isfinite(der)) return fail("non-finite mass");
         res = mass - target;
-        iters = it + 1;
     }
+    (void)certified;
     if (std::fabs(res) > tol) return fail("did not converge");
     if (ymin + lam < -P.Y_clip || ymax + lam > Ycap) return fail("shifted Y leaves [-Y_clip, Y_cap]");
     c->Yc += lam;
