@@ -202,20 +202,23 @@ struct AccSum2 {
 };
 // zero-mode statistics: min, max of Y*, and the Taylor moments
 // M_p = sum (1-h) sigma^{(p)}(Y*) (M_0 also + h v_B), p = 0..4
-// (m[5] = sum |1 - h|, the curvature bound of the zero-mode certification)
-struct AccZM {
+// (m[5] = sum |1 - h|, the curvature bound of the zero-mode certification).
+// Per-thread and per-block sums in FP32 (AccZMf, predictor / bound only),
+// block partials widened to FP64 for the grid reduction (AccZM).
+template <typename R>
+struct AccZMt {
     static constexpr bool kActive = true;
-    double mn, mx, m[6];
-    __device__ static AccZM identity() { return {1e300, -1e300, {0, 0, 0, 0, 0, 0}}; }
-    __device__ static AccZM combine(AccZM x, const AccZM &y) {
+    R mn, mx, m[6];
+    __device__ static AccZMt identity() { return {R(3e38), R(-3e38), {0, 0, 0, 0, 0, 0}}; }
+    __device__ static AccZMt combine(AccZMt x, const AccZMt &y) {
         x.mn = fmin(x.mn, y.mn);
         x.mx = fmax(x.mx, y.mx);
 #pragma unroll
         for (int i = 0; i < 6; ++i) x.m[i] += y.m[i];
         return x;
     }
-    __device__ static AccZM shfl_down(AccZM x, int o) {
-        AccZM r;
+    __device__ static AccZMt shfl_down(AccZMt x, int o) {
+        AccZMt r;
         r.mn = __shfl_down_sync(0xffffffffu, x.mn, o);
         r.mx = __shfl_down_sync(0xffffffffu, x.mx, o);
 #pragma unroll
@@ -223,6 +226,7 @@ struct AccZM {
         return r;
     }
 };
+using AccZM = AccZMt<double>;
 
 template <class Acc>
 __global__ void k_reduce_partials(const Acc *part, int n, double *out, int slot, double scale) {
@@ -471,7 +475,7 @@ struct OpYUpdX {
 // (6) final z pass: store Y_f, dY/dt, and the zero-mode statistics
 template <typename T, typename TE>
 struct OpYFinalZ {
-    using Acc = AccZM;
+    using Acc = AccZMt<T>;
     DevState<T, TE> d; PhysC c; const cplx_t<T> *src;
     __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * d.g.NzC + k]; }
     __device__ void point(long long cell, const T *in, T *, Acc &acc) const {
@@ -487,27 +491,33 @@ struct OpYFinalZ {
         d.Y[cell] = y;
         d.dYdt[cell] = (y - Yold) / T(c.dt);
         if (c.zm) {
-            // exact min / max of Y* (they fix the lambda bracket); the Taylor
-            // moments feed only the Newton predictor, so field precision is
-            // enough for them
-            const double ys = double(y) + d.Yc;
-            acc.mn = fmin(acc.mn, ys);
-            acc.mx = fmax(acc.mx, ys);
+            // min / max of the stored Y* (exact: the offset Yc is added after
+            // the reduction); the Taylor moments feed only the Newton
+            // predictor and sum|1-h| only a bound, so field precision is enough
+            acc.mn = fmin(acc.mn, y);
+            acc.mx = fmax(acc.mx, y);
             const T h = pf_h(d.phi_new[cell]);
             const T a = T(1) - h;
-            const T s = sigmoid_raw(T(ys));
+            const T s = sigmoid_raw(y + T(d.Yc));
             const T s1 = s * (T(1) - s);
             const T u = T(1) - T(2) * s;
-            acc.m[0] += double(a * s + h * T(c.vB));
-            acc.m[1] += double(a * s1);
-            acc.m[2] += double(a * s1 * u);
-            acc.m[3] += double(a * s1 * (T(1) - T(6) * s1));
-            acc.m[4] += double(a * s1 * u * (T(1) - T(12) * s1));
-            acc.m[5] += fabs(1.0 - pf_h(double(d.phi_new[cell])));
+            acc.m[0] += a * s + h * T(c.vB);
+            acc.m[1] += a * s1;
+            acc.m[2] += a * s1 * u;
+            acc.m[3] += a * s1 * (T(1) - T(6) * s1);
+            acc.m[4] += a * s1 * u * (T(1) - T(12) * s1);
+            acc.m[5] += fabs(a);
         }
     }
     __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
-    __device__ void finish(int b, const Acc &a) const { reinterpret_cast<Acc *>(d.partials)[b] = a; }
+    __device__ void finish(int b, const Acc &a) const {
+        AccZM w;
+        w.mn = double(a.mn);
+        w.mx = double(a.mx);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) w.m[i] = double(a.m[i]);
+        reinterpret_cast<AccZM *>(d.partials)[b] = w;
+    }
 };
 
 // zero-mode direct evaluation: mass(l) and d mass/dl at given shifts, FP64
@@ -729,7 +739,9 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
     T2 *oth = (cur == X) ? Yb : X;
     // per point: t_i = k_j tau_ij, u = -i G t (masked), residual, u stored,
     // then the six strain components of u into the other buffer
-    double rd = 0.0, rr = 0.0;
+    // residual sums: per element in elastic precision, per-thread partials
+    // (a handful of elements) in elastic precision, block / grid sums in FP64
+    TE rd = 0, rr = 0;
     for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
         const int q = e >> lgTK, l = e & (TK - 1), k = k0 + l;
         const int kk = min(k, A.g.NzC - 1);
@@ -768,14 +780,14 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
         if (l < kcnt) {
             const long long o = base + q * es + l;
             if (A.resid) {
-                const double w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? 1.0 : 2.0;
-                double ld_ = 0, lr = 0;
+                const TE w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? TE(1) : TE(2);
+                TE ld_ = 0, lr = 0;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     const T2 old = A.U[c][o];
-                    const double dr = double(u[c].x) - double(old.x), di = double(u[c].y) - double(old.y);
+                    const TE dr = u[c].x - old.x, di = u[c].y - old.y;
                     ld_ += dr * dr + di * di;
-                    lr += double(u[c].x) * double(u[c].x) + double(u[c].y) * double(u[c].y);
+                    lr += u[c].x * u[c].x + u[c].y * u[c].y;
                 }
                 rd += w * ld_;
                 rr += w * lr;
@@ -787,7 +799,7 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
         for (int c = 0; c < 6; ++c) oth[q * SP + c * TK + l] = strain_comp<TE>(c, kv[0], kv[1], kv[2], u);
     }
     if (A.resid) {
-        AccSum2 s{rd, rr};
+        AccSum2 s{double(rd), double(rr)};
         block_reduce_acc(s);
         if (threadIdx.x == 0)
             reinterpret_cast<AccSum2 *>(A.partials)[blockIdx.y * gridDim.x + blockIdx.x] = s;
@@ -966,10 +978,10 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     const pfgb_params &P = c->p;
     TRY(reduce_to<AccZM>(c, nb_final, DS_ZM));
     TRY(sync_read(c, DS_MEAN_DY, DS_ZM + 8));   // mean_DY rides along
-    const double ymin = c->hscal[DS_ZM], ymax = c->hscal[DS_ZM + 1];
+    const double ymin = c->hscal[DS_ZM] + c->Yc, ymax = c->hscal[DS_ZM + 1] + c->Yc;
     double M[5];
     for (int i = 0; i < 5; ++i) M[i] = c->hscal[DS_ZM + 2 + i];
-    c->sum_alpha = c->hscal[DS_ZM + 7] * (1.0 + 1e-6);
+    c->sum_alpha = c->hscal[DS_ZM + 7] * (1.0 + 1e-4);   // FP32 partial sums: generous margin
     const double Ycap = P.Y_clip;
     auto fail = [&](const char *why) {
         pfgb_set_error_msg("PF zero-mode rejected step=%d: %s", c->step + 1, why);
