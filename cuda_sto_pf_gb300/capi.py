@@ -117,6 +117,7 @@ EXPORTS = [
                                   POINTER(c_int), c_int]),
     ("pfgb_fft3d_r2c", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     ("pfgb_fft3d_c2r", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    ("pfgb_fft3d_r2c_noalloc", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
 ]
 
 _LIB = None

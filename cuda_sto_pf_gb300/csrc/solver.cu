@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1785,6 +1786,108 @@ pfgb_status pfgb_fft3d_c2r(int precision, int Nx, int Ny, int Nz, const void *in
                                         : fft_c2r_impl<float>(&c, (float2 *)in, (float *)out);
     fft_ctx_free(&c);
     return s;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// allocation-free forward transform: twiddle tables in a static device array
+// ---------------------------------------------------------------------------
+// Three tables (x, y, z), each starting on a 256-byte boundary.  Every call
+// rewrites the tables it reads, on its own stream, so no part of the array
+// has to start at zero.  Calls overlapping on one device race on it.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PFGB_NOALLOC_SCRATCH_BYTES];
+
+static constexpr int kNoallocMaxDevices = 64;
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_addr[kNoallocMaxDevices];
+
+static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// w_a[m] = exp(-2 pi i m / n_a), the same table the allocating path uploads
+template <typename T>
+__global__ void k_fill_twiddles(unsigned char *base, int n0, int n1, int n2, size_t off1, size_t off2) {
+    const int a = blockIdx.y;
+    const int n = a == 0 ? n0 : (a == 1 ? n1 : n2);
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    cplx_t<T> *w = (cplx_t<T> *)(base + (a == 0 ? 0 : (a == 1 ? off1 : off2)));
+    double s, co;
+    sincospi(-2.0 * (double)m / (double)n, &s, &co);
+    w[m].x = (T)co;
+    w[m].y = (T)s;
+}
+
+// Address of the scratch array on the calling thread's current device,
+// looked up once per device.
+static pfgb_status noalloc_scratch(unsigned char **out) {
+    int dev = -1;
+    PFGB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoallocMaxDevices) {
+        pfgb_set_error_msg("device ordinal %d beyond the %d supported by the static scratch table", dev,
+                           kNoallocMaxDevices);
+        return PFGB_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        PFGB_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_addr[dev] = p;
+    }
+    *out = (unsigned char *)g_noalloc_addr[dev];
+    return PFGB_OK;
+}
+
+template <typename T>
+static pfgb_status fft_r2c_noalloc(int Nx, int Ny, int Nz, const T *in, cplx_t<T> *out, void *stream) {
+    const size_t off1 = round256(sizeof(cplx_t<T>) * (size_t)Nx);
+    const size_t off2 = off1 + round256(sizeof(cplx_t<T>) * (size_t)Ny);
+    const size_t need = off2 + round256(sizeof(cplx_t<T>) * (size_t)Nz);
+    if (need > PFGB_NOALLOC_SCRATCH_BYTES) {
+        pfgb_set_error_msg("%s transform %dx%dx%d needs %zu bytes of twiddle scratch; the static array holds %d",
+                           sizeof(T) == 8 ? "FP64" : "FP32", Nx, Ny, Nz, need, PFGB_NOALLOC_SCRATCH_BYTES);
+        return PFGB_ERR_INVALID;
+    }
+    unsigned char *base = nullptr;
+    TRY(noalloc_scratch(&base));
+    pfgb_ctx c;
+    c.stream = (cudaStream_t)stream;
+    c.g.Nx = Nx; c.g.Ny = Ny; c.g.Nz = Nz; c.g.NzC = Nz / 2 + 1;
+    c.g.N = (long long)Nx * Ny * Nz;
+    c.g.Nk = (long long)Nx * Ny * c.g.NzC;
+    pfgb_make_plan(Nx, &c.plx);
+    pfgb_make_plan(Ny, &c.ply);
+    pfgb_make_plan(Nz, &c.plz);
+    const int pi = sizeof(T) == 8 ? 0 : 1;
+    c.tw[pi][0] = base;
+    c.tw[pi][1] = base + off1;
+    c.tw[pi][2] = base + off2;
+    const int nmax = std::max(Nx, std::max(Ny, Nz));
+    k_fill_twiddles<T><<<dim3((nmax + 255) / 256, 3), 256, 0, c.stream>>>(base, Nx, Ny, Nz, off1, off2);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    pfgb_status s = fft_r2c_impl<T>(&c, in, out);
+    c.tw[pi][0] = c.tw[pi][1] = c.tw[pi][2] = nullptr;
+    return s;
+}
+
+extern "C" {
+
+pfgb_status pfgb_fft3d_r2c_noalloc(int precision, int Nx, int Ny, int Nz, const void *in, void *out, void *stream) {
+    if (!in || !out) {
+        pfgb_set_error_msg("null device buffer");
+        return PFGB_ERR_INVALID;
+    }
+    if (precision != PFGB_PREC_FP64 && precision != PFGB_PREC_FP32) {
+        pfgb_set_error_msg("precision %d is neither PFGB_PREC_FP64 nor PFGB_PREC_FP32", precision);
+        return PFGB_ERR_INVALID;
+    }
+    if (Nx < 1 || Ny < 1 || Nz < 2 || Nx > PFGB_MAX_N || Ny > PFGB_MAX_N || Nz > PFGB_MAX_N) {
+        pfgb_set_error_msg("transform size %dx%dx%d outside [1..%d] (Nz >= 2)", Nx, Ny, Nz, PFGB_MAX_N);
+        return PFGB_ERR_INVALID;
+    }
+    return precision == PFGB_PREC_FP64
+               ? fft_r2c_noalloc<double>(Nx, Ny, Nz, (const double *)in, (double2 *)out, stream)
+               : fft_r2c_noalloc<float>(Nx, Ny, Nz, (const float *)in, (float2 *)out, stream);
 }
 
 }  // extern "C"

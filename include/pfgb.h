@@ -264,6 +264,33 @@ pfgb_status pfgb_fft3d_r2c(int precision, int Nx, int Ny, int Nz,
 pfgb_status pfgb_fft3d_c2r(int precision, int Nx, int Ny, int Nz,
                            const void *d_in, void *d_out, void *cuda_stream);
 
+/* --- allocation-free forward transform -------------------------------- */
+/* No counterpart in the reference (its transforms go through cuFFT plans
+ * that own their work areas).  Same result as pfgb_fft3d_r2c, but the call
+ * allocates no device memory and never synchronises: the per-axis twiddle
+ * tables are written into a fixed static device array of
+ * PFGB_NOALLOC_SCRATCH_BYTES, one table per axis, each rounded up to 256
+ * bytes: sizeof(complex) * (Nx + Ny + Nz) plus padding, i.e. 16 bytes per
+ * point of Nx+Ny+Nz in FP64 and 8 in FP32.  Larger requests (for example
+ * FP64 with Nx+Ny+Nz above 2048) return PFGB_ERR_INVALID with a message in
+ * pfgb_last_error(NULL); nothing is launched then.
+ *
+ * For callers that cannot allocate on the device: a process whose HBM is
+ * already reserved by its own pool allocator, or a stream pipeline that
+ * must not stall, since cudaMalloc/cudaFree can synchronise the device.
+ *
+ * Nothing in the scratch array has to start at zero: each call rewrites the
+ * tables it uses, on cuda_stream, before the transform reads them.  The
+ * first call on a device (the current device of the calling thread) looks
+ * up the array's address on that device and may load the module; make
+ * that first call before any stream capture.  All calls on one device share
+ * the one array, so calls that overlap in time (other streams, other host
+ * threads) race on it: order them on one stream or synchronise between
+ * them. */
+#define PFGB_NOALLOC_SCRATCH_BYTES 32768
+pfgb_status pfgb_fft3d_r2c_noalloc(int precision, int Nx, int Ny, int Nz,
+                                   const void *d_in, void *d_out, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
