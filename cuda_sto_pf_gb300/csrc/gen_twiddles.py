@@ -57,6 +57,15 @@ def main():
     lines.append(arr("rader41_bi", tables["inv"]))
     lines.append("// W40^e = exp(-2 pi i e / 40)")
     lines.append(arr("w40", w40))
+    # cos / sin (2 pi i / 41): constants of the direct symmetric 41-point DFT
+    lines.append("// cos(2 pi i / 41), sin(2 pi i / 41), i = 0..40")
+    # exactly symmetric: values for i <= 20, mirrored (cos even, sin odd)
+    cs = [cmath.cos(2 * cmath.pi * min(i, P - i) / P).real for i in range(P)]
+    sn = [(1 if i <= P // 2 else -1) * cmath.sin(2 * cmath.pi * min(i, P - i) / P).real for i in range(P)]
+    lines.append("__host__ __device__ constexpr double dft41_cos(int i) {\n"
+                 "    constexpr double t[41] = {" + ", ".join(f"{v:.17e}" for v in cs) + "};\n    return t[i];\n}")
+    lines.append("__host__ __device__ constexpr double dft41_sin(int i) {\n"
+                 "    constexpr double t[41] = {" + ", ".join(f"{v:.17e}" for v in sn) + "};\n    return t[i];\n}")
     # the same B tables as __constant__ arrays for run-time (per-lane) indexing
     for prec, typ, mk in (("d", "double2", "make_double2"), ("f", "float2", "make_float2")):
         for key, nm in (("fwd", "BF"), ("inv", "BI")):

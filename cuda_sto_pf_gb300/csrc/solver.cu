@@ -44,6 +44,7 @@ struct DevState {
     Grid3 g;
     KTab kt;
     T *phi_old, *phi_new, *eta_old, *eta_new, *Y, *dYdt;
+    T *Yprev;           // Y_f at the start of the step (the elastic solve's Y)
     TE *eps[6];
     cplx_t<T> *S[4];
     cplx_t<TE> *E[6], *U[3];
@@ -65,6 +66,7 @@ struct pfgb_ctx {
     double *kx = nullptr, *ky = nullptr, *kz = nullptr;
     unsigned char *mx = nullptr, *my = nullptr, *mz = nullptr;
     void *phi[2] = {nullptr, nullptr}, *eta[2] = {nullptr, nullptr}, *Y = nullptr, *dYdt = nullptr;
+    void *Yprev = nullptr;   // Y_f of the last step's start, for the stress export
     int cur = 0, ecur = 0;
     void *S[4] = {nullptr, nullptr, nullptr, nullptr};
     void *eps[6] = {}, *E[6] = {}, *U[3] = {};
@@ -72,6 +74,7 @@ struct pfgb_ctx {
     double *stage = nullptr;          // host<->device staging, 5 N doubles, lazily allocated
     size_t npartials = 0;
     double Yc = 0.0, dYoff = 0.0, target_mass = 0.0;
+    double Yc_prev = 0.0;    // Yc at the last step's start
     double sum_alpha = 0.0;   // sum (1 - h) of the last phi (zero-mode curvature bound)
     int warm_valid = 0, step = 0, loaded = 0;
     size_t bytes = 0;
@@ -490,6 +493,7 @@ struct OpYFinalZ {
             y = yt - T(d.Yc);
         }
         d.Y[cell] = y;
+        d.Yprev[cell] = Yold;
         d.dYdt[cell] = (y - Yold) / T(c.dt);
         if (c.zm) {
             // min / max of the stored Y* (exact: the offset Yc is added after
@@ -871,6 +875,7 @@ static DevState<T, TE> dev_state(pfgb_ctx *c) {
     d.eta_old = (T *)c->eta[c->ecur];
     d.eta_new = (T *)c->eta[1 - c->ecur];
     d.Y = (T *)c->Y;
+    d.Yprev = (T *)c->Yprev;
     d.dYdt = (T *)c->dYdt;
     for (int i = 0; i < 6; ++i) { d.eps[i] = (TE *)c->eps[i]; d.E[i] = (cplx_t<TE> *)c->E[i]; }
     for (int i = 0; i < 3; ++i) d.U[i] = (cplx_t<TE> *)c->U[i];
@@ -1110,6 +1115,7 @@ static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
     const pfgb_params &P = c->p;
     const PhysC pc = c->pc;
     const ElasC<TE> ec = elas_consts<TE>(c);
+    c->Yc_prev = c->Yc;
     if (P.elastic_enabled) TRY((elastic_solve<T, TE>(c, st)));
     DevState<T, TE> d = dev_state<T, TE>(c);
     const KTab kt = d.kt;
@@ -1165,7 +1171,7 @@ static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
     }
     TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
     int nbf = 0;
-    TRY((launch_z<T, 1, 0>(c, OpYFinalZ<T, TE>{d, pc, d.S[0]}, "z_y_final", (3.0 + pc.zm) * Nf * sizeof(T), &nbf)));
+    TRY((launch_z<T, 1, 0>(c, OpYFinalZ<T, TE>{d, pc, d.S[0]}, "z_y_final", (4.0 + pc.zm) * Nf * sizeof(T), &nbf)));
     c->dYoff = 0.0;
     if (P.zero_mode_enabled) TRY((zero_mode<T, TE>(c, nbf, st)));
     if (st) {
@@ -1312,7 +1318,7 @@ static void ctx_free(pfgb_ctx *c) {
     for (int i = 0; i < 2; ++i) f(c->phi[i]);
     f(c->eta[0]);
     if (c->eta[1] != c->eta[0]) f(c->eta[1]);
-    f(c->Y); f(c->dYdt);
+    f(c->Y); f(c->Yprev); f(c->dYdt);
     for (int i = 0; i < 4; ++i) f(c->S[i]);
     for (int i = 0; i < 6; ++i) { f(c->eps[i]); f(c->E[i]); }
     for (int i = 0; i < 3; ++i) f(c->U[i]);
@@ -1419,6 +1425,7 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
     if (c->pc.gp) { for (int i = 0; i < 2; ++i) { A_(&c->eta[i], rs * N); } }
     else { A_(&c->eta[0], rs * N); c->eta[1] = c->eta[0]; }
     A_(&c->Y, rs * N);
+    A_(&c->Yprev, rs * N);
     A_(&c->dYdt, rs * N);
     for (int i = 0; i < 4; ++i) { A_(&c->S[i], 2 * rs * Nk); }
     for (int i = 0; i < 6; ++i) { A_(&c->eps[i], sizeof(float) * N); }
@@ -1593,16 +1600,17 @@ pfgb_status pfgb_read_elastic(pfgb_ctx *c, float *sigma6, float *strain6) {
         PFGB_CUDA_TRY(cudaMalloc(&dptrs, sizeof(float *) * 6));
         PFGB_CUDA_TRY(cudaMemcpy(dptrs, c->eps, sizeof(float *) * 6, cudaMemcpyHostToDevice));
         const ElasC<float> ec = elas_consts<float>(c);
-        // Y of the elastic solve: the state before the last Y update is gone;
-        // xB enters sigma only through the chemical eigenstrain, so the
-        // export uses the current composition (exact before the first step).
+        // Y of the elastic solve: the copy the final Y pass kept, with the
+        // offset of that step's start
+        void *yv = c->step > 0 ? c->Yprev : c->Y;
+        const double yc = c->step > 0 ? c->Yc_prev : c->Yc;
         if (c->p.precision == PFGB_PREC_FP64)
             k_stress_export<double><<<304, 256, 0, c->stream>>>(c->pc, ec, (double *)c->phi[pc_],
-                                                                (double *)c->eta[ec_], (double *)c->Y, c->Yc,
+                                                                (double *)c->eta[ec_], (double *)yv, yc,
                                                                 dptrs, st, (long long)N);
         else
             k_stress_export<float><<<304, 256, 0, c->stream>>>(c->pc, ec, (float *)c->phi[pc_],
-                                                               (float *)c->eta[ec_], (float *)c->Y, c->Yc, dptrs,
+                                                               (float *)c->eta[ec_], (float *)yv, yc, dptrs,
                                                                st, (long long)N);
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess)

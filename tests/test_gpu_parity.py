@@ -64,6 +64,7 @@ def test_step_parity(capi, oracle, case, prec):
     if mm == 1:
         errs["eta"] = rel_l2(fg["eta"], fo["eta"])
     errs["strain"] = rel_l2(eg["strain"], eo["strain"])
+    errs["sigma"] = rel_l2(eg["sigma"], eo["sigma"])
     print(case[3], prec, {k: f"{v:.2e}" for k, v in errs.items()},
           "iters gpu/oracle", sg.elastic_iterations, so.elastic_iterations)
     for k, v in errs.items():
