@@ -19,9 +19,11 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "fft.cuh"
+#include "fft246.cuh"
 #include "physics.cuh"
 
 const char *pfgb_error_buffer(void);
@@ -75,6 +77,7 @@ struct pfgb_ctx {
     size_t npartials = 0;
     double Yc = 0.0, dYoff = 0.0, target_mass = 0.0;
     double Yc_prev = 0.0;    // Yc at the last step's start
+    bool f246[3] = {false, false, false};   // x, y, z elastic passes on the 246-point engine
     double sum_alpha = 0.0;   // sum (1 - h) of the last phi (zero-mode curvature bound)
     int warm_valid = 0, step = 0, loaded = 0;
     size_t bytes = 0;
@@ -862,6 +865,240 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
     return PFGB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// elastic-iteration passes on 246-long axes (FP32, fft246.cuh engine): the
+// same operations as k_x_green / k_zpass<OpHijZ> / the y OpCopy pass, with
+// 48 lines per block in one in-place shared buffer
+// ---------------------------------------------------------------------------
+template <bool EIGEN>
+__global__ void __launch_bounds__(f246::THREADS, 2)
+k_x_green246(GreenArgs<float> A) {
+    using namespace f246;
+    using T2 = float2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *buf = tw + N;
+    const int k0 = blockIdx.x * 8, j = blockIdx.y;
+    const int kcnt = min(8, A.g.NzC - k0);
+    const long long base = (long long)j * A.g.NzC + k0;
+    const long long es = (long long)A.g.Ny * A.g.NzC;   // stride of x
+    for (int e = threadIdx.x; e < 6 * N * 4; e += blockDim.x) {
+        const int tp = e & 3, r = e >> 2;
+        const int q = r % N, s = r / N;
+        const int t = 2 * tp;
+        float2 *dst = buf + q * PSTR + s * 8 + t;
+        const float2 *src = A.E[s] + base + q * es + t;
+        if (t + 1 < kcnt) {
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src));
+        } else {
+            dst[0] = t < kcnt ? src[0] : make_float2(0.f, 0.f);
+            dst[1] = make_float2(0.f, 0.f);
+        }
+    }
+    cp_async_commit();
+    load_twiddles(tw, A.tw);
+    cp_async_wait_all();
+    __syncthreads();
+    lines<-1, PSTR, 1>(buf, tw);
+    float rd = 0.f, rr = 0.f;
+    for (int e = threadIdx.x; e < N * 8; e += blockDim.x) {
+        const int q = e >> 3, l = e & 7, k = k0 + l;
+        const int kk = min(k, A.g.NzC - 1);
+        const float kv[3] = {float(A.kt.kx[q]), float(A.kt.ky[j]), float(A.kt.kz[kk])};
+        float2 *pt = buf + q * PSTR + l;
+        T2 x[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) x[c] = pt[c * 8];
+        T2 t[3];
+        if (EIGEN) {
+#pragma unroll
+            for (int ii = 0; ii < 3; ++ii) {
+                T2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    float sv = 0.f;
+#pragma unroll
+                    for (int jj = 0; jj < 3; ++jj) sv += kv[jj] * A.ec.S[vidx(tvoigt(ii, jj), c)];
+                    acc = cadd(acc, cscale(x[c], (c < 3 ? 1.f : 2.f) * sv));
+                }
+                t[ii] = acc;
+            }
+        } else {
+            t[0] = cadd(cadd(cscale(x[0], kv[0]), cscale(x[5], kv[1])), cscale(x[4], kv[2]));
+            t[1] = cadd(cadd(cscale(x[5], kv[0]), cscale(x[1], kv[1])), cscale(x[3], kv[2]));
+            t[2] = cadd(cadd(cscale(x[4], kv[0]), cscale(x[3], kv[1])), cscale(x[2], kv[2]));
+        }
+        T2 u[3];
+        if (l >= kcnt || A.kt.cut(q, j, k) || (q == 0 && j == 0 && k == 0)) {
+            u[0] = u[1] = u[2] = make_float2(0.f, 0.f);
+        } else {
+            green_u<float>(A.ec.S, kv[0], kv[1], kv[2], t, u);
+        }
+        if (l < kcnt) {
+            const long long o = base + q * es + l;
+            if (A.resid) {
+                const float w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? 1.f : 2.f;
+                float ld_ = 0.f, lr = 0.f;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const T2 old = A.U[c][o];
+                    const float dr = u[c].x - old.x, di = u[c].y - old.y;
+                    ld_ += dr * dr + di * di;
+                    lr += u[c].x * u[c].x + u[c].y * u[c].y;
+                }
+                rd += w * ld_;
+                rr += w * lr;
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) A.U[c][o] = u[c];
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) pt[c * 8] = strain_comp<float>(c, kv[0], kv[1], kv[2], u);
+    }
+    if (A.resid) {
+        AccSum2 sacc{double(rd), double(rr)};
+        block_reduce_acc(sacc);
+        if (threadIdx.x == 0)
+            reinterpret_cast<AccSum2 *>(A.partials)[blockIdx.y * gridDim.x + blockIdx.x] = sacc;
+    }
+    __syncthreads();
+    lines<+1, PSTR, 1>(buf, tw);
+    for (int e = threadIdx.x; e < 6 * N * 4; e += blockDim.x) {
+        const int tp = e & 3, r = e >> 2;
+        const int q = r % N, s = r / N;
+        const int t = 2 * tp;
+        const float2 *srcs = buf + q * PSTR + s * 8 + t;
+        float2 *dst = A.E[s] + base + q * es + t;
+        if (t + 1 < kcnt) *reinterpret_cast<float4 *>(dst) = *reinterpret_cast<const float4 *>(srcs);
+        else if (t < kcnt) dst[0] = srcs[0];
+    }
+}
+
+// z pass with six fields in and six out (C2R -> op.point -> R2C), 16 rows
+// per block: the rows' three field pairs are the block's 48 complex lines
+template <class Op>
+__global__ void __launch_bounds__(f246::THREADS, 2)
+k_zpass246(Grid3 g, const float2 *tw_g, Op op) {
+    using namespace f246;
+    constexpr int R = 16, NC = N / 2 + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *buf = tw + N;
+    const long long row0 = (long long)blockIdx.x * R;
+    const long long nrows = (long long)g.Nx * g.Ny;
+    const int rcnt = (int)min((long long)R, nrows - row0);
+    load_twiddles(tw, tw_g);
+    for (int e = threadIdx.x; e < R * NC; e += blockDim.x) {
+        const int rr = e / NC, k = e - rr * NC;
+        float2 v[6];
+        if (rr < rcnt) op.load_spec(row0 + rr, k, v);
+        else {
+#pragma unroll
+            for (int f = 0; f < 6; ++f) v[f] = make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            float2 Av = v[2 * f], Bv = v[2 * f + 1];
+            if (k == 0 || 2 * k == N) { Av.y = 0.f; Bv.y = 0.f; }
+            float2 *line = buf + (rr * 3 + f) * N;
+            // Z_k = A_k + i B_k ; Z_(n-k) = conj(A_k) + i conj(B_k)
+            line[k] = make_float2(Av.x - Bv.y, Av.y + Bv.x);
+            if (k > 0 && 2 * k != N) line[N - k] = make_float2(Av.x + Bv.y, Bv.x - Av.y);
+        }
+    }
+    __syncthreads();
+    lines<+1, 1, N>(buf, tw);
+    typename Op::Acc acc = Op::Acc::identity();
+    for (int e = threadIdx.x; e < rcnt * N; e += blockDim.x) {
+        const int r = e / N, z = e - r * N;
+        float vi[6], vo[6];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const float2 w = buf[(r * 3 + f) * N + z];
+            vi[2 * f] = w.x;
+            vi[2 * f + 1] = w.y;
+        }
+        op.point((row0 + r) * N + z, vi, vo, acc);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) buf[(r * 3 + f) * N + z] = make_float2(vo[2 * f], vo[2 * f + 1]);
+    }
+    if constexpr (Op::Acc::kActive) {
+        block_reduce_acc(acc);
+        if (threadIdx.x == 0) op.finish(blockIdx.x, acc);
+    }
+    __syncthreads();
+    lines<-1, 1, N>(buf, tw);
+    for (int e = threadIdx.x; e < rcnt * NC; e += blockDim.x) {
+        const int rr = e / NC, k = e - rr * NC;
+        float2 v[6];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const float2 *line = buf + (rr * 3 + f) * N;
+            const float2 Zk = line[k], Zm = line[k == 0 ? 0 : N - k];
+            // A_k = (Z_k + conj Z_-k) / 2 ; B_k = (Z_k - conj Z_-k) / (2 i)
+            v[2 * f] = make_float2(0.5f * (Zk.x + Zm.x), 0.5f * (Zk.y - Zm.y));
+            v[2 * f + 1] = make_float2(0.5f * (Zk.y + Zm.y), 0.5f * (Zm.x - Zk.x));
+        }
+        op.store_spec(row0 + rr, k, v);
+    }
+}
+
+template <int DIR>
+static pfgb_status launch_y246(pfgb_ctx *c, const char *tag) {
+    const size_t smem = f246::axis_smem_bytes();
+    auto kern = k_y246<DIR>;
+    PFGB_CUDA_TRY(allow_smem(kern, smem));
+    AxisIO<float, 6, 6> io;
+    for (int i = 0; i < 6; ++i) { io.in[i] = (const float2 *)c->E[i]; io.out[i] = (float2 *)c->E[i]; }
+    dim3 grid((c->g.NzC + 7) / 8, c->g.Nx);
+    ProfScope ps(c, {tag, 12.0 * (double)c->g.Nk * sizeof(float2)});
+    kern<<<grid, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][1], io);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    return PFGB_OK;
+}
+
+static pfgb_status launch_green246(pfgb_ctx *c, bool eigen, int resid, int *nblocks) {
+    const size_t smem = f246::axis_smem_bytes();
+    GreenArgs<float> A;
+    A.g = c->g;
+    A.kt = KTab{c->kx, c->ky, c->kz, c->mx, c->my, c->mz};
+    for (int i = 0; i < 21; ++i) { A.ec.S[i] = (float)c->p.S[i]; A.ec.Sp[i] = (float)c->p.S_p[i]; }
+    A.tw = (const float2 *)c->tw[1][0];
+    for (int i = 0; i < 6; ++i) A.E[i] = (float2 *)c->E[i];
+    for (int i = 0; i < 3; ++i) A.U[i] = (float2 *)c->U[i];
+    A.partials = c->partials;
+    A.resid = resid;
+    dim3 grid((c->g.NzC + 7) / 8, c->g.Ny);
+    ProfScope ps(c, {eigen ? "x_green_eigen" : "x_green_hij",
+                     (double)(6 + 3 + 6 + (resid ? 3 : 0)) * (double)c->g.Nk * sizeof(float2)});
+    if (eigen) {
+        auto kern = k_x_green246<true>;
+        PFGB_CUDA_TRY(allow_smem(kern, smem));
+        kern<<<grid, f246::THREADS, smem, c->stream>>>(A);
+    } else {
+        auto kern = k_x_green246<false>;
+        PFGB_CUDA_TRY(allow_smem(kern, smem));
+        kern<<<grid, f246::THREADS, smem, c->stream>>>(A);
+    }
+    PFGB_CUDA_TRY(cudaGetLastError());
+    *nblocks = grid.x * grid.y;
+    return PFGB_OK;
+}
+
+template <class Op>
+static pfgb_status launch_z246(pfgb_ctx *c, Op op, const char *tag, double extra_bytes) {
+    const size_t smem = f246::z_smem_bytes();
+    auto kern = k_zpass246<Op>;
+    PFGB_CUDA_TRY(allow_smem(kern, smem));
+    const long long rows = (long long)c->g.Nx * c->g.Ny;
+    const int nb = (int)((rows + 15) / 16);
+    ProfScope ps(c, {tag, 12.0 * (double)c->g.Nk * sizeof(float2) + extra_bytes});
+    kern<<<nb, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][2], op);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    return PFGB_OK;
+}
+
 // ===========================================================================
 // step orchestration
 // ===========================================================================
@@ -917,25 +1154,46 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     AxisIO<TE, 6, 6> io6;
     for (int i = 0; i < 6; ++i) { io6.in[i] = (const T2e *)c->E[i]; io6.out[i] = (T2e *)c->E[i]; }
     int nb = 0;
+    // the four passes of an iteration, on the 246-point engine where the axis allows
+    auto ypass = [&](int dir, const char *tag) -> pfgb_status {
+        if constexpr (std::is_same<TE, float>::value) {
+            if (c->f246[1]) return dir < 0 ? launch_y246<-1>(c, tag) : launch_y246<+1>(c, tag);
+        }
+        return dir < 0 ? launch_axis<TE, 6, 6, -1, 0>(c, 1, io6, OpCopy<TE, 6>{}, tag)
+                       : launch_axis<TE, 6, 6, +1, 0>(c, 1, io6, OpCopy<TE, 6>{}, tag);
+    };
+    auto green = [&](bool eigen, int resid) -> pfgb_status {
+        if constexpr (std::is_same<TE, float>::value) {
+            if (c->f246[0]) return launch_green246(c, eigen, resid, &nb);
+        }
+        return launch_green<TE>(c, eigen, resid, &nb);
+    };
+    auto hij = [&]() -> pfgb_status {
+        const double extra = (2.0 + pc.gp) * Nf * sizeof(T);
+        if constexpr (std::is_same<TE, float>::value) {
+            if (c->f246[2]) return launch_z246(c, OpHijZ<T, TE>{d, pc, ec}, "z_hij", extra);
+        }
+        return launch_z<TE, 6, 6>(c, OpHijZ<T, TE>{d, pc, ec}, "z_hij", extra);
+    };
     if (!warm_used) {
         TRY((launch_z<TE, 0, 6>(c, OpEigenR2C<T, TE>{d, pc, ec}, "z_eigen_r2c", (2.0 + pc.gp) * Nf * sizeof(T))));
-        TRY((launch_axis<TE, 6, 6, -1, 0>(c, 1, io6, OpCopy<TE, 6>{}, "y_fwd6")));
-        TRY(launch_green<TE>(c, true, 0, &nb));
+        TRY(ypass(-1, "y_fwd6"));
+        TRY(green(true, 0));
     } else {
         AxisIO<TE, 3, 6> io;
         for (int i = 0; i < 3; ++i) io.in[i] = (const T2e *)c->U[i];
         for (int i = 0; i < 6; ++i) io.out[i] = (T2e *)c->E[i];
         TRY((launch_axis<TE, 3, 6, 0, +1>(c, 2, io, OpStrainFromUX<TE>{kt}, "x_strain_from_u")));
     }
-    TRY((launch_axis<TE, 6, 6, +1, 0>(c, 1, io6, OpCopy<TE, 6>{}, "y_inv6")));
+    TRY(ypass(+1, "y_inv6"));
     int iter = accel ? 0 : 1;
     int conv = accel ? 0 : 1;
     double rel = NAN;
     for (;;) {
-        TRY((launch_z<TE, 6, 6>(c, OpHijZ<T, TE>{d, pc, ec}, "z_hij", (2.0 + pc.gp) * Nf * sizeof(T))));
-        TRY((launch_axis<TE, 6, 6, -1, 0>(c, 1, io6, OpCopy<TE, 6>{}, "y_fwd6")));
-        TRY(launch_green<TE>(c, false, accel, &nb));
-        TRY((launch_axis<TE, 6, 6, +1, 0>(c, 1, io6, OpCopy<TE, 6>{}, "y_inv6")));
+        TRY(hij());
+        TRY(ypass(-1, "y_fwd6"));
+        TRY(green(false, accel));
+        TRY(ypass(+1, "y_inv6"));
         if (accel) {
             TRY(reduce_to<AccSum2>(c, nb, DS_RES_DIFF));
             k_resid_final<<<1, 1, 0, c->stream>>>(c->dscal, P.elastic_residual_absolute_floor);
@@ -1416,6 +1674,13 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
     pfgb_make_plan(pin->Nx, &c->plx);
     pfgb_make_plan(pin->Ny, &c->ply);
     pfgb_make_plan(pin->Nz, &c->plz);
+    {
+        // the strided-axis kernels copy column pairs with 16-byte accesses
+        const bool e32 = pin->elastic_precision == PFGB_PREC_FP32, evenc = ((pin->Nz / 2 + 1) % 2) == 0;
+        c->f246[0] = e32 && pin->Nx == f246::N && evenc;
+        c->f246[1] = e32 && pin->Ny == f246::N && evenc;
+        c->f246[2] = e32 && pin->Nz == f246::N;
+    }
     build_physc(c);
     pfgb_status s = PFGB_OK;
     const size_t rs = pin->precision == PFGB_PREC_FP64 ? sizeof(double) : sizeof(float);
