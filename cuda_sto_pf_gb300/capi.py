@@ -84,7 +84,7 @@ class StepStats(Structure):
 class Diag(Structure):
     _fields_ = [("vf_precip", c_double), ("mass_xBtot", c_double), ("mean_xB", c_double),
                 ("phi_min", c_double), ("phi_max", c_double), ("xB_min", c_double),
-                ("xB_max", c_double), ("n_in", c_double)]
+                ("xB_max", c_double), ("n_in", c_double), ("n_if", c_double)]
 
 
 # (name, restype, argtypes) of every entry point declared in include/pfgb.h

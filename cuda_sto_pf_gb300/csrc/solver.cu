@@ -1905,10 +1905,10 @@ pfgb_status pfgb_read_displacement_k(pfgb_ctx *c, float *u3) {
 
 struct AccDiag {
     static constexpr bool kActive = true;
-    double vf, mass, xb, nin, pmn, pmx, xmn, xmx;
-    __device__ static AccDiag identity() { return {0, 0, 0, 0, 1e300, -1e300, 1e300, -1e300}; }
+    double vf, mass, xb, nin, pmn, pmx, xmn, xmx, nif;
+    __device__ static AccDiag identity() { return {0, 0, 0, 0, 1e300, -1e300, 1e300, -1e300, 0}; }
     __device__ static AccDiag combine(AccDiag a, const AccDiag &b) {
-        a.vf += b.vf; a.mass += b.mass; a.xb += b.xb; a.nin += b.nin;
+        a.vf += b.vf; a.mass += b.mass; a.xb += b.xb; a.nin += b.nin; a.nif += b.nif;
         a.pmn = fmin(a.pmn, b.pmn); a.pmx = fmax(a.pmx, b.pmx);
         a.xmn = fmin(a.xmn, b.xmn); a.xmx = fmax(a.xmx, b.xmx);
         return a;
@@ -1917,7 +1917,7 @@ struct AccDiag {
         AccDiag r;
         double *pa = reinterpret_cast<double *>(&a), *pr = reinterpret_cast<double *>(&r);
 #pragma unroll
-        for (int i = 0; i < 8; ++i) pr[i] = __shfl_down_sync(0xffffffffu, pa[i], o);
+        for (int i = 0; i < 9; ++i) pr[i] = __shfl_down_sync(0xffffffffu, pa[i], o);
         return r;
     }
 };
@@ -1935,7 +1935,8 @@ __global__ void k_diag(const T *phi, const T *Y, long long N, double Yc, int raw
         a.vf += pf_h(clamp01(p));             // reduce_sum_h_kernel (:5580)
         a.mass += (1.0 - h) * x + vB * h;      // reduce_sum_xBtot_kernel (:3792)
         a.xb += x;
-        a.nin += p >= 0.5 ? 1.0 : 0.0;
+        a.nin += p > 0.5 ? 1.0 : 0.0;                 // reduce_sum_N_in_N_if_kernel (:3746)
+        a.nif += (p > 0.12 && p < 0.88) ? 1.0 : 0.0;
         a.pmn = fmin(a.pmn, p); a.pmx = fmax(a.pmx, p);
         a.xmn = fmin(a.xmn, x); a.xmx = fmax(a.xmx, x);
     }
@@ -1958,7 +1959,7 @@ pfgb_status pfgb_diagnostics(pfgb_ctx *c, pfgb_diag *out) {
                                                  c->p.Y_clip, c->p.xB_eps, c->p.v_B, (AccDiag *)c->partials);
     PFGB_CUDA_TRY(cudaGetLastError());
     TRY(reduce_to<AccDiag>(c, nb, 24));
-    TRY(sync_read(c, 24, 8));
+    TRY(sync_read(c, 24, 9));
     const double *h = c->hscal + 24;
     const double N = (double)c->g.N;
     out->vf_precip = h[0] / N;
@@ -1967,6 +1968,7 @@ pfgb_status pfgb_diagnostics(pfgb_ctx *c, pfgb_diag *out) {
     out->n_in = h[3];
     out->phi_min = h[4]; out->phi_max = h[5];
     out->xB_min = h[6]; out->xB_max = h[7];
+    out->n_if = h[8];
     return PFGB_OK;
 }
 

@@ -1,0 +1,521 @@
+// main_cuda — command-line driver of the pfgb library with the reference
+// main_cuda's invocation, parameter file and output layout for the dynamics
+// path (main_cuda.cu main(), :22500-34800).  Host C++ over the C ABI only.
+//
+//   main_cuda Nx Ny Nz dt nsteps out_every csv_out_every elastic(0/1) \
+//       --pf-param-file <path> --init-mode raw_fields --init-phi-raw <f> \
+//       --init-xB-raw <f> [--init-eta-raw <f>] [--init-dY-dt-prev-raw <f>] \
+//       [--init-meta <json>] [--pf-zero-mode PF_CONSERVED_Y_ZERO_MODE_V1] ...
+//
+// Outputs (CUDA_STO_RESULTS_ROOT, default Results/):
+//   <chel|ch>_T%.0f_cuda_NxxNyxNz_dt%.3g_steps%d_xB%.3f/pf_input.params
+//   .../<case tag>/pf_input.params, vf_precip_vs_time_<tag>.csv,
+//   phi|xB|xBtot|eta VTK (init, every out_every steps, final),
+//   elastic_solver_trace.csv, pf_zero_mode_trace.csv,
+//   performance_summary.json, summary.txt
+// Exit status: 0 success, 2 invalid input or solver failure, 1 CUDA error.
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <string>
+#include <vector>
+
+#include "pfgb.h"
+
+namespace {
+
+struct Cli {
+    int pos_Nx = -1, pos_Ny = -1, pos_Nz = -1, nsteps = 100, out_every = 100, csv_out_every = 10;
+    int pos_elastic = -1;
+    double pos_dt = NAN;
+    std::string mode = "dynamics";
+    std::string param_file, init_mode, init_phi, init_xB, init_eta, init_dYdt, init_meta, case_tag;
+    int elastic = -1;
+    double temperature_C = NAN;
+    std::string zero_mode;
+    double zm_tol = NAN;
+    int zm_maxit = -1;
+    bool prev_level = false, no_gamma = false;
+    double h_scale = NAN;
+    int precision = PFGB_PREC_FP64;
+    int device = 0;
+};
+
+void usage() {
+    printf("Usage (positional, legacy):\n"
+           "  ./main_cuda Nx Ny Nz dt nsteps out_every csv_out_every elastic_enabled(0/1)\n"
+           "    dt is a fallback only: the parameter file's dt wins.\n"
+           "\nFlags:\n"
+           "  --mode=dynamics                 (minimize: not available in this build)\n"
+           "  --pf-param-file <path>          required: complete physical PF inputs (key=value)\n"
+           "  --elastic 0|1                   override elastic\n"
+           "  --temperature-C <val>\n"
+           "  --init-mode raw_fields          initialize from raw phi/xB[/eta][/dY_dt_prev] fields\n"
+           "  --init-phi-raw <path>           float64, C order, idx=i*(Ny*Nz)+j*Nz+k\n"
+           "  --init-xB-raw <path>\n"
+           "  --init-eta-raw <path>           optional (default zero)\n"
+           "  --init-dY-dt-prev-raw <path>    optional (default zero history)\n"
+           "  --init-meta <path>              init_meta.json (xB_max_safe, grid)\n"
+           "  --init-case-tag <tag>           case subdirectory name (default raw_fields_relax)\n"
+           "  --pf-zero-mode OFF|PF_CONSERVED_Y_ZERO_MODE_V1\n"
+           "  --pf-zero-mode-tol-rel <value>  default 1e-12\n"
+           "  --pf-zero-mode-max-iter <n>     default 24\n"
+           "  --enable-Y-rhs-previous-time-level\n"
+           "  --disable-Y-rhs-gamma-term\n"
+           "  --Y-rhs-term-h-scale <s>\n"
+           "  --precision fp64|fp32           field precision (default fp64, as the reference)\n"
+           "  --device <n>                    CUDA device ordinal\n");
+}
+
+// "--name value" or "--name=value"; advances i past a separate value
+const char *flag_value(int argc, char **argv, int *i, const char *name) {
+    const size_t n = strlen(name);
+    const char *a = argv[*i];
+    if (strncmp(a, name, n) != 0) return nullptr;
+    if (a[n] == '=') return a + n + 1;
+    if (a[n] != '\0') return nullptr;
+    if (*i + 1 >= argc) {
+        fprintf(stderr, "[fatal] %s needs a value\n", name);
+        exit(2);
+    }
+    return argv[++*i];
+}
+
+bool to_double(const char *s, double *v) {
+    char *e = nullptr;
+    *v = strtod(s, &e);
+    return e != s && *e == '\0' && std::isfinite(*v);
+}
+bool to_int(const char *s, int *v) {
+    char *e = nullptr;
+    long x = strtol(s, &e, 10);
+    if (e == s || *e != '\0') return false;
+    *v = (int)x;
+    return true;
+}
+[[noreturn]] void bad(const char *flag, const char *val) {
+    fprintf(stderr, "[fatal] invalid value for %s: %s\n", flag, val);
+    exit(2);
+}
+
+Cli parse(int argc, char **argv) {
+    Cli c;
+    // positional arguments sit at fixed places (main_cuda.cu:22527-22534)
+    auto posi = [&](int k, int *dst) {
+        if (argc > k && argv[k][0] != '-') *dst = atoi(argv[k]);
+    };
+    posi(1, &c.pos_Nx); posi(2, &c.pos_Ny); posi(3, &c.pos_Nz);
+    if (argc > 4 && argv[4][0] != '-') c.pos_dt = atof(argv[4]);
+    posi(5, &c.nsteps); posi(6, &c.out_every); posi(7, &c.csv_out_every); posi(8, &c.pos_elastic);
+    for (int i = 1; i < argc; ++i) {
+        const char *a = argv[i];
+        if (a[0] != '-') continue;
+        const char *v;
+        if (!strcmp(a, "--help") || !strcmp(a, "-h")) { usage(); exit(0); }
+        else if (!strncmp(a, "--mode=", 7)) c.mode = a + 7;
+        else if ((v = flag_value(argc, argv, &i, "--mode"))) c.mode = v;
+        else if ((v = flag_value(argc, argv, &i, "--pf-param-file"))) c.param_file = v;
+        else if ((v = flag_value(argc, argv, &i, "--elastic"))) { if (!to_int(v, &c.elastic)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--temperature-C"))) { if (!to_double(v, &c.temperature_C)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--init-mode"))) c.init_mode = v;
+        else if ((v = flag_value(argc, argv, &i, "--init-phi-raw"))) c.init_phi = v;
+        else if ((v = flag_value(argc, argv, &i, "--init-xB-raw"))) c.init_xB = v;
+        else if ((v = flag_value(argc, argv, &i, "--init-eta-raw"))) c.init_eta = v;
+        else if ((v = flag_value(argc, argv, &i, "--init-dY-dt-prev-raw"))) c.init_dYdt = v;
+        else if ((v = flag_value(argc, argv, &i, "--init-meta"))) c.init_meta = v;
+        else if ((v = flag_value(argc, argv, &i, "--init-case-tag"))) c.case_tag = v;
+        else if ((v = flag_value(argc, argv, &i, "--pf-zero-mode-tol-rel"))) { if (!to_double(v, &c.zm_tol)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--pf-zero-mode-max-iter"))) { if (!to_int(v, &c.zm_maxit)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--pf-zero-mode"))) c.zero_mode = v;
+        else if (!strcmp(a, "--enable-Y-rhs-previous-time-level")) c.prev_level = true;
+        else if (!strcmp(a, "--disable-Y-rhs-gamma-term")) c.no_gamma = true;
+        else if ((v = flag_value(argc, argv, &i, "--Y-rhs-term-h-scale"))) { if (!to_double(v, &c.h_scale)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--precision"))) {
+            if (!strcmp(v, "fp64")) c.precision = PFGB_PREC_FP64;
+            else if (!strcmp(v, "fp32")) c.precision = PFGB_PREC_FP32;
+            else bad(a, v);
+        }
+        else if ((v = flag_value(argc, argv, &i, "--device"))) { if (!to_int(v, &c.device)) bad(a, v); }
+        else fprintf(stderr, "[warn] unknown flag ignored: %s\n", a);
+    }
+    return c;
+}
+
+bool read_raw(const std::string &path, size_t n, std::vector<double> *out) {
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) { fprintf(stderr, "[fatal] cannot open raw field %s\n", path.c_str()); return false; }
+    fseek(f, 0, SEEK_END);
+    const long sz = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    if (sz != (long)(n * sizeof(double))) {
+        fprintf(stderr, "[fatal] raw field %s has %ld bytes, expected %zu (float64 x %zu)\n", path.c_str(), sz,
+                n * sizeof(double), n);
+        fclose(f);
+        return false;
+    }
+    out->resize(n);
+    const size_t got = fread(out->data(), sizeof(double), n, f);
+    fclose(f);
+    if (got != n) { fprintf(stderr, "[fatal] short read of %s\n", path.c_str()); return false; }
+    return true;
+}
+
+std::string slurp(const std::string &path) {
+    std::string s;
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) return s;
+    char buf[4096];
+    size_t k;
+    while ((k = fread(buf, 1, sizeof(buf), f)) > 0) s.append(buf, k);
+    fclose(f);
+    return s;
+}
+
+// number after "key": in a flat JSON text (init_meta.json); false if absent
+bool json_number(const std::string &txt, const char *key, double *v) {
+    const std::string k = std::string("\"") + key + "\"";
+    size_t p = txt.find(k);
+    if (p == std::string::npos) return false;
+    p = txt.find(':', p + k.size());
+    if (p == std::string::npos) return false;
+    const char *s = txt.c_str() + p + 1;
+    char *e = nullptr;
+    const double x = strtod(s, &e);
+    if (e == s) return false;
+    *v = x;
+    return true;
+}
+
+// a key of the parameter file that the library's parameter struct does not
+// carry (used for output naming only)
+double param_file_value(const std::string &txt, const char *key, double dflt) {
+    size_t p = 0;
+    while (p < txt.size()) {
+        size_t e = txt.find('\n', p);
+        if (e == std::string::npos) e = txt.size();
+        std::string line = txt.substr(p, e - p);
+        p = e + 1;
+        const size_t hash = line.find('#');
+        if (hash != std::string::npos) line.resize(hash);
+        const size_t eq = line.find('=');
+        if (eq == std::string::npos) continue;
+        std::string k = line.substr(0, eq), v = line.substr(eq + 1);
+        auto trim = [](std::string &s) {
+            while (!s.empty() && isspace((unsigned char)s.back())) s.pop_back();
+            size_t b = 0;
+            while (b < s.size() && isspace((unsigned char)s[b])) ++b;
+            s.erase(0, b);
+        };
+        trim(k); trim(v);
+        double x;
+        if (k == key && to_double(v.c_str(), &x)) return x;
+    }
+    return dflt;
+}
+
+bool copy_file(const std::string &from, const std::string &to) {
+    const std::string s = slurp(from);
+    FILE *f = fopen(to.c_str(), "wb");
+    if (!f) return false;
+    fwrite(s.data(), 1, s.size(), f);
+    fclose(f);
+    return true;
+}
+
+// ASCII STRUCTURED_POINTS, z outermost, x innermost, %.5f (io_vtk_cuda.h:80-128)
+bool write_vtk(const std::string &path, const char *name, const std::vector<double> &v, int Nx, int Ny, int Nz) {
+    FILE *fo = fopen(path.c_str(), "w");
+    if (!fo) { fprintf(stderr, "ERROR: Cannot create file %s\n", path.c_str()); return false; }
+    const int ny_out = Ny == 2 ? 1 : Ny;
+    fprintf(fo, "# vtk DataFile Version 3.0\nPhase Field Simulation\nASCII\nDATASET STRUCTURED_POINTS\n");
+    fprintf(fo, "DIMENSIONS %d %d %d\nASPECT_RATIO 1 1 1\nORIGIN 0 0 0\nPOINT_DATA %d\n", Nx, ny_out, Nz,
+            Nx * ny_out * Nz);
+    fprintf(fo, "SCALARS %s double 1\nLOOKUP_TABLE default\n", name);
+    std::string line;
+    char tmp[64];
+    for (int k = 0; k < Nz; ++k)
+        for (int j = 0; j < ny_out; ++j) {
+            line.clear();
+            for (int i = 0; i < Nx; ++i) {
+                const int n = snprintf(tmp, sizeof(tmp), "%.5f ", v[((size_t)i * Ny + j) * Nz + k]);
+                line.append(tmp, n);
+            }
+            fwrite(line.data(), 1, line.size(), fo);
+        }
+    fprintf(fo, "\n");
+    fclose(fo);
+    return true;
+}
+
+double h_of(double p) { return p * p * p * (6.0 * p * p - 15.0 * p + 10.0); }
+
+std::string now_str() {
+    char b[64];
+    time_t t = time(nullptr);
+    struct tm *lt = localtime(&t);
+    if (!lt || !strftime(b, sizeof(b), "%Y-%m-%d %H:%M:%S", lt)) return "unknown";
+    return b;
+}
+
+int fail(pfgb_status s, const char *where) {
+    fprintf(stderr, "[fatal] %s: %s (%s)\n", where, pfgb_status_string(s), pfgb_last_error(nullptr));
+    return s == PFGB_ERR_CUDA || s == PFGB_ERR_NOMEM ? 1 : 2;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    Cli c = parse(argc, argv);
+    if (c.param_file.empty()) {
+        fprintf(stderr, "[fatal] --pf-param-file <path> is required (complete physical PF inputs).\n");
+        return 2;
+    }
+    if (c.mode != "dynamics") {
+        fprintf(stderr, "[fatal] --mode=%s is not available in this build (dynamics only)\n", c.mode.c_str());
+        return 2;
+    }
+    pfgb_params P;
+    pfgb_params_default(&P);
+    if (c.pos_Nx > 0) P.Nx = c.pos_Nx;
+    if (c.pos_Ny > 0) P.Ny = c.pos_Ny;
+    if (c.pos_Nz > 0) P.Nz = c.pos_Nz;
+    if (std::isfinite(c.pos_dt)) P.dt = c.pos_dt;
+    if (c.pos_elastic >= 0) P.elastic_enabled = c.pos_elastic ? 1 : 0;
+    char err[512] = {0};
+    pfgb_status st = pfgb_params_load_file(&P, c.param_file.c_str(), err, sizeof(err));
+    if (st != PFGB_OK) {
+        fprintf(stderr, "[fatal] %s\n", err);
+        return 2;
+    }
+    // the parameter file does not set the grid: positional values stand
+    if (c.pos_Nx > 0) P.Nx = c.pos_Nx;
+    if (c.pos_Ny > 0) P.Ny = c.pos_Ny;
+    if (c.pos_Nz > 0) P.Nz = c.pos_Nz;
+    if (c.pos_elastic >= 0) P.elastic_enabled = c.pos_elastic ? 1 : 0;
+    if (c.elastic >= 0) P.elastic_enabled = c.elastic ? 1 : 0;
+    if (std::isfinite(c.temperature_C)) P.temperature_C = c.temperature_C;
+    if (!c.zero_mode.empty()) {
+        if (c.zero_mode == "PF_CONSERVED_Y_ZERO_MODE_V1") P.zero_mode_enabled = 1;
+        else if (c.zero_mode == "OFF") P.zero_mode_enabled = 0;
+        else bad("--pf-zero-mode", c.zero_mode.c_str());
+    }
+    if (std::isfinite(c.zm_tol)) P.zero_mode_tolerance_relative = c.zm_tol;
+    if (c.zm_maxit > 0) P.zero_mode_max_iterations = c.zm_maxit;
+    if (c.prev_level) P.enable_Y_rhs_previous_time_level = 1;
+    if (c.no_gamma) P.disable_Y_rhs_gamma_term = 1;
+    if (std::isfinite(c.h_scale)) P.Y_rhs_term_h_scale = c.h_scale;
+    P.precision = c.precision;
+    if (c.nsteps < 0 || c.out_every <= 0 || c.csv_out_every <= 0) {
+        fprintf(stderr, "[fatal] nsteps >= 0, out_every > 0 and csv_out_every > 0 are required\n");
+        return 2;
+    }
+    if ((st = pfgb_params_finalize(&P)) != PFGB_OK) return fail(st, "pfgb_params_finalize");
+
+    // ---- initial fields ---------------------------------------------------
+    if (c.init_mode != "raw_fields") {
+        fprintf(stderr, "[fatal] this build initialises from --init-mode raw_fields only\n");
+        return 2;
+    }
+    const size_t N = (size_t)P.Nx * P.Ny * P.Nz;
+    std::vector<double> phi, xB, eta, dYdt;
+    if (c.init_phi.empty() || c.init_xB.empty()) {
+        fprintf(stderr, "[fatal] raw_fields needs --init-phi-raw and --init-xB-raw\n");
+        return 2;
+    }
+    if (!read_raw(c.init_phi, N, &phi) || !read_raw(c.init_xB, N, &xB)) return 2;
+    if (!c.init_eta.empty() && !read_raw(c.init_eta, N, &eta)) return 2;
+    if (!c.init_dYdt.empty() && !read_raw(c.init_dYdt, N, &dYdt)) return 2;
+    double xB_max_safe = 0.07;   // reference default when init_meta.json does not set it
+    if (!c.init_meta.empty()) {
+        const std::string meta = slurp(c.init_meta);
+        if (meta.empty()) { fprintf(stderr, "[fatal] cannot read %s\n", c.init_meta.c_str()); return 2; }
+        double v;
+        if (json_number(meta, "xB_max_safe", &v)) xB_max_safe = v;
+        const char *dims[3] = {"Nx", "Ny", "Nz"};
+        const int have[3] = {P.Nx, P.Ny, P.Nz};
+        for (int a = 0; a < 3; ++a)
+            if (json_number(meta, dims[a], &v) && (int)v != have[a]) {
+                fprintf(stderr, "[fatal] init_meta %s=%d does not match the grid (%d)\n", dims[a], (int)v, have[a]);
+                return 2;
+            }
+    }
+    st = pfgb_prepare_raw_fields(&P, xB_max_safe, phi.data(), xB.data(), eta.empty() ? nullptr : eta.data(),
+                                 dYdt.empty() ? nullptr : dYdt.data(), N);
+    if (st != PFGB_OK) return fail(st, "pfgb_prepare_raw_fields");
+
+    // ---- output layout ----------------------------------------------------
+    const std::string ptxt = slurp(c.param_file);
+    const double xB_out = param_file_value(ptxt, "ic_23d_xB_out", param_file_value(ptxt, "xB_alpha_initial", 0.03));
+    const char *root_env = getenv("CUDA_STO_RESULTS_ROOT");
+    const std::string root = (root_env && root_env[0]) ? root_env : "Results";
+    char name[512];
+    snprintf(name, sizeof(name), "%s_T%.0f_cuda_%dx%dx%d_dt%.3g_steps%d_xB%.3f", P.elastic_enabled ? "chel" : "ch",
+             P.temperature_C, P.Nx, P.Ny, P.Nz, P.dt, c.nsteps, xB_out);
+    mkdir(root.c_str(), 0755);
+    const std::string out_dir = root + "/" + name;
+    mkdir(out_dir.c_str(), 0755);
+    copy_file(c.param_file, out_dir + "/pf_input.params");
+    const std::string tag = c.case_tag.empty() ? "raw_fields_relax" : c.case_tag;
+    const std::string case_dir = out_dir + "/" + tag;
+    mkdir(case_dir.c_str(), 0755);
+    copy_file(c.param_file, case_dir + "/pf_input.params");
+    const bool gp = P.model_mode == PFGB_MODEL_GP_ZONE;
+    const double dx_phys = P.ic_phi_iface_w > 1e-30 ? P.lambda_sm_m / (2.0 * P.ic_phi_iface_w) : P.dx * 1e-9;
+    const double unit_to_nm = (std::fabs(P.dx) > 1e-30 ? dx_phys / P.dx : 1e-9) * 1e9;
+    printf("output_dir=%s\ncase_output_dir=%s\n", out_dir.c_str(), case_dir.c_str());
+
+    // ---- solver -----------------------------------------------------------
+    pfgb_ctx *ctx = nullptr;
+    if ((st = pfgb_create(&P, c.device, &ctx)) != PFGB_OK) return fail(st, "pfgb_create");
+    st = pfgb_load_fields(ctx, phi.data(), xB.data(), eta.empty() ? nullptr : eta.data(),
+                          dYdt.empty() ? nullptr : dYdt.data());
+    if (st != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_load_fields"); }
+
+    std::vector<double> f_phi(N), f_xB(N), f_eta(N), f_xBtot(N);
+    auto read_state = [&]() -> pfgb_status {
+        return pfgb_read_fields(ctx, f_phi.data(), f_xB.data(), nullptr, gp ? f_eta.data() : nullptr, nullptr);
+    };
+    auto vtk_set = [&](const char *suffix) -> bool {
+        for (size_t i = 0; i < N; ++i) {
+            const double h = h_of(f_phi[i]);
+            f_xBtot[i] = (1.0 - h) * f_xB[i] + h * P.v_B;
+        }
+        bool ok = write_vtk(case_dir + "/xBtot" + suffix + ".vtk", "xB_tot", f_xBtot, P.Nx, P.Ny, P.Nz);
+        ok &= write_vtk(case_dir + "/xB" + suffix + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
+        ok &= write_vtk(case_dir + "/phi" + suffix + ".vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
+        if (gp) ok &= write_vtk(case_dir + "/eta" + suffix + ".vtk", "eta", f_eta, P.Nx, P.Ny, P.Nz);
+        return ok;
+    };
+
+    FILE *csv = fopen((case_dir + "/vf_precip_vs_time_" + tag + ".csv").c_str(), "w");
+    FILE *etrace = nullptr, *ztrace = nullptr;
+    const bool accel = P.elastic_enabled && (P.elastic_warm_start_enabled || P.elastic_residual_control_enabled);
+    if (accel) {
+        etrace = fopen((case_dir + "/elastic_solver_trace.csv").c_str(), "w");
+        if (etrace)
+            fprintf(etrace, "step,warm_start_used,iterations,relative_residual,converged,hard_cap,tolerance,"
+                            "solver_wall_s,source_field_step\n");
+    }
+    if (P.zero_mode_enabled) {
+        ztrace = fopen((case_dir + "/pf_zero_mode_trace.csv").c_str(), "w");
+        if (ztrace)
+            fprintf(ztrace, "step,target_mass_code,lambda,residual_code,derivative_code,iterations,newton_steps,"
+                            "bisection_steps,Y_star_min,Y_star_max,lambda_lower,lambda_upper,"
+                            "accepted_zero_mode_steps\n");
+    }
+    if (!csv || (accel && !etrace) || (P.zero_mode_enabled && !ztrace)) {
+        fprintf(stderr, "[fatal] cannot open the CSV outputs under %s\n", case_dir.c_str());
+        pfgb_destroy(ctx);
+        return 2;
+    }
+    fprintf(csv, "step,t_code,t_real_s,vf_precip,R_avg\n");
+
+    const char *dim = P.Ny == 2 ? "[2D]" : "[3D]";
+    auto csv_row = [&](int step) -> pfgb_status {
+        pfgb_diag d;
+        pfgb_status s = pfgb_diagnostics(ctx, &d);
+        if (s != PFGB_OK) return s;
+        double R_avg = 0.0;
+        if (d.n_if > 0.0) {
+            const double ratio = d.n_in / (d.n_if / (P.ic_phi_iface_w * 2.0));
+            R_avg = (P.Ny == 2 ? 2.0 : 3.0) * P.dx * ratio;
+        }
+        const double t = step * P.dt, t_real = t * P.t_real_unit;
+        fprintf(csv, "%d,%.8f,%.8e,%.8e,%.8e\n", step, t, t_real, d.vf_precip, R_avg);
+        fflush(csv);
+        printf("%s step=%05d t=%.6f t_real=%.6e s <x_B_tot>=%.6e vf_precip=%.6e R_avg_internal=%.6e "
+               "R_avg_nm=%.6e xB_range=[%.4f, %.4f] t_wall=%s\n",
+               dim, step, t, t_real, d.mass_xBtot / (double)N, d.vf_precip, R_avg, R_avg * unit_to_nm, d.xB_min,
+               d.xB_max, now_str().c_str());
+        return PFGB_OK;
+    };
+
+    if ((st = read_state()) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_read_fields"); }
+    vtk_set("_init");
+    write_vtk(case_dir + "/xB_0.vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
+    if ((st = csv_row(0)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_diagnostics"); }
+
+    std::vector<double> wall;
+    wall.reserve(c.nsteps);
+    const auto t0 = std::chrono::steady_clock::now();
+    int rc = 0;
+    unsigned long long accepted_zm = 0;
+    for (int step = 1; step <= c.nsteps; ++step) {
+        pfgb_step_stats s;
+        const auto a = std::chrono::steady_clock::now();
+        st = pfgb_step(ctx, 1, &s);
+        if (st == PFGB_OK) st = pfgb_sync(ctx);
+        const double w = std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+        if (st != PFGB_OK) { rc = fail(st, "pfgb_step"); break; }
+        wall.push_back(w);
+        if (etrace) {
+            fprintf(etrace, "%d,%d,%d,%.17e,%d,%d,%.17e,%.9f,%llu\n", step, s.elastic_warm_start_used,
+                    s.elastic_iterations, s.elastic_relative_residual, s.elastic_converged, P.elastic_iter_max,
+                    P.elastic_residual_tolerance, w, (unsigned long long)(step - 1));
+            fflush(etrace);
+        }
+        if (ztrace) {
+            ++accepted_zm;
+            fprintf(ztrace, "%d,%.17e,%.17e,%.17e,%.17e,%d,%d,%d,%.17e,%.17e,%.17e,%.17e,%llu\n", step,
+                    s.zero_mode_target_mass, s.zero_mode_lambda, s.zero_mode_residual, NAN, s.zero_mode_iterations,
+                    s.zero_mode_newton_steps, s.zero_mode_bisection_steps, NAN, NAN, NAN, NAN, accepted_zm);
+            fflush(ztrace);
+        }
+        if (step % c.csv_out_every == 0 && (st = csv_row(step)) != PFGB_OK) { rc = fail(st, "pfgb_diagnostics"); break; }
+        if (step % c.out_every == 0) {
+            if ((st = read_state()) != PFGB_OK) { rc = fail(st, "pfgb_read_fields"); break; }
+            vtk_set(("_" + std::to_string(step)).c_str());
+        }
+    }
+    const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (rc == 0) {
+        if ((st = read_state()) != PFGB_OK) rc = fail(st, "pfgb_read_fields");
+        else vtk_set("_final");
+    }
+    if (csv) fclose(csv);
+    if (etrace) fclose(etrace);
+    if (ztrace) fclose(ztrace);
+
+    // ---- performance summary (write_performance_summary_json, main_cuda.cu:3790) ----
+    std::vector<double> sorted = wall;
+    std::sort(sorted.begin(), sorted.end());
+    const double n = (double)wall.size();
+    double avg = 0.0, warm = 0.0;
+    for (double x : wall) avg += x;
+    avg = n > 0 ? avg / n : NAN;
+    for (size_t i = 1; i < wall.size(); ++i) warm += wall[i];
+    warm = wall.size() > 1 ? warm / (n - 1) : avg;
+    const double med = sorted.empty() ? NAN : sorted[sorted.size() / 2];
+    FILE *pj = fopen((case_dir + "/performance_summary.json").c_str(), "w");
+    if (pj) {
+        fprintf(pj,
+                "{\n  \"case_name\": \"%s\",\n  \"picard_enabled\": %.17e,\n  \"picard_iters\": %.17e,\n"
+                "  \"picard_omega\": %.17e,\n  \"nsteps\": %.17e,\n  \"dt\": %.17e,\n  \"total_walltime_s\": %.17e,\n"
+                "  \"avg_walltime_per_step_s\": %.17e,\n  \"median_walltime_per_step_s\": %.17e,\n"
+                "  \"min_walltime_per_step_s\": %.17e,\n  \"max_walltime_per_step_s\": %.17e,\n"
+                "  \"warmup_excluded_avg_walltime_per_step_s\": %.17e,\n  \"estimated_steps_per_hour\": %.17e,\n"
+                "  \"relative_slowdown_vs_baseline\": %.17e\n}\n",
+                tag.c_str(), 0.0, 1.0, 1.0, (double)c.nsteps, P.dt, total, avg, med,
+                sorted.empty() ? NAN : sorted.front(), sorted.empty() ? NAN : sorted.back(), warm,
+                warm > 0 ? 3600.0 / warm : NAN, NAN);
+        fclose(pj);
+    }
+    FILE *sm = fopen((case_dir + "/summary.txt").c_str(), "w");
+    if (sm) {
+        fprintf(sm, "case=%s\ngrid=%dx%dx%d\ndt=%.17g\nnsteps=%d\nsteps_done=%zu\nprecision=%s\n", tag.c_str(), P.Nx,
+                P.Ny, P.Nz, P.dt, c.nsteps, wall.size(), P.precision == PFGB_PREC_FP32 ? "fp32" : "fp64");
+        fprintf(sm, "total_walltime_s=%.6f\nMpts_per_s=%.6f\nexit_status=%d\n", total,
+                total > 0 ? (double)N * wall.size() / total / 1e6 : 0.0, rc);
+        fclose(sm);
+    }
+    printf("done: %zu steps, %.3f s, %.3f Mpts/s\n", wall.size(), total,
+           total > 0 ? (double)N * wall.size() / total / 1e6 : 0.0);
+    pfgb_destroy(ctx);
+    return rc;
+}

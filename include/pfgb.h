@@ -169,7 +169,9 @@ typedef struct pfgb_diag {
     double mean_xB;
     double phi_min, phi_max;
     double xB_min, xB_max;
-    double n_in;           /* cells with phi >= 0.5                      */
+    double n_in;           /* cells with phi > 0.5                       */
+    double n_if;           /* interface cells, 0.12 < phi < 0.88
+                              (gpu_reduce_sum_N_in_N_if, cuda_kernels.cu:5768) */
 } pfgb_diag;
 
 typedef struct pfgb_ctx pfgb_ctx;

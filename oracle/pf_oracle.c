@@ -1096,13 +1096,16 @@ int pfo_diagnostics(const pfo_state *s, pfgb_diag *d) {
     double *t = (double *)malloc(sizeof(double) * s->N);
     double *u = (double *)malloc(sizeof(double) * s->N);
     double *w = (double *)malloc(sizeof(double) * s->N);
+    double *f = (double *)malloc(sizeof(double) * s->N);
     double pmin = 1e300, pmax = -1e300, xmin = 1e300, xmax = -1e300;
     for (size_t i = 0; i < s->N; ++i) {
         double h = o_h(o_clamp01(s->phi[i]));
         t[i] = h;
         double hh = o_h(s->phi[i]);
         u[i] = (1.0 - hh) * s->xB[i] + P->v_B * hh;
-        w[i] = s->phi[i] >= 0.5 ? 1.0 : 0.0;
+        /* reduce_sum_N_in_N_if_kernel, cuda_kernels.cu:3746-3786 */
+        w[i] = s->phi[i] > 0.5 ? 1.0 : 0.0;
+        f[i] = (s->phi[i] > 0.12 && s->phi[i] < 0.88) ? 1.0 : 0.0;
         if (s->phi[i] < pmin) pmin = s->phi[i];
         if (s->phi[i] > pmax) pmax = s->phi[i];
         if (s->xB[i] < xmin) xmin = s->xB[i];
@@ -1112,7 +1115,8 @@ int pfo_diagnostics(const pfo_state *s, pfgb_diag *d) {
     d->mass_xBtot = dsum(u, s->N);
     d->mean_xB = dsum(s->xB, s->N) / (double)s->N;
     d->n_in = dsum(w, s->N);
+    d->n_if = dsum(f, s->N);
     d->phi_min = pmin; d->phi_max = pmax; d->xB_min = xmin; d->xB_max = xmax;
-    free(t); free(u); free(w);
+    free(t); free(u); free(w); free(f);
     return PFGB_OK;
 }

@@ -1,0 +1,106 @@
+"""The main_cuda driver: invocation, parameter file, raw-field input and the
+Results/ layout of the reference's dynamics runs (main_cuda.cu main())."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, params_for
+
+
+def _exe(capi):
+    from cuda_sto_pf_gb300 import build
+    return build.EXE
+
+
+def _run(capi, args, cwd, env=None):
+    e = dict(os.environ)
+    if env:
+        e.update(env)
+    return subprocess.run([_exe(capi), *args], cwd=cwd, env=e, capture_output=True, text=True, timeout=600)
+
+
+def test_cli_requires_param_file(capi, tmp_path):
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1"], tmp_path)
+    assert r.returncode == 2
+    assert "--pf-param-file" in r.stderr
+
+
+def test_cli_help(capi, tmp_path):
+    r = _run(capi, ["--help"], tmp_path)
+    assert r.returncode == 0 and "Nx Ny Nz dt nsteps out_every csv_out_every" in r.stdout
+
+
+def test_cli_rejects_bad_inputs(capi, tmp_path):
+    pf = os.path.join(GOLDEN, "c1.params")
+    # unsupported mode
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf, "--mode=minimize"], tmp_path)
+    assert r.returncode == 2
+    # no raw fields
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf], tmp_path)
+    assert r.returncode == 2 and "raw_fields" in r.stderr
+    # raw field of the wrong size
+    bad = tmp_path / "phi.raw"
+    np.zeros(10).tofile(bad)
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf, "--init-mode", "raw_fields",
+                    "--init-phi-raw", str(bad), "--init-xB-raw", str(bad)], tmp_path)
+    assert r.returncode == 2 and "expected" in r.stderr
+    # malformed parameter file
+    pbad = tmp_path / "bad.params"
+    pbad.write_text(open(pf).read() + "\nW=abc\n")
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", str(pbad)], tmp_path)
+    assert r.returncode == 2
+
+
+def _vtk_values(path, shape):
+    with open(path) as f:
+        lines = f.read().split("\n")
+    assert lines[0] == "# vtk DataFile Version 3.0" and lines[3] == "DATASET STRUCTURED_POINTS"
+    assert lines[4] == "DIMENSIONS %d %d %d" % shape
+    data = np.array(" ".join(lines[10:]).split(), dtype=np.float64)
+    nx, ny, nz = shape
+    # z outermost, x innermost
+    return data.reshape(nz, ny, nx).transpose(2, 1, 0)
+
+
+@pytest.mark.gpu
+def test_cli_dynamics_run_matches_library(capi, tmp_path):
+    from cuda_sto_pf_gb300 import workloads
+    from cuda_sto_pf_gb300.solver import Solver
+    n, steps = 16, 4
+    w = workloads.single_sphere(n=n, radius=5.0)
+    phi, xB = w["phi"], w["xB"]
+    phi.tofile(tmp_path / "phi.raw")
+    xB.tofile(tmp_path / "xB.raw")
+    pf = os.path.join(GOLDEN, "c2.params")
+    r = _run(capi, [str(n), str(n), str(n), "0.01", str(steps), "2", "1", "1", "--pf-param-file", pf,
+                    "--init-mode", "raw_fields", "--init-phi-raw", str(tmp_path / "phi.raw"),
+                    "--init-xB-raw", str(tmp_path / "xB.raw"), "--pf-zero-mode", "PF_CONSERVED_Y_ZERO_MODE_V1"],
+             tmp_path, env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "R")})
+    assert r.returncode == 0, r.stderr
+    runs = os.listdir(tmp_path / "R")
+    assert len(runs) == 1 and runs[0].startswith("chel_T") and "_cuda_16x16x16_dt0.01_steps4_xB0.030" in runs[0]
+    case = tmp_path / "R" / runs[0] / "raw_fields_relax"
+    for f in ("pf_input.params", "vf_precip_vs_time_raw_fields_relax.csv", "elastic_solver_trace.csv",
+              "pf_zero_mode_trace.csv", "performance_summary.json", "summary.txt", "phi_init.vtk", "phi_2.vtk",
+              "phi_4.vtk", "phi_final.vtk", "xB_0.vtk", "xBtot_final.vtk"):
+        assert (case / f).exists(), f
+    rows = (case / "vf_precip_vs_time_raw_fields_relax.csv").read_text().strip().split("\n")
+    assert rows[0] == "step,t_code,t_real_s,vf_precip,R_avg" and len(rows) == steps + 2
+    assert len((case / "elastic_solver_trace.csv").read_text().strip().split("\n")) == steps + 1
+    # the same run through the library API
+    p = params_for(capi, "c2.params", n=n, zero_mode_enabled=1, precision=0)
+    import ctypes
+    capi.load().pfgb_prepare_raw_fields(ctypes.byref(p), 0.07, phi.ctypes.data, xB.ctypes.data, None, None,
+                                        phi.size)
+    with Solver(p) as s:
+        s.load(phi, xB)
+        s.step(steps)
+        f = s.fields()
+        d = s.diagnostics()
+    last = rows[-1].split(",")
+    assert int(last[0]) == steps
+    assert abs(float(last[3]) - d.vf_precip) <= 1e-7 * max(1e-12, d.vf_precip)
+    got = _vtk_values(case / "phi_final.vtk", (n, n, n))
+    assert np.abs(got - f["phi"]).max() <= 6e-6

@@ -166,3 +166,25 @@ def test_parity_246_axes(capi, oracle, shape, prec):
     for k, v in errs.items():
         assert v <= (10 if k == "dYdt" else 1) * TOL[prec], (k, v)
     assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1
+
+
+def test_diagnostics_parity(capi, oracle):
+    """vf_precip, the xB_tot ledger, N_in / N_if (R_avg of the CSV row) and the
+    field ranges against the oracle after two steps."""
+    from cuda_sto_pf_gb300.solver import Solver
+    p = params_for(capi, "c2.params", n=24, precision=0)
+    phi, xB, _ = _inputs(capi, p, 24, False, seed=4)
+    o = oracle(p, threads=4)
+    o.load(phi, xB)
+    assert o.step(2) == 0
+    do = o.diagnostics(capi.Diag)
+    with Solver(p) as s:
+        s.load(phi, xB)
+        s.step(2)
+        d = s.diagnostics()
+    for f in ("vf_precip", "mass_xBtot", "mean_xB", "phi_min", "phi_max", "xB_min", "xB_max"):
+        a, b = getattr(d, f), getattr(do, f)
+        assert abs(a - b) <= 1e-7 * max(1e-12, abs(b)), (f, a, b)
+    # cell counts: a cell within 1e-9 of a threshold may fall either side
+    assert abs(d.n_in - do.n_in) <= 2 and abs(d.n_if - do.n_if) <= 2
+    assert d.n_if > 0 and d.n_in > 0
