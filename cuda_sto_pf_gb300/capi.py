@@ -66,6 +66,8 @@ class Params(Structure):
         ("t_real_unit", c_double),
         ("ic_vf_init_phi", c_double), ("ic_vf_target_phi", c_double), ("ic_phi_iface_w", c_double),
         ("gamma_Jm2", c_double), ("lambda_sm_m", c_double), ("Vm_alpha_0_phys_m3mol", c_double),
+        ("ic_23d_xB_out", c_double), ("ic_phi_seed_radius", c_double), ("minimize_min_pseudo_time", c_double),
+        ("ic_phi_num_seeds", c_int32), ("pad2", c_int32),
         ("temperature_K", c_double), ("mu0_compound", c_double), ("xB_eq_matrix", c_double),
     ]
 
@@ -79,6 +81,19 @@ class StepStats(Structure):
         ("zero_mode_lambda", c_double), ("zero_mode_residual", c_double),
         ("zero_mode_target_mass", c_double), ("mean_DY", c_double),
     ]
+
+
+class MinStats(Structure):
+    _fields_ = [("iteration", c_int32), ("converged", c_int32), ("converged_iteration", c_int32),
+                ("convergence_count", c_int32), ("condA", c_int32), ("condB", c_int32),
+                ("xB_clamped", c_int32), ("elastic_iterations", c_int32),
+                ("mean_h", c_double), ("V0_target", c_double), ("lambda_vol", c_double),
+                ("F_surf", c_double), ("F_el", c_double), ("F_chem_excess", c_double),
+                ("F_total_excess", c_double), ("F_chem_CNT", c_double), ("F_total_CNT", c_double),
+                ("total_interface_sum", c_double), ("total_el_core_sum", c_double),
+                ("rms_res", c_double), ("rms_dphi", c_double), ("rms_dY", c_double),
+                ("energy_diff_rel", c_double), ("vol_err_rel", c_double),
+                ("elastic_relative_residual", c_double)]
 
 
 class Diag(Structure):
@@ -106,6 +121,7 @@ EXPORTS = [
     ("pfgb_load_fields_device", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("pfgb_set_fields", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("pfgb_step", c_int, [c_void_p, c_int, POINTER(StepStats)]),
+    ("pfgb_minimize", c_int, [c_void_p, c_int, c_int, POINTER(MinStats)]),
     ("pfgb_read_fields", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("pfgb_read_elastic", c_int, [c_void_p, c_void_p, c_void_p]),
     ("pfgb_read_displacement_k", c_int, [c_void_p, c_void_p]),

@@ -82,6 +82,8 @@ const DKey kDoubles[] = {
     DK("ic_vf_init_phi", ic_vf_init_phi), DK("ic_vf_target_phi", ic_vf_target_phi),
     DK("ic_phi_iface_w", ic_phi_iface_w), DK("gamma_Jm2", gamma_Jm2), DK("lambda_sm_m", lambda_sm_m),
     DK("Vm_alpha_0_phys_m3mol", Vm_alpha_0_phys_m3mol),
+    DK("ic_23d_xB_out", ic_23d_xB_out), DK("xB_alpha_initial", ic_23d_xB_out),
+    DK("ic_phi_seed_radius", ic_phi_seed_radius), DK("minimize_min_pseudo_time", minimize_min_pseudo_time),
 };
 const DKey kInts[] = {
     DK("pf_params_schema_version", pf_params_schema_version),
@@ -97,6 +99,7 @@ const DKey kInts[] = {
     DK("minimize_full_model", minimize_full_model),
     DK("minimize_post_projection_iters", minimize_post_projection_iters),
     DK("minimize_max_iter", minimize_max_iter), DK("minimize_convergence_steps", minimize_convergence_steps),
+    DK("ic_phi_num_seeds", ic_phi_num_seeds),
 };
 #undef DK
 

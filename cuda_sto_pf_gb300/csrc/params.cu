@@ -131,6 +131,10 @@ void pfgb_params_default(pfgb_params *p) {
     p->minimize_V0 = 0.0;
     p->eta_lambda_vol = 0.2;
     p->minimize_xB_max_safe = 0.07;
+    p->minimize_min_pseudo_time = 0.0;
+    p->ic_23d_xB_out = 0.03;        // params_default, main_cuda.cu:16215
+    p->ic_phi_seed_radius = 10.0;   // main_cuda.cu:16221
+    p->ic_phi_num_seeds = 1;
     p->minimize_rms_dphi_threshold = 1.0e-6;
     p->minimize_rms_dY_threshold = 5.0e-5;
     p->minimize_energy_diff_rel_threshold = 1.0e-9;

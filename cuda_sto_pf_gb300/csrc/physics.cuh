@@ -38,8 +38,20 @@ struct PhysC {
     double gp_Cg;           // offA(xg)(1-xg) + offB(xg) xg - delta_g0
     int gp, gp_el, act_eta, act_phi;
     int coupling, elastic, zm, prev_level, disable_gamma, xb_raw;
+    // upper cap on the composition seen by the eigenstrain of the elastic
+    // solve and the stress (minimize_xB_max_safe once the minimize monitor
+    // has clamped xB; above 1 = inactive)
+    double xbcap;
+    double dx, dy, dz;
     ThermoConst tc;
 };
+
+// composition entering eps0 on the elastic side: clamp01, then the cap
+template <typename T>
+__device__ __forceinline__ T xB_el(const PhysC &c, T xB) {
+    const T x = clamp01(xB);
+    return x < T(c.xbcap) ? x : T(c.xbcap);
+}
 
 // Elastic constants in elastic precision (the reference casts S, S_p, eps00,
 // E0 to float, main_cuda.cu:28762-28790).
@@ -88,7 +100,7 @@ template <typename T, typename TE>
 __device__ __forceinline__ void stress_at(const PhysC &c, const ElasC<TE> &ec, T phi, T eta, T xB,
                                           const TE eps[6], TE sig[6]) {
     TE e0[6];
-    eigenstrain<T, TE>(c, ec, phi, eta, clamp01(xB), c.gp_el != 0, e0);
+    eigenstrain<T, TE>(c, ec, phi, eta, xB_el(c, xB), c.gp_el != 0, e0);
     TE el[6];
 #pragma unroll
     for (int a = 0; a < 6; ++a) el[a] = eps[a] - e0[a];
@@ -121,10 +133,11 @@ __device__ __forceinline__ T q_voigt(const double *Sp, const T el[6]) {
 }
 
 // explicit Allen-Cahn driving force of phi (compute_phi_rhs_kernel,
-// cuda_kernels.cu:390-555): double well + chemical + elastic.
+// cuda_kernels.cu:390-555): double well + chemical + elastic, with the
+// stress given (the reference reads its stored sigma arrays)
 template <typename T, typename TE>
-__device__ __forceinline__ T phi_rhs(const PhysC &c, const ElasC<TE> &ec, T phi, T eta_raw, T xBraw,
-                                     const TE *eps) {
+__device__ __forceinline__ T phi_rhs_sig(const PhysC &c, const ElasC<TE> &ec, T phi, T eta_raw, T xBraw,
+                                         const TE *eps, const TE *sg_) {
     const T hp = pf_hp(phi), gp = pf_gp(phi), h = pf_h(phi);
     const T eta = clamp01(eta_raw);
     const T xB = clamp01(xBraw);
@@ -139,8 +152,6 @@ __device__ __forceinline__ T phi_rhs(const PhysC &c, const ElasC<TE> &ec, T phi,
     const T vt = T(c.Vmc) - Vma + T(c.dVm) * (xB - T(c.vB));
     f += cb * hp * (dmu - cb * mt * vt);
     if (c.coupling) {
-        TE sg_[6];
-        stress_at<T, TE>(c, ec, phi, eta_raw, xBraw, eps, sg_);
         T sg[6];
 #pragma unroll
         for (int a = 0; a < 6; ++a) sg[a] = T(sg_[a]);
@@ -179,6 +190,16 @@ __device__ __forceinline__ T phi_rhs(const PhysC &c, const ElasC<TE> &ec, T phi,
         f += part;
     }
     return f;
+}
+
+// the same with sigma from Hooke's law at (phi, eta, xB): the dynamics step,
+// where the stored stress of the reference is that of the current fields
+template <typename T, typename TE>
+__device__ __forceinline__ T phi_rhs(const PhysC &c, const ElasC<TE> &ec, T phi, T eta_raw, T xBraw,
+                                     const TE *eps) {
+    TE sg[6];
+    if (c.coupling) stress_at<T, TE>(c, ec, phi, eta_raw, xBraw, eps, sg);
+    return phi_rhs_sig<T, TE>(c, ec, phi, eta_raw, xBraw, eps, sg);
 }
 
 // GP-zone Allen-Cahn driving force of eta (compute_eta_rhs_kernel,

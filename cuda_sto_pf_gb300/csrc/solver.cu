@@ -47,6 +47,8 @@ struct DevState {
     KTab kt;
     T *phi_old, *phi_new, *eta_old, *eta_new, *Y, *dYdt;
     T *Yprev;           // Y_f at the start of the step (the elastic solve's Y)
+    TE *sig[6];         // stored stress of the elastic solve (minimize only, else null)
+    T *mge, *mlap;      // minimize: explicit phi drive and Lap(phi)
     TE *eps[6];
     cplx_t<T> *S[4];
     cplx_t<TE> *E[6], *U[3];
@@ -78,6 +80,11 @@ struct pfgb_ctx {
     double Yc = 0.0, dYoff = 0.0, target_mass = 0.0;
     double Yc_prev = 0.0;    // Yc at the last step's start
     bool f246[3] = {false, false, false};   // x, y, z elastic passes on the 246-point engine
+    // minimize state (mode = minimize)
+    void *sig[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    void *mge = nullptr, *mlap = nullptr;
+    double lambda_vol = 0.0, V0_target = 0.0, prev_F_total = NAN;
+    int min_iter = 0, conv_count = 0, converged_iter = 0, xb_clamp = 0;
     double sum_alpha = 0.0;   // sum (1 - h) of the last phi (zero-mode curvature bound)
     int warm_valid = 0, step = 0, loaded = 0;
     size_t bytes = 0;
@@ -566,7 +573,7 @@ struct OpEigenR2C {
     DevState<T, TE> d; PhysC c; ElasC<TE> ec;
     __device__ void point(long long cell, const TE *, TE *out, Acc &) const {
         const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
-        eigenstrain<T, TE>(c, ec, d.phi_old[cell], c.gp ? d.eta_old[cell] : T(0), clamp01(xB),
+        eigenstrain<T, TE>(c, ec, d.phi_old[cell], c.gp ? d.eta_old[cell] : T(0), xB_el(c, xB),
                            c.gp_el != 0, out);
     }
     __device__ void load_spec(long long, int, cplx_t<TE> *) const {}
@@ -594,7 +601,7 @@ struct OpHijZ {
         for (int a = 0; a < 6; ++a) e[a] = in[a] * ec.invN;
         const T phi = d.phi_old[cell];
         const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
-        eigenstrain<T, TE>(c, ec, phi, c.gp ? d.eta_old[cell] : T(0), clamp01(xB), c.gp_el != 0, e0);
+        eigenstrain<T, TE>(c, ec, phi, c.gp ? d.eta_old[cell] : T(0), xB_el(c, xB), c.gp_el != 0, e0);
         const T h = pf_h(phi);
         TE tv[6];
 #pragma unroll
@@ -624,15 +631,28 @@ struct OpHijZ {
 template <typename T, typename TE>
 struct OpStrainFinalZ {
     using Acc = NoAcc;
-    DevState<T, TE> d; ElasC<TE> ec;
+    DevState<T, TE> d; ElasC<TE> ec; PhysC c;
     __device__ void load_spec(long long row, int k, cplx_t<TE> *v) const {
         const long long o = row * d.g.NzC + k;
 #pragma unroll
         for (int a = 0; a < 6; ++a) v[a] = d.E[a][o];
     }
     __device__ void point(long long cell, const TE *in, TE *, Acc &) const {
+        TE e[6];
 #pragma unroll
-        for (int a = 0; a < 6; ++a) d.eps[a][cell] = in[a] * ec.invN + ec.E0[a];
+        for (int a = 0; a < 6; ++a) {
+            e[a] = in[a] * ec.invN + ec.E0[a];
+            d.eps[a][cell] = e[a];
+        }
+        if (d.sig[0]) {
+            // compute_stress_from_strain_with_effective_stiffness_kernel
+            // (:7381-7480): the stress kept for the rest of the iteration
+            TE sg[6];
+            const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
+            stress_at<T, TE>(c, ec, d.phi_old[cell], c.gp ? d.eta_old[cell] : T(0), xB, e, sg);
+#pragma unroll
+            for (int a = 0; a < 6; ++a) d.sig[a][cell] = sg[a];
+        }
     }
     __device__ void store_spec(long long, int, const cplx_t<TE> *) const {}
 };
@@ -1113,6 +1133,9 @@ static DevState<T, TE> dev_state(pfgb_ctx *c) {
     d.eta_new = (T *)c->eta[1 - c->ecur];
     d.Y = (T *)c->Y;
     d.Yprev = (T *)c->Yprev;
+    for (int i = 0; i < 6; ++i) d.sig[i] = (TE *)c->sig[i];
+    d.mge = (T *)c->mge;
+    d.mlap = (T *)c->mlap;
     d.dYdt = (T *)c->dYdt;
     for (int i = 0; i < 6; ++i) { d.eps[i] = (TE *)c->eps[i]; d.E[i] = (cplx_t<TE> *)c->E[i]; }
     for (int i = 0; i < 3; ++i) d.U[i] = (cplx_t<TE> *)c->U[i];
@@ -1226,7 +1249,8 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
                            c->step + 1, iter, rel);
         return PFGB_ERR_NONCONVERGED;
     }
-    TRY((launch_z<TE, 6, 0>(c, OpStrainFinalZ<T, TE>{d, ec}, "z_strain_final", 6.0 * Nf * sizeof(TE))));
+    TRY((launch_z<TE, 6, 0>(c, OpStrainFinalZ<T, TE>{d, ec, pc}, "z_strain_final",
+                                (d.sig[0] ? 12.0 : 6.0) * Nf * sizeof(TE))));
     return PFGB_OK;
 }
 
@@ -1367,38 +1391,19 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     return PFGB_OK;
 }
 
+// Y (composition) update: mu -> flux -> semi-implicit update -> dY/dt and
+// the zero mode (main_cuda.cu:30280-30800, 31618-31623).  d.phi_old = phi^n,
+// d.phi_new = phi^{n+1}; Y and the stored strain are those of the step start.
 template <typename T, typename TE>
-static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
-    using T2 = cplx_t<T>;
+static pfgb_status y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_stats *st) {
     const pfgb_params &P = c->p;
     const PhysC pc = c->pc;
     const ElasC<TE> ec = elas_consts<TE>(c);
-    c->Yc_prev = c->Yc;
-    if (P.elastic_enabled) TRY((elastic_solve<T, TE>(c, st)));
-    DevState<T, TE> d = dev_state<T, TE>(c);
     const KTab kt = d.kt;
     const double invN = 1.0 / (double)c->g.N;
     const double Nf = (double)c->g.N;
     AxisIO<T, 1, 1> io1;
     io1.in[0] = d.S[0]; io1.out[0] = d.S[0];
-
-    // ---- phi ----
-    TRY((launch_z<T, 0, 1>(c, OpPhiR2C<T, TE>{d, pc, ec}, "z_phi_rhs", (2.0 + pc.gp) * Nf * sizeof(T) + (pc.coupling ? 6.0 : 0.0) * Nf * sizeof(TE))));
-    TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
-    TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpACFilterX<T>{kt, P.L_phi * P.dt * P.kappa_phi, invN}, "x_ac_filter")));
-    TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
-    TRY((launch_z<T, 1, 0>(c, OpACStoreZ<T, TE>{d.S[0], d.phi_new, c->g.NzC, T(-1e-6), T(1.0 + 1e-6)}, "z_ac_store", Nf * sizeof(T))));
-
-    // ---- eta (GP zone) ----
-    if (pc.gp) {
-        TRY((launch_z<T, 0, 1>(c, OpEtaR2C<T, TE>{d, pc, ec}, "z_eta_rhs", 3.0 * Nf * sizeof(T))));
-        TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
-        TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpACFilterX<T>{kt, P.gp_L_eta * P.dt * P.gp_kappa_eta, invN}, "x_ac_filter")));
-        TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
-        TRY((launch_z<T, 1, 0>(c, OpACStoreZ<T, TE>{d.S[0], d.eta_new, c->g.NzC, T(0), T(1)}, "z_ac_store", Nf * sizeof(T))));
-    }
-
-    // ---- Y ----
     int nb = 0;
     TRY((launch_z<T, 0, 1>(c, OpMuR2C<T, TE>{d, pc, ec}, "z_mu", (3.0 + pc.gp) * Nf * sizeof(T) + (pc.elastic ? 6.0 : 0.0) * Nf * sizeof(TE), &nb)));
     TRY(reduce_to<AccSum1>(c, nb, DS_MEAN_DY, invN));
@@ -1436,10 +1441,453 @@ static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
         if (!P.zero_mode_enabled) TRY(sync_read(c, DS_MEAN_DY, 1));
         st->mean_DY = c->hscal[DS_MEAN_DY];
     }
+    return PFGB_OK;
+}
+
+template <typename T, typename TE>
+static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
+    using T2 = cplx_t<T>;
+    const pfgb_params &P = c->p;
+    const PhysC pc = c->pc;
+    const ElasC<TE> ec = elas_consts<TE>(c);
+    c->Yc_prev = c->Yc;
+    if (P.elastic_enabled) TRY((elastic_solve<T, TE>(c, st)));
+    DevState<T, TE> d = dev_state<T, TE>(c);
+    const KTab kt = d.kt;
+    const double invN = 1.0 / (double)c->g.N;
+    const double Nf = (double)c->g.N;
+    AxisIO<T, 1, 1> io1;
+    io1.in[0] = d.S[0]; io1.out[0] = d.S[0];
+
+    // ---- phi ----
+    TRY((launch_z<T, 0, 1>(c, OpPhiR2C<T, TE>{d, pc, ec}, "z_phi_rhs", (2.0 + pc.gp) * Nf * sizeof(T) + (pc.coupling ? 6.0 : 0.0) * Nf * sizeof(TE))));
+    TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
+    TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpACFilterX<T>{kt, P.L_phi * P.dt * P.kappa_phi, invN}, "x_ac_filter")));
+    TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+    TRY((launch_z<T, 1, 0>(c, OpACStoreZ<T, TE>{d.S[0], d.phi_new, c->g.NzC, T(-1e-6), T(1.0 + 1e-6)}, "z_ac_store", Nf * sizeof(T))));
+
+    // ---- eta (GP zone) ----
+    if (pc.gp) {
+        TRY((launch_z<T, 0, 1>(c, OpEtaR2C<T, TE>{d, pc, ec}, "z_eta_rhs", 3.0 * Nf * sizeof(T))));
+        TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
+        TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpACFilterX<T>{kt, P.gp_L_eta * P.dt * P.gp_kappa_eta, invN}, "x_ac_filter")));
+        TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+        TRY((launch_z<T, 1, 0>(c, OpACStoreZ<T, TE>{d.S[0], d.eta_new, c->g.NzC, T(0), T(1)}, "z_ac_store", Nf * sizeof(T))));
+    }
+
+    TRY((y_update<T, TE>(c, d, st)));
     c->cur = 1 - c->cur;
     if (pc.gp) c->ecur = 1 - c->ecur;
     c->step++;
     (void)sizeof(T2);
+    return PFGB_OK;
+}
+
+// ===========================================================================
+// minimize (mode = minimize, full model, two_phase): gradient flow of phi
+// with the Lagrange volume multiplier, the Y update, post-projection and the
+// V0 projection (main_cuda.cu:29264-29750, 32100-32600)
+// ===========================================================================
+// z pass producer: explicit drive g_e at phi (stored in mge; stress frozen
+// at the iteration's elastic solve) and phi itself -> R2C for Lap(phi)
+template <typename T, typename TE>
+struct OpMinGradZ {
+    using Acc = NoAcc;
+    DevState<T, TE> d; PhysC c; ElasC<TE> ec; const T *phi;
+    __device__ void point(long long cell, const T *, T *out, Acc &) const {
+        const T p = phi[cell];
+        const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
+        TE e[6], sg[6];
+        if (c.coupling) {
+#pragma unroll
+            for (int a = 0; a < 6; ++a) { e[a] = d.eps[a][cell]; sg[a] = d.sig[a][cell]; }
+        }
+        d.mge[cell] = phi_rhs_sig<T, TE>(c, ec, p, T(0), xB, e, sg);
+        out[0] = p;
+    }
+    __device__ void load_spec(long long, int, cplx_t<T> *) const {}
+    __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
+        d.S[0][row * d.g.NzC + k] = v[0];
+    }
+};
+
+// x pass: Lap = mask (-k^2) mask phi_k / N (compute_laplacian_k_kernel)
+template <typename T>
+struct OpLapX {
+    static constexpr bool kInplace = false;
+    KTab kt; double invN;
+    __device__ void apply(int i, int j, int k, const cplx_t<T> *in, cplx_t<T> *out) const {
+        if (kt.cut(i, j, k)) { out[0] = mk2<cplx_t<T>>(T(0), T(0)); return; }
+        out[0] = cscale(in[0], T(-kt.k2(i, j, k) * invN));
+    }
+};
+
+// z pass consumer: store Lap(phi); sums of h'(phi) g_full and h'(phi)^2 with
+// g_full = g_e - kappa Lap (the volume multiplier, :29484-29489)
+template <typename T, typename TE>
+struct OpMinLapZ {
+    using Acc = AccSum2;
+    DevState<T, TE> d; const T *phi; double kappa;
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = d.S[0][row * d.g.NzC + k]; }
+    __device__ void point(long long cell, const T *in, T *, Acc &acc) const {
+        const T lap = in[0];
+        d.mlap[cell] = lap;
+        const T gf = d.mge[cell] - T(kappa) * lap;
+        const T hp = pf_hp(phi[cell]);
+        acc.a += double(hp * gf);
+        acc.b += double(hp * hp);
+    }
+    __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
+    __device__ void finish(int b, const Acc &a) const { reinterpret_cast<Acc *>(d.partials)[b] = a; }
+};
+
+// z pass producer of the constrained step: phi - L dt [(g_full + kappa Lap) + lambda h']
+template <typename T, typename TE>
+struct OpMinStepR2C {
+    using Acc = NoAcc;
+    DevState<T, TE> d; const T *phi; double kappa, Ldt, lambda;
+    __device__ void point(long long cell, const T *, T *out, Acc &) const {
+        const T p = phi[cell];
+        const T lap = d.mlap[cell];
+        const T gf = d.mge[cell] - T(kappa) * lap;
+        const T r = (gf - T(-kappa) * lap) + T(lambda) * pf_hp(p);
+        out[0] = p - T(Ldt) * r;
+    }
+    __device__ void load_spec(long long, int, cplx_t<T> *) const {}
+    __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
+        d.S[0][row * d.g.NzC + k] = v[0];
+    }
+};
+
+// energies of the iteration start (:29264-29345): <h>, gradient energy by
+// central differences, double well, elastic energy density and its h-weighted
+// sum (compute_gel_density_kernel), chemical excess (compute_gbulk_excess_hat)
+struct AccMinE {
+    static constexpr bool kActive = true;
+    double mh, grad, dw, gel, gelh, chem;
+    __device__ static AccMinE identity() { return {0, 0, 0, 0, 0, 0}; }
+    __device__ static AccMinE combine(AccMinE a, const AccMinE &b) {
+        a.mh += b.mh; a.grad += b.grad; a.dw += b.dw; a.gel += b.gel; a.gelh += b.gelh; a.chem += b.chem;
+        return a;
+    }
+    __device__ static AccMinE shfl_down(AccMinE a, int o) {
+        AccMinE r;
+        double *pa = reinterpret_cast<double *>(&a), *pr = reinterpret_cast<double *>(&r);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) pr[i] = __shfl_down_sync(0xffffffffu, pa[i], o);
+        return r;
+    }
+};
+
+template <typename T, typename TE>
+__global__ void __launch_bounds__(256)
+k_min_energy(DevState<T, TE> d, PhysC c, ElasC<TE> ec, const T *phi, double g0, AccMinE *part) {
+    AccMinE a = AccMinE::identity();
+    const int Nx = d.g.Nx, Ny = d.g.Ny, Nz = d.g.Nz;
+    const double idx2 = 0.5 / c.dx, idy2 = 0.5 / c.dy, idz2 = 0.5 / c.dz;
+    for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < d.g.N;
+         cell += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(cell % Nz);
+        const long long r = cell / Nz;
+        const int j = (int)(r % Ny), i = (int)(r / Ny);
+        const int ip = i + 1 == Nx ? 0 : i + 1, im = i == 0 ? Nx - 1 : i - 1;
+        const int jp = j + 1 == Ny ? 0 : j + 1, jm = j == 0 ? Ny - 1 : j - 1;
+        const int kp = k + 1 == Nz ? 0 : k + 1, km = k == 0 ? Nz - 1 : k - 1;
+        const double gx = (double(phi[((long long)ip * Ny + j) * Nz + k]) - double(phi[((long long)im * Ny + j) * Nz + k])) * idx2;
+        const double gy = (double(phi[((long long)i * Ny + jp) * Nz + k]) - double(phi[((long long)i * Ny + jm) * Nz + k])) * idy2;
+        const double gz = (double(phi[r * Nz + kp]) - double(phi[r * Nz + km])) * idz2;
+        const T p = phi[cell];
+        a.grad += 0.5 * c.kappa * (gx * gx + gy * gy + gz * gz);
+        a.dw += c.W * double(pf_g(p));
+        const T h = pf_h(clamp01(p));
+        a.mh += double(h);
+        // the monitor's composition: sigmoid(Y), capped once clamped
+        const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
+        const T xm = xB < T(c.xbcap) ? xB : T(c.xbcap);
+        if (c.elastic) {
+            TE e0[6];
+            eigenstrain<T, TE>(c, ec, p, T(0), clamp01(xm), false, e0);
+            double sd = 0.0;
+#pragma unroll
+            for (int q = 0; q < 6; ++q)
+                sd += (q < 3 ? 1.0 : 2.0) * double(d.sig[q][cell]) * (double(d.eps[q][cell]) - double(e0[q]));
+            a.gel += 0.5 * sd;
+            a.gelh += 0.5 * sd * double(h);
+        }
+        const T x = clamp_eps(xm, T(1e-12));
+        T offA, offB;
+        thermo_mu_off<T>(c.tc, x, offA, offB);
+        const double mix = (1.0 - double(x)) * (c.tc.GA_s + double(offA)) + double(x) * (c.tc.GB_s + double(offB));
+        a.chem += (1.0 - double(h)) * mix + double(h) * c.mu0 - g0;
+    }
+    block_reduce_acc(a);
+    if (threadIdx.x == 0) part[blockIdx.x] = a;
+}
+
+// projected KKT residual (:684-708) with the exact multiplier, and |phi - phi^n|^2
+template <typename T, typename TE>
+__global__ void __launch_bounds__(256)
+k_min_resid(DevState<T, TE> d, const T *phi, const T *phin, double kappa, double lk, AccSum2 *part) {
+    AccSum2 a = AccSum2::identity();
+    for (long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x; cell < d.g.N;
+         cell += (long long)gridDim.x * blockDim.x) {
+        const T p = phi[cell];
+        T rr = (d.mge[cell] - T(kappa) * d.mlap[cell]) + T(lk) * pf_hp(p);
+        if ((p <= T(1e-12) && rr > T(0)) || (p >= T(1) - T(1e-12) && rr < T(0))) rr = T(0);
+        a.a += double(rr) * double(rr);
+        const double dp = double(p) - double(phin[cell]);
+        a.b += dp * dp;
+    }
+    block_reduce_acc(a);
+    if (threadIdx.x == 0) part[blockIdx.x] = a;
+}
+
+// sum h(clamp01 phi) and sum h'(phi)^2 (gpu_compute_vf_from_h, :5609; hprime_sq)
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_min_hsums(const T *phi, long long N, AccSum2 *part) {
+    AccSum2 a = AccSum2::identity();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const T p = phi[i];
+        a.a += double(pf_h(clamp01(p)));
+        const T hp = pf_hp(p);
+        a.b += double(hp * hp);
+    }
+    block_reduce_acc(a);
+    if (threadIdx.x == 0) part[blockIdx.x] = a;
+}
+
+// apply_volume_projection_kernel (:636-645)
+template <typename T>
+__global__ void k_min_project(T *phi, long long N, double lc) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const T p = phi[i];
+        phi[i] = clamp01(p + T(lc) * pf_hp(p));
+    }
+}
+
+// |Y - Y^n|^2 and the largest xB (the monitor's safety clamp test)
+struct AccSumMax {
+    static constexpr bool kActive = true;
+    double s, m;
+    __device__ static AccSumMax identity() { return {0.0, -1e300}; }
+    __device__ static AccSumMax combine(AccSumMax a, AccSumMax b) { return {a.s + b.s, fmax(a.m, b.m)}; }
+    __device__ static AccSumMax shfl_down(AccSumMax x, int o) {
+        return {__shfl_down_sync(0xffffffffu, x.s, o), __shfl_down_sync(0xffffffffu, x.m, o)};
+    }
+};
+template <typename T, typename TE>
+__global__ void __launch_bounds__(256)
+k_min_dy(DevState<T, TE> d, PhysC c, double yc_prev, AccSumMax *part) {
+    AccSumMax a = AccSumMax::identity();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.g.N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double y = double(d.Y[i]) + d.Yc, yp = double(d.Yprev[i]) + yc_prev;
+        a.s += (y - yp) * (y - yp);
+        a.m = fmax(a.m, double(xB_of_Y<T>(c, T(y))));
+    }
+    block_reduce_acc(a);
+    if (threadIdx.x == 0) part[blockIdx.x] = a;
+}
+
+static const int kMinBlocks = 1216;   // 8 x 152 SMs
+
+// Lap(phi), g_e and the multiplier sums at `phi`; returns -sum h'g / sum h'^2
+template <typename T, typename TE>
+static pfgb_status min_gradient(pfgb_ctx *c, const DevState<T, TE> &d, const T *phi, double *lambda) {
+    const double invN = 1.0 / (double)c->g.N, Nf = (double)c->g.N;
+    const ElasC<TE> ec = elas_consts<TE>(c);
+    AxisIO<T, 1, 1> io1;
+    io1.in[0] = d.S[0]; io1.out[0] = d.S[0];
+    TRY((launch_z<T, 0, 1>(c, OpMinGradZ<T, TE>{d, c->pc, ec, phi}, "z_min_grad",
+                           3.0 * Nf * sizeof(T) + (c->pc.coupling ? 12.0 : 0.0) * Nf * sizeof(TE))));
+    TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
+    TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpLapX<T>{d.kt, invN}, "x_lap")));
+    TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+    int nb = 0;
+    TRY((launch_z<T, 1, 0>(c, OpMinLapZ<T, TE>{d, phi, c->p.kappa_phi}, "z_min_lap", 3.0 * Nf * sizeof(T), &nb)));
+    TRY(reduce_to<AccSum2>(c, nb, 40));
+    TRY(sync_read(c, 40, 2));
+    const double shg = c->hscal[40], sh2 = c->hscal[41];
+    *lambda = std::fabs(sh2) > 1e-30 ? -shg / sh2 : 0.0;
+    return PFGB_OK;
+}
+
+// semi-implicit constrained step from `src` into `dst` (the reference's
+// phi_semi_implicit_update + dealias + Z2D + normalize_and_clamp)
+template <typename T, typename TE>
+static pfgb_status min_step(pfgb_ctx *c, const DevState<T, TE> &d, const T *src, T *dst, double lambda) {
+    const pfgb_params &P = c->p;
+    const double invN = 1.0 / (double)c->g.N, Nf = (double)c->g.N;
+    AxisIO<T, 1, 1> io1;
+    io1.in[0] = d.S[0]; io1.out[0] = d.S[0];
+    TRY((launch_z<T, 0, 1>(c, OpMinStepR2C<T, TE>{d, src, P.kappa_phi, P.L_phi * P.dt, lambda}, "z_min_step",
+                           3.0 * Nf * sizeof(T))));
+    TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
+    TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpACFilterX<T>{d.kt, P.L_phi * P.dt * P.kappa_phi, invN}, "x_ac_filter")));
+    TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+    TRY((launch_z<T, 1, 0>(c, OpACStoreZ<T, TE>{d.S[0], dst, c->g.NzC, T(-1e-6), T(1.0 + 1e-6)}, "z_ac_store", Nf * sizeof(T))));
+    return PFGB_OK;
+}
+
+template <typename Acc, typename K, typename... A>
+static pfgb_status min_reduce(pfgb_ctx *c, const char *tag, double bytes, int slot, int n, K kern, A... args) {
+    {
+        ProfScope ps(c, {tag, bytes});
+        kern<<<kMinBlocks, 256, 0, c->stream>>>(args..., (Acc *)c->partials);
+        PFGB_CUDA_TRY(cudaGetLastError());
+    }
+    TRY(reduce_to<Acc>(c, kMinBlocks, slot));
+    TRY(sync_read(c, slot, n));
+    return PFGB_OK;
+}
+
+template <typename T, typename TE>
+static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
+    const pfgb_params &P = c->p;
+    const double Nf = (double)c->g.N;
+    const long long N = c->g.N;
+    c->pc.xbcap = c->xb_clamp ? P.minimize_xB_max_safe : 2.0;
+    c->Yc_prev = c->Yc;
+    pfgb_step_stats st;
+    memset(&st, 0, sizeof(st));
+    if (P.elastic_enabled) TRY((elastic_solve<T, TE>(c, &st)));
+    const int it = ++c->min_iter;
+    const PhysC pc = c->pc;
+    const ElasC<TE> ec = elas_consts<TE>(c);
+    DevState<T, TE> d = dev_state<T, TE>(c);
+    T *pa = (T *)c->phi[c->cur], *pb = (T *)c->phi[1 - c->cur];
+
+    // ---- energies of the iteration start ----
+    // reference state of the chemical excess (main_cuda.cu:27400-27431)
+    const double xref = P.ic_23d_xB_out;
+    double oA, oB;
+    thermo_mu_off<double>(c->pc.tc, xref, oA, oB);
+    const double muAr = c->pc.tc.GA_s + oA, muBf = c->pc.tc.GB_s + oB;
+    const double g0 = (1.0 - xref) * muAr + xref * muBf;
+    TRY((min_reduce<AccMinE>(c, "min_energy", (2.0 * Nf) * sizeof(T) + 12.0 * Nf * sizeof(TE), 42, 6,
+                             k_min_energy<T, TE>, d, pc, ec, (const T *)pa, g0)));
+    const double *E = c->hscal + 42;
+    double mean_h = E[0] / Nf;
+    if (it == 1 && !(c->V0_target > 0.0)) {
+        if (P.ic_phi_seed_radius > 0.0) {   // compute_effective_vf_target, :2459-2490 (spherical seeds)
+            double vf = std::fmin(0.999, std::fmax(1e-6, P.ic_vf_target_phi));
+            const int ns = P.ic_phi_num_seeds > 0 ? P.ic_phi_num_seeds : 1;
+            const double R = P.ic_phi_seed_radius;
+            const double Lx = P.Nx * P.dx, Ly = P.Ny * P.dy, Lz = P.Nz * P.dz;
+            if (P.Ny > 2) { if (Lx * Ly * Lz > 0.0) vf = ns * (4.0 * PFGB_PI / 3.0) * R * R * R / (Lx * Ly * Lz); }
+            else if (Lx * Lz > 0.0) vf = ns * PFGB_PI * R * R / (Lx * Lz);
+            c->V0_target = vf;
+        } else {
+            c->V0_target = mean_h;
+        }
+    }
+    const double total_interface = E[1] + E[2];
+    const double F_surf = total_interface / Nf;
+    const double F_el = P.elastic_enabled ? E[3] / Nf : 0.0;
+    const double total_el_core = P.elastic_enabled ? E[4] : 0.0;
+    const double F_chem = E[5] / Nf;
+    const double F_total = F_chem + F_surf + F_el;
+    const double F_chem_cnt = mean_h > 0.0 ? mean_h * (P.mu0_compound - muBf) : NAN;
+    const double F_total_cnt = F_surf + F_el + F_chem_cnt;
+    const double F_prev = c->prev_F_total;
+    c->prev_F_total = F_total;
+
+    // ---- phi step with the under-relaxed multiplier: pa = phi^n -> pb ----
+    double eta_r = std::min(1.0, std::max(0.0, P.eta_lambda_vol));
+    double lraw = 0.0;
+    TRY((min_gradient<T, TE>(c, d, pa, &lraw)));
+    c->lambda_vol = (1.0 - eta_r) * c->lambda_vol + eta_r * lraw;
+    TRY((min_step<T, TE>(c, d, pa, pb, c->lambda_vol)));
+
+    // ---- projected KKT residual and rms_dphi at phi^{n+1} ----
+    double lk = 0.0;
+    TRY((min_gradient<T, TE>(c, d, pb, &lk)));
+    TRY((min_reduce<AccSum2>(c, "min_resid", 4.0 * Nf * sizeof(T), 44, 2, k_min_resid<T, TE>, d, (const T *)pb,
+                             (const T *)pa, P.kappa_phi, lk)));
+    const double rms_res = std::sqrt(c->hscal[44] / Nf);
+    const double rms_dphi = std::sqrt(c->hscal[45] / Nf) / P.dt;
+
+    // ---- Y update (full model) with phi^n = pa, phi^{n+1} = pb ----
+    {
+        DevState<T, TE> dy = d;
+        dy.phi_old = pa;
+        dy.phi_new = pb;
+        TRY((y_update<T, TE>(c, dy, &st)));
+    }
+    d = dev_state<T, TE>(c);   // same buffers, updated scalars
+    T *cur = pb, *oth = pa;
+
+    // ---- post-projection substeps (elastic frozen, eta = 1) ----
+    for (int k = 0; k < P.minimize_post_projection_iters; ++k) {
+        double l = 0.0;
+        TRY((min_gradient<T, TE>(c, d, cur, &l)));
+        c->lambda_vol = l;
+        TRY((min_step<T, TE>(c, d, cur, oth, l)));
+        std::swap(cur, oth);
+    }
+    TRY((min_reduce<AccSum2>(c, "min_hsums", Nf * sizeof(T), 46, 2, k_min_hsums<T>, (const T *)cur, N)));
+    mean_h = c->hscal[46] / Nf;
+
+    // ---- first-order projection of <h> onto V0 ----
+    if (c->V0_target > 1e-30 && std::isfinite(mean_h)) {
+        const double vol_err = c->V0_target - mean_h;
+        if (std::fabs(vol_err) > 1e-14) {
+            const double mhp2 = c->hscal[47] / Nf;
+            const double lc = mhp2 > 1e-30 ? vol_err / mhp2 : 0.0;
+            {
+                ProfScope ps(c, {"min_project", 2.0 * Nf * sizeof(T)});
+                k_min_project<T><<<kMinBlocks, 256, 0, c->stream>>>(cur, N, lc);
+                PFGB_CUDA_TRY(cudaGetLastError());
+            }
+            TRY((min_reduce<AccSum2>(c, "min_hsums", Nf * sizeof(T), 46, 2, k_min_hsums<T>, (const T *)cur, N)));
+            mean_h = c->hscal[46] / Nf;
+        }
+    }
+    c->cur = cur == (T *)c->phi[0] ? 0 : 1;
+
+    // ---- stopping rule (:32405-32600) and the monitor's xB clamp ----
+    TRY((min_reduce<AccSumMax>(c, "min_dy", 2.0 * Nf * sizeof(T), 48, 2, k_min_dy<T, TE>, d, c->pc, c->Yc_prev)));
+    const double rms_dY = std::sqrt(c->hscal[48] / Nf) / P.dt;
+    const double xmax = c->hscal[49];
+    double edr = NAN;
+    if (std::isfinite(F_prev) && std::isfinite(F_total)) edr = std::fabs(F_total - F_prev) / std::fmax(std::fabs(F_prev), 1e-20);
+    const double ver = c->V0_target > 1e-30 ? std::fabs(mean_h - c->V0_target) / (c->V0_target + 1e-30) : 0.0;
+    const bool vol_ok = std::isfinite(ver) && ver < P.minimize_vol_err_rel_threshold;
+    const bool res_ok = std::isfinite(rms_res) && rms_res < P.minimize_rms_res_threshold;
+    const int condA = std::isfinite(rms_dphi) && std::isfinite(rms_dY) && rms_dphi < P.minimize_rms_dphi_threshold &&
+                      rms_dY < P.minimize_rms_dY_threshold && res_ok && vol_ok;
+    const int condB = std::isfinite(edr) && edr < P.minimize_energy_diff_rel_threshold && std::isfinite(rms_dphi) &&
+                      std::isfinite(rms_dY) && rms_dphi < 5.0 * P.minimize_rms_dphi_threshold &&
+                      rms_dY < 5.0 * P.minimize_rms_dY_threshold && res_ok && vol_ok;
+    const double pt = (double)it * P.dt;
+    const bool pt_ok = std::isfinite(pt) && pt + 1e-14 >= P.minimize_min_pseudo_time;
+    c->conv_count = ((condA || condB) && pt_ok) ? c->conv_count + 1 : 0;
+    if (c->conv_count >= P.minimize_convergence_steps && !c->converged_iter) c->converged_iter = it;
+    // the reference clamps its stored xB when the monitor sees max xB above
+    // minimize_xB_max_safe; the clamped xB is what the next iteration's
+    // elastic solve and energies read (here: the cap on the elastic side)
+    const int clamped = xmax > P.minimize_xB_max_safe + 1e-12;
+    c->xb_clamp = clamped;
+    c->step++;
+    if (ms) {
+        ms->iteration = it;
+        ms->converged = c->converged_iter != 0;
+        ms->converged_iteration = c->converged_iter;
+        ms->convergence_count = c->conv_count;
+        ms->condA = condA; ms->condB = condB;
+        ms->xB_clamped = clamped;
+        ms->elastic_iterations = st.elastic_iterations;
+        ms->elastic_relative_residual = st.elastic_relative_residual;
+        ms->mean_h = mean_h; ms->V0_target = c->V0_target; ms->lambda_vol = c->lambda_vol;
+        ms->F_surf = F_surf; ms->F_el = F_el; ms->F_chem_excess = F_chem; ms->F_total_excess = F_total;
+        ms->F_chem_CNT = F_chem_cnt; ms->F_total_CNT = F_total_cnt;
+        ms->total_interface_sum = total_interface; ms->total_el_core_sum = total_el_core;
+        ms->rms_res = rms_res; ms->rms_dphi = rms_dphi; ms->rms_dY = rms_dY;
+        ms->energy_diff_rel = edr; ms->vol_err_rel = ver;
+    }
     return PFGB_OK;
 }
 
@@ -1470,6 +1918,8 @@ static void build_physc(pfgb_ctx *c) {
     k.prev_level = P.enable_Y_rhs_previous_time_level;
     k.disable_gamma = P.disable_Y_rhs_gamma_term;
     k.xb_raw = P.zero_mode_enabled;
+    k.xbcap = 2.0;
+    k.dx = P.dx; k.dy = P.dy; k.dz = P.dz;
     pfgb_thermo_const(P.temperature_K, P.mu_reference_scale, P.thermo_convex_extrapolation_enabled, &k.tc);
     k.shift = k.coupling ? P.elastic_shift_dimless : 0.0;
     k.Cdmu = P.mu0_compound - P.v_A * k.tc.GA_s - P.v_B * k.tc.GB_s - k.shift;
@@ -1554,9 +2004,19 @@ static pfgb_status validate(const pfgb_params *p) {
         pfgb_set_error_msg("elastic_precision: only FP32 (the reference's elastic precision) is built");
         return PFGB_ERR_UNSUPPORTED;
     }
-    if (p->mode != PFGB_MODE_DYNAMICS) {
-        pfgb_set_error_msg("pfgb_step drives mode=dynamics; minimize runs through pfgb_minimize");
-        return PFGB_ERR_UNSUPPORTED;
+    if (p->mode != PFGB_MODE_DYNAMICS && p->mode != PFGB_MODE_MINIMIZE) {
+        pfgb_set_error_msg("mode must be dynamics or minimize");
+        return PFGB_ERR_INVALID;
+    }
+    if (p->mode == PFGB_MODE_MINIMIZE) {
+        if (!p->minimize_full_model || p->model_mode != PFGB_MODEL_TWO_PHASE || p->zero_mode_enabled) {
+            pfgb_set_error_msg("minimize is built for minimize_full_model=1, two_phase, zero mode off");
+            return PFGB_ERR_UNSUPPORTED;
+        }
+        if (!(p->minimize_dt > 0)) {
+            pfgb_set_error_msg("minimize_dt must be > 0");
+            return PFGB_ERR_INVALID;
+        }
     }
     if (p->model_mode != PFGB_MODEL_TWO_PHASE && p->model_mode != PFGB_MODEL_GP_ZONE) {
         pfgb_set_error_msg("model_mode must be two_phase or gp_zone");
@@ -1581,6 +2041,8 @@ static void ctx_free(pfgb_ctx *c) {
     for (int i = 0; i < 6; ++i) { f(c->eps[i]); f(c->E[i]); }
     for (int i = 0; i < 3; ++i) f(c->U[i]);
     f(c->partials); f(c->dscal); f(c->stage);
+    for (int i = 0; i < 6; ++i) f(c->sig[i]);
+    f(c->mge); f(c->mlap);
     for (auto e : c->pool) cudaEventDestroy(e);
     if (c->hscal) cudaFreeHost(c->hscal);
 }
@@ -1623,6 +2085,10 @@ static pfgb_status load_device(pfgb_ctx *c, const double *phi, const double *xB,
     for (int i = 0; i < 6; ++i) PFGB_CUDA_TRY(cudaMemsetAsync(c->eps[i], 0, sizeof(float) * c->g.N, c->stream));
     c->warm_valid = 0;
     c->step = 0;
+    c->min_iter = c->conv_count = c->converged_iter = c->xb_clamp = 0;
+    c->lambda_vol = 0.0;
+    c->prev_F_total = NAN;
+    c->V0_target = c->p.minimize_V0;
     c->loaded = 1;
     return PFGB_OK;
 }
@@ -1668,6 +2134,8 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
     c->p = *pin;
     c->device = device;
     pfgb_params_finalize(&c->p);
+    if (pin->mode == PFGB_MODE_MINIMIZE) c->p.dt = pin->minimize_dt;   // main_cuda.cu:24432-24435
+    c->V0_target = pin->minimize_V0;
     c->g.Nx = pin->Nx; c->g.Ny = pin->Ny; c->g.Nz = pin->Nz; c->g.NzC = pin->Nz / 2 + 1;
     c->g.N = (long long)pin->Nx * pin->Ny * pin->Nz;
     c->g.Nk = (long long)pin->Nx * pin->Ny * c->g.NzC;
@@ -1697,6 +2165,11 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
     if (pin->elastic_enabled) {
         for (int i = 0; i < 6; ++i) { A_(&c->E[i], sizeof(float2) * Nk); }
         for (int i = 0; i < 3; ++i) { A_(&c->U[i], sizeof(float2) * Nk); }
+    }
+    if (pin->mode == PFGB_MODE_MINIMIZE) {
+        for (int i = 0; i < 6; ++i) { A_(&c->sig[i], sizeof(float) * N); }
+        A_(&c->mge, rs * N);
+        A_(&c->mlap, rs * N);
     }
     c->npartials = std::max<size_t>((size_t)pin->Nx * pin->Ny, 4096) * 8;
     A_(&c->partials, sizeof(double) * c->npartials);
@@ -1741,6 +2214,24 @@ pfgb_status pfgb_set_stream(pfgb_ctx *c, void *s) {
 
 size_t pfgb_device_bytes(const pfgb_ctx *c) { return c ? c->bytes : 0; }
 
+pfgb_status pfgb_minimize(pfgb_ctx *c, int max_iter, int stop_on_convergence, pfgb_min_stats *st) {
+    if (!c || max_iter < 0) return PFGB_ERR_INVALID;
+    if (!c->loaded) { pfgb_set_error_msg("pfgb_minimize before pfgb_load_fields"); return PFGB_ERR_INVALID; }
+    if (c->p.mode != PFGB_MODE_MINIMIZE) {
+        pfgb_set_error_msg("pfgb_minimize needs a context created with mode=minimize");
+        return PFGB_ERR_INVALID;
+    }
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    if (st) memset(st, 0, sizeof(*st));
+    for (int i = 0; i < max_iter; ++i) {
+        pfgb_status s = c->p.precision == PFGB_PREC_FP64 ? minimize_once<double, float>(c, st)
+                                                         : minimize_once<float, float>(c, st);
+        if (s != PFGB_OK) return s;
+        if (stop_on_convergence && c->converged_iter) break;
+    }
+    return PFGB_OK;
+}
+
 pfgb_status pfgb_sync(pfgb_ctx *c) {
     if (!c) return PFGB_ERR_INVALID;
     PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -1768,6 +2259,10 @@ pfgb_status pfgb_set_fields(pfgb_ctx *c, const double *phi, const double *xB, co
 pfgb_status pfgb_step(pfgb_ctx *c, int nsteps, pfgb_step_stats *st) {
     if (!c || nsteps < 0) return PFGB_ERR_INVALID;
     if (!c->loaded) { pfgb_set_error_msg("pfgb_step before pfgb_load_fields"); return PFGB_ERR_INVALID; }
+    if (c->p.mode != PFGB_MODE_DYNAMICS) {
+        pfgb_set_error_msg("pfgb_step drives mode=dynamics; this context is mode=minimize (pfgb_minimize)");
+        return PFGB_ERR_INVALID;
+    }
     PFGB_CUDA_TRY(cudaSetDevice(c->device));
     if (st) memset(st, 0, sizeof(*st));
     for (int i = 0; i < nsteps; ++i) {

@@ -45,6 +45,11 @@ struct Cli {
     double h_scale = NAN;
     int precision = PFGB_PREC_FP64;
     int device = 0;
+    // minimize
+    bool min_full = false;
+    int min_max_iter = -1, min_conv_steps = -1, min_post_iters = -1;
+    double min_dt = NAN, V0 = NAN, eta_lambda = NAN, thr_dphi = NAN, thr_dY = NAN, thr_res = NAN, thr_vol = NAN,
+           thr_E = NAN, min_pt = NAN, xB_max_safe = NAN, radius = NAN;
 };
 
 void usage() {
@@ -52,7 +57,14 @@ void usage() {
            "  ./main_cuda Nx Ny Nz dt nsteps out_every csv_out_every elastic_enabled(0/1)\n"
            "    dt is a fallback only: the parameter file's dt wins.\n"
            "\nFlags:\n"
-           "  --mode=dynamics                 (minimize: not available in this build)\n"
+           "  --mode=dynamics|minimize\n"
+           "  --minimize-full-model           minimize with chemistry + diffusion + volume constraint\n"
+           "  --minimize-max-iter <n>  --minimize-dt <dt>  --V0 <v>  --eta-lambda-vol <v>\n"
+           "  --minimize-rms-dphi-threshold <v>  --minimize-rms-dY-threshold <v>\n"
+           "  --minimize-rms-res-threshold <v>   --minimize-vol-err-rel-threshold <v>\n"
+           "  --minimize-energy-diff-rel-threshold <v>  --minimize-convergence-steps <n>\n"
+           "  --minimize-post-projection-iters <n>  --minimize-min-pseudo-time <t>\n"
+           "  --minimize-xB-max-safe <v>  --radius <r>  (seed radius: V0 target when V0 <= 0)\n"
            "  --pf-param-file <path>          required: complete physical PF inputs (key=value)\n"
            "  --elastic 0|1                   override elastic\n"
            "  --temperature-C <val>\n"
@@ -142,6 +154,22 @@ Cli parse(int argc, char **argv) {
             else bad(a, v);
         }
         else if ((v = flag_value(argc, argv, &i, "--device"))) { if (!to_int(v, &c.device)) bad(a, v); }
+        else if (!strcmp(a, "--minimize-full-model")) c.min_full = true;
+        else if ((v = flag_value(argc, argv, &i, "--minimize-max-iter"))) { if (!to_int(v, &c.min_max_iter)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--minimize-dt"))) { if (!to_double(v, &c.min_dt)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--V0"))) { if (!to_double(v, &c.V0)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--eta-lambda-vol"))) { if (!to_double(v, &c.eta_lambda)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--minimize-rms-dphi-threshold"))) { if (!to_double(v, &c.thr_dphi)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--minimize-rms-dY-threshold")) ||
+                 (v = flag_value(argc, argv, &i, "--minimize-rms-dy-threshold"))) { if (!to_double(v, &c.thr_dY)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--minimize-rms-res-threshold"))) { if (!to_double(v, &c.thr_res)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--minimize-vol-err-rel-threshold"))) { if (!to_double(v, &c.thr_vol)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--minimize-energy-diff-rel-threshold"))) { if (!to_double(v, &c.thr_E)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--minimize-convergence-steps"))) { if (!to_int(v, &c.min_conv_steps)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--minimize-post-projection-iters"))) { if (!to_int(v, &c.min_post_iters) || c.min_post_iters < 0) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--minimize-min-pseudo-time"))) { if (!to_double(v, &c.min_pt)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--minimize-xB-max-safe"))) { if (!to_double(v, &c.xB_max_safe)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--radius"))) { if (!to_double(v, &c.radius) || c.radius < 0) bad(a, v); }
         else fprintf(stderr, "[warn] unknown flag ignored: %s\n", a);
     }
     return c;
@@ -276,10 +304,11 @@ int main(int argc, char **argv) {
         fprintf(stderr, "[fatal] --pf-param-file <path> is required (complete physical PF inputs).\n");
         return 2;
     }
-    if (c.mode != "dynamics") {
-        fprintf(stderr, "[fatal] --mode=%s is not available in this build (dynamics only)\n", c.mode.c_str());
+    if (c.mode != "dynamics" && c.mode != "minimize") {
+        fprintf(stderr, "[fatal] --mode=%s is not available in this build (dynamics, minimize)\n", c.mode.c_str());
         return 2;
     }
+    const bool minimize = c.mode == "minimize";
     pfgb_params P;
     pfgb_params_default(&P);
     if (c.pos_Nx > 0) P.Nx = c.pos_Nx;
@@ -311,6 +340,27 @@ int main(int argc, char **argv) {
     if (c.no_gamma) P.disable_Y_rhs_gamma_term = 1;
     if (std::isfinite(c.h_scale)) P.Y_rhs_term_h_scale = c.h_scale;
     P.precision = c.precision;
+    if (minimize) {
+        P.mode = PFGB_MODE_MINIMIZE;
+        P.minimize_dt = P.dt;   // the parameter file's dt unless --minimize-dt is given
+        if (c.min_full) P.minimize_full_model = 1;
+        if (c.min_max_iter > 0) P.minimize_max_iter = c.min_max_iter;
+        if (std::isfinite(c.min_dt)) P.minimize_dt = c.min_dt;
+        if (std::isfinite(c.V0)) P.minimize_V0 = c.V0;
+        if (std::isfinite(c.eta_lambda)) P.eta_lambda_vol = c.eta_lambda;
+        if (std::isfinite(c.thr_dphi)) P.minimize_rms_dphi_threshold = c.thr_dphi;
+        if (std::isfinite(c.thr_dY)) P.minimize_rms_dY_threshold = c.thr_dY;
+        if (std::isfinite(c.thr_res)) P.minimize_rms_res_threshold = c.thr_res;
+        if (std::isfinite(c.thr_vol)) P.minimize_vol_err_rel_threshold = c.thr_vol;
+        if (std::isfinite(c.thr_E)) P.minimize_energy_diff_rel_threshold = c.thr_E;
+        if (c.min_conv_steps > 0) P.minimize_convergence_steps = c.min_conv_steps;
+        if (c.min_post_iters >= 0) P.minimize_post_projection_iters = c.min_post_iters;
+        if (std::isfinite(c.min_pt)) P.minimize_min_pseudo_time = c.min_pt;
+        if (std::isfinite(c.xB_max_safe)) P.minimize_xB_max_safe = c.xB_max_safe;
+        if (std::isfinite(c.radius)) P.ic_phi_seed_radius = c.radius;
+        c.nsteps = P.minimize_max_iter;   // main_cuda.cu:24432-24435
+        P.dt = P.minimize_dt;
+    }
     if (c.nsteps < 0 || c.out_every <= 0 || c.csv_out_every <= 0) {
         fprintf(stderr, "[fatal] nsteps >= 0, out_every > 0 and csv_out_every > 0 are required\n");
         return 2;
@@ -354,9 +404,17 @@ int main(int argc, char **argv) {
     const double xB_out = param_file_value(ptxt, "ic_23d_xB_out", param_file_value(ptxt, "xB_alpha_initial", 0.03));
     const char *root_env = getenv("CUDA_STO_RESULTS_ROOT");
     const std::string root = (root_env && root_env[0]) ? root_env : "Results";
+    const double dx_phys = P.ic_phi_iface_w > 1e-30 ? P.lambda_sm_m / (2.0 * P.ic_phi_iface_w) : P.dx * 1e-9;
+    const double unit_to_m = std::fabs(P.dx) > 1e-30 ? dx_phys / P.dx : 1e-9;
+    const double unit_to_nm = unit_to_m * 1e9;
     char name[512];
-    snprintf(name, sizeof(name), "%s_T%.0f_cuda_%dx%dx%d_dt%.3g_steps%d_xB%.3f", P.elastic_enabled ? "chel" : "ch",
-             P.temperature_C, P.Nx, P.Ny, P.Nz, P.dt, c.nsteps, xB_out);
+    if (minimize)   // named with the physical seed radius (main_cuda.cu:25386-25396)
+        snprintf(name, sizeof(name), "%s_T%.0f_cuda_%dx%dx%d_dt%.3g_steps%d_r%.3fnm_xB%.3f",
+                 P.elastic_enabled ? "chel" : "ch", P.temperature_C, P.Nx, P.Ny, P.Nz, P.dt, c.nsteps,
+                 P.ic_phi_seed_radius * unit_to_nm, xB_out);
+    else
+        snprintf(name, sizeof(name), "%s_T%.0f_cuda_%dx%dx%d_dt%.3g_steps%d_xB%.3f", P.elastic_enabled ? "chel" : "ch",
+                 P.temperature_C, P.Nx, P.Ny, P.Nz, P.dt, c.nsteps, xB_out);
     mkdir(root.c_str(), 0755);
     const std::string out_dir = root + "/" + name;
     mkdir(out_dir.c_str(), 0755);
@@ -366,8 +424,6 @@ int main(int argc, char **argv) {
     mkdir(case_dir.c_str(), 0755);
     copy_file(c.param_file, case_dir + "/pf_input.params");
     const bool gp = P.model_mode == PFGB_MODEL_GP_ZONE;
-    const double dx_phys = P.ic_phi_iface_w > 1e-30 ? P.lambda_sm_m / (2.0 * P.ic_phi_iface_w) : P.dx * 1e-9;
-    const double unit_to_nm = (std::fabs(P.dx) > 1e-30 ? dx_phys / P.dx : 1e-9) * 1e9;
     printf("output_dir=%s\ncase_output_dir=%s\n", out_dir.c_str(), case_dir.c_str());
 
     // ---- solver -----------------------------------------------------------
@@ -415,12 +471,25 @@ int main(int argc, char **argv) {
         return 2;
     }
     fprintf(csv, "step,t_code,t_real_s,vf_precip,R_avg\n");
+    FILE *efp = nullptr;
+    if (minimize) {   // energy_minimize_T%.0f_r%.2f_xB%.3f_<tag>.csv (main_cuda.cu:27436-27467)
+        char en[512];
+        snprintf(en, sizeof(en), "/energy_minimize_T%.0f_r%.2f_xB%.3f_%s.csv", P.temperature_C, P.ic_phi_seed_radius,
+                 xB_out, tag.c_str());
+        efp = fopen((case_dir + en).c_str(), "w");
+        if (!efp) { fprintf(stderr, "[fatal] cannot open %s%s\n", case_dir.c_str(), en); pfgb_destroy(ctx); return 2; }
+        fprintf(efp, "iter,dt,mean_h,V0,lambda,F_surf_hat,F_el_hat,F_chem_excess_hat,F_total_excess_hat,"
+                     "F_chem_CNT_hat,F_total_CNT_hat,total_interface_sum,total_el_core_sum,"
+                     "rms_res,rms_dphi,rms_dY,rel_dF,vol_err_rel,mass_target_code,mass_current_code,mass_err_rel,"
+                     "mass_lambda,post_proj_iters_used\n");
+    }
 
     const char *dim = P.Ny == 2 ? "[2D]" : "[3D]";
-    auto csv_row = [&](int step) -> pfgb_status {
+    auto csv_row = [&](int step, double vf_override) -> pfgb_status {
         pfgb_diag d;
         pfgb_status s = pfgb_diagnostics(ctx, &d);
         if (s != PFGB_OK) return s;
+        if (std::isfinite(vf_override)) d.vf_precip = vf_override;   // minimize: mean_h of the iteration
         double R_avg = 0.0;
         if (d.n_if > 0.0) {
             const double ratio = d.n_in / (d.n_if / (P.ic_phi_iface_w * 2.0));
@@ -437,16 +506,51 @@ int main(int argc, char **argv) {
     };
 
     if ((st = read_state()) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_read_fields"); }
-    vtk_set("_init");
-    write_vtk(case_dir + "/xB_0.vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
-    if ((st = csv_row(0)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_diagnostics"); }
+    if (minimize) {   // minimize writes init / final fields only, with the case tag
+        write_vtk(case_dir + "/phi_init_" + tag + ".vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
+        write_vtk(case_dir + "/xB_init_" + tag + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
+    } else {
+        vtk_set("_init");
+        write_vtk(case_dir + "/xB_0.vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
+    }
+    if ((st = csv_row(0, NAN)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_diagnostics"); }
 
     std::vector<double> wall;
     wall.reserve(c.nsteps);
     const auto t0 = std::chrono::steady_clock::now();
     int rc = 0;
     unsigned long long accepted_zm = 0;
-    for (int step = 1; step <= c.nsteps; ++step) {
+    for (int step = 1; step <= c.nsteps && minimize; ++step) {
+        pfgb_min_stats m;
+        const auto a = std::chrono::steady_clock::now();
+        st = pfgb_minimize(ctx, 1, 1, &m);
+        if (st == PFGB_OK) st = pfgb_sync(ctx);
+        const double w = std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+        if (st != PFGB_OK) { rc = fail(st, "pfgb_minimize"); break; }
+        wall.push_back(w);
+        fprintf(efp, "%d,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,"
+                     "%.17e,%.17e,%.17e,%.17e,%d\n",
+                step, P.dt, m.mean_h, m.V0_target, m.lambda_vol, m.F_surf, m.F_el, m.F_chem_excess,
+                m.F_total_excess, m.F_chem_CNT, m.F_total_CNT, m.total_interface_sum, m.total_el_core_sum,
+                m.rms_res, m.rms_dphi, m.rms_dY, m.energy_diff_rel, m.vol_err_rel, NAN, NAN, NAN, NAN,
+                P.minimize_post_projection_iters);
+        fflush(efp);
+        if (etrace) {
+            fprintf(etrace, "%d,%d,%d,%.17e,%d,%d,%.17e,%.9f,%llu\n", step, step > 1 ? 1 : 0, m.elastic_iterations,
+                    m.elastic_relative_residual, m.elastic_relative_residual <= P.elastic_residual_tolerance ? 1 : 0,
+                    P.elastic_iter_max, P.elastic_residual_tolerance, w, (unsigned long long)(step - 1));
+            fflush(etrace);
+        }
+        if (step % c.csv_out_every == 0 && (st = csv_row(step, m.mean_h)) != PFGB_OK) {
+            rc = fail(st, "pfgb_diagnostics");
+            break;
+        }
+        if (m.converged) {
+            printf("[minimize] converged at iter %d (%s)\n", m.converged_iteration, m.condA ? "condA" : "condB");
+            break;
+        }
+    }
+    for (int step = 1; step <= c.nsteps && !minimize; ++step) {
         pfgb_step_stats s;
         const auto a = std::chrono::steady_clock::now();
         st = pfgb_step(ctx, 1, &s);
@@ -467,7 +571,7 @@ int main(int argc, char **argv) {
                     s.zero_mode_newton_steps, s.zero_mode_bisection_steps, NAN, NAN, NAN, NAN, accepted_zm);
             fflush(ztrace);
         }
-        if (step % c.csv_out_every == 0 && (st = csv_row(step)) != PFGB_OK) { rc = fail(st, "pfgb_diagnostics"); break; }
+        if (step % c.csv_out_every == 0 && (st = csv_row(step, NAN)) != PFGB_OK) { rc = fail(st, "pfgb_diagnostics"); break; }
         if (step % c.out_every == 0) {
             if ((st = read_state()) != PFGB_OK) { rc = fail(st, "pfgb_read_fields"); break; }
             vtk_set(("_" + std::to_string(step)).c_str());
@@ -476,9 +580,15 @@ int main(int argc, char **argv) {
     const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (rc == 0) {
         if ((st = read_state()) != PFGB_OK) rc = fail(st, "pfgb_read_fields");
-        else vtk_set("_final");
+        else if (minimize) {
+            write_vtk(case_dir + "/phi_final_" + tag + ".vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
+            write_vtk(case_dir + "/xB_final_" + tag + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
+        } else {
+            vtk_set("_final");
+        }
     }
     if (csv) fclose(csv);
+    if (efp) fclose(efp);
     if (etrace) fclose(etrace);
     if (ztrace) fclose(ztrace);
 

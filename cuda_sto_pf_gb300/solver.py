@@ -73,6 +73,13 @@ class Solver:
         self._chk(self.lib.pfgb_step(self.ctx, nsteps, ctypes.byref(st)), "pfgb_step")
         return st
 
+    def minimize(self, n: int = 1, stats: capi.MinStats | None = None,
+                 stop_on_convergence: bool = False) -> capi.MinStats:
+        st = stats if stats is not None else capi.MinStats()
+        self._chk(self.lib.pfgb_minimize(self.ctx, n, 1 if stop_on_convergence else 0, ctypes.byref(st)),
+                  "pfgb_minimize")
+        return st
+
     def step_nostats(self, nsteps: int = 1) -> None:
         self._chk(self.lib.pfgb_step(self.ctx, nsteps, None), "pfgb_step")
 

@@ -139,6 +139,16 @@ typedef struct pfgb_params {
     double t_real_unit;
     double ic_vf_init_phi, ic_vf_target_phi, ic_phi_iface_w;
     double gamma_Jm2, lambda_sm_m, Vm_alpha_0_phys_m3mol;
+    /* initial-condition keys read by minimize: far-field composition
+       (ic_23d_xB_out, alias xB_alpha_initial) for the chemical energy
+       baseline, and the legacy seed radius / count that set the volume
+       target when minimize_V0 <= 0 (compute_effective_vf_target,
+       main_cuda.cu:2459-2490) */
+    double ic_23d_xB_out;
+    double ic_phi_seed_radius;
+    double minimize_min_pseudo_time;
+    int32_t ic_phi_num_seeds;
+    int32_t pad2;
     /* derived by pfgb_params_finalize (pfparams_refresh_thermo) */
     double temperature_K;
     double mu0_compound;
@@ -161,6 +171,25 @@ typedef struct pfgb_step_stats {
     double zero_mode_target_mass;
     double mean_DY;
 } pfgb_step_stats;
+
+/* Minimize iteration statistics (energy_minimize.csv row and the stopping
+ * rule, main_cuda.cu:32400-32600).  Energies are the ones evaluated at the
+ * start of the last iteration, after its elastic solve, as the reference
+ * writes them. */
+typedef struct pfgb_min_stats {
+    int32_t iteration;            /* minimize iterations taken by the context   */
+    int32_t converged;            /* convergence_count reached minimize_convergence_steps */
+    int32_t converged_iteration;  /* iteration at which it did (0 if not)       */
+    int32_t convergence_count;
+    int32_t condA, condB;         /* of the last iteration                      */
+    int32_t xB_clamped;           /* the minimize_xB_max_safe clamp fired        */
+    int32_t elastic_iterations;   /* of the last iteration                      */
+    double mean_h, V0_target, lambda_vol;
+    double F_surf, F_el, F_chem_excess, F_total_excess, F_chem_CNT, F_total_CNT;
+    double total_interface_sum, total_el_core_sum;
+    double rms_res, rms_dphi, rms_dY, energy_diff_rel, vol_err_rel;
+    double elastic_relative_residual;
+} pfgb_min_stats;
 
 /* Scalar diagnostics of the current state (CSV row, mass ledger). */
 typedef struct pfgb_diag {
@@ -232,6 +261,12 @@ pfgb_status pfgb_load_fields_device(pfgb_ctx *ctx, const double *d_phi,
 
 /* Advance nsteps dynamics steps.  stats may be NULL. */
 pfgb_status pfgb_step(pfgb_ctx *ctx, int nsteps, pfgb_step_stats *stats);
+/* Minimize mode (mode = PFGB_MODE_MINIMIZE, minimize_full_model = 1,
+ * two_phase, zero mode off): up to max_iter gradient-flow iterations with
+ * the Lagrange volume constraint, post-projection and V0 projection
+ * (main_cuda.cu:29264-29750, 32100-32600), stopping early when the
+ * reference's convergence rule is met and stop_on_convergence != 0. */
+pfgb_status pfgb_minimize(pfgb_ctx *ctx, int max_iter, int stop_on_convergence, pfgb_min_stats *stats);
 
 /* Read the state back to HOST buffers (float64); any pointer may be NULL. */
 pfgb_status pfgb_read_fields(pfgb_ctx *ctx, double *phi, double *xB, double *Y,

@@ -28,6 +28,7 @@ def lib():
         _LIB.pfo_destroy.argtypes = [vp]
         _LIB.pfo_load_fields.argtypes = [vp, vp, vp, vp, vp]
         _LIB.pfo_step.argtypes = [vp, i, vp]
+        _LIB.pfo_minimize.argtypes = [vp, i, i, vp]
         _LIB.pfo_read_fields.argtypes = [vp, vp, vp, vp, vp, vp]
         _LIB.pfo_read_elastic.argtypes = [vp, vp, vp]
         _LIB.pfo_read_displacement_k.argtypes = [vp, vp]
@@ -79,6 +80,10 @@ class Oracle:
     def step(self, n=1, stats=None):
         rc = self.L.pfo_step(self.s, n, None if stats is None else ctypes.byref(stats))
         return rc
+
+    def minimize(self, n=1, stats=None, stop_on_convergence=False):
+        return self.L.pfo_minimize(self.s, n, 1 if stop_on_convergence else 0,
+                                   None if stats is None else ctypes.byref(stats))
 
     def fields(self):
         out = {k: np.empty(self.shape) for k in ("phi", "xB", "Y", "eta", "dYdt")}

@@ -251,6 +251,10 @@ struct pfo_state {
     double *kx, *ky, *kz;
     unsigned char *mx, *my, *mz;  /* 1 = dealiased (zeroed) */
     double target_mass;
+    /* minimize */
+    double *mlap, *mg;
+    double lambda_vol, V0_target, prev_F_total;
+    int min_iter, conv_count, converged_iter;
 };
 
 static inline double rf(const pfo_state *s, double v) { return s->fp32e ? (double)(float)v : v; }
@@ -297,6 +301,11 @@ pfo_state *pfo_create(const pfgb_params *pin) {
         s->u_k[c] = (cpx *)xalloc(kb);
         s->u_next[c] = (cpx *)xalloc(kb);
     }
+    s->mlap = (double *)xalloc(rb);
+    s->mg = (double *)xalloc(rb);
+    s->V0_target = pin->minimize_V0;
+    s->prev_F_total = NAN;
+    if (pin->mode == PFGB_MODE_MINIMIZE) s->p.dt = pin->minimize_dt;   /* main_cuda.cu:24432-24435 */
     s->kx = (double *)xalloc(sizeof(double) * s->Nx);
     s->ky = (double *)xalloc(sizeof(double) * s->Ny);
     s->kz = (double *)xalloc(sizeof(double) * s->NzC);
@@ -322,6 +331,7 @@ void pfo_destroy(pfo_state *s) {
     for (int c = 0; c < 6; ++c) { free(s->eps_r[c]); free(s->sig_r[c]); free(s->eps_k[c]); }
     for (int c = 0; c < 3; ++c) { free(s->u_k[c]); free(s->u_next[c]); }
     free(s->kx); free(s->ky); free(s->kz); free(s->mx); free(s->my); free(s->mz);
+    free(s->mlap); free(s->mg);
     free(s);
 }
 
@@ -833,65 +843,12 @@ static int zero_mode(pfo_state *s, const double *Ystar, double Y_upper_cap, pfgb
 /* ------------------------------------------------------------------ */
 /* one dynamics step — main_cuda.cu:28427-31623                        */
 /* ------------------------------------------------------------------ */
-static int step_once(pfo_state *s, pfgb_step_stats *st) {
+/* Y (composition) update and dY/dt history, main_cuda.cu:30280-30800 and
+ * 31618-31623; fields at entry: phi = phi^{n+1}, phi_n = phi^n, Y = Y^n. */
+static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
     pfgb_params *P = &s->p;
     const double T = P->temperature_K, sc = P->mu_reference_scale;
     const int cv = P->thermo_convex_extrapolation_enabled;
-    const double dt = P->dt;
-    memcpy(s->phi_n, s->phi, sizeof(double) * s->N);
-    memcpy(s->eta_prev, s->eta, sizeof(double) * s->N);
-    memcpy(s->Y_n, s->Y, sizeof(double) * s->N);
-
-    const int gp_el = s->gp && P->gp_elastic_enabled;
-    const int coupling = P->elastic_enabled && (!gp_el || P->gp_elastic_active_phi);
-    if (P->elastic_enabled) {
-        int rc = elastic_solve(s, st);
-        if (rc != PFGB_OK) return rc;
-    }
-
-    /* phi update, :29752-29860 */
-    fwd(s, s->phi, s->phi_k); dealias(s, s->phi_k);
-    phi_rhs(s, coupling);
-    fwd(s, s->rhs, s->rhs_k); dealias(s, s->rhs_k);
-    {
-        const double Ldt = P->L_phi * dt;
-        KLOOP_BEGIN(s)
-            double den = 1.0 + Ldt * P->kappa_phi * k2_at(s, ii_, jj_, kk_);
-            cpx a = s->phi_k[idx], r = s->rhs_k[idx];
-            s->phi_k[idx].re = (a.re - Ldt * r.re) / den;
-            s->phi_k[idx].im = (a.im - Ldt * r.im) / den;
-        KLOOP_END
-    }
-    dealias(s, s->phi_k);
-    inv(s, s->phi_k, s->phi);
-    RLOOP_BEGIN(s)   /* phi_normalize_and_clamp_kernel, cuda_kernels.cu:1071-1084 */
-        double v = s->phi[idx] * s->invN;
-        if (v < -1e-6) v = -1e-6;
-        if (v > 1.0 + 1e-6) v = 1.0 + 1e-6;
-        s->phi[idx] = v;
-    RLOOP_END
-
-    /* eta update (gp_zone), :29948-30006 */
-    if (s->gp) {
-        fwd(s, s->eta, s->eta_k); dealias(s, s->eta_k);
-        eta_rhs(s);
-        fwd(s, s->rhs, s->rhs_k); dealias(s, s->rhs_k);
-        const double Ldt = P->gp_L_eta * dt;
-        KLOOP_BEGIN(s)
-            double den = 1.0 + Ldt * P->gp_kappa_eta * k2_at(s, ii_, jj_, kk_);
-            cpx a = s->eta_k[idx], r = s->rhs_k[idx];
-            s->eta_k[idx].re = (a.re - Ldt * r.re) / den;
-            s->eta_k[idx].im = (a.im - Ldt * r.im) / den;
-        KLOOP_END
-        dealias(s, s->eta_k);
-        inv(s, s->eta_k, s->eta);
-        RLOOP_BEGIN(s)
-            double v = s->eta[idx] * s->invN;
-            s->eta[idx] = v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
-        RLOOP_END
-    }
-
-    /* Y update, :30280-30800 */
     const int zm = P->zero_mode_enabled;
     const double *phiY = zm ? s->phi_n : (P->enable_Y_rhs_previous_time_level ? s->phi_n : s->phi);
     const double *etaY = s->eta;
@@ -1030,7 +987,337 @@ static int step_once(pfo_state *s, pfgb_step_stats *st) {
     }
     /* update_dY_dt_prev_kernel, :3545 */
     RLOOP_BEGIN(s) s->dYdt[idx] = (s->Y[idx] - s->Y_n[idx]) / dt; RLOOP_END
+    return PFGB_OK;
+}
+
+/* new phi from its dealiased transform phi_k and the explicit drive in
+ * s->rhs: phi_semi_implicit_update_kernel (cuda_kernels.cu:821-843),
+ * dealias, Z2D, phi_normalize_and_clamp_kernel (:1071-1084) */
+static void phi_si_update(pfo_state *s, double dt) {
+    pfgb_params *P = &s->p;
+    fwd(s, s->rhs, s->rhs_k); dealias(s, s->rhs_k);
+    const double Ldt = P->L_phi * dt;
+    KLOOP_BEGIN(s)
+        double den = 1.0 + Ldt * P->kappa_phi * k2_at(s, ii_, jj_, kk_);
+        cpx a = s->phi_k[idx], r = s->rhs_k[idx];
+        s->phi_k[idx].re = (a.re - Ldt * r.re) / den;
+        s->phi_k[idx].im = (a.im - Ldt * r.im) / den;
+    KLOOP_END
+    dealias(s, s->phi_k);
+    inv(s, s->phi_k, s->phi);
+    RLOOP_BEGIN(s)
+        double v = s->phi[idx] * s->invN;
+        if (v < -1e-6) v = -1e-6;
+        if (v > 1.0 + 1e-6) v = 1.0 + 1e-6;
+        s->phi[idx] = v;
+    RLOOP_END
+}
+
+static int step_once(pfo_state *s, pfgb_step_stats *st) {
+    pfgb_params *P = &s->p;
+    const double dt = P->dt;
+    memcpy(s->phi_n, s->phi, sizeof(double) * s->N);
+    memcpy(s->eta_prev, s->eta, sizeof(double) * s->N);
+    memcpy(s->Y_n, s->Y, sizeof(double) * s->N);
+
+    const int gp_el = s->gp && P->gp_elastic_enabled;
+    const int coupling = P->elastic_enabled && (!gp_el || P->gp_elastic_active_phi);
+    if (P->elastic_enabled) {
+        int rc = elastic_solve(s, st);
+        if (rc != PFGB_OK) return rc;
+    }
+
+    /* phi update, :29752-29860 */
+    fwd(s, s->phi, s->phi_k); dealias(s, s->phi_k);
+    phi_rhs(s, coupling);
+    phi_si_update(s, dt);
+
+    /* eta update (gp_zone), :29948-30006 */
+    if (s->gp) {
+        fwd(s, s->eta, s->eta_k); dealias(s, s->eta_k);
+        eta_rhs(s);
+        fwd(s, s->rhs, s->rhs_k); dealias(s, s->rhs_k);
+        const double Ldt = P->gp_L_eta * dt;
+        KLOOP_BEGIN(s)
+            double den = 1.0 + Ldt * P->gp_kappa_eta * k2_at(s, ii_, jj_, kk_);
+            cpx a = s->eta_k[idx], r = s->rhs_k[idx];
+            s->eta_k[idx].re = (a.re - Ldt * r.re) / den;
+            s->eta_k[idx].im = (a.im - Ldt * r.im) / den;
+        KLOOP_END
+        dealias(s, s->eta_k);
+        inv(s, s->eta_k, s->eta);
+        RLOOP_BEGIN(s)
+            double v = s->eta[idx] * s->invN;
+            s->eta[idx] = v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
+        RLOOP_END
+    }
+
+    int rc = y_update(s, st, dt);
+    if (rc != PFGB_OK) return rc;
     s->step++;
+    return PFGB_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* minimize (mode = minimize, full model, two_phase)                    */
+/* ------------------------------------------------------------------ */
+/* lap = IFFT(mask (-k^2) phi_k) / N from the dealiased phi_k
+ * (compute_laplacian_k_kernel, dealias, Z2D, normalize_only_kernel) */
+static void phi_laplacian(pfo_state *s, double *out) {
+    KLOOP_BEGIN(s)
+        double k2 = k2_at(s, ii_, jj_, kk_);
+        s->scr_k[idx].re = -k2 * s->phi_k[idx].re;
+        s->scr_k[idx].im = -k2 * s->phi_k[idx].im;
+    KLOOP_END
+    dealias(s, s->scr_k);
+    inv(s, s->scr_k, out);
+    RLOOP_BEGIN(s) out[idx] *= s->invN; RLOOP_END
+}
+
+/* lambda = -sum h'(phi) g / sum h'(phi)^2 (compute_hprime_times_rhs_kernel,
+ * compute_hprime_sq_values_kernel + gpu_reduce_sum) */
+static double volume_lambda(pfo_state *s, const double *g) {
+    RLOOP_BEGIN(s)
+        double hp = o_hp(s->phi[idx]);
+        s->mass_t[idx] = hp * g[idx];
+        s->der_t[idx] = hp * hp;
+    RLOOP_END
+    const double shg = dsum(s->mass_t, s->N), sh2 = dsum(s->der_t, s->N);
+    return fabs(sh2) > 1e-30 ? -shg / sh2 : 0.0;
+}
+
+static double mean_h_clamped(pfo_state *s) {   /* gpu_compute_vf_from_h */
+    RLOOP_BEGIN(s) s->mass_t[idx] = o_h(o_clamp01(s->phi[idx])); RLOOP_END
+    return dsum(s->mass_t, s->N) / (double)s->N;
+}
+
+/* V0 target when minimize_V0 <= 0: compute_effective_vf_target
+ * (main_cuda.cu:2459-2490) for spherical seeds of ic_phi_seed_radius */
+static double effective_vf_target(const pfgb_params *P) {
+    double vf = fmin(0.999, fmax(1e-6, P->ic_vf_target_phi));
+    if (!(P->ic_phi_seed_radius > 0.0)) return vf;
+    const int n = P->ic_phi_num_seeds > 0 ? P->ic_phi_num_seeds : 1;
+    const double R = P->ic_phi_seed_radius;
+    const double Lx = P->Nx * P->dx, Ly = P->Ny * P->dy, Lz = P->Nz * P->dz;
+    if (P->Ny > 2) {
+        const double box = Lx * Ly * Lz;
+        if (box > 0.0) vf = n * (4.0 * M_PI / 3.0) * R * R * R / box;
+    } else {
+        const double box = Lx * Lz;
+        if (box > 0.0) vf = n * M_PI * R * R / box;
+    }
+    return vf;
+}
+
+/* explicit phi drive and its full variational derivative at the current
+ * phi: s->rhs = g_explicit, s->mg = g_full = g_explicit - kappa Lap(phi);
+ * phi_k is left holding the dealiased transform of phi */
+static void phi_gradient(pfo_state *s, int coupling) {
+    fwd(s, s->phi, s->phi_k); dealias(s, s->phi_k);
+    phi_rhs(s, coupling);
+    phi_laplacian(s, s->mlap);
+    const double kap = s->p.kappa_phi;
+    RLOOP_BEGIN(s) s->mg[idx] = s->rhs[idx] - kap * s->mlap[idx]; RLOOP_END
+}
+
+/* phi step with the volume multiplier: RHS = (g_full + kappa Lap) + lambda h'
+ * (subtract_scaled_kernel with -kappa, add_volume_constraint_kernel) */
+static void phi_constrained_step(pfo_state *s, double lambda, double dt) {
+    const double kap = s->p.kappa_phi;
+    RLOOP_BEGIN(s)
+        double r = s->mg[idx] - (-kap) * s->mlap[idx];
+        s->rhs[idx] = r + lambda * o_hp(s->phi[idx]);
+    RLOOP_END
+    phi_si_update(s, dt);
+}
+
+/* one minimize iteration, main_cuda.cu:29264-29750 (energies, phi step,
+ * KKT residual), 30280-30800 (Y), 32104-32290 (post-projection, V0
+ * projection), 32405-32600 (stopping rule) */
+static int minimize_iter(pfo_state *s, pfgb_min_stats *ms) {
+    pfgb_params *P = &s->p;
+    const double dt = P->dt;   /* = minimize_dt */
+    const double T = P->temperature_K, sc = P->mu_reference_scale;
+    const int cv = P->thermo_convex_extrapolation_enabled;
+    memcpy(s->phi_n, s->phi, sizeof(double) * s->N);
+    memcpy(s->eta_prev, s->eta, sizeof(double) * s->N);
+    memcpy(s->Y_n, s->Y, sizeof(double) * s->N);
+    const int coupling = P->elastic_enabled;
+    pfgb_step_stats st;
+    memset(&st, 0, sizeof(st));
+    if (P->elastic_enabled) {
+        int rc = elastic_solve(s, &st);
+        if (rc != PFGB_OK) return rc;
+    }
+    const int it = ++s->min_iter;
+    elast_consts ec;
+    for (int c = 0; c < 21; ++c) { ec.S[c] = rf(s, P->S[c]); ec.Sp[c] = rf(s, P->S_p[c]); }
+    for (int c = 0; c < 6; ++c) { ec.e00[c] = rf(s, P->eps00[c]); ec.E0[c] = rf(s, P->E0[c]); }
+
+    /* ---- energies (diagnostics for the CSV and the plateau test) ---- */
+    double mean_h = mean_h_clamped(s);
+    if (it == 1 && !(s->V0_target > 0.0))
+        s->V0_target = P->ic_phi_seed_radius > 0.0 ? effective_vf_target(P) : mean_h;
+    /* compute_grad_energy_density_kernel (central differences), dw energy */
+    {
+        const int Nx = s->Nx, Ny = s->Ny, Nz = s->Nz;
+        const double kap = P->kappa_phi;
+        RLOOP_BEGIN(s)
+            const int k = (int)(idx % Nz);
+            const size_t rem = idx / Nz;
+            const int j = (int)(rem % Ny), i = (int)(rem / Ny);
+            const int ip = (i + 1) % Nx, im = (i - 1 + Nx) % Nx;
+            const int jp = (j + 1) % Ny, jm = (j - 1 + Ny) % Ny;
+            const int kp = (k + 1) % Nz, km = (k - 1 + Nz) % Nz;
+            const double *f = s->phi;
+            const double gx = (f[((size_t)ip * Ny + j) * Nz + k] - f[((size_t)im * Ny + j) * Nz + k]) / (2.0 * P->dx);
+            const double gy = (f[((size_t)i * Ny + jp) * Nz + k] - f[((size_t)i * Ny + jm) * Nz + k]) / (2.0 * P->dy);
+            const double gz = (f[((size_t)i * Ny + j) * Nz + kp] - f[((size_t)i * Ny + j) * Nz + km]) / (2.0 * P->dz);
+            s->mass_t[idx] = 0.5 * kap * (gx * gx + gy * gy + gz * gz);
+            s->der_t[idx] = P->W * o_g(f[idx]);
+        RLOOP_END
+    }
+    const double total_interface = dsum(s->mass_t, s->N) + dsum(s->der_t, s->N);
+    const double F_surf = total_interface / (double)s->N;
+    double F_el = 0.0, total_el_core = 0.0;
+    if (P->elastic_enabled) {   /* compute_gel_density_kernel, cuda_kernels.cu:1789-1850 */
+        RLOOP_BEGIN(s)
+            double e0[6];
+            eigen_point(s, &ec, s->phi[idx], s->eta[idx], o_clamp01(s->xB[idx]), 0, e0);
+            double sd = 0.0;
+            for (int c = 0; c < 6; ++c) {
+                const double el = s->eps_r[c][idx] - e0[c];
+                sd += (c < 3 ? 1.0 : 2.0) * s->sig_r[c][idx] * el;
+            }
+            s->mass_t[idx] = 0.5 * sd;
+            s->der_t[idx] = 0.5 * sd * o_h(o_clamp01(s->phi[idx]));
+        RLOOP_END
+        F_el = dsum(s->mass_t, s->N) / (double)s->N;
+        total_el_core = dsum(s->der_t, s->N);
+    }
+    /* compute_gbulk_excess_hat_kernel, reference state main_cuda.cu:27400-27431 */
+    const double xref = P->ic_23d_xB_out;   /* > 0 (the <xB>_init fallback is not used) */
+    const double g0 = (1.0 - xref) * o_muA(xref, T, sc, cv) + xref * o_muB(xref, T, sc, cv);
+    RLOOP_BEGIN(s)
+        const double h = o_h(o_clamp01(s->phi[idx]));
+        const double x = o_clamp_eps(s->xB[idx], 1e-12);
+        const double mix = (1.0 - x) * o_muA(x, T, sc, cv) + x * o_muB(x, T, sc, cv);
+        s->mass_t[idx] = (1.0 - h) * mix + h * P->mu0_compound - g0;
+    RLOOP_END
+    const double F_chem = dsum(s->mass_t, s->N) / (double)s->N;
+    const double F_total = F_chem + F_surf + F_el;
+    const double muBf = o_muB(xref, T, sc, cv);
+    const double F_chem_cnt = mean_h > 0.0 ? mean_h * (P->mu0_compound - muBf) : NAN;
+    const double F_total_cnt = F_surf + F_el + F_chem_cnt;
+    const double F_prev = s->prev_F_total;
+    s->prev_F_total = F_total;
+
+    /* ---- phi step with the under-relaxed volume multiplier ---- */
+    double eta_r = P->eta_lambda_vol;
+    if (eta_r < 0.0) eta_r = 0.0;
+    if (eta_r > 1.0) eta_r = 1.0;
+    RLOOP_BEGIN(s) s->xB[idx] = o_sigmoid(s->Y[idx], P->Y_clip, P->xB_eps); RLOOP_END   /* compute_mu_x_kernel */
+    phi_gradient(s, coupling);
+    s->lambda_vol = (1.0 - eta_r) * s->lambda_vol + eta_r * volume_lambda(s, s->mg);
+    phi_constrained_step(s, s->lambda_vol, dt);
+
+    /* ---- projected KKT residual and rms_dphi at phi^{n+1} ---- */
+    phi_gradient(s, coupling);
+    {
+        const double lk = volume_lambda(s, s->mg);
+        RLOOP_BEGIN(s)   /* compute_projected_phi_kkt_residual_sq_kernel, :684-708 */
+            const double ph = s->phi[idx];
+            double r = s->mg[idx] + lk * o_hp(ph);
+            if ((ph <= 1e-12 && r > 0.0) || (ph >= 1.0 - 1e-12 && r < 0.0)) r = 0.0;
+            s->mass_t[idx] = r * r;
+        RLOOP_END
+    }
+    const double rms_res = sqrt(dsum(s->mass_t, s->N) / (double)s->N);
+    RLOOP_BEGIN(s) { const double d = s->phi[idx] - s->phi_n[idx]; s->mass_t[idx] = d * d; } RLOOP_END
+    const double rms_dphi = sqrt(dsum(s->mass_t, s->N) / (double)s->N) / dt;
+
+    /* ---- Y update (full model) ---- */
+    int rc = y_update(s, &st, dt);
+    if (rc != PFGB_OK) return rc;
+
+    /* ---- post-projection substeps, elastic frozen, eta = 1 ---- */
+    for (int k = 0; k < P->minimize_post_projection_iters; ++k) {
+        phi_gradient(s, coupling);
+        s->lambda_vol = volume_lambda(s, s->mg);
+        phi_constrained_step(s, s->lambda_vol, dt);
+    }
+    mean_h = mean_h_clamped(s);
+
+    /* ---- first-order projection of <h> onto V0 ---- */
+    if (s->V0_target > 1e-30 && isfinite(mean_h)) {
+        const double vol_err = s->V0_target - mean_h;
+        if (fabs(vol_err) > 1e-14) {
+            RLOOP_BEGIN(s) { const double hp = o_hp(s->phi[idx]); s->mass_t[idx] = hp * hp; } RLOOP_END
+            const double mhp2 = dsum(s->mass_t, s->N) / (double)s->N;
+            const double lc = mhp2 > 1e-30 ? vol_err / mhp2 : 0.0;
+            RLOOP_BEGIN(s)   /* apply_volume_projection_kernel, :636-645 */
+                const double ph = s->phi[idx];
+                s->phi[idx] = o_clamp01(ph + lc * o_hp(ph));
+            RLOOP_END
+            mean_h = mean_h_clamped(s);
+        }
+    }
+
+    /* ---- stopping rule ---- */
+    double edr = NAN;
+    if (isfinite(F_prev) && isfinite(F_total)) edr = fabs(F_total - F_prev) / fmax(fabs(F_prev), 1e-20);
+    const double ver = s->V0_target > 1e-30 ? fabs(mean_h - s->V0_target) / (s->V0_target + 1e-30) : 0.0;
+    RLOOP_BEGIN(s) { const double d = s->Y[idx] - s->Y_n[idx]; s->mass_t[idx] = d * d; } RLOOP_END
+    const double rms_dY = sqrt(dsum(s->mass_t, s->N) / (double)s->N) / dt;
+    const int vol_ok = isfinite(ver) && ver < P->minimize_vol_err_rel_threshold;
+    const int res_ok = isfinite(rms_res) && rms_res < P->minimize_rms_res_threshold;
+    const int condA = isfinite(rms_dphi) && isfinite(rms_dY) && rms_dphi < P->minimize_rms_dphi_threshold &&
+                      rms_dY < P->minimize_rms_dY_threshold && res_ok && vol_ok;
+    const int condB = isfinite(edr) && edr < P->minimize_energy_diff_rel_threshold && isfinite(rms_dphi) &&
+                      isfinite(rms_dY) && rms_dphi < 5.0 * P->minimize_rms_dphi_threshold &&
+                      rms_dY < 5.0 * P->minimize_rms_dY_threshold && res_ok && vol_ok;
+    const double pt = (double)it * dt;
+    const int pt_ok = isfinite(pt) && pt + 1e-14 >= P->minimize_min_pseudo_time;
+    s->conv_count = ((condA || condB) && pt_ok) ? s->conv_count + 1 : 0;
+    if (s->conv_count >= P->minimize_convergence_steps && !s->converged_iter) s->converged_iter = it;
+
+    /* ---- xB safety clamp of the monitor step (every iteration here) ---- */
+    double xmax = -1e300;
+    for (size_t i = 0; i < s->N; ++i) if (s->xB[i] > xmax) xmax = s->xB[i];
+    int clamped = 0;
+    if (xmax > P->minimize_xB_max_safe + 1e-12) {   /* launch_clamp_xB_max_kernel */
+        clamped = 1;
+        RLOOP_BEGIN(s) if (s->xB[idx] > P->minimize_xB_max_safe) s->xB[idx] = P->minimize_xB_max_safe; RLOOP_END
+    }
+    s->step++;
+    if (ms) {
+        ms->iteration = it;
+        ms->converged = s->converged_iter != 0;
+        ms->converged_iteration = s->converged_iter;
+        ms->convergence_count = s->conv_count;
+        ms->condA = condA; ms->condB = condB;
+        ms->xB_clamped = clamped;
+        ms->elastic_iterations = st.elastic_iterations;
+        ms->elastic_relative_residual = st.elastic_relative_residual;
+        ms->mean_h = mean_h; ms->V0_target = s->V0_target; ms->lambda_vol = s->lambda_vol;
+        ms->F_surf = F_surf; ms->F_el = F_el; ms->F_chem_excess = F_chem; ms->F_total_excess = F_total;
+        ms->F_chem_CNT = F_chem_cnt; ms->F_total_CNT = F_total_cnt;
+        ms->total_interface_sum = total_interface; ms->total_el_core_sum = total_el_core;
+        ms->rms_res = rms_res; ms->rms_dphi = rms_dphi; ms->rms_dY = rms_dY;
+        ms->energy_diff_rel = edr; ms->vol_err_rel = ver;
+    }
+    return PFGB_OK;
+}
+
+int pfo_minimize(pfo_state *s, int max_iter, int stop_on_convergence, pfgb_min_stats *ms) {
+    const pfgb_params *P = &s->p;
+    if (P->mode != PFGB_MODE_MINIMIZE || !P->minimize_full_model || s->gp || P->zero_mode_enabled)
+        return PFGB_ERR_UNSUPPORTED;
+    for (int i = 0; i < max_iter; ++i) {
+        int rc = minimize_iter(s, ms);
+        if (rc != PFGB_OK) return rc;
+        if (stop_on_convergence && s->converged_iter) break;
+    }
     return PFGB_OK;
 }
 

@@ -39,6 +39,8 @@ int pfo_load_fields(pfo_state *s, const double *phi, const double *xB,
                     const double *eta, const double *dYdt_prev);
 /* returns a pfgb_status code */
 int pfo_step(pfo_state *s, int nsteps, pfgb_step_stats *stats);
+/* minimize iterations (mode = minimize, full model, two_phase, zero mode off) */
+int pfo_minimize(pfo_state *s, int max_iter, int stop_on_convergence, pfgb_min_stats *stats);
 int pfo_read_fields(const pfo_state *s, double *phi, double *xB, double *Y,
                     double *eta, double *dYdt_prev);
 int pfo_read_elastic(const pfo_state *s, double *sigma6, double *strain6);

@@ -34,9 +34,9 @@ def test_cli_help(capi, tmp_path):
 
 def test_cli_rejects_bad_inputs(capi, tmp_path):
     pf = os.path.join(GOLDEN, "c1.params")
-    # unsupported mode
-    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf, "--mode=minimize"], tmp_path)
-    assert r.returncode == 2
+    # unknown mode
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf, "--mode=relax"], tmp_path)
+    assert r.returncode == 2 and "--mode=relax" in r.stderr
     # no raw fields
     r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf], tmp_path)
     assert r.returncode == 2 and "raw_fields" in r.stderr
@@ -104,3 +104,32 @@ def test_cli_dynamics_run_matches_library(capi, tmp_path):
     assert abs(float(last[3]) - d.vf_precip) <= 1e-7 * max(1e-12, d.vf_precip)
     got = _vtk_values(case / "phi_final.vtk", (n, n, n))
     assert np.abs(got - f["phi"]).max() <= 6e-6
+
+
+@pytest.mark.gpu
+def test_cli_minimize_run(capi, tmp_path):
+    from cuda_sto_pf_gb300 import workloads
+    n, iters = 16, 5
+    w = workloads.single_sphere(n=n, radius=5.0)
+    w["phi"].tofile(tmp_path / "phi.raw")
+    w["xB"].tofile(tmp_path / "xB.raw")
+    pf = os.path.join(GOLDEN, "c2.params")
+    r = _run(capi, [str(n), str(n), str(n), "0.05", "100", "50", "1", "1", "--pf-param-file", pf,
+                    "--mode=minimize", "--minimize-full-model", "--minimize-max-iter", str(iters),
+                    "--minimize-dt", "0.05", "--V0", "0.05", "--init-mode", "raw_fields",
+                    "--init-phi-raw", str(tmp_path / "phi.raw"), "--init-xB-raw", str(tmp_path / "xB.raw")],
+             tmp_path, env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "R")})
+    assert r.returncode == 0, r.stderr
+    runs = os.listdir(tmp_path / "R")
+    assert len(runs) == 1 and "_steps5_r" in runs[0] and runs[0].endswith("nm_xB0.030")
+    case = tmp_path / "R" / runs[0] / "raw_fields_relax"
+    energy = [f for f in os.listdir(case) if f.startswith("energy_minimize_T")]
+    assert len(energy) == 1 and energy[0].endswith("_raw_fields_relax.csv")
+    rows = (case / energy[0]).read_text().strip().split("\n")
+    assert rows[0].startswith("iter,dt,mean_h,V0,lambda,F_surf_hat") and len(rows) == iters + 1
+    last = rows[-1].split(",")
+    assert int(last[0]) == iters and abs(float(last[3]) - 0.05) < 1e-12
+    assert abs(float(last[2]) - 0.05) < 1e-3          # <h> held at V0
+    for f in ("phi_init_raw_fields_relax.vtk", "xB_init_raw_fields_relax.vtk", "phi_final_raw_fields_relax.vtk",
+              "xB_final_raw_fields_relax.vtk", "vf_precip_vs_time_raw_fields_relax.csv", "elastic_solver_trace.csv"):
+        assert (case / f).exists(), f
