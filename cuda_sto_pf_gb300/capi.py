@@ -41,6 +41,7 @@ class Params(Structure):
         ("elastic_enabled", c_int32), ("elastic_warm_start_enabled", c_int32),
         ("elastic_residual_control_enabled", c_int32), ("elastic_iter_min", c_int32),
         ("elastic_iter_max", c_int32), ("elastic_fail_on_nonconvergence", c_int32),
+        ("elastic_increment_form", c_int32), ("pad3", c_int32),
         ("elastic_residual_tolerance", c_double), ("elastic_residual_absolute_floor", c_double),
         ("eps_iso_over_vB", c_double),
         ("eps00", c_double * 6), ("E0", c_double * 6),
@@ -96,6 +97,13 @@ class MinStats(Structure):
                 ("elastic_relative_residual", c_double)]
 
 
+class Case(Structure):
+    _fields_ = [("params", Params), ("phi", c_void_p), ("xB", c_void_p), ("eta", c_void_p),
+                ("phi_out", c_void_p), ("xB_out", c_void_p), ("max_iter", c_int32),
+                ("stop_on_convergence", c_int32), ("stats", MinStats), ("status", c_int32), ("pad", c_int32),
+                ("seconds", c_double)]
+
+
 class Diag(Structure):
     _fields_ = [("vf_precip", c_double), ("mass_xBtot", c_double), ("mean_xB", c_double),
                 ("phi_min", c_double), ("phi_max", c_double), ("xB_min", c_double),
@@ -122,6 +130,7 @@ EXPORTS = [
     ("pfgb_set_fields", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("pfgb_step", c_int, [c_void_p, c_int, POINTER(StepStats)]),
     ("pfgb_minimize", c_int, [c_void_p, c_int, c_int, POINTER(MinStats)]),
+    ("pfgb_batch_minimize", c_int, [POINTER(Case), c_int, c_int, c_int]),
     ("pfgb_read_fields", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("pfgb_read_elastic", c_int, [c_void_p, c_void_p, c_void_p]),
     ("pfgb_read_displacement_k", c_int, [c_void_p, c_void_p]),

@@ -82,6 +82,7 @@ struct pfgb_ctx {
     bool f246[3] = {false, false, false};   // x, y, z elastic passes on the 246-point engine
     // minimize state (mode = minimize)
     void *sig[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    void *Rk[3] = {nullptr, nullptr, nullptr}, *Dk[3] = {nullptr, nullptr, nullptr};   // increment form
     void *mge = nullptr, *mlap = nullptr;
     double lambda_vol = 0.0, V0_target = 0.0, prev_F_total = NAN;
     int min_iter = 0, conv_count = 0, converged_iter = 0, xb_clamp = 0;
@@ -590,6 +591,7 @@ template <typename T, typename TE>
 struct OpHijZ {
     using Acc = NoAcc;
     DevState<T, TE> d; PhysC c; ElasC<TE> ec;
+    int lin;   // increment form: the linear part -(h dC):eps only
     __device__ void load_spec(long long row, int k, cplx_t<TE> *v) const {
         const long long o = row * d.g.NzC + k;
 #pragma unroll
@@ -600,12 +602,17 @@ struct OpHijZ {
 #pragma unroll
         for (int a = 0; a < 6; ++a) e[a] = in[a] * ec.invN;
         const T phi = d.phi_old[cell];
-        const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
-        eigenstrain<T, TE>(c, ec, phi, c.gp ? d.eta_old[cell] : T(0), xB_el(c, xB), c.gp_el != 0, e0);
         const T h = pf_h(phi);
         TE tv[6];
+        if (lin) {
 #pragma unroll
-        for (int a = 0; a < 6; ++a) tv[a] = e[a] + ec.E0[a] - e0[a];
+            for (int a = 0; a < 6; ++a) tv[a] = e[a];
+        } else {
+            const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
+            eigenstrain<T, TE>(c, ec, phi, c.gp ? d.eta_old[cell] : T(0), xB_el(c, xB), c.gp_el != 0, e0);
+#pragma unroll
+            for (int a = 0; a < 6; ++a) tv[a] = e[a] + ec.E0[a] - e0[a];
+        }
 #pragma unroll
         for (int a = 0; a < 6; ++a) {
             TE acc = 0;
@@ -696,9 +703,59 @@ struct GreenArgs {
     Grid3 g; KTab kt; ElasC<TE> ec;
     const cplx_t<TE> *tw;
     cplx_t<TE> *E[6], *U[3];
+    cplx_t<TE> *R[3], *D[3];   // increment form: r0 and delta
     double *partials;
     int resid;
+    int mode;                  // 0 u <- Phi(u); 1 first increment step; 2 delta <- r0 + L delta
 };
+
+// the Green's-operator output at one k-point, by update form: stores the new
+// state, accumulates the residual sums, and returns the field whose strain
+// goes on (u, or the increment delta)
+template <typename TE>
+__device__ __forceinline__ void green_update(const GreenArgs<TE> &A, long long o, const cplx_t<TE> u[3], TE w,
+                                             TE &rd, TE &rr, cplx_t<TE> out[3]) {
+    using T2 = cplx_t<TE>;
+    TE ld_ = 0, lr = 0;
+    if (A.mode == 0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (A.resid) {
+                const T2 old = A.U[c][o];
+                const TE dr = u[c].x - old.x, di = u[c].y - old.y;
+                ld_ += dr * dr + di * di;
+                lr += u[c].x * u[c].x + u[c].y * u[c].y;
+            }
+            A.U[c][o] = u[c];
+            out[c] = u[c];
+        }
+    } else if (A.mode == 1) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const T2 u0 = A.U[c][o];
+            const T2 r = mk2<T2>(u[c].x - u0.x, u[c].y - u0.y);
+            A.R[c][o] = r;
+            A.D[c][o] = r;
+            ld_ += r.x * r.x + r.y * r.y;
+            lr += u[c].x * u[c].x + u[c].y * u[c].y;
+            out[c] = r;
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const T2 r0 = A.R[c][o], d = A.D[c][o], u0 = A.U[c][o];
+            const T2 dn = mk2<T2>(r0.x + u[c].x, r0.y + u[c].y);
+            const TE dr = dn.x - d.x, di = dn.y - d.y;
+            const TE ur = u0.x + dn.x, ui = u0.y + dn.y;
+            ld_ += dr * dr + di * di;
+            lr += ur * ur + ui * ui;
+            A.D[c][o] = dn;
+            out[c] = dn;
+        }
+    }
+    rd += w * ld_;
+    rr += w * lr;
+}
 
 template <typename TE>
 __device__ __forceinline__ void green_u(const TE *S, TE kx, TE ky, TE kz, const cplx_t<TE> t[3],
@@ -805,26 +862,14 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
         } else {
             green_u<TE>(A.ec.S, kv[0], kv[1], kv[2], t, u);
         }
+        T2 v[3] = {u[0], u[1], u[2]};
         if (l < kcnt) {
             const long long o = base + q * es + l;
-            if (A.resid) {
-                const TE w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? TE(1) : TE(2);
-                TE ld_ = 0, lr = 0;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const T2 old = A.U[c][o];
-                    const TE dr = u[c].x - old.x, di = u[c].y - old.y;
-                    ld_ += dr * dr + di * di;
-                    lr += u[c].x * u[c].x + u[c].y * u[c].y;
-                }
-                rd += w * ld_;
-                rr += w * lr;
-            }
-#pragma unroll
-            for (int c = 0; c < 3; ++c) A.U[c][o] = u[c];
+            const TE w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? TE(1) : TE(2);
+            green_update<TE>(A, o, u, w, rd, rr, v);
         }
 #pragma unroll
-        for (int c = 0; c < 6; ++c) oth[q * SP + c * TK + l] = strain_comp<TE>(c, kv[0], kv[1], kv[2], u);
+        for (int c = 0; c < 6; ++c) oth[q * SP + c * TK + l] = strain_comp<TE>(c, kv[0], kv[1], kv[2], v);
     }
     if (A.resid) {
         AccSum2 s{double(rd), double(rr)};
@@ -850,7 +895,7 @@ __global__ void k_resid_final(double *dscal, double floor_) {
 }
 
 template <typename TE>
-static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks) {
+static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks, int mode = 0) {
     using T2 = cplx_t<TE>;
     const int n = c->plx.n;
     auto bytes = [&](int tk) { return ((size_t)n + 2 * (size_t)n * (6 * tk + 1)) * sizeof(T2); };
@@ -864,13 +909,14 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
     for (int i = 0; i < 21; ++i) { A.ec.S[i] = (TE)c->p.S[i]; A.ec.Sp[i] = (TE)c->p.S_p[i]; }
     A.tw = (const T2 *)c->tw[sizeof(TE) == 8 ? 0 : 1][0];
     for (int i = 0; i < 6; ++i) A.E[i] = (T2 *)c->E[i];
-    for (int i = 0; i < 3; ++i) A.U[i] = (T2 *)c->U[i];
+    for (int i = 0; i < 3; ++i) { A.U[i] = (T2 *)c->U[i]; A.R[i] = (T2 *)c->Rk[i]; A.D[i] = (T2 *)c->Dk[i]; }
     A.partials = c->partials;
     A.resid = resid;
+    A.mode = mode;
     dim3 grid((c->g.NzC + TK - 1) / TK, c->g.Ny);
     // reads 6 source spectra (+3 old u for the residual), writes 3 u + 6 strain spectra
     ProfScope ps(c, {eigen ? "x_green_eigen" : "x_green_hij",
-                     (double)(6 + 3 + 6 + (resid ? 3 : 0)) * (double)c->g.Nk * sizeof(T2)});
+                     (double)(6 + 3 + 6 + (mode == 2 ? 9 : mode == 1 ? 6 : (resid ? 3 : 0))) * (double)c->g.Nk * sizeof(T2)});
     if (eigen) {
         auto kern = k_x_green<TE, true>;
         PFGB_CUDA_TRY(allow_smem(kern, smem));
@@ -955,26 +1001,14 @@ k_x_green246(GreenArgs<float> A) {
         } else {
             green_u<float>(A.ec.S, kv[0], kv[1], kv[2], t, u);
         }
+        T2 v[3] = {u[0], u[1], u[2]};
         if (l < kcnt) {
             const long long o = base + q * es + l;
-            if (A.resid) {
-                const float w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? 1.f : 2.f;
-                float ld_ = 0.f, lr = 0.f;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const T2 old = A.U[c][o];
-                    const float dr = u[c].x - old.x, di = u[c].y - old.y;
-                    ld_ += dr * dr + di * di;
-                    lr += u[c].x * u[c].x + u[c].y * u[c].y;
-                }
-                rd += w * ld_;
-                rr += w * lr;
-            }
-#pragma unroll
-            for (int c = 0; c < 3; ++c) A.U[c][o] = u[c];
+            const float w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? 1.f : 2.f;
+            green_update<float>(A, o, u, w, rd, rr, v);
         }
 #pragma unroll
-        for (int c = 0; c < 6; ++c) pt[c * 8] = strain_comp<float>(c, kv[0], kv[1], kv[2], u);
+        for (int c = 0; c < 6; ++c) pt[c * 8] = strain_comp<float>(c, kv[0], kv[1], kv[2], v);
     }
     if (A.resid) {
         AccSum2 sacc{double(rd), double(rr)};
@@ -1078,7 +1112,7 @@ static pfgb_status launch_y246(pfgb_ctx *c, const char *tag) {
     return PFGB_OK;
 }
 
-static pfgb_status launch_green246(pfgb_ctx *c, bool eigen, int resid, int *nblocks) {
+static pfgb_status launch_green246(pfgb_ctx *c, bool eigen, int resid, int *nblocks, int mode = 0) {
     const size_t smem = f246::axis_smem_bytes();
     GreenArgs<float> A;
     A.g = c->g;
@@ -1086,12 +1120,13 @@ static pfgb_status launch_green246(pfgb_ctx *c, bool eigen, int resid, int *nblo
     for (int i = 0; i < 21; ++i) { A.ec.S[i] = (float)c->p.S[i]; A.ec.Sp[i] = (float)c->p.S_p[i]; }
     A.tw = (const float2 *)c->tw[1][0];
     for (int i = 0; i < 6; ++i) A.E[i] = (float2 *)c->E[i];
-    for (int i = 0; i < 3; ++i) A.U[i] = (float2 *)c->U[i];
+    for (int i = 0; i < 3; ++i) { A.U[i] = (float2 *)c->U[i]; A.R[i] = (float2 *)c->Rk[i]; A.D[i] = (float2 *)c->Dk[i]; }
     A.partials = c->partials;
     A.resid = resid;
+    A.mode = mode;
     dim3 grid((c->g.NzC + 7) / 8, c->g.Ny);
     ProfScope ps(c, {eigen ? "x_green_eigen" : "x_green_hij",
-                     (double)(6 + 3 + 6 + (resid ? 3 : 0)) * (double)c->g.Nk * sizeof(float2)});
+                     (double)(6 + 3 + 6 + (mode == 2 ? 9 : mode == 1 ? 6 : (resid ? 3 : 0))) * (double)c->g.Nk * sizeof(float2)});
     if (eigen) {
         auto kern = k_x_green246<true>;
         PFGB_CUDA_TRY(allow_smem(kern, smem));
@@ -1163,6 +1198,17 @@ static pfgb_status sync_read(pfgb_ctx *c, int first, int count) {
     return PFGB_OK;
 }
 
+template <typename TE>
+__global__ void k_add_increment(cplx_t<TE> *u0, cplx_t<TE> *u1, cplx_t<TE> *u2, const cplx_t<TE> *d0,
+                                const cplx_t<TE> *d1, const cplx_t<TE> *d2, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        u0[i] = cadd(u0[i], d0[i]);
+        u1[i] = cadd(u1[i], d1[i]);
+        u2[i] = cadd(u2[i], d2[i]);
+    }
+}
+
 template <typename T, typename TE>
 static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     using T2e = cplx_t<TE>;
@@ -1185,23 +1231,25 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
         return dir < 0 ? launch_axis<TE, 6, 6, -1, 0>(c, 1, io6, OpCopy<TE, 6>{}, tag)
                        : launch_axis<TE, 6, 6, +1, 0>(c, 1, io6, OpCopy<TE, 6>{}, tag);
     };
-    auto green = [&](bool eigen, int resid) -> pfgb_status {
+    auto green = [&](bool eigen, int resid, int mode) -> pfgb_status {
         if constexpr (std::is_same<TE, float>::value) {
-            if (c->f246[0]) return launch_green246(c, eigen, resid, &nb);
+            if (c->f246[0]) return launch_green246(c, eigen, resid, &nb, mode);
         }
-        return launch_green<TE>(c, eigen, resid, &nb);
+        return launch_green<TE>(c, eigen, resid, &nb, mode);
     };
-    auto hij = [&]() -> pfgb_status {
-        const double extra = (2.0 + pc.gp) * Nf * sizeof(T);
+    auto hij = [&](int lin) -> pfgb_status {
+        const double extra = lin ? 2.0 * Nf * sizeof(T) : (2.0 + pc.gp) * Nf * sizeof(T);
         if constexpr (std::is_same<TE, float>::value) {
-            if (c->f246[2]) return launch_z246(c, OpHijZ<T, TE>{d, pc, ec}, "z_hij", extra);
+            if (c->f246[2]) return launch_z246(c, OpHijZ<T, TE>{d, pc, ec, lin}, "z_hij", extra);
         }
-        return launch_z<TE, 6, 6>(c, OpHijZ<T, TE>{d, pc, ec}, "z_hij", extra);
+        return launch_z<TE, 6, 6>(c, OpHijZ<T, TE>{d, pc, ec, lin}, "z_hij", extra);
     };
+    // increment form: one full update, then delta <- r0 + L delta
+    const int inc = accel && P.elastic_increment_form && c->Rk[0] != nullptr;
     if (!warm_used) {
         TRY((launch_z<TE, 0, 6>(c, OpEigenR2C<T, TE>{d, pc, ec}, "z_eigen_r2c", (2.0 + pc.gp) * Nf * sizeof(T))));
         TRY(ypass(-1, "y_fwd6"));
-        TRY(green(true, 0));
+        TRY(green(true, 0, 0));
     } else {
         AxisIO<TE, 3, 6> io;
         for (int i = 0; i < 3; ++i) io.in[i] = (const T2e *)c->U[i];
@@ -1213,9 +1261,10 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     int conv = accel ? 0 : 1;
     double rel = NAN;
     for (;;) {
-        TRY(hij());
+        const int lin = inc && iter >= 1;
+        TRY(hij(lin));
         TRY(ypass(-1, "y_fwd6"));
-        TRY(green(false, accel));
+        TRY(green(false, accel, inc ? (lin ? 2 : 1) : 0));
         TRY(ypass(+1, "y_inv6"));
         if (accel) {
             TRY(reduce_to<AccSum2>(c, nb, DS_RES_DIFF));
@@ -1248,6 +1297,21 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
         pfgb_set_error_msg("elastic solver did not converge at step %d: iterations=%d residual=%.17e",
                            c->step + 1, iter, rel);
         return PFGB_ERR_NONCONVERGED;
+    }
+    if (inc) {
+        // u = u0 + delta, and the strain of u for the final pass
+        {
+            ProfScope ps(c, {"add_increment", 9.0 * (double)c->g.Nk * sizeof(T2e)});
+            k_add_increment<TE><<<1216, 256, 0, c->stream>>>((T2e *)c->U[0], (T2e *)c->U[1], (T2e *)c->U[2],
+                                                             (const T2e *)c->Dk[0], (const T2e *)c->Dk[1],
+                                                             (const T2e *)c->Dk[2], c->g.Nk);
+            PFGB_CUDA_TRY(cudaGetLastError());
+        }
+        AxisIO<TE, 3, 6> io;
+        for (int i = 0; i < 3; ++i) io.in[i] = (const T2e *)c->U[i];
+        for (int i = 0; i < 6; ++i) io.out[i] = (T2e *)c->E[i];
+        TRY((launch_axis<TE, 3, 6, 0, +1>(c, 2, io, OpStrainFromUX<TE>{kt}, "x_strain_from_u")));
+        TRY(ypass(+1, "y_inv6"));
     }
     TRY((launch_z<TE, 6, 0>(c, OpStrainFinalZ<T, TE>{d, ec, pc}, "z_strain_final",
                                 (d.sig[0] ? 12.0 : 6.0) * Nf * sizeof(TE))));
@@ -2042,6 +2106,7 @@ static void ctx_free(pfgb_ctx *c) {
     for (int i = 0; i < 3; ++i) f(c->U[i]);
     f(c->partials); f(c->dscal); f(c->stage);
     for (int i = 0; i < 6; ++i) f(c->sig[i]);
+    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); }
     f(c->mge); f(c->mlap);
     for (auto e : c->pool) cudaEventDestroy(e);
     if (c->hscal) cudaFreeHost(c->hscal);
@@ -2165,6 +2230,10 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
     if (pin->elastic_enabled) {
         for (int i = 0; i < 6; ++i) { A_(&c->E[i], sizeof(float2) * Nk); }
         for (int i = 0; i < 3; ++i) { A_(&c->U[i], sizeof(float2) * Nk); }
+        if (pin->elastic_increment_form &&
+            (pin->elastic_warm_start_enabled || pin->elastic_residual_control_enabled)) {
+            for (int i = 0; i < 3; ++i) { A_(&c->Rk[i], sizeof(float2) * Nk); A_(&c->Dk[i], sizeof(float2) * Nk); }
+        }
     }
     if (pin->mode == PFGB_MODE_MINIMIZE) {
         for (int i = 0; i < 6; ++i) { A_(&c->sig[i], sizeof(float) * N); }

@@ -116,3 +116,43 @@ def ellipsoid_population(n=246, count=60, median_r=6.0, sigma_ln=0.3, eta_sites=
     eta = ellipsoid_field(shape, ecs, [np.full(3, eta_r)] * len(ecs), [np.eye(3)] * len(ecs), w)
     return {"phi": phi, "xB": composition(phi, rng), "eta": eta,
             "n_particles": len(centers), "n_eta": len(ecs)}
+
+
+EIGEN_DIAG = (0.046, -0.022, -0.017)
+
+
+def rotated_eigenstrain(rot, diag=EIGEN_DIAG):
+    """R diag(e) R^T as the 6-vector xx, yy, zz, yz, xz, xy."""
+    E = rot @ np.diag(diag) @ rot.T
+    return [E[0, 0], E[1, 1], E[2, 2], E[1, 2], E[0, 2], E[0, 1]]
+
+
+def sweep_cases(count=48, sizes=(64, 80, 96, 112, 128, 144, 160), ratios=(1.0, 0.6, 0.3),
+                r_range=(10.0, 40.0), n_rot=8, w=2.5, seed=7):
+    """The batched minimize sweep: cubic grids cycled through `sizes`, a
+    sphere or oblate spheroid (semi-axes R, R, (c/a) R) of radius R in
+    r_range (capped below n/2 - 2w), and the eigenstrain rotated by one of
+    n_rot seeded rotations (the spheroid shares the rotation)."""
+    rng = np.random.default_rng(seed)
+    rots = [random_rotation(rng) for _ in range(n_rot)]
+    cases = []
+    for i in range(count):
+        n = sizes[i % len(sizes)]
+        ca = ratios[int(rng.integers(len(ratios)))]
+        R = float(rng.uniform(*r_range))
+        R = min(R, n / 2 - 2 * w - 1)
+        k = int(rng.integers(n_rot))
+        cases.append({"n": n, "ca": ca, "radius": R, "rot": rots[k], "rot_index": k,
+                      "eps00": rotated_eigenstrain(rots[k]), "seed": int(rng.integers(1 << 30))})
+    return cases
+
+
+def spheroid_fields(case, w=2.5):
+    """Centred spheroid seed (tanh profile of init_phi_kernel) and the
+    composition of `composition`."""
+    n, R, ca = case["n"], case["radius"], case["ca"]
+    shape = (n, n, n)
+    c = np.array([n / 2, n / 2, n / 2])
+    phi = ellipsoid_field(shape, [c], [np.array([R, R, ca * R])], [case["rot"]], w)
+    rng = np.random.default_rng(case["seed"])
+    return {"phi": phi, "xB": composition(phi, rng)}

@@ -94,6 +94,14 @@ typedef struct pfgb_params {
     int32_t elastic_iter_min;
     int32_t elastic_iter_max;
     int32_t elastic_fail_on_nonconvergence;
+    /* 1: iterate the increment delta = u - u0 from the warm start u0 (after
+       one full evaluation r0 = Phi(u0) - u0, each update is delta <- r0 +
+       L delta with only the linear part of the operator); the same iterates
+       and residual as the reference's u <- Phi(u) in exact arithmetic, with
+       FP32 rounding noise relative to |delta| instead of |u|.  0: the
+       reference's form.  No counterpart key in the reference. */
+    int32_t elastic_increment_form;
+    int32_t pad3;
     double elastic_residual_tolerance;
     double elastic_residual_absolute_floor;
     double eps_iso_over_vB;
@@ -191,6 +199,20 @@ typedef struct pfgb_min_stats {
     double elastic_relative_residual;
 } pfgb_min_stats;
 
+/* One case of a batched minimize sweep (pfgb_batch_minimize). */
+typedef struct pfgb_case {
+    pfgb_params params;        /* mode = minimize; grids may differ per case   */
+    const double *phi, *xB;    /* host raw fields, N = Nx*Ny*Nz float64 each   */
+    const double *eta;         /* may be NULL                                  */
+    double *phi_out, *xB_out;  /* final fields (host, may be NULL)             */
+    int32_t max_iter;          /* minimize iterations (minimize_max_iter if <= 0) */
+    int32_t stop_on_convergence;
+    pfgb_min_stats stats;      /* out: statistics of the last iteration        */
+    int32_t status;            /* out: pfgb_status of the case                 */
+    int32_t pad;
+    double seconds;            /* out: wall time of the case                   */
+} pfgb_case;
+
 /* Scalar diagnostics of the current state (CSV row, mass ledger). */
 typedef struct pfgb_diag {
     double vf_precip;      /* <h(phi)>, gpu_compute_vf_from_h            */
@@ -267,6 +289,14 @@ pfgb_status pfgb_step(pfgb_ctx *ctx, int nsteps, pfgb_step_stats *stats);
  * (main_cuda.cu:29264-29750, 32100-32600), stopping early when the
  * reference's convergence rule is met and stop_on_convergence != 0. */
 pfgb_status pfgb_minimize(pfgb_ctx *ctx, int max_iter, int stop_on_convergence, pfgb_min_stats *stats);
+/* Batched minimize sweep: the reference runs such sweeps (radius, shape and
+ * eigenstrain-direction scans) as separate main_cuda jobs.  Here the cases
+ * share the device: up to `concurrency` cases run at once, each with its
+ * own context and stream, fed from a queue by host threads.  Every case's
+ * status lands in cases[i].status; the return value is PFGB_OK when all
+ * succeeded, else the first failing status.  No counterpart in the
+ * reference's library (it has none); replaces the sweep job scripts. */
+pfgb_status pfgb_batch_minimize(pfgb_case *cases, int ncases, int device, int concurrency);
 
 /* Read the state back to HOST buffers (float64); any pointer may be NULL. */
 pfgb_status pfgb_read_fields(pfgb_ctx *ctx, double *phi, double *xB, double *Y,

@@ -246,6 +246,7 @@ struct pfo_state {
     /* elastic */
     double *eps_r[6], *sig_r[6];
     cpx *eps_k[6], *u_k[3], *u_next[3];
+    cpx *r_k[3], *d_k[3];   /* increment form: r0 = Phi(u0) - u0 and delta */
     int warm_valid;
     /* k tables */
     double *kx, *ky, *kz;
@@ -300,6 +301,8 @@ pfo_state *pfo_create(const pfgb_params *pin) {
     for (int c = 0; c < 3; ++c) {
         s->u_k[c] = (cpx *)xalloc(kb);
         s->u_next[c] = (cpx *)xalloc(kb);
+        s->r_k[c] = (cpx *)xalloc(kb);
+        s->d_k[c] = (cpx *)xalloc(kb);
     }
     s->mlap = (double *)xalloc(rb);
     s->mg = (double *)xalloc(rb);
@@ -329,7 +332,7 @@ void pfo_destroy(pfo_state *s) {
     cpx *kk[] = {s->phi_k, s->rhs_k, s->mu_k, s->divJ_k, s->Y_k, s->scr_k, s->eta_k};
     for (size_t i = 0; i < sizeof(kk) / sizeof(kk[0]); ++i) free(kk[i]);
     for (int c = 0; c < 6; ++c) { free(s->eps_r[c]); free(s->sig_r[c]); free(s->eps_k[c]); }
-    for (int c = 0; c < 3; ++c) { free(s->u_k[c]); free(s->u_next[c]); }
+    for (int c = 0; c < 3; ++c) { free(s->u_k[c]); free(s->u_next[c]); free(s->r_k[c]); free(s->d_k[c]); }
     free(s->kx); free(s->ky); free(s->kz); free(s->mx); free(s->my); free(s->mz);
     free(s->mlap); free(s->mg);
     free(s);
@@ -594,8 +597,13 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
     int iter = accel ? 0 : 1;
     int conv = accel ? 0 : 1;
     double rel = NAN;
+    /* increment form (elastic_increment_form): the first update is the full
+     * u1 = Phi(u0); then delta <- r0 + L delta with r0 = u1 - u0 and L the
+     * linear part h_lin = -(h dC):eps(delta) of the operator */
+    const int inc = accel && P->elastic_increment_form;
     for (;;) {
-        strain_from_u(s, s->u_k, s->eps_k);
+        const int lin = inc && iter >= 1;
+        strain_from_u(s, lin ? s->d_k : s->u_k, s->eps_k);
         for (int c = 0; c < 6; ++c) dealias(s, s->eps_k[c]);
         for (int c = 0; c < 6; ++c) elastic_inv(s, s->eps_k[c], s->eps_r[c]);
         /* normalize_strain_kernel (float invN) */
@@ -612,7 +620,7 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
             double hw = o_h(s->phi[idx]);   /* stiffness_beta_weight_point */
             double ev[6], tv[6];
             double tot[6];
-            for (int c = 0; c < 6; ++c) tot[c] = e[c] + ec.E0[c] - e0[c];
+            for (int c = 0; c < 6; ++c) tot[c] = lin ? e[c] : e[c] + ec.E0[c] - e0[c];
             eng(e, ev); eng(tot, tv);
             static const int rowv[6] = {1, 2, 3, 4, 5, 6};
             for (int c = 0; c < 6; ++c) {
@@ -629,7 +637,38 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
         cpx **target = accel ? s->u_next : s->u_k;
         green_apply(s, &ec, s->eps_k, 0, target);
         for (int c = 0; c < 3; ++c) dealias(s, target[c]);
-        if (accel) {
+        if (inc) {
+            /* the same residual on the increment iterates */
+            double *dif = s->mass_t, *ref = s->der_t;
+            KLOOP_BEGIN(s)
+                double w = (kk_ == 0 || ((s->Nz % 2) == 0 && kk_ == s->Nz / 2)) ? 1.0 : 2.0;
+                double ld = 0.0, lr = 0.0;
+                for (int c = 0; c < 3; ++c) {
+                    const cpx v = s->u_next[c][idx];
+                    if (!lin) {   /* r0 = u1 - u0, delta = r0, u_new = u1 */
+                        cpx r = {rf(s, v.re - s->u_k[c][idx].re), rf(s, v.im - s->u_k[c][idx].im)};
+                        s->r_k[c][idx] = r;
+                        s->d_k[c][idx] = r;
+                        ld += r.re * r.re + r.im * r.im;
+                        lr += v.re * v.re + v.im * v.im;
+                    } else {      /* delta_new = r0 + L delta, u_new = u0 + delta_new */
+                        cpx dn = {rf(s, s->r_k[c][idx].re + v.re), rf(s, s->r_k[c][idx].im + v.im)};
+                        const double dr = dn.re - s->d_k[c][idx].re, di = dn.im - s->d_k[c][idx].im;
+                        const double ur = rf(s, s->u_k[c][idx].re + dn.re), ui = rf(s, s->u_k[c][idx].im + dn.im);
+                        s->d_k[c][idx] = dn;
+                        ld += dr * dr + di * di;
+                        lr += ur * ur + ui * ui;
+                    }
+                }
+                dif[idx] = w * ld; ref[idx] = w * lr;
+            KLOOP_END
+            double ds = dsum(dif, s->Nk), rs = dsum(ref, s->Nk);
+            if (!isfinite(ds) || !isfinite(rs) || ds < 0.0 || rs < 0.0) return PFGB_ERR_NONFINITE;
+            rel = sqrt(ds / fmax(rs, P->elastic_residual_absolute_floor));
+            ++iter;
+            if (iter >= P->elastic_iter_min && rel <= P->elastic_residual_tolerance) { conv = 1; break; }
+            if (iter >= P->elastic_iter_max) break;
+        } else if (accel) {
             /* compute_elastic_displacement_residual_kernel, :6436-6467 */
             double *dif = s->mass_t, *ref = s->der_t;
             /* residual arrays sized Nk <= N */
@@ -656,6 +695,14 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
             ++iter;
             if (iter >= P->elastic_iter_max) break;
         }
+    }
+    if (inc) {
+        KLOOP_BEGIN(s)
+            for (int c = 0; c < 3; ++c) {
+                s->u_k[c][idx].re = rf(s, s->u_k[c][idx].re + s->d_k[c][idx].re);
+                s->u_k[c][idx].im = rf(s, s->u_k[c][idx].im + s->d_k[c][idx].im);
+            }
+        KLOOP_END
     }
     if (accel) s->warm_valid = 1;
     if (st) {

@@ -188,3 +188,33 @@ def test_diagnostics_parity(capi, oracle):
     # cell counts: a cell within 1e-9 of a threshold may fall either side
     assert abs(d.n_in - do.n_in) <= 2 and abs(d.n_if - do.n_if) <= 2
     assert d.n_if > 0 and d.n_in > 0
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_increment_form_matches_reference_form(capi, oracle, prec):
+    """elastic_increment_form = 0 (the reference's u <- Phi(u)) and = 1 (delta
+    iteration) on the GPU against the oracle in the same form, and against
+    each other."""
+    from cuda_sto_pf_gb300.solver import Solver
+    out = {}
+    for inc in (0, 1):
+        p = params_for(capi, "c2.params", n=32, precision=prec, elastic_increment_form=inc)
+        phi, xB, _ = _inputs(capi, p, 32, False, seed=13)
+        o = oracle(p, threads=4)
+        o.load(phi, xB)
+        so = capi.StepStats()
+        assert o.step(3, so) == 0
+        with Solver(p) as s:
+            s.load(phi, xB)
+            sg = s.step(3)
+            fg = s.fields()
+            eg = s.elastic()
+        fo = o.fields()
+        for k in ("phi", "xB", "Y"):
+            assert rel_l2(fg[k], fo[k]) <= TOL[prec], (inc, k)
+        assert rel_l2(eg["strain"], o.elastic()["strain"]) <= TOL[prec]
+        assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1
+        out[inc] = (fg, eg)
+    for k in ("phi", "xB"):
+        assert rel_l2(out[1][0][k], out[0][0][k]) <= TOL[prec], k
+    assert rel_l2(out[1][1]["strain"], out[0][1]["strain"]) <= TOL[prec]
