@@ -41,7 +41,7 @@ class Params(Structure):
         ("elastic_enabled", c_int32), ("elastic_warm_start_enabled", c_int32),
         ("elastic_residual_control_enabled", c_int32), ("elastic_iter_min", c_int32),
         ("elastic_iter_max", c_int32), ("elastic_fail_on_nonconvergence", c_int32),
-        ("elastic_increment_form", c_int32), ("pad3", c_int32),
+        ("elastic_increment_form", c_int32), ("elastic_warm_start_extrapolate", c_int32),
         ("elastic_residual_tolerance", c_double), ("elastic_residual_absolute_floor", c_double),
         ("eps_iso_over_vB", c_double),
         ("eps00", c_double * 6), ("E0", c_double * 6),
@@ -101,7 +101,7 @@ class Case(Structure):
     _fields_ = [("params", Params), ("phi", c_void_p), ("xB", c_void_p), ("eta", c_void_p),
                 ("phi_out", c_void_p), ("xB_out", c_void_p), ("max_iter", c_int32),
                 ("stop_on_convergence", c_int32), ("stats", MinStats), ("status", c_int32), ("pad", c_int32),
-                ("seconds", c_double)]
+                ("seconds", c_double), ("message", ctypes.c_char * 160)]
 
 
 class Diag(Structure):

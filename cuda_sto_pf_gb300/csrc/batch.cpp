@@ -2,6 +2,7 @@
 // host worker threads, one context (and CUDA stream) per running case so the
 // small grids of a sweep share the device.
 #include <atomic>
+#include <cstdio>
 #include <chrono>
 #include <cstring>
 #include <thread>
@@ -46,7 +47,10 @@ extern "C" pfgb_status pfgb_batch_minimize(pfgb_case *cases, int ncases, int dev
         for (;;) {
             const int i = next.fetch_add(1);
             if (i >= ncases) return;
+            cases[i].message[0] = '\0';
             cases[i].status = run_case(&cases[i], device);
+            if (cases[i].status != PFGB_OK)
+                snprintf(cases[i].message, sizeof(cases[i].message), "%s", pfgb_last_error(nullptr));
         }
     };
     for (int i = 0; i < ncases; ++i) cases[i].status = -1;

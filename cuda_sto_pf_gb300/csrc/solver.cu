@@ -15,8 +15,10 @@
 // filters; see the op comments), with Y carried as Y_f + c where the scalar
 // offset c (FP64) absorbs the zero-mode shift.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <type_traits>
@@ -83,6 +85,8 @@ struct pfgb_ctx {
     // minimize state (mode = minimize)
     void *sig[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     void *Rk[3] = {nullptr, nullptr, nullptr}, *Dk[3] = {nullptr, nullptr, nullptr};   // increment form
+    void *Uprev[3] = {nullptr, nullptr, nullptr};   // extrapolated warm start: u of the step before
+    int warm_count = 0;
     void *mge = nullptr, *mlap = nullptr;
     double lambda_vol = 0.0, V0_target = 0.0, prev_F_total = NAN;
     int min_iter = 0, conv_count = 0, converged_iter = 0, xb_clamp = 0;
@@ -134,10 +138,43 @@ struct ProfScope {
 // ---------------------------------------------------------------------------
 static const size_t kSmemBudget = 112 * 1024;
 
+// The dynamic shared-memory limit is an attribute of the kernel function,
+// shared by every context in the process: it is raised to the device's
+// opt-in maximum (the same value from every thread), never set to one
+// launch's size, so contexts of different grids can launch concurrently.
+static int smem_optin_max() {
+    static std::atomic<int> v(0);
+    int m = v.load();
+    if (m == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&m, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || m <= 0)
+            m = 227 * 1024;
+        v.store(m);
+    }
+    return m;
+}
+static std::mutex g_smem_mu;
+static std::map<std::pair<int, const void *>, int> g_smem_limit;   // (device, kernel) -> dynamic limit
+
 template <typename K>
 static cudaError_t allow_smem(K kernel, size_t bytes) {
     if (bytes <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const auto key = std::make_pair(dev, (const void *)kernel);
+    std::lock_guard<std::mutex> lk(g_smem_mu);
+    auto it = g_smem_limit.find(key);
+    if (it == g_smem_limit.end()) {
+        // static + dynamic shared memory may not exceed the opt-in maximum
+        cudaFuncAttributes fa;
+        if ((e = cudaFuncGetAttributes(&fa, kernel)) != cudaSuccess) return e;
+        const int m = smem_optin_max() - (int)fa.sharedSizeBytes;
+        if ((e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, m)) != cudaSuccess) return e;
+        it = g_smem_limit.emplace(key, m).first;
+    }
+    return (int)bytes <= it->second ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 template <typename T>
@@ -1209,6 +1246,21 @@ __global__ void k_add_increment(cplx_t<TE> *u0, cplx_t<TE> *u1, cplx_t<TE> *u2, 
     }
 }
 
+template <typename TE>
+__global__ void k_extrapolate_u(cplx_t<TE> *u0, cplx_t<TE> *u1, cplx_t<TE> *u2, cplx_t<TE> *p0, cplx_t<TE> *p1,
+                                cplx_t<TE> *p2, long long n, int extrapolate) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        cplx_t<TE> *u[3] = {u0, u1, u2}, *p[3] = {p0, p1, p2};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const cplx_t<TE> un = u[c][i];
+            if (extrapolate) u[c][i] = mk2<cplx_t<TE>>(TE(2) * un.x - p[c][i].x, TE(2) * un.y - p[c][i].y);
+            p[c][i] = un;
+        }
+    }
+}
+
 template <typename T, typename TE>
 static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     using T2e = cplx_t<TE>;
@@ -1251,6 +1303,14 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
         TRY(ypass(-1, "y_fwd6"));
         TRY(green(true, 0, 0));
     } else {
+        if (c->Uprev[0]) {
+            // u0 = 2 u^n - u^{n-1} once both exist; keep u^n for the next step
+            ProfScope ps(c, {"extrapolate_u", 12.0 * (double)c->g.Nk * sizeof(T2e)});
+            k_extrapolate_u<TE><<<1216, 256, 0, c->stream>>>((T2e *)c->U[0], (T2e *)c->U[1], (T2e *)c->U[2],
+                                                             (T2e *)c->Uprev[0], (T2e *)c->Uprev[1],
+                                                             (T2e *)c->Uprev[2], c->g.Nk, c->warm_count >= 2);
+            PFGB_CUDA_TRY(cudaGetLastError());
+        }
         AxisIO<TE, 3, 6> io;
         for (int i = 0; i < 3; ++i) io.in[i] = (const T2e *)c->U[i];
         for (int i = 0; i < 6; ++i) io.out[i] = (T2e *)c->E[i];
@@ -1285,7 +1345,7 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
             if (iter >= P.elastic_iter_max) break;
         }
     }
-    if (accel) c->warm_valid = 1;
+    if (accel) { c->warm_valid = 1; c->warm_count++; }
     if (st) {
         st->elastic_iterations = iter;
         st->elastic_converged = conv;
@@ -2106,7 +2166,7 @@ static void ctx_free(pfgb_ctx *c) {
     for (int i = 0; i < 3; ++i) f(c->U[i]);
     f(c->partials); f(c->dscal); f(c->stage);
     for (int i = 0; i < 6; ++i) f(c->sig[i]);
-    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); }
+    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); f(c->Uprev[i]); }
     f(c->mge); f(c->mlap);
     for (auto e : c->pool) cudaEventDestroy(e);
     if (c->hscal) cudaFreeHost(c->hscal);
@@ -2149,6 +2209,7 @@ static pfgb_status load_device(pfgb_ctx *c, const double *phi, const double *xB,
     c->target_mass = c->hscal[DS_ZM];
     for (int i = 0; i < 6; ++i) PFGB_CUDA_TRY(cudaMemsetAsync(c->eps[i], 0, sizeof(float) * c->g.N, c->stream));
     c->warm_valid = 0;
+    c->warm_count = 0;
     c->step = 0;
     c->min_iter = c->conv_count = c->converged_iter = c->xb_clamp = 0;
     c->lambda_vol = 0.0;
@@ -2234,6 +2295,10 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
             (pin->elastic_warm_start_enabled || pin->elastic_residual_control_enabled)) {
             for (int i = 0; i < 3; ++i) { A_(&c->Rk[i], sizeof(float2) * Nk); A_(&c->Dk[i], sizeof(float2) * Nk); }
         }
+        if (pin->elastic_warm_start_extrapolate &&
+            (pin->elastic_warm_start_enabled || pin->elastic_residual_control_enabled)) {
+            for (int i = 0; i < 3; ++i) { A_(&c->Uprev[i], sizeof(float2) * Nk); }
+        }
     }
     if (pin->mode == PFGB_MODE_MINIMIZE) {
         for (int i = 0; i < 6; ++i) { A_(&c->sig[i], sizeof(float) * N); }
@@ -2256,6 +2321,12 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
         cudaError_t e = cudaMemset(c->eta[0], 0, rs * N);
         if (e != cudaSuccess) { pfgb_set_error("cudaMemset", e, __FILE__, __LINE__); s = PFGB_ERR_CUDA; }
     }
+    // the table uploads and the memset above run on the legacy default
+    // stream, which a non-blocking caller stream does not wait for
+    if (s == PFGB_OK) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) { pfgb_set_error("cudaDeviceSynchronize", e, __FILE__, __LINE__); s = PFGB_ERR_CUDA; }
+    }
     if (s != PFGB_OK) {
         ctx_free(c);
         delete c;
@@ -2277,6 +2348,8 @@ const char *pfgb_last_error(const pfgb_ctx *) { return pfgb_error_buffer(); }
 
 pfgb_status pfgb_set_stream(pfgb_ctx *c, void *s) {
     if (!c) return PFGB_ERR_INVALID;
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));   // work queued on the previous stream
     c->stream = (cudaStream_t)s;
     return PFGB_OK;
 }

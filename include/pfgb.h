@@ -101,7 +101,11 @@ typedef struct pfgb_params {
        FP32 rounding noise relative to |delta| instead of |u|.  0: the
        reference's form.  No counterpart key in the reference. */
     int32_t elastic_increment_form;
-    int32_t pad3;
+    /* 1: once two earlier steps' solutions exist, start the fixed point from
+       the linear extrapolation 2 u^n - u^{n-1} instead of u^n (the
+       reference's warm start, main_cuda.cu:28795-28807); it converges to the
+       same tolerance from a guess accurate to O(dt^2).  Default 0. */
+    int32_t elastic_warm_start_extrapolate;
     double elastic_residual_tolerance;
     double elastic_residual_absolute_floor;
     double eps_iso_over_vB;
@@ -211,6 +215,7 @@ typedef struct pfgb_case {
     int32_t status;            /* out: pfgb_status of the case                 */
     int32_t pad;
     double seconds;            /* out: wall time of the case                   */
+    char message[160];         /* out: pfgb_last_error text when status != OK  */
 } pfgb_case;
 
 /* Scalar diagnostics of the current state (CSV row, mass ledger). */

@@ -247,6 +247,8 @@ struct pfo_state {
     double *eps_r[6], *sig_r[6];
     cpx *eps_k[6], *u_k[3], *u_next[3];
     cpx *r_k[3], *d_k[3];   /* increment form: r0 = Phi(u0) - u0 and delta */
+    cpx *u_prev[3];         /* extrapolated warm start: u of the step before */
+    int warm_count;         /* solutions available for the warm start */
     int warm_valid;
     /* k tables */
     double *kx, *ky, *kz;
@@ -303,6 +305,7 @@ pfo_state *pfo_create(const pfgb_params *pin) {
         s->u_next[c] = (cpx *)xalloc(kb);
         s->r_k[c] = (cpx *)xalloc(kb);
         s->d_k[c] = (cpx *)xalloc(kb);
+        s->u_prev[c] = (cpx *)xalloc(kb);
     }
     s->mlap = (double *)xalloc(rb);
     s->mg = (double *)xalloc(rb);
@@ -332,7 +335,7 @@ void pfo_destroy(pfo_state *s) {
     cpx *kk[] = {s->phi_k, s->rhs_k, s->mu_k, s->divJ_k, s->Y_k, s->scr_k, s->eta_k};
     for (size_t i = 0; i < sizeof(kk) / sizeof(kk[0]); ++i) free(kk[i]);
     for (int c = 0; c < 6; ++c) { free(s->eps_r[c]); free(s->sig_r[c]); free(s->eps_k[c]); }
-    for (int c = 0; c < 3; ++c) { free(s->u_k[c]); free(s->u_next[c]); free(s->r_k[c]); free(s->d_k[c]); }
+    for (int c = 0; c < 3; ++c) { free(s->u_k[c]); free(s->u_next[c]); free(s->r_k[c]); free(s->d_k[c]); free(s->u_prev[c]); }
     free(s->kx); free(s->ky); free(s->kz); free(s->mx); free(s->my); free(s->mz);
     free(s->mlap); free(s->mg);
     free(s);
@@ -594,6 +597,19 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
         for (int c = 0; c < 3; ++c) dealias(s, s->u_k[c]);
     }
 
+    if (warm_used && P->elastic_warm_start_extrapolate) {
+        /* u0 = 2 u^n - u^{n-1} once both exist; keep u^n for the next step */
+        KLOOP_BEGIN(s)
+            for (int c = 0; c < 3; ++c) {
+                const cpx un = s->u_k[c][idx];
+                if (s->warm_count >= 2) {
+                    s->u_k[c][idx].re = rf(s, 2.0 * un.re - s->u_prev[c][idx].re);
+                    s->u_k[c][idx].im = rf(s, 2.0 * un.im - s->u_prev[c][idx].im);
+                }
+                s->u_prev[c][idx] = un;
+            }
+        KLOOP_END
+    }
     int iter = accel ? 0 : 1;
     int conv = accel ? 0 : 1;
     double rel = NAN;
@@ -704,7 +720,7 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
             }
         KLOOP_END
     }
-    if (accel) s->warm_valid = 1;
+    if (accel) { s->warm_valid = 1; s->warm_count++; }
     if (st) {
         st->elastic_iterations = iter;
         st->elastic_converged = conv;
@@ -1377,6 +1393,7 @@ int pfo_load_fields(pfo_state *s, const double *phi, const double *xB, const dou
     if (dYdt) memcpy(s->dYdt, dYdt, sizeof(double) * s->N); else memset(s->dYdt, 0, sizeof(double) * s->N);
     for (size_t i = 0; i < s->N; ++i) s->Y[i] = o_logit(s->xB[i], P->xB_eps, P->Y_clip);
     s->warm_valid = 0;
+    s->warm_count = 0;
     s->step = 0;
     /* gpu_reduce_sum_xBtot, main_cuda.cu:28079-28086 */
     RLOOP_BEGIN(s)

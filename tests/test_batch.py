@@ -35,7 +35,7 @@ def test_batch_minimize_equals_single_runs(capi):
     from cuda_sto_pf_gb300 import workloads
     from cuda_sto_pf_gb300.solver import Solver
     lib = capi.load()
-    specs = [dict(c, n=n, radius=5.0) for c, n in zip(workloads.sweep_cases(count=4), (16, 24, 20, 16))]
+    specs = [dict(c, n=n, radius=5.0) for c, n in zip(workloads.sweep_cases(count=4), (16, 64, 40, 96))]
     iters = 4
     arr = (capi.Case * len(specs))()
     keep = []

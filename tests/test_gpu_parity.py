@@ -218,3 +218,25 @@ def test_increment_form_matches_reference_form(capi, oracle, prec):
     for k in ("phi", "xB"):
         assert rel_l2(out[1][0][k], out[0][0][k]) <= TOL[prec], k
     assert rel_l2(out[1][1]["strain"], out[0][1]["strain"]) <= TOL[prec]
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_extrapolated_warm_start_parity(capi, oracle, prec):
+    """elastic_warm_start_extrapolate = 1: from the third step the fixed point
+    starts at 2 u^n - u^{n-1}; GPU against the oracle doing the same."""
+    from cuda_sto_pf_gb300.solver import Solver
+    p = params_for(capi, "c2.params", n=32, precision=prec, elastic_warm_start_extrapolate=1)
+    phi, xB, _ = _inputs(capi, p, 32, False, seed=17)
+    o = oracle(p, threads=4)
+    o.load(phi, xB)
+    so, sg = capi.StepStats(), None
+    with Solver(p) as s:
+        s.load(phi, xB)
+        for k in range(5):
+            assert o.step(1, so) == 0
+            sg = s.step(1)
+            assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1, k
+        fg = s.fields()
+    fo = o.fields()
+    for k in ("phi", "xB", "Y"):
+        assert rel_l2(fg[k], fo[k]) <= TOL[prec], k
