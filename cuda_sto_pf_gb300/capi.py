@@ -21,7 +21,12 @@ MODE_DYNAMICS, MODE_MINIMIZE = 0, 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device out of memory",
           4: "elastic solver did not converge", 5: "zero-mode mass solve rejected the step",
-          6: "non-finite value", 7: "bounded device wait timed out", 8: "unsupported option"}
+          6: "non-finite value", 7: "bounded device wait timed out", 8: "unsupported option",
+          9: "model file read/write failed"}
+
+FNO_WIDTH, FNO_HIDDEN, FNO_IN, FNO_OUT = 32, 64, 8, 3
+# elastic_warm_start_source
+WARM_PREVIOUS, WARM_MODEL_COLD_STARTS, WARM_MODEL_EVERY_STEP, WARM_NONE = 0, 1, 2, 3
 
 
 class Params(Structure):
@@ -68,7 +73,7 @@ class Params(Structure):
         ("ic_vf_init_phi", c_double), ("ic_vf_target_phi", c_double), ("ic_phi_iface_w", c_double),
         ("gamma_Jm2", c_double), ("lambda_sm_m", c_double), ("Vm_alpha_0_phys_m3mol", c_double),
         ("ic_23d_xB_out", c_double), ("ic_phi_seed_radius", c_double), ("minimize_min_pseudo_time", c_double),
-        ("ic_phi_num_seeds", c_int32), ("pad2", c_int32),
+        ("ic_phi_num_seeds", c_int32), ("elastic_warm_start_source", c_int32),
         ("temperature_K", c_double), ("mu0_compound", c_double), ("xB_eq_matrix", c_double),
     ]
 
@@ -110,6 +115,17 @@ class Diag(Structure):
                 ("xB_max", c_double), ("n_in", c_double), ("n_if", c_double)]
 
 
+class FnoConfig(Structure):
+    _fields_ = [("Nx", c_int32), ("Ny", c_int32), ("Nz", c_int32), ("modes", c_int32), ("layers", c_int32),
+                ("pad", c_int32), ("seed", ctypes.c_uint64), ("in_scale", ctypes.c_float * 8),
+                ("out_scale", ctypes.c_float * 3), ("pad2", ctypes.c_float)]
+
+
+class FnoAdam(Structure):
+    _fields_ = [("lr", ctypes.c_float), ("beta1", ctypes.c_float), ("beta2", ctypes.c_float),
+                ("eps", ctypes.c_float), ("weight_decay", ctypes.c_float), ("clip_norm", ctypes.c_float)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/pfgb.h
 EXPORTS = [
     ("pfgb_params_size", c_size_t, []),
@@ -143,6 +159,23 @@ EXPORTS = [
     ("pfgb_fft3d_r2c", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     ("pfgb_fft3d_c2r", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     ("pfgb_fft3d_r2c_noalloc", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    ("pfgb_fno_config_default", None, [POINTER(FnoConfig)]),
+    ("pfgb_fno_create", c_int, [POINTER(FnoConfig), c_int, POINTER(c_void_p)]),
+    ("pfgb_fno_destroy", None, [c_void_p]),
+    ("pfgb_fno_set_stream", c_int, [c_void_p, c_void_p]),
+    ("pfgb_fno_get_config", c_int, [c_void_p, POINTER(FnoConfig)]),
+    ("pfgb_fno_set_scales", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("pfgb_fno_num_params", ctypes.c_longlong, [c_void_p]),
+    ("pfgb_fno_get_params", c_int, [c_void_p, c_void_p, ctypes.c_longlong]),
+    ("pfgb_fno_set_params", c_int, [c_void_p, c_void_p, ctypes.c_longlong]),
+    ("pfgb_fno_forward", c_int, [c_void_p, c_void_p, c_void_p]),
+    ("pfgb_fno_loss_grad", c_int, [c_void_p, c_void_p, c_void_p, c_int, POINTER(c_double)]),
+    ("pfgb_fno_get_grad", c_int, [c_void_p, c_void_p, ctypes.c_longlong]),
+    ("pfgb_fno_adam_step", c_int, [c_void_p, POINTER(FnoAdam)]),
+    ("pfgb_fno_save", c_int, [c_void_p, c_char_p]),
+    ("pfgb_fno_load", c_int, [c_char_p, c_int, c_int, c_int, c_int, POINTER(c_void_p)]),
+    ("pfgb_set_warm_start_model", c_int, [c_void_p, c_void_p]),
+    ("pfgb_elastic_training_pair", c_int, [c_void_p, c_void_p, c_void_p, POINTER(StepStats)]),
 ]
 
 _LIB = None

@@ -39,7 +39,17 @@ template <typename T> PFGB_HD T pf_hp(T p) { T p2 = p * p; return T(30) * p2 * (
 template <typename T> PFGB_HD T pf_g(T p) { return p * p * (T(1) - p) * (T(1) - p); }
 template <typename T> PFGB_HD T pf_gp(T p) { return T(2) * p * (T(1) - p) * (T(1) - T(2) * p); }
 template <typename T> PFGB_HD T clamp01(T v) { return v < T(0) ? T(0) : (v > T(1) ? T(1) : v); }
-template <typename T> PFGB_HD T clamp_eps(T v, T e) { return v < e ? e : (v > T(1) - e ? T(1) - e : v); }
+// upper clamp 1 - e, kept below 1: in float, 1 - e rounds to 1 for e below
+// 2^-25 (the reference's 1e-8 / 1e-12 guards), which would let log(1 - x)
+// and 1 / (1 - x) reach infinity; the largest float below 1 is used then
+template <typename T> PFGB_HD T one_minus_eps(T e) {
+    const T r = T(1) - e;
+    return r < T(1) ? r : T(1) - T(sizeof(T) == 4 ? 5.9604644775390625e-8 : 1.1102230246251565e-16);
+}
+template <typename T> PFGB_HD T clamp_eps(T v, T e) {
+    const T hi = one_minus_eps(e);
+    return v < e ? e : (v > hi ? hi : v);
+}
 
 // ---------------------------------------------------------------------------
 // Thermodynamics.  The model (thermo_utils.h:248-579): SGTE unary Gibbs
@@ -168,7 +178,8 @@ PFGB_HD T sigmoid_clip(T Y, T Yc, T eps) {
     if (Y < -Yc) Y = -Yc;
     T x = sigmoid_raw(Y);
     if (x < eps) x = eps;
-    if (x > T(1) - eps) x = T(1) - eps;
+    const T hi = one_minus_eps(eps);
+    if (x > hi) x = hi;
     return x;
 }
 template <typename T>
@@ -195,3 +206,6 @@ PFGB_HD T logit_clip(T xB, T eps, T Yc) {
 
 void pfgb_set_error(const char *what, cudaError_t e, const char *file, int line);
 void pfgb_set_error_msg(const char *fmt, ...);
+// learned elastic start (fno.cu): device of a model and kernel launches of one forward
+int pfgb_fno_device(const pfgb_fno *f);
+long long pfgb_fno_forward_launches(const pfgb_fno *f);

@@ -87,6 +87,11 @@ struct pfgb_ctx {
     void *Rk[3] = {nullptr, nullptr, nullptr}, *Dk[3] = {nullptr, nullptr, nullptr};   // increment form
     void *Uprev[3] = {nullptr, nullptr, nullptr};   // extrapolated warm start: u of the step before
     int warm_count = 0;
+    // learned start (elastic_warm_start_source 1, 2) and training pairs
+    pfgb_fno *fno = nullptr;
+    float *fno_in = nullptr, *fno_out = nullptr;     // [8][N], [3][N]
+    void *Uhom[3] = {nullptr, nullptr, nullptr};     // u_hom of a training pair's cold start
+    int pair_mode = 0;
     void *mge = nullptr, *mlap = nullptr;
     double lambda_vol = 0.0, V0_target = 0.0, prev_F_total = NAN;
     int min_iter = 0, conv_count = 0, converged_iter = 0, xb_clamp = 0;
@@ -1261,6 +1266,118 @@ __global__ void k_extrapolate_u(cplx_t<TE> *u0, cplx_t<TE> *u1, cplx_t<TE> *u2, 
     }
 }
 
+// ---------------------------------------------------------------------------
+// learned start of the heterogeneous iteration (no reference counterpart;
+// the reference's warm-start point is main_cuda.cu:28792-28870)
+// ---------------------------------------------------------------------------
+// model inputs: phi, eta and the 6 eigenstrain components the cold start's
+// eigenstrain pass sees (OpEigenR2C), as float [8][N]
+template <typename T, typename TE>
+__global__ void k_fno_inputs(DevState<T, TE> d, PhysC c, ElasC<TE> ec, float *__restrict__ out) {
+    const long long N = d.g.N;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N;
+         n += (long long)gridDim.x * blockDim.x) {
+        const T xB = xB_of_Y<T>(c, d.Y[n] + T(d.Yc));
+        const T phi = d.phi_old[n], eta = c.gp ? d.eta_old[n] : T(0);
+        TE e0[6];
+        eigenstrain<T, TE>(c, ec, phi, eta, xB_el(c, xB), c.gp_el != 0, e0);
+        out[n] = (float)phi;
+        out[N + n] = (float)eta;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) out[(2 + a) * N + n] = (float)e0[a];
+    }
+}
+
+// z r2c of three real float fields into E[0..2]
+template <typename TE>
+struct OpReal3In {
+    using Acc = NoAcc;
+    const float *src; cplx_t<TE> *E0, *E1, *E2; long long N; int NzC;
+    __device__ void point(long long cell, const TE *, TE *out, Acc &) const {
+        out[0] = (TE)src[cell];
+        out[1] = (TE)src[N + cell];
+        out[2] = (TE)src[2 * N + cell];
+    }
+    __device__ void load_spec(long long, int, cplx_t<TE> *) const {}
+    __device__ void store_spec(long long row, int k, const cplx_t<TE> *v) const {
+        const long long o = row * NzC + k;
+        E0[o] = v[0]; E1[o] = v[1]; E2[o] = v[2];
+    }
+};
+// z c2r of E[0..2] into three real float fields, times 1/N
+template <typename TE>
+struct OpReal3Out {
+    using Acc = NoAcc;
+    const cplx_t<TE> *E0, *E1, *E2; float *dst; long long N; int NzC; TE invN;
+    __device__ void load_spec(long long row, int k, cplx_t<TE> *v) const {
+        const long long o = row * NzC + k;
+        v[0] = E0[o]; v[1] = E1[o]; v[2] = E2[o];
+    }
+    __device__ void point(long long cell, const TE *in, TE *, Acc &) const {
+        dst[cell] = (float)(in[0] * invN);
+        dst[N + cell] = (float)(in[1] * invN);
+        dst[2 * N + cell] = (float)(in[2] * invN);
+    }
+    __device__ void store_spec(long long, int, const cplx_t<TE> *) const {}
+};
+// x pass of the displacement correction: dealiased like u, u(k = 0) = 0
+template <typename TE>
+struct OpCutU3 {
+    static constexpr bool kInplace = false;
+    KTab kt;
+    __device__ void apply(int i, int j, int k, const cplx_t<TE> *in, cplx_t<TE> *out) const {
+        const bool z = kt.cut(i, j, k) || (i == 0 && j == 0 && k == 0);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) out[a] = z ? mk2<cplx_t<TE>>(TE(0), TE(0)) : in[a];
+    }
+};
+template <typename TE>
+__global__ void k_sub3(cplx_t<TE> *d0, cplx_t<TE> *d1, cplx_t<TE> *d2, const cplx_t<TE> *u0, const cplx_t<TE> *u1,
+                       const cplx_t<TE> *u2, const cplx_t<TE> *h0, const cplx_t<TE> *h1, const cplx_t<TE> *h2,
+                       long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        d0[i] = csub(u0[i], h0[i]);
+        d1[i] = csub(u1[i], h1[i]);
+        d2[i] = csub(u2[i], h2[i]);
+    }
+}
+
+template <typename T, typename TE>
+static pfgb_status launch_fno_inputs(pfgb_ctx *c, float *out) {
+    ProfScope ps(c, {"model_inputs", (double)c->g.N * (3.0 * sizeof(T) + 8.0 * sizeof(float))});
+    k_fno_inputs<T, TE><<<1216, 256, 0, c->stream>>>(dev_state<T, TE>(c), c->pc, elas_consts<TE>(c), out);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    return PFGB_OK;
+}
+
+// U <- U + FFT(model prediction), E[0..2] as scratch
+template <typename T, typename TE>
+static pfgb_status model_start(pfgb_ctx *c) {
+    using T2e = cplx_t<TE>;
+    const double Nf = (double)c->g.N;
+    TRY((launch_fno_inputs<T, TE>(c, c->fno_in)));
+    TRY(pfgb_fno_set_stream(c->fno, c->stream));
+    {
+        ProfScope ps(c, {"model_forward", 0.0});
+        c->launches += pfgb_fno_forward_launches(c->fno) - 1;
+        TRY(pfgb_fno_forward(c->fno, c->fno_in, c->fno_out));
+    }
+    T2e *E0 = (T2e *)c->E[0], *E1 = (T2e *)c->E[1], *E2 = (T2e *)c->E[2];
+    TRY((launch_z<TE, 0, 3>(c, OpReal3In<TE>{c->fno_out, E0, E1, E2, c->g.N, c->g.NzC}, "z_model_r2c",
+                            3.0 * Nf * sizeof(float))));
+    AxisIO<TE, 3, 3> io;
+    for (int i = 0; i < 3; ++i) { io.in[i] = (const T2e *)c->E[i]; io.out[i] = (T2e *)c->E[i]; }
+    TRY((launch_axis<TE, 3, 3, -1, 0>(c, 1, io, OpCopy<TE, 3>{}, "y_fwd3")));
+    TRY((launch_axis<TE, 3, 3, -1, 0>(c, 2, io, OpCutU3<TE>{KTab{c->kx, c->ky, c->kz, c->mx, c->my, c->mz}},
+                                      "x_fwd3")));
+    ProfScope ps(c, {"add_increment", 9.0 * (double)c->g.Nk * sizeof(T2e)});
+    k_add_increment<TE><<<1216, 256, 0, c->stream>>>((T2e *)c->U[0], (T2e *)c->U[1], (T2e *)c->U[2], E0, E1, E2,
+                                                     c->g.Nk);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    return PFGB_OK;
+}
+
 template <typename T, typename TE>
 static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     using T2e = cplx_t<TE>;
@@ -1270,7 +1387,9 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     DevState<T, TE> d = dev_state<T, TE>(c);
     const KTab kt = d.kt;
     const int accel = P.elastic_enabled && (P.elastic_warm_start_enabled || P.elastic_residual_control_enabled);
-    const int warm_used = accel && c->warm_valid;
+    const int src = P.elastic_warm_start_source;
+    const int use_model = accel && !c->pair_mode && c->fno && (src == 2 || (src == 1 && !c->warm_valid));
+    const int warm_used = accel && !c->pair_mode && !use_model && c->warm_valid && src <= 1;
     const double Nf = (double)c->g.N;
     AxisIO<TE, 6, 6> io6;
     for (int i = 0; i < 6; ++i) { io6.in[i] = (const T2e *)c->E[i]; io6.out[i] = (T2e *)c->E[i]; }
@@ -1298,12 +1417,22 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     };
     // increment form: one full update, then delta <- r0 + L delta
     const int inc = accel && P.elastic_increment_form && c->Rk[0] != nullptr;
+    if (accel && (src == 1 || src == 2) && !c->pair_mode && !c->fno && (src == 2 || !c->warm_valid)) {
+        pfgb_set_error_msg("elastic_warm_start_source=%d needs a model (pfgb_set_warm_start_model)", src);
+        return PFGB_ERR_INVALID;
+    }
     if (!warm_used) {
         TRY((launch_z<TE, 0, 6>(c, OpEigenR2C<T, TE>{d, pc, ec}, "z_eigen_r2c", (2.0 + pc.gp) * Nf * sizeof(T))));
         TRY(ypass(-1, "y_fwd6"));
         TRY(green(true, 0, 0));
-    } else {
-        if (c->Uprev[0]) {
+        if (c->pair_mode)
+            for (int i = 0; i < 3; ++i)
+                PFGB_CUDA_TRY(cudaMemcpyAsync(c->Uhom[i], c->U[i], sizeof(T2e) * c->g.Nk, cudaMemcpyDeviceToDevice,
+                                              c->stream));
+    }
+    if (use_model) TRY((model_start<T, TE>(c)));
+    if (warm_used || use_model) {
+        if (warm_used && c->Uprev[0]) {
             // u0 = 2 u^n - u^{n-1} once both exist; keep u^n for the next step
             ProfScope ps(c, {"extrapolate_u", 12.0 * (double)c->g.Nk * sizeof(T2e)});
             k_extrapolate_u<TE><<<1216, 256, 0, c->stream>>>((T2e *)c->U[0], (T2e *)c->U[1], (T2e *)c->U[2],
@@ -1349,7 +1478,7 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     if (st) {
         st->elastic_iterations = iter;
         st->elastic_converged = conv;
-        st->elastic_warm_start_used = warm_used;
+        st->elastic_warm_start_used = use_model ? 2 : warm_used;
         st->elastic_relative_residual = rel;
         st->elastic_iterations_total += iter;
     }
@@ -2150,6 +2279,10 @@ static pfgb_status validate(const pfgb_params *p) {
         pfgb_set_error_msg("elastic_iter_max must be >= 1");
         return PFGB_ERR_INVALID;
     }
+    if (p->elastic_warm_start_source < 0 || p->elastic_warm_start_source > 3) {
+        pfgb_set_error_msg("elastic_warm_start_source must be 0, 1, 2 or 3");
+        return PFGB_ERR_INVALID;
+    }
     return PFGB_OK;
 }
 
@@ -2168,6 +2301,8 @@ static void ctx_free(pfgb_ctx *c) {
     for (int i = 0; i < 6; ++i) f(c->sig[i]);
     for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); f(c->Uprev[i]); }
     f(c->mge); f(c->mlap);
+    f(c->fno_in); f(c->fno_out);
+    for (int i = 0; i < 3; ++i) f(c->Uhom[i]);
     for (auto e : c->pool) cudaEventDestroy(e);
     if (c->hscal) cudaFreeHost(c->hscal);
 }
@@ -2524,6 +2659,78 @@ pfgb_status pfgb_read_elastic(pfgb_ctx *c, float *sigma6, float *strain6) {
     }
     PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return PFGB_OK;
+}
+
+}  // extern "C"
+
+// training pair: cold solve with u_hom kept, then the model inputs and the
+// real-space correction (U - U_hom) / N
+template <typename T>
+static pfgb_status training_pair(pfgb_ctx *c, float *in8, float *tgt3, pfgb_step_stats *st) {
+    using T2e = float2;
+    c->Yc_prev = c->Yc;
+    c->pair_mode = 1;
+    pfgb_status s = elastic_solve<T, float>(c, st);
+    c->pair_mode = 0;
+    TRY(s);
+    T2e *E0 = (T2e *)c->E[0], *E1 = (T2e *)c->E[1], *E2 = (T2e *)c->E[2];
+    {
+        ProfScope ps(c, {"pair_difference", 9.0 * (double)c->g.Nk * sizeof(T2e)});
+        k_sub3<float><<<1216, 256, 0, c->stream>>>(E0, E1, E2, (const T2e *)c->U[0], (const T2e *)c->U[1],
+                                                   (const T2e *)c->U[2], (const T2e *)c->Uhom[0],
+                                                   (const T2e *)c->Uhom[1], (const T2e *)c->Uhom[2], c->g.Nk);
+        PFGB_CUDA_TRY(cudaGetLastError());
+    }
+    AxisIO<float, 3, 3> io;
+    for (int i = 0; i < 3; ++i) { io.in[i] = (const T2e *)c->E[i]; io.out[i] = (T2e *)c->E[i]; }
+    TRY((launch_axis<float, 3, 3, +1, 0>(c, 2, io, OpCopy<float, 3>{}, "x_inv3")));
+    TRY((launch_axis<float, 3, 3, +1, 0>(c, 1, io, OpCopy<float, 3>{}, "y_inv3")));
+    TRY((launch_z<float, 3, 0>(c, OpReal3Out<float>{E0, E1, E2, tgt3, c->g.N, c->g.NzC, (float)(1.0 / (double)c->g.N)},
+                               "z_pair_c2r", 3.0 * (double)c->g.N * sizeof(float))));
+    return launch_fno_inputs<T, float>(c, in8);
+}
+
+extern "C" {
+
+pfgb_status pfgb_set_warm_start_model(pfgb_ctx *c, pfgb_fno *f) {
+    if (!c) return PFGB_ERR_INVALID;
+    if (!f) { c->fno = nullptr; return PFGB_OK; }
+    pfgb_fno_config cfg;
+    TRY(pfgb_fno_get_config(f, &cfg));
+    if (cfg.Nx != c->g.Nx || cfg.Ny != c->g.Ny || cfg.Nz != c->g.Nz || pfgb_fno_device(f) != c->device) {
+        pfgb_set_error_msg("warm-start model is on %dx%dx%d (device %d), the context on %dx%dx%d (device %d)", cfg.Nx,
+                           cfg.Ny, cfg.Nz, pfgb_fno_device(f), c->g.Nx, c->g.Ny, c->g.Nz, c->device);
+        return PFGB_ERR_INVALID;
+    }
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    if (!c->fno_in) {
+        PFGB_CUDA_TRY(cudaMalloc(&c->fno_in, sizeof(float) * 8 * (size_t)c->g.N));
+        PFGB_CUDA_TRY(cudaMalloc(&c->fno_out, sizeof(float) * 3 * (size_t)c->g.N));
+        c->bytes += sizeof(float) * 11 * (size_t)c->g.N;
+    }
+    c->fno = f;
+    return PFGB_OK;
+}
+
+pfgb_status pfgb_elastic_training_pair(pfgb_ctx *c, float *d_in8, float *d_target3, pfgb_step_stats *st) {
+    if (!c || !d_in8 || !d_target3) return PFGB_ERR_INVALID;
+    const pfgb_params &P = c->p;
+    if (!c->loaded) { pfgb_set_error_msg("training pair: no fields loaded"); return PFGB_ERR_INVALID; }
+    if (!P.elastic_enabled || !P.elastic_warm_start_enabled || !P.elastic_residual_control_enabled) {
+        pfgb_set_error_msg("training pair: needs elastic_enabled, elastic_warm_start_enabled and "
+                           "elastic_residual_control_enabled");
+        return PFGB_ERR_UNSUPPORTED;
+    }
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    if (!c->Uhom[0]) {
+        for (int i = 0; i < 3; ++i) PFGB_CUDA_TRY(cudaMalloc(&c->Uhom[i], sizeof(float2) * (size_t)c->g.Nk));
+        c->bytes += 3 * sizeof(float2) * (size_t)c->g.Nk;
+    }
+    pfgb_step_stats local{};
+    pfgb_step_stats *sp = st ? st : &local;
+    sp->elastic_iterations_total = 0;
+    return c->p.precision == PFGB_PREC_FP64 ? training_pair<double>(c, d_in8, d_target3, sp)
+                                            : training_pair<float>(c, d_in8, d_target3, sp);
 }
 
 pfgb_status pfgb_read_displacement_k(pfgb_ctx *c, float *u3) {

@@ -80,6 +80,21 @@ class Solver:
                   "pfgb_minimize")
         return st
 
+    def set_warm_start_model(self, model) -> None:
+        """Attach a ``fno.WarmStartModel`` (None detaches); it is used when
+        elastic_warm_start_source is 1 or 2."""
+        self._model = model
+        self._chk(self.lib.pfgb_set_warm_start_model(self.ctx, model.handle if model is not None else None),
+                  "pfgb_set_warm_start_model")
+
+    def training_pair(self, d_in8, d_target3) -> capi.StepStats:
+        """Cold elastic solve on the current fields; writes the model inputs
+        [8][N] and the correction u - u_hom [3][N] into device float32 buffers."""
+        st = capi.StepStats()
+        self._chk(self.lib.pfgb_elastic_training_pair(self.ctx, _ptr(d_in8), _ptr(d_target3), ctypes.byref(st)),
+                  "pfgb_elastic_training_pair")
+        return st
+
     def step_nostats(self, nsteps: int = 1) -> None:
         self._chk(self.lib.pfgb_step(self.ctx, nsteps, None), "pfgb_step")
 

@@ -26,6 +26,11 @@
  *                             gpu_reduce_min_max, cuda_kernels.cu:5609-5942
  *   pfgb_fft3d_*           <- cufftExecD2Z/Z2D/R2C/C2R call sites,
  *                             main_cuda.cu:28163-28173 (own kernels, no cuFFT)
+ *   pfgb_fno_*, pfgb_set_warm_start_model, pfgb_elastic_training_pair
+ *                          <- no counterpart: a learned start for the
+ *                             heterogeneous elastic iteration at the
+ *                             reference's warm-start point,
+ *                             main_cuda.cu:28792-28870
  *
  * Layouts: real fields are C-order [Nx][Ny][Nz] (z fastest, idx=(i*Ny+j)*Nz+k,
  * io_vtk_cuda.h:104-108); spectral fields are the half spectrum
@@ -54,7 +59,8 @@ typedef enum pfgb_status {
     PFGB_ERR_ZERO_MODE = 5,      /* zero-mode mass solve rejected the step */
     PFGB_ERR_NONFINITE = 6,      /* NaN/Inf residual or field              */
     PFGB_ERR_TIMEOUT = 7,        /* a bounded device wait ran out          */
-    PFGB_ERR_UNSUPPORTED = 8     /* option outside the implemented path    */
+    PFGB_ERR_UNSUPPORTED = 8,    /* option outside the implemented path    */
+    PFGB_ERR_IO = 9              /* a model file could not be read/written */
 } pfgb_status;
 
 /* field / transform precision */
@@ -160,7 +166,15 @@ typedef struct pfgb_params {
     double ic_phi_seed_radius;
     double minimize_min_pseudo_time;
     int32_t ic_phi_num_seeds;
-    int32_t pad2;
+    /* starting point of each heterogeneous elastic solve (no counterpart
+       key in the reference, which always uses 0):
+       0 = the previous step's displacement once one exists (reference);
+       1 = the attached model's prediction when no previous solution exists
+           (first step, after a load), the previous step's otherwise;
+       2 = the model's prediction on every step;
+       3 = the homogeneous solution on every step (cold).
+       1 and 2 need pfgb_set_warm_start_model. */
+    int32_t elastic_warm_start_source;
     /* derived by pfgb_params_finalize (pfparams_refresh_thermo) */
     double temperature_K;
     double mu0_compound;
@@ -362,6 +376,82 @@ pfgb_status pfgb_fft3d_c2r(int precision, int Nx, int Ny, int Nz,
 #define PFGB_NOALLOC_SCRATCH_BYTES 32768
 pfgb_status pfgb_fft3d_r2c_noalloc(int precision, int Nx, int Ny, int Nz,
                                    const void *d_in, void *d_out, void *cuda_stream);
+
+/* --- learned start of the heterogeneous elastic iteration ------------- */
+/* No counterpart in the reference, which starts each solve from the
+ * previous step's displacement (main_cuda.cu:28792-28870).  A Fourier
+ * neural operator (FNO-3d, Li et al. 2021: lift 8 -> 32, `layers` spectral
+ * layers of width 32 keeping `modes` modes per axis, GELU, projection
+ * 32 -> 64 -> 3) maps the 8 input channels
+ *     phi, eta, eps0_xx, eps0_yy, eps0_zz, eps0_yz, eps0_xz, eps0_xy
+ * (the eigenstrain field the elastic solve sees) to the heterogeneous
+ * displacement correction u - u_hom (3 channels, the real-space
+ * displacement in grid units of the solver's u).  The solver adds the
+ * prediction to the homogeneous solution and then runs the plain fixed
+ * point to its residual tolerance: the model moves the starting point
+ * only.  Weights are bfloat16 (float32 master copy for training),
+ * arithmetic float32.  All tensors are DEVICE float32, channel-major
+ * [C][Nx][Ny][Nz]. */
+#define PFGB_FNO_WIDTH 32
+#define PFGB_FNO_HIDDEN 64
+#define PFGB_FNO_IN 8
+#define PFGB_FNO_OUT 3
+typedef struct pfgb_fno pfgb_fno;
+typedef struct pfgb_fno_config {
+    int32_t Nx, Ny, Nz;
+    int32_t modes;            /* retained modes per axis; 2*modes <= Nx, Ny, Nz */
+    int32_t layers;           /* spectral layers                              */
+    int32_t pad;
+    uint64_t seed;            /* initial weights                              */
+    float in_scale[PFGB_FNO_IN];    /* inputs are multiplied by these first  */
+    float out_scale[PFGB_FNO_OUT];  /* outputs are multiplied by these last  */
+    float pad2;
+} pfgb_fno_config;
+typedef struct pfgb_fno_adam {
+    float lr, beta1, beta2, eps;
+    float weight_decay;       /* decoupled (AdamW)                            */
+    float clip_norm;          /* global gradient-norm clip; 0 = off           */
+} pfgb_fno_adam;
+
+/* Defaults: 128^3, 12 modes, 4 layers, unit scales. */
+void pfgb_fno_config_default(pfgb_fno_config *cfg);
+pfgb_status pfgb_fno_create(const pfgb_fno_config *cfg, int device, pfgb_fno **out);
+void pfgb_fno_destroy(pfgb_fno *fno);
+pfgb_status pfgb_fno_set_stream(pfgb_fno *fno, void *cuda_stream);
+pfgb_status pfgb_fno_get_config(const pfgb_fno *fno, pfgb_fno_config *cfg);
+pfgb_status pfgb_fno_set_scales(pfgb_fno *fno, const float *in_scale, const float *out_scale);
+/* Flat float32 parameter vector, in order: P[32][8] p[32], per layer
+ * W[32][32] b[32] R[32 in][32 out][4 modes^3][re,im], then Q1[64][32]
+ * q1[64] Q2[3][64] q2[3].  Mode index = (jx*2m + jy)*m + kz with jx, jy
+ * in [0, 2m) (j < m: wavenumber j, else N - 2m + j) and kz in [0, m). */
+long long pfgb_fno_num_params(const pfgb_fno *fno);
+pfgb_status pfgb_fno_get_params(pfgb_fno *fno, float *host, long long n);
+pfgb_status pfgb_fno_set_params(pfgb_fno *fno, const float *host, long long n);
+/* d_in [8][N] -> d_out [3][N] on the model's stream. */
+pfgb_status pfgb_fno_forward(pfgb_fno *fno, const float *d_in, float *d_out);
+/* Forward and backward of the loss sum (y - t)^2 / sum t^2; the gradient
+ * goes to the model's gradient buffer (added to it when accumulate != 0).
+ * loss may be NULL (no synchronisation then). */
+pfgb_status pfgb_fno_loss_grad(pfgb_fno *fno, const float *d_in, const float *d_target,
+                               int accumulate, double *loss);
+pfgb_status pfgb_fno_get_grad(pfgb_fno *fno, float *host, long long n);
+pfgb_status pfgb_fno_adam_step(pfgb_fno *fno, const pfgb_fno_adam *opt);
+/* Model file: header, scales and the float32 parameter vector.  load may
+ * place the model on another grid (Nx, Ny, Nz > 0) with the same weights. */
+pfgb_status pfgb_fno_save(pfgb_fno *fno, const char *path);
+pfgb_status pfgb_fno_load(const char *path, int Nx, int Ny, int Nz, int device, pfgb_fno **out);
+
+/* Attach (or with NULL detach) the model used by elastic_warm_start_source
+ * 1 and 2.  The model must be on the context's grid and device; it stays
+ * owned by the caller and must outlive its use by the context. */
+pfgb_status pfgb_set_warm_start_model(pfgb_ctx *ctx, pfgb_fno *fno);
+/* Training pair from the context's current fields: one cold heterogeneous
+ * elastic solve to the residual tolerance, then d_in8 [8][N] = the model
+ * inputs and d_target3 [3][N] = u - u_hom in real space (DEVICE float32).
+ * The fields are not advanced; the solution becomes the context's warm
+ * state, as after a step.  stats (may be NULL) gets the iteration count. */
+pfgb_status pfgb_elastic_training_pair(pfgb_ctx *ctx, float *d_in8, float *d_target3,
+                                       pfgb_step_stats *stats);
 
 #ifdef __cplusplus
 }
