@@ -51,7 +51,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain-fp64", action="store_true")
     ap.add_argument("--profile-json", default="")
-    ap.add_argument("--workload", default="c2", choices=["c2", "sweep"],
+    ap.add_argument("--fno-n", type=int, default=128)
+    ap.add_argument("--fno-base", type=int, default=128, help="distinct generated microstructures")
+    ap.add_argument("--fno-pairs", type=int, default=1024, help="training pairs (base x cube symmetries)")
+    ap.add_argument("--fno-train-steps", type=int, default=6000)
+    ap.add_argument("--fno-eval-steps", type=int, default=300)
+    ap.add_argument("--workload", default="c2", choices=["c2", "sweep", "fno", "fno-step"],
                     help="c2: the 246^3 dynamics step (default); sweep: the batched minimize sweep")
     ap.add_argument("--sweep-cases", type=int, default=48)
     ap.add_argument("--sweep-iters", type=int, default=500)
@@ -498,10 +503,184 @@ def run_sweep(args):
     print(json.dumps(line), flush=True)
 
 
+def _fno_micro(args):
+    """One seeded C1-like microstructure (5-30 ellipsoids, GP-zone eta seeds)
+    as float32 arrays; runs in a worker process."""
+    n, seed, w = args
+    from cuda_sto_pf_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    count = int(rng.integers(5, 31))
+    m = workloads.ellipsoid_population(n, count=count, eta_sites=max(1, count // 3), w=w, seed=seed)
+    return tuple(m[k].astype(np.float32) for k in ("phi", "xB", "eta"))
+
+
+def _cube_symmetry(fields, k):
+    """The k-th of the 48 symmetries of the cube (axis permutation + flips)."""
+    import itertools
+    perm = list(itertools.permutations((0, 1, 2)))[k % 6]
+    flips = [a for a in range(3) if (k // 6) >> a & 1]
+    return tuple(np.ascontiguousarray(np.flip(np.transpose(f, perm), axis=flips) if flips else np.transpose(f, perm))
+                 for f in fields)
+
+
+def run_fno(args):
+    """Learned elastic start at 128^3: a 4-layer FNO (width 32, 12 modes,
+    bfloat16 weights) fitted on pairs from the solver's own cold elastic
+    solves of C1-like microstructures (5-30 particles, cube-symmetry copies
+    of the generated ones), then dynamics steps of held-out microstructures
+    started cold, from the previous step (the reference's warm start) and
+    from the model, all to the same residual tolerance."""
+    import multiprocessing as mp
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    n = args.fno_n
+    # microstructures first, in spawned workers, before any GPU call
+    nbase = args.fno_base
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        base = pool.map(_fno_micro, [(n, 5000 + i, 2.5) for i in range(nbase + 2)])
+    import torch
+    from cuda_sto_pf_gb300 import capi, fno
+    from cuda_sto_pf_gb300.solver import Solver
+    lib = capi.load(build_if_missing=True)
+    torch.cuda.set_device(local)
+    p = make_params(capi, n, "fp32", args.elastic_tol)
+    N = n ** 3
+
+    def prepared(fields):
+        phi, xB, eta = (np.ascontiguousarray(f, dtype=np.float64) for f in fields)
+        assert lib.pfgb_prepare_raw_fields(ctypes.byref(p), 0.07, phi.ctypes.data, xB.ctypes.data,
+                                           eta.ctypes.data, None, phi.size) == 0
+        return phi, xB, eta
+
+    P = args.fno_pairs
+    inputs = torch.empty((P, 8, N), device="cuda")
+    targets = torch.empty((P, 3, N), device="cuda")
+    t0 = time.perf_counter()
+    cold_its = []
+    with Solver(p, device=local) as s:
+        for i in range(P):
+            s.load(*prepared(_cube_symmetry(base[i % nbase], i // nbase)))
+            st = s.training_pair(inputs[i], targets[i])
+            cold_its.append(st.elastic_iterations)
+        s.sync()
+    t_pairs = time.perf_counter() - t0
+    hold = P // 16
+    in_scale, out_scale = fno.channel_scales(inputs[hold:], targets[hold:])
+    model = fno.WarmStartModel((n, n, n), modes=12, layers=4, in_scale=in_scale, out_scale=out_scale, device=local)
+    t0 = time.perf_counter()
+    losses = fno.train(model, inputs[hold:], targets[hold:], steps=args.fno_train_steps, lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    # held-out relative error of the prediction
+    pred = torch.empty((3, N), device="cuda")
+    errs = []
+    for i in range(hold):
+        model.forward(inputs[i], pred)
+        errs.append(float((pred - targets[i]).norm() / targets[i].norm()))
+    fwd_ms = []
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        model.forward(inputs[0], pred)
+        b.record()
+        torch.cuda.synchronize()
+        fwd_ms.append(a.elapsed_time(b))
+    del inputs, targets
+    torch.cuda.empty_cache()
+    # dynamics from the two held-out generated microstructures
+    modes = {"cold": 3, "previous_step": 0, "model_every_step": 2, "model_cold_start_then_previous": 1}
+    res = {}
+    for name, src in modes.items():
+        pm = make_params(capi, n, "fp32", args.elastic_tol)
+        pm.elastic_warm_start_source = src
+        its, ms, first, err = [], [], [], None
+        for k in range(2):
+            with Solver(pm, device=local) as s:
+                s.set_warm_start_model(model)
+                s.load(*prepared(base[nbase + k]))
+                try:
+                    for j in range(args.fno_eval_steps):
+                        torch.cuda.synchronize()
+                        t1 = time.perf_counter()
+                        st = s.step(1)
+                        torch.cuda.synchronize()
+                        ms.append(1e3 * (time.perf_counter() - t1))
+                        its.append(st.elastic_iterations)
+                        if j == 0:
+                            first.append(st.elastic_iterations)
+                except capi.PfgbError as e:
+                    err = str(e)
+                s.set_warm_start_model(None)
+        res[name] = {"iterations_per_step": float(np.mean(its)) if its else None,
+                     "ms_per_step": float(np.mean(ms)) if ms else None,
+                     "first_step_iterations": first, "steps": len(its), "error": err}
+    model.close()
+    line = {"metric": "elastic iterations per step (learned start)",
+            "value": res["model_every_step"]["iterations_per_step"], "unit": "iterations/step",
+            "higher_is_better": False, "n_gpus": 1, "steps": args.fno_eval_steps, "dtype": "f32",
+            "data": "synthetic (seeded C1-like microstructures, cube-symmetry copies)",
+            "config": {"workload": f"{n}^3 gp_zone dynamics, heterogeneous elasticity, zero mode, elastic tol "
+                                   f"{args.elastic_tol:g}; FNO width 32, 12 modes, 4 layers, bf16 weights",
+                       "pairs": P, "held_out_pairs": hold, "distinct_microstructures": nbase,
+                       "train_steps": args.fno_train_steps},
+            "starts": res,
+            "model": {"held_out_rel_l2": float(np.mean(errs)), "forward_ms": float(np.median(fwd_ms)),
+                      "train_loss_first_100": float(np.mean(losses[:100])),
+                      "train_loss_last_100": float(np.mean(losses[-100:])),
+                      "pair_cold_iterations_mean": float(np.mean(cold_its)),
+                      "seconds_pairs": t_pairs, "seconds_train": t_train}}
+    print(json.dumps(line), flush=True)
+
+
+def run_fno_step(args):
+    """Cost of the learned start's kernels at --fno-n: one forward (the
+    solver's use) and one training step (forward, backward, Adam) on seeded
+    random inputs, CUDA-event timed after --warmup repeats."""
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    import torch
+    from cuda_sto_pf_gb300 import capi, fno
+    capi.load(build_if_missing=True)
+    torch.cuda.set_device(local)
+    n = args.fno_n
+    N = n ** 3
+    g = torch.Generator(device="cuda").manual_seed(1)
+    x = torch.randn((8, N), device="cuda", generator=g)
+    t = torch.randn((3, N), device="cuda", generator=g)
+    y = torch.empty((3, N), device="cuda")
+    model = fno.WarmStartModel((n, n, n), modes=12, layers=4, device=local)
+
+    def timed(fn, reps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    fwd = timed(lambda: model.forward(x, y), args.steps)
+    trn = timed(lambda: (model.loss_grad(x, t, want_loss=False), model.adam_step(1e-5)), max(1, args.steps // 2))
+    model.close()
+    print(json.dumps({"metric": "learned-start model cost", "grid": n, "forward_ms": fwd, "train_step_ms": trn,
+                      "steps": args.steps, "warmup": args.warmup}), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "sweep":
         run_sweep(args)
+        return
+    if args.workload == "fno":
+        run_fno(args)
+        return
+    if args.workload == "fno-step":
+        run_fno_step(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -133,8 +133,14 @@ def channel_scales(inputs, targets):
     units."""
     import torch
     with torch.no_grad():
-        i_rms = inputs.double().pow(2).mean(dim=(0, 2)).sqrt().cpu().numpy()
-        t_rms = targets.double().pow(2).mean(dim=(0, 2)).sqrt().cpu().numpy()
+        si = torch.zeros(inputs.shape[1], dtype=torch.float64, device=inputs.device)
+        st = torch.zeros(targets.shape[1], dtype=torch.float64, device=targets.device)
+        for i in range(inputs.shape[0]):   # one pair at a time: no full-size float64 copy
+            si += inputs[i].double().pow(2).sum(dim=1)
+            st += targets[i].double().pow(2).sum(dim=1)
+        cnt = float(inputs.shape[0] * inputs.shape[2])
+        i_rms = (si / cnt).sqrt().cpu().numpy()
+        t_rms = (st / cnt).sqrt().cpu().numpy()
     in_scale = np.where(i_rms > 0, 1.0 / np.maximum(i_rms, 1e-30), 1.0)
     out_scale = np.where(t_rms > 0, t_rms, 1.0)
     return in_scale, out_scale

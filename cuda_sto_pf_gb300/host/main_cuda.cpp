@@ -45,6 +45,8 @@ struct Cli {
     double h_scale = NAN;
     int precision = PFGB_PREC_FP64;
     int device = 0;
+    std::string warm_model;   // learned start of the elastic iteration (no reference counterpart)
+    int warm_source = -1;
     // minimize
     bool min_full = false;
     int min_max_iter = -1, min_conv_steps = -1, min_post_iters = -1;
@@ -82,7 +84,10 @@ void usage() {
            "  --disable-Y-rhs-gamma-term\n"
            "  --Y-rhs-term-h-scale <s>\n"
            "  --precision fp64|fp32           field precision (default fp64, as the reference)\n"
-           "  --device <n>                    CUDA device ordinal\n");
+           "  --device <n>                    CUDA device ordinal\n"
+           "  --elastic-warm-start-model <f>  model file (pfgb_fno_save) for the elastic start\n"
+           "  --elastic-warm-start-source <n> 0 previous step (default), 1 model at cold starts,\n"
+           "                                  2 model every step, 3 cold every step\n");
 }
 
 // "--name value" or "--name=value"; advances i past a separate value
@@ -154,6 +159,10 @@ Cli parse(int argc, char **argv) {
             else bad(a, v);
         }
         else if ((v = flag_value(argc, argv, &i, "--device"))) { if (!to_int(v, &c.device)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--elastic-warm-start-model"))) c.warm_model = v;
+        else if ((v = flag_value(argc, argv, &i, "--elastic-warm-start-source"))) {
+            if (!to_int(v, &c.warm_source) || c.warm_source < 0 || c.warm_source > 3) bad(a, v);
+        }
         else if (!strcmp(a, "--minimize-full-model")) c.min_full = true;
         else if ((v = flag_value(argc, argv, &i, "--minimize-max-iter"))) { if (!to_int(v, &c.min_max_iter)) bad(a, v); }
         else if ((v = flag_value(argc, argv, &i, "--minimize-dt"))) { if (!to_double(v, &c.min_dt)) bad(a, v); }
@@ -365,6 +374,13 @@ int main(int argc, char **argv) {
         fprintf(stderr, "[fatal] nsteps >= 0, out_every > 0 and csv_out_every > 0 are required\n");
         return 2;
     }
+    if (c.warm_source >= 0) P.elastic_warm_start_source = c.warm_source;
+    else if (!c.warm_model.empty()) P.elastic_warm_start_source = 1;
+    if ((P.elastic_warm_start_source == 1 || P.elastic_warm_start_source == 2) && c.warm_model.empty()) {
+        fprintf(stderr, "[fatal] --elastic-warm-start-source %d needs --elastic-warm-start-model\n",
+                P.elastic_warm_start_source);
+        return 2;
+    }
     if ((st = pfgb_params_finalize(&P)) != PFGB_OK) return fail(st, "pfgb_params_finalize");
 
     // ---- initial fields ---------------------------------------------------
@@ -427,8 +443,19 @@ int main(int argc, char **argv) {
     printf("output_dir=%s\ncase_output_dir=%s\n", out_dir.c_str(), case_dir.c_str());
 
     // ---- solver -----------------------------------------------------------
+    struct ModelHolder {   // released after the context (declared first)
+        pfgb_fno *m = nullptr;
+        ~ModelHolder() { if (m) pfgb_fno_destroy(m); }
+    } model;
     pfgb_ctx *ctx = nullptr;
     if ((st = pfgb_create(&P, c.device, &ctx)) != PFGB_OK) return fail(st, "pfgb_create");
+    if (!c.warm_model.empty()) {
+        if ((st = pfgb_fno_load(c.warm_model.c_str(), P.Nx, P.Ny, P.Nz, c.device, &model.m)) != PFGB_OK ||
+            (st = pfgb_set_warm_start_model(ctx, model.m)) != PFGB_OK) {
+            pfgb_destroy(ctx);
+            return fail(st, "--elastic-warm-start-model");
+        }
+    }
     st = pfgb_load_fields(ctx, phi.data(), xB.data(), eta.empty() ? nullptr : eta.data(),
                           dYdt.empty() ? nullptr : dYdt.data());
     if (st != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_load_fields"); }

@@ -46,6 +46,10 @@ def test_cli_rejects_bad_inputs(capi, tmp_path):
     r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf, "--init-mode", "raw_fields",
                     "--init-phi-raw", str(bad), "--init-xB-raw", str(bad)], tmp_path)
     assert r.returncode == 2 and "expected" in r.stderr
+    # a model start without a model file
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf,
+                    "--elastic-warm-start-source", "2"], tmp_path)
+    assert r.returncode == 2 and "--elastic-warm-start-model" in r.stderr
     # malformed parameter file
     pbad = tmp_path / "bad.params"
     pbad.write_text(open(pf).read() + "\nW=abc\n")
@@ -133,3 +137,28 @@ def test_cli_minimize_run(capi, tmp_path):
     for f in ("phi_init_raw_fields_relax.vtk", "xB_init_raw_fields_relax.vtk", "phi_final_raw_fields_relax.vtk",
               "xB_final_raw_fields_relax.vtk", "vf_precip_vs_time_raw_fields_relax.csv", "elastic_solver_trace.csv"):
         assert (case / f).exists(), f
+
+
+@pytest.mark.gpu
+def test_cli_learned_start(capi, tmp_path):
+    """--elastic-warm-start-model: the trace marks model-started solves (2)."""
+    from cuda_sto_pf_gb300 import workloads
+    from cuda_sto_pf_gb300.fno import WarmStartModel
+    n, steps = 16, 3
+    w = workloads.single_sphere(n=n, radius=5.0)
+    w["phi"].tofile(tmp_path / "phi.raw")
+    w["xB"].tofile(tmp_path / "xB.raw")
+    with WarmStartModel((n, n, n), modes=4, layers=2, out_scale=[1e-3] * 3) as m:
+        m.save(str(tmp_path / "start.pfgbfno"))
+    pf = os.path.join(GOLDEN, "c2.params")
+    r = _run(capi, [str(n), str(n), str(n), "0.01", str(steps), "10", "1", "1", "--pf-param-file", pf,
+                    "--init-mode", "raw_fields", "--init-phi-raw", str(tmp_path / "phi.raw"),
+                    "--init-xB-raw", str(tmp_path / "xB.raw"), "--precision", "fp32",
+                    "--elastic-warm-start-model", str(tmp_path / "start.pfgbfno"),
+                    "--elastic-warm-start-source", "2"],
+             tmp_path, env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "R")})
+    assert r.returncode == 0, r.stderr
+    run = os.listdir(tmp_path / "R")[0]
+    rows = (tmp_path / "R" / run / "raw_fields_relax" / "elastic_solver_trace.csv").read_text().strip().split("\n")
+    assert len(rows) == steps + 1
+    assert all(row.split(",")[1] == "2" for row in rows[1:])
