@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain-fp64", action="store_true")
+    ap.add_argument("--no-chebyshev", action="store_true", help="the reference's plain elastic iteration")
     ap.add_argument("--profile-json", default="")
     ap.add_argument("--fno-n", type=int, default=128)
     ap.add_argument("--fno-base", type=int, default=128, help="distinct generated microstructures")
@@ -71,7 +72,13 @@ def dist_env():
     return ws, rank, local
 
 
-def make_params(capi, n, precision, tol, shape=None):
+# elastic iteration of our arm: Chebyshev semi-iteration of the increment
+# (--no-chebyshev: the reference's plain iteration); the CPU reference arm
+# and the plain FP64 comparison always run the reference's iteration
+CHEBYSHEV = 1
+
+
+def make_params(capi, n, precision, tol, shape=None, chebyshev=None):
     p = capi.load_params_file(PARAMS)
     p.Nx, p.Ny, p.Nz = shape if shape else (n, n, n)
     p.model_mode = capi.MODEL_GP_ZONE
@@ -81,6 +88,7 @@ def make_params(capi, n, precision, tol, shape=None):
     # with FP32 elastic fields the residual levels off near 8e-8 at 246^3, so
     # a 1e-8 tolerance runs to elastic_iter_max; the step continues there
     p.elastic_fail_on_nonconvergence = 0
+    p.elastic_chebyshev = CHEBYSHEV if chebyshev is None else chebyshev
     capi.finalize(p)
     return p
 
@@ -179,7 +187,7 @@ def cpu_oracle_rate(capi, n, precision, tol, threads=None, steps=1):
     warm-up step (cold elastic start) + `steps` timed steps at n^3."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     from oracle_py import Oracle
-    p = make_params(capi, n, precision, tol)
+    p = make_params(capi, n, precision, tol, chebyshev=0)
     phi, xB, eta, _, _ = make_fields(capi, p, n)
     threads = threads or os.cpu_count() or 1
     o = Oracle(p, threads=threads)
@@ -205,7 +213,7 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     from oracle_py import Oracle
     n = args.cpu_sample_n
-    p = make_params(capi, n, args.precision, args.elastic_tol)
+    p = make_params(capi, n, args.precision, args.elastic_tol, chebyshev=0)
     phi, xB, eta, _, _ = make_fields(capi, p, n)
     o = Oracle(p, threads=threads)
     o.load(phi, xB, eta)
@@ -237,11 +245,11 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def short_run(capi, Solver, n, shape, fields, dev, stream, prec, tol, nsteps, warm, read=True):
+def short_run(capi, Solver, n, shape, fields, dev, stream, prec, tol, nsteps, warm, read=True, chebyshev=None):
     """nsteps steps from the initial fields; CUDA-event time per step over
     the last nsteps - warm; optionally the final fields and stress."""
     import torch
-    p = make_params(capi, n, prec, tol, shape)
+    p = make_params(capi, n, prec, tol, shape, chebyshev=chebyshev)
     s = Solver(p, device=dev)
     s.set_stream(stream.cuda_stream)
     s.load(*fields)
@@ -265,7 +273,8 @@ def compare_plain_fp64(args, capi, Solver, n, shape, fields, dev, stream, nsteps
     initial fields on the same GPU: time per step of each over the last
     nsteps - warm steps, and the relative L2 field error of the chosen path
     against FP64 after nsteps steps."""
-    res = {prec: short_run(capi, Solver, n, shape, fields, dev, stream, prec, args.elastic_tol, nsteps, warm)
+    res = {prec: short_run(capi, Solver, n, shape, fields, dev, stream, prec, args.elastic_tol, nsteps, warm,
+                           chebyshev=None if prec == "fp32" else 0)
            for prec in ("fp32", "fp64")}
     f32, s32, ms32, it32 = res["fp32"]
     f64, s64, ms64, it64 = res["fp64"]
@@ -278,8 +287,9 @@ def compare_plain_fp64(args, capi, Solver, n, shape, fields, dev, stream, nsteps
                                 "elastic_iters_per_step": sum(it32[warm:]) / max(1, nsteps - warm)},
             "speedup_vs_plain_fp64": ms64 / ms32,
             "field_rel_l2_vs_fp64": err, "after_steps": nsteps,
-            "what": f"both forms from the same initial fields, {nsteps} steps; time over the last "
-                    f"{nsteps - warm}; relative L2 error of phi, xB, eta and the 6 stress components"}
+            "what": f"the chosen path and the plain FP64 form with the reference's elastic iteration, from the "
+                    f"same initial fields, {nsteps} steps; time over the last {nsteps - warm}; relative L2 error "
+                    f"of phi, xB, eta and the 6 stress components"}
 
 
 def run_ours(args):
@@ -427,6 +437,8 @@ def run_ours(args):
                                        f"heterogeneous elasticity, zero mode",
                            "grid": n, "fields": args.precision, "elastic": "fp32",
                            "elastic_tol": args.elastic_tol, "dt": p.dt,
+                           "elastic_iteration": "chebyshev semi-iteration of the increment" if CHEBYSHEV
+                           else "plain (the reference's)",
                            "l2": "inputs larger than L2 (working set > 1 GB at 246^3)",
                            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
                 "elastic_iters_per_step": sum(iters) / max(1, len(iters)),
@@ -672,7 +684,9 @@ def run_fno_step(args):
 
 
 def main():
+    global CHEBYSHEV
     args = parse()
+    CHEBYSHEV = 0 if args.no_chebyshev else 1
     if args.workload == "sweep":
         run_sweep(args)
         return

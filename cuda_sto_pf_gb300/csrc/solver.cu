@@ -85,6 +85,11 @@ struct pfgb_ctx {
     // minimize state (mode = minimize)
     void *sig[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     void *Rk[3] = {nullptr, nullptr, nullptr}, *Dk[3] = {nullptr, nullptr, nullptr};   // increment form
+    // Chebyshev semi-iteration of the increment: the previous iterate, the
+    // relaxation gam = 2 / (2 - a - b) and sig = (b - a) / (2 - a - b) from
+    // the spectral bounds [a, b] of the linear part; rho of the next update
+    void *Dkm[3] = {nullptr, nullptr, nullptr};
+    double cheb_gam = 1.0, cheb_sig = 0.0, cheb_rho = 1.0;
     void *Uprev[3] = {nullptr, nullptr, nullptr};   // extrapolated warm start: u of the step before
     int warm_count = 0;
     // learned start (elastic_warm_start_source 1, 2) and training pairs
@@ -746,6 +751,8 @@ struct GreenArgs {
     const cplx_t<TE> *tw;
     cplx_t<TE> *E[6], *U[3];
     cplx_t<TE> *R[3], *D[3];   // increment form: r0 and delta
+    cplx_t<TE> *Dm[3];         // Chebyshev: the iterate before delta (null: plain update)
+    TE gam, rho;
     double *partials;
     int resid;
     int mode;                  // 0 u <- Phi(u); 1 first increment step; 2 delta <- r0 + L delta
@@ -772,17 +779,28 @@ __device__ __forceinline__ void green_update(const GreenArgs<TE> &A, long long o
             out[c] = u[c];
         }
     } else if (A.mode == 1) {
+        // r0 = u1 - u0; delta_1 = r0 (Chebyshev: the relaxed gam r0, with the
+        // iterate before it, delta_0 = 0)
+        const bool cheb = A.Dm[0] != nullptr;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const T2 u0 = A.U[c][o];
             const T2 r = mk2<T2>(u[c].x - u0.x, u[c].y - u0.y);
             A.R[c][o] = r;
-            A.D[c][o] = r;
+            const T2 x1 = cheb ? mk2<T2>(A.gam * r.x, A.gam * r.y) : r;
+            A.D[c][o] = x1;
+            if (cheb) A.Dm[c][o] = mk2<T2>(TE(0), TE(0));
             ld_ += r.x * r.x + r.y * r.y;
             lr += u[c].x * u[c].x + u[c].y * u[c].y;
-            out[c] = r;
+            out[c] = x1;
         }
     } else {
+        // g = r0 + L delta; the residual |g - delta| / |u0 + g| is the
+        // reference's |u_new - u_old| / |u_new| for a plain step from delta.
+        // Plain: delta <- g.  Chebyshev: y = delta + gam (g - delta),
+        // delta_new = delta_prev + rho (y - delta_prev), written over delta_prev
+        // (the host swaps the two buffers).
+        const bool cheb = A.Dm[0] != nullptr;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const T2 r0 = A.R[c][o], d = A.D[c][o], u0 = A.U[c][o];
@@ -791,8 +809,16 @@ __device__ __forceinline__ void green_update(const GreenArgs<TE> &A, long long o
             const TE ur = u0.x + dn.x, ui = u0.y + dn.y;
             ld_ += dr * dr + di * di;
             lr += ur * ur + ui * ui;
-            A.D[c][o] = dn;
-            out[c] = dn;
+            if (cheb) {
+                const T2 xm = A.Dm[c][o];
+                const TE yr = d.x + A.gam * dr, yi = d.y + A.gam * di;
+                const T2 xn = mk2<T2>(xm.x + A.rho * (yr - xm.x), xm.y + A.rho * (yi - xm.y));
+                A.Dm[c][o] = xn;
+                out[c] = xn;
+            } else {
+                A.D[c][o] = dn;
+                out[c] = dn;
+            }
         }
     }
     rd += w * ld_;
@@ -936,6 +962,17 @@ __global__ void k_resid_final(double *dscal, double floor_) {
     dscal[3] = sqrt(d / fmax(r, floor_));
 }
 
+// spectra a Green pass moves besides its 6 sources, 6 strains and 3 written
+// displacements: the increment update reads r0, delta and u0 (and the
+// Chebyshev iterate before delta); the first update writes r0 and delta
+// (and zeroes that iterate); the plain form reads the old u for the residual
+static int green_extra(const pfgb_ctx *c, int mode, int resid) {
+    const bool cheb = c->Dkm[0] != nullptr;
+    if (mode == 2) return cheb ? 12 : 9;
+    if (mode == 1) return cheb ? 9 : 6;
+    return resid ? 3 : 0;
+}
+
 template <typename TE>
 static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks, int mode = 0) {
     using T2 = cplx_t<TE>;
@@ -951,14 +988,18 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
     for (int i = 0; i < 21; ++i) { A.ec.S[i] = (TE)c->p.S[i]; A.ec.Sp[i] = (TE)c->p.S_p[i]; }
     A.tw = (const T2 *)c->tw[sizeof(TE) == 8 ? 0 : 1][0];
     for (int i = 0; i < 6; ++i) A.E[i] = (T2 *)c->E[i];
-    for (int i = 0; i < 3; ++i) { A.U[i] = (T2 *)c->U[i]; A.R[i] = (T2 *)c->Rk[i]; A.D[i] = (T2 *)c->Dk[i]; }
+    for (int i = 0; i < 3; ++i) {
+        A.U[i] = (T2 *)c->U[i]; A.R[i] = (T2 *)c->Rk[i]; A.D[i] = (T2 *)c->Dk[i]; A.Dm[i] = (T2 *)c->Dkm[i];
+    }
+    A.gam = (TE)c->cheb_gam;
+    A.rho = (TE)c->cheb_rho;
     A.partials = c->partials;
     A.resid = resid;
     A.mode = mode;
     dim3 grid((c->g.NzC + TK - 1) / TK, c->g.Ny);
     // reads 6 source spectra (+3 old u for the residual), writes 3 u + 6 strain spectra
     ProfScope ps(c, {eigen ? "x_green_eigen" : "x_green_hij",
-                     (double)(6 + 3 + 6 + (mode == 2 ? 9 : mode == 1 ? 6 : (resid ? 3 : 0))) * (double)c->g.Nk * sizeof(T2)});
+                     (double)(6 + 3 + 6 + green_extra(c, mode, resid)) * (double)c->g.Nk * sizeof(T2)});
     if (eigen) {
         auto kern = k_x_green<TE, true>;
         PFGB_CUDA_TRY(allow_smem(kern, smem));
@@ -1162,13 +1203,18 @@ static pfgb_status launch_green246(pfgb_ctx *c, bool eigen, int resid, int *nblo
     for (int i = 0; i < 21; ++i) { A.ec.S[i] = (float)c->p.S[i]; A.ec.Sp[i] = (float)c->p.S_p[i]; }
     A.tw = (const float2 *)c->tw[1][0];
     for (int i = 0; i < 6; ++i) A.E[i] = (float2 *)c->E[i];
-    for (int i = 0; i < 3; ++i) { A.U[i] = (float2 *)c->U[i]; A.R[i] = (float2 *)c->Rk[i]; A.D[i] = (float2 *)c->Dk[i]; }
+    for (int i = 0; i < 3; ++i) {
+        A.U[i] = (float2 *)c->U[i]; A.R[i] = (float2 *)c->Rk[i]; A.D[i] = (float2 *)c->Dk[i];
+        A.Dm[i] = (float2 *)c->Dkm[i];
+    }
+    A.gam = (float)c->cheb_gam;
+    A.rho = (float)c->cheb_rho;
     A.partials = c->partials;
     A.resid = resid;
     A.mode = mode;
     dim3 grid((c->g.NzC + 7) / 8, c->g.Ny);
     ProfScope ps(c, {eigen ? "x_green_eigen" : "x_green_hij",
-                     (double)(6 + 3 + 6 + (mode == 2 ? 9 : mode == 1 ? 6 : (resid ? 3 : 0))) * (double)c->g.Nk * sizeof(float2)});
+                     (double)(6 + 3 + 6 + green_extra(c, mode, resid)) * (double)c->g.Nk * sizeof(float2)});
     if (eigen) {
         auto kern = k_x_green246<true>;
         PFGB_CUDA_TRY(allow_smem(kern, smem));
@@ -1449,11 +1495,24 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     int iter = accel ? 0 : 1;
     int conv = accel ? 0 : 1;
     double rel = NAN;
+    // Chebyshev semi-iteration of the increment (elastic_chebyshev): rho of
+    // each update from the recurrence rho_2 = 2 / (2 - sig^2),
+    // rho_{k+1} = 1 / (1 - sig^2 rho_k / 4); the new iterate is written over
+    // the one before, so the two buffers swap after every update
+    const bool cheb = inc && c->Dkm[0] != nullptr;
+    int cheb_it = 0;
     for (;;) {
         const int lin = inc && iter >= 1;
         TRY(hij(lin));
         TRY(ypass(-1, "y_fwd6"));
+        if (cheb && lin) {
+            const double s2 = c->cheb_sig * c->cheb_sig;
+            c->cheb_rho = cheb_it == 0 ? 2.0 / (2.0 - s2) : 1.0 / (1.0 - 0.25 * s2 * c->cheb_rho);
+            ++cheb_it;
+        }
         TRY(green(false, accel, inc ? (lin ? 2 : 1) : 0));
+        if (cheb && lin)
+            for (int i = 0; i < 3; ++i) std::swap(c->Dk[i], c->Dkm[i]);
         TRY(ypass(+1, "y_inv6"));
         if (accel) {
             TRY(reduce_to<AccSum2>(c, nb, DS_RES_DIFF));
@@ -2240,6 +2299,77 @@ static pfgb_status make_ktab(pfgb_ctx *c) {
     return PFGB_OK;
 }
 
+// Spectral bounds of the increment operator L = -Gamma0 (h dC).  Gamma0 C0
+// projects onto compatible strains and is self-adjoint in the C0 energy
+// inner product, so L is too, and its Rayleigh quotient -<e, h dC e> /
+// <e, C0 e> lies in [min(0, -mu_max), max(0, -mu_min)] for h in [0, 1],
+// with mu the generalised eigenvalues of (dC, C0) (Voigt with engineering
+// shear: the same quadratic forms as the stress kernels).  mu from the
+// Cholesky factor C0 = L L^T and cyclic Jacobi on L^-1 dC L^-T.  The
+// interval is widened by 2% of its length; false unless C0 is positive
+// definite and the upper bound is below 1 (a convergent iteration).
+static bool chebyshev_bounds(const double S[21], const double Sp[21], double *a, double *b) {
+    static const int st[6] = {0, 6, 11, 15, 18, 20};
+    auto V = [&](const double *c21, int i, int j) { if (i > j) std::swap(i, j); return c21[st[i] + j - i]; };
+    double L[6][6] = {}, M[6][6], B[6][6];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j <= i; ++j) {
+            double t = V(S, i, j);
+            for (int k = 0; k < j; ++k) t -= L[i][k] * L[j][k];
+            if (i == j) {
+                if (!(t > 0.0)) return false;
+                L[i][i] = std::sqrt(t);
+            } else {
+                L[i][j] = t / L[j][j];
+            }
+        }
+    for (int col = 0; col < 6; ++col)       // M = L^-1 dC
+        for (int i = 0; i < 6; ++i) {
+            double t = V(Sp, i, col);
+            for (int k = 0; k < i; ++k) t -= L[i][k] * M[k][col];
+            M[i][col] = t / L[i][i];
+        }
+    for (int row = 0; row < 6; ++row)       // B = M L^-T: B^T = L^-1 M^T
+        for (int i = 0; i < 6; ++i) {
+            double t = M[row][i];
+            for (int k = 0; k < i; ++k) t -= L[i][k] * B[row][k];
+            B[row][i] = t / L[i][i];
+        }
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) { tot += B[i][j] * B[i][j]; if (i != j) off += B[i][j] * B[i][j]; }
+        if (!(off > 1e-30 * tot)) break;
+        for (int p = 0; p < 5; ++p)
+            for (int q = p + 1; q < 6; ++q) {
+                if (std::fabs(B[p][q]) < 1e-300) continue;
+                const double th = (B[q][q] - B[p][p]) / (2.0 * B[p][q]);
+                const double t = (th >= 0.0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+                const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+                for (int k = 0; k < 6; ++k) {
+                    const double bp = B[k][p], bq = B[k][q];
+                    B[k][p] = cs * bp - sn * bq;
+                    B[k][q] = sn * bp + cs * bq;
+                }
+                for (int k = 0; k < 6; ++k) {
+                    const double bp = B[p][k], bq = B[q][k];
+                    B[p][k] = cs * bp - sn * bq;
+                    B[q][k] = sn * bp + cs * bq;
+                }
+            }
+    }
+    double mn = B[0][0], mx = B[0][0];
+    for (int i = 1; i < 6; ++i) { mn = std::min(mn, B[i][i]); mx = std::max(mx, B[i][i]); }
+    double lo = std::min(0.0, -mx), hi = std::max(0.0, -mn);
+    const double w = 0.02 * (hi - lo);
+    lo -= w;
+    hi += w;
+    if (!std::isfinite(lo) || !std::isfinite(hi) || !(hi < 1.0)) return false;
+    *a = lo;
+    *b = hi;
+    return true;
+}
+
 static pfgb_status validate(const pfgb_params *p) {
     if (p->Nx < 1 || p->Ny < 1 || p->Nz < 2 || p->Nx > PFGB_MAX_N || p->Ny > PFGB_MAX_N || p->Nz > PFGB_MAX_N) {
         pfgb_set_error_msg("grid %dx%dx%d outside [1..%d] (Nz >= 2)", p->Nx, p->Ny, p->Nz, PFGB_MAX_N);
@@ -2279,6 +2409,18 @@ static pfgb_status validate(const pfgb_params *p) {
         pfgb_set_error_msg("elastic_iter_max must be >= 1");
         return PFGB_ERR_INVALID;
     }
+    if (p->elastic_chebyshev && p->elastic_enabled) {
+        double a, b;
+        if (!p->elastic_increment_form) {
+            pfgb_set_error_msg("elastic_chebyshev needs elastic_increment_form = 1");
+            return PFGB_ERR_INVALID;
+        }
+        if (!chebyshev_bounds(p->S, p->S_p, &a, &b)) {
+            pfgb_set_error_msg("elastic_chebyshev: the elastic iteration's spectral bounds are not below 1 "
+                               "(C0 not positive definite, or the stiffness contrast too large)");
+            return PFGB_ERR_UNSUPPORTED;
+        }
+    }
     if (p->elastic_warm_start_source < 0 || p->elastic_warm_start_source > 3) {
         pfgb_set_error_msg("elastic_warm_start_source must be 0, 1, 2 or 3");
         return PFGB_ERR_INVALID;
@@ -2299,7 +2441,7 @@ static void ctx_free(pfgb_ctx *c) {
     for (int i = 0; i < 3; ++i) f(c->U[i]);
     f(c->partials); f(c->dscal); f(c->stage);
     for (int i = 0; i < 6; ++i) f(c->sig[i]);
-    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); f(c->Uprev[i]); }
+    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); f(c->Dkm[i]); f(c->Uprev[i]); }
     f(c->mge); f(c->mlap);
     f(c->fno_in); f(c->fno_out);
     for (int i = 0; i < 3; ++i) f(c->Uhom[i]);
@@ -2429,6 +2571,12 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
         if (pin->elastic_increment_form &&
             (pin->elastic_warm_start_enabled || pin->elastic_residual_control_enabled)) {
             for (int i = 0; i < 3; ++i) { A_(&c->Rk[i], sizeof(float2) * Nk); A_(&c->Dk[i], sizeof(float2) * Nk); }
+            double a = 0.0, b = 0.0;
+            if (pin->elastic_chebyshev && chebyshev_bounds(pin->S, pin->S_p, &a, &b)) {   // checked in validate
+                c->cheb_gam = 2.0 / (2.0 - a - b);
+                c->cheb_sig = (b - a) / (2.0 - a - b);
+                for (int i = 0; i < 3; ++i) A_(&c->Dkm[i], sizeof(float2) * Nk);
+            }
         }
         if (pin->elastic_warm_start_extrapolate &&
             (pin->elastic_warm_start_enabled || pin->elastic_residual_control_enabled)) {

@@ -112,6 +112,17 @@ typedef struct pfgb_params {
        reference's warm start, main_cuda.cu:28795-28807); it converges to the
        same tolerance from a guess accurate to O(dt^2).  Default 0. */
     int32_t elastic_warm_start_extrapolate;
+    /* 1: Chebyshev semi-iteration of the increment fixed point (with
+       elastic_increment_form).  The linear part L = -Gamma0 (h dC) is
+       self-adjoint in the C0 energy inner product, so its spectrum is real
+       and lies in [min(0, -mu_max), max(0, -mu_min)], mu the generalised
+       eigenvalues of (dC, C0) (h in [0, 1]).  From those bounds the update
+       takes the relaxation 2 / (2 - a - b) and the Chebyshev three-term
+       recurrence.  Same fixed point and the same residual test as the
+       reference's iteration, in fewer iterations.  No counterpart key in the
+       reference; default 0. */
+    int32_t elastic_chebyshev;
+    int32_t elastic_pad0;
     double elastic_residual_tolerance;
     double elastic_residual_absolute_floor;
     double eps_iso_over_vB;

@@ -248,6 +248,9 @@ struct pfo_state {
     cpx *eps_k[6], *u_k[3], *u_next[3];
     cpx *r_k[3], *d_k[3];   /* increment form: r0 = Phi(u0) - u0 and delta */
     cpx *u_prev[3];         /* extrapolated warm start: u of the step before */
+    cpx *dm_k[3];           /* Chebyshev semi-iteration: the iterate before delta */
+    int cheb;               /* elastic_chebyshev with the increment form */
+    double cheb_gam, cheb_sig;
     int warm_count;         /* solutions available for the warm start */
     int warm_valid;
     /* k tables */
@@ -306,6 +309,15 @@ pfo_state *pfo_create(const pfgb_params *pin) {
         s->r_k[c] = (cpx *)xalloc(kb);
         s->d_k[c] = (cpx *)xalloc(kb);
         s->u_prev[c] = (cpx *)xalloc(kb);
+        s->dm_k[c] = (cpx *)xalloc(kb);
+    }
+    if (pin->elastic_chebyshev && pin->elastic_increment_form) {
+        double a, b;
+        if (pfo_chebyshev_bounds(pin->S, pin->S_p, &a, &b)) {
+            s->cheb = 1;
+            s->cheb_gam = 2.0 / (2.0 - a - b);
+            s->cheb_sig = (b - a) / (2.0 - a - b);
+        }
     }
     s->mlap = (double *)xalloc(rb);
     s->mg = (double *)xalloc(rb);
@@ -335,7 +347,9 @@ void pfo_destroy(pfo_state *s) {
     cpx *kk[] = {s->phi_k, s->rhs_k, s->mu_k, s->divJ_k, s->Y_k, s->scr_k, s->eta_k};
     for (size_t i = 0; i < sizeof(kk) / sizeof(kk[0]); ++i) free(kk[i]);
     for (int c = 0; c < 6; ++c) { free(s->eps_r[c]); free(s->sig_r[c]); free(s->eps_k[c]); }
-    for (int c = 0; c < 3; ++c) { free(s->u_k[c]); free(s->u_next[c]); free(s->r_k[c]); free(s->d_k[c]); free(s->u_prev[c]); }
+    for (int c = 0; c < 3; ++c) {
+        free(s->u_k[c]); free(s->u_next[c]); free(s->r_k[c]); free(s->d_k[c]); free(s->u_prev[c]); free(s->dm_k[c]);
+    }
     free(s->kx); free(s->ky); free(s->kz); free(s->mx); free(s->my); free(s->mz);
     free(s->mlap); free(s->mg);
     free(s);
@@ -617,6 +631,13 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
      * u1 = Phi(u0); then delta <- r0 + L delta with r0 = u1 - u0 and L the
      * linear part h_lin = -(h dC):eps(delta) of the operator */
     const int inc = accel && P->elastic_increment_form;
+    /* Chebyshev semi-iteration of the increment (elastic_chebyshev):
+     * y = delta + gam (g - delta), delta_new = delta_prev + rho (y - delta_prev),
+     * rho_2 = 2 / (2 - sig^2), rho_{k+1} = 1 / (1 - sig^2 rho_k / 4); the first
+     * update is delta_1 = gam r0 from delta_0 = 0 */
+    const int chb = inc && s->cheb;
+    int cheb_it = 0;
+    double rho = 1.0;
     for (;;) {
         const int lin = inc && iter >= 1;
         strain_from_u(s, lin ? s->d_k : s->u_k, s->eps_k);
@@ -656,6 +677,11 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
         if (inc) {
             /* the same residual on the increment iterates */
             double *dif = s->mass_t, *ref = s->der_t;
+            if (chb && lin) {
+                const double s2 = s->cheb_sig * s->cheb_sig;
+                rho = cheb_it == 0 ? 2.0 / (2.0 - s2) : 1.0 / (1.0 - 0.25 * s2 * rho);
+                ++cheb_it;
+            }
             KLOOP_BEGIN(s)
                 double w = (kk_ == 0 || ((s->Nz % 2) == 0 && kk_ == s->Nz / 2)) ? 1.0 : 2.0;
                 double ld = 0.0, lr = 0.0;
@@ -664,14 +690,30 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
                     if (!lin) {   /* r0 = u1 - u0, delta = r0, u_new = u1 */
                         cpx r = {rf(s, v.re - s->u_k[c][idx].re), rf(s, v.im - s->u_k[c][idx].im)};
                         s->r_k[c][idx] = r;
-                        s->d_k[c][idx] = r;
+                        if (chb) {
+                            const cpx x1 = {rf(s, s->cheb_gam * r.re), rf(s, s->cheb_gam * r.im)};
+                            const cpx z = {0.0, 0.0};
+                            s->d_k[c][idx] = x1;
+                            s->dm_k[c][idx] = z;
+                        } else {
+                            s->d_k[c][idx] = r;
+                        }
                         ld += r.re * r.re + r.im * r.im;
                         lr += v.re * v.re + v.im * v.im;
                     } else {      /* delta_new = r0 + L delta, u_new = u0 + delta_new */
                         cpx dn = {rf(s, s->r_k[c][idx].re + v.re), rf(s, s->r_k[c][idx].im + v.im)};
-                        const double dr = dn.re - s->d_k[c][idx].re, di = dn.im - s->d_k[c][idx].im;
+                        const cpx d = s->d_k[c][idx];
+                        const double dr = dn.re - d.re, di = dn.im - d.im;
                         const double ur = rf(s, s->u_k[c][idx].re + dn.re), ui = rf(s, s->u_k[c][idx].im + dn.im);
-                        s->d_k[c][idx] = dn;
+                        if (chb) {
+                            const cpx xm = s->dm_k[c][idx];
+                            const double yr = d.re + s->cheb_gam * dr, yi = d.im + s->cheb_gam * di;
+                            const cpx xn = {rf(s, xm.re + rho * (yr - xm.re)), rf(s, xm.im + rho * (yi - xm.im))};
+                            s->dm_k[c][idx] = d;
+                            s->d_k[c][idx] = xn;
+                        } else {
+                            s->d_k[c][idx] = dn;
+                        }
                         ld += dr * dr + di * di;
                         lr += ur * ur + ui * ui;
                     }
@@ -1470,4 +1512,81 @@ int pfo_diagnostics(const pfo_state *s, pfgb_diag *d) {
     d->phi_min = pmin; d->phi_max = pmax; d->xB_min = xmin; d->xB_max = xmax;
     free(t); free(u); free(w); free(f);
     return PFGB_OK;
+}
+
+/* Spectral bounds of the increment operator -Gamma0 (h dC) for h in [0, 1]:
+ * [min(0, -mu_max), max(0, -mu_min)] with mu the generalised eigenvalues of
+ * (dC, C0) in Voigt form (engineering shear), widened by 2% of the length.
+ * Restated here with a symmetric C0^(-1/2) built from C0's own eigen
+ * decomposition (Jacobi), then Jacobi on C0^(-1/2) dC C0^(-1/2). */
+static void o_jacobi6(double A[6][6], double V[6][6]) {
+    for (int i = 0; i < 6; ++i) for (int j = 0; j < 6; ++j) V[i][j] = (i == j);
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0;
+        for (int i = 0; i < 6; ++i) for (int j = i + 1; j < 6; ++j) off += A[i][j] * A[i][j];
+        if (off < 1e-40) break;
+        for (int p = 0; p < 6; ++p)
+            for (int q = p + 1; q < 6; ++q) {
+                if (fabs(A[p][q]) < 1e-300) continue;
+                const double phi = 0.5 * atan2(2.0 * A[p][q], A[q][q] - A[p][p]);
+                const double c = cos(phi), sn = sin(phi);
+                for (int k = 0; k < 6; ++k) {   /* columns p, q */
+                    const double ap = A[k][p], aq = A[k][q];
+                    A[k][p] = c * ap - sn * aq;
+                    A[k][q] = sn * ap + c * aq;
+                }
+                for (int k = 0; k < 6; ++k) {   /* rows p, q */
+                    const double ap = A[p][k], aq = A[q][k];
+                    A[p][k] = c * ap - sn * aq;
+                    A[q][k] = sn * ap + c * aq;
+                }
+                for (int k = 0; k < 6; ++k) {
+                    const double vp = V[k][p], vq = V[k][q];
+                    V[k][p] = c * vp - sn * vq;
+                    V[k][q] = sn * vp + c * vq;
+                }
+            }
+    }
+}
+
+int pfo_chebyshev_bounds(const double S[21], const double Sp[21], double *a, double *b) {
+    static const int st[6] = {0, 6, 11, 15, 18, 20};
+    double C[6][6], D[6][6], V[6][6], W[6][6], T[6][6], B[6][6];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            const int lo = i < j ? i : j, hi = i < j ? j : i;
+            C[i][j] = S[st[lo] + hi - lo];
+            D[i][j] = Sp[st[lo] + hi - lo];
+        }
+    o_jacobi6(C, V);   /* C0 = V diag V^T */
+    for (int i = 0; i < 6; ++i) if (!(C[i][i] > 0.0)) return 0;
+    for (int i = 0; i < 6; ++i)   /* W = C0^(-1/2) = V diag(1/sqrt) V^T */
+        for (int j = 0; j < 6; ++j) {
+            double t = 0.0;
+            for (int k = 0; k < 6; ++k) t += V[i][k] * V[j][k] / sqrt(C[k][k]);
+            W[i][j] = t;
+        }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            double t = 0.0;
+            for (int k = 0; k < 6; ++k) t += D[i][k] * W[k][j];
+            T[i][j] = t;
+        }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            double t = 0.0;
+            for (int k = 0; k < 6; ++k) t += W[i][k] * T[k][j];
+            B[i][j] = t;
+        }
+    o_jacobi6(B, V);
+    double mn = B[0][0], mx = B[0][0];
+    for (int i = 1; i < 6; ++i) { if (B[i][i] < mn) mn = B[i][i]; if (B[i][i] > mx) mx = B[i][i]; }
+    double lo = fmin(0.0, -mx), hi = fmax(0.0, -mn);
+    const double w = 0.02 * (hi - lo);
+    lo -= w;
+    hi += w;
+    if (!isfinite(lo) || !isfinite(hi) || !(hi < 1.0)) return 0;
+    *a = lo;
+    *b = hi;
+    return 1;
 }

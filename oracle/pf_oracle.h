@@ -47,6 +47,9 @@ int pfo_read_elastic(const pfo_state *s, double *sigma6, double *strain6);
 int pfo_read_displacement_k(const pfo_state *s, double *u3);
 int pfo_diagnostics(const pfo_state *s, pfgb_diag *d);
 int pfo_set_threads(int n);
+/* spectral bounds [a, b] of the elastic increment operator (elastic_chebyshev);
+ * returns 0 when they are not below 1 */
+int pfo_chebyshev_bounds(const double S[21], const double Sp[21], double *a, double *b);
 
 /* FP64 3D transforms, cuFFT D2Z/Z2D conventions (unnormalised). */
 void pfo_fft3d_r2c(int Nx, int Ny, int Nz, const double *in, double *out);

@@ -240,3 +240,50 @@ def test_extrapolated_warm_start_parity(capi, oracle, prec):
     fo = o.fields()
     for k in ("phi", "xB", "Y"):
         assert rel_l2(fg[k], fo[k]) <= TOL[prec], k
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_chebyshev_iteration_parity(capi, oracle, prec):
+    """elastic_chebyshev = 1: the increment iterated by Chebyshev
+    semi-iteration from the spectral bounds of the linear part.  GPU against
+    the oracle doing the same, step by step (iterations within one), and the
+    converged fields against the plain increment form at tolerance 1e-8."""
+    from cuda_sto_pf_gb300.solver import Solver
+    out, its = {}, {}
+    for ch in (0, 1):
+        p = params_for(capi, "c2.params", n=32, precision=prec, model_mode=1, zero_mode_enabled=1,
+                       elastic_residual_tolerance=1e-8, elastic_fail_on_nonconvergence=0, elastic_chebyshev=ch)
+        phi, xB, eta = _inputs(capi, p, 32, True, seed=19)
+        o = oracle(p, threads=4)
+        o.load(phi, xB, eta)
+        so = capi.StepStats()
+        its[ch] = []
+        with Solver(p) as s:
+            s.load(phi, xB, eta)
+            for k in range(3):
+                assert o.step(1, so) == 0
+                sg = s.step(1)
+                # the plain iteration's cold first step can run into the cap
+                # (32) at 1e-8; Chebyshev converges on every step
+                if ch == 1 or k > 0:
+                    assert sg.elastic_converged == 1 and so.elastic_converged == 1, (ch, k)
+                assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1, (ch, k)
+                its[ch].append(sg.elastic_iterations)
+            fg = s.fields()
+            eg = s.elastic()
+        fo = o.fields()
+        for k in ("phi", "xB", "Y", "eta"):
+            assert rel_l2(fg[k], fo[k]) <= TOL[prec], (ch, k)
+        assert rel_l2(eg["strain"], o.elastic()["strain"]) <= TOL[prec]
+        out[ch] = (fg, eg)
+    for k in ("phi", "xB", "eta"):
+        assert rel_l2(out[1][0][k], out[0][0][k]) <= TOL[prec], k
+    assert rel_l2(out[1][1]["strain"], out[0][1]["strain"]) <= TOL[prec]
+    assert sum(its[1]) < sum(its[0]), its
+
+
+def test_chebyshev_needs_increment_form(capi):
+    from cuda_sto_pf_gb300.solver import Solver
+    p = params_for(capi, "c2.params", n=16, elastic_chebyshev=1, elastic_increment_form=0)
+    with pytest.raises(capi.PfgbError):
+        Solver(p)

@@ -19,10 +19,13 @@ is pinned to closed-form results that hold exactly on the grid:
   reach.  The profile is band-limited well inside the 2/3 mask, so the
   dealiasing of the spectral solve does not alter the answer.
 """
+import os
+import sys
+
 import numpy as np
 import pytest
 
-from conftest import params_for
+from conftest import REPO, params_for
 
 
 def h_of(phi):
@@ -151,3 +154,31 @@ def test_gpu_elastic_laminate(capi, heterogeneous, precision):
         assert st.elastic_converged == 1
         el = s.elastic()
     _check_laminate(el, p, phi, xB, 2e-5)
+
+
+def test_chebyshev_bounds_match_generalised_eigenvalues(capi):
+    """The oracle's spectral bounds of the elastic increment operator are
+    [min(0, -mu_max), max(0, -mu_min)] widened by 2%, mu the generalised
+    eigenvalues of (dC, C0) in Voigt form."""
+    import ctypes
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_py
+    L = oracle_py.lib()
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.pfo_chebyshev_bounds.restype = ctypes.c_int
+    L.pfo_chebyshev_bounds.argtypes = [dp, dp, dp, dp]
+    p = params_for(capi, "c2.params", n=16)
+    a, b = ctypes.c_double(), ctypes.c_double()
+    assert L.pfo_chebyshev_bounds(p.S, p.S_p, ctypes.byref(a), ctypes.byref(b)) == 1
+    st = [0, 6, 11, 15, 18, 20]
+    V = lambda c, i, j: c[st[min(i, j)] + max(i, j) - min(i, j)]
+    C0 = np.array([[V(p.S, i, j) for j in range(6)] for i in range(6)])
+    dC = np.array([[V(p.S_p, i, j) for j in range(6)] for i in range(6)])
+    mu = np.linalg.eigvals(np.linalg.solve(C0, dC)).real
+    lo, hi = min(0.0, -mu.max()), max(0.0, -mu.min())
+    w = 0.02 * (hi - lo)
+    assert abs(a.value - (lo - w)) < 1e-12 and abs(b.value - (hi + w)) < 1e-12
+    # a contrast whose bound reaches 1 is refused
+    Sp = np.array(p.S[:]) * -1.2
+    arr = (ctypes.c_double * 21)(*Sp)
+    assert L.pfo_chebyshev_bounds(p.S, arr, ctypes.byref(a), ctypes.byref(b)) == 0
