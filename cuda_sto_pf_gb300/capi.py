@@ -116,6 +116,27 @@ class Diag(Structure):
                 ("xB_max", c_double), ("n_in", c_double), ("n_if", c_double)]
 
 
+class CkptProvenance(Structure):
+    _fields_ = [("zero_mode", ctypes.c_char * 64), ("backend", ctypes.c_char * 64),
+                ("composition_mode", ctypes.c_char * 64), ("y_update_mode", ctypes.c_char * 64),
+                ("explicit_context", ctypes.c_char * 64), ("reaction_discretization", ctypes.c_char * 64),
+                ("elastic_solver_mode", ctypes.c_char * 64), ("initial_state_class", ctypes.c_char * 96),
+                ("fixture_manifest_sha256", ctypes.c_char * 96),
+                ("profile_library_manifest_sha256", ctypes.c_char * 96),
+                ("elastic_solver_fingerprint", ctypes.c_uint64), ("parameter_fingerprint", ctypes.c_uint64)]
+
+
+class CkptState(Structure):
+    _fields_ = [("accepted_step", ctypes.c_uint64), ("nx", c_int32), ("ny", c_int32), ("nz", c_int32),
+                ("elastic_present", c_int32), ("dt_code", c_double), ("temperature_K", c_double),
+                ("target_mass_code", c_double), ("last_lambda", c_double), ("last_residual_code", c_double),
+                ("last_derivative_code", c_double), ("last_iterations", ctypes.c_uint64),
+                ("accepted_zero_mode_steps", ctypes.c_uint64), ("elastic_source_field_step", ctypes.c_uint64),
+                ("elastic_last_iterations", ctypes.c_uint64), ("elastic_last_relative_residual", c_double),
+                ("provenance", CkptProvenance), ("phi", c_void_p), ("Y", c_void_p), ("xB", c_void_p),
+                ("dY_dt_prev", c_void_p), ("displacement_k", c_void_p)]
+
+
 class FnoConfig(Structure):
     _fields_ = [("Nx", c_int32), ("Ny", c_int32), ("Nz", c_int32), ("modes", c_int32), ("layers", c_int32),
                 ("pad", c_int32), ("seed", ctypes.c_uint64), ("in_scale", ctypes.c_float * 8),
@@ -160,6 +181,17 @@ EXPORTS = [
     ("pfgb_fft3d_r2c", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     ("pfgb_fft3d_c2r", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     ("pfgb_fft3d_r2c_noalloc", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    ("pfgb_fnv1a64", ctypes.c_uint64, [c_void_p, c_size_t, ctypes.c_uint64]),
+    ("pfgb_parameter_fingerprint", ctypes.c_uint64, [POINTER(Params)]),
+    ("pfgb_elastic_solver_fingerprint", ctypes.c_uint64, [POINTER(Params)]),
+    ("pfgb_checkpoint_provenance_for", c_int, [POINTER(Params), c_char_p, c_char_p, c_char_p,
+                                               POINTER(CkptProvenance)]),
+    ("pfgb_checkpoint_write_file", c_int, [c_char_p, POINTER(CkptState)]),
+    ("pfgb_checkpoint_peek", c_int, [c_char_p, POINTER(c_int32), POINTER(c_int32), POINTER(c_int32),
+                                     POINTER(c_int32), POINTER(c_int32)]),
+    ("pfgb_checkpoint_read_file", c_int, [c_char_p, POINTER(CkptProvenance), POINTER(CkptState)]),
+    ("pfgb_checkpoint_save", c_int, [c_void_p, c_char_p, c_char_p, c_char_p, c_char_p]),
+    ("pfgb_checkpoint_restore", c_int, [c_void_p, c_char_p, c_char_p, c_char_p, c_char_p]),
     ("pfgb_fno_config_default", None, [POINTER(FnoConfig)]),
     ("pfgb_fno_create", c_int, [POINTER(FnoConfig), c_int, POINTER(c_void_p)]),
     ("pfgb_fno_destroy", None, [c_void_p]),

@@ -102,6 +102,12 @@ struct pfgb_ctx {
     int min_iter = 0, conv_count = 0, converged_iter = 0, xb_clamp = 0;
     double sum_alpha = 0.0;   // sum (1 - h) of the last phi (zero-mode curvature bound)
     int warm_valid = 0, step = 0, loaded = 0;
+    // runtime state a checkpoint carries: the last zero-mode solve and the
+    // last elastic solve
+    double zm_lambda = 0.0, zm_residual = 0.0, zm_derivative = 0.0;
+    uint64_t zm_iterations = 0, zm_accepted = 0;
+    uint64_t el_iterations = 0;
+    double el_residual = 0.0;
     size_t bytes = 0;
     std::string err;
     PhysC pc;
@@ -1534,6 +1540,8 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
         }
     }
     if (accel) { c->warm_valid = 1; c->warm_count++; }
+    c->el_iterations = (uint64_t)iter;
+    c->el_residual = rel;
     if (st) {
         st->elastic_iterations = iter;
         st->elastic_converged = conv;
@@ -1692,6 +1700,11 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     if (ymin + lam < -P.Y_clip || ymax + lam > Ycap) return fail("shifted Y leaves [-Y_clip, Y_cap]");
     c->Yc += lam;
     c->dYoff = lam / P.dt;
+    c->zm_lambda = lam;
+    c->zm_residual = res;
+    c->zm_derivative = der;
+    c->zm_iterations = (uint64_t)iters;
+    c->zm_accepted++;
     if (st) {
         st->zero_mode_iterations = iters;
         st->zero_mode_newton_steps = nwt;
@@ -2488,6 +2501,8 @@ static pfgb_status load_device(pfgb_ctx *c, const double *phi, const double *xB,
     c->warm_valid = 0;
     c->warm_count = 0;
     c->step = 0;
+    c->zm_lambda = c->zm_residual = c->zm_derivative = 0.0;
+    c->zm_iterations = c->zm_accepted = 0;
     c->min_iter = c->conv_count = c->converged_iter = c->xb_clamp = 0;
     c->lambda_vol = 0.0;
     c->prev_F_total = NAN;
@@ -2515,6 +2530,41 @@ static pfgb_status load_host(pfgb_ctx *c, const double *phi, const double *xB, c
     if (dYdt) PFGB_CUDA_TRY(cudaMemcpyAsync(dd, dYdt, b, cudaMemcpyHostToDevice, c->stream));
     return c->p.precision == PFGB_PREC_FP64 ? load_device<double>(c, dp, dx, de, dd, keep)
                                             : load_device<float>(c, dp, dx, de, dd, keep);
+}
+
+// checkpoint restart: phi, Y and dY/dt as stored (eta zero, as the
+// reference restores it), and the mass ledger sum (1 - h) xB + v_B h of the
+// stored phi and xB (gpu_reduce_sum_xBtot)
+template <typename T>
+__global__ void k_restore_state(const double *phi, const double *Y, const double *xB, const double *dYdt,
+                                T *phi_o, T *eta_o, T *Y_o, T *dYdt_o, long long N, double vB, double *partials) {
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double p = phi[i];
+        phi_o[i] = (T)p;
+        eta_o[i] = T(0);
+        Y_o[i] = (T)Y[i];
+        dYdt_o[i] = (T)dYdt[i];
+        const double h = pf_h(p);
+        acc += (1.0 - h) * xB[i] + vB * h;
+    }
+    AccSum1 s{acc};
+    block_reduce_acc(s);
+    if (threadIdx.x == 0) reinterpret_cast<AccSum1 *>(partials)[blockIdx.x] = s;
+}
+
+static pfgb_status checkpoint_context_ok(const pfgb_ctx *c, const char *what) {
+    if (!c->p.zero_mode_enabled || c->p.model_mode != PFGB_MODEL_TWO_PHASE || c->p.mode != PFGB_MODE_DYNAMICS) {
+        pfgb_set_error_msg("%s: checkpoints are the zero-mode dynamics contract (zero mode on, two_phase; the file "
+                           "carries no eta)", what);
+        return PFGB_ERR_UNSUPPORTED;
+    }
+    return PFGB_OK;
+}
+
+static bool accel_solver(const pfgb_params &P) {
+    return P.elastic_enabled && (P.elastic_warm_start_enabled || P.elastic_residual_control_enabled);
 }
 
 // ---------------------------------------------------------------------------
@@ -2879,6 +2929,128 @@ pfgb_status pfgb_elastic_training_pair(pfgb_ctx *c, float *d_in8, float *d_targe
     sp->elastic_iterations_total = 0;
     return c->p.precision == PFGB_PREC_FP64 ? training_pair<double>(c, d_in8, d_target3, sp)
                                             : training_pair<float>(c, d_in8, d_target3, sp);
+}
+
+pfgb_status pfgb_checkpoint_save(pfgb_ctx *c, const char *path, const char *initial_state_class,
+                                 const char *fixture_manifest_sha256,
+                                 const char *profile_library_manifest_sha256) {
+    if (!c || !path) return PFGB_ERR_INVALID;
+    TRY(checkpoint_context_ok(c, "pfgb_checkpoint_save"));
+    if (!c->loaded) { pfgb_set_error_msg("pfgb_checkpoint_save: no fields loaded"); return PFGB_ERR_INVALID; }
+    const bool accel = accel_solver(c->p);
+    if (accel && (!c->warm_valid || c->step < 1)) {
+        pfgb_set_error_msg("pfgb_checkpoint_save: refusing to checkpoint an invalid elastic warm state at step %d",
+                           c->step);
+        return PFGB_ERR_INVALID;
+    }
+    pfgb_checkpoint_state st;
+    std::memset(&st, 0, sizeof(st));
+    TRY(pfgb_checkpoint_provenance_for(&c->p, initial_state_class, fixture_manifest_sha256,
+                                       profile_library_manifest_sha256, &st.provenance));
+    const size_t N = (size_t)c->g.N, Nk = (size_t)c->g.Nk;
+    std::vector<double> phi(N), Y(N), xB(N), dYdt(N);
+    std::vector<float> u;
+    TRY(pfgb_read_fields(c, phi.data(), xB.data(), Y.data(), nullptr, dYdt.data()));
+    if (accel) {
+        u.resize(6 * Nk);
+        TRY(pfgb_read_displacement_k(c, u.data()));
+    }
+    st.accepted_step = (uint64_t)c->step;
+    st.nx = c->g.Nx; st.ny = c->g.Ny; st.nz = c->g.Nz;
+    st.elastic_present = accel ? 1 : 0;
+    st.dt_code = c->p.dt;
+    st.temperature_K = c->p.temperature_C + 273.15;
+    st.target_mass_code = c->target_mass;
+    st.last_lambda = c->zm_lambda;
+    st.last_residual_code = c->zm_residual;
+    st.last_derivative_code = c->zm_derivative;
+    st.last_iterations = c->zm_iterations;
+    st.accepted_zero_mode_steps = c->zm_accepted;
+    st.elastic_source_field_step = accel ? (uint64_t)(c->step - 1) : 0;
+    st.elastic_last_iterations = accel ? c->el_iterations : 0;
+    st.elastic_last_relative_residual = accel ? c->el_residual : 0.0;
+    st.phi = phi.data(); st.Y = Y.data(); st.xB = xB.data(); st.dY_dt_prev = dYdt.data();
+    st.displacement_k = accel ? u.data() : nullptr;
+    return pfgb_checkpoint_write_file(path, &st);
+}
+
+pfgb_status pfgb_checkpoint_restore(pfgb_ctx *c, const char *path, const char *initial_state_class,
+                                    const char *fixture_manifest_sha256,
+                                    const char *profile_library_manifest_sha256) {
+    if (!c || !path) return PFGB_ERR_INVALID;
+    TRY(checkpoint_context_ok(c, "pfgb_checkpoint_restore"));
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    pfgb_checkpoint_provenance expect;
+    TRY(pfgb_checkpoint_provenance_for(&c->p, initial_state_class, fixture_manifest_sha256,
+                                       profile_library_manifest_sha256, &expect));
+    const size_t N = (size_t)c->g.N, Nk = (size_t)c->g.Nk;
+    std::vector<double> phi(N), Y(N), xB(N), dYdt(N);
+    std::vector<float> u(6 * Nk);
+    pfgb_checkpoint_state st;
+    std::memset(&st, 0, sizeof(st));
+    st.nx = c->g.Nx; st.ny = c->g.Ny; st.nz = c->g.Nz;
+    st.phi = phi.data(); st.Y = Y.data(); st.xB = xB.data(); st.dY_dt_prev = dYdt.data();
+    st.displacement_k = u.data();
+    TRY(pfgb_checkpoint_read_file(path, &expect, &st));
+    if (st.dt_code != c->p.dt || st.temperature_K != c->p.temperature_C + 273.15) {
+        pfgb_set_error_msg("checkpoint %s: restart grid/dt/temperature mismatch", path);
+        return PFGB_ERR_INVALID;
+    }
+    const bool accel = accel_solver(c->p);
+    if (accel && !st.elastic_present) {
+        pfgb_set_error_msg("checkpoint %s: accelerated elastic restart lacks the V4 warm state", path);
+        return PFGB_ERR_INVALID;
+    }
+    TRY(ensure_stage(c));
+    double *d = c->stage;
+    const size_t b = sizeof(double) * N;
+    PFGB_CUDA_TRY(cudaMemcpyAsync(d, phi.data(), b, cudaMemcpyHostToDevice, c->stream));
+    PFGB_CUDA_TRY(cudaMemcpyAsync(d + N, Y.data(), b, cudaMemcpyHostToDevice, c->stream));
+    PFGB_CUDA_TRY(cudaMemcpyAsync(d + 2 * N, xB.data(), b, cudaMemcpyHostToDevice, c->stream));
+    PFGB_CUDA_TRY(cudaMemcpyAsync(d + 3 * N, dYdt.data(), b, cudaMemcpyHostToDevice, c->stream));
+    const int nb = 304;
+    if (c->p.precision == PFGB_PREC_FP64)
+        k_restore_state<double><<<nb, 256, 0, c->stream>>>(d, d + N, d + 2 * N, d + 3 * N, (double *)c->phi[c->cur],
+                                                           (double *)c->eta[c->ecur], (double *)c->Y,
+                                                           (double *)c->dYdt, c->g.N, c->p.v_B, c->partials);
+    else
+        k_restore_state<float><<<nb, 256, 0, c->stream>>>(d, d + N, d + 2 * N, d + 3 * N, (float *)c->phi[c->cur],
+                                                          (float *)c->eta[c->ecur], (float *)c->Y, (float *)c->dYdt,
+                                                          c->g.N, c->p.v_B, c->partials);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    TRY(reduce_to<AccSum1>(c, nb, DS_ZM));
+    TRY(sync_read(c, DS_ZM, 1));
+    const double mass = c->hscal[DS_ZM];
+    if (!std::isfinite(mass) ||
+        std::fabs(mass - st.target_mass_code) > 1.0e-12 * std::max(std::fabs(st.target_mass_code), 1.0)) {
+        pfgb_set_error_msg("checkpoint %s: field ledger does not match the frozen zero-mode target: current=%.17e "
+                           "target=%.17e", path, mass, st.target_mass_code);
+        c->loaded = 0;
+        return PFGB_ERR_ZERO_MODE;
+    }
+    if (accel) {
+        for (int a = 0; a < 3; ++a)
+            PFGB_CUDA_TRY(cudaMemcpyAsync(c->U[a], u.data() + 2 * a * Nk, sizeof(float2) * Nk,
+                                          cudaMemcpyHostToDevice, c->stream));
+    }
+    for (int i = 0; i < 6; ++i) PFGB_CUDA_TRY(cudaMemsetAsync(c->eps[i], 0, sizeof(float) * N, c->stream));
+    PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->Yc = 0.0;
+    c->dYoff = 0.0;
+    c->target_mass = st.target_mass_code;
+    c->zm_lambda = st.last_lambda;
+    c->zm_residual = st.last_residual_code;
+    c->zm_derivative = st.last_derivative_code;
+    c->zm_iterations = st.last_iterations;
+    c->zm_accepted = st.accepted_zero_mode_steps;
+    c->warm_valid = accel ? 1 : 0;
+    c->warm_count = accel ? 1 : 0;
+    c->el_iterations = st.elastic_last_iterations;
+    c->el_residual = st.elastic_last_relative_residual;
+    c->step = (int)st.accepted_step;
+    c->min_iter = c->conv_count = c->converged_iter = c->xb_clamp = 0;
+    c->loaded = 1;
+    return PFGB_OK;
 }
 
 pfgb_status pfgb_read_displacement_k(pfgb_ctx *c, float *u3) {

@@ -47,6 +47,10 @@ struct Cli {
     int device = 0;
     std::string warm_model;   // learned start of the elastic iteration (no reference counterpart)
     int warm_source = -1;
+    // zero-mode checkpoints (main_cuda.cu:22715-22760)
+    int ckpt_every = 0;
+    std::string ckpt_path, restart_from;
+    std::string isc = "LEGACY_UNSPECIFIED", fsha = "LEGACY_UNSPECIFIED", psha = "LEGACY_UNSPECIFIED";
     // minimize
     bool min_full = false;
     int min_max_iter = -1, min_conv_steps = -1, min_post_iters = -1;
@@ -85,6 +89,11 @@ void usage() {
            "  --Y-rhs-term-h-scale <s>\n"
            "  --precision fp64|fp32           field precision (default fp64, as the reference)\n"
            "  --device <n>                    CUDA device ordinal\n"
+           "  --pf-checkpoint-every <n>       zero-mode checkpoint every n steps and at the end\n"
+           "  --pf-checkpoint-path <f>        checkpoint file (V4 with the elastic warm state, else V3)\n"
+           "  --pf-restart-from <f>           continue from a zero-mode checkpoint\n"
+           "  --pf-initial-state-class <s>  --pf-fixture-manifest-sha256 <s>\n"
+           "  --pf-profile-library-manifest-sha256 <s>   restart identity (default LEGACY_UNSPECIFIED)\n"
            "  --elastic-warm-start-model <f>  model file (pfgb_fno_save) for the elastic start\n"
            "  --elastic-warm-start-source <n> 0 previous step (default), 1 model at cold starts,\n"
            "                                  2 model every step, 3 cold every step\n");
@@ -159,6 +168,18 @@ Cli parse(int argc, char **argv) {
             else bad(a, v);
         }
         else if ((v = flag_value(argc, argv, &i, "--device"))) { if (!to_int(v, &c.device)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--pf-checkpoint-every")) ||
+                 (v = flag_value(argc, argv, &i, "--pf_checkpoint_every"))) { if (!to_int(v, &c.ckpt_every)) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--pf-checkpoint-path")) ||
+                 (v = flag_value(argc, argv, &i, "--pf_checkpoint_path"))) c.ckpt_path = v;
+        else if ((v = flag_value(argc, argv, &i, "--pf-restart-from")) ||
+                 (v = flag_value(argc, argv, &i, "--pf_restart_from"))) c.restart_from = v;
+        else if ((v = flag_value(argc, argv, &i, "--pf-initial-state-class")) ||
+                 (v = flag_value(argc, argv, &i, "--pf_initial_state_class"))) c.isc = v;
+        else if ((v = flag_value(argc, argv, &i, "--pf-fixture-manifest-sha256")) ||
+                 (v = flag_value(argc, argv, &i, "--pf_fixture_manifest_sha256"))) c.fsha = v;
+        else if ((v = flag_value(argc, argv, &i, "--pf-profile-library-manifest-sha256")) ||
+                 (v = flag_value(argc, argv, &i, "--pf_profile_library_manifest_sha256"))) c.psha = v;
         else if ((v = flag_value(argc, argv, &i, "--elastic-warm-start-model"))) c.warm_model = v;
         else if ((v = flag_value(argc, argv, &i, "--elastic-warm-start-source"))) {
             if (!to_int(v, &c.warm_source) || c.warm_source < 0 || c.warm_source > 3) bad(a, v);
@@ -381,39 +402,58 @@ int main(int argc, char **argv) {
                 P.elastic_warm_start_source);
         return 2;
     }
+    // checkpoint contract (main_cuda.cu:22760-22790)
+    const bool restarting = !c.restart_from.empty();
+    if (c.ckpt_every < 0) { fprintf(stderr, "[fatal] --pf-checkpoint-every must be >= 0\n"); return 2; }
+    if ((c.ckpt_every > 0 || restarting) && !P.zero_mode_enabled) {
+        fprintf(stderr, "[fatal] PF checkpoint/restart provenance is available only with "
+                        "PF_CONSERVED_Y_ZERO_MODE_V1\n");
+        return 2;
+    }
+    if (c.ckpt_every > 0 && c.ckpt_path.empty()) {
+        fprintf(stderr, "[fatal] --pf-checkpoint-path is required when periodic checkpointing is enabled\n");
+        return 2;
+    }
+    if ((c.ckpt_every > 0 || restarting) && minimize) {
+        fprintf(stderr, "[fatal] checkpoints are written and read by dynamics runs only\n");
+        return 2;
+    }
     if ((st = pfgb_params_finalize(&P)) != PFGB_OK) return fail(st, "pfgb_params_finalize");
 
     // ---- initial fields ---------------------------------------------------
-    if (c.init_mode != "raw_fields") {
-        fprintf(stderr, "[fatal] this build initialises from --init-mode raw_fields only\n");
-        return 2;
-    }
     const size_t N = (size_t)P.Nx * P.Ny * P.Nz;
     std::vector<double> phi, xB, eta, dYdt;
-    if (c.init_phi.empty() || c.init_xB.empty()) {
+    if (restarting) {
+        // the fields come from the checkpoint (main_cuda.cu:27340-27380)
+    } else if (c.init_mode != "raw_fields") {
+        fprintf(stderr, "[fatal] this build initialises from --init-mode raw_fields only\n");
+        return 2;
+    } else if (c.init_phi.empty() || c.init_xB.empty()) {
         fprintf(stderr, "[fatal] raw_fields needs --init-phi-raw and --init-xB-raw\n");
         return 2;
     }
-    if (!read_raw(c.init_phi, N, &phi) || !read_raw(c.init_xB, N, &xB)) return 2;
-    if (!c.init_eta.empty() && !read_raw(c.init_eta, N, &eta)) return 2;
-    if (!c.init_dYdt.empty() && !read_raw(c.init_dYdt, N, &dYdt)) return 2;
-    double xB_max_safe = 0.07;   // reference default when init_meta.json does not set it
-    if (!c.init_meta.empty()) {
-        const std::string meta = slurp(c.init_meta);
-        if (meta.empty()) { fprintf(stderr, "[fatal] cannot read %s\n", c.init_meta.c_str()); return 2; }
-        double v;
-        if (json_number(meta, "xB_max_safe", &v)) xB_max_safe = v;
-        const char *dims[3] = {"Nx", "Ny", "Nz"};
-        const int have[3] = {P.Nx, P.Ny, P.Nz};
-        for (int a = 0; a < 3; ++a)
-            if (json_number(meta, dims[a], &v) && (int)v != have[a]) {
-                fprintf(stderr, "[fatal] init_meta %s=%d does not match the grid (%d)\n", dims[a], (int)v, have[a]);
-                return 2;
-            }
+    if (!restarting) {
+        if (!read_raw(c.init_phi, N, &phi) || !read_raw(c.init_xB, N, &xB)) return 2;
+        if (!c.init_eta.empty() && !read_raw(c.init_eta, N, &eta)) return 2;
+        if (!c.init_dYdt.empty() && !read_raw(c.init_dYdt, N, &dYdt)) return 2;
+        double xB_max_safe = 0.07;   // reference default when init_meta.json does not set it
+        if (!c.init_meta.empty()) {
+            const std::string meta = slurp(c.init_meta);
+            if (meta.empty()) { fprintf(stderr, "[fatal] cannot read %s\n", c.init_meta.c_str()); return 2; }
+            double v;
+            if (json_number(meta, "xB_max_safe", &v)) xB_max_safe = v;
+            const char *dims[3] = {"Nx", "Ny", "Nz"};
+            const int have[3] = {P.Nx, P.Ny, P.Nz};
+            for (int a = 0; a < 3; ++a)
+                if (json_number(meta, dims[a], &v) && (int)v != have[a]) {
+                    fprintf(stderr, "[fatal] init_meta %s=%d does not match the grid (%d)\n", dims[a], (int)v, have[a]);
+                    return 2;
+                }
+        }
+        st = pfgb_prepare_raw_fields(&P, xB_max_safe, phi.data(), xB.data(), eta.empty() ? nullptr : eta.data(),
+                                     dYdt.empty() ? nullptr : dYdt.data(), N);
+        if (st != PFGB_OK) return fail(st, "pfgb_prepare_raw_fields");
     }
-    st = pfgb_prepare_raw_fields(&P, xB_max_safe, phi.data(), xB.data(), eta.empty() ? nullptr : eta.data(),
-                                 dYdt.empty() ? nullptr : dYdt.data(), N);
-    if (st != PFGB_OK) return fail(st, "pfgb_prepare_raw_fields");
 
     // ---- output layout ----------------------------------------------------
     const std::string ptxt = slurp(c.param_file);
@@ -456,9 +496,25 @@ int main(int argc, char **argv) {
             return fail(st, "--elastic-warm-start-model");
         }
     }
-    st = pfgb_load_fields(ctx, phi.data(), xB.data(), eta.empty() ? nullptr : eta.data(),
-                          dYdt.empty() ? nullptr : dYdt.data());
-    if (st != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_load_fields"); }
+    int first_step = 1;
+    if (restarting) {
+        st = pfgb_checkpoint_restore(ctx, c.restart_from.c_str(), c.isc.c_str(), c.fsha.c_str(), c.psha.c_str());
+        if (st != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "PF zero-mode restart rejected"); }
+        pfgb_step_stats s0;
+        if ((st = pfgb_step(ctx, 0, &s0)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_step"); }
+        if (s0.step >= c.nsteps) {
+            fprintf(stderr, "[fatal] restart accepted_step=%d must be less than requested final nsteps=%d\n",
+                    s0.step, c.nsteps);
+            pfgb_destroy(ctx);
+            return 2;
+        }
+        first_step = s0.step + 1;
+        printf("PF_ZERO_MODE_RESTART checkpoint=%s accepted_step=%d\n", c.restart_from.c_str(), s0.step);
+    } else {
+        st = pfgb_load_fields(ctx, phi.data(), xB.data(), eta.empty() ? nullptr : eta.data(),
+                              dYdt.empty() ? nullptr : dYdt.data());
+        if (st != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_load_fields"); }
+    }
 
     std::vector<double> f_phi(N), f_xB(N), f_eta(N), f_xBtot(N);
     auto read_state = [&]() -> pfgb_status {
@@ -546,7 +602,7 @@ int main(int argc, char **argv) {
     wall.reserve(c.nsteps);
     const auto t0 = std::chrono::steady_clock::now();
     int rc = 0;
-    unsigned long long accepted_zm = 0;
+    unsigned long long accepted_zm = (unsigned long long)(first_step - 1);
     for (int step = 1; step <= c.nsteps && minimize; ++step) {
         pfgb_min_stats m;
         const auto a = std::chrono::steady_clock::now();
@@ -577,7 +633,7 @@ int main(int argc, char **argv) {
             break;
         }
     }
-    for (int step = 1; step <= c.nsteps && !minimize; ++step) {
+    for (int step = first_step; step <= c.nsteps && !minimize; ++step) {
         pfgb_step_stats s;
         const auto a = std::chrono::steady_clock::now();
         st = pfgb_step(ctx, 1, &s);
@@ -602,6 +658,11 @@ int main(int argc, char **argv) {
         if (step % c.out_every == 0) {
             if ((st = read_state()) != PFGB_OK) { rc = fail(st, "pfgb_read_fields"); break; }
             vtk_set(("_" + std::to_string(step)).c_str());
+        }
+        if (c.ckpt_every > 0 && (step % c.ckpt_every == 0 || step == c.nsteps)) {   // main_cuda.cu:33494-33560
+            st = pfgb_checkpoint_save(ctx, c.ckpt_path.c_str(), c.isc.c_str(), c.fsha.c_str(), c.psha.c_str());
+            if (st != PFGB_OK) { rc = fail(st, "PF zero-mode checkpoint write"); break; }
+            printf("PF_ZERO_MODE_CHECKPOINT_WRITTEN step=%d path=%s\n", step, c.ckpt_path.c_str());
         }
     }
     const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -80,6 +80,23 @@ class Solver:
                   "pfgb_minimize")
         return st
 
+    def checkpoint_save(self, path: str, initial_state_class=None, fixture_manifest_sha256=None,
+                        profile_library_manifest_sha256=None) -> None:
+        """pfgb_checkpoint_save: the reference's zero-mode checkpoint file."""
+        enc = lambda v: None if v is None else v.encode()
+        self._chk(self.lib.pfgb_checkpoint_save(self.ctx, path.encode(), enc(initial_state_class),
+                                                enc(fixture_manifest_sha256), enc(profile_library_manifest_sha256)),
+                  "pfgb_checkpoint_save")
+
+    def checkpoint_restore(self, path: str, initial_state_class=None, fixture_manifest_sha256=None,
+                           profile_library_manifest_sha256=None) -> None:
+        """pfgb_checkpoint_restore: continue from a zero-mode checkpoint."""
+        enc = lambda v: None if v is None else v.encode()
+        self._chk(self.lib.pfgb_checkpoint_restore(self.ctx, path.encode(), enc(initial_state_class),
+                                                   enc(fixture_manifest_sha256),
+                                                   enc(profile_library_manifest_sha256)),
+                  "pfgb_checkpoint_restore")
+
     def set_warm_start_model(self, model) -> None:
         """Attach a ``fno.WarmStartModel`` (None detaches); it is used when
         elastic_warm_start_source is 1 or 2."""

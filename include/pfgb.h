@@ -26,6 +26,14 @@
  *                             gpu_reduce_min_max, cuda_kernels.cu:5609-5942
  *   pfgb_fft3d_*           <- cufftExecD2Z/Z2D/R2C/C2R call sites,
  *                             main_cuda.cu:28163-28173 (own kernels, no cuFFT)
+ *   pfgb_checkpoint_*      <- pf_zero_mode::write_checkpoint / read_checkpoint
+ *                             (pf_zero_mode_checkpoint.h:80-95) and their use
+ *                             by main_cuda.cu:27340-28100 (restart) and
+ *                             33494-33560 (periodic write); same file format
+ *   pfgb_parameter_fingerprint, pfgb_elastic_solver_fingerprint
+ *                          <- pf_zero_mode_parameter_fingerprint /
+ *                             elastic_solver_parameter_fingerprint,
+ *                             main_cuda.cu:4187-4264
  *   pfgb_fno_*, pfgb_set_warm_start_model, pfgb_elastic_training_pair
  *                          <- no counterpart: a learned start for the
  *                             heterogeneous elastic iteration at the
@@ -387,6 +395,80 @@ pfgb_status pfgb_fft3d_c2r(int precision, int Nx, int Ny, int Nz,
 #define PFGB_NOALLOC_SCRATCH_BYTES 32768
 pfgb_status pfgb_fft3d_r2c_noalloc(int precision, int Nx, int Ny, int Nz,
                                    const void *d_in, void *d_out, void *cuda_stream);
+
+/* --- zero-mode checkpoints in the reference's file format ----------------
+ * V3 (no elastic state) and V4 (with the elastic warm state u_k) are
+ * written; V2, V3 and V4 are read.  The provenance is a restart identity:
+ * a file whose selectors, identities or fingerprints differ from the
+ * expected ones is rejected before any field is returned, and so is a file
+ * whose payload checksum (FNV-1a 64) does not match.  Text fields are
+ * NUL-terminated; selectors hold at most 63 characters, identities 95. */
+typedef struct pfgb_checkpoint_provenance {
+    char zero_mode[64];                 /* PF_CONSERVED_Y_ZERO_MODE_V1           */
+    char backend[64];                   /* HOST_NEWTON_BISECTION_V1              */
+    char composition_mode[64];          /* legacy                                */
+    char y_update_mode[64];             /* lagged_rhs                            */
+    char explicit_context[64];          /* SM_EXPLICIT_CONTEXT_N_V1              */
+    char reaction_discretization[64];   /* SM_TANGENT_N_V1                       */
+    char elastic_solver_mode[64];       /* ELASTIC_WARM_START_RESIDUAL_V1 or
+                                           ELASTIC_RUNTIME_STATE_NOT_REQUIRED    */
+    char initial_state_class[96];       /* --pf-initial-state-class (default
+                                           LEGACY_UNSPECIFIED), and the two
+                                           manifest hashes likewise              */
+    char fixture_manifest_sha256[96];
+    char profile_library_manifest_sha256[96];
+    uint64_t elastic_solver_fingerprint;   /* 0 without the accelerated solver */
+    uint64_t parameter_fingerprint;
+} pfgb_checkpoint_provenance;
+
+typedef struct pfgb_checkpoint_state {
+    uint64_t accepted_step;
+    int32_t nx, ny, nz;
+    int32_t elastic_present;            /* 1: V4 with the warm state            */
+    double dt_code, temperature_K;
+    /* zero-mode runtime state */
+    double target_mass_code, last_lambda, last_residual_code, last_derivative_code;
+    uint64_t last_iterations, accepted_zero_mode_steps;
+    /* elastic warm state: the converged u_k used at the start of step
+       accepted_step, i.e. of the fields after step accepted_step - 1 */
+    uint64_t elastic_source_field_step, elastic_last_iterations;
+    double elastic_last_relative_residual;
+    pfgb_checkpoint_provenance provenance;
+    /* caller-owned host buffers: N = nx*ny*nz float64 each, and
+       6 * nx*ny*(nz/2+1) floats (ux_k | uy_k | uz_k, interleaved re/im) */
+    double *phi, *Y, *xB, *dY_dt_prev;
+    float *displacement_k;
+} pfgb_checkpoint_state;
+
+uint64_t pfgb_fnv1a64(const void *data, size_t size, uint64_t seed);
+uint64_t pfgb_parameter_fingerprint(const pfgb_params *p);
+uint64_t pfgb_elastic_solver_fingerprint(const pfgb_params *p);
+/* The provenance the reference builds for these parameters
+ * (main_cuda.cu:24721-24743); NULL identities mean LEGACY_UNSPECIFIED. */
+pfgb_status pfgb_checkpoint_provenance_for(const pfgb_params *p, const char *initial_state_class,
+                                           const char *fixture_manifest_sha256,
+                                           const char *profile_library_manifest_sha256,
+                                           pfgb_checkpoint_provenance *out);
+/* Host-buffer level: validate and write atomically (<path>.tmp, rename). */
+pfgb_status pfgb_checkpoint_write_file(const char *path, const pfgb_checkpoint_state *state);
+/* Header only: version (2, 3, 4), grid and whether the elastic state is present. */
+pfgb_status pfgb_checkpoint_peek(const char *path, int32_t *version, int32_t *nx, int32_t *ny, int32_t *nz,
+                                 int32_t *elastic_present);
+/* Read into the caller's buffers; state->nx/ny/nz must give the file's grid. */
+pfgb_status pfgb_checkpoint_read_file(const char *path, const pfgb_checkpoint_provenance *expected,
+                                      pfgb_checkpoint_state *state);
+/* Context level (zero mode on, two_phase): write the state after the last
+ * step (V4 when the accelerated elastic solver runs), or restore one --
+ * fields, zero-mode target and runtime, the elastic warm state and the step
+ * count -- after checking grid, dt and temperature and that the restored
+ * field's mass ledger matches the frozen target to 1e-12 relative
+ * (main_cuda.cu:27342-27365, 28069-28100). */
+pfgb_status pfgb_checkpoint_save(pfgb_ctx *ctx, const char *path, const char *initial_state_class,
+                                 const char *fixture_manifest_sha256,
+                                 const char *profile_library_manifest_sha256);
+pfgb_status pfgb_checkpoint_restore(pfgb_ctx *ctx, const char *path, const char *initial_state_class,
+                                    const char *fixture_manifest_sha256,
+                                    const char *profile_library_manifest_sha256);
 
 /* --- learned start of the heterogeneous elastic iteration ------------- */
 /* No counterpart in the reference, which starts each solve from the

@@ -50,6 +50,13 @@ def test_cli_rejects_bad_inputs(capi, tmp_path):
     r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf,
                     "--elastic-warm-start-source", "2"], tmp_path)
     assert r.returncode == 2 and "--elastic-warm-start-model" in r.stderr
+    # checkpoints need the zero mode and a path
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf,
+                    "--pf-checkpoint-every", "1", "--pf-checkpoint-path", "x.ckpt"], tmp_path)
+    assert r.returncode == 2 and "PF_CONSERVED_Y_ZERO_MODE_V1" in r.stderr
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf,
+                    "--pf-zero-mode", "PF_CONSERVED_Y_ZERO_MODE_V1", "--pf-checkpoint-every", "1"], tmp_path)
+    assert r.returncode == 2 and "--pf-checkpoint-path" in r.stderr
     # malformed parameter file
     pbad = tmp_path / "bad.params"
     pbad.write_text(open(pf).read() + "\nW=abc\n")
@@ -162,3 +169,56 @@ def test_cli_learned_start(capi, tmp_path):
     rows = (tmp_path / "R" / run / "raw_fields_relax" / "elastic_solver_trace.csv").read_text().strip().split("\n")
     assert len(rows) == steps + 1
     assert all(row.split(",")[1] == "2" for row in rows[1:])
+
+
+@pytest.mark.gpu
+def test_cli_checkpoint_restart(capi, tmp_path):
+    """--pf-checkpoint-every / --pf-restart-from: two steps, a checkpoint,
+    a restarted run to step 4; its final checkpoint holds the same fields
+    as an uninterrupted 4-step run's."""
+    import ctypes
+    from cuda_sto_pf_gb300 import workloads
+    n = 16
+    w = workloads.single_sphere(n=n, radius=5.0)
+    w["phi"].tofile(tmp_path / "phi.raw")
+    w["xB"].tofile(tmp_path / "xB.raw")
+    pf = os.path.join(GOLDEN, "c2.params")
+    base = [str(n), str(n), str(n), "0.01", "STEPS", "10", "1", "1", "--pf-param-file", pf, "--init-mode",
+            "raw_fields", "--init-phi-raw", str(tmp_path / "phi.raw"), "--init-xB-raw", str(tmp_path / "xB.raw"),
+            "--pf-zero-mode", "PF_CONSERVED_Y_ZERO_MODE_V1", "--pf-initial-state-class", "SPHERE_16"]
+
+    def run(steps, root, extra):
+        args = [steps if a == "STEPS" else a for a in base] + extra
+        r = _run(capi, args, tmp_path, env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / root)})
+        assert r.returncode == 0, r.stderr
+        return r
+
+    run("2", "A", ["--pf-checkpoint-every", "2", "--pf-checkpoint-path", str(tmp_path / "s2.ckpt")])
+    r = run("4", "B", ["--pf-restart-from", str(tmp_path / "s2.ckpt"), "--pf-checkpoint-every", "4",
+                       "--pf-checkpoint-path", str(tmp_path / "b4.ckpt")])
+    assert "accepted_step=2" in r.stdout
+    run("4", "C", ["--pf-checkpoint-every", "4", "--pf-checkpoint-path", str(tmp_path / "c4.ckpt")])
+    # a restart with another identity is refused
+    args = [("4" if a == "STEPS" else a) for a in base] + ["--pf-restart-from", str(tmp_path / "s2.ckpt")]
+    args[args.index("SPHERE_16")] = "OTHER"
+    r = _run(capi, args, tmp_path, env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "D")})
+    assert r.returncode == 2 and "rejected" in r.stderr
+    lib = capi.load()
+    p = params_for(capi, "c2.params", n=n, zero_mode_enabled=1)
+    out = {}
+    for tag in ("b4", "c4"):
+        st = capi.CkptState()
+        st.nx = st.ny = st.nz = n
+        buf = {k: np.zeros(n ** 3) for k in ("phi", "Y", "xB", "dY")}
+        u = np.zeros(6 * n * n * (n // 2 + 1), dtype=np.float32)
+        st.phi, st.Y, st.xB, st.dY_dt_prev = (buf[k].ctypes.data for k in ("phi", "Y", "xB", "dY"))
+        st.displacement_k = u.ctypes.data
+        prov = capi.CkptProvenance()
+        capi.check(lib.pfgb_checkpoint_provenance_for(ctypes.byref(p), b"SPHERE_16", None, None, ctypes.byref(prov)),
+                   "provenance")
+        capi.check(lib.pfgb_checkpoint_read_file(str(tmp_path / (tag + ".ckpt")).encode(), ctypes.byref(prov),
+                                                 ctypes.byref(st)), "read " + tag)
+        assert st.accepted_step == 4 and st.elastic_source_field_step == 3
+        out[tag] = buf
+    for k in ("phi", "Y", "xB", "dY"):
+        assert np.abs(out["b4"][k] - out["c4"][k]).max() <= 1e-12 * max(1.0, np.abs(out["c4"][k]).max()), k

