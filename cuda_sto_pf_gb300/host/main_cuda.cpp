@@ -24,11 +24,18 @@
 #include <cstring>
 #include <ctime>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "pfgb.h"
 
 namespace {
+
+// field output: ASCII VTK (the reference's format and the default), legacy
+// binary VTK (big-endian float64, the same point order), or raw float64 in
+// the C order [Nx][Ny][Nz] that --init-*-raw reads
+enum class OutFmt { VtkAscii, VtkBinary, Raw };
+OutFmt g_out_fmt = OutFmt::VtkAscii;
 
 struct Cli {
     int pos_Nx = -1, pos_Ny = -1, pos_Nz = -1, nsteps = 100, out_every = 100, csv_out_every = 10;
@@ -94,6 +101,8 @@ void usage() {
            "  --pf-restart-from <f>           continue from a zero-mode checkpoint\n"
            "  --pf-initial-state-class <s>  --pf-fixture-manifest-sha256 <s>\n"
            "  --pf-profile-library-manifest-sha256 <s>   restart identity (default LEGACY_UNSPECIFIED)\n"
+           "  --output-format vtk|vtk-binary|raw  field files: ASCII VTK (default), legacy binary VTK\n"
+           "                                  (big-endian float64) or raw float64 C-order (*.raw)\n"
            "  --elastic-warm-start-model <f>  model file (pfgb_fno_save) for the elastic start\n"
            "  --elastic-warm-start-source <n> 0 previous step (default), 1 model at cold starts,\n"
            "                                  2 model every step, 3 cold every step\n");
@@ -180,6 +189,12 @@ Cli parse(int argc, char **argv) {
                  (v = flag_value(argc, argv, &i, "--pf_fixture_manifest_sha256"))) c.fsha = v;
         else if ((v = flag_value(argc, argv, &i, "--pf-profile-library-manifest-sha256")) ||
                  (v = flag_value(argc, argv, &i, "--pf_profile_library_manifest_sha256"))) c.psha = v;
+        else if ((v = flag_value(argc, argv, &i, "--output-format"))) {
+            if (!strcmp(v, "vtk")) g_out_fmt = OutFmt::VtkAscii;
+            else if (!strcmp(v, "vtk-binary")) g_out_fmt = OutFmt::VtkBinary;
+            else if (!strcmp(v, "raw")) g_out_fmt = OutFmt::Raw;
+            else bad(a, v);
+        }
         else if ((v = flag_value(argc, argv, &i, "--elastic-warm-start-model"))) c.warm_model = v;
         else if ((v = flag_value(argc, argv, &i, "--elastic-warm-start-source"))) {
             if (!to_int(v, &c.warm_source) || c.warm_source < 0 || c.warm_source > 3) bad(a, v);
@@ -287,28 +302,54 @@ bool copy_file(const std::string &from, const std::string &to) {
 }
 
 // ASCII STRUCTURED_POINTS, z outermost, x innermost, %.5f (io_vtk_cuda.h:80-128)
-bool write_vtk(const std::string &path, const char *name, const std::vector<double> &v, int Nx, int Ny, int Nz) {
-    FILE *fo = fopen(path.c_str(), "w");
+bool write_vtk(const std::string &vtk_path, const char *name, const std::vector<double> &v, int Nx, int Ny, int Nz,
+               int step = -1) {
+    const char *sup = getenv("CUDA_STO_SUPPRESS_VTK_OUTPUT");   // io_vtk_cuda.h:17-45
+    if (sup && strcmp(sup, "1") == 0) {
+        printf("VTK_OUTPUT_SUPPRESSED field=%s step=%d path=%s\n", name, step, vtk_path.c_str());
+        return true;
+    }
+    std::string path = vtk_path;
+    if (g_out_fmt == OutFmt::Raw && path.size() > 4 && path.compare(path.size() - 4, 4, ".vtk") == 0)
+        path = path.substr(0, path.size() - 4) + ".raw";
+    FILE *fo = fopen(path.c_str(), g_out_fmt == OutFmt::VtkAscii ? "w" : "wb");
     if (!fo) { fprintf(stderr, "ERROR: Cannot create file %s\n", path.c_str()); return false; }
+    bool ok = true;
+    if (g_out_fmt == OutFmt::Raw) {
+        ok = fwrite(v.data(), sizeof(double), v.size(), fo) == v.size();
+        return (fclose(fo) == 0) && ok;
+    }
     const int ny_out = Ny == 2 ? 1 : Ny;
-    fprintf(fo, "# vtk DataFile Version 3.0\nPhase Field Simulation\nASCII\nDATASET STRUCTURED_POINTS\n");
+    const bool bin = g_out_fmt == OutFmt::VtkBinary;
+    fprintf(fo, "# vtk DataFile Version 3.0\nPhase Field Simulation\n%s\nDATASET STRUCTURED_POINTS\n",
+            bin ? "BINARY" : "ASCII");
     fprintf(fo, "DIMENSIONS %d %d %d\nASPECT_RATIO 1 1 1\nORIGIN 0 0 0\nPOINT_DATA %d\n", Nx, ny_out, Nz,
             Nx * ny_out * Nz);
     fprintf(fo, "SCALARS %s double 1\nLOOKUP_TABLE default\n", name);
     std::string line;
     char tmp[64];
+    std::vector<unsigned char> row((size_t)Nx * 8);
     for (int k = 0; k < Nz; ++k)
         for (int j = 0; j < ny_out; ++j) {
+            if (bin) {
+                for (int i = 0; i < Nx; ++i) {   // big-endian, as legacy VTK binary requires
+                    uint64_t u;
+                    const double d = v[((size_t)i * Ny + j) * Nz + k];
+                    memcpy(&u, &d, 8);
+                    for (int b = 0; b < 8; ++b) row[(size_t)i * 8 + b] = (unsigned char)(u >> (56 - 8 * b));
+                }
+                ok = ok && fwrite(row.data(), 1, row.size(), fo) == row.size();
+                continue;
+            }
             line.clear();
             for (int i = 0; i < Nx; ++i) {
                 const int n = snprintf(tmp, sizeof(tmp), "%.5f ", v[((size_t)i * Ny + j) * Nz + k]);
                 line.append(tmp, n);
             }
-            fwrite(line.data(), 1, line.size(), fo);
+            ok = ok && fwrite(line.data(), 1, line.size(), fo) == line.size();
         }
     fprintf(fo, "\n");
-    fclose(fo);
-    return true;
+    return (fclose(fo) == 0) && ok;
 }
 
 double h_of(double p) { return p * p * p * (6.0 * p * p - 15.0 * p + 10.0); }
@@ -520,15 +561,23 @@ int main(int argc, char **argv) {
     auto read_state = [&]() -> pfgb_status {
         return pfgb_read_fields(ctx, f_phi.data(), f_xB.data(), nullptr, gp ? f_eta.data() : nullptr, nullptr);
     };
-    auto vtk_set = [&](const char *suffix) -> bool {
+    auto vtk_set = [&](const char *suffix, int step) -> bool {
         for (size_t i = 0; i < N; ++i) {
             const double h = h_of(f_phi[i]);
             f_xBtot[i] = (1.0 - h) * f_xB[i] + h * P.v_B;
         }
-        bool ok = write_vtk(case_dir + "/xBtot" + suffix + ".vtk", "xB_tot", f_xBtot, P.Nx, P.Ny, P.Nz);
-        ok &= write_vtk(case_dir + "/xB" + suffix + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
-        ok &= write_vtk(case_dir + "/phi" + suffix + ".vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
-        if (gp) ok &= write_vtk(case_dir + "/eta" + suffix + ".vtk", "eta", f_eta, P.Nx, P.Ny, P.Nz);
+        // the fields of one output set are written in parallel
+        struct Job { std::string path; const char *name; const std::vector<double> *v; bool ok; };
+        std::vector<Job> jobs = {{case_dir + "/xBtot" + suffix + ".vtk", "xB_tot", &f_xBtot, false},
+                                 {case_dir + "/xB" + suffix + ".vtk", "xB", &f_xB, false},
+                                 {case_dir + "/phi" + suffix + ".vtk", "phi", &f_phi, false}};
+        if (gp) jobs.push_back({case_dir + "/eta" + suffix + ".vtk", "eta", &f_eta, false});
+        std::vector<std::thread> th;
+        for (Job &j : jobs)
+            th.emplace_back([&j, &P, step]() { j.ok = write_vtk(j.path, j.name, *j.v, P.Nx, P.Ny, P.Nz, step); });
+        for (std::thread &t : th) t.join();
+        bool ok = true;
+        for (const Job &j : jobs) ok = ok && j.ok;
         return ok;
     };
 
@@ -593,7 +642,7 @@ int main(int argc, char **argv) {
         write_vtk(case_dir + "/phi_init_" + tag + ".vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
         write_vtk(case_dir + "/xB_init_" + tag + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
     } else {
-        vtk_set("_init");
+        vtk_set("_init", 0);
         write_vtk(case_dir + "/xB_0.vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
     }
     if ((st = csv_row(0, NAN)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_diagnostics"); }
@@ -657,7 +706,7 @@ int main(int argc, char **argv) {
         if (step % c.csv_out_every == 0 && (st = csv_row(step, NAN)) != PFGB_OK) { rc = fail(st, "pfgb_diagnostics"); break; }
         if (step % c.out_every == 0) {
             if ((st = read_state()) != PFGB_OK) { rc = fail(st, "pfgb_read_fields"); break; }
-            vtk_set(("_" + std::to_string(step)).c_str());
+            vtk_set(("_" + std::to_string(step)).c_str(), step);
         }
         if (c.ckpt_every > 0 && (step % c.ckpt_every == 0 || step == c.nsteps)) {   // main_cuda.cu:33494-33560
             st = pfgb_checkpoint_save(ctx, c.ckpt_path.c_str(), c.isc.c_str(), c.fsha.c_str(), c.psha.c_str());
@@ -672,7 +721,7 @@ int main(int argc, char **argv) {
             write_vtk(case_dir + "/phi_final_" + tag + ".vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
             write_vtk(case_dir + "/xB_final_" + tag + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
         } else {
-            vtk_set("_final");
+            vtk_set("_final", c.nsteps);
         }
     }
     if (csv) fclose(csv);

@@ -222,3 +222,36 @@ def test_cli_checkpoint_restart(capi, tmp_path):
         out[tag] = buf
     for k in ("phi", "Y", "xB", "dY"):
         assert np.abs(out["b4"][k] - out["c4"][k]).max() <= 1e-12 * max(1.0, np.abs(out["c4"][k]).max()), k
+
+
+@pytest.mark.gpu
+def test_cli_output_formats(capi, tmp_path):
+    """--output-format vtk-binary / raw beside the default ASCII VTK, and the
+    reference's CUDA_STO_SUPPRESS_VTK_OUTPUT switch."""
+    from cuda_sto_pf_gb300 import workloads
+    n = 16
+    w = workloads.single_sphere(n=n, radius=5.0)
+    w["phi"].tofile(tmp_path / "phi.raw")
+    w["xB"].tofile(tmp_path / "xB.raw")
+    pf = os.path.join(GOLDEN, "c2.params")
+    base = [str(n), str(n), str(n), "0.01", "2", "10", "1", "1", "--pf-param-file", pf, "--init-mode", "raw_fields",
+            "--init-phi-raw", str(tmp_path / "phi.raw"), "--init-xB-raw", str(tmp_path / "xB.raw")]
+    dirs = {}
+    for fmt in ("vtk", "vtk-binary", "raw"):
+        r = _run(capi, base + ["--output-format", fmt], tmp_path, env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / fmt)})
+        assert r.returncode == 0, r.stderr
+        run = os.listdir(tmp_path / fmt)[0]
+        dirs[fmt] = tmp_path / fmt / run / "raw_fields_relax"
+    raw = np.fromfile(dirs["raw"] / "phi_final.raw", dtype=np.float64).reshape(n, n, n)
+    blob = (dirs["vtk-binary"] / "phi_final.vtk").read_bytes()
+    head = b"LOOKUP_TABLE default\n"
+    data = np.frombuffer(blob[blob.index(head) + len(head):][:8 * n ** 3], dtype=">f8")
+    assert blob[blob.index(b"Simulation\n") + 11:].startswith(b"BINARY\n")
+    assert np.array_equal(data.reshape(n, n, n).transpose(2, 1, 0), raw)   # z outer, x inner
+    asc = _vtk_values(dirs["vtk"] / "phi_final.vtk", (n, n, n))
+    assert np.abs(asc - raw).max() <= 5.1e-6
+    assert (dirs["raw"] / "xBtot_final.raw").exists() and not (dirs["raw"] / "phi_final.vtk").exists()
+    r = _run(capi, base, tmp_path, env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "S"), "CUDA_STO_SUPPRESS_VTK_OUTPUT": "1"})
+    assert r.returncode == 0 and "VTK_OUTPUT_SUPPRESSED field=phi" in r.stdout
+    run = os.listdir(tmp_path / "S")[0]
+    assert not any(f.endswith(".vtk") for f in os.listdir(tmp_path / "S" / run / "raw_fields_relax"))
