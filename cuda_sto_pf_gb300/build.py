@@ -35,7 +35,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE,
               "--expt-relaxed-constexpr"] + ARCH
 
-CU_SOURCES = ["solver.cu", "params.cu", "paramfile.cpp", "batch.cpp", "fno.cu", "checkpoint.cpp"]
+CU_SOURCES = ["solver.cu", "params.cu", "paramfile.cpp", "batch.cpp", "fno.cu", "checkpoint.cpp", "init.cu"]
 HEADERS = ["common.cuh", "fft.cuh", "fft246.cuh", "physics.cuh", "rader41.cuh"]
 
 

@@ -75,6 +75,11 @@ class Params(Structure):
         ("gamma_Jm2", c_double), ("lambda_sm_m", c_double), ("Vm_alpha_0_phys_m3mol", c_double),
         ("ic_23d_xB_out", c_double), ("ic_phi_seed_radius", c_double), ("minimize_min_pseudo_time", c_double),
         ("ic_phi_num_seeds", c_int32), ("elastic_warm_start_source", c_int32),
+        ("init_shape_mode", c_int32), ("init_use_rotation", c_int32),
+        ("init_axis_ratio_rx", c_double), ("init_axis_ratio_ry", c_double), ("init_axis_ratio_rz", c_double),
+        ("init_tilt_theta_deg", c_double), ("init_tilt_phi_deg", c_double),
+        ("init_center_shift_x", c_double), ("init_center_shift_y", c_double), ("init_center_shift_z", c_double),
+        ("init_phi_noise_amp", c_double), ("init_phi_noise_seed", ctypes.c_uint64), ("seed", ctypes.c_uint64),
         ("temperature_K", c_double), ("mu0_compound", c_double), ("xB_eq_matrix", c_double),
     ]
 
@@ -169,6 +174,8 @@ EXPORTS = [
     ("pfgb_step", c_int, [c_void_p, c_int, POINTER(StepStats)]),
     ("pfgb_minimize", c_int, [c_void_p, c_int, c_int, POINTER(MinStats)]),
     ("pfgb_batch_minimize", c_int, [POINTER(Case), c_int, c_int, c_int]),
+    ("pfgb_init_fields", c_int, [c_void_p]),
+    ("pfgb_seed_fields", c_int, [POINTER(Params), c_int, c_void_p, c_void_p]),
     ("pfgb_read_fields", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("pfgb_read_elastic", c_int, [c_void_p, c_void_p, c_void_p]),
     ("pfgb_read_displacement_k", c_int, [c_void_p, c_void_p]),

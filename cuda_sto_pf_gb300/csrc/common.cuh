@@ -206,6 +206,9 @@ PFGB_HD T logit_clip(T xB, T eps, T Yc) {
 
 void pfgb_set_error(const char *what, cudaError_t e, const char *file, int line);
 void pfgb_set_error_msg(const char *fmt, ...);
+// seeded initial fields (init.cu): phi and xB into device buffers; scratch 2 * 304 doubles
+pfgb_status pfgb_seed_fields_device(const pfgb_params *p, double *d_phi, double *d_xB, double *d_scratch,
+                                    cudaStream_t stream);
 // learned elastic start (fno.cu): device of a model and kernel launches of one forward
 int pfgb_fno_device(const pfgb_fno *f);
 long long pfgb_fno_forward_launches(const pfgb_fno *f);

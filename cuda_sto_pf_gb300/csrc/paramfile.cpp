@@ -84,6 +84,11 @@ const DKey kDoubles[] = {
     DK("Vm_alpha_0_phys_m3mol", Vm_alpha_0_phys_m3mol),
     DK("ic_23d_xB_out", ic_23d_xB_out), DK("xB_alpha_initial", ic_23d_xB_out),
     DK("ic_phi_seed_radius", ic_phi_seed_radius), DK("minimize_min_pseudo_time", minimize_min_pseudo_time),
+    DK("init_axis_ratio_rx", init_axis_ratio_rx), DK("init_axis_ratio_ry", init_axis_ratio_ry),
+    DK("init_axis_ratio_rz", init_axis_ratio_rz), DK("init_tilt_theta_deg", init_tilt_theta_deg),
+    DK("init_tilt_phi_deg", init_tilt_phi_deg), DK("init_center_shift_x", init_center_shift_x),
+    DK("init_center_shift_y", init_center_shift_y), DK("init_center_shift_z", init_center_shift_z),
+    DK("init_phi_noise_amp", init_phi_noise_amp),
 };
 const DKey kInts[] = {
     DK("pf_params_schema_version", pf_params_schema_version),
@@ -104,13 +109,14 @@ const DKey kInts[] = {
     DK("minimize_post_projection_iters", minimize_post_projection_iters),
     DK("minimize_max_iter", minimize_max_iter), DK("minimize_convergence_steps", minimize_convergence_steps),
     DK("ic_phi_num_seeds", ic_phi_num_seeds),
+    DK("init_shape_mode", init_shape_mode), DK("init_use_rotation", init_use_rotation),
 };
 #undef DK
 
 // keys of the reference schema that do not drive this path (GP/event
 // engines, converter provenance): accepted without a warning
 const char *kKnownUnused[] = {
-    "seed", "gp_W_eta_phys", "gp_kappa_eta_phys", "gp_L_eta_phys", "gp_gamma_alpha_gp", "gp_l_eta_nm",
+    "gp_W_eta_phys", "gp_kappa_eta_phys", "gp_L_eta_phys", "gp_gamma_alpha_gp", "gp_l_eta_nm",
     "gp_D_ratio", "gp_reaction_nu_A", "gp_reaction_nu_B", "gp_xB_eq_alpha_for_eta",
     "gp_M_eta_ratio_to_crit", "gp_M_eta_phys", "gp_delta_g_stab",
 };
@@ -177,6 +183,14 @@ extern "C" pfgb_status pfgb_params_set(pfgb_params *p, const char *key, const ch
     } else if (!strncmp(key, "S_", 2)) {
         int v = voigt21(key + 2);
         if (v >= 0) return parse_double(value, &p->S[v]) ? PFGB_OK : PFGB_ERR_INVALID;
+    }
+    if (!strcmp(key, "seed") || !strcmp(key, "init_phi_noise_seed")) {   // unsigned long (TRY_SET_ULONG)
+        char *e = nullptr;
+        errno = 0;
+        const unsigned long long v = strtoull(value, &e, 10);
+        if (e == value || *e != '\0' || errno != 0 || value[0] == '-') return PFGB_ERR_INVALID;
+        (!strcmp(key, "seed") ? p->seed : p->init_phi_noise_seed) = (uint64_t)v;
+        return PFGB_OK;
     }
     if (!strcmp(key, "model_mode")) {
         if (!strcmp(value, "two_phase")) { p->model_mode = PFGB_MODEL_TWO_PHASE; return PFGB_OK; }

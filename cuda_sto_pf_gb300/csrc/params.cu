@@ -136,6 +136,11 @@ void pfgb_params_default(pfgb_params *p) {
     p->ic_23d_xB_out = 0.03;        // params_default, main_cuda.cu:16215
     p->ic_phi_seed_radius = 10.0;   // main_cuda.cu:16221
     p->ic_phi_num_seeds = 1;
+    // seeded initialisation (main_cuda.cu:16226-16238, 15791)
+    p->init_shape_mode = -1;
+    p->init_use_rotation = 0;
+    p->init_axis_ratio_rx = p->init_axis_ratio_ry = p->init_axis_ratio_rz = 1.0;
+    p->seed = 12345;
     p->minimize_rms_dphi_threshold = 1.0e-6;
     p->minimize_rms_dY_threshold = 5.0e-5;
     p->minimize_energy_diff_rel_threshold = 1.0e-9;

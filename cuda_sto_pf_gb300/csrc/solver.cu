@@ -2931,6 +2931,16 @@ pfgb_status pfgb_elastic_training_pair(pfgb_ctx *c, float *d_in8, float *d_targe
                                             : training_pair<float>(c, d_in8, d_target3, sp);
 }
 
+pfgb_status pfgb_init_fields(pfgb_ctx *c) {
+    if (!c) return PFGB_ERR_INVALID;
+    PFGB_CUDA_TRY(cudaSetDevice(c->device));
+    TRY(ensure_stage(c));
+    double *dp = c->stage, *dx = c->stage + c->g.N;
+    TRY(pfgb_seed_fields_device(&c->p, dp, dx, c->partials, c->stream));
+    return c->p.precision == PFGB_PREC_FP64 ? load_device<double>(c, dp, dx, nullptr, nullptr, false)
+                                            : load_device<float>(c, dp, dx, nullptr, nullptr, false);
+}
+
 pfgb_status pfgb_checkpoint_save(pfgb_ctx *c, const char *path, const char *initial_state_class,
                                  const char *fixture_manifest_sha256,
                                  const char *profile_library_manifest_sha256) {

@@ -55,6 +55,10 @@ struct Cli {
     std::string warm_model;   // learned start of the elastic iteration (no reference counterpart)
     int warm_source = -1;
     // zero-mode checkpoints (main_cuda.cu:22715-22760)
+    // seeded initialisation flags, applied as parameter keys (main_cuda.cu:23915-23972)
+    std::vector<std::pair<std::string, std::string>> init_sets;
+    bool tilt_given = false;
+    double radius_nm = NAN;
     int ckpt_every = 0;
     std::string ckpt_path, restart_from;
     std::string isc = "LEGACY_UNSPECIFIED", fsha = "LEGACY_UNSPECIFIED", psha = "LEGACY_UNSPECIFIED";
@@ -82,6 +86,10 @@ void usage() {
            "  --elastic 0|1                   override elastic\n"
            "  --temperature-C <val>\n"
            "  --init-mode raw_fields          initialize from raw phi/xB[/eta][/dY_dt_prev] fields\n"
+           "                                  (without it: seeded fields, --radius / --radius-phys-nm,\n"
+           "                                  --init-shape sphere|ellipsoid, --init-axis-ratio-r{x,y,z},\n"
+           "                                  --init-tilt-{theta,phi}-deg, --init-center-shift-{x,y,z},\n"
+           "                                  --init-phi-noise-amp/-seed, --seed, --ic-23d-xB-out)\n"
            "  --init-phi-raw <path>           float64, C order, idx=i*(Ny*Nz)+j*Nz+k\n"
            "  --init-xB-raw <path>\n"
            "  --init-eta-raw <path>           optional (default zero)\n"
@@ -215,6 +223,25 @@ Cli parse(int argc, char **argv) {
         else if ((v = flag_value(argc, argv, &i, "--minimize-min-pseudo-time"))) { if (!to_double(v, &c.min_pt)) bad(a, v); }
         else if ((v = flag_value(argc, argv, &i, "--minimize-xB-max-safe"))) { if (!to_double(v, &c.xB_max_safe)) bad(a, v); }
         else if ((v = flag_value(argc, argv, &i, "--radius"))) { if (!to_double(v, &c.radius) || c.radius < 0) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--radius-phys-nm"))) { if (!to_double(v, &c.radius_nm) || c.radius_nm < 0) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--init-shape"))) {
+            if (!strcmp(v, "sphere")) c.init_sets.push_back({"init_shape_mode", "0"});
+            else if (!strcmp(v, "ellipsoid")) c.init_sets.push_back({"init_shape_mode", "1"});
+            else bad(a, v);
+        }
+        else if (!strncmp(a, "--init-axis-ratio-r", 19) || !strncmp(a, "--init-center-shift-", 20) ||
+                 !strncmp(a, "--init-tilt-", 12) || !strncmp(a, "--init-phi-noise-", 17) ||
+                 !strcmp(a, "--seed") || !strncmp(a, "--seed=", 7) || !strncmp(a, "--ic-23d-xB-out", 15)) {
+            // --init-axis-ratio-rx -> init_axis_ratio_rx, --ic-23d-xB-out -> ic_23d_xB_out, ...
+            std::string flag = a;
+            const size_t eq = flag.find('=');
+            if (eq != std::string::npos) flag = flag.substr(0, eq);
+            v = flag_value(argc, argv, &i, flag.c_str());
+            std::string key = flag.substr(2);
+            for (char &ch : key) if (ch == '-') ch = '_';
+            c.init_sets.push_back({key, v ? v : ""});
+            if (!strncmp(key.c_str(), "init_tilt_", 10)) c.tilt_given = true;
+        }
         else fprintf(stderr, "[warn] unknown flag ignored: %s\n", a);
     }
     return c;
@@ -428,9 +455,17 @@ int main(int argc, char **argv) {
         if (c.min_post_iters >= 0) P.minimize_post_projection_iters = c.min_post_iters;
         if (std::isfinite(c.min_pt)) P.minimize_min_pseudo_time = c.min_pt;
         if (std::isfinite(c.xB_max_safe)) P.minimize_xB_max_safe = c.xB_max_safe;
-        if (std::isfinite(c.radius)) P.ic_phi_seed_radius = c.radius;
         c.nsteps = P.minimize_max_iter;   // main_cuda.cu:24432-24435
         P.dt = P.minimize_dt;
+    }
+    if (std::isfinite(c.radius)) P.ic_phi_seed_radius = c.radius;
+    for (const auto &kv : c.init_sets)
+        if (pfgb_params_set(&P, kv.first.c_str(), kv.second.c_str()) != PFGB_OK) bad(kv.first.c_str(), kv.second.c_str());
+    if (c.tilt_given && (P.init_tilt_theta_deg != 0.0 || P.init_tilt_phi_deg != 0.0)) P.init_use_rotation = 1;
+    if (std::isfinite(c.radius_nm)) {   // main_cuda.cu:25288-25310: physical radius -> code units
+        const double dxp = P.ic_phi_iface_w > 1e-30 ? P.lambda_sm_m / (2.0 * P.ic_phi_iface_w) : P.dx * 1e-9;
+        const double u2m = std::fabs(P.dx) > 1e-30 ? dxp / P.dx : 1e-9;
+        P.ic_phi_seed_radius = c.radius_nm * 1e-9 / u2m;
     }
     if (c.nsteps < 0 || c.out_every <= 0 || c.csv_out_every <= 0) {
         fprintf(stderr, "[fatal] nsteps >= 0, out_every > 0 and csv_out_every > 0 are required\n");
@@ -464,16 +499,19 @@ int main(int argc, char **argv) {
     // ---- initial fields ---------------------------------------------------
     const size_t N = (size_t)P.Nx * P.Ny * P.Nz;
     std::vector<double> phi, xB, eta, dYdt;
-    if (restarting) {
-        // the fields come from the checkpoint (main_cuda.cu:27340-27380)
+    const bool seeded = !restarting && c.init_mode.empty();
+    if (restarting || seeded) {
+        // the fields come from the checkpoint (main_cuda.cu:27340-27380) or
+        // from the seeded initialiser on the device (main_cuda.cu:15157-15430)
     } else if (c.init_mode != "raw_fields") {
-        fprintf(stderr, "[fatal] this build initialises from --init-mode raw_fields only\n");
+        fprintf(stderr, "[fatal] unknown --init-mode %s (raw_fields, or none for the seeded initialiser)\n",
+                c.init_mode.c_str());
         return 2;
     } else if (c.init_phi.empty() || c.init_xB.empty()) {
         fprintf(stderr, "[fatal] raw_fields needs --init-phi-raw and --init-xB-raw\n");
         return 2;
     }
-    if (!restarting) {
+    if (!restarting && !seeded) {
         if (!read_raw(c.init_phi, N, &phi) || !read_raw(c.init_xB, N, &xB)) return 2;
         if (!c.init_eta.empty() && !read_raw(c.init_eta, N, &eta)) return 2;
         if (!c.init_dYdt.empty() && !read_raw(c.init_dYdt, N, &dYdt)) return 2;
@@ -516,7 +554,15 @@ int main(int argc, char **argv) {
     const std::string out_dir = root + "/" + name;
     mkdir(out_dir.c_str(), 0755);
     copy_file(c.param_file, out_dir + "/pf_input.params");
-    const std::string tag = c.case_tag.empty() ? "raw_fields_relax" : c.case_tag;
+    std::string tag = c.case_tag;
+    if (tag.empty() && seeded) {   // main_cuda.cu:25425-25436
+        char t[256];
+        snprintf(t, sizeof(t), "case_test%d_%s_th%.0f_ph%.0f_noise%.0e", -1,
+                 P.init_shape_mode == 0 ? "sphere" : P.init_shape_mode == 1 ? "ellipsoid" : "legacy",
+                 P.init_tilt_theta_deg, P.init_tilt_phi_deg, P.init_phi_noise_amp);
+        tag = t;
+    }
+    if (tag.empty()) tag = "raw_fields_relax";
     const std::string case_dir = out_dir + "/" + tag;
     mkdir(case_dir.c_str(), 0755);
     copy_file(c.param_file, case_dir + "/pf_input.params");
@@ -551,6 +597,8 @@ int main(int argc, char **argv) {
         }
         first_step = s0.step + 1;
         printf("PF_ZERO_MODE_RESTART checkpoint=%s accepted_step=%d\n", c.restart_from.c_str(), s0.step);
+    } else if (seeded) {
+        if ((st = pfgb_init_fields(ctx)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_init_fields"); }
     } else {
         st = pfgb_load_fields(ctx, phi.data(), xB.data(), eta.empty() ? nullptr : eta.data(),
                               dYdt.empty() ? nullptr : dYdt.data());

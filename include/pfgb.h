@@ -194,6 +194,22 @@ typedef struct pfgb_params {
        3 = the homogeneous solution on every step (cold).
        1 and 2 need pfgb_set_warm_start_model. */
     int32_t elastic_warm_start_source;
+    /* seeded initial fields (initialize_fields_cuda, main_cuda.cu:15157-15430;
+       flags --init-shape, --init-axis-ratio-r*, --init-tilt-*-deg,
+       --init-center-shift-*, --init-phi-noise-*, --seed): shape -1 legacy /
+       0 sphere / 1 ellipsoid with the axis ratios (normalised to the volume
+       of the radius-R sphere); the short axis tilted by (theta, phi) when
+       init_use_rotation; every centre shifted; uniform phi noise of
+       amplitude init_phi_noise_amp hashed from init_phi_noise_seed (seed
+       when 0); seed also places several seeds (srand / rand) */
+    int32_t init_shape_mode;
+    int32_t init_use_rotation;
+    double init_axis_ratio_rx, init_axis_ratio_ry, init_axis_ratio_rz;
+    double init_tilt_theta_deg, init_tilt_phi_deg;
+    double init_center_shift_x, init_center_shift_y, init_center_shift_z;
+    double init_phi_noise_amp;
+    uint64_t init_phi_noise_seed;
+    uint64_t seed;
     /* derived by pfgb_params_finalize (pfparams_refresh_thermo) */
     double temperature_K;
     double mu0_compound;
@@ -335,6 +351,16 @@ pfgb_status pfgb_minimize(pfgb_ctx *ctx, int max_iter, int stop_on_convergence, 
  * succeeded, else the first failing status.  No counterpart in the
  * reference's library (it has none); replaces the sweep job scripts. */
 pfgb_status pfgb_batch_minimize(pfgb_case *cases, int ncases, int device, int concurrency);
+
+/* Seeded initial fields on the device, as the reference builds them when no
+ * raw fields are given (initialize_fields_cuda, main_cuda.cu:15157-15430:
+ * init_phi_kernel, apply_phi_noise_kernel, init_xB_Y_from_phi_kernel, the
+ * seed placement and the diffuse-interface lever rule for xB outside the
+ * seeds), loaded as the context's initial state like pfgb_load_fields
+ * (eta zero). */
+pfgb_status pfgb_init_fields(pfgb_ctx *ctx);
+/* The same fields into HOST buffers (N float64 each), without a context. */
+pfgb_status pfgb_seed_fields(const pfgb_params *p, int device, double *phi, double *xB);
 
 /* Read the state back to HOST buffers (float64); any pointer may be NULL. */
 pfgb_status pfgb_read_fields(pfgb_ctx *ctx, double *phi, double *xB, double *Y,

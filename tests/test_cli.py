@@ -37,9 +37,16 @@ def test_cli_rejects_bad_inputs(capi, tmp_path):
     # unknown mode
     r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf, "--mode=relax"], tmp_path)
     assert r.returncode == 2 and "--mode=relax" in r.stderr
-    # no raw fields
-    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf], tmp_path)
-    assert r.returncode == 2 and "raw_fields" in r.stderr
+    # raw_fields without the files, an unknown init mode
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf, "--init-mode", "raw_fields"],
+             tmp_path)
+    assert r.returncode == 2 and "raw_fields needs" in r.stderr
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf, "--init-mode", "vtk"],
+             tmp_path)
+    assert r.returncode == 2 and "unknown --init-mode" in r.stderr
+    r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf, "--init-shape", "cube"],
+             tmp_path)
+    assert r.returncode == 2 and "--init-shape" in r.stderr
     # raw field of the wrong size
     bad = tmp_path / "phi.raw"
     np.zeros(10).tofile(bad)
@@ -255,3 +262,28 @@ def test_cli_output_formats(capi, tmp_path):
     assert r.returncode == 0 and "VTK_OUTPUT_SUPPRESSED field=phi" in r.stdout
     run = os.listdir(tmp_path / "S")[0]
     assert not any(f.endswith(".vtk") for f in os.listdir(tmp_path / "S" / run / "raw_fields_relax"))
+
+
+@pytest.mark.gpu
+def test_cli_seeded_initialisation(capi, tmp_path):
+    """Without raw fields the run starts from the seeded initialiser
+    (initialize_fields_cuda): case directory named after the shape, and the
+    initial phi equal to the restatement in oracle/init_oracle.py."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(GOLDEN), "..", "oracle"))
+    import init_oracle
+    n = 24
+    pf = os.path.join(GOLDEN, "c2.params")
+    r = _run(capi, [str(n), str(n), str(n), "0.01", "1", "10", "1", "1", "--pf-param-file", pf, "--radius", "6",
+                    "--init-shape", "ellipsoid", "--init-axis-ratio-rz", "0.5", "--init-tilt-theta-deg", "30",
+                    "--init-phi-noise-amp", "0.01", "--seed", "99"],
+             tmp_path, env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "R")})
+    assert r.returncode == 0, r.stderr
+    run = os.listdir(tmp_path / "R")[0]
+    case = tmp_path / "R" / run / "case_test-1_ellipsoid_th30_ph0_noise1e-02"
+    assert case.is_dir(), os.listdir(tmp_path / "R" / run)
+    p = params_for(capi, "c2.params", n=n, ic_phi_seed_radius=6.0, init_shape_mode=1, init_axis_ratio_rz=0.5,
+                   init_tilt_theta_deg=30.0, init_use_rotation=1, init_phi_noise_amp=0.01, seed=99)
+    want, _ = init_oracle.seed_fields(p)
+    got = _vtk_values(case / "phi_init.vtk", (n, n, n))
+    assert np.abs(got - want).max() <= 5.1e-6
