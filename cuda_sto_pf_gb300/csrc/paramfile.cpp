@@ -88,7 +88,7 @@ const DKey kDoubles[] = {
     DK("init_axis_ratio_rz", init_axis_ratio_rz), DK("init_tilt_theta_deg", init_tilt_theta_deg),
     DK("init_tilt_phi_deg", init_tilt_phi_deg), DK("init_center_shift_x", init_center_shift_x),
     DK("init_center_shift_y", init_center_shift_y), DK("init_center_shift_z", init_center_shift_z),
-    DK("init_phi_noise_amp", init_phi_noise_amp),
+    DK("init_phi_noise_amp", init_phi_noise_amp), DK("gp_h_alpha_eps", gp_h_alpha_eps),
 };
 const DKey kInts[] = {
     DK("pf_params_schema_version", pf_params_schema_version),
@@ -191,6 +191,13 @@ extern "C" pfgb_status pfgb_params_set(pfgb_params *p, const char *key, const ch
         if (e == value || *e != '\0' || errno != 0 || value[0] == '-') return PFGB_ERR_INVALID;
         (!strcmp(key, "seed") ? p->seed : p->init_phi_noise_seed) = (uint64_t)v;
         return PFGB_OK;
+    }
+    if (!strcmp(key, "pf_y_update_mode")) {   // pf_params.h:345, checked fatally at main_cuda.cu:1688-1696
+        if (!strcmp(value, "lagged_rhs")) { p->pf_y_update_mode = PFGB_Y_LAGGED_RHS; return PFGB_OK; }
+        if (!strcmp(value, "storage_exact")) { p->pf_y_update_mode = PFGB_Y_STORAGE_EXACT; return PFGB_OK; }
+        // x_/q_transport_projection_split are valid there but not built here:
+        // refused rather than run as another update
+        return PFGB_ERR_INVALID;
     }
     if (!strcmp(key, "model_mode")) {
         if (!strcmp(value, "two_phase")) { p->model_mode = PFGB_MODEL_TWO_PHASE; return PFGB_OK; }

@@ -107,6 +107,8 @@ void pfgb_params_default(pfgb_params *p) {
     p->elastic_iter_max = 32;
     p->elastic_fail_on_nonconvergence = 1;
     p->elastic_increment_form = 1;
+    p->pf_y_update_mode = PFGB_Y_LAGGED_RHS;
+    p->gp_h_alpha_eps = 1.0e-8;   // main_cuda.cu:16187
     p->elastic_residual_tolerance = 1.0e-6;
     p->elastic_residual_absolute_floor = 1.0e-30;
     p->eps_iso_over_vB = -1.0;

@@ -501,12 +501,13 @@ struct OpFluxZ {
         out[3] = src;
         out[4] = Yf;
     }
+    int no_src = 0;   // storage_exact: the divergence of J alone
     __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
         const long long o = row * d.g.NzC + k;
         const T kz = T(d.kt.kz[k]);
         d.S[0][o] = v[0];
         d.S[1][o] = v[1];
-        d.S[2][o] = csub(cmul_is(v[2], kz), v[3]);
+        d.S[2][o] = no_src ? cmul_is(v[2], kz) : csub(cmul_is(v[2], kz), v[3]);
         d.S[3][o] = v[4];
     }
 };
@@ -538,6 +539,48 @@ struct OpYUpdX {
         const T2 div = cadd(cmul_is(in[0], T(kt.kx[i])), in[1]);
         out[0] = cscale(cadd(in[2], cscale(div, a)), T(invN));
     }
+};
+
+// storage_exact x pass: divJ_k = mask (i kx J_x + i ky J_y + i kz J_z) / N
+template <typename T>
+struct OpDivX {
+    static constexpr bool kInplace = false;
+    KTab kt; double invN;
+    __device__ void apply(int i, int j, int k, const cplx_t<T> *in, cplx_t<T> *out) const {
+        using T2 = cplx_t<T>;
+        if (kt.cut(i, j, k)) { out[0] = mk2<T2>(T(0), T(0)); return; }
+        out[0] = cscale(cadd(cmul_is(in[0], T(kt.kx[i])), in[1]), T(invN));
+    }
+};
+
+// storage_exact final z pass (two_phase_storage_exact_Y_update_kernel,
+// cuda_kernels.cu:2859-2921): C^n = (1-h^n) x^n + h^n v_B, the target
+// C^n + dt div J, solved for x_alpha with h^{n+1}; where the matrix storage
+// 1 - h^{n+1} is below its floor or the solution leaves [eps, 1-eps], x^n
+// stays.  Y from the clipped logit, capped at Y_clip.
+template <typename T, typename TE>
+struct OpStorageExactZ {
+    using Acc = NoAcc;
+    DevState<T, TE> d; PhysC c; const cplx_t<T> *src; double ha_eps;
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * d.g.NzC + k]; }
+    __device__ void point(long long cell, const T *in, T *, Acc &) const {
+        const T Yold = d.Y[cell];
+        const T ho = pf_h(clamp01(d.phi_old[cell])), hn = pf_h(clamp01(d.phi_new[cell]));
+        const T eps = T(c.xBeps), yc = T(c.Yclip);
+        const T xo = sigmoid_clip(Yold + T(d.Yc), yc, eps);
+        const T Ct = (T(1) - ho) * xo + ho * T(c.vB) + T(c.dt) * in[0];
+        const T han = T(1) - hn;
+        const bool small = !(han >= T(ha_eps));
+        T xt = xo;
+        if (!small && isfinite(Ct)) xt = (Ct - hn * T(c.vB)) / han;
+        const bool bad = small || !isfinite(xt) || xt < eps || xt > one_minus_eps(eps);
+        const T y = logit_clip(bad ? xo : xt, eps, yc);
+        const T yn = y - T(d.Yc);
+        d.Y[cell] = yn;
+        d.Yprev[cell] = Yold;
+        d.dYdt[cell] = (yn - Yold) / T(c.dt);
+    }
+    __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
 };
 
 // (6) final z pass: store Y_f, dY/dt, and the zero-mode statistics
@@ -1744,7 +1787,31 @@ static pfgb_status y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_sta
         for (int i = 0; i < 3; ++i) { io.in[i] = d.S[i]; io.out[i] = d.S[i]; }
         TRY((launch_axis<T, 3, 3, +1, 0>(c, 1, io, OpCopy<T, 3>{}, "y_inv3")));
     }
-    TRY((launch_z<T, 3, 5>(c, OpFluxZ<T, TE>{d, pc}, "z_flux", (4.0 + pc.gp) * Nf * sizeof(T))));
+    const bool storage_exact = P.pf_y_update_mode == PFGB_Y_STORAGE_EXACT;
+    TRY((launch_z<T, 3, 5>(c, OpFluxZ<T, TE>{d, pc, storage_exact ? 1 : 0}, "z_flux", (4.0 + pc.gp) * Nf * sizeof(T))));
+    if (storage_exact) {
+        {
+            AxisIO<T, 4, 3> io;
+            for (int i = 0; i < 4; ++i) io.in[i] = d.S[i];
+            io.out[0] = d.S[0]; io.out[1] = d.S[1]; io.out[2] = d.S[3];
+            TRY((launch_axis<T, 4, 3, -1, 0>(c, 1, io, OpYCombY<T>{kt}, "y_ycomb")));
+        }
+        {
+            AxisIO<T, 2, 1> io;
+            io.in[0] = d.S[0]; io.in[1] = d.S[1];
+            io.out[0] = d.S[0];
+            TRY((launch_axis<T, 2, 1, -1, +1>(c, 2, io, OpDivX<T>{kt, invN}, "x_div")));
+        }
+        TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+        TRY((launch_z<T, 1, 0>(c, OpStorageExactZ<T, TE>{d, pc, d.S[0], P.gp_h_alpha_eps}, "z_storage_exact",
+                               5.0 * Nf * sizeof(T))));
+        c->dYoff = 0.0;
+        if (st) {
+            TRY(sync_read(c, DS_MEAN_DY, 1));
+            st->mean_DY = c->hscal[DS_MEAN_DY];
+        }
+        return PFGB_OK;
+    }
     {
         AxisIO<T, 4, 3> io;
         for (int i = 0; i < 4; ++i) io.in[i] = d.S[i];
@@ -2433,6 +2500,20 @@ static pfgb_status validate(const pfgb_params *p) {
                                "(C0 not positive definite, or the stiffness contrast too large)");
             return PFGB_ERR_UNSUPPORTED;
         }
+    }
+    if (p->pf_y_update_mode != PFGB_Y_LAGGED_RHS && p->pf_y_update_mode != PFGB_Y_STORAGE_EXACT) {
+        pfgb_set_error_msg("pf_y_update_mode: lagged_rhs or storage_exact (the transport-projection splits are not "
+                           "built)");
+        return PFGB_ERR_UNSUPPORTED;
+    }
+    // the zero mode and minimize refuse every mode but lagged_rhs
+    // (main_cuda.cu:24600-24612, 24692-24702); storage_exact without the GP
+    // storage coupling is the two_phase path (main_cuda.cu:30627-30628)
+    if (p->pf_y_update_mode == PFGB_Y_STORAGE_EXACT &&
+        (p->zero_mode_enabled || p->model_mode != PFGB_MODEL_TWO_PHASE || p->mode != PFGB_MODE_DYNAMICS)) {
+        pfgb_set_error_msg("pf_y_update_mode=storage_exact: two_phase dynamics with the zero mode off (the zero "
+                           "mode owns lagged_rhs; the GP storage-coupled modes are not built)");
+        return PFGB_ERR_UNSUPPORTED;
     }
     if (p->elastic_warm_start_source < 0 || p->elastic_warm_start_source > 3) {
         pfgb_set_error_msg("elastic_warm_start_source must be 0, 1, 2 or 3");

@@ -56,7 +56,7 @@ struct Cli {
     int warm_source = -1;
     // zero-mode checkpoints (main_cuda.cu:22715-22760)
     // seeded initialisation flags, applied as parameter keys (main_cuda.cu:23915-23972)
-    std::vector<std::pair<std::string, std::string>> init_sets;
+    std::vector<std::pair<std::string, std::string>> param_sets;
     bool tilt_given = false;
     double radius_nm = NAN;
     int ckpt_every = 0;
@@ -224,9 +224,11 @@ Cli parse(int argc, char **argv) {
         else if ((v = flag_value(argc, argv, &i, "--minimize-xB-max-safe"))) { if (!to_double(v, &c.xB_max_safe)) bad(a, v); }
         else if ((v = flag_value(argc, argv, &i, "--radius"))) { if (!to_double(v, &c.radius) || c.radius < 0) bad(a, v); }
         else if ((v = flag_value(argc, argv, &i, "--radius-phys-nm"))) { if (!to_double(v, &c.radius_nm) || c.radius_nm < 0) bad(a, v); }
+        else if ((v = flag_value(argc, argv, &i, "--pf_y_update_mode")))   // main_cuda.cu:23411
+            c.param_sets.push_back({"pf_y_update_mode", v});
         else if ((v = flag_value(argc, argv, &i, "--init-shape"))) {
-            if (!strcmp(v, "sphere")) c.init_sets.push_back({"init_shape_mode", "0"});
-            else if (!strcmp(v, "ellipsoid")) c.init_sets.push_back({"init_shape_mode", "1"});
+            if (!strcmp(v, "sphere")) c.param_sets.push_back({"init_shape_mode", "0"});
+            else if (!strcmp(v, "ellipsoid")) c.param_sets.push_back({"init_shape_mode", "1"});
             else bad(a, v);
         }
         else if (!strncmp(a, "--init-axis-ratio-r", 19) || !strncmp(a, "--init-center-shift-", 20) ||
@@ -239,7 +241,7 @@ Cli parse(int argc, char **argv) {
             v = flag_value(argc, argv, &i, flag.c_str());
             std::string key = flag.substr(2);
             for (char &ch : key) if (ch == '-') ch = '_';
-            c.init_sets.push_back({key, v ? v : ""});
+            c.param_sets.push_back({key, v ? v : ""});
             if (!strncmp(key.c_str(), "init_tilt_", 10)) c.tilt_given = true;
         }
         else fprintf(stderr, "[warn] unknown flag ignored: %s\n", a);
@@ -459,7 +461,7 @@ int main(int argc, char **argv) {
         P.dt = P.minimize_dt;
     }
     if (std::isfinite(c.radius)) P.ic_phi_seed_radius = c.radius;
-    for (const auto &kv : c.init_sets)
+    for (const auto &kv : c.param_sets)
         if (pfgb_params_set(&P, kv.first.c_str(), kv.second.c_str()) != PFGB_OK) bad(kv.first.c_str(), kv.second.c_str());
     if (c.tilt_given && (P.init_tilt_theta_deg != 0.0 || P.init_tilt_phi_deg != 0.0)) P.init_use_rotation = 1;
     if (std::isfinite(c.radius_nm)) {   // main_cuda.cu:25288-25310: physical radius -> code units

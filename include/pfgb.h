@@ -77,6 +77,8 @@ enum { PFGB_PREC_FP64 = 0, PFGB_PREC_FP32 = 1 };
 enum { PFGB_MODEL_TWO_PHASE = 0, PFGB_MODEL_GP_ZONE = 1 };
 /* mode (pf_params.h: 0=dynamics, 1=minimize) */
 enum { PFGB_MODE_DYNAMICS = 0, PFGB_MODE_MINIMIZE = 1 };
+/* pf_y_update_mode (pf_params.h:345) */
+enum { PFGB_Y_LAGGED_RHS = 0, PFGB_Y_STORAGE_EXACT = 1 };
 
 /*
  * Stiffness tensors are the 21 independent Voigt entries in the reference's
@@ -142,6 +144,14 @@ typedef struct pfgb_params {
     int32_t enable_Y_rhs_previous_time_level;
     int32_t disable_Y_rhs_gamma_term;
     double Y_rhs_term_h_scale;
+    /* pf_y_update_mode: PFGB_Y_LAGGED_RHS (the semi-implicit spectral update,
+       default) or PFGB_Y_STORAGE_EXACT (two_phase, zero mode off: the
+       storage-consistent point update C^{n+1} = C^n + dt div J solved for
+       x_alpha, two_phase_storage_exact_Y_update_kernel,
+       cuda_kernels.cu:2859-2921); gp_h_alpha_eps is its matrix-storage floor */
+    int32_t pf_y_update_mode;
+    int32_t pad_y;
+    double gp_h_alpha_eps;
     /* zero mode (PF_CONSERVED_Y_ZERO_MODE_V1) */
     int32_t zero_mode_enabled;
     int32_t zero_mode_max_iterations;

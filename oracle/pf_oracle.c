@@ -1020,6 +1020,36 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
     dealias(s, s->divJ_k);
     inv(s, s->divJ_k, s->divJ);
     RLOOP_BEGIN(s) s->divJ[idx] *= s->invN; RLOOP_END
+    if (P->pf_y_update_mode == PFGB_Y_STORAGE_EXACT) {
+        /* two_phase_storage_exact_Y_update_kernel, cuda_kernels.cu:2859-2921:
+         * C^n + dt divJ solved for x_alpha with h^{n+1}; x^n kept where the
+         * matrix storage is below its floor or the solution leaves [eps, 1-eps] */
+        RLOOP_BEGIN(s)
+            const double ho = o_h(o_clamp01(s->phi_n[idx])), hn = o_h(o_clamp01(s->phi[idx]));
+            const double xo = o_sigmoid(s->Y_n[idx], P->Y_clip, P->xB_eps);
+            const double Ct = (1.0 - ho) * xo + ho * P->v_B + dt * s->divJ[idx];
+            const double han = 1.0 - hn;
+            const int small = !(han >= P->gp_h_alpha_eps);
+            double xt = xo;
+            if (!small && isfinite(Ct)) xt = (Ct - hn * P->v_B) / han;
+            const int bad = small || !isfinite(xt) || xt < P->xB_eps || xt > 1.0 - P->xB_eps;
+            const double y = o_logit(bad ? xo : xt, P->xB_eps, P->Y_clip);
+            s->Y[idx] = y;
+            s->xB[idx] = o_sigmoid(y, P->Y_clip, P->xB_eps);
+            s->dYdt[idx] = (y - s->Y_n[idx]) / dt;
+        RLOOP_END
+        if (st) {
+            RLOOP_BEGIN(s)
+                double h = o_h(phiY[idx]);
+                double x = o_sigmoid_raw(s->Y_n[idx]);
+                if (x < 1e-12) x = 1e-12;
+                if (x > 1.0 - 1e-12) x = 1.0 - 1e-12;
+                s->mass_t[idx] = o_Dmix(h, P->D_alpha, P->D_compound) * x * (1.0 - x);
+            RLOOP_END
+            st->mean_DY = dsum(s->mass_t, s->N) / (double)s->N;
+        }
+        return PFGB_OK;
+    }
     /* Laplacian of Y, :30572-30581 */
     fwd(s, s->Y, s->Y_k); dealias(s, s->Y_k);
     KLOOP_BEGIN(s)

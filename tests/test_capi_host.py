@@ -78,6 +78,17 @@ def test_unknown_key_warns_and_is_ignored(capi, tmp_path, capfd):
     assert "unknown key ignored: not_a_key" in capfd.readouterr().err
 
 
+def test_y_update_mode_key(capi, tmp_path):
+    base = open(os.path.join(GOLDEN, "c1.params")).read()
+    p = capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = storage_exact\ngp_h_alpha_eps = 1e-6\n"))
+    assert p.pf_y_update_mode == capi.Y_STORAGE_EXACT and p.gp_h_alpha_eps == 1e-6
+    assert capi.default_params().pf_y_update_mode == capi.Y_LAGGED_RHS
+    # the transport-projection splits are refused, not silently replaced
+    with pytest.raises(capi.PfgbError) as e:
+        capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = x_transport_projection_split\n"))
+    assert "pf_y_update_mode" in str(e.value)
+
+
 def test_finalize_matches_oracle(capi, oracle):
     import oracle_py
     p = capi.load_params_file(os.path.join(GOLDEN, "c2.params"))

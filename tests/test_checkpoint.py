@@ -51,7 +51,8 @@ def _param_fp(p):
               p.kappa_phi, p.W, p.Y_clip, p.xB_eps):
         d += struct.pack("<d", v)
     d += struct.pack("<2i", p.enable_Y_rhs_previous_time_level, p.disable_Y_rhs_gamma_term)
-    for s in ("legacy", "lagged_rhs", "SM_EXPLICIT_CONTEXT_N_V1", "SM_TANGENT_N_V1"):
+    ymode = "storage_exact" if p.pf_y_update_mode == 1 else "lagged_rhs"
+    for s in ("legacy", ymode, "SM_EXPLICIT_CONTEXT_N_V1", "SM_TANGENT_N_V1"):
         d += s.encode() + b"\0"
     h = _fnv(d)
     return h or 1
@@ -75,6 +76,8 @@ def test_fingerprints_match_their_definition(capi, name):
     assert lib.pfgb_parameter_fingerprint(ctypes.byref(p)) == _param_fp(p)
     assert lib.pfgb_elastic_solver_fingerprint(ctypes.byref(p)) == _elastic_fp(p)
     assert lib.pfgb_fnv1a64(b"abc", 3, 1469598103934665603) == _fnv(b"abc")
+    q = params_for(capi, name, n=24, pf_y_update_mode=capi.Y_STORAGE_EXACT)
+    assert lib.pfgb_parameter_fingerprint(ctypes.byref(q)) == _param_fp(q) != _param_fp(p)
 
 
 class _State:

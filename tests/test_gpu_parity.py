@@ -291,3 +291,83 @@ def test_chebyshev_needs_increment_form(capi):
     p = params_for(capi, "c2.params", n=16, elastic_chebyshev=1, elastic_increment_form=0)
     with pytest.raises(capi.PfgbError):
         Solver(p)
+
+
+
+def _diffuse_seed(capi, p, n, amp=0.35, seed=23):
+    """A low-amplitude seed (phi <= amp, matrix storage 1 - h >= 0.76) in a
+    noisy matrix: the storage-exact reconstruction stays inside its bounds."""
+    from cuda_sto_pf_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    phi = amp * workloads.ellipsoid_field((n, n, n), [np.full(3, n / 2.0)], [np.array([7.0, 6.0, 5.0])],
+                                          [workloads.random_rotation(rng)], p.ic_phi_iface_w)
+    xB = 0.03 + 1e-3 * rng.standard_normal(phi.shape)
+    return phi, xB
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_storage_exact_y_update_parity(capi, oracle, prec):
+    """pf_y_update_mode=storage_exact (two_phase, zero mode off) against the
+    oracle over 8 steps, and its conservation of the B ledger
+    sum((1-h) xB + h v_B): the spectral divergence has no k = 0 part, so only
+    clipped cells could change it.  The update is explicit in the flux, so dt
+    is taken inside the explicit-diffusion limit (D_alpha dt / dx^2 = 0.0625;
+    the file's dt = 0.01 is 100x larger and runs away in a few steps)."""
+    from cuda_sto_pf_gb300.solver import Solver
+    n, steps = 32, 8
+    p = params_for(capi, "c2.params", n=n, precision=prec, pf_y_update_mode=capi.Y_STORAGE_EXACT, dt=1e-4)
+    phi, xB = _diffuse_seed(capi, p, n)
+    o = oracle(p, threads=4)
+    o.load(phi, xB)
+    assert o.step(steps) == 0
+    with Solver(p) as s:
+        s.load(phi, xB)
+        d0 = s.diagnostics()
+        s.step(steps)
+        fg = s.fields()
+        d1 = s.diagnostics()
+    fo = o.fields()
+    for k in ("phi", "xB", "Y"):
+        assert rel_l2(fg[k], fo[k]) <= TOL[prec], (k, rel_l2(fg[k], fo[k]))
+    # dY/dt is a difference quotient of the stored Y: in FP32 one ulp of
+    # |Y| ~ 3.5 over dt = 1e-4 is 2.4e-3 against |dY/dt| ~ 10
+    assert rel_l2(fg["dYdt"], fo["dYdt"]) <= (1e-5 if prec == 0 else 1e-3)
+    assert abs(d1.mass_xBtot - d0.mass_xBtot) <= (1e-12 if prec == 0 else 2e-6) * d0.mass_xBtot
+    # the lagged form moves along another path
+    p2 = params_for(capi, "c2.params", n=n, precision=prec, dt=1e-4)
+    with Solver(p2) as s:
+        s.load(phi, xB)
+        s.step(steps)
+        assert rel_l2(s.fields()["xB"], fg["xB"]) > 10 * TOL[prec]
+
+
+def test_storage_exact_clipped_cells_one_step(capi, oracle):
+    """One step on a seeded particle at the file's dt: interface cells with a
+    small matrix storage leave [eps, 1 - eps] or fall below gp_h_alpha_eps and
+    keep x^n.  The kept set must agree cell for cell (away from a handful of
+    cells at the bound, where the FP32 elastic solve decides) and the fields
+    stay within the amplified round-off of the reconstruction (1 / (1 - h)
+    reaches 50 here), looser than the lagged form's bound."""
+    from cuda_sto_pf_gb300.solver import Solver
+    p = params_for(capi, "c2.params", n=32, precision=0, pf_y_update_mode=capi.Y_STORAGE_EXACT)
+    phi, xB, _ = _inputs(capi, p, 32, False, seed=23)
+    o = oracle(p, threads=4)
+    o.load(phi, xB)
+    assert o.step(1) == 0
+    with Solver(p) as s:
+        s.load(phi, xB)
+        s.step(1)
+        fg = s.fields()
+    fo = o.fields()
+    kept_g, kept_o = np.abs(fg["dYdt"]) < 1e-6, np.abs(fo["dYdt"]) < 1e-6
+    assert kept_o.sum() > 0 and kept_o.sum() < kept_o.size // 2
+    assert (kept_g != kept_o).sum() <= 4
+    assert rel_l2(fg["phi"], fo["phi"]) <= TOL[0]
+    assert rel_l2(fg["xB"], fo["xB"]) <= 1e-6
+    assert rel_l2(fg["Y"], fo["Y"]) <= 2e-5
+
+def test_storage_exact_refuses_the_zero_mode(capi):
+    from cuda_sto_pf_gb300.solver import Solver
+    p = params_for(capi, "c2.params", n=16, pf_y_update_mode=capi.Y_STORAGE_EXACT, zero_mode_enabled=1)
+    with pytest.raises(capi.PfgbError):
+        Solver(p)
