@@ -18,7 +18,7 @@ c_float_p = POINTER(ctypes.c_float)
 PREC_FP64, PREC_FP32 = 0, 1
 MODEL_TWO_PHASE, MODEL_GP_ZONE = 0, 1
 MODE_DYNAMICS, MODE_MINIMIZE = 0, 1
-Y_LAGGED_RHS, Y_STORAGE_EXACT = 0, 1
+Y_LAGGED_RHS, Y_STORAGE_EXACT, Y_X_TRANSPORT_SPLIT = 0, 1, 2
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device out of memory",
           4: "elastic solver did not converge", 5: "zero-mode mass solve rejected the step",
@@ -56,6 +56,7 @@ class Params(Structure):
         ("enable_Y_rhs_previous_time_level", c_int32), ("disable_Y_rhs_gamma_term", c_int32),
         ("Y_rhs_term_h_scale", c_double),
         ("pf_y_update_mode", c_int32), ("pad_y", c_int32), ("gp_h_alpha_eps", c_double),
+        ("pf_matrix_storage_floor", c_double), ("pf_composition_stabilizer_Dalpha_multiplier", c_double),
         ("zero_mode_enabled", c_int32), ("zero_mode_max_iterations", c_int32),
         ("zero_mode_tolerance_relative", c_double),
         ("gp_elastic_enabled", c_int32), ("gp_elastic_active_eta", c_int32),

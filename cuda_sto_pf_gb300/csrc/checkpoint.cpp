@@ -304,7 +304,9 @@ uint64_t pfgb_parameter_fingerprint(const pfgb_params *p) {
         add(&d, sizeof(d));
     const int32_t flags[2] = {p->enable_Y_rhs_previous_time_level, p->disable_Y_rhs_gamma_term};
     add(flags, sizeof(flags));
-    const char *ymode = p->pf_y_update_mode == PFGB_Y_STORAGE_EXACT ? "storage_exact" : kYUpdateLagged;
+    const char *ymode = p->pf_y_update_mode == PFGB_Y_STORAGE_EXACT      ? "storage_exact"
+                        : p->pf_y_update_mode == PFGB_Y_X_TRANSPORT_SPLIT ? "x_transport_projection_split"
+                                                                           : kYUpdateLagged;
     for (const char *s : {kCompositionLegacy, ymode, kExplicitContextV1, kReactionTangentV1})
         add(s, std::strlen(s) + 1);
     return h == 0 ? 1 : h;

@@ -89,6 +89,8 @@ const DKey kDoubles[] = {
     DK("init_tilt_phi_deg", init_tilt_phi_deg), DK("init_center_shift_x", init_center_shift_x),
     DK("init_center_shift_y", init_center_shift_y), DK("init_center_shift_z", init_center_shift_z),
     DK("init_phi_noise_amp", init_phi_noise_amp), DK("gp_h_alpha_eps", gp_h_alpha_eps),
+    DK("pf_matrix_storage_floor", pf_matrix_storage_floor),
+    DK("pf_composition_stabilizer_Dalpha_multiplier", pf_composition_stabilizer_Dalpha_multiplier),
 };
 const DKey kInts[] = {
     DK("pf_params_schema_version", pf_params_schema_version),
@@ -195,7 +197,11 @@ extern "C" pfgb_status pfgb_params_set(pfgb_params *p, const char *key, const ch
     if (!strcmp(key, "pf_y_update_mode")) {   // pf_params.h:345, checked fatally at main_cuda.cu:1688-1696
         if (!strcmp(value, "lagged_rhs")) { p->pf_y_update_mode = PFGB_Y_LAGGED_RHS; return PFGB_OK; }
         if (!strcmp(value, "storage_exact")) { p->pf_y_update_mode = PFGB_Y_STORAGE_EXACT; return PFGB_OK; }
-        // x_/q_transport_projection_split are valid there but not built here:
+        if (!strcmp(value, "x_transport_projection_split")) {
+            p->pf_y_update_mode = PFGB_Y_X_TRANSPORT_SPLIT;
+            return PFGB_OK;
+        }
+        // q_transport_projection_split is valid there but not built here:
         // refused rather than run as another update
         return PFGB_ERR_INVALID;
     }

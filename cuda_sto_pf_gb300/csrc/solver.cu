@@ -583,6 +583,68 @@ struct OpStorageExactZ {
     __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
 };
 
+// x_transport_projection_split (main_cuda.cu:30564-30676).  z pass: div J
+// to real space, the storage source s = div J / (1 - h^{n+1}) where the
+// matrix storage reaches its floor, else 0 (compute_xB_storage_rhs_kernel,
+// cuda_kernels.cu:2922-2951), and x^n; both forward-transformed
+template <typename T, typename TE>
+struct OpXSplitSrcZ {
+    using Acc = NoAcc;
+    DevState<T, TE> d; PhysC c; double floor_;
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = d.S[0][row * d.g.NzC + k]; }
+    __device__ void point(long long cell, const T *in, T *out, Acc &) const {
+        const T ha = T(1) - pf_h(clamp01(d.phi_new[cell]));
+        out[0] = ha >= T(floor_) ? in[0] / ha : T(0);
+        out[1] = sigmoid_clip(d.Y[cell] + T(d.Yc), T(c.Yclip), T(c.xBeps));
+    }
+    __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
+        const long long o = row * d.g.NzC + k;
+        d.S[0][o] = v[0];
+        d.S[1][o] = v[1];
+    }
+};
+
+// x pass: the reference's Y_semi_implicit_update_kernel on x with the
+// right-hand side S - m Lap(x), m = D_alpha * multiplier:
+//   x_k = mask [X_k + dt (S_k + m k^2 X_k)] / (1 + dt m k^2)
+//       = mask [X_k + dt S_k / (1 + dt m k^2)]          (exact algebra)
+// so the stabiliser damps only the source; / N for the inverse transform
+template <typename T>
+struct OpXSplitX {
+    static constexpr bool kInplace = false;
+    KTab kt; double dt, invN, m;
+    __device__ void apply(int i, int j, int k, const cplx_t<T> *in, cplx_t<T> *out) const {
+        using T2 = cplx_t<T>;
+        if (kt.cut(i, j, k)) { out[0] = mk2<T2>(T(0), T(0)); return; }
+        const T a = T(dt / (1.0 + dt * m * kt.k2(i, j, k)));
+        out[0] = cscale(cadd(in[1], cscale(in[0], a)), T(invN));
+    }
+};
+
+// final z pass of the x split (xB_normalize_clamp_and_logit_kernel,
+// cuda_kernels.cu:2953-2973): non-finite x keeps x^n, clamp to
+// [eps, 1 - eps], Y = logit, capped at +-Y_clip
+template <typename T, typename TE>
+struct OpXSplitFinalZ {
+    using Acc = NoAcc;
+    DevState<T, TE> d; PhysC c; const cplx_t<T> *src;
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * d.g.NzC + k]; }
+    __device__ void point(long long cell, const T *in, T *, Acc &) const {
+        const T Yold = d.Y[cell];
+        const T eps = T(c.xBeps), yc = T(c.Yclip);
+        T x = in[0];
+        if (!isfinite(x)) x = sigmoid_clip(Yold + T(d.Yc), yc, eps);
+        x = fmin(fmax(x, eps), one_minus_eps(eps));
+        T y = logit_clip(x, eps, yc);
+        y = fmin(fmax(y, -yc), yc);
+        const T yn = y - T(d.Yc);
+        d.Y[cell] = yn;
+        d.Yprev[cell] = Yold;
+        d.dYdt[cell] = (yn - Yold) / T(c.dt);
+    }
+    __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
+};
+
 // (6) final z pass: store Y_f, dY/dt, and the zero-mode statistics
 template <typename T, typename TE>
 struct OpYFinalZ {
@@ -1788,8 +1850,9 @@ static pfgb_status y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_sta
         TRY((launch_axis<T, 3, 3, +1, 0>(c, 1, io, OpCopy<T, 3>{}, "y_inv3")));
     }
     const bool storage_exact = P.pf_y_update_mode == PFGB_Y_STORAGE_EXACT;
-    TRY((launch_z<T, 3, 5>(c, OpFluxZ<T, TE>{d, pc, storage_exact ? 1 : 0}, "z_flux", (4.0 + pc.gp) * Nf * sizeof(T))));
-    if (storage_exact) {
+    const bool divj_real = storage_exact || P.pf_y_update_mode == PFGB_Y_X_TRANSPORT_SPLIT;
+    TRY((launch_z<T, 3, 5>(c, OpFluxZ<T, TE>{d, pc, divj_real ? 1 : 0}, "z_flux", (4.0 + pc.gp) * Nf * sizeof(T))));
+    if (divj_real) {
         {
             AxisIO<T, 4, 3> io;
             for (int i = 0; i < 4; ++i) io.in[i] = d.S[i];
@@ -1803,12 +1866,31 @@ static pfgb_status y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_sta
             TRY((launch_axis<T, 2, 1, -1, +1>(c, 2, io, OpDivX<T>{kt, invN}, "x_div")));
         }
         TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
-        TRY((launch_z<T, 1, 0>(c, OpStorageExactZ<T, TE>{d, pc, d.S[0], P.gp_h_alpha_eps}, "z_storage_exact",
-                               5.0 * Nf * sizeof(T))));
+        if (storage_exact) {
+            TRY((launch_z<T, 1, 0>(c, OpStorageExactZ<T, TE>{d, pc, d.S[0], P.gp_h_alpha_eps}, "z_storage_exact",
+                                   5.0 * Nf * sizeof(T))));
+        } else {
+            const double mDx = P.D_alpha * P.pf_composition_stabilizer_Dalpha_multiplier;
+            TRY((launch_z<T, 1, 2>(c, OpXSplitSrcZ<T, TE>{d, pc, P.pf_matrix_storage_floor}, "z_xsplit_src",
+                                   2.0 * Nf * sizeof(T))));
+            AxisIO<T, 2, 2> io2;
+            for (int i = 0; i < 2; ++i) { io2.in[i] = d.S[i]; io2.out[i] = d.S[i]; }
+            TRY((launch_axis<T, 2, 2, -1, 0>(c, 1, io2, OpCopy<T, 2>{}, "y_fwd2")));
+            AxisIO<T, 2, 1> iox;
+            iox.in[0] = d.S[0]; iox.in[1] = d.S[1];
+            iox.out[0] = d.S[0];
+            TRY((launch_axis<T, 2, 1, -1, +1>(c, 2, iox, OpXSplitX<T>{kt, P.dt, invN, mDx}, "x_xsplit")));
+            TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+            TRY((launch_z<T, 1, 0>(c, OpXSplitFinalZ<T, TE>{d, pc, d.S[0]}, "z_xsplit_final", 4.0 * Nf * sizeof(T))));
+        }
         c->dYoff = 0.0;
         if (st) {
-            TRY(sync_read(c, DS_MEAN_DY, 1));
-            st->mean_DY = c->hscal[DS_MEAN_DY];
+            if (storage_exact) {
+                TRY(sync_read(c, DS_MEAN_DY, 1));
+                st->mean_DY = c->hscal[DS_MEAN_DY];
+            } else {
+                st->mean_DY = P.D_alpha * P.pf_composition_stabilizer_Dalpha_multiplier;
+            }
         }
         return PFGB_OK;
     }
@@ -2501,18 +2583,29 @@ static pfgb_status validate(const pfgb_params *p) {
             return PFGB_ERR_UNSUPPORTED;
         }
     }
-    if (p->pf_y_update_mode != PFGB_Y_LAGGED_RHS && p->pf_y_update_mode != PFGB_Y_STORAGE_EXACT) {
-        pfgb_set_error_msg("pf_y_update_mode: lagged_rhs or storage_exact (the transport-projection splits are not "
-                           "built)");
+    if (p->pf_y_update_mode < PFGB_Y_LAGGED_RHS || p->pf_y_update_mode > PFGB_Y_X_TRANSPORT_SPLIT) {
+        pfgb_set_error_msg("pf_y_update_mode: lagged_rhs, storage_exact or x_transport_projection_split (the q "
+                           "split is not built)");
         return PFGB_ERR_UNSUPPORTED;
     }
+    if (p->pf_y_update_mode == PFGB_Y_X_TRANSPORT_SPLIT &&
+        (!(p->pf_matrix_storage_floor > 0.0 && p->pf_matrix_storage_floor <= 1.0) ||
+         !(p->pf_composition_stabilizer_Dalpha_multiplier > 0.0) ||
+         !std::isfinite(p->pf_composition_stabilizer_Dalpha_multiplier))) {
+        // main_cuda.cu:1728-1739
+        pfgb_set_error_msg("pf_matrix_storage_floor must be in (0,1] and "
+                           "pf_composition_stabilizer_Dalpha_multiplier finite and > 0");
+        return PFGB_ERR_INVALID;
+    }
     // the zero mode and minimize refuse every mode but lagged_rhs
-    // (main_cuda.cu:24600-24612, 24692-24702); storage_exact without the GP
-    // storage coupling is the two_phase path (main_cuda.cu:30627-30628)
-    if (p->pf_y_update_mode == PFGB_Y_STORAGE_EXACT &&
+    // (main_cuda.cu:24600-24612, 24692-24702); storage_exact and the x split
+    // without the GP storage coupling are the two_phase paths
+    // (main_cuda.cu:30564-30566, 30627-30628)
+    if (p->pf_y_update_mode != PFGB_Y_LAGGED_RHS &&
         (p->zero_mode_enabled || p->model_mode != PFGB_MODEL_TWO_PHASE || p->mode != PFGB_MODE_DYNAMICS)) {
-        pfgb_set_error_msg("pf_y_update_mode=storage_exact: two_phase dynamics with the zero mode off (the zero "
-                           "mode owns lagged_rhs; the GP storage-coupled modes are not built)");
+        pfgb_set_error_msg("pf_y_update_mode storage_exact / x_transport_projection_split: two_phase dynamics with "
+                           "the zero mode off (the zero mode owns lagged_rhs; the GP storage-coupled modes are not "
+                           "built)");
         return PFGB_ERR_UNSUPPORTED;
     }
     if (p->elastic_warm_start_source < 0 || p->elastic_warm_start_source > 3) {

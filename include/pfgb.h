@@ -78,7 +78,7 @@ enum { PFGB_MODEL_TWO_PHASE = 0, PFGB_MODEL_GP_ZONE = 1 };
 /* mode (pf_params.h: 0=dynamics, 1=minimize) */
 enum { PFGB_MODE_DYNAMICS = 0, PFGB_MODE_MINIMIZE = 1 };
 /* pf_y_update_mode (pf_params.h:345) */
-enum { PFGB_Y_LAGGED_RHS = 0, PFGB_Y_STORAGE_EXACT = 1 };
+enum { PFGB_Y_LAGGED_RHS = 0, PFGB_Y_STORAGE_EXACT = 1, PFGB_Y_X_TRANSPORT_SPLIT = 2 };
 
 /*
  * Stiffness tensors are the 21 independent Voigt entries in the reference's
@@ -148,10 +148,16 @@ typedef struct pfgb_params {
        default) or PFGB_Y_STORAGE_EXACT (two_phase, zero mode off: the
        storage-consistent point update C^{n+1} = C^n + dt div J solved for
        x_alpha, two_phase_storage_exact_Y_update_kernel,
-       cuda_kernels.cu:2859-2921); gp_h_alpha_eps is its matrix-storage floor */
+       cuda_kernels.cu:2859-2921); gp_h_alpha_eps is its matrix-storage floor;
+       or PFGB_Y_X_TRANSPORT_SPLIT (two_phase, zero mode off: x_alpha advanced
+       semi-implicitly with the source div J / (1 - h) where 1 - h is at least
+       pf_matrix_storage_floor, stabilised by D_alpha times
+       pf_composition_stabilizer_Dalpha_multiplier, main_cuda.cu:30564-30676) */
     int32_t pf_y_update_mode;
     int32_t pad_y;
     double gp_h_alpha_eps;
+    double pf_matrix_storage_floor;
+    double pf_composition_stabilizer_Dalpha_multiplier;
     /* zero mode (PF_CONSERVED_Y_ZERO_MODE_V1) */
     int32_t zero_mode_enabled;
     int32_t zero_mode_max_iterations;

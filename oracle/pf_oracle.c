@@ -1050,6 +1050,49 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
         }
         return PFGB_OK;
     }
+    if (P->pf_y_update_mode == PFGB_Y_X_TRANSPORT_SPLIT) {
+        /* x_transport_projection_split, main_cuda.cu:30564-30593 and
+         * 30648-30676: the Laplacian of x^n, the storage source
+         * compute_xB_storage_rhs_kernel (cuda_kernels.cu:2922-2951), the
+         * semi-implicit update Y_semi_implicit_update_kernel (:2528-2550) with
+         * the stabiliser D_alpha * multiplier in place of <DY>, then
+         * xB_normalize_clamp_and_logit_kernel (:2953-2973) */
+        const double mDx = P->D_alpha * P->pf_composition_stabilizer_Dalpha_multiplier;
+        fwd(s, s->xB, s->divJ_k); dealias(s, s->divJ_k);   /* x^n in k space */
+        KLOOP_BEGIN(s)
+            double k2 = k2_at(s, ii_, jj_, kk_);
+            s->Y_k[idx].re = -k2 * s->divJ_k[idx].re; s->Y_k[idx].im = -k2 * s->divJ_k[idx].im;
+        KLOOP_END
+        dealias(s, s->Y_k);
+        inv(s, s->Y_k, s->lapY);
+        RLOOP_BEGIN(s)
+            const double lap = s->lapY[idx] * s->invN;
+            const double ha = 1.0 - o_h(o_clamp01(s->phi[idx]));
+            const double rate = ha >= P->pf_matrix_storage_floor ? s->divJ[idx] / ha : 0.0;
+            s->rhs[idx] = rate - mDx * lap;
+        RLOOP_END
+        fwd(s, s->rhs, s->rhs_k); dealias(s, s->rhs_k);
+        KLOOP_BEGIN(s)
+            double den = 1.0 + dt * mDx * k2_at(s, ii_, jj_, kk_);
+            cpx a = s->divJ_k[idx], r = s->rhs_k[idx];
+            s->Y_k[idx].re = (a.re + dt * r.re) / den;
+            s->Y_k[idx].im = (a.im + dt * r.im) / den;
+        KLOOP_END
+        dealias(s, s->Y_k);
+        inv(s, s->Y_k, s->scr);
+        RLOOP_BEGIN(s)
+            double x = s->scr[idx] * s->invN;
+            if (!isfinite(x)) x = s->xB[idx];
+            x = fmin(fmax(x, P->xB_eps), 1.0 - P->xB_eps);
+            double y = o_logit(x, P->xB_eps, P->Y_clip);
+            y = fmin(fmax(y, -P->Y_clip), P->Y_clip);
+            s->Y[idx] = y;
+            s->xB[idx] = o_sigmoid(y, P->Y_clip, P->xB_eps);
+            s->dYdt[idx] = (y - s->Y_n[idx]) / dt;
+        RLOOP_END
+        if (st) st->mean_DY = mDx;
+        return PFGB_OK;
+    }
     /* Laplacian of Y, :30572-30581 */
     fwd(s, s->Y, s->Y_k); dealias(s, s->Y_k);
     KLOOP_BEGIN(s)

@@ -83,9 +83,13 @@ def test_y_update_mode_key(capi, tmp_path):
     p = capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = storage_exact\ngp_h_alpha_eps = 1e-6\n"))
     assert p.pf_y_update_mode == capi.Y_STORAGE_EXACT and p.gp_h_alpha_eps == 1e-6
     assert capi.default_params().pf_y_update_mode == capi.Y_LAGGED_RHS
-    # the transport-projection splits are refused, not silently replaced
+    # the q split is refused, not silently replaced
+    p = capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = x_transport_projection_split\n"
+                                     "pf_matrix_storage_floor = 0.2\n"))
+    assert p.pf_y_update_mode == capi.Y_X_TRANSPORT_SPLIT and p.pf_matrix_storage_floor == 0.2
+    assert p.pf_composition_stabilizer_Dalpha_multiplier == 10.0
     with pytest.raises(capi.PfgbError) as e:
-        capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = x_transport_projection_split\n"))
+        capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = q_transport_projection_split\n"))
     assert "pf_y_update_mode" in str(e.value)
 
 

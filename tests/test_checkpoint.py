@@ -51,7 +51,7 @@ def _param_fp(p):
               p.kappa_phi, p.W, p.Y_clip, p.xB_eps):
         d += struct.pack("<d", v)
     d += struct.pack("<2i", p.enable_Y_rhs_previous_time_level, p.disable_Y_rhs_gamma_term)
-    ymode = "storage_exact" if p.pf_y_update_mode == 1 else "lagged_rhs"
+    ymode = ["lagged_rhs", "storage_exact", "x_transport_projection_split"][p.pf_y_update_mode]
     for s in ("legacy", ymode, "SM_EXPLICIT_CONTEXT_N_V1", "SM_TANGENT_N_V1"):
         d += s.encode() + b"\0"
     h = _fnv(d)

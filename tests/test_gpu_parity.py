@@ -366,8 +366,61 @@ def test_storage_exact_clipped_cells_one_step(capi, oracle):
     assert rel_l2(fg["xB"], fo["xB"]) <= 1e-6
     assert rel_l2(fg["Y"], fo["Y"]) <= 2e-5
 
-def test_storage_exact_refuses_the_zero_mode(capi):
+@pytest.mark.parametrize("mode", ["storage_exact", "x_split"])
+def test_composition_modes_refuse_the_zero_mode(capi, mode):
     from cuda_sto_pf_gb300.solver import Solver
-    p = params_for(capi, "c2.params", n=16, pf_y_update_mode=capi.Y_STORAGE_EXACT, zero_mode_enabled=1)
+    m = capi.Y_STORAGE_EXACT if mode == "storage_exact" else capi.Y_X_TRANSPORT_SPLIT
+    p = params_for(capi, "c2.params", n=16, pf_y_update_mode=m, zero_mode_enabled=1)
     with pytest.raises(capi.PfgbError):
         Solver(p)
+    p = params_for(capi, "c2.params", n=16, pf_y_update_mode=m, model_mode=1)
+    with pytest.raises(capi.PfgbError):
+        Solver(p)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_x_transport_split_parity(capi, oracle, prec):
+    """pf_y_update_mode=x_transport_projection_split against the oracle: x
+    advanced semi-implicitly with the storage source div J / (1 - h) and the
+    stabiliser D_alpha * 10.  Semi-implicit, so the file's dt is stable."""
+    from cuda_sto_pf_gb300.solver import Solver
+    n, steps = 32, 4
+    p = params_for(capi, "c2.params", n=n, precision=prec, pf_y_update_mode=capi.Y_X_TRANSPORT_SPLIT)
+    phi, xB, _ = _inputs(capi, p, n, False, seed=23)
+    o = oracle(p, threads=4)
+    o.load(phi, xB)
+    so = capi.StepStats()
+    assert o.step(steps, so) == 0
+    with Solver(p) as s:
+        s.load(phi, xB)
+        sg = s.step(steps)
+        fg = s.fields()
+    fo = o.fields()
+    for k in ("phi", "xB", "Y"):
+        assert rel_l2(fg[k], fo[k]) <= TOL[prec], (k, rel_l2(fg[k], fo[k]))
+    assert rel_l2(fg["dYdt"], fo["dYdt"]) <= 10 * TOL[prec]
+    assert sg.mean_DY == so.mean_DY == p.D_alpha * p.pf_composition_stabilizer_Dalpha_multiplier
+    p2 = params_for(capi, "c2.params", n=n, precision=prec)
+    with Solver(p2) as s:
+        s.load(phi, xB)
+        s.step(steps)
+        assert rel_l2(s.fields()["xB"], fg["xB"]) > 10 * TOL[prec]
+
+
+def test_x_transport_split_conserves_matrix_mean(capi):
+    """With phi = 0 everywhere the storage source is div J itself, which has
+    no k = 0 part: the mean of x is unchanged to round-off, at 64^3."""
+    from cuda_sto_pf_gb300.solver import Solver
+    n = 64
+    p = params_for(capi, "c2.params", n=n, pf_y_update_mode=capi.Y_X_TRANSPORT_SPLIT)
+    rng = np.random.default_rng(4)
+    phi = np.zeros((n, n, n))
+    xB = 0.03 + 2e-3 * rng.standard_normal(phi.shape)
+    with Solver(p) as s:
+        s.load(phi, xB)
+        x0 = s.fields()["xB"].mean()
+        s.step(6)
+        f = s.fields()
+    assert np.abs(f["phi"]).max() == 0.0
+    assert abs(f["xB"].mean() - x0) <= 1e-14
+    assert f["xB"].std() < 0.5 * xB.std()   # and the noise diffuses
