@@ -57,6 +57,7 @@ class Params(Structure):
         ("Y_rhs_term_h_scale", c_double),
         ("pf_y_update_mode", c_int32), ("pad_y", c_int32), ("gp_h_alpha_eps", c_double),
         ("pf_matrix_storage_floor", c_double), ("pf_composition_stabilizer_Dalpha_multiplier", c_double),
+        ("gp_barrier_only_mode", c_int32), ("enable_legacy_gp_storage_coupling", c_int32),
         ("zero_mode_enabled", c_int32), ("zero_mode_max_iterations", c_int32),
         ("zero_mode_tolerance_relative", c_double),
         ("gp_elastic_enabled", c_int32), ("gp_elastic_active_eta", c_int32),

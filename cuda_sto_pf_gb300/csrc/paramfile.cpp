@@ -117,6 +117,16 @@ const DKey kInts[] = {
 
 // keys of the reference schema that do not drive this path (GP/event
 // engines, converter provenance): accepted without a warning
+// reference keys whose other values select paths this library does not
+// build (pf_params.h; defaults at main_cuda.cu:15829, 15883, 16080, 16108,
+// 16137, 16424): any other value is refused, not ignored
+struct Selector { const char *key, *allowed; };
+const Selector kSelectors[] = {
+    {"pf_composition_mode", "legacy"},         {"y_update_mass_projection_enabled", "0"},
+    {"enable_Y_rhs_picard", "0"},              {"enable_gp_assisted_beta_nucleation", "0"},
+    {"gp_nuc_enabled", "0"},                   {"diagnostic_rsmd_enabled", "0"},
+};
+
 const char *kKnownUnused[] = {
     "gp_W_eta_phys", "gp_kappa_eta_phys", "gp_L_eta_phys", "gp_gamma_alpha_gp", "gp_l_eta_nm",
     "gp_D_ratio", "gp_reaction_nu_A", "gp_reaction_nu_B", "gp_xB_eq_alpha_for_eta",
@@ -194,6 +204,16 @@ extern "C" pfgb_status pfgb_params_set(pfgb_params *p, const char *key, const ch
         (!strcmp(key, "seed") ? p->seed : p->init_phi_noise_seed) = (uint64_t)v;
         return PFGB_OK;
     }
+    for (const Selector &sel : kSelectors)
+        if (!strcmp(key, sel.key)) return strcmp(value, sel.allowed) ? PFGB_ERR_INVALID : PFGB_OK;
+    if (!strcmp(key, "gp_barrier_only_mode") || !strcmp(key, "enable_legacy_gp_storage_coupling")) {
+        char *e = nullptr;
+        const long v = strtol(value, &e, 10);
+        if (e == value || *e != '\0') return PFGB_ERR_INVALID;
+        (!strcmp(key, "gp_barrier_only_mode") ? p->gp_barrier_only_mode : p->enable_legacy_gp_storage_coupling) =
+            (int32_t)v;
+        return PFGB_OK;
+    }
     if (!strcmp(key, "pf_y_update_mode")) {   // pf_params.h:345, checked fatally at main_cuda.cu:1688-1696
         if (!strcmp(value, "lagged_rhs")) { p->pf_y_update_mode = PFGB_Y_LAGGED_RHS; return PFGB_OK; }
         if (!strcmp(value, "storage_exact")) { p->pf_y_update_mode = PFGB_Y_STORAGE_EXACT; return PFGB_OK; }
@@ -249,7 +269,13 @@ extern "C" pfgb_status pfgb_params_load_file(pfgb_params *p, const char *path, c
         trim(val);
         pfgb_status st = pfgb_params_set(p, key.c_str(), val.c_str());
         if (st == PFGB_ERR_INVALID) {
-            seterr(errbuf, errlen, "%s:%d invalid value for %s: %s", path, line_no, key.c_str(), val.c_str());
+            bool selector = !strcmp(key.c_str(), "pf_y_update_mode");
+            for (const Selector &sel : kSelectors) selector = selector || key == sel.key;
+            if (selector)
+                seterr(errbuf, errlen, "%s:%d %s=%s selects a path that is not built", path, line_no, key.c_str(),
+                       val.c_str());
+            else
+                seterr(errbuf, errlen, "%s:%d invalid value for %s: %s", path, line_no, key.c_str(), val.c_str());
             fclose(fp);
             return PFGB_ERR_INVALID;
         }

@@ -111,6 +111,8 @@ void pfgb_params_default(pfgb_params *p) {
     p->gp_h_alpha_eps = 1.0e-8;   // main_cuda.cu:16187
     p->pf_matrix_storage_floor = 0.1;                      // main_cuda.cu:16116
     p->pf_composition_stabilizer_Dalpha_multiplier = 10.0; // main_cuda.cu:16117
+    p->gp_barrier_only_mode = 1;                           // main_cuda.cu:15823
+    p->enable_legacy_gp_storage_coupling = 0;              // main_cuda.cu:15824
     p->elastic_residual_tolerance = 1.0e-6;
     p->elastic_residual_absolute_floor = 1.0e-30;
     p->eps_iso_over_vB = -1.0;

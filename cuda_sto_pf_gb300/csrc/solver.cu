@@ -2597,6 +2597,13 @@ static pfgb_status validate(const pfgb_params *p) {
                            "pf_composition_stabilizer_Dalpha_multiplier finite and > 0");
         return PFGB_ERR_INVALID;
     }
+    if (p->model_mode == PFGB_MODEL_GP_ZONE && (p->enable_legacy_gp_storage_coupling || !p->gp_barrier_only_mode)) {
+        // gp_storage_coupling_enabled (main_cuda.cu:16767-16772) selects the
+        // storage-coupled Y path and the eta feasibility limiter
+        pfgb_set_error_msg("gp_zone with the GP storage coupling (gp_barrier_only_mode=0 or "
+                           "enable_legacy_gp_storage_coupling=1) is not built");
+        return PFGB_ERR_UNSUPPORTED;
+    }
     // the zero mode and minimize refuse every mode but lagged_rhs
     // (main_cuda.cu:24600-24612, 24692-24702); storage_exact and the x split
     // without the GP storage coupling are the two_phase paths

@@ -158,6 +158,11 @@ typedef struct pfgb_params {
     double gp_h_alpha_eps;
     double pf_matrix_storage_floor;
     double pf_composition_stabilizer_Dalpha_multiplier;
+    /* GP storage coupling switches (gp_storage_coupling_enabled,
+       main_cuda.cu:16767-16772; defaults 1 and 0).  The storage-coupled gp_zone
+       path is not built: pfgb_create refuses gp_zone with coupling on. */
+    int32_t gp_barrier_only_mode;
+    int32_t enable_legacy_gp_storage_coupling;
     /* zero mode (PF_CONSERVED_Y_ZERO_MODE_V1) */
     int32_t zero_mode_enabled;
     int32_t zero_mode_max_iterations;

@@ -78,6 +78,28 @@ def test_unknown_key_warns_and_is_ignored(capi, tmp_path, capfd):
     assert "unknown key ignored: not_a_key" in capfd.readouterr().err
 
 
+@pytest.mark.parametrize("line", ["pf_composition_mode = ctot_conservative_split",
+                                  "y_update_mass_projection_enabled = 1", "enable_Y_rhs_picard = 1",
+                                  "gp_nuc_enabled = 1", "diagnostic_rsmd_enabled = 1",
+                                  "enable_gp_assisted_beta_nucleation = 1"])
+def test_unbuilt_path_selectors_are_refused(capi, tmp_path, line):
+    base = open(os.path.join(GOLDEN, "c1.params")).read()
+    with pytest.raises(capi.PfgbError) as e:
+        capi.load_params_file(_write(tmp_path, base + "\n" + line + "\n"))
+    assert "not built" in str(e.value)
+    # the default value is accepted
+    key = line.split("=")[0].strip()
+    default = "legacy" if key == "pf_composition_mode" else "0"
+    capi.load_params_file(_write(tmp_path, base + "\n%s = %s\n" % (key, default)))
+
+
+def test_gp_storage_coupling_keys(capi, tmp_path):
+    base = open(os.path.join(GOLDEN, "c2.params")).read()
+    p = capi.load_params_file(_write(tmp_path, base + "\ngp_barrier_only_mode = 0\n"))
+    assert p.gp_barrier_only_mode == 0 and p.enable_legacy_gp_storage_coupling == 0
+    assert capi.default_params().gp_barrier_only_mode == 1
+
+
 def test_y_update_mode_key(capi, tmp_path):
     base = open(os.path.join(GOLDEN, "c1.params")).read()
     p = capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = storage_exact\ngp_h_alpha_eps = 1e-6\n"))
@@ -125,3 +147,20 @@ def test_create_rejects_bad_grid_without_touching_gpu(capi):
     p.Nx = 0
     ctx = ctypes.c_void_p()
     assert capi.load().pfgb_create(ctypes.byref(p), 0, ctypes.byref(ctx)) == 1
+
+
+@pytest.mark.parametrize("over", [dict(model_mode=1, gp_barrier_only_mode=0),
+                                  dict(model_mode=1, enable_legacy_gp_storage_coupling=1),
+                                  dict(pf_y_update_mode=1, zero_mode_enabled=1),
+                                  dict(pf_y_update_mode=2, mode=1),
+                                  dict(pf_y_update_mode=2, pf_matrix_storage_floor=0.0),
+                                  dict(pf_y_update_mode=3)])
+def test_create_refuses_unbuilt_or_invalid_composition_paths(capi, over):
+    """Refused by the parameter check before any device work."""
+    p = capi.load_params_file(os.path.join(GOLDEN, "c2.params"))
+    for k, v in over.items():
+        setattr(p, k, v)
+    capi.finalize(p)
+    ctx = ctypes.c_void_p()
+    assert capi.load().pfgb_create(ctypes.byref(p), 0, ctypes.byref(ctx)) in (1, 8)
+    assert not ctx.value
