@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain-fp64", action="store_true")
     ap.add_argument("--no-chebyshev", action="store_true", help="the reference's plain elastic iteration")
+    ap.add_argument("--extrapolate", action="store_true", help="extrapolated elastic warm start")
     ap.add_argument("--profile-json", default="")
     ap.add_argument("--fno-n", type=int, default=128)
     ap.add_argument("--fno-base", type=int, default=128, help="distinct generated microstructures")
@@ -76,6 +77,9 @@ def dist_env():
 # (--no-chebyshev: the reference's plain iteration); the CPU reference arm
 # and the plain FP64 comparison always run the reference's iteration
 CHEBYSHEV = 1
+# --extrapolate: the elastic warm start extrapolated linearly from the last
+# two solutions (same fixed point, fewer iterations when the fields move)
+EXTRAPOLATE = 0
 
 
 def make_params(capi, n, precision, tol, shape=None, chebyshev=None):
@@ -89,6 +93,7 @@ def make_params(capi, n, precision, tol, shape=None, chebyshev=None):
     # a 1e-8 tolerance runs to elastic_iter_max; the step continues there
     p.elastic_fail_on_nonconvergence = 0
     p.elastic_chebyshev = CHEBYSHEV if chebyshev is None else chebyshev
+    p.elastic_warm_start_extrapolate = EXTRAPOLATE if chebyshev is None else 0
     capi.finalize(p)
     return p
 
@@ -684,9 +689,10 @@ def run_fno_step(args):
 
 
 def main():
-    global CHEBYSHEV
+    global CHEBYSHEV, EXTRAPOLATE
     args = parse()
     CHEBYSHEV = 0 if args.no_chebyshev else 1
+    EXTRAPOLATE = 1 if args.extrapolate else 0
     if args.workload == "sweep":
         run_sweep(args)
         return

@@ -23,9 +23,17 @@
 namespace f246 {
 
 constexpr int N = 246;
-constexpr int NL = 48;            // lines per block (6 spectra x 8 columns)
+constexpr int NL = 48;            // lines per block: 6 spectra x TC columns, or ZR z rows x 3 field pairs
+constexpr int TC = NL / 6;        // columns per block of the strided-axis passes (even: 16-byte pairs)
+constexpr int ZR = NL / 3;        // rows per block of the z pass
 constexpr int THREADS = NL * 6;   // one stage-C item per thread
-constexpr int PSTR = 52;          // position stride of the lines-fast layout
+constexpr int BLOCKS_PER_SM = 96 / NL;
+// position stride of the lines-fast layout.  (With NL = 24 a warp's second
+// half of stage-C reads spans two items 41 * PSTR apart, which land on
+// disjoint banks when 82 * PSTR = 16 (mod 32); 24 lines per block measured
+// slower than 48: 32-byte column segments and twice the per-block overhead.)
+constexpr int PSTR = NL == 24 ? 24 : NL + 4;
+static_assert(NL % 6 == 0 && TC % 2 == 0, "lines per block: 6 spectra x an even column count");
 
 // stage A over NL lines; element (line l, position p) at buf[p * PS + l * LS]
 template <int DIR, int PS, int LS>
@@ -118,24 +126,25 @@ constexpr size_t z_smem_bytes() { return (size_t)(N + NL * N) * sizeof(float2); 
 
 // ---------------------------------------------------------------------------
 // y-axis transform of six spectra in place.  Block (bx, i): columns
-// kz = 8 bx .. 8 bx + 7 of x-plane i; line (s, t) = spectrum s, column t.
+// kz = TC bx .. TC bx + TC - 1 of x-plane i; line (s, t) = spectrum s, column t.
 // ---------------------------------------------------------------------------
 template <int DIR>
-__global__ void __launch_bounds__(f246::THREADS, 2)
+__global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
 k_y246(Grid3 g, const float2 *tw_g, AxisIO<float, 6, 6> io) {
     using namespace f246;
+    constexpr int TP = TC / 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     float2 *buf = tw + N;
-    const int k0 = blockIdx.x * 8, i = blockIdx.y;
-    const int kcnt = min(8, g.NzC - k0);
+    const int k0 = blockIdx.x * TC, i = blockIdx.y;
+    const int kcnt = min(TC, g.NzC - k0);
     const long long base = (long long)i * N * g.NzC + k0;   // (i, y = 0, k0)
     // 16-byte copies: (spectrum, y, column pair)
-    for (int e = threadIdx.x; e < 6 * N * 4; e += blockDim.x) {
-        const int tp = e & 3, r = e >> 2;
+    for (int e = threadIdx.x; e < 6 * N * TP; e += blockDim.x) {
+        const int tp = e % TP, r = e / TP;
         const int y = r % N, s = r / N;
         const int t = 2 * tp;
-        float2 *dst = buf + y * PSTR + s * 8 + t;
+        float2 *dst = buf + y * PSTR + s * TC + t;
         const float2 *src = io.in[s] + base + (long long)y * g.NzC + t;
         if (t + 1 < kcnt) {
             const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
@@ -151,11 +160,11 @@ k_y246(Grid3 g, const float2 *tw_g, AxisIO<float, 6, 6> io) {
     __syncthreads();
     lines<DIR, PSTR, 1>(buf, tw);
     // the stage-C outputs are in natural order: position k of line l
-    for (int e = threadIdx.x; e < 6 * N * 4; e += blockDim.x) {
-        const int tp = e & 3, r = e >> 2;
+    for (int e = threadIdx.x; e < 6 * N * TP; e += blockDim.x) {
+        const int tp = e % TP, r = e / TP;
         const int y = r % N, s = r / N;
         const int t = 2 * tp;
-        const float2 *srcs = buf + y * PSTR + s * 8 + t;
+        const float2 *srcs = buf + y * PSTR + s * TC + t;
         float2 *dst = io.out[s] + base + (long long)y * g.NzC + t;
         if (t + 1 < kcnt) *reinterpret_cast<float4 *>(dst) = *reinterpret_cast<const float4 *>(srcs);
         else if (t < kcnt) dst[0] = srcs[0];

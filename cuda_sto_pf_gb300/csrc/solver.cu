@@ -936,6 +936,51 @@ __device__ __forceinline__ void green_update(const GreenArgs<TE> &A, long long o
     rr += w * lr;
 }
 
+// the state the increment update (mode 2) reads at one k-point, loaded as
+// one batch ahead of use: r0, delta, u0 and the Chebyshev iterate before delta
+template <typename TE>
+struct GreenIn { cplx_t<TE> r0[3], d[3], u0[3], dm[3]; };
+
+template <typename TE>
+__device__ __forceinline__ void green_fetch(const GreenArgs<TE> &A, long long o, GreenIn<TE> &in) {
+    const bool cheb = A.Dm[0] != nullptr;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        in.r0[c] = __ldg(A.R[c] + o);
+        in.d[c] = __ldg(A.D[c] + o);
+        in.u0[c] = __ldg(A.U[c] + o);
+        in.dm[c] = cheb ? A.Dm[c][o] : cplx_t<TE>{};
+    }
+}
+
+// green_update's mode 2 on prefetched state; the stores go last
+template <typename TE>
+__device__ __forceinline__ void green_update_in(const GreenArgs<TE> &A, long long o, const GreenIn<TE> &in,
+                                                const cplx_t<TE> u[3], TE w, TE &rd, TE &rr, cplx_t<TE> out[3]) {
+    using T2 = cplx_t<TE>;
+    const bool cheb = A.Dm[0] != nullptr;
+    TE ld_ = 0, lr = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const T2 dn = mk2<T2>(in.r0[c].x + u[c].x, in.r0[c].y + u[c].y);
+        const TE dr = dn.x - in.d[c].x, di = dn.y - in.d[c].y;
+        const TE ur = in.u0[c].x + dn.x, ui = in.u0[c].y + dn.y;
+        ld_ += dr * dr + di * di;
+        lr += ur * ur + ui * ui;
+        if (cheb) {
+            const T2 xm = in.dm[c];
+            const TE yr = in.d[c].x + A.gam * dr, yi = in.d[c].y + A.gam * di;
+            out[c] = mk2<T2>(xm.x + A.rho * (yr - xm.x), xm.y + A.rho * (yi - xm.y));
+        } else {
+            out[c] = dn;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) (cheb ? A.Dm[c] : A.D[c])[o] = out[c];
+    rd += w * ld_;
+    rr += w * lr;
+}
+
 template <typename TE>
 __device__ __forceinline__ void green_u(const TE *S, TE kx, TE ky, TE kz, const cplx_t<TE> t[3],
                                         cplx_t<TE> u[3]) {
@@ -1006,8 +1051,11 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
     // residual sums: per element in elastic precision, per-thread partials
     // (a handful of elements) in elastic precision, block / grid sums in FP64
     TE rd = 0, rr = 0;
+    const bool pre = A.mode == 2;   // increment update: its state loaded as one batch first
     for (int e = threadIdx.x; e < n * TK; e += blockDim.x) {
         const int q = e >> lgTK, l = e & (TK - 1), k = k0 + l;
+        GreenIn<TE> gin;
+        if (pre && l < kcnt) green_fetch<TE>(A, base + q * es + l, gin);
         const int kk = min(k, A.g.NzC - 1);
         const TE kv[3] = {TE(A.kt.kx[q]), TE(A.kt.ky[j]), TE(A.kt.kz[kk])};
         T2 x[6];
@@ -1045,7 +1093,8 @@ k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
         if (l < kcnt) {
             const long long o = base + q * es + l;
             const TE w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? TE(1) : TE(2);
-            green_update<TE>(A, o, u, w, rd, rr, v);
+            if (pre) green_update_in<TE>(A, o, gin, u, w, rd, rr, v);
+            else green_update<TE>(A, o, u, w, rd, rr, v);
         }
 #pragma unroll
         for (int c = 0; c < 6; ++c) oth[q * SP + c * TK + l] = strain_comp<TE>(c, kv[0], kv[1], kv[2], v);
@@ -1128,25 +1177,26 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
 // ---------------------------------------------------------------------------
 // elastic-iteration passes on 246-long axes (FP32, fft246.cuh engine): the
 // same operations as k_x_green / k_zpass<OpHijZ> / the y OpCopy pass, with
-// 48 lines per block in one in-place shared buffer
+// f246::NL lines per block in one in-place shared buffer
 // ---------------------------------------------------------------------------
 template <bool EIGEN>
-__global__ void __launch_bounds__(f246::THREADS, 2)
+__global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
 k_x_green246(GreenArgs<float> A) {
     using namespace f246;
     using T2 = float2;
+    constexpr int TP = TC / 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     float2 *buf = tw + N;
-    const int k0 = blockIdx.x * 8, j = blockIdx.y;
-    const int kcnt = min(8, A.g.NzC - k0);
+    const int k0 = blockIdx.x * TC, j = blockIdx.y;
+    const int kcnt = min(TC, A.g.NzC - k0);
     const long long base = (long long)j * A.g.NzC + k0;
     const long long es = (long long)A.g.Ny * A.g.NzC;   // stride of x
-    for (int e = threadIdx.x; e < 6 * N * 4; e += blockDim.x) {
-        const int tp = e & 3, r = e >> 2;
+    for (int e = threadIdx.x; e < 6 * N * TP; e += blockDim.x) {
+        const int tp = e % TP, r = e / TP;
         const int q = r % N, s = r / N;
         const int t = 2 * tp;
-        float2 *dst = buf + q * PSTR + s * 8 + t;
+        float2 *dst = buf + q * PSTR + s * TC + t;
         const float2 *src = A.E[s] + base + q * es + t;
         if (t + 1 < kcnt) {
             const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
@@ -1162,14 +1212,19 @@ k_x_green246(GreenArgs<float> A) {
     __syncthreads();
     lines<-1, PSTR, 1>(buf, tw);
     float rd = 0.f, rr = 0.f;
-    for (int e = threadIdx.x; e < N * 8; e += blockDim.x) {
-        const int q = e >> 3, l = e & 7, k = k0 + l;
+    // mode 2 (every iteration after the first of a step): the k-point's
+    // r0 / delta / u0 / previous iterate are loaded as one batch first
+    const bool pre = A.mode == 2;
+    for (int e = threadIdx.x; e < N * TC; e += blockDim.x) {
+        const int q = e / TC, l = e % TC, k = k0 + l;
+        GreenIn<float> cur;
+        if (pre && l < kcnt) green_fetch<float>(A, base + q * es + l, cur);
         const int kk = min(k, A.g.NzC - 1);
         const float kv[3] = {float(A.kt.kx[q]), float(A.kt.ky[j]), float(A.kt.kz[kk])};
         float2 *pt = buf + q * PSTR + l;
         T2 x[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) x[c] = pt[c * 8];
+        for (int c = 0; c < 6; ++c) x[c] = pt[c * TC];
         T2 t[3];
         if (EIGEN) {
 #pragma unroll
@@ -1199,10 +1254,11 @@ k_x_green246(GreenArgs<float> A) {
         if (l < kcnt) {
             const long long o = base + q * es + l;
             const float w = (k == 0 || ((A.g.Nz % 2) == 0 && k == A.g.Nz / 2)) ? 1.f : 2.f;
-            green_update<float>(A, o, u, w, rd, rr, v);
+            if (pre) green_update_in<float>(A, o, cur, u, w, rd, rr, v);
+            else green_update<float>(A, o, u, w, rd, rr, v);
         }
 #pragma unroll
-        for (int c = 0; c < 6; ++c) pt[c * 8] = strain_comp<float>(c, kv[0], kv[1], kv[2], v);
+        for (int c = 0; c < 6; ++c) pt[c * TC] = strain_comp<float>(c, kv[0], kv[1], kv[2], v);
     }
     if (A.resid) {
         AccSum2 sacc{double(rd), double(rr)};
@@ -1212,24 +1268,24 @@ k_x_green246(GreenArgs<float> A) {
     }
     __syncthreads();
     lines<+1, PSTR, 1>(buf, tw);
-    for (int e = threadIdx.x; e < 6 * N * 4; e += blockDim.x) {
-        const int tp = e & 3, r = e >> 2;
+    for (int e = threadIdx.x; e < 6 * N * TP; e += blockDim.x) {
+        const int tp = e % TP, r = e / TP;
         const int q = r % N, s = r / N;
         const int t = 2 * tp;
-        const float2 *srcs = buf + q * PSTR + s * 8 + t;
+        const float2 *srcs = buf + q * PSTR + s * TC + t;
         float2 *dst = A.E[s] + base + q * es + t;
         if (t + 1 < kcnt) *reinterpret_cast<float4 *>(dst) = *reinterpret_cast<const float4 *>(srcs);
         else if (t < kcnt) dst[0] = srcs[0];
     }
 }
 
-// z pass with six fields in and six out (C2R -> op.point -> R2C), 16 rows
-// per block: the rows' three field pairs are the block's 48 complex lines
+// z pass with six fields in and six out (C2R -> op.point -> R2C), ZR rows
+// per block: the rows' three field pairs are the block's NL complex lines
 template <class Op>
-__global__ void __launch_bounds__(f246::THREADS, 2)
+__global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
 k_zpass246(Grid3 g, const float2 *tw_g, Op op) {
     using namespace f246;
-    constexpr int R = 16, NC = N / 2 + 1;
+    constexpr int R = ZR, NC = N / 2 + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     float2 *buf = tw + N;
@@ -1299,7 +1355,7 @@ static pfgb_status launch_y246(pfgb_ctx *c, const char *tag) {
     PFGB_CUDA_TRY(allow_smem(kern, smem));
     AxisIO<float, 6, 6> io;
     for (int i = 0; i < 6; ++i) { io.in[i] = (const float2 *)c->E[i]; io.out[i] = (float2 *)c->E[i]; }
-    dim3 grid((c->g.NzC + 7) / 8, c->g.Nx);
+    dim3 grid((c->g.NzC + f246::TC - 1) / f246::TC, c->g.Nx);
     ProfScope ps(c, {tag, 12.0 * (double)c->g.Nk * sizeof(float2)});
     kern<<<grid, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][1], io);
     PFGB_CUDA_TRY(cudaGetLastError());
@@ -1323,7 +1379,7 @@ static pfgb_status launch_green246(pfgb_ctx *c, bool eigen, int resid, int *nblo
     A.partials = c->partials;
     A.resid = resid;
     A.mode = mode;
-    dim3 grid((c->g.NzC + 7) / 8, c->g.Ny);
+    dim3 grid((c->g.NzC + f246::TC - 1) / f246::TC, c->g.Ny);
     ProfScope ps(c, {eigen ? "x_green_eigen" : "x_green_hij",
                      (double)(6 + 3 + 6 + green_extra(c, mode, resid)) * (double)c->g.Nk * sizeof(float2)});
     if (eigen) {
@@ -1346,7 +1402,7 @@ static pfgb_status launch_z246(pfgb_ctx *c, Op op, const char *tag, double extra
     auto kern = k_zpass246<Op>;
     PFGB_CUDA_TRY(allow_smem(kern, smem));
     const long long rows = (long long)c->g.Nx * c->g.Ny;
-    const int nb = (int)((rows + 15) / 16);
+    const int nb = (int)((rows + f246::ZR - 1) / f246::ZR);
     ProfScope ps(c, {tag, 12.0 * (double)c->g.Nk * sizeof(float2) + extra_bytes});
     kern<<<nb, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][2], op);
     PFGB_CUDA_TRY(cudaGetLastError());
