@@ -139,19 +139,22 @@ k_y246(Grid3 g, const float2 *tw_g, AxisIO<float, 6, 6> io) {
     const int k0 = blockIdx.x * TC, i = blockIdx.y;
     const int kcnt = min(TC, g.NzC - k0);
     const long long base = (long long)i * N * g.NzC + k0;   // (i, y = 0, k0)
-    // 16-byte copies: (spectrum, y, column pair)
-    for (int e = threadIdx.x; e < 6 * N * TP; e += blockDim.x) {
-        const int tp = e % TP, r = e / TP;
-        const int y = r % N, s = r / N;
-        const int t = 2 * tp;
-        float2 *dst = buf + y * PSTR + s * TC + t;
-        const float2 *src = io.in[s] + base + (long long)y * g.NzC + t;
-        if (t + 1 < kcnt) {
-            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src));
-        } else {
-            dst[0] = t < kcnt ? src[0] : make_float2(0.f, 0.f);
-            dst[1] = make_float2(0.f, 0.f);
+    // 16-byte copies: (spectrum, y, column pair); the spectrum loop is
+    // unrolled so that io.in[s] is a compile-time index
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
+        for (int e = threadIdx.x; e < N * TP; e += blockDim.x) {
+            const int tp = e % TP, y = e / TP;
+            const int t = 2 * tp;
+            float2 *dst = buf + y * PSTR + s * TC + t;
+            const float2 *src = io.in[s] + base + (long long)y * g.NzC + t;
+            if (t + 1 < kcnt) {
+                const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src));
+            } else {
+                dst[0] = t < kcnt ? src[0] : make_float2(0.f, 0.f);
+                dst[1] = make_float2(0.f, 0.f);
+            }
         }
     }
     cp_async_commit();
@@ -160,13 +163,15 @@ k_y246(Grid3 g, const float2 *tw_g, AxisIO<float, 6, 6> io) {
     __syncthreads();
     lines<DIR, PSTR, 1>(buf, tw);
     // the stage-C outputs are in natural order: position k of line l
-    for (int e = threadIdx.x; e < 6 * N * TP; e += blockDim.x) {
-        const int tp = e % TP, r = e / TP;
-        const int y = r % N, s = r / N;
-        const int t = 2 * tp;
-        const float2 *srcs = buf + y * PSTR + s * TC + t;
-        float2 *dst = io.out[s] + base + (long long)y * g.NzC + t;
-        if (t + 1 < kcnt) *reinterpret_cast<float4 *>(dst) = *reinterpret_cast<const float4 *>(srcs);
-        else if (t < kcnt) dst[0] = srcs[0];
+#pragma unroll
+    for (int s = 0; s < 6; ++s) {
+        for (int e = threadIdx.x; e < N * TP; e += blockDim.x) {
+            const int tp = e % TP, y = e / TP;
+            const int t = 2 * tp;
+            const float2 *srcs = buf + y * PSTR + s * TC + t;
+            float2 *dst = io.out[s] + base + (long long)y * g.NzC + t;
+            if (t + 1 < kcnt) *reinterpret_cast<float4 *>(dst) = *reinterpret_cast<const float4 *>(srcs);
+            else if (t < kcnt) dst[0] = srcs[0];
+        }
     }
 }

@@ -699,22 +699,39 @@ struct OpYFinalZ {
 // at once; used for the bracket ends and when the Taylor model is out of range.
 // TV = evaluation precision: double for every convergence decision; the
 // field precision for the bracket-end check, whose margin is then verified
-template <typename T, typename TV>
+// mass and its derivative at NL trial multipliers (NL = 1 or 2; compile
+// time, so the sums stay in registers).  sigmoid(y + lam) is evaluated as
+// 1 / (1 + e^-y e^-lam): one exponential per cell, e^-lam once per thread.
+// Cells with |y| beyond half the exponent range of TV (where e^-y could
+// overflow) take sigmoid(y + lam) directly.
+template <typename T, typename TV, int NL>
 __global__ void k_zm_eval(const T *Y, const T *phi, long long N, double Yc, double vB,
-                          const double *lam, int nl, double *partials) {
-    double m[4] = {0, 0, 0, 0}, dd[4] = {0, 0, 0, 0};
+                          const double *lam, double *partials) {
+    constexpr double kBig = sizeof(TV) == 4 ? 40.0 : 300.0;
+    double m[NL], dd[NL], lv[NL];
+    TV el[NL];
+#pragma unroll
+    for (int q = 0; q < NL; ++q) {
+        m[q] = 0.0; dd[q] = 0.0; lv[q] = lam[q];
+        el[q] = fabs(lv[q]) < kBig ? exp(TV(-lv[q])) : TV(0);
+    }
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
          i += (long long)gridDim.x * blockDim.x) {
         const TV h = pf_h(TV(phi[i]));
         const TV a = TV(1) - h;
         const double y = double(Y[i]) + Yc;
-        for (int q = 0; q < nl; ++q) {
-            const TV x = sigmoid_raw(TV(y + lam[q]));
-            m[q] += double(a * x + h * TV(vB));
+        const TV ey = exp(TV(-y));
+        const double hv = double(h * TV(vB));
+#pragma unroll
+        for (int q = 0; q < NL; ++q) {
+            const TV x = (fabs(y) < kBig && fabs(lv[q]) < kBig) ? TV(1) / (TV(1) + ey * el[q])
+                                                               : sigmoid_raw(TV(y + lv[q]));
+            m[q] += double(a * x) + hv;
             dd[q] += double(a * x * (TV(1) - x));
         }
     }
-    for (int q = 0; q < nl; ++q) {
+#pragma unroll
+    for (int q = 0; q < NL; ++q) {
         AccSum2 s{m[q], dd[q]};
         block_reduce_acc(s);
         if (threadIdx.x == 0) reinterpret_cast<AccSum2 *>(partials)[q * gridDim.x + blockIdx.x] = s;
@@ -1293,6 +1310,8 @@ k_zpass246(Grid3 g, const float2 *tw_g, Op op) {
     const long long nrows = (long long)g.Nx * g.Ny;
     const int rcnt = (int)min((long long)R, nrows - row0);
     load_twiddles(tw, tw_g);
+    // unrolled by two: two trips' spectral loads in flight together
+#pragma unroll 2
     for (int e = threadIdx.x; e < R * NC; e += blockDim.x) {
         const int rr = e / NC, k = e - rr * NC;
         float2 v[6];
@@ -1765,15 +1784,16 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     const long long N = c->g.N;
     const int eb = 304;
     auto direct = [&](const double *lams, int nl, double *mass, double *der, bool exact = true) -> pfgb_status {
+        if (nl < 1 || nl > 2) return fail("internal: 1 or 2 trial multipliers per evaluation");
         PFGB_CUDA_TRY(cudaMemcpyAsync(c->dscal + DS_EV, lams, sizeof(double) * nl, cudaMemcpyHostToDevice, c->stream));
         {
             ProfScope ps(c, {"zero_mode_eval", (double)N * 2.0 * sizeof(T)});
-            if (exact)
-                k_zm_eval<T, double><<<eb, 256, 0, c->stream>>>((const T *)c->Y, (const T *)c->phi[1 - c->cur], N,
-                                                                c->Yc, P.v_B, c->dscal + DS_EV, nl, c->partials);
-            else
-                k_zm_eval<T, T><<<eb, 256, 0, c->stream>>>((const T *)c->Y, (const T *)c->phi[1 - c->cur], N,
-                                                           c->Yc, P.v_B, c->dscal + DS_EV, nl, c->partials);
+            const T *Yp = (const T *)c->Y, *ph = (const T *)c->phi[1 - c->cur];
+            const double *lp = c->dscal + DS_EV;
+            if (exact && nl == 2) k_zm_eval<T, double, 2><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
+            else if (exact) k_zm_eval<T, double, 1><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
+            else if (nl == 2) k_zm_eval<T, T, 2><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
+            else k_zm_eval<T, T, 1><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
         }
         PFGB_CUDA_TRY(cudaGetLastError());
         for (int q = 0; q < nl; ++q) {
