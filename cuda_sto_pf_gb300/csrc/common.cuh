@@ -60,17 +60,32 @@ template <typename T> PFGB_HD T clamp_eps(T v, T e) {
 // For a fixed temperature every quantity the kernels need reduces to a few
 // constants: mu_A(x) = (G_A + RT ln(1-x) + L x^2) / s,
 //            mu_B(x) = (G_B + RT ln x + L (1-x)^2) / s.
-// ThermoConst holds those constants, computed once on the host in FP64.
+// ThermoConst holds those constants, computed once on the host in FP64;
+// FP32 kernels receive a float copy (ThermoConstT<float>) so that every
+// constant is a plain operand of their arithmetic.
 // ---------------------------------------------------------------------------
-struct ThermoConst {
-    double GA_s, GB_s;     // G_PbTe / s, G_Ag2Te / s
-    double RT_s, L_s;      // R T / s, L(T) / s
+template <typename S>
+struct ThermoConstT {
+    S GA_s, GB_s;          // G_PbTe / s, G_Ag2Te / s
+    S RT_s, L_s;           // R T / s, L(T) / s
     int convex;            // thermo_convex_extrapolation_enabled
     // convex-extrapolation anchors at xc = 0.09: offsets (mu - G_s) and
     // slopes, already divided by s
-    double muA_c, dmuA_c, muB_c, dmuB_c;
-    double Kpen_s;         // 5000 / s
+    S muA_c, dmuA_c, muB_c, dmuB_c;
+    S Kpen_s;              // 5000 / s
+    S ddmu_c;              // dmuB_c - dmuA_c, formed in FP64
 };
+using ThermoConst = ThermoConstT<double>;
+
+template <typename S>
+ThermoConstT<S> thermo_as(const ThermoConst &c) {
+    ThermoConstT<S> t;
+    t.GA_s = S(c.GA_s); t.GB_s = S(c.GB_s); t.RT_s = S(c.RT_s); t.L_s = S(c.L_s);
+    t.convex = c.convex;
+    t.muA_c = S(c.muA_c); t.dmuA_c = S(c.dmuA_c); t.muB_c = S(c.muB_c); t.dmuB_c = S(c.dmuB_c);
+    t.Kpen_s = S(c.Kpen_s); t.ddmu_c = S(c.ddmu_c);
+    return t;
+}
 
 #define PFGB_RGAS 8.31446261815324
 #define PFGB_XC_CONVEX 0.09
@@ -86,8 +101,8 @@ void pfgb_thermo_const(double T, double scale, int convex, ThermoConst *tc);
 // dependent part, so FP32 kernels can form differences such as mu_B - mu_A or
 // mu0 - mu_B without cancelling a large constant.  x is clamped to
 // [1e-12, 1-1e-12] like clamp_fraction_eps.
-template <typename T>
-PFGB_HD void thermo_mu_off(const ThermoConst &c, T xB, T &offA, T &offB) {
+template <typename T, typename TC>
+PFGB_HD void thermo_mu_off(const TC &c, T xB, T &offA, T &offB) {
     if (c.convex && xB > T(PFGB_XC_CONVEX)) {
         T d = xB - T(PFGB_XC_CONVEX);
         offA = T(c.muA_c) + T(c.dmuA_c) * d + T(c.Kpen_s) * d * d;
@@ -99,8 +114,8 @@ PFGB_HD void thermo_mu_off(const ThermoConst &c, T xB, T &offA, T &offB) {
     offA = T(c.RT_s) * log(omx) + T(c.L_s) * x * x;
     offB = T(c.RT_s) * log(x) + T(c.L_s) * omx * omx;
 }
-template <typename T>
-PFGB_HD void thermo_mu(const ThermoConst &c, T xB, T &muA, T &muB) {
+template <typename T, typename TC>
+PFGB_HD void thermo_mu(const TC &c, T xB, T &muA, T &muB) {
     T a, b;
     thermo_mu_off<T>(c, xB, a, b);
     muA = T(c.GA_s) + a;
@@ -114,7 +129,8 @@ PFGB_HD void thermo_mu(const ThermoConst &c, T xB, T &muA, T &muB) {
 // O(1e-10) relative, far below FP32 resolution).
 template <typename T> struct GammaEval;
 template <> struct GammaEval<double> {
-    static PFGB_HD double dmu_diff(const ThermoConst &c, double xc) {
+    template <typename TC>
+    static PFGB_HD double dmu_diff(const TC &c, double xc) {
         double dx = 1e-5;
         double xp = clamp_eps(xc + dx, 1e-12), xm = clamp_eps(xc - dx, 1e-12);
         double aP, bP, aM, bM;
@@ -126,12 +142,13 @@ template <> struct GammaEval<double> {
     }
 };
 template <> struct GammaEval<float> {
-    static PFGB_HD float dmu_diff(const ThermoConst &c, float xc) {
+    template <typename TC>
+    static PFGB_HD float dmu_diff(const TC &c, float xc) {
         // d/dx[(G_B - G_A) + RT ln(x/(1-x)) + L((1-x)^2 - x^2)]
         //   = RT / (x (1-x)) - 2 L     (regular-solution branch)
         if (c.convex && xc > float(PFGB_XC_CONVEX)) {
             // both extrapolations are quadratics with equal curvature
-            return float(c.dmuB_c - c.dmuA_c);
+            return float(c.ddmu_c);
         }
         float x = clamp_eps(xc, 1e-12f);
         return float(c.RT_s) / (x * (1.0f - x)) - 2.0f * float(c.L_s);
@@ -157,8 +174,8 @@ PFGB_HD T stabilized_meff(T Dm, T g) {
 }
 
 // thermodynamic factor, gamma_thermo_nonlinear (thermo_utils.h:552-577)
-template <typename T>
-PFGB_HD T gamma_thermo(const ThermoConst &c, T xB, T h, T Vm0, T dVm, T Vmc) {
+template <typename T, typename TC>
+PFGB_HD T gamma_thermo(const TC &c, T xB, T h, T Vm0, T dVm, T Vmc) {
     T xc = xB;
     if (c.convex && xc > T(0.08)) xc = T(0.08);
     T cb = c_xB_phi(xc, Vm0, dVm, Vmc, h);

@@ -19,6 +19,8 @@
 // of the reference.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "rader41.cuh"
 
@@ -529,6 +531,14 @@ k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
     }
 }
 
+// ops of the z pass may declare kBatch > 1 with a Pre type, fetch(cell, pre)
+// and point_with(cell, pre, in, out, acc): their global reads are then
+// issued for kBatch cells of a thread at once
+template <class Op, class = void>
+struct op_batch { static constexpr int value = 1; };
+template <class Op>
+struct op_batch<Op, std::void_t<decltype(Op::kBatch)>> { static constexpr int value = Op::kBatch; };
+
 // identity op for plain axis transforms
 template <typename T, int NF>
 struct OpCopy {
@@ -645,7 +655,7 @@ k_zpass(Grid3 g, AxisPlan plan, const cplx_t<T> *tw_g, int R, Op op) {
     if constexpr (SAME) { outA = inA; outB = inB; }
     // pointwise stage
     typename Op::Acc acc = Op::Acc::identity();
-    for (int e = threadIdx.x; e < R * n; e += blockDim.x) {
+    auto cell_step = [&](int e, auto &&pointf) {
         const int r = e / n, z = e - r * n;
         if (r >= rcnt) {
             if (NFO > 0) {
@@ -656,7 +666,7 @@ k_zpass(Grid3 g, AxisPlan plan, const cplx_t<T> *tw_g, int R, Op op) {
                     dst[l & 1] = T(0);
                 }
             }
-            continue;
+            return;
         }
         T vi[NFI > 0 ? NFI : 1], vo[NFO > 0 ? NFO : 1];
 #pragma unroll
@@ -665,14 +675,37 @@ k_zpass(Grid3 g, AxisPlan plan, const cplx_t<T> *tw_g, int R, Op op) {
             const T *src = reinterpret_cast<const T *>(&inA[(l >> 1) * n + z]);
             vi[f] = src[l & 1];
         }
-        const long long cell = (row0 + r) * n + z;
-        op.point(cell, vi, vo, acc);
+        pointf((row0 + r) * n + z, vi, vo);
 #pragma unroll
         for (int f = 0; f < NFO; ++f) {
             const int l = r * NFO + f;
             T *dst = reinterpret_cast<T *>(&outA[(l >> 1) * n + z]);
             dst[l & 1] = vo[f];
         }
+    };
+    constexpr int B = op_batch<Op>::value;
+    if constexpr (B > 1) {
+        // the op's global reads of B cells go out together before any of
+        // their stores (an op that reads and writes the same field cannot
+        // have them reordered by the compiler)
+        for (int e0 = threadIdx.x; e0 < R * n; e0 += B * blockDim.x) {
+            typename Op::Pre pre[B];
+#pragma unroll
+            for (int b = 0; b < B; ++b) {
+                const int e = e0 + b * blockDim.x;
+                const int r = e / n;
+                if (e < R * n && r < rcnt) op.fetch((row0 + r) * n + (e - r * n), pre[b]);
+            }
+#pragma unroll
+            for (int b = 0; b < B; ++b) {
+                const int e = e0 + b * blockDim.x;
+                if (e < R * n)
+                    cell_step(e, [&](long long cell, const T *vi, T *vo) { op.point_with(cell, pre[b], vi, vo, acc); });
+            }
+        }
+    } else {
+        for (int e = threadIdx.x; e < R * n; e += blockDim.x)
+            cell_step(e, [&](long long cell, const T *vi, T *vo) { op.point(cell, vi, vo, acc); });
     }
     if constexpr (Op::Acc::kActive) {
         block_reduce_acc(acc);

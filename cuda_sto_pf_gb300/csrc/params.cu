@@ -51,6 +51,7 @@ void pfgb_thermo_const(double T, double scale, int convex, ThermoConst *tc) {
     tc->dmuA_c = (-RT / (1.0 - xc) + 2.0 * L * xc) / s;
     tc->dmuB_c = (RT / xc - 2.0 * L * (1.0 - xc)) / s;
     tc->Kpen_s = 5000.0 / s;
+    tc->ddmu_c = tc->dmuB_c - tc->dmuA_c;
 }
 
 namespace {

@@ -19,36 +19,64 @@ __host__ __device__ __forceinline__ int tvoigt(int i, int j) {
 }
 
 // Constants of the physics, FP64 on the host, passed by value to kernels.
-struct PhysC {
+// Kernels on FP32 fields take the float copy PhysCT<float> (phys_as): each
+// constant is then a plain operand rather than a conversion per use.
+template <typename R>
+struct PhysCT {
     // grid / time
-    double dt, invN;
+    R dt, invN;
     // Allen-Cahn phi
-    double W, kappa, Lphi;
+    R W, kappa, Lphi;
+    R Ldt, gpLdt;      // L_phi dt and L_eta dt, formed in FP64
     // transport
-    double Da, Dc;
-    double vA, vB, Vm0, dVm, Vmc;
-    double mu0, eiv, Yclip, xBeps, hscale;
-    double Cdmu;            // mu0 - vA GA_s - vB GB_s - shift (cancellation-free delta_mu)
-    double dG;              // GB_s - GA_s
-    double shift;
-    double e00[6], E0[6];
-    double S[21], Sp[21];
+    R Da, Dc;
+    R vA, vB, Vm0, dVm, Vmc;
+    R mu0, eiv, Yclip, xBeps, hscale;
+    R Cdmu;            // mu0 - vA GA_s - vB GB_s - shift (cancellation-free delta_mu)
+    R dG;              // GB_s - GA_s
+    R shift;
+    R e00[6], E0[6];
+    R S[21], Sp[21];
     // GP zone
-    double gpxB, gpW, gpkap, gpL, gpMGP, gpMb, gpeiso, gpscale;
-    double gp_Cg;           // offA(xg)(1-xg) + offB(xg) xg - delta_g0
+    R gpxB, gpW, gpkap, gpL, gpMGP, gpMb, gpeiso, gpscale;
+    R gp_Cg;           // offA(xg)(1-xg) + offB(xg) xg - delta_g0
     int gp, gp_el, act_eta, act_phi;
     int coupling, elastic, zm, prev_level, disable_gamma, xb_raw;
     // upper cap on the composition seen by the eigenstrain of the elastic
     // solve and the stress (minimize_xB_max_safe once the minimize monitor
     // has clamped xB; above 1 = inactive)
-    double xbcap;
-    double dx, dy, dz;
-    ThermoConst tc;
+    R xbcap;
+    R dx, dy, dz;
+    ThermoConstT<R> tc;
 };
+using PhysC = PhysCT<double>;
+
+template <typename R>
+PhysCT<R> phys_as(const PhysC &c) {
+    PhysCT<R> o;
+    o.dt = R(c.dt); o.invN = R(c.invN);
+    o.W = R(c.W); o.kappa = R(c.kappa); o.Lphi = R(c.Lphi);
+    o.Ldt = R(c.Lphi * c.dt); o.gpLdt = R(c.gpL * c.dt);
+    o.Da = R(c.Da); o.Dc = R(c.Dc);
+    o.vA = R(c.vA); o.vB = R(c.vB); o.Vm0 = R(c.Vm0); o.dVm = R(c.dVm); o.Vmc = R(c.Vmc);
+    o.mu0 = R(c.mu0); o.eiv = R(c.eiv); o.Yclip = R(c.Yclip); o.xBeps = R(c.xBeps); o.hscale = R(c.hscale);
+    o.Cdmu = R(c.Cdmu); o.dG = R(c.dG); o.shift = R(c.shift);
+    for (int i = 0; i < 6; ++i) { o.e00[i] = R(c.e00[i]); o.E0[i] = R(c.E0[i]); }
+    for (int i = 0; i < 21; ++i) { o.S[i] = R(c.S[i]); o.Sp[i] = R(c.Sp[i]); }
+    o.gpxB = R(c.gpxB); o.gpW = R(c.gpW); o.gpkap = R(c.gpkap); o.gpL = R(c.gpL);
+    o.gpMGP = R(c.gpMGP); o.gpMb = R(c.gpMb); o.gpeiso = R(c.gpeiso); o.gpscale = R(c.gpscale);
+    o.gp_Cg = R(c.gp_Cg);
+    o.gp = c.gp; o.gp_el = c.gp_el; o.act_eta = c.act_eta; o.act_phi = c.act_phi;
+    o.coupling = c.coupling; o.elastic = c.elastic; o.zm = c.zm; o.prev_level = c.prev_level;
+    o.disable_gamma = c.disable_gamma; o.xb_raw = c.xb_raw;
+    o.xbcap = R(c.xbcap); o.dx = R(c.dx); o.dy = R(c.dy); o.dz = R(c.dz);
+    o.tc = thermo_as<R>(c.tc);
+    return o;
+}
 
 // composition entering eps0 on the elastic side: clamp01, then the cap
-template <typename T>
-__device__ __forceinline__ T xB_el(const PhysC &c, T xB) {
+template <typename T, typename PC>
+__device__ __forceinline__ T xB_el(const PC &c, T xB) {
     const T x = clamp01(xB);
     return x < T(c.xbcap) ? x : T(c.xbcap);
 }
@@ -64,15 +92,15 @@ struct ElasC {
 // xB from the logit Y: clipped form (sigmoid_from_logit) unless the zero mode
 // owns the composition, which uses the unclipped logistic
 // (apply_pf_Y_zero_mode_shift_kernel, cuda_kernels.cu:3434-3442).
-template <typename T>
-__device__ __forceinline__ T xB_of_Y(const PhysC &c, T Y) {
+template <typename T, typename PC>
+__device__ __forceinline__ T xB_of_Y(const PC &c, T Y) {
     return c.xb_raw ? sigmoid_raw(Y) : sigmoid_clip(Y, T(c.Yclip), T(c.xBeps));
 }
 
 // eigenstrain_phi_xB_point / eigenstrain_phi_eta_xB_point
 // (cuda_kernels.cu:193-290); gp3 selects the three-phase GP form.
-template <typename T, typename TE>
-__device__ __forceinline__ void eigenstrain(const PhysC &c, const ElasC<TE> &ec, T phi, T eta,
+template <typename T, typename TE, typename PC>
+__device__ __forceinline__ void eigenstrain(const PC &c, const ElasC<TE> &ec, T phi, T eta,
                                             T xBc, bool gp3, TE e0[6]) {
     if (!gp3) {
         T h = pf_h(phi);
@@ -96,8 +124,8 @@ __device__ __forceinline__ void eigenstrain(const PhysC &c, const ElasC<TE> &ec,
 // Hooke's law with C_eff = C0 + h dC on the elastic strain eps - eps0,
 // engineering shear (compute_stress_from_strain_with_effective_stiffness_kernel,
 // cuda_kernels.cu:7381-7480).
-template <typename T, typename TE>
-__device__ __forceinline__ void stress_at(const PhysC &c, const ElasC<TE> &ec, T phi, T eta, T xB,
+template <typename T, typename TE, typename PC>
+__device__ __forceinline__ void stress_at(const PC &c, const ElasC<TE> &ec, T phi, T eta, T xB,
                                           const TE eps[6], TE sig[6]) {
     TE e0[6];
     eigenstrain<T, TE>(c, ec, phi, eta, xB_el(c, xB), c.gp_el != 0, e0);
@@ -119,8 +147,8 @@ __device__ __forceinline__ void stress_at(const PhysC &c, const ElasC<TE> &ec, T
 }
 
 // e^T dC e with engineering shear (compute_Q_voigt, cuda_kernels.cu:162-181)
-template <typename T>
-__device__ __forceinline__ T q_voigt(const double *Sp, const T el[6]) {
+template <typename T, typename SP>
+__device__ __forceinline__ T q_voigt(const SP *Sp, const T el[6]) {
     T e[6] = {el[0], el[1], el[2], T(2) * el[3], T(2) * el[4], T(2) * el[5]};
     T q = 0;
 #pragma unroll
@@ -135,8 +163,8 @@ __device__ __forceinline__ T q_voigt(const double *Sp, const T el[6]) {
 // explicit Allen-Cahn driving force of phi (compute_phi_rhs_kernel,
 // cuda_kernels.cu:390-555): double well + chemical + elastic, with the
 // stress given (the reference reads its stored sigma arrays)
-template <typename T, typename TE>
-__device__ __forceinline__ T phi_rhs_sig(const PhysC &c, const ElasC<TE> &ec, T phi, T eta_raw, T xBraw,
+template <typename T, typename TE, typename PC>
+__device__ __forceinline__ T phi_rhs_sig(const PC &c, const ElasC<TE> &ec, T phi, T eta_raw, T xBraw,
                                          const TE *eps, const TE *sg_) {
     const T hp = pf_hp(phi), gp = pf_gp(phi), h = pf_h(phi);
     const T eta = clamp01(eta_raw);
@@ -194,8 +222,8 @@ __device__ __forceinline__ T phi_rhs_sig(const PhysC &c, const ElasC<TE> &ec, T 
 
 // the same with sigma from Hooke's law at (phi, eta, xB): the dynamics step,
 // where the stored stress of the reference is that of the current fields
-template <typename T, typename TE>
-__device__ __forceinline__ T phi_rhs(const PhysC &c, const ElasC<TE> &ec, T phi, T eta_raw, T xBraw,
+template <typename T, typename TE, typename PC>
+__device__ __forceinline__ T phi_rhs(const PC &c, const ElasC<TE> &ec, T phi, T eta_raw, T xBraw,
                                      const TE *eps) {
     TE sg[6];
     if (c.coupling) stress_at<T, TE>(c, ec, phi, eta_raw, xBraw, eps, sg);
@@ -204,8 +232,8 @@ __device__ __forceinline__ T phi_rhs(const PhysC &c, const ElasC<TE> &ec, T phi,
 
 // GP-zone Allen-Cahn driving force of eta (compute_eta_rhs_kernel,
 // non-raw-drive branch, cuda_kernels.cu:845-946)
-template <typename T, typename TE>
-__device__ __forceinline__ T eta_rhs(const PhysC &c, const ElasC<TE> &ec, T eta_raw, T phi_raw,
+template <typename T, typename TE, typename PC>
+__device__ __forceinline__ T eta_rhs(const PC &c, const ElasC<TE> &ec, T eta_raw, T phi_raw,
                                      T xBraw, T sig_hydro) {
     const T eta = clamp01(eta_raw), phi = clamp01(phi_raw);
     const T xa = clamp_eps(xBraw, T(1e-12));
@@ -228,8 +256,8 @@ __device__ __forceinline__ T eta_rhs(const PhysC &c, const ElasC<TE> &ec, T eta_
 
 // transport mobility (compute_flux_single_component_kernel :1985 and the
 // GP variant :2039)
-template <typename T>
-__device__ __forceinline__ T mobility(const PhysC &c, T phiY, T etaN, T xBp) {
+template <typename T, typename PC>
+__device__ __forceinline__ T mobility(const PC &c, T phiY, T etaN, T xBp) {
     if (!c.gp) {
         const T h = pf_h(phiY);
         const T Dm = (T(1) - h) * T(c.Da) + h * T(c.Dc);

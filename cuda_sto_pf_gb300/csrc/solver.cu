@@ -324,18 +324,28 @@ static pfgb_status reduce_to(pfgb_ctx *c, int nblocks, int slot, double scale = 
 template <typename T, typename TE>
 struct OpPhiR2C {   // z pass producer: phi - L dt rhs_phi
     using Acc = NoAcc;
-    DevState<T, TE> d; PhysC c; ElasC<TE> ec;
-    __device__ void point(long long cell, const T *, T *out, Acc &) const {
-        const T phi = d.phi_old[cell];
-        const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
-        const T eta = c.gp ? d.eta_old[cell] : T(0);
-        TE e[6];
+    DevState<T, TE> d; PhysCT<T> c; ElasC<TE> ec;
+    // the fields of two cells read ahead of their work
+    static constexpr int kBatch = 2;
+    struct Pre { T phi, Y, eta; TE e[6]; };
+    __device__ void fetch(long long cell, Pre &p) const {
+        p.phi = d.phi_old[cell];
+        p.Y = d.Y[cell];
+        p.eta = c.gp ? d.eta_old[cell] : T(0);
         if (c.coupling) {
 #pragma unroll
-            for (int a = 0; a < 6; ++a) e[a] = d.eps[a][cell];
+            for (int a = 0; a < 6; ++a) p.e[a] = d.eps[a][cell];
         }
-        const T r = phi_rhs<T, TE>(c, ec, phi, eta, xB, e);
-        out[0] = phi - T(c.Lphi * c.dt) * r;
+    }
+    __device__ void point(long long cell, const T *in, T *out, Acc &acc) const {
+        Pre p;
+        fetch(cell, p);
+        point_with(cell, p, in, out, acc);
+    }
+    __device__ void point_with(long long, const Pre &p, const T *, T *out, Acc &) const {
+        const T xB = xB_of_Y<T>(c, p.Y + T(d.Yc));
+        const T r = phi_rhs<T, TE>(c, ec, p.phi, p.eta, xB, p.e);
+        out[0] = p.phi - T(c.Ldt) * r;
     }
     __device__ void load_spec(long long, int, cplx_t<T> *) const {}
     __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
@@ -346,7 +356,7 @@ struct OpPhiR2C {   // z pass producer: phi - L dt rhs_phi
 template <typename T, typename TE>
 struct OpEtaR2C {   // z pass producer: eta - L_eta dt rhs_eta (phi = updated phi)
     using Acc = NoAcc;
-    DevState<T, TE> d; PhysC c; ElasC<TE> ec;
+    DevState<T, TE> d; PhysCT<T> c; ElasC<TE> ec;
     __device__ void point(long long cell, const T *, T *out, Acc &) const {
         const T eta = d.eta_old[cell];
         const T phi = d.phi_new[cell];
@@ -360,7 +370,7 @@ struct OpEtaR2C {   // z pass producer: eta - L_eta dt rhs_eta (phi = updated ph
             sh = T(s[0]) + T(s[1]) + T(s[2]);
         }
         const T r = eta_rhs<T, TE>(c, ec, eta, phi, xB, sh);
-        out[0] = eta - T(c.gpL * c.dt) * r;
+        out[0] = eta - T(c.gpLdt) * r;
     }
     __device__ void load_spec(long long, int, cplx_t<T> *) const {}
     __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
@@ -401,10 +411,28 @@ struct OpACStoreZ {   // z pass consumer: clamp and store the new order paramete
 template <typename T, typename TE>
 struct OpMuR2C {
     using Acc = AccSum1;
-    DevState<T, TE> d; PhysC c; ElasC<TE> ec;
-    __device__ void point(long long cell, const T *, T *out, Acc &acc) const {
-        const T Yv = d.Y[cell] + T(d.Yc);
-        const T phiY = (c.zm || c.prev_level) ? d.phi_old[cell] : d.phi_new[cell];
+    DevState<T, TE> d; PhysCT<T> c; ElasC<TE> ec;
+    // the fields of two cells read ahead of their work
+    static constexpr int kBatch = 2;
+    struct Pre { T Y, po, pn, eta; TE e[6]; };
+    __device__ void fetch(long long cell, Pre &p) const {
+        p.Y = d.Y[cell];
+        p.po = d.phi_old[cell];
+        p.pn = (c.zm || c.prev_level) ? p.po : d.phi_new[cell];
+        p.eta = (c.elastic && c.gp) ? d.eta_old[cell] : T(0);
+        if (c.elastic) {
+#pragma unroll
+            for (int a = 0; a < 6; ++a) p.e[a] = d.eps[a][cell];
+        }
+    }
+    __device__ void point(long long cell, const T *in, T *out, Acc &acc) const {
+        Pre p;
+        fetch(cell, p);
+        point_with(cell, p, in, out, acc);
+    }
+    __device__ void point_with(long long, const Pre &p, const T *, T *out, Acc &acc) const {
+        const T Yv = p.Y + T(d.Yc);
+        const T phiY = p.pn;
         const T xB = sigmoid_clip(Yv, T(c.Yclip), T(c.xBeps));
         T offA, offB;
         thermo_mu_off<T>(c.tc, xB, offA, offB);
@@ -421,11 +449,9 @@ struct OpMuR2C {
         }
         if (c.elastic) {
             // stress of the elastic solve of this step: phi, eta, xB at step start
-            TE e[6], s[6];
-#pragma unroll
-            for (int a = 0; a < 6; ++a) e[a] = d.eps[a][cell];
+            TE s[6];
             const T xB0 = xB_of_Y<T>(c, Yv);
-            stress_at<T, TE>(c, ec, d.phi_old[cell], c.gp ? d.eta_old[cell] : T(0), xB0, e, s);
+            stress_at<T, TE>(c, ec, p.po, p.eta, xB0, p.e, s);
             mu += -T(c.eiv) * (T(s[0]) + T(s[1]) + T(s[2]));
         }
         out[0] = mu;
@@ -465,18 +491,33 @@ struct OpGradX {
 template <typename T, typename TE>
 struct OpFluxZ {
     using Acc = NoAcc;
-    DevState<T, TE> d; PhysC c;
+    DevState<T, TE> d; PhysCT<T> c;
     __device__ void load_spec(long long row, int k, cplx_t<T> *v) const {
         const long long o = row * d.g.NzC + k;
         v[0] = d.S[0][o]; v[1] = d.S[1][o]; v[2] = d.S[2][o];
     }
-    __device__ void point(long long cell, const T *g, T *out, Acc &) const {
-        const T Yf = d.Y[cell];
+    // the five fields of four cells read ahead of their work
+    static constexpr int kBatch = 4;
+    struct Pre { T Y, pn, pp, eta, dydt; };
+    __device__ void fetch(long long cell, Pre &p) const {
+        p.Y = d.Y[cell];
+        p.pn = d.phi_old[cell];
+        p.pp = d.phi_new[cell];
+        p.eta = c.gp ? d.eta_new[cell] : T(0);
+        p.dydt = d.dYdt[cell];
+    }
+    __device__ void point(long long cell, const T *g, T *out, Acc &acc) const {
+        Pre p;
+        fetch(cell, p);
+        point_with(cell, p, g, out, acc);
+    }
+    __device__ void point_with(long long, const Pre &p, const T *g, T *out, Acc &) const {
+        const T Yf = p.Y;
         const T Yv = Yf + T(d.Yc);
-        const T pn = d.phi_old[cell], pp = d.phi_new[cell];
+        const T pn = p.pn, pp = p.pp;
         const T phiY = (c.zm || c.prev_level) ? pn : pp;
         const T xBp = sigmoid_clip(Yv, T(c.Yclip), T(c.xBeps));
-        const T M = mobility<T>(c, phiY, c.gp ? d.eta_new[cell] : T(0), xBp);
+        const T M = mobility<T>(c, phiY, p.eta, xBp);
         out[0] = M * g[0];
         out[1] = M * g[1];
         out[2] = M * g[2];
@@ -484,7 +525,7 @@ struct OpFluxZ {
         if (x < T(1e-12)) x = T(1e-12);
         if (x > T(1) - T(1e-12)) x = T(1) - T(1e-12);
         const T ld = x * (T(1) - x);
-        const T dYdt = d.dYdt[cell] + T(d.dYoff);
+        const T dYdt = p.dydt + T(d.dYoff);
         const T dt = T(c.dt);
         T src;
         if (c.zm) {
@@ -561,7 +602,7 @@ struct OpDivX {
 template <typename T, typename TE>
 struct OpStorageExactZ {
     using Acc = NoAcc;
-    DevState<T, TE> d; PhysC c; const cplx_t<T> *src; double ha_eps;
+    DevState<T, TE> d; PhysCT<T> c; const cplx_t<T> *src; double ha_eps;
     __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * d.g.NzC + k]; }
     __device__ void point(long long cell, const T *in, T *, Acc &) const {
         const T Yold = d.Y[cell];
@@ -590,7 +631,7 @@ struct OpStorageExactZ {
 template <typename T, typename TE>
 struct OpXSplitSrcZ {
     using Acc = NoAcc;
-    DevState<T, TE> d; PhysC c; double floor_;
+    DevState<T, TE> d; PhysCT<T> c; double floor_;
     __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = d.S[0][row * d.g.NzC + k]; }
     __device__ void point(long long cell, const T *in, T *out, Acc &) const {
         const T ha = T(1) - pf_h(clamp01(d.phi_new[cell]));
@@ -627,7 +668,7 @@ struct OpXSplitX {
 template <typename T, typename TE>
 struct OpXSplitFinalZ {
     using Acc = NoAcc;
-    DevState<T, TE> d; PhysC c; const cplx_t<T> *src;
+    DevState<T, TE> d; PhysCT<T> c; const cplx_t<T> *src;
     __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * d.g.NzC + k]; }
     __device__ void point(long long cell, const T *in, T *, Acc &) const {
         const T Yold = d.Y[cell];
@@ -649,10 +690,22 @@ struct OpXSplitFinalZ {
 template <typename T, typename TE>
 struct OpYFinalZ {
     using Acc = AccZMt<T>;
-    DevState<T, TE> d; PhysC c; const cplx_t<T> *src;
+    DevState<T, TE> d; PhysCT<T> c; const cplx_t<T> *src;
+    // Y^n (and phi^{n+1} for the moments) of four cells read ahead of their stores
+    static constexpr int kBatch = 4;
+    struct Pre { T Y, phin; };
+    __device__ void fetch(long long cell, Pre &p) const {
+        p.Y = d.Y[cell];
+        p.phin = c.zm ? d.phi_new[cell] : T(0);
+    }
     __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * d.g.NzC + k]; }
-    __device__ void point(long long cell, const T *in, T *, Acc &acc) const {
-        const T Yold = d.Y[cell];
+    __device__ void point(long long cell, const T *in, T *out, Acc &acc) const {
+        Pre p;
+        fetch(cell, p);
+        point_with(cell, p, in, out, acc);
+    }
+    __device__ void point_with(long long cell, const Pre &p, const T *in, T *, Acc &acc) const {
+        const T Yold = p.Y;
         T y = in[0];
         if (!c.zm) {
             // Y_normalize_and_clamp_kernel (:2554-2572), Y_cap = Y_clip
@@ -670,7 +723,7 @@ struct OpYFinalZ {
             // predictor and sum|1-h| only a bound, so field precision is enough
             acc.mn = fmin(acc.mn, y);
             acc.mx = fmax(acc.mx, y);
-            const T h = pf_h(d.phi_new[cell]);
+            const T h = pf_h(p.phin);
             const T a = T(1) - h;
             const T s = sigmoid_raw(y + T(d.Yc));
             const T s1 = s * (T(1) - s);
@@ -715,21 +768,35 @@ __global__ void k_zm_eval(const T *Y, const T *phi, long long N, double Yc, doub
         m[q] = 0.0; dd[q] = 0.0; lv[q] = lam[q];
         el[q] = fabs(lv[q]) < kBig ? exp(TV(-lv[q])) : TV(0);
     }
+    // sums in TV over chunks of 16 cells of a thread, then into FP64: the
+    // FP32 evaluation (bracket decisions with a 1e-5 relative margin) no
+    // longer spends the FP64 pipe on every cell
+    TV cm[NL], cd[NL];
+#pragma unroll
+    for (int q = 0; q < NL; ++q) { cm[q] = TV(0); cd[q] = TV(0); }
+    int cnt = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
          i += (long long)gridDim.x * blockDim.x) {
         const TV h = pf_h(TV(phi[i]));
         const TV a = TV(1) - h;
         const double y = double(Y[i]) + Yc;
         const TV ey = exp(TV(-y));
-        const double hv = double(h * TV(vB));
+        const TV hv = h * TV(vB);
 #pragma unroll
         for (int q = 0; q < NL; ++q) {
             const TV x = (fabs(y) < kBig && fabs(lv[q]) < kBig) ? TV(1) / (TV(1) + ey * el[q])
                                                                : sigmoid_raw(TV(y + lv[q]));
-            m[q] += double(a * x) + hv;
-            dd[q] += double(a * x * (TV(1) - x));
+            cm[q] += a * x + hv;
+            cd[q] += a * x * (TV(1) - x);
+        }
+        if (++cnt == (sizeof(TV) == 4 ? 16 : 1)) {
+#pragma unroll
+            for (int q = 0; q < NL; ++q) { m[q] += double(cm[q]); dd[q] += double(cd[q]); cm[q] = TV(0); cd[q] = TV(0); }
+            cnt = 0;
         }
     }
+#pragma unroll
+    for (int q = 0; q < NL; ++q) { m[q] += double(cm[q]); dd[q] += double(cd[q]); }
 #pragma unroll
     for (int q = 0; q < NL; ++q) {
         AccSum2 s{m[q], dd[q]};
@@ -746,7 +813,7 @@ __global__ void k_zm_eval(const T *Y, const T *phi, long long N, double Yc, doub
 template <typename T, typename TE>
 struct OpEigenR2C {
     using Acc = NoAcc;
-    DevState<T, TE> d; PhysC c; ElasC<TE> ec;
+    DevState<T, TE> d; PhysCT<T> c; ElasC<TE> ec;
     __device__ void point(long long cell, const TE *, TE *out, Acc &) const {
         const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
         eigenstrain<T, TE>(c, ec, d.phi_old[cell], c.gp ? d.eta_old[cell] : T(0), xB_el(c, xB),
@@ -765,7 +832,7 @@ struct OpEigenR2C {
 template <typename T, typename TE>
 struct OpHijZ {
     using Acc = NoAcc;
-    DevState<T, TE> d; PhysC c; ElasC<TE> ec;
+    DevState<T, TE> d; PhysCT<T> c; ElasC<TE> ec;
     int lin;   // increment form: the linear part -(h dC):eps only
     __device__ void load_spec(long long row, int k, cplx_t<TE> *v) const {
         const long long o = row * d.g.NzC + k;
@@ -813,7 +880,7 @@ struct OpHijZ {
 template <typename T, typename TE>
 struct OpStrainFinalZ {
     using Acc = NoAcc;
-    DevState<T, TE> d; ElasC<TE> ec; PhysC c;
+    DevState<T, TE> d; ElasC<TE> ec; PhysCT<T> c;
     __device__ void load_spec(long long row, int k, cplx_t<TE> *v) const {
         const long long o = row * d.g.NzC + k;
 #pragma unroll
@@ -1505,7 +1572,7 @@ __global__ void k_extrapolate_u(cplx_t<TE> *u0, cplx_t<TE> *u1, cplx_t<TE> *u2, 
 // model inputs: phi, eta and the 6 eigenstrain components the cold start's
 // eigenstrain pass sees (OpEigenR2C), as float [8][N]
 template <typename T, typename TE>
-__global__ void k_fno_inputs(DevState<T, TE> d, PhysC c, ElasC<TE> ec, float *__restrict__ out) {
+__global__ void k_fno_inputs(DevState<T, TE> d, PhysCT<T> c, ElasC<TE> ec, float *__restrict__ out) {
     const long long N = d.g.N;
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N;
          n += (long long)gridDim.x * blockDim.x) {
@@ -1578,7 +1645,7 @@ __global__ void k_sub3(cplx_t<TE> *d0, cplx_t<TE> *d1, cplx_t<TE> *d2, const cpl
 template <typename T, typename TE>
 static pfgb_status launch_fno_inputs(pfgb_ctx *c, float *out) {
     ProfScope ps(c, {"model_inputs", (double)c->g.N * (3.0 * sizeof(T) + 8.0 * sizeof(float))});
-    k_fno_inputs<T, TE><<<1216, 256, 0, c->stream>>>(dev_state<T, TE>(c), c->pc, elas_consts<TE>(c), out);
+    k_fno_inputs<T, TE><<<1216, 256, 0, c->stream>>>(dev_state<T, TE>(c), phys_as<T>(c->pc), elas_consts<TE>(c), out);
     PFGB_CUDA_TRY(cudaGetLastError());
     return PFGB_OK;
 }
@@ -1614,7 +1681,7 @@ template <typename T, typename TE>
 static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     using T2e = cplx_t<TE>;
     const pfgb_params &P = c->p;
-    const PhysC pc = c->pc;
+    const PhysCT<T> pc = phys_as<T>(c->pc);
     const ElasC<TE> ec = elas_consts<TE>(c);
     DevState<T, TE> d = dev_state<T, TE>(c);
     const KTab kt = d.kt;
@@ -1903,7 +1970,7 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
 template <typename T, typename TE>
 static pfgb_status y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_stats *st) {
     const pfgb_params &P = c->p;
-    const PhysC pc = c->pc;
+    const PhysCT<T> pc = phys_as<T>(c->pc);
     const ElasC<TE> ec = elas_consts<TE>(c);
     const KTab kt = d.kt;
     const double invN = 1.0 / (double)c->g.N;
@@ -1998,7 +2065,7 @@ template <typename T, typename TE>
 static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
     using T2 = cplx_t<T>;
     const pfgb_params &P = c->p;
-    const PhysC pc = c->pc;
+    const PhysCT<T> pc = phys_as<T>(c->pc);
     const ElasC<TE> ec = elas_consts<TE>(c);
     c->Yc_prev = c->Yc;
     if (P.elastic_enabled) TRY((elastic_solve<T, TE>(c, st)));
@@ -2043,7 +2110,7 @@ static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
 template <typename T, typename TE>
 struct OpMinGradZ {
     using Acc = NoAcc;
-    DevState<T, TE> d; PhysC c; ElasC<TE> ec; const T *phi;
+    DevState<T, TE> d; PhysCT<T> c; ElasC<TE> ec; const T *phi;
     __device__ void point(long long cell, const T *, T *out, Acc &) const {
         const T p = phi[cell];
         const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
@@ -2230,7 +2297,7 @@ struct AccSumMax {
 };
 template <typename T, typename TE>
 __global__ void __launch_bounds__(256)
-k_min_dy(DevState<T, TE> d, PhysC c, double yc_prev, AccSumMax *part) {
+k_min_dy(DevState<T, TE> d, PhysCT<T> c, double yc_prev, AccSumMax *part) {
     AccSumMax a = AccSumMax::identity();
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.g.N;
          i += (long long)gridDim.x * blockDim.x) {
@@ -2251,7 +2318,7 @@ static pfgb_status min_gradient(pfgb_ctx *c, const DevState<T, TE> &d, const T *
     const ElasC<TE> ec = elas_consts<TE>(c);
     AxisIO<T, 1, 1> io1;
     io1.in[0] = d.S[0]; io1.out[0] = d.S[0];
-    TRY((launch_z<T, 0, 1>(c, OpMinGradZ<T, TE>{d, c->pc, ec, phi}, "z_min_grad",
+    TRY((launch_z<T, 0, 1>(c, OpMinGradZ<T, TE>{d, phys_as<T>(c->pc), ec, phi}, "z_min_grad",
                            3.0 * Nf * sizeof(T) + (c->pc.coupling ? 12.0 : 0.0) * Nf * sizeof(TE))));
     TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
     TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpLapX<T>{d.kt, invN}, "x_lap")));
@@ -2305,7 +2372,7 @@ static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
     memset(&st, 0, sizeof(st));
     if (P.elastic_enabled) TRY((elastic_solve<T, TE>(c, &st)));
     const int it = ++c->min_iter;
-    const PhysC pc = c->pc;
+    const PhysCT<T> pc = phys_as<T>(c->pc);
     const ElasC<TE> ec = elas_consts<TE>(c);
     DevState<T, TE> d = dev_state<T, TE>(c);
     T *pa = (T *)c->phi[c->cur], *pb = (T *)c->phi[1 - c->cur];
@@ -2318,7 +2385,7 @@ static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
     const double muAr = c->pc.tc.GA_s + oA, muBf = c->pc.tc.GB_s + oB;
     const double g0 = (1.0 - xref) * muAr + xref * muBf;
     TRY((min_reduce<AccMinE>(c, "min_energy", (2.0 * Nf) * sizeof(T) + 12.0 * Nf * sizeof(TE), 42, 6,
-                             k_min_energy<T, TE>, d, pc, ec, (const T *)pa, g0)));
+                             k_min_energy<T, TE>, d, c->pc, ec, (const T *)pa, g0)));
     const double *E = c->hscal + 42;
     double mean_h = E[0] / Nf;
     if (it == 1 && !(c->V0_target > 0.0)) {
@@ -2399,7 +2466,7 @@ static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
     c->cur = cur == (T *)c->phi[0] ? 0 : 1;
 
     // ---- stopping rule (:32405-32600) and the monitor's xB clamp ----
-    TRY((min_reduce<AccSumMax>(c, "min_dy", 2.0 * Nf * sizeof(T), 48, 2, k_min_dy<T, TE>, d, c->pc, c->Yc_prev)));
+    TRY((min_reduce<AccSumMax>(c, "min_dy", 2.0 * Nf * sizeof(T), 48, 2, k_min_dy<T, TE>, d, phys_as<T>(c->pc), c->Yc_prev)));
     const double rms_dY = std::sqrt(c->hscal[48] / Nf) / P.dt;
     const double xmax = c->hscal[49];
     double edr = NAN;
@@ -3056,7 +3123,7 @@ pfgb_status pfgb_read_fields(pfgb_ctx *c, double *phi, double *xB, double *Y, do
 }  // extern "C"
 
 template <typename T>
-__global__ void k_stress_export(PhysC pc, ElasC<float> ec, const T *phi, const T *eta, const T *Y, double Yc,
+__global__ void k_stress_export(PhysCT<T> pc, ElasC<float> ec, const T *phi, const T *eta, const T *Y, double Yc,
                                 float *const *eps, float *sig, long long N) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
          i += (long long)gridDim.x * blockDim.x) {
@@ -3101,7 +3168,7 @@ pfgb_status pfgb_read_elastic(pfgb_ctx *c, float *sigma6, float *strain6) {
                                                                 (double *)c->eta[ec_], (double *)yv, yc,
                                                                 dptrs, st, (long long)N);
         else
-            k_stress_export<float><<<304, 256, 0, c->stream>>>(c->pc, ec, (float *)c->phi[pc_],
+            k_stress_export<float><<<304, 256, 0, c->stream>>>(phys_as<float>(c->pc), ec, (float *)c->phi[pc_],
                                                                (float *)c->eta[ec_], (float *)yv, yc, dptrs,
                                                                st, (long long)N);
         cudaError_t e = cudaGetLastError();
