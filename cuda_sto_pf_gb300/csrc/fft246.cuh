@@ -175,3 +175,80 @@ k_y246(Grid3 g, const float2 *tw_g, AxisIO<float, 6, 6> io) {
         }
     }
 }
+
+// ---------------------------------------------------------------------------
+// generic strided-axis pass on the 246-point engine: NIN spectra in, an
+// optional forward transform (DIN), the op's per-point apply(i, j, k, in, out)
+// in place, an optional inverse transform (DOUT), NOUT spectra out.  The 48
+// lines of a block are NW = max(NIN, NOUT) arrays x TC = 48 / NW columns.
+// axis 1: y (block (bx, x-plane)); axis 2: x (block (bx, y-row)).  Lines
+// beyond the NIN inputs are transformed too and never stored.
+// ---------------------------------------------------------------------------
+template <int NIN, int NOUT>
+constexpr bool f246_axis_fits() {
+    constexpr int NW = NIN > NOUT ? NIN : NOUT;
+    return NW >= 1 && NW <= 6 && f246::NL % NW == 0 && (f246::NL / NW) % 2 == 0;
+}
+
+template <int NIN, int NOUT, int DIN, int DOUT, class Op>
+__global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
+k_axis246(Grid3 g, int axis, const float2 *tw_g, AxisIO<float, NIN, NOUT> io, Op op) {
+    using namespace f246;
+    constexpr int NW = NIN > NOUT ? NIN : NOUT;
+    constexpr int TCW = NL / NW, TPW = TCW / 2;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *buf = tw + N;
+    const int k0 = blockIdx.x * TCW, slab = blockIdx.y;
+    const int kcnt = min(TCW, g.NzC - k0);
+    long long base, es;
+    if (axis == 1) { base = (long long)slab * N * g.NzC + k0; es = g.NzC; }
+    else { base = (long long)slab * g.NzC + k0; es = (long long)g.Ny * g.NzC; }
+#pragma unroll
+    for (int s = 0; s < NIN; ++s) {
+        for (int e = threadIdx.x; e < N * TPW; e += blockDim.x) {
+            const int tp = e % TPW, q = e / TPW;
+            const int t = 2 * tp;
+            float2 *dst = buf + q * PSTR + s * TCW + t;
+            const float2 *src = io.in[s] + base + (long long)q * es + t;
+            if (t + 1 < kcnt) {
+                const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src));
+            } else {
+                dst[0] = t < kcnt ? src[0] : make_float2(0.f, 0.f);
+                dst[1] = make_float2(0.f, 0.f);
+            }
+        }
+    }
+    cp_async_commit();
+    if (DIN != 0 || DOUT != 0) load_twiddles(tw, tw_g);
+    cp_async_wait_all();
+    __syncthreads();
+    if (DIN != 0) lines<DIN, PSTR, 1>(buf, tw);
+    if constexpr (!Op::kInplace) {
+        for (int e = threadIdx.x; e < N * TCW; e += blockDim.x) {
+            const int q = e / TCW, t = e % TCW;
+            const int i = axis == 1 ? slab : q, j = axis == 1 ? q : slab;
+            float2 vin[NIN > 0 ? NIN : 1], vout[NOUT > 0 ? NOUT : 1];
+            float2 *pt = buf + q * PSTR + t;
+#pragma unroll
+            for (int s = 0; s < NIN; ++s) vin[s] = pt[s * TCW];
+            op.apply(i, j, k0 + t, vin, vout);
+#pragma unroll
+            for (int s = 0; s < NOUT; ++s) pt[s * TCW] = vout[s];
+        }
+        __syncthreads();
+    }
+    if (DOUT != 0) lines<DOUT, PSTR, 1>(buf, tw);
+#pragma unroll
+    for (int s = 0; s < NOUT; ++s) {
+        for (int e = threadIdx.x; e < N * TPW; e += blockDim.x) {
+            const int tp = e % TPW, q = e / TPW;
+            const int t = 2 * tp;
+            const float2 *srcs = buf + q * PSTR + s * TCW + t;
+            float2 *dst = io.out[s] + base + (long long)q * es + t;
+            if (t + 1 < kcnt) *reinterpret_cast<float4 *>(dst) = *reinterpret_cast<const float4 *>(srcs);
+            else if (t < kcnt) dst[0] = srcs[0];
+        }
+    }
+}

@@ -203,6 +203,21 @@ static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, O
     using T2 = cplx_t<T>;
     const AxisPlan &pl = axis == 1 ? c->ply : c->plx;
     const int n = pl.n;
+    if constexpr (std::is_same<T, float>::value && f246_axis_fits<NIN, NOUT>()) {
+        // 246-long FP32 axes with an even half-spectrum row: the 6 x 41 engine
+        if (n == f246::N && c->g.NzC % 2 == 0) {
+            constexpr int TCW = f246::NL / axis_width<NIN, NOUT>();
+            const size_t smem = f246::axis_smem_bytes();
+            auto kern = k_axis246<NIN, NOUT, DIN, DOUT, Op>;
+            PFGB_CUDA_TRY(allow_smem(kern, smem));
+            dim3 grid((c->g.NzC + TCW - 1) / TCW, axis == 1 ? c->g.Nx : c->g.Ny);
+            ProfScope ps(c, {tag, (double)(NIN + NOUT) * (double)c->g.Nk * sizeof(T2)});
+            kern<<<grid, f246::THREADS, smem, c->stream>>>(c->g, axis, (const float2 *)twp<T>(c, axis == 1 ? 1 : 0),
+                                                         io, op);
+            PFGB_CUDA_TRY(cudaGetLastError());
+            return PFGB_OK;
+        }
+    }
     constexpr int NW = axis_width<NIN, NOUT>();
     auto bytes = [&](int tk) { return ((size_t)n + 2 * (size_t)n * (NW * tk + 1)) * sizeof(T2); };
     int TK = 16;
