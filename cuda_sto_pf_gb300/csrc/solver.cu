@@ -233,11 +233,132 @@ static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, O
     return PFGB_OK;
 }
 
+// generic z pass on the 246-point engine: NFI half spectra per row in
+// (Hermitian-packed two per complex line), C2R, the op's pointwise stage,
+// R2C, NFO half spectra out.  A row takes LW = max(ceil(NFI/2), ceil(NFO/2))
+// lines, a block NL / LW rows.
+template <int NFI, int NFO>
+constexpr bool f246_z_fits() {
+    constexpr int LI = (NFI + 1) / 2, LO = (NFO + 1) / 2, LW = LI > LO ? LI : LO;
+    return LW >= 1 && LW <= 3;
+}
+
+template <int NFI, int NFO, class Op>
+__global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
+k_zpass246g(Grid3 g, const float2 *tw_g, Op op) {
+    using namespace f246;
+    constexpr int LI = (NFI + 1) / 2, LO = (NFO + 1) / 2, LW = LI > LO ? LI : LO;
+    constexpr int R = NL / LW, NC = N / 2 + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *buf = tw + N;
+    const long long row0 = (long long)blockIdx.x * R;
+    const long long nrows = (long long)g.Nx * g.Ny;
+    const int rcnt = (int)min((long long)R, nrows - row0);
+    load_twiddles(tw, tw_g);
+    if constexpr (NFI > 0) {
+#pragma unroll 2
+        for (int e = threadIdx.x; e < R * NC; e += blockDim.x) {
+            const int rr = e / NC, k = e - rr * NC;
+            float2 v[NFI];
+            if (rr < rcnt) op.load_spec(row0 + rr, k, v);
+            else {
+#pragma unroll
+                for (int f = 0; f < NFI; ++f) v[f] = make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int f = 0; f < LI; ++f) {
+                float2 Av = v[2 * f], Bv = 2 * f + 1 < NFI ? v[2 * f + 1] : make_float2(0.f, 0.f);
+                if (k == 0 || 2 * k == N) { Av.y = 0.f; Bv.y = 0.f; }
+                float2 *line = buf + (rr * LW + f) * N;
+                // Z_k = A_k + i B_k ; Z_(n-k) = conj(A_k) + i conj(B_k)
+                line[k] = make_float2(Av.x - Bv.y, Av.y + Bv.x);
+                if (k > 0 && 2 * k != N) line[N - k] = make_float2(Av.x + Bv.y, Bv.x - Av.y);
+            }
+        }
+        __syncthreads();
+        lines<+1, 1, N>(buf, tw);
+    } else {
+        __syncthreads();   // twiddles
+    }
+    typename Op::Acc acc = Op::Acc::identity();
+    auto cell_step = [&](int e, auto &&pointf) {
+        const int r = e / N, z = e - r * N;
+        float vi[NFI > 0 ? NFI : 1], vo[NFO > 0 ? NFO : 1];
+#pragma unroll
+        for (int f = 0; f < NFI; ++f) {
+            const float2 w = buf[(r * LW + f / 2) * N + z];
+            vi[f] = (f & 1) ? w.y : w.x;
+        }
+        pointf((row0 + r) * N + z, vi, vo);
+#pragma unroll
+        for (int f = 0; f < LO; ++f)
+            buf[(r * LW + f) * N + z] = make_float2(vo[2 * f], 2 * f + 1 < NFO ? vo[2 * f + 1] : 0.f);
+    };
+    constexpr int B = op_batch<Op>::value;
+    if constexpr (B > 1) {
+        for (int e0 = threadIdx.x; e0 < rcnt * N; e0 += B * blockDim.x) {
+            typename Op::Pre pre[B];
+#pragma unroll
+            for (int b = 0; b < B; ++b) {
+                const int e = e0 + b * blockDim.x;
+                if (e < rcnt * N) op.fetch(row0 * N + e, pre[b]);
+            }
+#pragma unroll
+            for (int b = 0; b < B; ++b) {
+                const int e = e0 + b * blockDim.x;
+                if (e < rcnt * N)
+                    cell_step(e, [&](long long cell, const float *vi, float *vo) { op.point_with(cell, pre[b], vi, vo, acc); });
+            }
+        }
+    } else {
+        for (int e = threadIdx.x; e < rcnt * N; e += blockDim.x)
+            cell_step(e, [&](long long cell, const float *vi, float *vo) { op.point(cell, vi, vo, acc); });
+    }
+    if constexpr (Op::Acc::kActive) {
+        block_reduce_acc(acc);
+        if (threadIdx.x == 0) op.finish(blockIdx.x, acc);
+    }
+    if constexpr (NFO > 0) {
+        __syncthreads();
+        lines<-1, 1, N>(buf, tw);
+        for (int e = threadIdx.x; e < rcnt * NC; e += blockDim.x) {
+            const int rr = e / NC, k = e - rr * NC;
+            float2 v[NFO];
+#pragma unroll
+            for (int f = 0; f < LO; ++f) {
+                const float2 *line = buf + (rr * LW + f) * N;
+                const float2 Zk = line[k], Zm = line[k == 0 ? 0 : N - k];
+                // A_k = (Z_k + conj Z_-k) / 2 ; B_k = (Z_k - conj Z_-k) / (2 i)
+                v[2 * f] = make_float2(0.5f * (Zk.x + Zm.x), 0.5f * (Zk.y - Zm.y));
+                if (2 * f + 1 < NFO) v[2 * f + 1] = make_float2(0.5f * (Zk.y + Zm.y), 0.5f * (Zm.x - Zk.x));
+            }
+            op.store_spec(row0 + rr, k, v);
+        }
+    }
+}
+
 // extra_bytes: field bytes the op reads/writes per call besides its NFI/NFO spectra
 template <typename T, int NFI, int NFO, class Op>
 static pfgb_status launch_z(pfgb_ctx *c, Op op, const char *tag, double extra_bytes, int *nblocks = nullptr) {
     using T2 = cplx_t<T>;
     const int n = c->g.Nz;
+    if constexpr (std::is_same<T, float>::value && f246_z_fits<NFI, NFO>()) {
+        if (n == f246::N) {   // 246-long FP32 rows: the 6 x 41 engine
+            constexpr int LW = ((NFI + 1) / 2 > (NFO + 1) / 2) ? (NFI + 1) / 2 : (NFO + 1) / 2;
+            constexpr int R = f246::NL / LW;
+            const size_t smem = f246::z_smem_bytes();
+            auto kern = k_zpass246g<NFI, NFO, Op>;
+            PFGB_CUDA_TRY(allow_smem(kern, smem));
+            const long long rows = (long long)c->g.Nx * c->g.Ny;
+            const int nb = (int)((rows + R - 1) / R);
+            ProfScope ps(c, {tag, (double)(NFI + NFO) * (double)c->g.Nk * sizeof(T2) + extra_bytes});
+            kern<<<nb, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)twp<T>(c, 2), op);
+            PFGB_CUDA_TRY(cudaGetLastError());
+            if (nblocks) *nblocks = nb;
+            return PFGB_OK;
+        }
+    }
     auto bytes = [&](int R) {
         int PI_ = NFI > 0 ? (R * NFI + 1) / 2 : 0, PO_ = NFO > 0 ? (R * NFO + 1) / 2 : 0;
         if (NFI == NFO) PO_ = 0;   // in-place pointwise stage
