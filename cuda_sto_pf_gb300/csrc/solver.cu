@@ -827,8 +827,8 @@ template <typename T, typename TE>
 struct OpYFinalZ {
     using Acc = AccZMt<T>;
     DevState<T, TE> d; PhysCT<T> c; const cplx_t<T> *src;
-    // Y^n (and phi^{n+1} for the moments) of four cells read ahead of their stores
-    static constexpr int kBatch = 4;
+    // Y^n (and phi^{n+1} for the moments) of eight cells read ahead of their stores
+    static constexpr int kBatch = 8;
     struct Pre { T Y, phin; };
     __device__ void fetch(long long cell, Pre &p) const {
         p.Y = d.Y[cell];
