@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain-fp64", action="store_true")
     ap.add_argument("--no-chebyshev", action="store_true", help="the reference's plain elastic iteration")
-    ap.add_argument("--extrapolate", action="store_true", help="extrapolated elastic warm start")
+    ap.add_argument("--no-extrapolate", action="store_true",
+                    help="start each elastic solve from the previous solution (the reference's warm start)")
     ap.add_argument("--profile-json", default="")
     ap.add_argument("--fno-n", type=int, default=128)
     ap.add_argument("--fno-base", type=int, default=128, help="distinct generated microstructures")
@@ -77,9 +78,10 @@ def dist_env():
 # (--no-chebyshev: the reference's plain iteration); the CPU reference arm
 # and the plain FP64 comparison always run the reference's iteration
 CHEBYSHEV = 1
-# --extrapolate: the elastic warm start extrapolated linearly from the last
-# two solutions (same fixed point, fewer iterations when the fields move)
-EXTRAPOLATE = 0
+# the elastic warm start extrapolated linearly from the last two solutions
+# (same fixed point and stopping test, fewer iterations when the fields
+# move; --no-extrapolate: the reference's previous-solution start)
+EXTRAPOLATE = 1
 
 
 def make_params(capi, n, precision, tol, shape=None, chebyshev=None):
@@ -444,6 +446,8 @@ def run_ours(args):
                            "elastic_tol": args.elastic_tol, "dt": p.dt,
                            "elastic_iteration": "chebyshev semi-iteration of the increment" if CHEBYSHEV
                            else "plain (the reference's)",
+                           "elastic_warm_start": "extrapolated from the last two solutions" if EXTRAPOLATE
+                           else "previous solution (the reference's)",
                            "l2": "inputs larger than L2 (working set > 1 GB at 246^3)",
                            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
                 "elastic_iters_per_step": sum(iters) / max(1, len(iters)),
@@ -692,7 +696,7 @@ def main():
     global CHEBYSHEV, EXTRAPOLATE
     args = parse()
     CHEBYSHEV = 0 if args.no_chebyshev else 1
-    EXTRAPOLATE = 1 if args.extrapolate else 0
+    EXTRAPOLATE = 0 if args.no_extrapolate else 1
     if args.workload == "sweep":
         run_sweep(args)
         return
