@@ -902,9 +902,11 @@ static int zero_mode(pfo_state *s, const double *Ystar, double Y_upper_cap, pfgb
         (M) = dsum(s->mass_t, s->N);                                          \
         (D) = dsum(s->der_t, s->N);                                           \
     } while (0)
-    double mlo, dlo, mhi, dhi;
+    double mlo, dlo, mhi, dhi;   /* the derivatives at the bracket ends are not used */
     ZM_EVAL(lo, mlo, dlo);
     ZM_EVAL(hi, mhi, dhi);
+    (void)dlo;
+    (void)dhi;
     if (!isfinite(mlo) || !isfinite(mhi)) return PFGB_ERR_ZERO_MODE;
     if (mlo - target > tol || mhi - target < -tol) return PFGB_ERR_ZERO_MODE;
     double lam = fmin(fmax(0.0, lo), hi), mass, der;
