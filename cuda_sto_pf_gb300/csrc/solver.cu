@@ -2009,10 +2009,16 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
         for (int q = 0; q < nl; ++q) { mass[q] = c->hscal[DS_BR + 2 * q]; der[q] = c->hscal[DS_BR + 2 * q + 1]; }
         return PFGB_OK;
     };
-    {
+    // the reference's bracket test: mass(lo) <= target + tol and
+    // mass(hi) >= target - tol.  Evaluated only when the iteration does not
+    // reach the tolerance, to name the failure: mass is increasing in the
+    // shift, so an accepted point inside [lo, hi] (evaluated or certified
+    // within tol) already implies both conditions.
+    const double lo0 = lo, hi0 = hi;
+    auto check_bracket = [&]() -> pfgb_status {
         // bracket ends: evaluated in field precision; an FP64 re-evaluation is
         // taken only when the FP32 value is within 1e-5 of the decision limit
-        double ls[2] = {lo, hi}, ms[2], ds[2];
+        double ls[2] = {lo0, hi0}, ms[2], ds[2];
         const bool fp32 = sizeof(T) == 4;
         TRY(direct(ls, 2, ms, ds, !fp32));
         if (fp32) {
@@ -2023,7 +2029,8 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
         }
         if (!std::isfinite(ms[0]) || !std::isfinite(ms[1])) return fail("non-finite bracket mass");
         if (ms[0] - target > tol || ms[1] - target < -tol) return fail("target outside bracket");
-    }
+        return PFGB_OK;
+    };
     int iters = 0, nwt = 0, bis = 0;
     // one safeguarded Newton / bisection update (same rule as the reference)
     auto update = [&](double &lam, double res, double der) {
@@ -2080,7 +2087,10 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
         res = mass - target;
     }
     (void)certified;
-    if (std::fabs(res) > tol) return fail("did not converge");
+    if (!(std::fabs(res) <= tol)) {
+        TRY(check_bracket());
+        return fail("did not converge");
+    }
     if (ymin + lam < -P.Y_clip || ymax + lam > Ycap) return fail("shifted Y leaves [-Y_clip, Y_cap]");
     c->Yc += lam;
     c->dYoff = lam / P.dt;

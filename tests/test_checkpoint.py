@@ -249,3 +249,4 @@ def test_restart_continues_the_run(capi, tmp_path, prec, tol):
         got = s.fields()
     for k in ("phi", "xB", "Y", "dYdt"):
         assert rel_l2(got[k], want[k]) <= tol, k
+
