@@ -66,6 +66,10 @@ struct pfgb_ctx {
     pfgb_params p;
     int device = 0;
     cudaStream_t stream = 0;
+    // read-back: a side stream and two events (created on first use) let the
+    // FP64 composition export run beside the copies of the other fields
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_rd[2] = {nullptr, nullptr};
     Grid3 g;
     AxisPlan plx, ply, plz;
     void *tw[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};  // [fp64|fp32][x,y,z]
@@ -2929,10 +2933,28 @@ static void ctx_free(pfgb_ctx *c) {
     f(c->fno_in); f(c->fno_out);
     for (int i = 0; i < 3; ++i) f(c->Uhom[i]);
     for (auto e : c->pool) cudaEventDestroy(e);
+    for (auto e : c->ev_rd) if (e) cudaEventDestroy(e);
+    if (c->aux) cudaStreamDestroy(c->aux);
     if (c->hscal) cudaFreeHost(c->hscal);
 }
 
+// float fields: Y = log x - log(1 - x) from the two float logarithms of the
+// double x and 1 - x (each within an ulp of its value), so the FP64 pipe is
+// not spent on a result stored in float; double fields keep logit_clip
 template <typename T>
+__device__ __forceinline__ T load_logit(double x, double eps, double Yclip) {
+    if constexpr (sizeof(T) == 8) {
+        return logit_clip(x, eps, Yclip);
+    } else {
+        const double xc = fmin(fmax(x, eps), 1.0 - eps);
+        const float y = logf(float(xc)) - logf(float(1.0 - xc));
+        return fminf(fmaxf(y, -float(Yclip)), float(Yclip));
+    }
+}
+
+// MASS: also the block partials of the target mass of the zero mode
+// (gpu_reduce_sum_xBtot, :28079-28086), taken on a first load only
+template <typename T, bool MASS>
 __global__ void k_load_state(const double *phi, const double *xB, const double *eta, const double *dYdt,
                              T *phi_o, T *eta_o, T *Y_o, T *dYdt_o, long long N, double xBeps, double Yclip,
                              double vB, double *partials) {
@@ -2943,27 +2965,36 @@ __global__ void k_load_state(const double *phi, const double *xB, const double *
         phi_o[i] = (T)p;
         eta_o[i] = eta ? (T)eta[i] : T(0);
         dYdt_o[i] = dYdt ? (T)dYdt[i] : T(0);
-        Y_o[i] = (T)logit_clip(x, xBeps, Yclip);
-        // target mass of the zero mode, gpu_reduce_sum_xBtot (:28079-28086)
-        const double h = pf_h(p);
-        acc += (1.0 - h) * x + vB * h;
+        Y_o[i] = load_logit<T>(x, xBeps, Yclip);
+        if (MASS) {
+            const double h = pf_h(p);
+            acc += (1.0 - h) * x + vB * h;
+        }
     }
-    AccSum1 s{acc};
-    block_reduce_acc(s);
-    if (threadIdx.x == 0) reinterpret_cast<AccSum1 *>(partials)[blockIdx.x] = s;
+    if (MASS) {
+        AccSum1 s{acc};
+        block_reduce_acc(s);
+        if (threadIdx.x == 0) reinterpret_cast<AccSum1 *>(partials)[blockIdx.x] = s;
+    }
 }
 
 template <typename T>
 static pfgb_status load_device(pfgb_ctx *c, const double *phi, const double *xB, const double *eta,
                                const double *dYdt, bool keep_history) {
     const int nb = 304;
-    k_load_state<T><<<nb, 256, 0, c->stream>>>(phi, xB, eta, dYdt, (T *)c->phi[c->cur], (T *)c->eta[c->ecur],
-                                               (T *)c->Y, (T *)c->dYdt, c->g.N, c->p.xB_eps, c->p.Y_clip,
-                                               c->p.v_B, c->partials);
+    const bool keep = keep_history && c->loaded;
+    if (keep)
+        k_load_state<T, false><<<nb, 256, 0, c->stream>>>(phi, xB, eta, dYdt, (T *)c->phi[c->cur],
+                                                          (T *)c->eta[c->ecur], (T *)c->Y, (T *)c->dYdt, c->g.N,
+                                                          c->p.xB_eps, c->p.Y_clip, c->p.v_B, c->partials);
+    else
+        k_load_state<T, true><<<nb, 256, 0, c->stream>>>(phi, xB, eta, dYdt, (T *)c->phi[c->cur],
+                                                         (T *)c->eta[c->ecur], (T *)c->Y, (T *)c->dYdt, c->g.N,
+                                                         c->p.xB_eps, c->p.Y_clip, c->p.v_B, c->partials);
     PFGB_CUDA_TRY(cudaGetLastError());
     c->Yc = 0.0;
     c->dYoff = 0.0;
-    if (keep_history && c->loaded) return PFGB_OK;
+    if (keep) return PFGB_OK;
     TRY(reduce_to<AccSum1>(c, nb, DS_ZM));
     TRY(sync_read(c, DS_ZM, 1));
     c->target_mass = c->hscal[DS_ZM];
@@ -3243,24 +3274,53 @@ pfgb_status pfgb_read_fields(pfgb_ctx *c, double *phi, double *xB, double *Y, do
     PFGB_CUDA_TRY(cudaSetDevice(c->device));
     const size_t b = sizeof(double) * (size_t)c->g.N;
     TRY(ensure_stage(c));
+    if (!c->aux) PFGB_CUDA_TRY(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+    for (auto &ev : c->ev_rd)
+        if (!ev) PFGB_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     double *st = c->stage;
     const long long N = c->g.N;
     double *o[5] = {st, st + N, st + 2 * N, st + 3 * N, st + 4 * N};
     const int raw = c->p.zero_mode_enabled && c->step > 0;
-    if (c->p.precision == PFGB_PREC_FP64)
-        k_export<double><<<304, 256, 0, c->stream>>>((double *)c->phi[c->cur], (double *)c->Y,
-                                                     (double *)c->eta[c->ecur], (double *)c->dYdt, N, c->Yc,
-                                                     c->dYoff, raw, c->p.Y_clip, c->p.xB_eps, o[0], o[1], o[2],
-                                                     o[3], o[4]);
-    else
-        k_export<float><<<304, 256, 0, c->stream>>>((float *)c->phi[c->cur], (float *)c->Y,
-                                                    (float *)c->eta[c->ecur], (float *)c->dYdt, N, c->Yc,
-                                                    c->dYoff, raw, c->p.Y_clip, c->p.xB_eps, o[0], o[1], o[2],
-                                                    o[3], o[4]);
-    cudaError_t e = cudaGetLastError();
+    const bool fp64 = c->p.precision == PFGB_PREC_FP64;
+    // the composition (an FP64 sigmoid per cell) on the side stream, after
+    // the work queued so far; the other fields' export and copies meanwhile
+    cudaError_t e = cudaSuccess;
+    if (xB) {
+        e = cudaEventRecord(c->ev_rd[0], c->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->aux, c->ev_rd[0], 0);
+        if (e == cudaSuccess) {
+            if (fp64)
+                k_export<double><<<304, 256, 0, c->aux>>>(nullptr, (double *)c->Y, nullptr, nullptr, N, c->Yc,
+                                                          c->dYoff, raw, c->p.Y_clip, c->p.xB_eps, nullptr, o[1],
+                                                          nullptr, nullptr, nullptr);
+            else
+                k_export<float><<<304, 256, 0, c->aux>>>(nullptr, (float *)c->Y, nullptr, nullptr, N, c->Yc,
+                                                         c->dYoff, raw, c->p.Y_clip, c->p.xB_eps, nullptr, o[1],
+                                                         nullptr, nullptr, nullptr);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev_rd[1], c->aux);
+    }
+    if (e == cudaSuccess) {
+        if (fp64)
+            k_export<double><<<304, 256, 0, c->stream>>>((double *)c->phi[c->cur], (double *)c->Y,
+                                                         (double *)c->eta[c->ecur], (double *)c->dYdt, N, c->Yc,
+                                                         c->dYoff, raw, c->p.Y_clip, c->p.xB_eps, o[0], nullptr,
+                                                         o[2], o[3], o[4]);
+        else
+            k_export<float><<<304, 256, 0, c->stream>>>((float *)c->phi[c->cur], (float *)c->Y,
+                                                        (float *)c->eta[c->ecur], (float *)c->dYdt, N, c->Yc,
+                                                        c->dYoff, raw, c->p.Y_clip, c->p.xB_eps, o[0], nullptr,
+                                                        o[2], o[3], o[4]);
+        e = cudaGetLastError();
+    }
     double *dst[5] = {phi, xB, Y, eta, dYdt};
     for (int i = 0; i < 5 && e == cudaSuccess; ++i)
-        if (dst[i]) e = cudaMemcpyAsync(dst[i], o[i], b, cudaMemcpyDeviceToHost, c->stream);
+        if (dst[i] && i != 1) e = cudaMemcpyAsync(dst[i], o[i], b, cudaMemcpyDeviceToHost, c->stream);
+    if (xB && e == cudaSuccess) {
+        e = cudaStreamWaitEvent(c->stream, c->ev_rd[1], 0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(xB, o[1], b, cudaMemcpyDeviceToHost, c->stream);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) { pfgb_set_error("pfgb_read_fields", e, __FILE__, __LINE__); return PFGB_ERR_CUDA; }
     return PFGB_OK;
