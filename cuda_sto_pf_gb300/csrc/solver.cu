@@ -157,6 +157,10 @@ struct ProfScope {
 // launch helpers
 // ---------------------------------------------------------------------------
 static const size_t kSmemBudget = 112 * 1024;
+// strided-axis tiles narrower than 4 columns (8 bytes each) leave half of
+// every 32-byte DRAM sector unused; long axes take 4 columns at one block
+// per SM instead, up to this budget
+static const size_t kSmemWide = 220 * 1024;
 
 // The dynamic shared-memory limit is an attribute of the kernel function,
 // shared by every context in the process: it is raised to the device's
@@ -226,6 +230,7 @@ static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, O
     auto bytes = [&](int tk) { return ((size_t)n + 2 * (size_t)n * (NW * tk + 1)) * sizeof(T2); };
     int TK = 16;
     while (TK > 1 && bytes(TK) > kSmemBudget) TK >>= 1;
+    if (TK < 4 && sizeof(T) == 4 && bytes(4) <= kSmemWide) TK = 4;
     while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
     const size_t smem = bytes(TK);
     auto kern = k_axis_pass<T, NIN, NOUT, DIN, DOUT, Op>;
@@ -1364,6 +1369,7 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
     auto bytes = [&](int tk) { return ((size_t)n + 2 * (size_t)n * (6 * tk + 1)) * sizeof(T2); };
     int TK = 16;
     while (TK > 1 && bytes(TK) > kSmemBudget) TK >>= 1;
+    if (TK < 4 && sizeof(TE) == 4 && bytes(4) <= kSmemWide) TK = 4;
     while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
     const size_t smem = bytes(TK);
     GreenArgs<TE> A;
