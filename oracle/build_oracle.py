@@ -9,7 +9,9 @@ own thermo_utils.h / phase_functions.h (read in place under the reference
 tree; nothing is copied) into oracle/_ref/ for pinning the restatement,
 and the reference's pf_zero_mode_checkpoint.cpp (also read in place) with
 the shim ckpt_ref_shim.cpp into oracle/_ref/libpfckpt.so for pinning the
-checkpoint files.
+checkpoint files, and the kernel section of the reference's cuda_kernels.cu
+(read in place, written to oracle/_ref/) with the shim ref_kernels.cpp into
+oracle/_ref/librefk.so for pinning the oracle's per-cell physics.
 """
 from __future__ import annotations
 
@@ -23,6 +25,9 @@ REF_OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD, "libpforacle.so")
 REF_LIB = os.path.join(REF_OUT, "libpfref.so")
 CKPT_LIB = os.path.join(REF_OUT, "libpfckpt.so")
+KERN_LIB = os.path.join(REF_OUT, "librefk.so")
+KERN_SECTION = os.path.join(REF_OUT, "ref_kernels_section.inc")
+CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
 REFERENCE_TREE = "/root/reference"
 
 CFLAGS = ["-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
@@ -87,8 +92,46 @@ def build_ref_checkpoint(force: bool = False) -> str | None:
     return CKPT_LIB
 
 
+def _kernel_section(path: str) -> str:
+    """The kernel section of the reference's cuda_kernels.cu: everything
+    after its #include lines up to the first top-level definition that
+    contains a kernel launch (the host launch wrappers)."""
+    import re
+    lines = open(path).read().split("\n")
+    last_inc = max(i for i, l in enumerate(lines[:60]) if l.startswith("#include"))
+    first_launch = next(i for i, l in enumerate(lines) if "<<<" in l)
+    depth, starts = 0, []
+    for i, l in enumerate(lines[:first_launch]):
+        if depth == 0 and re.match(r"^[A-Za-z_]", l) and not l.startswith("#"):
+            starts.append(i)
+        depth += l.count("{") - l.count("}")
+    return "\n".join(lines[last_inc + 1:starts[-1]]) + "\n"
+
+
+def build_ref_kernels(force: bool = False) -> str | None:
+    """Compile the reference's per-cell kernels for the host (ref_kernels.cpp).
+
+    The kernel section is read from cuda_kernels.cu where it lies and written
+    to oracle/_ref/ (a build output, git-ignored); only where the reference
+    tree and the CUDA headers are present; returns None otherwise."""
+    src = os.path.join(REFERENCE_TREE, "cuda_kernels.cu")
+    if not os.path.exists(src) or not os.path.isdir(CUDA_INCLUDE):
+        return None
+    os.makedirs(REF_OUT, exist_ok=True)
+    shim = os.path.join(HERE, "ref_kernels.cpp")
+    if force or _stale(KERN_LIB, [shim, src]):
+        with open(KERN_SECTION, "w") as f:
+            f.write(_kernel_section(src))
+        tmp = KERN_LIB + ".tmp"
+        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w",
+                        "-I", REFERENCE_TREE, "-I", REF_OUT, "-I", CUDA_INCLUDE, "-o", tmp, shim], check=True)
+        os.replace(tmp, KERN_LIB)
+    return KERN_LIB
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     if "--ref" in sys.argv:
         print(build_ref(force="--force" in sys.argv))
         print(build_ref_checkpoint(force="--force" in sys.argv))
+        print(build_ref_kernels(force="--force" in sys.argv))

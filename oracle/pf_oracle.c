@@ -827,8 +827,17 @@ static void phi_rhs(pfo_state *s, int coupling) {
             for (int c = 0; c < 6; ++c) sg[c] = s->sig_r[c][idx];
             double epsc = xB * P->eps_iso_over_vB;
             double diag = -epsc + P->eps_iso_over_vB * (xB - P->v_B);
+            /* the GP form of d eps0 / d phi when GP elasticity acts on phi
+             * (compute_dgel_dphi_gp_point, cuda_kernels.cu:313-372, taken at
+             * :513-526): the iso part weighted by 1 - h(eta), the GP strain by
+             * h(eta), the whole elastic term scaled by
+             * gp_elastic_derivative_scale */
+            const int gp_phi = s->gp && P->gp_elastic_enabled && P->gp_elastic_active_phi;
+            const double he = gp_phi ? o_h(o_clamp01(s->eta[idx])) : 0.0;
             double de[6];
-            for (int c = 0; c < 3; ++c) de[c] = hp * (P->eps00[c] + diag);
+            for (int c = 0; c < 3; ++c)
+                de[c] = gp_phi ? hp * (P->eps00[c] + (1.0 - he) * diag - he * P->gp_eps_iso)
+                               : hp * (P->eps00[c] + diag);
             for (int c = 3; c < 6; ++c) de[c] = hp * P->eps00[c];
             double dg = -(sg[0] * de[0] + sg[1] * de[1] + sg[2] * de[2]
                           + 2.0 * sg[5] * de[5] + 2.0 * sg[4] * de[4] + 2.0 * sg[3] * de[3]);
@@ -843,7 +852,7 @@ static void phi_rhs(pfo_state *s, int coupling) {
             double Q = 0.0;  /* compute_Q_voigt, :162-181 */
             for (int a = 0; a < 6; ++a)
                 for (int b = 0; b < 6; ++b) Q += voigt(P->S_p, a + 1, b + 1) * ev[a] * ev[b];
-            f += dg + 0.5 * hp * Q;
+            f += gp_phi ? P->gp_elastic_derivative_scale * (dg + 0.5 * hp * Q) : dg + 0.5 * hp * Q;
         }
         s->rhs[idx] = f;
     RLOOP_END
@@ -874,6 +883,34 @@ static void eta_rhs(pfo_state *s) {
         }
         s->rhs[idx] = d + P->gp_W_eta * gpe + el;
     RLOOP_END
+}
+
+/* Test hooks (the pinning tests against the reference's own kernels): the
+ * step's phi and eta right-hand sides on given fields.  sig / eps: 6 N values
+ * in Voigt order xx yy zz yz xz xy. */
+void pfo_test_phi_rhs(pfo_state *s, int coupling, const double *phi, const double *eta, const double *xB,
+                      const double *sig, const double *eps, double *out) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->phi, phi, b);
+    memcpy(s->xB, xB, b);
+    if (eta) memcpy(s->eta, eta, b);
+    for (int c = 0; c < 6; ++c) {
+        if (sig) memcpy(s->sig_r[c], sig + (size_t)c * s->N, b);
+        if (eps) memcpy(s->eps_r[c], eps + (size_t)c * s->N, b);
+    }
+    phi_rhs(s, coupling);
+    memcpy(out, s->rhs, b);
+}
+void pfo_test_eta_rhs(pfo_state *s, const double *eta, const double *phi, const double *xB, const double *sig,
+                      double *out) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->eta, eta, b);
+    memcpy(s->phi, phi, b);
+    memcpy(s->xB, xB, b);
+    for (int c = 0; c < 6; ++c)
+        if (sig) memcpy(s->sig_r[c], sig + (size_t)c * s->N, b);
+    eta_rhs(s);
+    memcpy(out, s->rhs, b);
 }
 
 /* ------------------------------------------------------------------ */

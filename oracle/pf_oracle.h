@@ -39,6 +39,11 @@ int pfo_load_fields(pfo_state *s, const double *phi, const double *xB,
                     const double *eta, const double *dYdt_prev);
 /* returns a pfgb_status code */
 int pfo_step(pfo_state *s, int nsteps, pfgb_step_stats *stats);
+/* test hooks: the step's phi / eta right-hand sides on given fields */
+void pfo_test_phi_rhs(pfo_state *s, int coupling, const double *phi, const double *eta, const double *xB,
+                      const double *sig, const double *eps, double *out);
+void pfo_test_eta_rhs(pfo_state *s, const double *eta, const double *phi, const double *xB, const double *sig,
+                      double *out);
 /* minimize iterations (mode = minimize, full model, two_phase, zero mode off) */
 int pfo_minimize(pfo_state *s, int max_iter, int stop_on_convergence, pfgb_min_stats *stats);
 int pfo_read_fields(const pfo_state *s, double *phi, double *xB, double *Y,

@@ -1,0 +1,124 @@
+// ref_kernels.cpp — host build of the reference's own per-cell kernels
+// (cuda_kernels.cu, the kernel section before its launch wrappers), used
+// only to pin the oracle's restatement of the step.  Test infrastructure.
+//
+// oracle/build_oracle.py (build_ref_kernels) writes the kernel section of
+// the reference's cuda_kernels.cu, as it lies in the reference tree, to
+// oracle/_ref/ref_kernels_section.inc and compiles this file with the
+// reference tree on the include path.  The CUDA qualifiers are defined
+// away, the few device intrinsics the section names get host stand-ins, and
+// a launch is a loop over the flat index: every kernel used here is one
+// thread per cell, so the loop gives the kernel's exact arithmetic.
+#include <cuda_runtime.h>
+#include <cuComplex.h>
+#include <cufft.h>
+#include <vector_types.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#undef __global__
+#undef __device__
+#undef __host__
+#undef __forceinline__
+#undef __constant__
+#undef __shared__
+#define __global__
+#define __device__
+#define __host__
+#define __forceinline__ inline
+#define __constant__
+#define __shared__
+#define THERMO_UTILS_DEFINE_GLOBALS
+
+static uint3 threadIdx, blockIdx;
+static dim3 blockDim, gridDim;
+static inline void __syncthreads() {}
+template <typename T> static inline T atomicAdd(T *a, T v) {
+    const T o = *a;
+    *a = o + v;
+    return o;
+}
+static inline unsigned long long atomicCAS(unsigned long long *a, unsigned long long cmp, unsigned long long v) {
+    const unsigned long long o = *a;
+    if (o == cmp) *a = v;
+    return o;
+}
+template <typename T> static inline T atomicExch(T *a, T v) {
+    const T o = *a;
+    *a = v;
+    return o;
+}
+static inline long long __double_as_longlong(double d) {
+    long long r;
+    std::memcpy(&r, &d, sizeof(r));
+    return r;
+}
+static inline double __longlong_as_double(long long l) {
+    double r;
+    std::memcpy(&r, &l, sizeof(r));
+    return r;
+}
+
+#include "thermo_utils.h"
+#include "phase_functions.h"
+#include "pf_params.h"
+#include "cuda_common.h"
+#include "cuda_kernels.h"
+
+// the dynamic shared arrays the section's reduction kernels declare extern
+// (those kernels are compiled, never called here)
+double sdata[1];
+double pair_sdata[1];
+
+#include "ref_kernels_section.inc"
+
+// a launch of a one-thread-per-cell kernel over n cells
+#define REF_LAUNCH(n, call)                                          \
+    do {                                                             \
+        blockDim.x = 1; blockDim.y = 1; blockDim.z = 1;              \
+        gridDim.x = (unsigned)(n); gridDim.y = 1; gridDim.z = 1;     \
+        threadIdx.x = 0; threadIdx.y = 0; threadIdx.z = 0;           \
+        for (long long i_ = 0; i_ < (long long)(n); ++i_) {          \
+            blockIdx.x = (unsigned)i_; blockIdx.y = 0; blockIdx.z = 0; \
+            call;                                                    \
+        }                                                            \
+    } while (0)
+
+extern "C" {
+
+void refk_set_convex(int on) { h_thermo_convex_extrapolation_enabled = on; }
+
+// compute_phi_rhs_kernel over n cells.  sig / eps: 6 n floats each, Voigt
+// order xx yy zz yz xz xy (tensor strain); Sp: the 21 entries S_p_11 ..
+// S_p_66; e00: xx yy zz yz xz xy.  d: T_K, mu_reference_scale, v_A, v_B,
+// mu0_compound, Vm_compound, Vm_alpha_0, dVm_alpha_dxB, W, eps_iso_over_vB,
+// gp_eps_iso, gp_elastic_derivative_scale, elastic_shift_dimless.
+// i: gp_mode_enabled, gp_elastic_enabled, gp_elastic_active_phi,
+// disable_chem, elastic_enabled.
+void refk_phi_rhs(const double *phi, const double *eta, const double *xB, double *rhs, int n, const double *d,
+                  const int *i, const float *sig, const float *eps, const double *Sp, const double *e00) {
+    REF_LAUNCH(n, compute_phi_rhs_kernel(
+        phi, eta, xB, rhs, n, 1, 1, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8],
+        sig, sig + n, sig + 2 * n, sig + 5 * n, sig + 4 * n, sig + 3 * n,
+        eps, eps + n, eps + 2 * n, eps + 5 * n, eps + 4 * n, eps + 3 * n,
+        Sp[0], Sp[1], Sp[2], Sp[3], Sp[4], Sp[5], Sp[6], Sp[7], Sp[8], Sp[9], Sp[10], Sp[11], Sp[12], Sp[13],
+        Sp[14], Sp[15], Sp[16], Sp[17], Sp[18], Sp[19], Sp[20],
+        e00[0], e00[1], e00[2], e00[3], e00[4], e00[5], d[9], i[0], i[1], i[2], d[10], d[11], d[12], i[3], n,
+        i[4], (double *)nullptr));
+}
+
+// compute_eta_rhs_kernel (non-raw-drive branch) over n cells.  d: T_K,
+// mu_reference_scale, Vm_alpha_0, dVm_alpha_dxB, gp_xB_fixed, gp_delta_g0,
+// gp_W_eta, eps_iso_over_vB, gp_eps_iso, gp_elastic_derivative_scale.
+// i: gp_elastic_enabled, gp_elastic_active_eta.
+void refk_eta_rhs(const double *eta, const double *phi, const double *xB, double *rhs, int n, const double *d,
+                  const int *i, const float *sig) {
+    REF_LAUNCH(n, compute_eta_rhs_kernel(
+        eta, phi, xB, sig, sig + n, sig + 2 * n, sig + 5 * n, sig + 4 * n, sig + 3 * n, rhs,
+        d[0], d[1], d[2], d[3], d[4], d[5], 0, 0, 0.0, 0.0, 0.0, d[6], d[7], i[0], i[1], d[8], d[9], n,
+        (double *)nullptr));
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+"""The oracle's per-cell physics against the reference's own kernels.
+
+oracle/_ref/librefk.so is the kernel section of the reference's
+cuda_kernels.cu (lines after its includes up to the launch wrappers) built
+for the host by oracle/build_oracle.py, with a shim that defines the CUDA
+qualifiers away; a launch is a loop over cells, so each value is the
+reference kernel's own arithmetic.  The oracle's step functions run on the
+same seeded fields through its test hooks.  Skipped where the reference tree
+is absent (the library is built only beside it)."""
+import ctypes
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import REPO, params_for
+
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+dp = ctypes.POINTER(ctypes.c_double)
+fp = ctypes.POINTER(ctypes.c_float)
+ip = ctypes.POINTER(ctypes.c_int)
+
+
+def _refk():
+    path = os.path.join(REPO, "oracle", "_ref", "librefk.so")
+    if not os.path.exists(path):
+        import build_oracle
+        path = build_oracle.build_ref_kernels()
+    if not path or not os.path.exists(path):
+        pytest.skip("reference kernels not built (reference tree absent)")
+    L = ctypes.CDLL(path)
+    L.refk_set_convex.argtypes = [ctypes.c_int]
+    L.refk_phi_rhs.argtypes = [dp, dp, dp, dp, ctypes.c_int, dp, ip, fp, fp, dp, dp]
+    L.refk_eta_rhs.argtypes = [dp, dp, dp, dp, ctypes.c_int, dp, ip, fp]
+    return L
+
+
+def _ptr(a, t=dp):
+    return a.ctypes.data_as(t)
+
+
+def _fields(n, seed):
+    rng = np.random.default_rng(seed)
+    phi = rng.uniform(-0.05, 1.05, n)
+    eta = rng.uniform(-0.05, 1.05, n)
+    xB = rng.uniform(1e-4, 0.45, n)
+    sig = rng.normal(0.0, 0.05, 6 * n).astype(np.float32)
+    eps = rng.normal(0.0, 0.01, 6 * n).astype(np.float32)
+    return phi, eta, xB, sig, eps
+
+
+def _oracle_state(capi, p):
+    import oracle_py
+    o = oracle_py.Oracle(p, threads=1)
+    L = o.L
+    L.pfo_test_phi_rhs.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, dp, dp, dp]
+    L.pfo_test_eta_rhs.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp]
+    return o
+
+
+CASES = [
+    # (label, model_mode, gp_elastic_enabled, gp_elastic_active_phi, convex)
+    ("two_phase", 0, 0, 0, 0),
+    ("two_phase_convex", 0, 0, 0, 1),
+    ("gp_zone", 1, 0, 0, 0),
+    ("gp_zone_gp_elastic", 1, 1, 1, 0),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_phi_rhs_matches_reference_kernel(capi, case):
+    _, mm, gel, act, cv = case
+    L = _refk()
+    n = 8
+    p = params_for(capi, "c2.params", n=n, model_mode=mm, gp_elastic_enabled=gel, gp_elastic_active_phi=act,
+                   thermo_convex_extrapolation_enabled=cv, elastic_shift_dimless=0.0125)
+    N = n ** 3
+    phi, eta, xB, sig, eps = _fields(N, 11 + mm + 2 * gel + 4 * cv)
+    L.refk_set_convex(cv)
+    d = np.array([p.temperature_K, p.mu_reference_scale, p.v_A, p.v_B, p.mu0_compound, p.Vm_compound,
+                  p.Vm_alpha_0, p.dVm_alpha_dxB, p.W, p.eps_iso_over_vB, p.gp_eps_iso,
+                  p.gp_elastic_derivative_scale, p.elastic_shift_dimless])
+    flags = np.array([mm, gel, act, 0, 1], dtype=np.int32)
+    Sp = np.array(p.S_p[:])
+    e00 = np.array(p.eps00[:])
+    ref = np.zeros(N)
+    L.refk_phi_rhs(_ptr(phi), _ptr(eta), _ptr(xB), _ptr(ref), N, _ptr(d), _ptr(flags, ip), _ptr(sig, fp),
+                   _ptr(eps, fp), _ptr(Sp), _ptr(e00))
+    o = _oracle_state(capi, p)
+    coupling = 1 if (not (mm and gel) or act) else 0
+    got = np.zeros(N)
+    o.L.pfo_test_phi_rhs(o.s, coupling, _ptr(phi), _ptr(eta), _ptr(xB), _ptr(sig.astype(np.float64)),
+                         _ptr(eps.astype(np.float64)), _ptr(got))
+    scale = np.abs(ref).max()
+    assert np.abs(got - ref).max() <= 1e-12 * scale, np.abs(got - ref).max() / scale
+
+
+@pytest.mark.parametrize("gel", [0, 1])
+def test_eta_rhs_matches_reference_kernel(capi, gel):
+    L = _refk()
+    n = 8
+    p = params_for(capi, "c2.params", n=n, model_mode=1, gp_elastic_enabled=gel, gp_elastic_active_eta=gel)
+    N = n ** 3
+    phi, eta, xB, sig, _ = _fields(N, 31 + gel)
+    L.refk_set_convex(p.thermo_convex_extrapolation_enabled)
+    d = np.array([p.temperature_K, p.mu_reference_scale, p.Vm_alpha_0, p.dVm_alpha_dxB, p.gp_xB_fixed,
+                  p.gp_delta_g0, p.gp_W_eta, p.eps_iso_over_vB, p.gp_eps_iso, p.gp_elastic_derivative_scale])
+    flags = np.array([gel, gel], dtype=np.int32)
+    ref = np.zeros(N)
+    L.refk_eta_rhs(_ptr(eta), _ptr(phi), _ptr(xB), _ptr(ref), N, _ptr(d), _ptr(flags, ip), _ptr(sig, fp))
+    o = _oracle_state(capi, p)
+    got = np.zeros(N)
+    o.L.pfo_test_eta_rhs(o.s, _ptr(eta), _ptr(phi), _ptr(xB), _ptr(sig.astype(np.float64)), _ptr(got))
+    scale = np.abs(ref).max()
+    assert np.abs(got - ref).max() <= 1e-12 * scale, np.abs(got - ref).max() / scale
