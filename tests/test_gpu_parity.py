@@ -38,6 +38,10 @@ CASES = [
     ("c2.params", 0, 0, "heterogeneous"),
     ("c2.params", 1, 0, "heterogeneous+zero_mode"),
     ("c2.params", 1, 1, "gp_zone+zero_mode"),
+    # GP elasticity acting on phi and eta: the three-phase eigenstrain and
+    # the GP elastic driving terms (gp_elastic_enabled and the two active
+    # switches; off by default as in the reference)
+    ("c2.params", 1, 2, "gp_zone+gp_elastic+zero_mode"),
 ]
 
 
@@ -47,7 +51,10 @@ def test_step_parity(capi, oracle, case, prec):
     from cuda_sto_pf_gb300.solver import Solver
     name, zm, mm, _ = case
     n, steps = 32, 4
-    p = params_for(capi, name, n=n, zero_mode_enabled=zm, model_mode=mm, precision=prec)
+    gel = 1 if mm == 2 else 0
+    mm = min(mm, 1)
+    p = params_for(capi, name, n=n, zero_mode_enabled=zm, model_mode=mm, precision=prec, gp_elastic_enabled=gel,
+                   gp_elastic_active_phi=gel, gp_elastic_active_eta=gel)
     phi, xB, eta = _inputs(capi, p, n, mm == 1)
     o = oracle(p, threads=4)
     o.load(phi, xB, eta)
