@@ -984,18 +984,14 @@ static int zero_mode(pfo_state *s, const double *Ystar, double Y_upper_cap, pfgb
     return PFGB_OK;
 }
 
-/* ------------------------------------------------------------------ */
-/* one dynamics step — main_cuda.cu:28427-31623                        */
-/* ------------------------------------------------------------------ */
-/* Y (composition) update and dY/dt history, main_cuda.cu:30280-30800 and
- * 31618-31623; fields at entry: phi = phi^{n+1}, phi_n = phi^n, Y = Y^n. */
-static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
+/* mu of the flux, in place of Y^n's composition (compute_mu_x_kernel,
+ * cuda_kernels.cu:1266-1324; gp_zone: compute_mu_C_gp_kernel, :1326-1366);
+ * also xB = sigmoid(Y) */
+static void mu_field(pfo_state *s, const double *phiY, const double *etaY) {
     pfgb_params *P = &s->p;
     const double T = P->temperature_K, sc = P->mu_reference_scale;
     const int cv = P->thermo_convex_extrapolation_enabled;
-    const int zm = P->zero_mode_enabled;
-    const double *phiY = zm ? s->phi_n : (P->enable_Y_rhs_previous_time_level ? s->phi_n : s->phi);
-    const double *etaY = s->eta;
+    (void)etaY;
     RLOOP_BEGIN(s)
         double Yv = s->Y[idx];
         double xB = o_sigmoid(Yv, P->Y_clip, P->xB_eps);
@@ -1017,6 +1013,78 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
         }
         s->mu[idx] = mu;
     RLOOP_END
+}
+
+/* the lagged Y right-hand side (compute_Y_rhs_kernel, :2185-2266; zero mode:
+ * compute_Y_rhs_sm_tangent_n_kernel, :2268-2359) from divJ, lapY and Y^n */
+static void y_rhs_field(pfo_state *s, double dt, double mean_DY) {
+    pfgb_params *P = &s->p;
+    const int zm = P->zero_mode_enabled;
+    RLOOP_BEGIN(s)
+        double Yv = s->Y[idx];
+        double x = o_sigmoid_raw(Yv);
+        if (x < 1e-12) x = 1e-12;
+        if (x > 1.0 - 1e-12) x = 1.0 - 1e-12;
+        double ld = x * (1.0 - x);
+        double dYdt = s->dYdt[idx];
+        double f;
+        if (zm) {   /* compute_Y_rhs_sm_tangent_n_kernel, :2268-2359 */
+            double pn = s->phi_n[idx], pp = s->phi[idx];
+            double hn = o_h(pn), hpn = o_hp(pn);
+            double th = hpn * ((pp - pn) / dt) * (P->v_B - x);
+            double gl = (1.0 - hn) * ld - 1.0;
+            f = s->divJ[idx] - th - mean_DY * s->lapY[idx] - gl * dYdt;
+        } else {    /* compute_Y_rhs_kernel, :2185-2266 */
+            double hn = o_h(s->phi[idx]), ho = o_h(s->phi_n[idx]);
+            double dhdt = (hn - ho) / dt;
+            double th = P->Y_rhs_term_h_scale * dhdt * (P->v_B - x);
+            double hx = P->enable_Y_rhs_previous_time_level ? ho : hn;
+            double gl = (1.0 - hx) * ld - 1.0;
+            double tg = P->disable_Y_rhs_gamma_term ? 0.0 : gl * dYdt;
+            f = s->divJ[idx] + (-th - mean_DY * s->lapY[idx] - tg);
+        }
+        s->rhs[idx] = f;
+    RLOOP_END
+}
+
+/* test hooks for mu_field and y_rhs_field (the pinning tests): inputs are
+ * copied into the state, outputs read back */
+void pfo_test_mu(pfo_state *s, const double *Y, const double *phiY, const double *sig, double *xB, double *mu) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->Y, Y, b);
+    memcpy(s->scr, phiY, b);
+    for (int c = 0; c < 6; ++c)
+        if (sig) memcpy(s->sig_r[c], sig + (size_t)c * s->N, b);
+    mu_field(s, s->scr, s->eta);
+    memcpy(xB, s->xB, b);
+    memcpy(mu, s->mu, b);
+}
+void pfo_test_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ, const double *phi_new,
+                    const double *phi_old, const double *lapY, const double *Y, const double *dYdt, double *out) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->divJ, divJ, b);
+    memcpy(s->phi, phi_new, b);
+    memcpy(s->phi_n, phi_old, b);
+    memcpy(s->lapY, lapY, b);
+    memcpy(s->Y, Y, b);
+    memcpy(s->dYdt, dYdt, b);
+    y_rhs_field(s, dt, mean_DY);
+    memcpy(out, s->rhs, b);
+}
+
+/* ------------------------------------------------------------------ */
+/* one dynamics step — main_cuda.cu:28427-31623                        */
+/* ------------------------------------------------------------------ */
+/* Y (composition) update and dY/dt history, main_cuda.cu:30280-30800 and
+ * 31618-31623; fields at entry: phi = phi^{n+1}, phi_n = phi^n, Y = Y^n. */
+static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
+    pfgb_params *P = &s->p;
+    const double T = P->temperature_K, sc = P->mu_reference_scale;
+    const int cv = P->thermo_convex_extrapolation_enabled;
+    const int zm = P->zero_mode_enabled;
+    const double *phiY = zm ? s->phi_n : (P->enable_Y_rhs_previous_time_level ? s->phi_n : s->phi);
+    const double *etaY = s->eta;
+    mu_field(s, phiY, etaY);
     fwd(s, s->mu, s->mu_k); dealias(s, s->mu_k);
     memset(s->divJ_k, 0, sizeof(cpx) * s->Nk);
     memcpy(s->xB_prev, s->xB, sizeof(double) * s->N);
@@ -1154,31 +1222,7 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
     if (st) st->mean_DY = mean_DY;
     /* Y^n in k space (stored in divJ_k like the reference) */
     fwd(s, s->Y_n, s->divJ_k); dealias(s, s->divJ_k);
-    RLOOP_BEGIN(s)
-        double Yv = s->Y[idx];
-        double x = o_sigmoid_raw(Yv);
-        if (x < 1e-12) x = 1e-12;
-        if (x > 1.0 - 1e-12) x = 1.0 - 1e-12;
-        double ld = x * (1.0 - x);
-        double dYdt = s->dYdt[idx];
-        double f;
-        if (zm) {   /* compute_Y_rhs_sm_tangent_n_kernel, :2268-2359 */
-            double pn = s->phi_n[idx], pp = s->phi[idx];
-            double hn = o_h(pn), hpn = o_hp(pn);
-            double th = hpn * ((pp - pn) / dt) * (P->v_B - x);
-            double gl = (1.0 - hn) * ld - 1.0;
-            f = s->divJ[idx] - th - mean_DY * s->lapY[idx] - gl * dYdt;
-        } else {    /* compute_Y_rhs_kernel, :2185-2266 */
-            double hn = o_h(s->phi[idx]), ho = o_h(s->phi_n[idx]);
-            double dhdt = (hn - ho) / dt;
-            double th = P->Y_rhs_term_h_scale * dhdt * (P->v_B - x);
-            double hx = P->enable_Y_rhs_previous_time_level ? ho : hn;
-            double gl = (1.0 - hx) * ld - 1.0;
-            double tg = P->disable_Y_rhs_gamma_term ? 0.0 : gl * dYdt;
-            f = s->divJ[idx] + (-th - mean_DY * s->lapY[idx] - tg);
-        }
-        s->rhs[idx] = f;
-    RLOOP_END
+    y_rhs_field(s, dt, mean_DY);
     fwd(s, s->rhs, s->rhs_k); dealias(s, s->rhs_k);
     KLOOP_BEGIN(s)   /* Y_semi_implicit_update_kernel, :2528-2550 */
         double den = 1.0 + dt * mean_DY * k2_at(s, ii_, jj_, kk_);

@@ -44,6 +44,9 @@ void pfo_test_phi_rhs(pfo_state *s, int coupling, const double *phi, const doubl
                       const double *sig, const double *eps, double *out);
 void pfo_test_eta_rhs(pfo_state *s, const double *eta, const double *phi, const double *xB, const double *sig,
                       double *out);
+void pfo_test_mu(pfo_state *s, const double *Y, const double *phiY, const double *sig, double *xB, double *mu);
+void pfo_test_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ, const double *phi_new,
+                    const double *phi_old, const double *lapY, const double *Y, const double *dYdt, double *out);
 /* minimize iterations (mode = minimize, full model, two_phase, zero mode off) */
 int pfo_minimize(pfo_state *s, int max_iter, int stop_on_convergence, pfgb_min_stats *stats);
 int pfo_read_fields(const pfo_state *s, double *phi, double *xB, double *Y,

@@ -121,4 +121,31 @@ void refk_eta_rhs(const double *eta, const double *phi, const double *xB, double
         (double *)nullptr));
 }
 
+// compute_mu_x_kernel (gp = 0) or compute_mu_C_gp_kernel (gp = 1) over n
+// cells; xB out as the kernels write it.  d: T_K, mu_reference_scale, v_A,
+// v_B, mu0_compound, Vm_compound, Vm_alpha_0, dVm_alpha_dxB, Y_clip, xB_eps,
+// eps_iso_over_vB.  sig: 6 n floats (the first three are read).
+void refk_mu(int gp, const double *Y, const double *phi, double *xB, double *mu, int n, const double *d,
+             const float *sig, int elastic) {
+    if (gp)
+        REF_LAUNCH(n, compute_mu_C_gp_kernel(Y, xB, mu, d[0], d[1], d[6], d[7], d[8], d[9], sig, sig + n,
+                                             sig + 2 * n, d[10], n, elastic));
+    else
+        REF_LAUNCH(n, compute_mu_x_kernel(Y, phi, xB, mu, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8],
+                                          d[9], sig, sig + n, sig + 2 * n, d[10], n, elastic));
+}
+
+// compute_Y_rhs_kernel (zm = 0) or compute_Y_rhs_sm_tangent_n_kernel (zm = 1)
+// over n cells.  d: dt, v_B, mean_DY, term_h_scale.  i: previous time
+// level, gamma term disabled.
+void refk_y_rhs(int zm, const double *divJ, const double *phi_new, const double *phi_old, const double *lapY,
+                const double *Y, const double *dYdt, double *rhs, int n, const double *d, const int *i) {
+    if (zm)
+        REF_LAUNCH(n, compute_Y_rhs_sm_tangent_n_kernel(divJ, phi_old, phi_new, lapY, Y, dYdt, rhs, d[0], d[1],
+                                                        d[2], n, (double *)nullptr));
+    else
+        REF_LAUNCH(n, compute_Y_rhs_kernel(divJ, phi_new, phi_old, lapY, Y, dYdt, rhs, d[0], d[1], d[2], n, i[0],
+                                           i[1], d[3], (double *)nullptr));
+}
+
 }  // extern "C"

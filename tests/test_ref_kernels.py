@@ -115,3 +115,60 @@ def test_eta_rhs_matches_reference_kernel(capi, gel):
     o.L.pfo_test_eta_rhs(o.s, _ptr(eta), _ptr(phi), _ptr(xB), _ptr(sig.astype(np.float64)), _ptr(got))
     scale = np.abs(ref).max()
     assert np.abs(got - ref).max() <= 1e-12 * scale, np.abs(got - ref).max() / scale
+
+
+@pytest.mark.parametrize("gp", [0, 1])
+def test_mu_matches_reference_kernel(capi, gp):
+    L = _refk()
+    L.refk_mu.argtypes = [ctypes.c_int, dp, dp, dp, dp, ctypes.c_int, dp, fp, ctypes.c_int]
+    n = 8
+    p = params_for(capi, "c2.params", n=n, model_mode=gp)
+    N = n ** 3
+    rng = np.random.default_rng(41 + gp)
+    Y = rng.uniform(-19.0, 3.0, N)
+    phi = rng.uniform(-0.05, 1.05, N)
+    sig = rng.normal(0.0, 0.05, 6 * N).astype(np.float32)
+    L.refk_set_convex(p.thermo_convex_extrapolation_enabled)
+    d = np.array([p.temperature_K, p.mu_reference_scale, p.v_A, p.v_B, p.mu0_compound, p.Vm_compound,
+                  p.Vm_alpha_0, p.dVm_alpha_dxB, p.Y_clip, p.xB_eps, p.eps_iso_over_vB])
+    rx, rmu = np.zeros(N), np.zeros(N)
+    L.refk_mu(gp, _ptr(Y), _ptr(phi), _ptr(rx), _ptr(rmu), N, _ptr(d), _ptr(sig, fp), 1)
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_mu.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp]
+    gx, gmu = np.zeros(N), np.zeros(N)
+    o.L.pfo_test_mu(o.s, _ptr(Y), _ptr(phi), _ptr(sig.astype(np.float64)), _ptr(gx), _ptr(gmu))
+    assert np.array_equal(gx, rx) or np.abs(gx - rx).max() <= 1e-15
+    assert np.abs(gmu - rmu).max() <= 1e-12 * np.abs(rmu).max()
+
+
+@pytest.mark.parametrize("form", ["lagged", "previous_level", "no_gamma", "zero_mode"])
+def test_y_rhs_matches_reference_kernel(capi, form):
+    L = _refk()
+    L.refk_y_rhs.argtypes = [ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int, dp, ip]
+    n = 8
+    zm = 1 if form == "zero_mode" else 0
+    prev = 1 if form == "previous_level" else 0
+    nogam = 1 if form == "no_gamma" else 0
+    p = params_for(capi, "c2.params", n=n, zero_mode_enabled=zm, enable_Y_rhs_previous_time_level=prev,
+                   disable_Y_rhs_gamma_term=nogam, Y_rhs_term_h_scale=1.0 if form != "lagged" else 0.75)
+    N = n ** 3
+    rng = np.random.default_rng(53)
+    divJ = rng.normal(0.0, 1.0, N)
+    phi_new = rng.uniform(0.0, 1.0, N)
+    phi_old = np.clip(phi_new + rng.normal(0.0, 0.01, N), 0.0, 1.0)
+    lapY = rng.normal(0.0, 0.5, N)
+    Y = rng.uniform(-10.0, 2.0, N)
+    dYdt = rng.normal(0.0, 0.3, N)
+    dt, mean_DY = p.dt, 123.25
+    L.refk_set_convex(p.thermo_convex_extrapolation_enabled)
+    d = np.array([dt, p.v_B, mean_DY, p.Y_rhs_term_h_scale])
+    flags = np.array([prev, nogam], dtype=np.int32)
+    ref = np.zeros(N)
+    L.refk_y_rhs(zm, _ptr(divJ), _ptr(phi_new), _ptr(phi_old), _ptr(lapY), _ptr(Y), _ptr(dYdt), _ptr(ref), N,
+                 _ptr(d), _ptr(flags, ip))
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_y_rhs.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, dp, dp, dp, dp, dp, dp, dp]
+    got = np.zeros(N)
+    o.L.pfo_test_y_rhs(o.s, dt, mean_DY, _ptr(divJ), _ptr(phi_new), _ptr(phi_old), _ptr(lapY), _ptr(Y), _ptr(dYdt),
+                       _ptr(got))
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
