@@ -105,7 +105,19 @@ def _kernel_section(path: str) -> str:
         if depth == 0 and re.match(r"^[A-Za-z_]", l) and not l.startswith("#"):
             starts.append(i)
         depth += l.count("{") - l.count("}")
-    return "\n".join(lines[last_inc + 1:starts[-1]]) + "\n"
+    out = lines[last_inc + 1:starts[-1]]
+    # kernels defined among the launch wrappers, taken whole by name
+    for name in ("compute_displacement_from_hij_green_kernel", "compute_strain_with_perturbation_kernel"):
+        i0 = next(i for i, l in enumerate(lines) if l.startswith("__global__ void " + name + "("))
+        depth, seen, i = 0, False, i0
+        while True:
+            depth += lines[i].count("{") - lines[i].count("}")
+            seen = seen or "{" in lines[i]
+            i += 1
+            if seen and depth == 0:
+                break
+        out += lines[i0:i]
+    return "\n".join(out) + "\n"
 
 
 def build_ref_kernels(force: bool = False) -> str | None:

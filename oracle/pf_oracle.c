@@ -589,11 +589,69 @@ static void elastic_inv(pfo_state *s, const cpx *k, double *r) {
     if (s->fp32e) for (size_t i = 0; i < s->N; ++i) r[i] = (double)(float)r[i];
 }
 
+/* the elastic constants in elastic precision (the reference casts S, S_p,
+ * eps00 and E0 to float, main_cuda.cu:28762-28790) */
+static void elastic_consts(pfo_state *s, elast_consts *ec) {
+    const pfgb_params *P = &s->p;
+    for (int c = 0; c < 21; ++c) { ec->S[c] = rf(s, P->S[c]); ec->Sp[c] = rf(s, P->S_p[c]); }
+    for (int c = 0; c < 6; ++c) { ec->e00[c] = rf(s, P->eps00[c]); ec->E0[c] = rf(s, P->E0[c]); }
+}
+
+/* compute_strain_with_perturbation_kernel, cuda_kernels.cu:7002-7157:
+ * h = C0:eps - (C0 + h dC):(eps + E0 - eps0) over s->eps_r in place (the
+ * increment form's linear part: eps only) */
+static void polarization(pfo_state *s, const elast_consts *ecp, int gp_el, int lin) {
+    const elast_consts ec = *ecp;
+    RLOOP_BEGIN(s)
+        double e[6], e0[6];
+        for (int c = 0; c < 6; ++c) e[c] = s->eps_r[c][idx];
+        eigen_point(s, &ec, s->phi[idx], s->eta[idx], o_clamp01(s->xB[idx]), gp_el, e0);
+        double hw = o_h(s->phi[idx]);   /* stiffness_beta_weight_point */
+        double ev[6], tv[6];
+        double tot[6];
+        for (int c = 0; c < 6; ++c) tot[c] = lin ? e[c] : e[c] + ec.E0[c] - e0[c];
+        eng(e, ev); eng(tot, tv);
+        static const int rowv[6] = {1, 2, 3, 4, 5, 6};
+        for (int c = 0; c < 6; ++c) {
+            double acc = 0.0;
+            for (int b = 0; b < 6; ++b) {
+                double c0 = voigt(ec.S, rowv[c], b + 1);
+                double ce = c0 + rf(s, hw * voigt(ec.Sp, rowv[c], b + 1));
+                acc += c0 * ev[b] - ce * tv[b];
+            }
+            s->eps_r[c][idx] = rf(s, acc);
+        }
+    RLOOP_END
+}
+
+/* test hooks for the pinning tests: the polarization on given strains
+ * (eps: 6 N, Voigt xx yy zz yz xz xy, tensor strain) and the Green's
+ * contraction of given polarization spectra (tau: 6 Nk, u: 3 Nk complex) */
+void pfo_test_polarization(pfo_state *s, int lin, const double *phi, const double *eta, const double *xB,
+                           const double *eps, double *out) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->phi, phi, b);
+    memcpy(s->eta, eta, b);
+    memcpy(s->xB, xB, b);
+    for (int c = 0; c < 6; ++c) memcpy(s->eps_r[c], eps + (size_t)c * s->N, b);
+    elast_consts ec;
+    elastic_consts(s, &ec);
+    polarization(s, &ec, s->gp && s->p.gp_elastic_enabled, lin);
+    for (int c = 0; c < 6; ++c) memcpy(out + (size_t)c * s->N, s->eps_r[c], b);
+}
+void pfo_test_green(pfo_state *s, const double *tau, double *u) {
+    const size_t kb = sizeof(cpx) * s->Nk;
+    for (int c = 0; c < 6; ++c) memcpy(s->eps_k[c], tau + 2 * (size_t)c * s->Nk, kb);
+    elast_consts ec;
+    elastic_consts(s, &ec);
+    green_apply(s, &ec, s->eps_k, 0, s->u_next);
+    for (int c = 0; c < 3; ++c) memcpy(u + 2 * (size_t)c * s->Nk, s->u_next[c], kb);
+}
+
 static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
     const pfgb_params *P = &s->p;
     elast_consts ec;
-    for (int c = 0; c < 21; ++c) { ec.S[c] = rf(s, P->S[c]); ec.Sp[c] = rf(s, P->S_p[c]); }
-    for (int c = 0; c < 6; ++c) { ec.e00[c] = rf(s, P->eps00[c]); ec.E0[c] = rf(s, P->E0[c]); }
+    elastic_consts(s, &ec);
     const double invNf = rf(s, s->invN);
     const int gp_el = s->gp && P->gp_elastic_enabled;
     const int accel = P->elastic_enabled && (P->elastic_warm_start_enabled || P->elastic_residual_control_enabled);
@@ -648,28 +706,7 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
             double *e = s->eps_r[c];
             RLOOP_BEGIN(s) e[idx] = rf(s, e[idx] * invNf); RLOOP_END
         }
-        /* compute_strain_with_perturbation_kernel, cuda_kernels.cu:7002-7157:
-         * h = C0:eps - (C0 + h dC):(eps + E0 - eps0) */
-        RLOOP_BEGIN(s)
-            double e[6], e0[6];
-            for (int c = 0; c < 6; ++c) e[c] = s->eps_r[c][idx];
-            eigen_point(s, &ec, s->phi[idx], s->eta[idx], o_clamp01(s->xB[idx]), gp_el, e0);
-            double hw = o_h(s->phi[idx]);   /* stiffness_beta_weight_point */
-            double ev[6], tv[6];
-            double tot[6];
-            for (int c = 0; c < 6; ++c) tot[c] = lin ? e[c] : e[c] + ec.E0[c] - e0[c];
-            eng(e, ev); eng(tot, tv);
-            static const int rowv[6] = {1, 2, 3, 4, 5, 6};
-            for (int c = 0; c < 6; ++c) {
-                double acc = 0.0;
-                for (int b = 0; b < 6; ++b) {
-                    double c0 = voigt(ec.S, rowv[c], b + 1);
-                    double ce = c0 + rf(s, hw * voigt(ec.Sp, rowv[c], b + 1));
-                    acc += c0 * ev[b] - ce * tv[b];
-                }
-                s->eps_r[c][idx] = rf(s, acc);
-            }
-        RLOOP_END
+        polarization(s, &ec, gp_el, lin);
         for (int c = 0; c < 6; ++c) { elastic_fwd(s, s->eps_r[c], s->eps_k[c]); dealias(s, s->eps_k[c]); }
         cpx **target = accel ? s->u_next : s->u_k;
         green_apply(s, &ec, s->eps_k, 0, target);

@@ -45,6 +45,9 @@ void pfo_test_phi_rhs(pfo_state *s, int coupling, const double *phi, const doubl
 void pfo_test_eta_rhs(pfo_state *s, const double *eta, const double *phi, const double *xB, const double *sig,
                       double *out);
 void pfo_test_mu(pfo_state *s, const double *Y, const double *phiY, const double *sig, double *xB, double *mu);
+void pfo_test_polarization(pfo_state *s, int lin, const double *phi, const double *eta, const double *xB,
+                           const double *eps, double *out);
+void pfo_test_green(pfo_state *s, const double *tau, double *u);
 void pfo_test_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ, const double *phi_new,
                     const double *phi_old, const double *lapY, const double *Y, const double *dYdt, double *out);
 /* minimize iterations (mode = minimize, full model, two_phase, zero mode off) */

@@ -148,4 +148,33 @@ void refk_y_rhs(int zm, const double *divJ, const double *phi_new, const double 
                                            i[1], d[3], (double *)nullptr));
 }
 
+// compute_strain_with_perturbation_kernel over n cells: the strains
+// (6 n floats, xx yy zz yz xz xy) to the polarization written the same way.
+// S, Sp: the 21 entries each; e00: xx yy zz yz xz xy; E0 likewise.
+// i: gp_mode_enabled, gp_elastic_enabled.  d: eps_iso_over_vB, gp_eps_iso.
+void refk_polarization(const float *eps, const double *phi, const double *eta, const double *xB, float *out,
+                       int n, const float *S, const float *Sp, const float *e00, const float *E0, const double *d,
+                       const int *i) {
+    REF_LAUNCH(n, compute_strain_with_perturbation_kernel(
+        eps, eps + n, eps + 2 * n, eps + 5 * n, eps + 4 * n, eps + 3 * n, phi, eta, xB,
+        out, out + n, out + 2 * n, out + 5 * n, out + 4 * n, out + 3 * n,
+        S[0], S[1], S[2], S[3], S[4], S[5], S[6], S[7], S[8], S[9], S[10], S[11], S[12], S[13], S[14], S[15],
+        S[16], S[17], S[18], S[19], S[20],
+        Sp[0], Sp[1], Sp[2], Sp[3], Sp[4], Sp[5], Sp[6], Sp[7], Sp[8], Sp[9], Sp[10], Sp[11], Sp[12], Sp[13],
+        Sp[14], Sp[15], Sp[16], Sp[17], Sp[18], Sp[19], Sp[20],
+        e00[0], e00[1], e00[2], e00[3], e00[4], e00[5], d[0], i[0], i[1], d[1],
+        E0[0], E0[1], E0[2], E0[3], E0[4], E0[5], n));
+}
+
+// compute_displacement_from_hij_green_kernel over the Nk points of an
+// Nx x Ny x Nz grid: tau (6 Nk cufftComplex, xx yy zz yz xz xy) to u (3 Nk).
+void refk_green(const cufftComplex *tau, cufftComplex *u, int Nx, int Ny, int Nz, const float *S, double dx,
+                double dy, double dz) {
+    const int NzC = Nz / 2 + 1, nk = Nx * Ny * NzC;
+    REF_LAUNCH(nk, compute_displacement_from_hij_green_kernel(
+        tau, tau + nk, tau + 2 * nk, tau + 5 * nk, tau + 4 * nk, tau + 3 * nk, u, u + nk, u + 2 * nk,
+        S[0], S[1], S[2], S[3], S[4], S[5], S[6], S[7], S[8], S[9], S[10], S[11], S[12], S[13], S[14], S[15],
+        S[16], S[17], S[18], S[19], S[20], Nx, Ny, Nz, NzC, dx, dy, dz, nk));
+}
+
 }  // extern "C"

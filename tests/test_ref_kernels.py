@@ -172,3 +172,56 @@ def test_y_rhs_matches_reference_kernel(capi, form):
     o.L.pfo_test_y_rhs(o.s, dt, mean_DY, _ptr(divJ), _ptr(phi_new), _ptr(phi_old), _ptr(lapY), _ptr(Y), _ptr(dYdt),
                        _ptr(got))
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("mode", ["two_phase", "gp_zone", "gp_zone_gp_elastic"])
+def test_polarization_matches_reference_kernel(capi, mode):
+    """The elastic iteration's polarization h = C0:eps - C:(eps + E0 - eps0).
+    The reference computes it in float arithmetic, the oracle in double with
+    float storage, so the bound is float round-off: 1e-5 of the largest
+    component."""
+    L = _refk()
+    L.refk_polarization.argtypes = [fp, dp, dp, dp, fp, ctypes.c_int, fp, fp, fp, fp, dp, ip]
+    n = 8
+    mm = 0 if mode == "two_phase" else 1
+    gel = 1 if mode == "gp_zone_gp_elastic" else 0
+    p = params_for(capi, "c2.params", n=n, model_mode=mm, gp_elastic_enabled=gel, elastic_precision=capi.PREC_FP32)
+    N = n ** 3
+    phi, eta, xB, _, eps = _fields(N, 61 + mm + gel)
+    f32 = lambda a: np.array(a[:], dtype=np.float32)   # noqa: E731
+    S, Sp, e00, E0 = f32(p.S), f32(p.S_p), f32(p.eps00), f32(p.E0)
+    d = np.array([p.eps_iso_over_vB, p.gp_eps_iso])
+    flags = np.array([mm, gel], dtype=np.int32)
+    ref = np.zeros(6 * N, dtype=np.float32)
+    L.refk_polarization(_ptr(eps, fp), _ptr(phi), _ptr(eta), _ptr(xB), _ptr(ref, fp), N, _ptr(S, fp), _ptr(Sp, fp),
+                        _ptr(e00, fp), _ptr(E0, fp), _ptr(d), _ptr(flags, ip))
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_polarization.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, dp, dp]
+    got = np.zeros(6 * N)
+    o.L.pfo_test_polarization(o.s, 0, _ptr(phi), _ptr(eta), _ptr(xB), _ptr(eps.astype(np.float64)), _ptr(got))
+    ref = ref.astype(np.float64)
+    assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), np.abs(got - ref).max() / np.abs(ref).max()
+
+
+def test_green_matches_reference_kernel(capi):
+    """u = -i G(k) (k . tau) of the homogeneous medium, on a non-cubic grid
+    (Nyquist planes included); float arithmetic on the reference side."""
+    L = _refk()
+    L.refk_green.argtypes = [fp, fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, fp, ctypes.c_double,
+                             ctypes.c_double, ctypes.c_double]
+    Nx, Ny, Nz = 6, 8, 10
+    p = params_for(capi, "c2.params", n=8, elastic_precision=capi.PREC_FP32)
+    p.Nx, p.Ny, p.Nz = Nx, Ny, Nz
+    capi.finalize(p)
+    Nk = Nx * Ny * (Nz // 2 + 1)
+    rng = np.random.default_rng(71)
+    tau = rng.normal(0.0, 1.0, 12 * Nk).astype(np.float32)
+    S = np.array(p.S[:], dtype=np.float32)
+    ref = np.zeros(6 * Nk, dtype=np.float32)
+    L.refk_green(_ptr(tau, fp), _ptr(ref, fp), Nx, Ny, Nz, _ptr(S, fp), p.dx, p.dy, p.dz)
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_green.argtypes = [ctypes.c_void_p, dp, dp]
+    got = np.zeros(6 * Nk)
+    o.L.pfo_test_green(o.s, _ptr(tau.astype(np.float64)), _ptr(got))
+    ref = ref.astype(np.float64)
+    assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), np.abs(got - ref).max() / np.abs(ref).max()
