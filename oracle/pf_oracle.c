@@ -1021,6 +1021,39 @@ static int zero_mode(pfo_state *s, const double *Ystar, double Y_upper_cap, pfgb
     return PFGB_OK;
 }
 
+/* two_phase_storage_exact_Y_update_kernel, cuda_kernels.cu:2859-2921: the
+ * point update of the composition from divJ, Y^n, phi^n and phi^{n+1} */
+static void storage_exact_update(pfo_state *s, double dt) {
+    const pfgb_params *P = &s->p;
+    RLOOP_BEGIN(s)
+        const double ho = o_h(o_clamp01(s->phi_n[idx])), hn = o_h(o_clamp01(s->phi[idx]));
+        const double xo = o_sigmoid(s->Y_n[idx], P->Y_clip, P->xB_eps);
+        const double Ct = (1.0 - ho) * xo + ho * P->v_B + dt * s->divJ[idx];
+        const double han = 1.0 - hn;
+        const int small = !(han >= P->gp_h_alpha_eps);
+        double xt = xo;
+        if (!small && isfinite(Ct)) xt = (Ct - hn * P->v_B) / han;
+        const int bad = small || !isfinite(xt) || xt < P->xB_eps || xt > 1.0 - P->xB_eps;
+        const double y = o_logit(bad ? xo : xt, P->xB_eps, P->Y_clip);
+        s->Y[idx] = y;
+        s->xB[idx] = o_sigmoid(y, P->Y_clip, P->xB_eps);
+        s->dYdt[idx] = (y - s->Y_n[idx]) / dt;
+    RLOOP_END
+}
+
+/* test hook (the pinning tests): the storage-exact update on given fields */
+void pfo_test_storage_exact(pfo_state *s, double dt, const double *divJ, const double *phi_new,
+                            const double *phi_old, const double *Y_old, double *Y, double *xB) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->divJ, divJ, b);
+    memcpy(s->phi, phi_new, b);
+    memcpy(s->phi_n, phi_old, b);
+    memcpy(s->Y_n, Y_old, b);
+    storage_exact_update(s, dt);
+    memcpy(Y, s->Y, b);
+    memcpy(xB, s->xB, b);
+}
+
 /* mu of the flux, in place of Y^n's composition (compute_mu_x_kernel,
  * cuda_kernels.cu:1266-1324; gp_zone: compute_mu_C_gp_kernel, :1326-1366);
  * also xB = sigmoid(Y) */
@@ -1168,20 +1201,7 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
         /* two_phase_storage_exact_Y_update_kernel, cuda_kernels.cu:2859-2921:
          * C^n + dt divJ solved for x_alpha with h^{n+1}; x^n kept where the
          * matrix storage is below its floor or the solution leaves [eps, 1-eps] */
-        RLOOP_BEGIN(s)
-            const double ho = o_h(o_clamp01(s->phi_n[idx])), hn = o_h(o_clamp01(s->phi[idx]));
-            const double xo = o_sigmoid(s->Y_n[idx], P->Y_clip, P->xB_eps);
-            const double Ct = (1.0 - ho) * xo + ho * P->v_B + dt * s->divJ[idx];
-            const double han = 1.0 - hn;
-            const int small = !(han >= P->gp_h_alpha_eps);
-            double xt = xo;
-            if (!small && isfinite(Ct)) xt = (Ct - hn * P->v_B) / han;
-            const int bad = small || !isfinite(xt) || xt < P->xB_eps || xt > 1.0 - P->xB_eps;
-            const double y = o_logit(bad ? xo : xt, P->xB_eps, P->Y_clip);
-            s->Y[idx] = y;
-            s->xB[idx] = o_sigmoid(y, P->Y_clip, P->xB_eps);
-            s->dYdt[idx] = (y - s->Y_n[idx]) / dt;
-        RLOOP_END
+        storage_exact_update(s, dt);
         if (st) {
             RLOOP_BEGIN(s)
                 double h = o_h(phiY[idx]);

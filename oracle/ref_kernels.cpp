@@ -177,4 +177,12 @@ void refk_green(const cufftComplex *tau, cufftComplex *u, int Nx, int Ny, int Nz
         S[16], S[17], S[18], S[19], S[20], Nx, Ny, Nz, NzC, dx, dy, dz, nk));
 }
 
+// two_phase_storage_exact_Y_update_kernel over n cells.  d: dt, v_B, Y_clip,
+// Y_upper_cap, xB_eps, h_alpha_eps.
+void refk_storage_exact(const double *divJ, const double *phi_new, const double *phi_old, const double *Y_old,
+                        double *Y, double *xB, int n, const double *d) {
+    REF_LAUNCH(n, two_phase_storage_exact_Y_update_kernel(divJ, phi_new, phi_old, Y_old, Y, xB, d[0], d[1], d[2],
+                                                          d[3], d[4], d[5], (double *)nullptr, n));
+}
+
 }  // extern "C"

@@ -225,3 +225,30 @@ def test_green_matches_reference_kernel(capi):
     o.L.pfo_test_green(o.s, _ptr(tau.astype(np.float64)), _ptr(got))
     ref = ref.astype(np.float64)
     assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), np.abs(got - ref).max() / np.abs(ref).max()
+
+
+def test_storage_exact_update_matches_reference_kernel(capi):
+    """The storage-exact point update, with cells that take the kept branch
+    (small matrix storage, solutions outside [eps, 1 - eps]) and the trial."""
+    L = _refk()
+    L.refk_storage_exact.argtypes = [dp, dp, dp, dp, dp, dp, ctypes.c_int, dp]
+    n = 8
+    p = params_for(capi, "c2.params", n=n, pf_y_update_mode=capi.Y_STORAGE_EXACT)
+    N = n ** 3
+    rng = np.random.default_rng(81)
+    phi_new = rng.uniform(0.0, 1.0, N)
+    phi_old = np.clip(phi_new + rng.normal(0.0, 0.05, N), 0.0, 1.0)
+    phi_new[:20] = 1.0                       # no matrix storage left
+    Y_old = rng.uniform(-6.0, 0.5, N)
+    divJ = rng.normal(0.0, 2.0, N)
+    d = np.array([p.dt, p.v_B, p.Y_clip, p.Y_clip, p.xB_eps, p.gp_h_alpha_eps])
+    rY, rx = np.zeros(N), np.zeros(N)
+    L.refk_storage_exact(_ptr(divJ), _ptr(phi_new), _ptr(phi_old), _ptr(Y_old), _ptr(rY), _ptr(rx), N, _ptr(d))
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_storage_exact.argtypes = [ctypes.c_void_p, ctypes.c_double, dp, dp, dp, dp, dp, dp]
+    gY, gx = np.zeros(N), np.zeros(N)
+    o.L.pfo_test_storage_exact(o.s, p.dt, _ptr(divJ), _ptr(phi_new), _ptr(phi_old), _ptr(Y_old), _ptr(gY), _ptr(gx))
+    kept = np.abs(gY - Y_old) < 1e-9
+    assert 20 <= kept.sum() < N                  # both branches are exercised
+    assert np.abs(gY - rY).max() <= 1e-12 * np.abs(rY).max()
+    assert np.abs(gx - rx).max() <= 1e-14
