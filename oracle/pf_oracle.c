@@ -1054,6 +1054,46 @@ void pfo_test_storage_exact(pfo_state *s, double dt, const double *divJ, const d
     memcpy(xB, s->xB, b);
 }
 
+/* one flux component J_a = M g_a over s->scr in place, g_a the unnormalised
+ * inverse transform of i k_a mu (compute_flux_single_component_kernel,
+ * cuda_kernels.cu:1985-2037; gp_zone: compute_flux_single_component_gp_kernel,
+ * :2039-2110), the mobility from the composition of Y^n in s->xB_prev */
+static void flux_field(pfo_state *s, const double *phiY, const double *etaY) {
+    const pfgb_params *P = &s->p;
+    const double T = P->temperature_K, sc = P->mu_reference_scale;
+    const int cv = P->thermo_convex_extrapolation_enabled;
+    RLOOP_BEGIN(s)
+        double g = s->scr[idx] * s->invN;
+        double M;
+        if (s->gp) {   /* compute_flux_single_component_gp_kernel, :2039 */
+            double hb = o_h(phiY[idx]), he = o_h(etaY[idx]);
+            double hg = (1.0 - hb) * he, ha = (1.0 - hb) * (1.0 - he);
+            double Ga = o_gamma(s->xB_prev[idx], 0.0, P->Vm_alpha_0, P->dVm_alpha_dxB,
+                                P->Vm_compound, T, sc, cv);
+            double Ma = o_meff(P->D_alpha, Ga);
+            M = ha * Ma + hg * P->gp_M_GP + hb * P->gp_M_beta;
+        } else {       /* compute_flux_single_component_kernel, :1985 */
+            double h = o_h(phiY[idx]);
+            double Dm = o_Dmix(h, P->D_alpha, P->D_compound);
+            double G = o_gamma(s->xB_prev[idx], h, P->Vm_alpha_0, P->dVm_alpha_dxB,
+                               P->Vm_compound, T, sc, cv);
+            M = o_meff(Dm, G);
+        }
+        s->scr[idx] = M * g;
+    RLOOP_END
+}
+
+/* test hook (the pinning tests): one flux component on given fields; g is
+ * the normalised gradient */
+void pfo_test_flux(pfo_state *s, const double *g, const double *phiY, const double *etaY, const double *xB_prev,
+                   double *J) {
+    const size_t b = sizeof(double) * s->N;
+    for (size_t i = 0; i < s->N; ++i) s->scr[i] = g[i] * (double)s->N;
+    memcpy(s->xB_prev, xB_prev, b);
+    flux_field(s, phiY, etaY);
+    memcpy(J, s->scr, b);
+}
+
 /* mu of the flux, in place of Y^n's composition (compute_mu_x_kernel,
  * cuda_kernels.cu:1266-1324; gp_zone: compute_mu_C_gp_kernel, :1326-1366);
  * also xB = sigmoid(Y) */
@@ -1149,8 +1189,6 @@ void pfo_test_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ,
  * 31618-31623; fields at entry: phi = phi^{n+1}, phi_n = phi^n, Y = Y^n. */
 static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
     pfgb_params *P = &s->p;
-    const double T = P->temperature_K, sc = P->mu_reference_scale;
-    const int cv = P->thermo_convex_extrapolation_enabled;
     const int zm = P->zero_mode_enabled;
     const double *phiY = zm ? s->phi_n : (P->enable_Y_rhs_previous_time_level ? s->phi_n : s->phi);
     const double *etaY = s->eta;
@@ -1167,25 +1205,7 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
         KLOOP_END
         dealias(s, s->scr_k);
         inv(s, s->scr_k, s->scr);
-        RLOOP_BEGIN(s)
-            double g = s->scr[idx] * s->invN;
-            double M;
-            if (s->gp) {   /* compute_flux_single_component_gp_kernel, :2039 */
-                double hb = o_h(phiY[idx]), he = o_h(etaY[idx]);
-                double hg = (1.0 - hb) * he, ha = (1.0 - hb) * (1.0 - he);
-                double Ga = o_gamma(s->xB_prev[idx], 0.0, P->Vm_alpha_0, P->dVm_alpha_dxB,
-                                    P->Vm_compound, T, sc, cv);
-                double Ma = o_meff(P->D_alpha, Ga);
-                M = ha * Ma + hg * P->gp_M_GP + hb * P->gp_M_beta;
-            } else {       /* compute_flux_single_component_kernel, :1985 */
-                double h = o_h(phiY[idx]);
-                double Dm = o_Dmix(h, P->D_alpha, P->D_compound);
-                double G = o_gamma(s->xB_prev[idx], h, P->Vm_alpha_0, P->dVm_alpha_dxB,
-                                   P->Vm_compound, T, sc, cv);
-                M = o_meff(Dm, G);
-            }
-            s->scr[idx] = M * g;
-        RLOOP_END
+        flux_field(s, phiY, etaY);
         fwd(s, s->scr, s->scr_k); dealias(s, s->scr_k);
         KLOOP_BEGIN(s)   /* divJ_accumulate_kernel, :2112 */
             double ka = a == 0 ? s->kx[ii_] : (a == 1 ? s->ky[jj_] : s->kz[kk_]);

@@ -48,6 +48,8 @@ void pfo_test_mu(pfo_state *s, const double *Y, const double *phiY, const double
 void pfo_test_polarization(pfo_state *s, int lin, const double *phi, const double *eta, const double *xB,
                            const double *eps, double *out);
 void pfo_test_green(pfo_state *s, const double *tau, double *u);
+void pfo_test_flux(pfo_state *s, const double *g, const double *phiY, const double *etaY, const double *xB_prev,
+                   double *J);
 void pfo_test_storage_exact(pfo_state *s, double dt, const double *divJ, const double *phi_new,
                             const double *phi_old, const double *Y_old, double *Y, double *xB);
 void pfo_test_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ, const double *phi_new,

@@ -185,4 +185,17 @@ void refk_storage_exact(const double *divJ, const double *phi_new, const double 
                                                           d[3], d[4], d[5], (double *)nullptr, n));
 }
 
+// compute_flux_single_component_kernel (gp = 0) or the _gp_ variant over n
+// cells.  d: D_alpha, D_compound, Vm_alpha_0, dVm_alpha_dxB, Vm_compound,
+// T_K, mu_reference_scale, gp_M_GP, gp_M_beta.
+void refk_flux(int gp, const double *g, const double *phi, const double *eta, const double *xB_prev, double *J,
+               int n, const double *d) {
+    if (gp)
+        REF_LAUNCH(n, compute_flux_single_component_gp_kernel(g, phi, eta, xB_prev, J, d[0], d[7], d[8], d[2], d[3],
+                                                              d[4], d[5], d[6], n));
+    else
+        REF_LAUNCH(n, compute_flux_single_component_kernel(g, phi, xB_prev, J, d[0], d[1], d[2], d[3], d[4], d[5],
+                                                           d[6], n));
+}
+
 }  // extern "C"

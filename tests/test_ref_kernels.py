@@ -252,3 +252,29 @@ def test_storage_exact_update_matches_reference_kernel(capi):
     assert 20 <= kept.sum() < N                  # both branches are exercised
     assert np.abs(gY - rY).max() <= 1e-12 * np.abs(rY).max()
     assert np.abs(gx - rx).max() <= 1e-14
+
+
+@pytest.mark.parametrize("gp", [0, 1])
+def test_flux_matches_reference_kernel(capi, gp):
+    """One flux component J = M grad(mu) with the stabilised mobility (D_mix
+    over the thermodynamic factor, or the GP-zone phase-weighted form)."""
+    L = _refk()
+    L.refk_flux.argtypes = [ctypes.c_int, dp, dp, dp, dp, dp, ctypes.c_int, dp]
+    n = 8                      # N = 512: the oracle's 1/N scaling is exact
+    p = params_for(capi, "c2.params", n=n, model_mode=gp)
+    N = n ** 3
+    rng = np.random.default_rng(91 + gp)
+    g = rng.normal(0.0, 1.0, N)
+    phi = rng.uniform(0.0, 1.0, N)
+    eta = rng.uniform(0.0, 1.0, N)
+    xB = rng.uniform(1e-4, 0.3, N)
+    L.refk_set_convex(p.thermo_convex_extrapolation_enabled)
+    d = np.array([p.D_alpha, p.D_compound, p.Vm_alpha_0, p.dVm_alpha_dxB, p.Vm_compound, p.temperature_K,
+                  p.mu_reference_scale, p.gp_M_GP, p.gp_M_beta])
+    ref = np.zeros(N)
+    L.refk_flux(gp, _ptr(g), _ptr(phi), _ptr(eta), _ptr(xB), _ptr(ref), N, _ptr(d))
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_flux.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp]
+    got = np.zeros(N)
+    o.L.pfo_test_flux(o.s, _ptr(g), _ptr(phi), _ptr(eta), _ptr(xB), _ptr(got))
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
