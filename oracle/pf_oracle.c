@@ -1094,6 +1094,57 @@ void pfo_test_flux(pfo_state *s, const double *g, const double *phiY, const doub
     memcpy(J, s->scr, b);
 }
 
+/* the x split's right-hand side S - m Lap(x^n) with the storage source
+ * S = divJ / (1 - h^{n+1}) where the matrix storage reaches its floor
+ * (compute_xB_storage_rhs_kernel, cuda_kernels.cu:2922-2951); lapY holds the
+ * unnormalised inverse transform of -k^2 x^n */
+static void xsplit_source(pfo_state *s, double mDx) {
+    const pfgb_params *P = &s->p;
+    RLOOP_BEGIN(s)
+        const double lap = s->lapY[idx] * s->invN;
+        const double ha = 1.0 - o_h(o_clamp01(s->phi[idx]));
+        const double rate = ha >= P->pf_matrix_storage_floor ? s->divJ[idx] / ha : 0.0;
+        s->rhs[idx] = rate - mDx * lap;
+    RLOOP_END
+}
+
+/* the x split's new composition from the unnormalised inverse transform in
+ * scr (xB_normalize_clamp_and_logit_kernel, :2953-2973) */
+static void xsplit_final(pfo_state *s, double dt) {
+    const pfgb_params *P = &s->p;
+    RLOOP_BEGIN(s)
+        double x = s->scr[idx] * s->invN;
+        if (!isfinite(x)) x = s->xB[idx];
+        x = fmin(fmax(x, P->xB_eps), 1.0 - P->xB_eps);
+        double y = o_logit(x, P->xB_eps, P->Y_clip);
+        y = fmin(fmax(y, -P->Y_clip), P->Y_clip);
+        s->Y[idx] = y;
+        s->xB[idx] = o_sigmoid(y, P->Y_clip, P->xB_eps);
+        s->dYdt[idx] = (y - s->Y_n[idx]) / dt;
+    RLOOP_END
+}
+
+/* test hooks (the pinning tests) for the two x-split functions; lap and x
+ * are normalised */
+void pfo_test_xsplit_source(pfo_state *s, double mDx, const double *divJ, const double *phi_new,
+                            const double *lap, double *rhs) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->divJ, divJ, b);
+    memcpy(s->phi, phi_new, b);
+    for (size_t i = 0; i < s->N; ++i) s->lapY[i] = lap[i] * (double)s->N;
+    xsplit_source(s, mDx);
+    memcpy(rhs, s->rhs, b);
+}
+void pfo_test_xsplit_final(pfo_state *s, double dt, const double *x, const double *xB_old, double *Y, double *xB) {
+    const size_t b = sizeof(double) * s->N;
+    for (size_t i = 0; i < s->N; ++i) s->scr[i] = x[i] * (double)s->N;
+    memcpy(s->xB, xB_old, b);
+    memset(s->Y_n, 0, b);
+    xsplit_final(s, dt);
+    memcpy(Y, s->Y, b);
+    memcpy(xB, s->xB, b);
+}
+
 /* mu of the flux, in place of Y^n's composition (compute_mu_x_kernel,
  * cuda_kernels.cu:1266-1324; gp_zone: compute_mu_C_gp_kernel, :1326-1366);
  * also xB = sigmoid(Y) */
@@ -1249,12 +1300,7 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
         KLOOP_END
         dealias(s, s->Y_k);
         inv(s, s->Y_k, s->lapY);
-        RLOOP_BEGIN(s)
-            const double lap = s->lapY[idx] * s->invN;
-            const double ha = 1.0 - o_h(o_clamp01(s->phi[idx]));
-            const double rate = ha >= P->pf_matrix_storage_floor ? s->divJ[idx] / ha : 0.0;
-            s->rhs[idx] = rate - mDx * lap;
-        RLOOP_END
+        xsplit_source(s, mDx);
         fwd(s, s->rhs, s->rhs_k); dealias(s, s->rhs_k);
         KLOOP_BEGIN(s)
             double den = 1.0 + dt * mDx * k2_at(s, ii_, jj_, kk_);
@@ -1264,16 +1310,7 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
         KLOOP_END
         dealias(s, s->Y_k);
         inv(s, s->Y_k, s->scr);
-        RLOOP_BEGIN(s)
-            double x = s->scr[idx] * s->invN;
-            if (!isfinite(x)) x = s->xB[idx];
-            x = fmin(fmax(x, P->xB_eps), 1.0 - P->xB_eps);
-            double y = o_logit(x, P->xB_eps, P->Y_clip);
-            y = fmin(fmax(y, -P->Y_clip), P->Y_clip);
-            s->Y[idx] = y;
-            s->xB[idx] = o_sigmoid(y, P->Y_clip, P->xB_eps);
-            s->dYdt[idx] = (y - s->Y_n[idx]) / dt;
-        RLOOP_END
+        xsplit_final(s, dt);
         if (st) st->mean_DY = mDx;
         return PFGB_OK;
     }

@@ -198,4 +198,19 @@ void refk_flux(int gp, const double *g, const double *phi, const double *eta, co
                                                            d[6], n));
 }
 
+// compute_xB_storage_rhs_kernel over n cells (lap normalised).  d: dt, v_B,
+// mean_Dx, h_alpha_eps (the matrix storage floor).
+void refk_xsplit_source(const double *divJ, const double *phi_new, const double *phi_old, const double *lap,
+                        const double *xB_old, double *rhs, int n, const double *d) {
+    REF_LAUNCH(n, compute_xB_storage_rhs_kernel(divJ, phi_new, phi_old, lap, xB_old, rhs, d[0], d[1], d[2], d[3],
+                                                n));
+}
+
+// xB_normalize_clamp_and_logit_kernel over n cells (x normalised: invN 1);
+// xB holds the previous composition on entry.  d: xB_eps, Y_clip,
+// Y_upper_cap.
+void refk_xsplit_final(const double *x, double *xB, double *Y, int n, const double *d) {
+    REF_LAUNCH(n, xB_normalize_clamp_and_logit_kernel(const_cast<double *>(x), xB, Y, 1.0, d[0], d[1], d[2], n));
+}
+
 }  // extern "C"

@@ -278,3 +278,39 @@ def test_flux_matches_reference_kernel(capi, gp):
     got = np.zeros(N)
     o.L.pfo_test_flux(o.s, _ptr(g), _ptr(phi), _ptr(eta), _ptr(xB), _ptr(got))
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_x_split_functions_match_reference_kernels(capi):
+    """The x split's storage source (cells below and above the matrix-storage
+    floor) and its clamp-and-logit of the new composition (non-finite and
+    out-of-range values included)."""
+    L = _refk()
+    L.refk_xsplit_source.argtypes = [dp, dp, dp, dp, dp, dp, ctypes.c_int, dp]
+    L.refk_xsplit_final.argtypes = [dp, dp, dp, ctypes.c_int, dp]
+    n = 8                      # N = 512: the oracle's 1/N scaling is exact
+    p = params_for(capi, "c2.params", n=n, pf_y_update_mode=capi.Y_X_TRANSPORT_SPLIT)
+    N = n ** 3
+    rng = np.random.default_rng(101)
+    divJ = rng.normal(0.0, 1.0, N)
+    phi_new = rng.uniform(0.0, 1.0, N)
+    phi_old = rng.uniform(0.0, 1.0, N)
+    lap = rng.normal(0.0, 0.1, N)
+    xB_old = rng.uniform(1e-3, 0.3, N)
+    mDx = p.D_alpha * p.pf_composition_stabilizer_Dalpha_multiplier
+    d = np.array([p.dt, p.v_B, mDx, p.pf_matrix_storage_floor])
+    ref = np.zeros(N)
+    L.refk_xsplit_source(_ptr(divJ), _ptr(phi_new), _ptr(phi_old), _ptr(lap), _ptr(xB_old), _ptr(ref), N, _ptr(d))
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_xsplit_source.argtypes = [ctypes.c_void_p, ctypes.c_double, dp, dp, dp, dp]
+    o.L.pfo_test_xsplit_final.argtypes = [ctypes.c_void_p, ctypes.c_double, dp, dp, dp, dp]
+    got = np.zeros(N)
+    o.L.pfo_test_xsplit_source(o.s, mDx, _ptr(divJ), _ptr(phi_new), _ptr(lap), _ptr(got))
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+    x = rng.uniform(-0.05, 1.05, N)
+    x[:4] = [np.nan, np.inf, -np.inf, 0.5]
+    rx, rY = xB_old.copy(), np.zeros(N)
+    L.refk_xsplit_final(_ptr(x), _ptr(rx), _ptr(rY), N, _ptr(np.array([p.xB_eps, p.Y_clip, p.Y_clip])))
+    gY, gx = np.zeros(N), np.zeros(N)
+    o.L.pfo_test_xsplit_final(o.s, p.dt, _ptr(x), _ptr(xB_old), _ptr(gY), _ptr(gx))
+    assert np.abs(gY - rY).max() <= 1e-12 * np.abs(rY).max()
+    assert np.abs(gx - rx).max() <= 1e-15
