@@ -8,7 +8,7 @@
  * FP64; where the reference stores elastic quantities in FP32 (cuda_kernels.cu
  * elastic kernels, main_cuda.cu:28760-28790 casts) the oracle rounds the stored
  * value to float at the same point when elastic_precision == PFGB_PREC_FP32.
- * The sequence of the driver (main_cuda.cu:28427-31623) is followed literally:
+ * The step sequence of main_cuda's time loop (main_cuda.cu:28427-31623) is followed literally:
  * one FFT per reference FFT, one dealias per reference dealias call.
  */
 #include "pf_oracle.h"
