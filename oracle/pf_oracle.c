@@ -1145,6 +1145,14 @@ void pfo_test_xsplit_final(pfo_state *s, double dt, const double *x, const doubl
     memcpy(xB, s->xB, b);
 }
 
+/* test hook (the pinning tests): the 2/3 dealias rule on a given half
+ * spectrum (Nk complex values, in place) */
+void pfo_test_dealias(pfo_state *s, double *k) {
+    memcpy(s->scr_k, k, sizeof(cpx) * s->Nk);
+    dealias(s, s->scr_k);
+    memcpy(k, s->scr_k, sizeof(cpx) * s->Nk);
+}
+
 /* mu of the flux, in place of Y^n's composition (compute_mu_x_kernel,
  * cuda_kernels.cu:1266-1324; gp_zone: compute_mu_C_gp_kernel, :1326-1366);
  * also xB = sigmoid(Y) */

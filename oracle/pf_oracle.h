@@ -48,6 +48,7 @@ void pfo_test_mu(pfo_state *s, const double *Y, const double *phiY, const double
 void pfo_test_polarization(pfo_state *s, int lin, const double *phi, const double *eta, const double *xB,
                            const double *eps, double *out);
 void pfo_test_green(pfo_state *s, const double *tau, double *u);
+void pfo_test_dealias(pfo_state *s, double *k);
 void pfo_test_xsplit_source(pfo_state *s, double mDx, const double *divJ, const double *phi_new,
                             const double *lap, double *rhs);
 void pfo_test_xsplit_final(pfo_state *s, double dt, const double *x, const double *xB_old, double *Y, double *xB);

@@ -213,4 +213,10 @@ void refk_xsplit_final(const double *x, double *xB, double *Y, int n, const doub
     REF_LAUNCH(n, xB_normalize_clamp_and_logit_kernel(const_cast<double *>(x), xB, Y, 1.0, d[0], d[1], d[2], n));
 }
 
+// dealias_23_kernel on a half spectrum of an Nx x Ny x Nz grid, in place
+void refk_dealias(cuDoubleComplex *k, int Nx, int Ny, int Nz, double dx, double dy, double dz) {
+    const int NzC = Nz / 2 + 1, nk = Nx * Ny * NzC;
+    REF_LAUNCH(nk, dealias_23_kernel(k, Nx, Ny, Nz, NzC, dx, dy, dz, nk));
+}
+
 }  // extern "C"
