@@ -340,9 +340,12 @@ def run_ours(args):
     s.profile_enable(False)   # resets the launch counter; no per-launch events in the timed region
     ev0.record(stream)
     w0 = time.perf_counter()
+    conv, resid = [], []
     for _ in range(args.steps):
         st = s.step(1)
         iters.append(st.elastic_iterations)
+        conv.append(st.elastic_converged)
+        resid.append(st.elastic_relative_residual)
     ev1.record(stream)
     barrier()
     wall = time.perf_counter() - w0
@@ -451,6 +454,14 @@ def run_ours(args):
                            "l2": "inputs larger than L2 (working set > 1 GB at 246^3)",
                            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
                 "elastic_iters_per_step": sum(iters) / max(1, len(iters)),
+                # every timed step's elastic solve against the tolerance (the
+                # step continues at the cap, so this is the check)
+                "elastic_converged_steps": int(sum(conv)), "elastic_timed_steps": len(conv),
+                "elastic_max_final_residual": max(resid) if resid else None,
+                "elastic_max_iters": max(iters) if iters else None,
+                # summed per-launch kernel time over the step time: the rest is
+                # host round trips (residual reads, zero-mode scalars) and gaps
+                "kernel_busy_fraction": (total_ms / max(1, prof_steps)) / (ms_max / args.steps),
                 "wall_ms_per_step": 1e3 * wall / args.steps,
                 "gpu_launches": launches,
                 "clocks": clk, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "vs_plain_fp64": plain,

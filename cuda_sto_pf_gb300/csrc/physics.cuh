@@ -220,6 +220,31 @@ __device__ __forceinline__ T phi_rhs_sig(const PC &c, const ElasC<TE> &ec, T phi
     return f;
 }
 
+// phi-only minimize drive (compute_phi_rhs_minimize_kernel,
+// cuda_kernels.cu:6298-6374): double well plus, with elasticity on, the
+// eigenstrain and stiffness terms of the phi-only eigenstrain h(phi) eps00
+// (eigenstrain_phi_only_point, float eps00); no chemistry, no composition.
+template <typename T, typename TE, typename PC>
+__device__ __forceinline__ T phi_rhs_phi_only(const PC &c, const ElasC<TE> &ec, T phi, const TE *eps,
+                                              const TE *sg_) {
+    T f = T(c.W) * pf_gp(phi);
+    if (c.elastic) {
+        const T hp = pf_hp(phi);
+        T sg[6], de[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) { sg[a] = T(sg_[a]); de[a] = hp * T(c.e00[a]); }
+        const T dg = -(sg[0] * de[0] + sg[1] * de[1] + sg[2] * de[2] +
+                       T(2) * (sg[5] * de[5] + sg[4] * de[4] + sg[3] * de[3]));
+        TE e0[6];
+        eigenstrain<T, TE>(c, ec, phi, T(0), T(0), false, e0);
+        T el[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) el[a] = T(eps[a]) - T(e0[a]);
+        f += dg + T(0.5) * hp * q_voigt<T>(c.Sp, el);
+    }
+    return f;
+}
+
 // the same with sigma from Hooke's law at (phi, eta, xB): the dynamics step,
 // where the stored stress of the reference is that of the current fields
 template <typename T, typename TE, typename PC>

@@ -2267,15 +2267,20 @@ template <typename T, typename TE>
 struct OpMinGradZ {
     using Acc = NoAcc;
     DevState<T, TE> d; PhysCT<T> c; ElasC<TE> ec; const T *phi;
+    int phi_only;   // minimize_full_model = 0: compute_phi_rhs_minimize_kernel
     __device__ void point(long long cell, const T *, T *out, Acc &) const {
         const T p = phi[cell];
-        const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
         TE e[6], sg[6];
         if (c.coupling) {
 #pragma unroll
             for (int a = 0; a < 6; ++a) { e[a] = d.eps[a][cell]; sg[a] = d.sig[a][cell]; }
         }
-        d.mge[cell] = phi_rhs_sig<T, TE>(c, ec, p, T(0), xB, e, sg);
+        if (phi_only) {
+            d.mge[cell] = phi_rhs_phi_only<T, TE>(c, ec, p, e, sg);
+        } else {
+            const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
+            d.mge[cell] = phi_rhs_sig<T, TE>(c, ec, p, T(0), xB, e, sg);
+        }
         out[0] = p;
     }
     __device__ void load_spec(long long, int, cplx_t<T> *) const {}
@@ -2354,7 +2359,7 @@ struct AccMinE {
 
 template <typename T, typename TE>
 __global__ void __launch_bounds__(256)
-k_min_energy(DevState<T, TE> d, PhysC c, ElasC<TE> ec, const T *phi, double g0, AccMinE *part) {
+k_min_energy(DevState<T, TE> d, PhysC c, ElasC<TE> ec, const T *phi, double g0, int chem, AccMinE *part) {
     AccMinE a = AccMinE::identity();
     const int Nx = d.g.Nx, Ny = d.g.Ny, Nz = d.g.Nz;
     const double idx2 = 0.5 / c.dx, idy2 = 0.5 / c.dy, idz2 = 0.5 / c.dz;
@@ -2387,11 +2392,13 @@ k_min_energy(DevState<T, TE> d, PhysC c, ElasC<TE> ec, const T *phi, double g0, 
             a.gel += 0.5 * sd;
             a.gelh += 0.5 * sd * double(h);
         }
-        const T x = clamp_eps(xm, T(1e-12));
-        T offA, offB;
-        thermo_mu_off<T>(c.tc, x, offA, offB);
-        const double mix = (1.0 - double(x)) * (c.tc.GA_s + double(offA)) + double(x) * (c.tc.GB_s + double(offB));
-        a.chem += (1.0 - double(h)) * mix + double(h) * c.mu0 - g0;
+        if (chem) {
+            const T x = clamp_eps(xm, T(1e-12));
+            T offA, offB;
+            thermo_mu_off<T>(c.tc, x, offA, offB);
+            const double mix = (1.0 - double(x)) * (c.tc.GA_s + double(offA)) + double(x) * (c.tc.GB_s + double(offB));
+            a.chem += (1.0 - double(h)) * mix + double(h) * c.mu0 - g0;
+        }
     }
     block_reduce_acc(a);
     if (threadIdx.x == 0) part[blockIdx.x] = a;
@@ -2474,7 +2481,7 @@ static pfgb_status min_gradient(pfgb_ctx *c, const DevState<T, TE> &d, const T *
     const ElasC<TE> ec = elas_consts<TE>(c);
     AxisIO<T, 1, 1> io1;
     io1.in[0] = d.S[0]; io1.out[0] = d.S[0];
-    TRY((launch_z<T, 0, 1>(c, OpMinGradZ<T, TE>{d, phys_as<T>(c->pc), ec, phi}, "z_min_grad",
+    TRY((launch_z<T, 0, 1>(c, OpMinGradZ<T, TE>{d, phys_as<T>(c->pc), ec, phi, !c->p.minimize_full_model}, "z_min_grad",
                            3.0 * Nf * sizeof(T) + (c->pc.coupling ? 12.0 : 0.0) * Nf * sizeof(TE))));
     TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
     TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpLapX<T>{d.kt, invN}, "x_lap")));
@@ -2522,7 +2529,12 @@ static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
     const pfgb_params &P = c->p;
     const double Nf = (double)c->g.N;
     const long long N = c->g.N;
-    c->pc.xbcap = c->xb_clamp ? P.minimize_xB_max_safe : 2.0;
+    // phi-only minimize (minimize_full_model = 0) carries no composition
+    // (main_cuda.cu:27208-27217): its elastic solve, stress and energies use
+    // the phi-only eigenstrain h(phi) eps00 (main_cuda.cu:28816-28824 and
+    // the NULL xB of :28920, :29303), which is the composition cap at 0
+    const bool phi_only = !P.minimize_full_model;
+    c->pc.xbcap = phi_only ? 0.0 : (c->xb_clamp ? P.minimize_xB_max_safe : 2.0);
     c->Yc_prev = c->Yc;
     pfgb_step_stats st;
     memset(&st, 0, sizeof(st));
@@ -2541,7 +2553,7 @@ static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
     const double muAr = c->pc.tc.GA_s + oA, muBf = c->pc.tc.GB_s + oB;
     const double g0 = (1.0 - xref) * muAr + xref * muBf;
     TRY((min_reduce<AccMinE>(c, "min_energy", (2.0 * Nf) * sizeof(T) + 12.0 * Nf * sizeof(TE), 42, 6,
-                             k_min_energy<T, TE>, d, c->pc, ec, (const T *)pa, g0)));
+                             k_min_energy<T, TE>, d, c->pc, ec, (const T *)pa, g0, phi_only ? 0 : 1)));
     const double *E = c->hscal + 42;
     double mean_h = E[0] / Nf;
     if (it == 1 && !(c->V0_target > 0.0)) {
@@ -2561,10 +2573,13 @@ static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
     const double F_surf = total_interface / Nf;
     const double F_el = P.elastic_enabled ? E[3] / Nf : 0.0;
     const double total_el_core = P.elastic_enabled ? E[4] : 0.0;
-    const double F_chem = E[5] / Nf;
-    const double F_total = F_chem + F_surf + F_el;
-    const double F_chem_cnt = mean_h > 0.0 ? mean_h * (P.mu0_compound - muBf) : NAN;
-    const double F_total_cnt = F_surf + F_el + F_chem_cnt;
+    // the chemical excess and the CNT summary are full-model only
+    // (main_cuda.cu:29322-29343); NaN in phi-only minimize, and so is the
+    // total, which disables the energy-plateau test there
+    const double F_chem = phi_only ? NAN : E[5] / Nf;
+    const double F_total = phi_only ? NAN : F_chem + F_surf + F_el;
+    const double F_chem_cnt = (!phi_only && mean_h > 0.0) ? mean_h * (P.mu0_compound - muBf) : NAN;
+    const double F_total_cnt = phi_only ? NAN : F_surf + F_el + F_chem_cnt;
     const double F_prev = c->prev_F_total;
     c->prev_F_total = F_total;
 
@@ -2583,8 +2598,8 @@ static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
     const double rms_res = std::sqrt(c->hscal[44] / Nf);
     const double rms_dphi = std::sqrt(c->hscal[45] / Nf) / P.dt;
 
-    // ---- Y update (full model) with phi^n = pa, phi^{n+1} = pb ----
-    {
+    // ---- Y update (full model only, main_cuda.cu:30284) with phi^n = pa, phi^{n+1} = pb ----
+    if (!phi_only) {
         DevState<T, TE> dy = d;
         dy.phi_old = pa;
         dy.phi_new = pb;
@@ -2622,19 +2637,32 @@ static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
     c->cur = cur == (T *)c->phi[0] ? 0 : 1;
 
     // ---- stopping rule (:32405-32600) and the monitor's xB clamp ----
-    TRY((min_reduce<AccSumMax>(c, "min_dy", 2.0 * Nf * sizeof(T), 48, 2, k_min_dy<T, TE>, d, phys_as<T>(c->pc), c->Yc_prev)));
-    const double rms_dY = std::sqrt(c->hscal[48] / Nf) / P.dt;
-    const double xmax = c->hscal[49];
+    // rms_dY and the xB monitor are full-model only (NaN / off in phi-only
+    // minimize, main_cuda.cu:32425-32440, 25262)
+    double rms_dY = NAN, xmax = 0.0;
+    if (!phi_only) {
+        TRY((min_reduce<AccSumMax>(c, "min_dy", 2.0 * Nf * sizeof(T), 48, 2, k_min_dy<T, TE>, d, phys_as<T>(c->pc),
+                                   c->Yc_prev)));
+        rms_dY = std::sqrt(c->hscal[48] / Nf) / P.dt;
+        xmax = c->hscal[49];
+    }
     double edr = NAN;
     if (std::isfinite(F_prev) && std::isfinite(F_total)) edr = std::fabs(F_total - F_prev) / std::fmax(std::fabs(F_prev), 1e-20);
     const double ver = c->V0_target > 1e-30 ? std::fabs(mean_h - c->V0_target) / (c->V0_target + 1e-30) : 0.0;
     const bool vol_ok = std::isfinite(ver) && ver < P.minimize_vol_err_rel_threshold;
     const bool res_ok = std::isfinite(rms_res) && rms_res < P.minimize_rms_res_threshold;
-    const int condA = std::isfinite(rms_dphi) && std::isfinite(rms_dY) && rms_dphi < P.minimize_rms_dphi_threshold &&
-                      rms_dY < P.minimize_rms_dY_threshold && res_ok && vol_ok;
-    const int condB = std::isfinite(edr) && edr < P.minimize_energy_diff_rel_threshold && std::isfinite(rms_dphi) &&
-                      std::isfinite(rms_dY) && rms_dphi < 5.0 * P.minimize_rms_dphi_threshold &&
-                      rms_dY < 5.0 * P.minimize_rms_dY_threshold && res_ok && vol_ok;
+    int condA, condB;
+    if (phi_only) {   // main_cuda.cu:32541-32550: phi convergence and the energy plateau
+        condA = std::isfinite(rms_dphi) && rms_dphi < P.minimize_rms_dphi_threshold && res_ok && vol_ok;
+        condB = std::isfinite(edr) && edr < P.minimize_energy_diff_rel_threshold && std::isfinite(rms_dphi) &&
+                rms_dphi < 5.0 * P.minimize_rms_dphi_threshold && res_ok && vol_ok;
+    } else {
+        condA = std::isfinite(rms_dphi) && std::isfinite(rms_dY) && rms_dphi < P.minimize_rms_dphi_threshold &&
+                rms_dY < P.minimize_rms_dY_threshold && res_ok && vol_ok;
+        condB = std::isfinite(edr) && edr < P.minimize_energy_diff_rel_threshold && std::isfinite(rms_dphi) &&
+                std::isfinite(rms_dY) && rms_dphi < 5.0 * P.minimize_rms_dphi_threshold &&
+                rms_dY < 5.0 * P.minimize_rms_dY_threshold && res_ok && vol_ok;
+    }
     const double pt = (double)it * P.dt;
     const bool pt_ok = std::isfinite(pt) && pt + 1e-14 >= P.minimize_min_pseudo_time;
     c->conv_count = ((condA || condB) && pt_ok) ? c->conv_count + 1 : 0;
@@ -2642,7 +2670,7 @@ static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
     // the reference clamps its stored xB when the monitor sees max xB above
     // minimize_xB_max_safe; the clamped xB is what the next iteration's
     // elastic solve and energies read (here: the cap on the elastic side)
-    const int clamped = xmax > P.minimize_xB_max_safe + 1e-12;
+    const int clamped = !phi_only && xmax > P.minimize_xB_max_safe + 1e-12;
     c->xb_clamp = clamped;
     c->step++;
     if (ms) {
@@ -2853,8 +2881,8 @@ static pfgb_status validate(const pfgb_params *p) {
         return PFGB_ERR_INVALID;
     }
     if (p->mode == PFGB_MODE_MINIMIZE) {
-        if (!p->minimize_full_model || p->model_mode != PFGB_MODEL_TWO_PHASE || p->zero_mode_enabled) {
-            pfgb_set_error_msg("minimize is built for minimize_full_model=1, two_phase, zero mode off");
+        if (p->model_mode != PFGB_MODEL_TWO_PHASE || p->zero_mode_enabled) {
+            pfgb_set_error_msg("minimize is built for two_phase with the zero mode off");
             return PFGB_ERR_UNSUPPORTED;
         }
         if (!(p->minimize_dt > 0)) {
@@ -3748,10 +3776,25 @@ static pfgb_status fft_c2r_impl(pfgb_ctx *c, cplx_t<T> *in, T *out) {
     return PFGB_OK;
 }
 
+// The line engines stage tiles with 16-byte cp.async copies from the
+// buffers' base addresses, so caller buffers must be 16-byte aligned (every
+// cudaMalloc'd pointer is).  Checked on the host before anything launches.
+static pfgb_status check_transform_buffers(const void *in, const void *out) {
+    if (!in || !out) {
+        pfgb_set_error_msg("null device buffer");
+        return PFGB_ERR_INVALID;
+    }
+    if ((((uintptr_t)in) | ((uintptr_t)out)) & 15u) {
+        pfgb_set_error_msg("transform buffers must be 16-byte aligned (in %p, out %p)", in, out);
+        return PFGB_ERR_INVALID;
+    }
+    return PFGB_OK;
+}
+
 extern "C" {
 
 pfgb_status pfgb_fft3d_r2c(int precision, int Nx, int Ny, int Nz, const void *in, void *out, void *stream) {
-    if (!in || !out) return PFGB_ERR_INVALID;
+    TRY(check_transform_buffers(in, out));
     pfgb_ctx c;
     pfgb_status s = fft_ctx_init(&c, Nx, Ny, Nz, stream);
     if (s == PFGB_OK)
@@ -3763,7 +3806,7 @@ pfgb_status pfgb_fft3d_r2c(int precision, int Nx, int Ny, int Nz, const void *in
 
 // The half-spectrum input is used as workspace and is overwritten.
 pfgb_status pfgb_fft3d_c2r(int precision, int Nx, int Ny, int Nz, const void *in, void *out, void *stream) {
-    if (!in || !out) return PFGB_ERR_INVALID;
+    TRY(check_transform_buffers(in, out));
     pfgb_ctx c;
     pfgb_status s = fft_ctx_init(&c, Nx, Ny, Nz, stream);
     if (s == PFGB_OK)
@@ -3858,10 +3901,7 @@ static pfgb_status fft_r2c_noalloc(int Nx, int Ny, int Nz, const T *in, cplx_t<T
 extern "C" {
 
 pfgb_status pfgb_fft3d_r2c_noalloc(int precision, int Nx, int Ny, int Nz, const void *in, void *out, void *stream) {
-    if (!in || !out) {
-        pfgb_set_error_msg("null device buffer");
-        return PFGB_ERR_INVALID;
-    }
+    TRY(check_transform_buffers(in, out));
     if (precision != PFGB_PREC_FP64 && precision != PFGB_PREC_FP32) {
         pfgb_set_error_msg("precision %d is neither PFGB_PREC_FP64 nor PFGB_PREC_FP32", precision);
         return PFGB_ERR_INVALID;

@@ -249,20 +249,30 @@ Cli parse(int argc, char **argv) {
     return c;
 }
 
-bool read_raw(const std::string &path, size_t n, std::vector<double> *out) {
+// A raw field of n values in C order, float64 or float32 (read_raw_field_to_double,
+// main_cuda.cu:2764-2799: the size must match exactly), widened to double.
+bool read_raw(const std::string &path, size_t n, std::vector<double> *out, bool f32 = false) {
+    const size_t esz = f32 ? sizeof(float) : sizeof(double);
     FILE *f = fopen(path.c_str(), "rb");
     if (!f) { fprintf(stderr, "[fatal] cannot open raw field %s\n", path.c_str()); return false; }
     fseek(f, 0, SEEK_END);
     const long sz = ftell(f);
     fseek(f, 0, SEEK_SET);
-    if (sz != (long)(n * sizeof(double))) {
-        fprintf(stderr, "[fatal] raw field %s has %ld bytes, expected %zu (float64 x %zu)\n", path.c_str(), sz,
-                n * sizeof(double), n);
+    if (sz != (long)(n * esz)) {
+        fprintf(stderr, "[fatal] raw field %s has %ld bytes, expected %zu (%s x %zu)\n", path.c_str(), sz, n * esz,
+                f32 ? "float32" : "float64", n);
         fclose(f);
         return false;
     }
     out->resize(n);
-    const size_t got = fread(out->data(), sizeof(double), n, f);
+    size_t got;
+    if (f32) {
+        std::vector<float> tmp(n);
+        got = fread(tmp.data(), sizeof(float), n, f);
+        for (size_t i = 0; i < n; ++i) (*out)[i] = tmp[i];
+    } else {
+        got = fread(out->data(), sizeof(double), n, f);
+    }
     fclose(f);
     if (got != n) { fprintf(stderr, "[fatal] short read of %s\n", path.c_str()); return false; }
     return true;
@@ -291,6 +301,21 @@ bool json_number(const std::string &txt, const char *key, double *v) {
     const double x = strtod(s, &e);
     if (e == s) return false;
     *v = x;
+    return true;
+}
+
+// string after "key": in a flat JSON text; false if absent
+bool json_string(const std::string &txt, const char *key, std::string *v) {
+    const std::string k = std::string("\"") + key + "\"";
+    size_t p = txt.find(k);
+    if (p == std::string::npos) return false;
+    p = txt.find(':', p + k.size());
+    if (p == std::string::npos) return false;
+    const size_t q0 = txt.find('"', p + 1);
+    if (q0 == std::string::npos) return false;
+    const size_t q1 = txt.find('"', q0 + 1);
+    if (q1 == std::string::npos) return false;
+    *v = txt.substr(q0 + 1, q1 - q0 - 1);
     return true;
 }
 
@@ -404,8 +429,13 @@ int main(int argc, char **argv) {
         fprintf(stderr, "[fatal] --pf-param-file <path> is required (complete physical PF inputs).\n");
         return 2;
     }
+    // dynamics-continue is the dynamics run under another name
+    // (main_cuda.cu:22752-22763); its raw-field / checkpoint inputs are the
+    // ordinary ones
+    if (c.mode == "dynamics-continue") c.mode = "dynamics";
     if (c.mode != "dynamics" && c.mode != "minimize") {
-        fprintf(stderr, "[fatal] --mode=%s is not available in this build (dynamics, minimize)\n", c.mode.c_str());
+        fprintf(stderr, "[fatal] --mode=%s is not available in this build (dynamics, dynamics-continue, minimize)\n",
+                c.mode.c_str());
         return 2;
     }
     const bool minimize = c.mode == "minimize";
@@ -464,6 +494,13 @@ int main(int argc, char **argv) {
     for (const auto &kv : c.param_sets)
         if (pfgb_params_set(&P, kv.first.c_str(), kv.second.c_str()) != PFGB_OK) bad(kv.first.c_str(), kv.second.c_str());
     if (c.tilt_given && (P.init_tilt_theta_deg != 0.0 || P.init_tilt_phi_deg != 0.0)) P.init_use_rotation = 1;
+    // the zero mode is a dynamics-only two-phase mode (main_cuda.cu:24662-24690);
+    // the library also runs it with gp_zone, the drop-in driver refuses it
+    if (P.zero_mode_enabled && (minimize || P.model_mode == PFGB_MODEL_GP_ZONE)) {
+        fprintf(stderr, "[fatal] PF_CONSERVED_Y_ZERO_MODE_V1 is a dynamics-only PF mode and requires every GP, "
+                        "RSMD, scheduled-source, and bridge path OFF\n");
+        return 2;
+    }
     if (std::isfinite(c.radius_nm)) {   // main_cuda.cu:25288-25310: physical radius -> code units
         const double dxp = P.ic_phi_iface_w > 1e-30 ? P.lambda_sm_m / (2.0 * P.ic_phi_iface_w) : P.dx * 1e-9;
         const double u2m = std::fabs(P.dx) > 1e-30 ? dxp / P.dx : 1e-9;
@@ -513,14 +550,21 @@ int main(int argc, char **argv) {
         fprintf(stderr, "[fatal] raw_fields needs --init-phi-raw and --init-xB-raw\n");
         return 2;
     }
+    if (!restarting && !seeded && minimize && !P.minimize_full_model) {
+        fprintf(stderr, "[fatal] --init-mode raw_fields requires dynamics mode or full-model minimize "
+                        "(--mode=minimize --minimize-full-model).\n");
+        return 2;
+    }
     if (!restarting && !seeded) {
-        if (!read_raw(c.init_phi, N, &phi) || !read_raw(c.init_xB, N, &xB)) return 2;
-        if (!c.init_eta.empty() && !read_raw(c.init_eta, N, &eta)) return 2;
-        if (!c.init_dYdt.empty() && !read_raw(c.init_dYdt, N, &dYdt)) return 2;
-        double xB_max_safe = 0.07;   // reference default when init_meta.json does not set it
+        // init_meta.json (load_raw_init_meta, main_cuda.cu:2733-2762): the
+        // grid must match, order must be C, dtype is float32 (the default)
+        // or float64, and xB_max_safe caps xB (the minimize monitor cap when
+        // absent).  Without --init-meta the fields are read as float64.
+        double xB_max_safe = P.minimize_xB_max_safe;
+        bool f32 = false;
         if (!c.init_meta.empty()) {
             const std::string meta = slurp(c.init_meta);
-            if (meta.empty()) { fprintf(stderr, "[fatal] cannot read %s\n", c.init_meta.c_str()); return 2; }
+            if (meta.empty()) { fprintf(stderr, "[fatal] cannot read raw init meta: %s\n", c.init_meta.c_str()); return 2; }
             double v;
             if (json_number(meta, "xB_max_safe", &v)) xB_max_safe = v;
             const char *dims[3] = {"Nx", "Ny", "Nz"};
@@ -530,7 +574,22 @@ int main(int argc, char **argv) {
                     fprintf(stderr, "[fatal] init_meta %s=%d does not match the grid (%d)\n", dims[a], (int)v, have[a]);
                     return 2;
                 }
+            std::string dtype = "float32", order = "C";
+            json_string(meta, "dtype", &dtype);
+            json_string(meta, "order", &order);
+            if (order != "C") {
+                fprintf(stderr, "[fatal] raw init order mismatch: meta order='%s', only C is supported\n", order.c_str());
+                return 2;
+            }
+            if (dtype != "float32" && dtype != "float64") {
+                fprintf(stderr, "[fatal] unsupported raw dtype '%s'; use float32 or float64\n", dtype.c_str());
+                return 2;
+            }
+            f32 = dtype == "float32";
         }
+        if (!read_raw(c.init_phi, N, &phi, f32) || !read_raw(c.init_xB, N, &xB, f32)) return 2;
+        if (!c.init_eta.empty() && !read_raw(c.init_eta, N, &eta, f32)) return 2;
+        if (!c.init_dYdt.empty() && !read_raw(c.init_dYdt, N, &dYdt, f32)) return 2;
         st = pfgb_prepare_raw_fields(&P, xB_max_safe, phi.data(), xB.data(), eta.empty() ? nullptr : eta.data(),
                                      dYdt.empty() ? nullptr : dYdt.data(), N);
         if (st != PFGB_OK) return fail(st, "pfgb_prepare_raw_fields");
@@ -601,6 +660,16 @@ int main(int argc, char **argv) {
         printf("PF_ZERO_MODE_RESTART checkpoint=%s accepted_step=%d\n", c.restart_from.c_str(), s0.step);
     } else if (seeded) {
         if ((st = pfgb_init_fields(ctx)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_init_fields"); }
+        if (minimize && !P.minimize_full_model) {
+            // phi-only minimize starts from the seeded phi with no composition
+            // (initialize_phi_only_cuda and the zeroed xB / Y, main_cuda.cu:27208-27217)
+            std::vector<double> p0(N), x0(N, 0.0);
+            if ((st = pfgb_read_fields(ctx, p0.data(), nullptr, nullptr, nullptr, nullptr)) != PFGB_OK ||
+                (st = pfgb_load_fields(ctx, p0.data(), x0.data(), nullptr, nullptr)) != PFGB_OK) {
+                pfgb_destroy(ctx);
+                return fail(st, "phi-only minimize initial fields");
+            }
+        }
     } else {
         st = pfgb_load_fields(ctx, phi.data(), xB.data(), eta.empty() ? nullptr : eta.data(),
                               dYdt.empty() ? nullptr : dYdt.data());
@@ -688,11 +757,21 @@ int main(int argc, char **argv) {
     };
 
     if ((st = read_state()) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_read_fields"); }
-    if (minimize) {   // minimize writes init / final fields only, with the case tag
+    // initial files (main_cuda.cu:27475-27530): minimize writes phi (and, in
+    // the full model, xB) with the case tag; dynamics writes xBtot_0 (and
+    // xBtot_gp_init in gp_zone), phi_init, eta_init (gp_zone) and xB_0
+    if (minimize) {
         write_vtk(case_dir + "/phi_init_" + tag + ".vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
-        write_vtk(case_dir + "/xB_init_" + tag + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
+        if (P.minimize_full_model) write_vtk(case_dir + "/xB_init_" + tag + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
     } else {
-        vtk_set("_init", 0);
+        for (size_t i = 0; i < N; ++i) {
+            const double h = h_of(f_phi[i]);
+            f_xBtot[i] = (1.0 - h) * f_xB[i] + h * P.v_B;
+        }
+        write_vtk(case_dir + "/xBtot_0.vtk", "xB_tot", f_xBtot, P.Nx, P.Ny, P.Nz);
+        if (gp) write_vtk(case_dir + "/xBtot_gp_init.vtk", "xBtot_gp", f_xBtot, P.Nx, P.Ny, P.Nz);
+        write_vtk(case_dir + "/phi_init.vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
+        if (gp) write_vtk(case_dir + "/eta_init.vtk", "eta", f_eta, P.Nx, P.Ny, P.Nz);
         write_vtk(case_dir + "/xB_0.vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
     }
     if ((st = csv_row(0, NAN)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_diagnostics"); }
@@ -767,11 +846,15 @@ int main(int argc, char **argv) {
     const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (rc == 0) {
         if ((st = read_state()) != PFGB_OK) rc = fail(st, "pfgb_read_fields");
-        else if (minimize) {
-            write_vtk(case_dir + "/phi_final_" + tag + ".vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
-            write_vtk(case_dir + "/xB_final_" + tag + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
-        } else {
-            vtk_set("_final", c.nsteps);
+        else if (minimize) {   // main_cuda.cu:33635-33665
+            write_vtk(case_dir + "/phi_final_" + tag + ".vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz, c.nsteps);
+            if (P.minimize_full_model)
+                write_vtk(case_dir + "/xB_final_" + tag + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz, c.nsteps);
+        } else if (c.nsteps % c.out_every != 0) {
+            // the last step off the output schedule, numbered nsteps / out_every + 1
+            // (main_cuda.cu:33815-33840)
+            const int os = c.nsteps / c.out_every + 1;
+            vtk_set(("_" + std::to_string(os)).c_str(), os);
         }
     }
     if (csv) fclose(csv);

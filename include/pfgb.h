@@ -410,7 +410,11 @@ int         pfgb_profile_read(pfgb_ctx *ctx, const char **names, double *ms, dou
 
 /* --- standalone 3D transforms on DEVICE buffers (test / tooling) ------ */
 /* precision: PFGB_PREC_FP64 (double in, double2 out) or PFGB_PREC_FP32.
- * Unnormalised, same conventions as cuFFT D2Z/Z2D (R2C/C2R).             */
+ * Unnormalised, same conventions as cuFFT D2Z/Z2D (R2C/C2R).  Both
+ * buffers must start on a 16-byte boundary (any cudaMalloc'd pointer
+ * does): the line engines copy tiles in 16-byte units.  A misaligned
+ * buffer gets PFGB_ERR_INVALID before anything is launched (this also
+ * holds for pfgb_fft3d_r2c_noalloc).                                       */
 pfgb_status pfgb_fft3d_r2c(int precision, int Nx, int Ny, int Nz,
                            const void *d_in, void *d_out, void *cuda_stream);
 pfgb_status pfgb_fft3d_c2r(int precision, int Nx, int Ny, int Nz,

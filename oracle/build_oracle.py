@@ -1,7 +1,11 @@
 """Build recipe for the CPU oracle (test infrastructure, not the product).
 
-    python oracle/build_oracle.py          # -> oracle/_build/libpforacle.so
-    python oracle/build_oracle.py --ref    # also oracle/_ref/libpfref.so, libpfckpt.so
+    python oracle/build_oracle.py            # -> oracle/_build/libpforacle.so
+    python oracle/build_oracle.py --ref      # also oracle/_ref/libpfref.so, libpfckpt.so, librefk.so
+    python oracle/build_oracle.py --ref-main # stage the reference main_cuda sources and build it
+
+The reference tree is $PFGB_REFERENCE_TREE, or else the checkout named
+``reference`` beside this repository.
 
 The oracle is plain C99 + OpenMP.  FP contraction is disabled so x86 and
 aarch64 builds give the same roundings.  ``--ref`` compiles the reference's
@@ -28,7 +32,19 @@ CKPT_LIB = os.path.join(REF_OUT, "libpfckpt.so")
 KERN_LIB = os.path.join(REF_OUT, "librefk.so")
 KERN_SECTION = os.path.join(REF_OUT, "ref_kernels_section.inc")
 CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
-REFERENCE_TREE = "/root/reference"
+REFERENCE_TREE = os.environ.get("PFGB_REFERENCE_TREE") or os.path.normpath(
+    os.path.join(HERE, "..", "..", "reference"))
+# The reference's own GPU program, rebuilt for sm_103a as the whole-step
+# oracle.  Its sources are staged (copied unchanged, git-ignored) into
+# oracle/_ref/main_src/ where the reference tree is present, so that a
+# machine without the tree (the GPU host) can still build it; the binary is
+# named for the host architecture because it is rebuilt on each machine.
+REF_MAIN_SOURCES = ["main_cuda.cu", "cuda_kernels.cu", "cuda_common.cu", "pf_zero_mode_checkpoint.cpp"]
+REF_MAIN_HEADERS = ["cuda_common.h", "cuda_kernels.h", "pf_params.h", "phase_functions.h", "thermo_utils.h",
+                    "io_vtk_cuda.h", "pf_zero_mode_checkpoint.h"]
+REF_MAIN_SRC = os.path.join(REF_OUT, "main_src")
+REF_MAIN_BIN = os.path.join(REF_OUT, "main_cuda_ref." + os.uname().machine)
+NVCC = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
 
 CFLAGS = ["-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
           "-fno-fast-math", "-Wall", "-Wno-unused-function"]
@@ -141,9 +157,47 @@ def build_ref_kernels(force: bool = False) -> str | None:
     return KERN_LIB
 
 
+def stage_ref_main() -> str | None:
+    """Copy the reference main_cuda's source files, unchanged, into
+    oracle/_ref/main_src/ (git-ignored).  Only where the reference tree is
+    present; returns the staging directory, or None."""
+    import shutil
+    if not all(os.path.exists(os.path.join(REFERENCE_TREE, f)) for f in REF_MAIN_SOURCES + REF_MAIN_HEADERS):
+        return None
+    os.makedirs(REF_MAIN_SRC, exist_ok=True)
+    for f in REF_MAIN_SOURCES + REF_MAIN_HEADERS:
+        src, dst = os.path.join(REFERENCE_TREE, f), os.path.join(REF_MAIN_SRC, f)
+        if _stale(dst, [src]):
+            shutil.copyfile(src, dst + ".tmp")
+            os.replace(dst + ".tmp", dst)
+    return REF_MAIN_SRC
+
+
+def build_ref_main(force: bool = False) -> str | None:
+    """Build the reference main_cuda for sm_103a from the staged sources:
+    nvcc on its four translation units with the flags of its Makefile
+    (-O3 -std=c++14 --expt-relaxed-constexpr) and CUDA_ARCH=sm_103a, linked
+    with cuFFT.  Returns the binary, or None when no staged sources exist
+    (no reference tree here and none staged before)."""
+    stage_ref_main()
+    srcs = [os.path.join(REF_MAIN_SRC, f) for f in REF_MAIN_SOURCES]
+    if not all(os.path.exists(f) for f in srcs) or not os.path.exists(NVCC):
+        return None
+    hdrs = [os.path.join(REF_MAIN_SRC, f) for f in REF_MAIN_HEADERS]
+    if force or _stale(REF_MAIN_BIN, srcs + hdrs):
+        tmp = REF_MAIN_BIN + ".tmp"
+        subprocess.run([NVCC, "-arch=sm_103a", "-O3", "-std=c++14", "--expt-relaxed-constexpr",
+                        "-Xcompiler", "-Wno-format-truncation", "-w", "-o", tmp, *srcs, "-lcufft", "-lcudart", "-lm"],
+                       check=True, cwd=REF_MAIN_SRC, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
+        os.replace(tmp, REF_MAIN_BIN)
+    return REF_MAIN_BIN
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     if "--ref" in sys.argv:
         print(build_ref(force="--force" in sys.argv))
         print(build_ref_checkpoint(force="--force" in sys.argv))
         print(build_ref_kernels(force="--force" in sys.argv))
+    if "--ref-main" in sys.argv:
+        print(build_ref_main(force="--force" in sys.argv))

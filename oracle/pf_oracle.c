@@ -895,6 +895,36 @@ static void phi_rhs(pfo_state *s, int coupling) {
     RLOOP_END
 }
 
+/* phi-only minimize drive (compute_phi_rhs_minimize_kernel,
+ * cuda_kernels.cu:6298-6374): double well and the elastic terms with the
+ * phi-only eigenstrain h(phi) eps00 (eigenstrain_phi_only_point,
+ * cuda_kernels.cu:363-384, float eps00, stored as float); no chemistry */
+static void phi_rhs_phi_only(pfo_state *s) {
+    const pfgb_params *P = &s->p;
+    double e00f[6];
+    for (int c = 0; c < 6; ++c) e00f[c] = rf(s, P->eps00[c]);
+    RLOOP_BEGIN(s)
+        const double phi = s->phi[idx];
+        double f = P->W * o_gp(phi);
+        if (P->elastic_enabled) {
+            const double hp = o_hp(phi), h = o_h(phi);
+            double de[6], e0[6], el[6], ev[6];
+            for (int c = 0; c < 6; ++c) de[c] = hp * P->eps00[c];
+            const double dg = -(s->sig_r[0][idx] * de[0] + s->sig_r[1][idx] * de[1] + s->sig_r[2][idx] * de[2] +
+                                2.0 * (s->sig_r[5][idx] * de[5] + s->sig_r[4][idx] * de[4] +
+                                       s->sig_r[3][idx] * de[3]));
+            for (int c = 0; c < 6; ++c) e0[c] = rf(s, h * e00f[c]);
+            for (int c = 0; c < 6; ++c) el[c] = s->eps_r[c][idx] - e0[c];
+            eng(el, ev);
+            double Q = 0.0;   /* compute_Q_voigt, :162-181 */
+            for (int a = 0; a < 6; ++a)
+                for (int b = 0; b < 6; ++b) Q += voigt(P->S_p, a + 1, b + 1) * ev[a] * ev[b];
+            f += dg + 0.5 * hp * Q;
+        }
+        s->rhs[idx] = f;
+    RLOOP_END
+}
+
 /* compute_eta_rhs_kernel (non-raw-drive branch), cuda_kernels.cu:845-946 */
 static void eta_rhs(pfo_state *s) {
     const pfgb_params *P = &s->p;
@@ -1497,7 +1527,8 @@ static double effective_vf_target(const pfgb_params *P) {
  * phi_k is left holding the dealiased transform of phi */
 static void phi_gradient(pfo_state *s, int coupling) {
     fwd(s, s->phi, s->phi_k); dealias(s, s->phi_k);
-    phi_rhs(s, coupling);
+    if (s->p.minimize_full_model) phi_rhs(s, coupling);
+    else phi_rhs_phi_only(s);   /* main_cuda.cu:29414-29429 */
     phi_laplacian(s, s->mlap);
     const double kap = s->p.kappa_phi;
     RLOOP_BEGIN(s) s->mg[idx] = s->rhs[idx] - kap * s->mlap[idx]; RLOOP_END
@@ -1526,6 +1557,13 @@ static int minimize_iter(pfo_state *s, pfgb_min_stats *ms) {
     memcpy(s->eta_prev, s->eta, sizeof(double) * s->N);
     memcpy(s->Y_n, s->Y, sizeof(double) * s->N);
     const int coupling = P->elastic_enabled;
+    /* phi-only minimize (minimize_full_model = 0) carries no composition:
+     * xB and Y stay zero (main_cuda.cu:27208-27217), so the eigenstrain of
+     * the elastic solve and the energies is h(phi) eps00 (the phi-only
+     * eigenstrain, main_cuda.cu:28816-28824 and the NULL xB of
+     * :28920, :29303) */
+    const int phi_only = !P->minimize_full_model;
+    if (phi_only) memset(s->xB, 0, sizeof(double) * s->N);
     pfgb_step_stats st;
     memset(&st, 0, sizeof(st));
     if (P->elastic_enabled) {
@@ -1587,11 +1625,14 @@ static int minimize_iter(pfo_state *s, pfgb_min_stats *ms) {
         const double mix = (1.0 - x) * o_muA(x, T, sc, cv) + x * o_muB(x, T, sc, cv);
         s->mass_t[idx] = (1.0 - h) * mix + h * P->mu0_compound - g0;
     RLOOP_END
-    const double F_chem = dsum(s->mass_t, s->N) / (double)s->N;
-    const double F_total = F_chem + F_surf + F_el;
+    /* the chemical excess and the CNT summary are full-model only
+     * (main_cuda.cu:29322-29343); in phi-only minimize they stay NaN and so
+     * does the total, which disables the energy-plateau test */
+    const double F_chem = phi_only ? NAN : dsum(s->mass_t, s->N) / (double)s->N;
+    const double F_total = phi_only ? NAN : F_chem + F_surf + F_el;
     const double muBf = o_muB(xref, T, sc, cv);
-    const double F_chem_cnt = mean_h > 0.0 ? mean_h * (P->mu0_compound - muBf) : NAN;
-    const double F_total_cnt = F_surf + F_el + F_chem_cnt;
+    const double F_chem_cnt = (!phi_only && mean_h > 0.0) ? mean_h * (P->mu0_compound - muBf) : NAN;
+    const double F_total_cnt = phi_only ? NAN : F_surf + F_el + F_chem_cnt;
     const double F_prev = s->prev_F_total;
     s->prev_F_total = F_total;
 
@@ -1599,7 +1640,9 @@ static int minimize_iter(pfo_state *s, pfgb_min_stats *ms) {
     double eta_r = P->eta_lambda_vol;
     if (eta_r < 0.0) eta_r = 0.0;
     if (eta_r > 1.0) eta_r = 1.0;
-    RLOOP_BEGIN(s) s->xB[idx] = o_sigmoid(s->Y[idx], P->Y_clip, P->xB_eps); RLOOP_END   /* compute_mu_x_kernel */
+    if (!phi_only) {
+        RLOOP_BEGIN(s) s->xB[idx] = o_sigmoid(s->Y[idx], P->Y_clip, P->xB_eps); RLOOP_END   /* compute_mu_x_kernel */
+    }
     phi_gradient(s, coupling);
     s->lambda_vol = (1.0 - eta_r) * s->lambda_vol + eta_r * volume_lambda(s, s->mg);
     phi_constrained_step(s, s->lambda_vol, dt);
@@ -1619,9 +1662,11 @@ static int minimize_iter(pfo_state *s, pfgb_min_stats *ms) {
     RLOOP_BEGIN(s) { const double d = s->phi[idx] - s->phi_n[idx]; s->mass_t[idx] = d * d; } RLOOP_END
     const double rms_dphi = sqrt(dsum(s->mass_t, s->N) / (double)s->N) / dt;
 
-    /* ---- Y update (full model) ---- */
-    int rc = y_update(s, &st, dt);
-    if (rc != PFGB_OK) return rc;
+    /* ---- Y update (full model only, main_cuda.cu:30284) ---- */
+    if (!phi_only) {
+        int rc = y_update(s, &st, dt);
+        if (rc != PFGB_OK) return rc;
+    }
 
     /* ---- post-projection substeps, elastic frozen, eta = 1 ---- */
     for (int k = 0; k < P->minimize_post_projection_iters; ++k) {
@@ -1650,25 +1695,37 @@ static int minimize_iter(pfo_state *s, pfgb_min_stats *ms) {
     double edr = NAN;
     if (isfinite(F_prev) && isfinite(F_total)) edr = fabs(F_total - F_prev) / fmax(fabs(F_prev), 1e-20);
     const double ver = s->V0_target > 1e-30 ? fabs(mean_h - s->V0_target) / (s->V0_target + 1e-30) : 0.0;
-    RLOOP_BEGIN(s) { const double d = s->Y[idx] - s->Y_n[idx]; s->mass_t[idx] = d * d; } RLOOP_END
-    const double rms_dY = sqrt(dsum(s->mass_t, s->N) / (double)s->N) / dt;
+    /* rms_dY is a full-model column (NaN in phi-only minimize, :32425-32440) */
+    double rms_dY = NAN;
+    if (!phi_only) {
+        RLOOP_BEGIN(s) { const double d = s->Y[idx] - s->Y_n[idx]; s->mass_t[idx] = d * d; } RLOOP_END
+        rms_dY = sqrt(dsum(s->mass_t, s->N) / (double)s->N) / dt;
+    }
     const int vol_ok = isfinite(ver) && ver < P->minimize_vol_err_rel_threshold;
     const int res_ok = isfinite(rms_res) && rms_res < P->minimize_rms_res_threshold;
-    const int condA = isfinite(rms_dphi) && isfinite(rms_dY) && rms_dphi < P->minimize_rms_dphi_threshold &&
-                      rms_dY < P->minimize_rms_dY_threshold && res_ok && vol_ok;
-    const int condB = isfinite(edr) && edr < P->minimize_energy_diff_rel_threshold && isfinite(rms_dphi) &&
-                      isfinite(rms_dY) && rms_dphi < 5.0 * P->minimize_rms_dphi_threshold &&
-                      rms_dY < 5.0 * P->minimize_rms_dY_threshold && res_ok && vol_ok;
+    int condA, condB;
+    if (phi_only) {   /* :32541-32550: phi convergence and the energy plateau */
+        condA = isfinite(rms_dphi) && rms_dphi < P->minimize_rms_dphi_threshold && res_ok && vol_ok;
+        condB = isfinite(edr) && edr < P->minimize_energy_diff_rel_threshold && isfinite(rms_dphi) &&
+                rms_dphi < 5.0 * P->minimize_rms_dphi_threshold && res_ok && vol_ok;
+    } else {
+        condA = isfinite(rms_dphi) && isfinite(rms_dY) && rms_dphi < P->minimize_rms_dphi_threshold &&
+                rms_dY < P->minimize_rms_dY_threshold && res_ok && vol_ok;
+        condB = isfinite(edr) && edr < P->minimize_energy_diff_rel_threshold && isfinite(rms_dphi) &&
+                isfinite(rms_dY) && rms_dphi < 5.0 * P->minimize_rms_dphi_threshold &&
+                rms_dY < 5.0 * P->minimize_rms_dY_threshold && res_ok && vol_ok;
+    }
     const double pt = (double)it * dt;
     const int pt_ok = isfinite(pt) && pt + 1e-14 >= P->minimize_min_pseudo_time;
     s->conv_count = ((condA || condB) && pt_ok) ? s->conv_count + 1 : 0;
     if (s->conv_count >= P->minimize_convergence_steps && !s->converged_iter) s->converged_iter = it;
 
-    /* ---- xB safety clamp of the monitor step (every iteration here) ---- */
+    /* ---- xB safety clamp of the monitor step (every iteration here;
+     *      full model only, main_cuda.cu:25262) ---- */
     double xmax = -1e300;
     for (size_t i = 0; i < s->N; ++i) if (s->xB[i] > xmax) xmax = s->xB[i];
     int clamped = 0;
-    if (xmax > P->minimize_xB_max_safe + 1e-12) {   /* launch_clamp_xB_max_kernel */
+    if (!phi_only && xmax > P->minimize_xB_max_safe + 1e-12) {   /* launch_clamp_xB_max_kernel */
         clamped = 1;
         RLOOP_BEGIN(s) if (s->xB[idx] > P->minimize_xB_max_safe) s->xB[idx] = P->minimize_xB_max_safe; RLOOP_END
     }
@@ -1694,7 +1751,7 @@ static int minimize_iter(pfo_state *s, pfgb_min_stats *ms) {
 
 int pfo_minimize(pfo_state *s, int max_iter, int stop_on_convergence, pfgb_min_stats *ms) {
     const pfgb_params *P = &s->p;
-    if (P->mode != PFGB_MODE_MINIMIZE || !P->minimize_full_model || s->gp || P->zero_mode_enabled)
+    if (P->mode != PFGB_MODE_MINIMIZE || s->gp || P->zero_mode_enabled)
         return PFGB_ERR_UNSUPPORTED;
     for (int i = 0; i < max_iter; ++i) {
         int rc = minimize_iter(s, ms);

@@ -29,7 +29,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.abspath(os.path.join(HERE, "..", ".."))
-REFERENCE_TREE = "/root/reference"
+REFERENCE_TREE = os.environ.get("PFGB_REFERENCE_TREE") or os.path.normpath(
+    os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "..", "reference"))
 
 
 def cubic(c11: float, c12: float, c44: float) -> list[list[float]]:

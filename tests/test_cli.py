@@ -106,8 +106,11 @@ def test_cli_dynamics_run_matches_library(capi, tmp_path):
     case = tmp_path / "R" / runs[0] / "raw_fields_relax"
     for f in ("pf_input.params", "vf_precip_vs_time_raw_fields_relax.csv", "elastic_solver_trace.csv",
               "pf_zero_mode_trace.csv", "performance_summary.json", "summary.txt", "phi_init.vtk", "phi_2.vtk",
-              "phi_4.vtk", "phi_final.vtk", "xB_0.vtk", "xBtot_final.vtk"):
+              "phi_4.vtk", "xB_0.vtk", "xBtot_0.vtk", "xBtot_4.vtk"):
         assert (case / f).exists(), f
+    # dynamics writes no *_final files (main_cuda.cu:33815-33840: only a last
+    # step off the out_every schedule gets its own set)
+    assert not any("_final" in f for f in os.listdir(case))
     rows = (case / "vf_precip_vs_time_raw_fields_relax.csv").read_text().strip().split("\n")
     assert rows[0] == "step,t_code,t_real_s,vf_precip,R_avg" and len(rows) == steps + 2
     assert len((case / "elastic_solver_trace.csv").read_text().strip().split("\n")) == steps + 1
@@ -124,7 +127,7 @@ def test_cli_dynamics_run_matches_library(capi, tmp_path):
     last = rows[-1].split(",")
     assert int(last[0]) == steps
     assert abs(float(last[3]) - d.vf_precip) <= 1e-7 * max(1e-12, d.vf_precip)
-    got = _vtk_values(case / "phi_final.vtk", (n, n, n))
+    got = _vtk_values(case / "phi_4.vtk", (n, n, n))
     assert np.abs(got - f["phi"]).max() <= 6e-6
 
 
@@ -253,15 +256,17 @@ def test_cli_output_formats(capi, tmp_path):
         assert r.returncode == 0, r.stderr
         run = os.listdir(tmp_path / fmt)[0]
         dirs[fmt] = tmp_path / fmt / run / "raw_fields_relax"
-    raw = np.fromfile(dirs["raw"] / "phi_final.raw", dtype=np.float64).reshape(n, n, n)
-    blob = (dirs["vtk-binary"] / "phi_final.vtk").read_bytes()
+    # 2 steps with out_every 10: the last step is written as output number
+    # 2 // 10 + 1 = 1 (main_cuda.cu:33815-33840)
+    raw = np.fromfile(dirs["raw"] / "phi_1.raw", dtype=np.float64).reshape(n, n, n)
+    blob = (dirs["vtk-binary"] / "phi_1.vtk").read_bytes()
     head = b"LOOKUP_TABLE default\n"
     data = np.frombuffer(blob[blob.index(head) + len(head):][:8 * n ** 3], dtype=">f8")
     assert blob[blob.index(b"Simulation\n") + 11:].startswith(b"BINARY\n")
     assert np.array_equal(data.reshape(n, n, n).transpose(2, 1, 0), raw)   # z outer, x inner
-    asc = _vtk_values(dirs["vtk"] / "phi_final.vtk", (n, n, n))
+    asc = _vtk_values(dirs["vtk"] / "phi_1.vtk", (n, n, n))
     assert np.abs(asc - raw).max() <= 5.1e-6
-    assert (dirs["raw"] / "xBtot_final.raw").exists() and not (dirs["raw"] / "phi_final.vtk").exists()
+    assert (dirs["raw"] / "xBtot_1.raw").exists() and not (dirs["raw"] / "phi_1.vtk").exists()
     r = _run(capi, base, tmp_path, env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "S"), "CUDA_STO_SUPPRESS_VTK_OUTPUT": "1"})
     assert r.returncode == 0 and "VTK_OUTPUT_SUPPRESSED field=phi" in r.stdout
     run = os.listdir(tmp_path / "S")[0]

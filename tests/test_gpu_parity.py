@@ -175,6 +175,53 @@ def test_parity_246_axes(capi, oracle, shape, prec):
     assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1
 
 
+@pytest.mark.parametrize("shape", SHAPES_246, ids=["x246", "y246", "z246", "xy246"])
+def test_bench_configuration_246_axes(capi, oracle, shape):
+    """The elastic configuration the benchmark times, on the 6 x 41 engine:
+    FP32 fields, gp_zone, zero mode, heterogeneous S_p, tolerance 1e-8
+    without the fail-closed rule, the Chebyshev semi-iteration of the
+    increment and the extrapolated warm start (bench.py make_params).  Six
+    steps against the oracle doing the same, step by step: iterations within
+    one, every warm step converged below 1e-8 on both sides (a warm step at
+    the cap fails), fields within the FP32 tolerance."""
+    from cuda_sto_pf_gb300.solver import Solver
+    p = params_for(capi, "c2.params", n=16, zero_mode_enabled=1, model_mode=1, precision=1,
+                   elastic_residual_tolerance=1e-8, elastic_fail_on_nonconvergence=0, elastic_chebyshev=1,
+                   elastic_warm_start_extrapolate=1)
+    p.Nx, p.Ny, p.Nz = shape
+    phi, xB, eta = _inputs(capi, p, 16, True, seed=23, shape=shape)
+    o = oracle(p, threads=8)
+    o.load(phi, xB, eta)
+    so = capi.StepStats()
+    with Solver(p) as s:
+        s.load(phi, xB, eta)
+        for k in range(6):
+            assert o.step(1, so) == 0
+            sg = s.step(1)
+            # the cold first step: its increment is most of u, and with FP32
+            # elastic fields the residual approaches its noise floor near
+            # 1e-8 where the oracle's float64 transforms converge sooner (as
+            # in test_chebyshev_iteration_parity); the warm steps -- the ones
+            # the benchmark times -- converge and are compared
+            if k == 0:
+                continue
+            assert sg.elastic_converged == 1 and so.elastic_converged == 1, (k, sg.elastic_iterations)
+            assert sg.elastic_iterations < p.elastic_iter_max, k
+            assert sg.elastic_relative_residual <= 1e-8, (k, sg.elastic_relative_residual)
+            assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1, (k, sg.elastic_iterations,
+                                                                              so.elastic_iterations)
+        fg = s.fields()
+        eg = s.elastic()
+    fo = o.fields()
+    eo = o.elastic()
+    errs = {k: rel_l2(fg[k], fo[k]) for k in ("phi", "xB", "Y", "eta", "dYdt")}
+    errs["strain"] = rel_l2(eg["strain"], eo["strain"])
+    errs["sigma"] = rel_l2(eg["sigma"], eo["sigma"])
+    print(shape, {k: f"{v:.2e}" for k, v in errs.items()})
+    for k, v in errs.items():
+        assert v <= (10 if k == "dYdt" else 1) * TOL[1], (k, v)
+
+
 def test_diagnostics_parity(capi, oracle):
     """vf_precip, the xB_tot ledger, N_in / N_if (R_avg of the CSV row) and the
     field ranges against the oracle after two steps."""

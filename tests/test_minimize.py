@@ -74,6 +74,62 @@ def test_minimize_parity(capi, oracle, precision, tol):
         assert rel_l2(fg[k], fo[k]) <= tol, k
 
 
+PHI_ONLY_FIELDS = ("mean_h", "lambda_vol", "F_surf", "F_el", "rms_res", "rms_dphi", "vol_err_rel")
+
+
+def test_oracle_phi_only_minimize(capi, oracle):
+    """minimize_full_model = 0 (the reference's default minimize): no
+    composition, so the chemical energies and rms_dY are NaN and the
+    composition does not move; the volume projection and the KKT residual
+    behave as in the full model."""
+    p, phi, xB = _case(capi, n=24, minimize_full_model=0, minimize_V0=0.1)
+    o = oracle(p, threads=4)
+    o.load(phi, xB)
+    ms = capi.MinStats()
+    res = []
+    for _ in range(6):
+        assert o.minimize(1, ms) == 0
+        assert np.isnan(ms.F_chem_excess) and np.isnan(ms.F_total_excess) and np.isnan(ms.rms_dY)
+        assert np.isnan(ms.F_chem_CNT) and ms.condB == 0 and ms.xB_clamped == 0
+        res.append((ms.rms_res, ms.vol_err_rel, ms.F_el))
+    assert all(v[1] < 1e-4 for v in res[2:])
+    assert res[-1][0] < res[1][0]
+    assert all(v[2] > 0 for v in res)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, 1e-6), (1, 2e-5)])
+def test_phi_only_minimize_parity(capi, oracle, precision, tol):
+    """Phi-only minimize (compute_phi_rhs_minimize_kernel, cuda_kernels.cu:6298-6374;
+    the phi-only eigenstrain h(phi) eps00) on the GPU against the oracle,
+    iteration by iteration, heterogeneous elasticity, V0 = 0.1."""
+    from cuda_sto_pf_gb300.solver import Solver
+    p, phi, xB = _case(capi, precision=precision, minimize_full_model=0, minimize_V0=0.1)
+    o = oracle(p, threads=8)
+    o.load(phi, xB)
+    mo, mg = capi.MinStats(), capi.MinStats()
+    with Solver(p) as s:
+        s.load(phi, xB)
+        for it in range(6):
+            assert o.minimize(1, mo) == 0
+            s.minimize(1, mg)
+            assert mg.iteration == mo.iteration == it + 1
+            for f in ("F_chem_excess", "F_total_excess", "F_chem_CNT", "F_total_CNT", "rms_dY"):
+                assert np.isnan(getattr(mg, f)), f
+            for f in PHI_ONLY_FIELDS:
+                a, b = getattr(mg, f), getattr(mo, f)
+                if f == "vol_err_rel":
+                    assert abs(a - b) <= (1e-10 if precision == 0 else 1e-7), (it, f, a, b)
+                    continue
+                scale = max(abs(b), 1e-6 if f.startswith("rms") else 1e-12)
+                assert abs(a - b) <= (50 * tol if f == "rms_res" else tol) * scale, (it, f, a, b)
+            assert (mg.condA, mg.condB, mg.xB_clamped) == (mo.condA, mo.condB, 0)
+            assert abs(mg.elastic_iterations - mo.elastic_iterations) <= 1
+        fg = s.fields()
+    fo = o.fields()
+    assert rel_l2(fg["phi"], fo["phi"]) <= tol
+
+
 @pytest.mark.gpu
 def test_minimize_stops_on_convergence(capi):
     from cuda_sto_pf_gb300.solver import Solver

@@ -1,0 +1,341 @@
+"""Whole-step parity against the reference program itself.
+
+The reference main_cuda (main_cuda.cu, cuda_kernels.cu, cuda_common.cu,
+pf_zero_mode_checkpoint.cpp) is rebuilt for sm_103a by
+oracle/build_oracle.py (build_ref_main) and run on the same raw initial
+fields (--init-mode raw_fields, main_cuda.cu:2904-2990) as this library,
+through both this repository's main_cuda (same command line) and the C ABI
+(FP64 and the FP32 chosen form).
+
+Full-precision fields come from the reference's zero-mode checkpoints
+(--pf-checkpoint-every, main_cuda.cu:33494-33560): phi, Y, xB and dY/dt as
+float64.  The zero mode is refused with gp_zone by the reference
+(main_cuda.cu:24662-24690), so the gp_zone case runs without it and is
+compared through the ASCII VTK files (%.5f, io_vtk_cuda.h:80-128), whose
+rounding (5e-6) sets that case's tolerance.
+
+Contract: every field within 1e-5 relative L2 of the reference; the B
+ledger sum((1-h) xB + h v_B) on the frozen target to 1e-12 relative on both
+sides.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, REPO, params_for, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+ZM = "PF_CONSERVED_Y_ZERO_MODE_V1"
+FIELD_TOL = 1e-5
+MASS_TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def ref_main():
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import build_oracle
+    try:
+        exe = build_oracle.build_ref_main()
+    except subprocess.CalledProcessError as e:
+        pytest.fail("reference main_cuda did not build: " + (e.stderr or b"")[-3000:].decode(errors="replace"))
+    if exe is None:
+        pytest.skip("reference main_cuda sources are neither present nor staged (oracle/_ref/main_src)")
+    return exe
+
+
+def _h(phi):
+    return phi ** 3 * (6 * phi ** 2 - 15 * phi + 10)
+
+
+def _mass(phi, xB, vB=1.0):
+    h = _h(phi)
+    return float(np.sum((1.0 - h) * xB + h * vB))
+
+
+def _write_inputs(d, fields, n, xB_max_safe):
+    os.makedirs(d, exist_ok=True)
+    paths = {}
+    for k, v in fields.items():
+        p = os.path.join(d, k + ".raw")
+        np.ascontiguousarray(v, dtype=np.float64).tofile(p)
+        paths[k] = p
+    meta = {"Nx": n, "Ny": n, "Nz": n, "dx_nm": 1.0, "interface_width_nm": 5.0, "dtype": "float64",
+            "order": "C", "xB_max_safe": xB_max_safe}
+    paths["meta"] = os.path.join(d, "init_meta.json")
+    with open(paths["meta"], "w") as f:
+        json.dump(meta, f)
+    return paths
+
+
+def _params_file(d, base, extra):
+    p = os.path.join(d, "run.params")
+    with open(p, "w") as f:
+        f.write(open(os.path.join(GOLDEN, base)).read())
+        for k, v in extra.items():
+            f.write(f"\n{k}={v}")
+        f.write("\n")
+    return p
+
+
+def _argv(n, steps, out_every, pf, paths, zero_mode, ckpt):
+    a = [str(n), str(n), str(n), "0.01", str(steps), str(out_every), str(steps), "1", "--pf-param-file", pf,
+         "--init-mode", "raw_fields", "--init-phi-raw", paths["phi"], "--init-xB-raw", paths["xB"],
+         "--init-meta", paths["meta"]]
+    if "eta" in paths:
+        a += ["--init-eta-raw", paths["eta"]]
+    if zero_mode:
+        a += ["--pf-zero-mode", ZM, "--pf-checkpoint-every", str(steps), "--pf-checkpoint-path", ckpt]
+    return a
+
+
+def _run(exe, argv, results):
+    env = dict(os.environ, CUDA_STO_RESULTS_ROOT=results)
+    r = subprocess.run([exe, *argv], capture_output=True, text=True, timeout=1200, env=env,
+                       cwd=os.path.dirname(results))
+    out = os.path.join(REPO, "gpurun_out")
+    if os.path.isdir(out):
+        tag = os.path.basename(os.path.dirname(results)) + "_" + os.path.basename(results)
+        with open(os.path.join(out, f"ref_main_{tag}.log"), "w") as f:
+            f.write(" ".join(argv) + f"\nrc={r.returncode}\n" + r.stdout[-20000:] + "\n---- stderr\n" +
+                    r.stderr[-5000:])
+    return r
+
+
+def _read_ckpt(capi, path, n):
+    """phi, Y, xB, dY/dt (float64) of a V3/V4 checkpoint: the payload sits
+    at the end of the file, fields first, then (V4) u_k as complex float."""
+    lib = capi.load()
+    ver, el = ctypes.c_int32(), ctypes.c_int32()
+    capi.check(lib.pfgb_checkpoint_peek(path.encode(), ctypes.byref(ver), None, None, None, ctypes.byref(el)),
+               "pfgb_checkpoint_peek")
+    N, Nk = n ** 3, n * n * (n // 2 + 1)
+    tail = 4 * N * 8 + (6 * Nk * 4 if el.value else 0)
+    raw = open(path, "rb").read()
+    f = np.frombuffer(raw[len(raw) - tail:len(raw) - tail + 4 * N * 8], dtype="<f8").reshape(4, n, n, n)
+    return {"phi": f[0], "Y": f[1], "xB": f[2], "dYdt": f[3], "version": ver.value}
+
+
+def _vtk(path, n):
+    with open(path) as f:
+        lines = f.read().split("\n")
+    data = np.array(" ".join(lines[10:]).split(), dtype=np.float64)
+    return data.reshape(n, n, n).transpose(2, 1, 0)
+
+
+def _case_dir(results):
+    runs = os.listdir(results)
+    assert len(runs) == 1, runs
+    top = os.path.join(results, runs[0])
+    subs = [s for s in os.listdir(top) if os.path.isdir(os.path.join(top, s))]
+    assert len(subs) == 1, subs
+    return os.path.join(top, subs[0])
+
+
+def _report(name, rec):
+    out = os.path.join(REPO, "gpurun_out")
+    if os.path.isdir(out):
+        with open(os.path.join(out, "ref_main_parity.jsonl"), "a") as f:
+            f.write(json.dumps({"case": name, **rec}) + "\n")
+
+
+def _library_fields(capi, base, n, extra, fields, xB_max_safe, steps, precision, zero_mode):
+    from cuda_sto_pf_gb300.solver import Solver
+    over = {"precision": precision, "zero_mode_enabled": 1 if zero_mode else 0}
+    p = params_for(capi, base, n=n, **over)
+    for k, v in extra.items():
+        capi.set_param(p, k, v)
+    capi.finalize(p)
+    phi = fields["phi"].copy()
+    xB = fields["xB"].copy()
+    eta = fields["eta"].copy() if "eta" in fields else None
+    capi.check(capi.load().pfgb_prepare_raw_fields(ctypes.byref(p), xB_max_safe, phi.ctypes.data,
+                                                   xB.ctypes.data, None if eta is None else eta.ctypes.data,
+                                                   None, phi.size), "prepare")
+    with Solver(p) as s:
+        s.load(phi, xB, eta)
+        st = s.step(steps)
+        f = s.fields()
+    return f, st
+
+
+def _prepared_mass(capi, base, n, extra, fields, xB_max_safe):
+    """The B ledger of the initial state after the raw-field loader rules."""
+    p = params_for(capi, base, n=n)
+    for k, v in extra.items():
+        capi.set_param(p, k, v)
+    capi.finalize(p)
+    phi, xB = fields["phi"].copy(), fields["xB"].copy()
+    capi.check(capi.load().pfgb_prepare_raw_fields(ctypes.byref(p), xB_max_safe, phi.ctypes.data,
+                                                   xB.ctypes.data, None, None, phi.size), "prepare")
+    return _mass(phi, xB, p.v_B)
+
+
+def _compare(ref, ours, keys):
+    return {k: rel_l2(ours[k], ref[k]) for k in keys}
+
+
+def _zero_mode_case(capi, ref_main, tmp_path, name, base, extra, fields, n, steps, xB_max_safe):
+    """Run the reference and this repository's main_cuda with one command
+    line, and the library in FP32; compare the checkpointed fields."""
+    d = str(tmp_path)
+    paths = _write_inputs(os.path.join(d, "in"), fields, n, xB_max_safe)
+    pf = _params_file(d, base, extra)
+    ck_ref, ck_ours = os.path.join(d, "ref.ckpt"), os.path.join(d, "ours.ckpt")
+    r = _run(ref_main, _argv(n, steps, steps, pf, paths, True, ck_ref), os.path.join(d, "R_ref"))
+    assert r.returncode == 0, "reference main_cuda failed:\n" + r.stdout[-3000:] + r.stderr[-3000:]
+    from cuda_sto_pf_gb300 import build
+    o = _run(build.EXE, _argv(n, steps, steps, pf, paths, True, ck_ours), os.path.join(d, "R_ours"))
+    assert o.returncode == 0, o.stdout[-3000:] + o.stderr[-3000:]
+    ref = _read_ckpt(capi, ck_ref, n)
+    cli = _read_ckpt(capi, ck_ours, n)
+    f32, st32 = _library_fields(capi, base, n, extra, fields, xB_max_safe, steps, 1, True)
+    keys = ("phi", "xB", "Y", "dYdt")
+    e_cli = _compare(ref, cli, keys)
+    e_32 = _compare(ref, {"phi": f32["phi"], "xB": f32["xB"], "Y": f32["Y"], "dYdt": f32["dYdt"]}, keys)
+    m0 = _prepared_mass(capi, base, n, extra, fields, xB_max_safe)
+    tgt = [float(l.split("target_mass_code=")[1].split()[0]) for l in r.stdout.split("\n")
+           if "PF_ZERO_MODE_CHECKPOINT_WRITTEN" in l and "target_mass_code=" in l]
+    m_ref, m_cli, m_32 = _mass(ref["phi"], ref["xB"]), _mass(cli["phi"], cli["xB"]), _mass(f32["phi"], f32["xB"])
+    rec = {"n": n, "steps": steps, "cli_fp64": e_cli, "lib_fp32": e_32, "mass0": m0,
+           "mass_rel": {"ref": abs(m_ref - m0) / m0, "cli_fp64": abs(m_cli - m0) / m0, "lib_fp32": abs(m_32 - m0) / m0},
+           "ref_target_mass": tgt[-1] if tgt else None,
+           "ref_version": ref["version"], "xB_max": float(ref["xB"].max())}
+    _compare_outputs(_case_dir(os.path.join(d, "R_ref")), _case_dir(os.path.join(d, "R_ours")), name, rec)
+    _report(name, rec)
+    for k in keys:
+        if k == "dYdt":
+            continue
+        assert e_cli[k] <= FIELD_TOL, (name, "fp64 cli", k, e_cli)
+        assert e_32[k] <= FIELD_TOL, (name, "fp32 library", k, e_32)
+    # dY/dt is a difference quotient (Y^{n+1} - Y^n) / dt: its relative
+    # error is that of Y times |Y| / |dt dY/dt|; checked at 1e-5 on FP64
+    assert e_cli["dYdt"] <= FIELD_TOL, (name, e_cli)
+    for side, m in (("ref", m_ref), ("cli_fp64", m_cli), ("lib_fp32", m_32)):
+        assert abs(m - m0) <= MASS_TOL * m0 * 4, (name, side, abs(m - m0) / m0)
+    return rec
+
+
+def _c1_fields(n=64, radius=8.0):
+    from cuda_sto_pf_gb300 import workloads
+    w = workloads.single_sphere(n=n, radius=radius)
+    return {"phi": w["phi"], "xB": w["xB"]}
+
+
+def _csv(path):
+    rows = open(path).read().strip().split("\n")
+    return rows[0], np.array([[float(x) for x in r.split(",")] for r in rows[1:]])
+
+
+def _compare_outputs(cr, co, name, rec):
+    """The two programs' case directories: the same file names, the same
+    CSV rows (step, t_code, t_real_s, vf_precip, R_avg), the same elastic
+    iteration counts per step (within one)."""
+    fr, fo = sorted(os.listdir(cr)), sorted(os.listdir(co))
+    vtk_r = [f for f in fr if f.endswith(".vtk")]
+    vtk_o = [f for f in fo if f.endswith(".vtk")]
+    assert vtk_r == vtk_o, (name, vtk_r, vtk_o)
+    csvs = [f for f in fr if f.startswith("vf_precip_vs_time_")]
+    assert csvs and all(f in fo for f in csvs), (fr, fo)
+    hr, ar = _csv(os.path.join(cr, csvs[0]))
+    ho, ao = _csv(os.path.join(co, csvs[0]))
+    assert hr == ho and ar.shape == ao.shape, (hr, ho, ar.shape, ao.shape)
+    assert np.array_equal(ar[:, 0], ao[:, 0])
+    rec["csv_max_rel"] = float(np.max(np.abs(ao[:, 1:] - ar[:, 1:]) / np.maximum(np.abs(ar[:, 1:]), 1e-30)))
+    assert rec["csv_max_rel"] <= 1e-5, (name, rec["csv_max_rel"])
+    if "elastic_solver_trace.csv" in fr:
+        er = _csv(os.path.join(cr, "elastic_solver_trace.csv"))[1]
+        eo = _csv(os.path.join(co, "elastic_solver_trace.csv"))[1]
+        assert er.shape[0] == eo.shape[0]
+        rec["elastic_iters_ref"] = [int(x) for x in er[:, 2]]
+        rec["elastic_iters_ours"] = [int(x) for x in eo[:, 2]]
+        assert np.abs(er[:, 2] - eo[:, 2]).max() <= 1, (name, rec)
+
+
+def test_c1_sphere_homogeneous_100_steps(capi, ref_main, tmp_path):
+    """C1: 64^3, dt 0.01, 100 steps, one sphere R = 8 with 0.03 + N(0, 1e-3)
+    outside and c = 0.33 inside, homogeneous cubic elasticity (C11 108,
+    C12 7.7, C44 13 GPa: S_p = 0), under the reference's raw-field rules:
+    xB capped at xB_max_safe = 0.07, the loader default (main_cuda.cu:2940,
+    2961-2963).  Fields, CSV rows and per-step elastic iterations of the
+    reference against this repository's main_cuda (FP64, same command
+    line), and the fields against the library's FP32 form."""
+    _zero_mode_case(capi, ref_main, tmp_path, "c1_sphere_64_100", "c1.params", {}, _c1_fields(), 64, 100, 0.07)
+
+
+def test_c1_uncapped_composition_fails_closed_in_both(capi, ref_main, tmp_path):
+    """C1 as written, c = 0.33 inside the sphere uncapped (xB_max_safe 0.34):
+    at dt = 0.01 the composition update leaves the logit clip in the first
+    step, so the zero mode finds no admissible shift (an empty bracket) and
+    the reference stops with exit 2 at step 1.  This repository's main_cuda
+    must refuse the same step the same way."""
+    from cuda_sto_pf_gb300 import build
+    d = str(tmp_path)
+    paths = _write_inputs(os.path.join(d, "in"), _c1_fields(), 64, 0.34)
+    pf = _params_file(d, "c1.params", {})
+    r = _run(ref_main, _argv(64, 5, 5, pf, paths, True, os.path.join(d, "ref.ckpt")), os.path.join(d, "R_ref"))
+    o = _run(build.EXE, _argv(64, 5, 5, pf, paths, True, os.path.join(d, "ours.ckpt")), os.path.join(d, "R_ours"))
+    _report("c1_uncapped_64", {"ref_rc": r.returncode, "ours_rc": o.returncode,
+                               "ref_err": r.stderr.strip()[-300:], "ours_err": o.stderr.strip()[-300:]})
+    assert r.returncode == 2 and "zero-mode rejected step=1" in r.stderr, r.stderr[-2000:]
+    assert o.returncode == 2 and "zero-mode" in o.stderr, o.stdout[-2000:] + o.stderr[-2000:]
+    assert not os.path.exists(os.path.join(d, "ref.ckpt")) and not os.path.exists(os.path.join(d, "ours.ckpt"))
+
+
+def test_two_phase_heterogeneous_elasticity(capi, ref_main, tmp_path):
+    """C2's physics at 64^3 (two_phase, since the reference refuses the zero
+    mode with gp_zone): 8 ellipsoids with log-normal radii, heterogeneous
+    stiffness S_p = C_Ag2Te - C_PbTe, elastic tolerance 1e-8 without the
+    fail-closed rule, 30 steps, the loader's default composition cap."""
+    from cuda_sto_pf_gb300 import workloads
+    w = workloads.ellipsoid_population(n=64, count=8, eta_sites=0, seed=11)
+    extra = {"elastic_residual_tolerance": "1e-8", "elastic_fail_on_nonconvergence": "0"}
+    _zero_mode_case(capi, ref_main, tmp_path, "c2_two_phase_64_30", "c2.params", extra,
+                    {"phi": w["phi"], "xB": w["xB"]}, 64, 30, 0.07)
+
+
+def test_gp_zone_heterogeneous_vtk(capi, ref_main, tmp_path):
+    """gp_zone with eta sites and heterogeneous stiffness, no zero mode (the
+    reference refuses it there), 10 steps with out_every 4 (so the last step
+    is off the output schedule): the two programs' output files, CSV rows
+    and elastic iterations, and the last phi, xB and eta VTK files of both
+    against the library's FP64 and FP32 fields."""
+    from cuda_sto_pf_gb300 import build, workloads
+    n, steps, every = 48, 10, 4
+    w = workloads.ellipsoid_population(n=n, count=5, eta_sites=4, seed=5)
+    fields = {"phi": w["phi"], "xB": w["xB"], "eta": w["eta"]}
+    extra = {"model_mode": "gp_zone"}
+    d = str(tmp_path)
+    paths = _write_inputs(os.path.join(d, "in"), fields, n, 0.07)
+    pf = _params_file(d, "c2.params", extra)
+    argv = _argv(n, steps, every, pf, paths, False, None)
+    argv[6] = "1"   # csv_out_every: a CSV row every step
+    r = _run(ref_main, argv, os.path.join(d, "R_ref"))
+    assert r.returncode == 0, "reference main_cuda failed:\n" + r.stdout[-3000:] + r.stderr[-3000:]
+    o = _run(build.EXE, argv, os.path.join(d, "R_ours"))
+    assert o.returncode == 0, o.stdout[-3000:] + o.stderr[-3000:]
+    cr, co = _case_dir(os.path.join(d, "R_ref")), _case_dir(os.path.join(d, "R_ours"))
+    rec = {"n": n, "steps": steps}
+    _compare_outputs(cr, co, "gp_zone", rec)
+    last = steps // every + 1   # main_cuda.cu:33815-33840
+    for prec in (0, 1):
+        f, _ = _library_fields(capi, "c2.params", n, extra, fields, 0.07, steps, prec, False)
+        for k in ("phi", "xB", "eta"):
+            ref = _vtk(os.path.join(cr, f"{k}_{last}.vtk"), n)
+            cli = _vtk(os.path.join(co, f"{k}_{last}.vtk"), n)
+            tag = "fp64" if prec == 0 else "fp32"
+            rec[f"{k}_maxabs_lib_{tag}"] = float(np.abs(f[k] - ref).max())
+            rec[f"{k}_maxabs_cli"] = float(np.abs(cli - ref).max())
+            rec[f"{k}_rel_l2_lib_{tag}"] = rel_l2(f[k], ref)
+    _report("gp_zone_48_10", rec)
+    for k, v in rec.items():
+        if "maxabs" in k:
+            # 5e-6 of VTK rounding plus 1e-5 of the field scale (all in [0, 1])
+            assert v <= 1.5e-5, (k, rec)
