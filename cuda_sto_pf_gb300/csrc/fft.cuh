@@ -463,7 +463,8 @@ template <int NIN, int NOUT> constexpr int axis_width() { return NIN > NOUT ? NI
 template <typename T, int NIN, int NOUT, int DIN, int DOUT, class Op>
 __global__ void __launch_bounds__(256)
 k_axis_pass(Grid3 g, int axis, AxisPlan plan, const cplx_t<T> *tw_g, int TK,
-            AxisIO<T, NIN, NOUT> io, Op op) {
+            AxisIO<T, NIN, NOUT> io, Op op, const double *skip) {
+    if (skip && *skip != 0.0) return;   // a finished elastic iteration: launched ahead, nothing to do
     using T2 = cplx_t<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2 *sm = reinterpret_cast<T2 *>(smem_raw);
@@ -586,7 +587,8 @@ __device__ void block_reduce_acc(Acc &a) {
 
 template <typename T, int NFI, int NFO, class Op>
 __global__ void __launch_bounds__(256)
-k_zpass(Grid3 g, AxisPlan plan, const cplx_t<T> *tw_g, int R, Op op) {
+k_zpass(Grid3 g, AxisPlan plan, const cplx_t<T> *tw_g, int R, Op op, const double *skip) {
+    if (skip && *skip != 0.0) return;
     using T2 = cplx_t<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2 *sm = reinterpret_cast<T2 *>(smem_raw);

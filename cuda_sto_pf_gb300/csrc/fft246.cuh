@@ -130,7 +130,8 @@ constexpr size_t z_smem_bytes() { return (size_t)(N + NL * N) * sizeof(float2); 
 // ---------------------------------------------------------------------------
 template <int DIR>
 __global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
-k_y246(Grid3 g, const float2 *tw_g, AxisIO<float, 6, 6> io) {
+k_y246(Grid3 g, const float2 *tw_g, AxisIO<float, 6, 6> io, const double *skip) {
+    if (skip && *skip != 0.0) return;
     using namespace f246;
     constexpr int TP = TC / 2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -192,7 +193,8 @@ constexpr bool f246_axis_fits() {
 
 template <int NIN, int NOUT, int DIN, int DOUT, class Op>
 __global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
-k_axis246(Grid3 g, int axis, const float2 *tw_g, AxisIO<float, NIN, NOUT> io, Op op) {
+k_axis246(Grid3 g, int axis, const float2 *tw_g, AxisIO<float, NIN, NOUT> io, Op op, const double *skip) {
+    if (skip && *skip != 0.0) return;
     using namespace f246;
     constexpr int NW = NIN > NOUT ? NIN : NOUT;
     constexpr int TCW = NL / NW, TPW = TCW / 2;

@@ -61,6 +61,10 @@ struct DevState {
 
 // device scalar slots
 enum { DS_MEAN_DY = 0, DS_RES_DIFF = 1, DS_RES_REF = 2, DS_ZM = 4, DS_BR = 12, DS_EV = 16, DS_N = 24 };
+// elastic-iteration status on the device (slots of the same array): done,
+// updates taken, non-finite residual, converged.  While `done` is set, the
+// kernels of further iterations launched ahead return at once.
+enum { DS_EL = 56 };
 
 struct pfgb_ctx {
     pfgb_params p;
@@ -122,6 +126,10 @@ struct pfgb_ctx {
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> pool;
     size_t pool_used = 0;
+    // while an elastic solve runs: &dscal[DS_EL] (its kernels return at once
+    // once the device has decided the solve), else null
+    const double *skip = nullptr;
+    int last_el_iters = 0;   // updates of the last solve: the first batch launched ahead
 };
 
 // tag + algorithmic bytes of the next launch (set by the op-level wrappers)
@@ -221,7 +229,7 @@ static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, O
             dim3 grid((c->g.NzC + TCW - 1) / TCW, axis == 1 ? c->g.Nx : c->g.Ny);
             ProfScope ps(c, {tag, (double)(NIN + NOUT) * (double)c->g.Nk * sizeof(T2)});
             kern<<<grid, f246::THREADS, smem, c->stream>>>(c->g, axis, (const float2 *)twp<T>(c, axis == 1 ? 1 : 0),
-                                                         io, op);
+                                                         io, op, c->skip);
             PFGB_CUDA_TRY(cudaGetLastError());
             return PFGB_OK;
         }
@@ -237,7 +245,7 @@ static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, O
     PFGB_CUDA_TRY(allow_smem(kern, smem));
     dim3 grid((c->g.NzC + TK - 1) / TK, axis == 1 ? c->g.Nx : c->g.Ny);
     ProfScope ps(c, {tag, (double)(NIN + NOUT) * (double)c->g.Nk * sizeof(T2)});
-    kern<<<grid, 256, smem, c->stream>>>(c->g, axis, pl, twp<T>(c, axis == 1 ? 1 : 0), TK, io, op);
+    kern<<<grid, 256, smem, c->stream>>>(c->g, axis, pl, twp<T>(c, axis == 1 ? 1 : 0), TK, io, op, c->skip);
     PFGB_CUDA_TRY(cudaGetLastError());
     return PFGB_OK;
 }
@@ -254,7 +262,8 @@ constexpr bool f246_z_fits() {
 
 template <int NFI, int NFO, class Op>
 __global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
-k_zpass246g(Grid3 g, const float2 *tw_g, Op op) {
+k_zpass246g(Grid3 g, const float2 *tw_g, Op op, const double *skip) {
+    if (skip && *skip != 0.0) return;
     using namespace f246;
     constexpr int LI = (NFI + 1) / 2, LO = (NFO + 1) / 2, LW = LI > LO ? LI : LO;
     constexpr int R = NL / LW, NC = N / 2 + 1;
@@ -362,7 +371,7 @@ static pfgb_status launch_z(pfgb_ctx *c, Op op, const char *tag, double extra_by
             const long long rows = (long long)c->g.Nx * c->g.Ny;
             const int nb = (int)((rows + R - 1) / R);
             ProfScope ps(c, {tag, (double)(NFI + NFO) * (double)c->g.Nk * sizeof(T2) + extra_bytes});
-            kern<<<nb, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)twp<T>(c, 2), op);
+            kern<<<nb, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)twp<T>(c, 2), op, c->skip);
             PFGB_CUDA_TRY(cudaGetLastError());
             if (nblocks) *nblocks = nb;
             return PFGB_OK;
@@ -382,7 +391,7 @@ static pfgb_status launch_z(pfgb_ctx *c, Op op, const char *tag, double extra_by
     PFGB_CUDA_TRY(allow_smem(kern, smem));
     const int nb = (int)((rows + R - 1) / R);
     ProfScope ps(c, {tag, (double)(NFI + NFO) * (double)c->g.Nk * sizeof(T2) + extra_bytes});
-    kern<<<nb, 256, smem, c->stream>>>(c->g, c->plz, twp<T>(c, 2), R, op);
+    kern<<<nb, 256, smem, c->stream>>>(c->g, c->plz, twp<T>(c, 2), R, op, c->skip);
     PFGB_CUDA_TRY(cudaGetLastError());
     if (nblocks) *nblocks = nb;
     return PFGB_OK;
@@ -442,7 +451,9 @@ struct AccZMt {
 using AccZM = AccZMt<double>;
 
 template <class Acc>
-__global__ void k_reduce_partials(const Acc *part, int n, double *out, int slot, double scale) {
+__global__ void k_reduce_partials(const Acc *part, int n, double *out, int slot, double scale,
+                                  const double *skip = nullptr) {
+    if (skip && *skip != 0.0) return;
     Acc a = Acc::identity();
     for (int i = threadIdx.x; i < n; i += blockDim.x) a = Acc::combine(a, part[i]);
     block_reduce_acc(a);
@@ -455,7 +466,8 @@ __global__ void k_reduce_partials(const Acc *part, int n, double *out, int slot,
 template <class Acc>
 static pfgb_status reduce_to(pfgb_ctx *c, int nblocks, int slot, double scale = 1.0) {
     ProfScope ps(c, {"reduce_partials", (double)nblocks * sizeof(Acc)});
-    k_reduce_partials<Acc><<<1, 256, 0, c->stream>>>((const Acc *)c->partials, nblocks, c->dscal, slot, scale);
+    k_reduce_partials<Acc><<<1, 256, 0, c->stream>>>((const Acc *)c->partials, nblocks, c->dscal, slot, scale,
+                                                     c->skip);
     PFGB_CUDA_TRY(cudaGetLastError());
     return PFGB_OK;
 }
@@ -1094,6 +1106,7 @@ struct GreenArgs {
     cplx_t<TE> *Dm[3];         // Chebyshev: the iterate before delta (null: plain update)
     TE gam, rho;
     double *partials;
+    const double *skip;        // return at once when *skip != 0 (a finished solve)
     int resid;
     int mode;                  // 0 u <- Phi(u); 1 first increment step; 2 delta <- r0 + L delta
 };
@@ -1250,6 +1263,7 @@ __device__ __forceinline__ void green_u(const TE *S, TE kx, TE ky, TE kz, const 
 template <typename TE, bool EIGEN>
 __global__ void __launch_bounds__(256)
 k_x_green(GreenArgs<TE> A, AxisPlan plan, int TK) {
+    if (A.skip && *A.skip != 0.0) return;
     using T2 = cplx_t<TE>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2 *sm = reinterpret_cast<T2 *>(smem_raw);
@@ -1351,6 +1365,36 @@ __global__ void k_resid_final(double *dscal, double floor_) {
     dscal[3] = sqrt(d / fmax(r, floor_));
 }
 
+// the stopping rule of the accelerated elastic solver on the device (loop
+// control of main_cuda.cu:28982-29050): after an update, rel = sqrt(diff /
+// max(ref, floor)); stop when iter >= iter_min and rel <= tol, at iter_max,
+// or on a non-finite / negative residual sum.  Slots DS_EL + 0..3: done,
+// updates taken, non-finite, converged.  Nothing changes once done is set.
+__global__ void k_resid_step(double *dscal, double floor_, double tol, int iter_min, int iter_max) {
+    double *st = dscal + DS_EL;
+    if (st[0] != 0.0) return;
+    const double d = dscal[DS_RES_DIFF], r = dscal[DS_RES_REF];
+    const double it = st[1] + 1.0;
+    st[1] = it;
+    if (!isfinite(d) || !isfinite(r) || d < 0.0 || r < 0.0) {
+        st[2] = 1.0;
+        st[0] = 1.0;
+        return;
+    }
+    const double rel = sqrt(d / fmax(r, floor_));
+    dscal[3] = rel;
+    if (it >= (double)iter_min && rel <= tol) {
+        st[3] = 1.0;
+        st[0] = 1.0;
+    } else if (it >= (double)iter_max) {
+        st[0] = 1.0;
+    }
+}
+
+__global__ void k_el_status_reset(double *dscal) {
+    if (threadIdx.x < 4) dscal[DS_EL + threadIdx.x] = 0.0;
+}
+
 // spectra a Green pass moves besides its 6 sources, 6 strains and 3 written
 // displacements: the increment update reads r0, delta and u0 (and the
 // Chebyshev iterate before delta); the first update writes r0 and delta
@@ -1384,6 +1428,7 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
     A.gam = (TE)c->cheb_gam;
     A.rho = (TE)c->cheb_rho;
     A.partials = c->partials;
+    A.skip = c->skip;
     A.resid = resid;
     A.mode = mode;
     dim3 grid((c->g.NzC + TK - 1) / TK, c->g.Ny);
@@ -1412,6 +1457,7 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
 template <bool EIGEN>
 __global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
 k_x_green246(GreenArgs<float> A) {
+    if (A.skip && *A.skip != 0.0) return;
     using namespace f246;
     using T2 = float2;
     constexpr int TP = TC / 2;
@@ -1513,7 +1559,8 @@ k_x_green246(GreenArgs<float> A) {
 // per block: the rows' three field pairs are the block's NL complex lines
 template <class Op>
 __global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
-k_zpass246(Grid3 g, const float2 *tw_g, Op op) {
+k_zpass246(Grid3 g, const float2 *tw_g, Op op, const double *skip) {
+    if (skip && *skip != 0.0) return;
     using namespace f246;
     constexpr int R = ZR, NC = N / 2 + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1589,7 +1636,7 @@ static pfgb_status launch_y246(pfgb_ctx *c, const char *tag) {
     for (int i = 0; i < 6; ++i) { io.in[i] = (const float2 *)c->E[i]; io.out[i] = (float2 *)c->E[i]; }
     dim3 grid((c->g.NzC + f246::TC - 1) / f246::TC, c->g.Nx);
     ProfScope ps(c, {tag, 12.0 * (double)c->g.Nk * sizeof(float2)});
-    kern<<<grid, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][1], io);
+    kern<<<grid, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][1], io, c->skip);
     PFGB_CUDA_TRY(cudaGetLastError());
     return PFGB_OK;
 }
@@ -1609,6 +1656,7 @@ static pfgb_status launch_green246(pfgb_ctx *c, bool eigen, int resid, int *nblo
     A.gam = (float)c->cheb_gam;
     A.rho = (float)c->cheb_rho;
     A.partials = c->partials;
+    A.skip = c->skip;
     A.resid = resid;
     A.mode = mode;
     dim3 grid((c->g.NzC + f246::TC - 1) / f246::TC, c->g.Ny);
@@ -1636,7 +1684,7 @@ static pfgb_status launch_z246(pfgb_ctx *c, Op op, const char *tag, double extra
     const long long rows = (long long)c->g.Nx * c->g.Ny;
     const int nb = (int)((rows + f246::ZR - 1) / f246::ZR);
     ProfScope ps(c, {tag, 12.0 * (double)c->g.Nk * sizeof(float2) + extra_bytes});
-    kern<<<nb, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][2], op);
+    kern<<<nb, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][2], op, c->skip);
     PFGB_CUDA_TRY(cudaGetLastError());
     return PFGB_OK;
 }
@@ -1900,8 +1948,9 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     // the one before, so the two buffers swap after every update
     const bool cheb = inc && c->Dkm[0] != nullptr;
     int cheb_it = 0;
-    for (;;) {
-        const int lin = inc && iter >= 1;
+    // one update of the fixed point (iteration index k from 0)
+    auto update = [&](int k) -> pfgb_status {
+        const int lin = inc && k >= 1;
         TRY(hij(lin));
         TRY(ypass(-1, "y_fwd6"));
         if (cheb && lin) {
@@ -1912,22 +1961,58 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
         TRY(green(false, accel, inc ? (lin ? 2 : 1) : 0));
         if (cheb && lin)
             for (int i = 0; i < 3; ++i) std::swap(c->Dk[i], c->Dkm[i]);
-        TRY(ypass(+1, "y_inv6"));
-        if (accel) {
-            TRY(reduce_to<AccSum2>(c, nb, DS_RES_DIFF));
-            k_resid_final<<<1, 1, 0, c->stream>>>(c->dscal, P.elastic_residual_absolute_floor);
-            PFGB_CUDA_TRY(cudaGetLastError());
-            TRY(sync_read(c, DS_RES_DIFF, 3));
-            const double ds = c->hscal[DS_RES_DIFF], rs = c->hscal[DS_RES_REF];
-            if (!std::isfinite(ds) || !std::isfinite(rs) || ds < 0.0 || rs < 0.0) {
-                pfgb_set_error_msg("elastic residual is non-finite at step %d", c->step + 1);
-                return PFGB_ERR_NONFINITE;
+        return ypass(+1, "y_inv6");
+    };
+    if (accel) {
+        // The residual test runs on the device (k_resid_step) and the host
+        // launches the updates in batches, reading the status once per
+        // batch: the first batch is one update short of the last solve's
+        // count, later ones two.  Updates launched past the stopping point
+        // return at once (c->skip); the Chebyshev buffer swaps they made on
+        // the host are undone below.
+        struct SkipGuard { pfgb_ctx *c; ~SkipGuard() { c->skip = nullptr; } } guard{c};
+        k_el_status_reset<<<1, 32, 0, c->stream>>>(c->dscal);
+        PFGB_CUDA_TRY(cudaGetLastError());
+        c->skip = c->dscal + DS_EL;
+        const int imax = std::max(1, P.elastic_iter_max);
+        int batch = c->last_el_iters > 1 ? c->last_el_iters - 1 : 4;
+        batch = std::max(1, std::min(std::max(batch, P.elastic_iter_min), imax));
+        int launched = 0;
+        for (;;) {
+            const int nbat = std::min(batch, imax - launched);
+            for (int b = 0; b < nbat; ++b) {
+                TRY(update(launched + b));
+                TRY(reduce_to<AccSum2>(c, nb, DS_RES_DIFF));
+                k_resid_step<<<1, 1, 0, c->stream>>>(c->dscal, P.elastic_residual_absolute_floor,
+                                                     P.elastic_residual_tolerance, P.elastic_iter_min, imax);
+                PFGB_CUDA_TRY(cudaGetLastError());
             }
-            rel = c->hscal[3];
-            ++iter;
-            if (iter >= P.elastic_iter_min && rel <= P.elastic_residual_tolerance) { conv = 1; break; }
-            if (iter >= P.elastic_iter_max) break;
-        } else {
+            launched += nbat;
+            PFGB_CUDA_TRY(cudaMemcpyAsync(c->hscal + 3, c->dscal + 3, sizeof(double), cudaMemcpyDeviceToHost,
+                                          c->stream));
+            TRY(sync_read(c, DS_EL, 4));
+            if (c->hscal[DS_EL] != 0.0 || launched >= imax) break;
+            batch = 2;
+        }
+        c->skip = nullptr;
+        iter = (int)c->hscal[DS_EL + 1];
+        conv = c->hscal[DS_EL + 3] != 0.0;
+        rel = c->hscal[3];
+        if (cheb) {
+            // the host swapped after every launched linear update; the device
+            // ran iter updates (linear from the second on)
+            const int done_swaps = std::max(0, iter - 1), host_swaps = std::max(0, launched - 1);
+            if ((host_swaps - done_swaps) % 2 != 0)
+                for (int i = 0; i < 3; ++i) std::swap(c->Dk[i], c->Dkm[i]);
+        }
+        if (c->hscal[DS_EL + 2] != 0.0) {
+            pfgb_set_error_msg("elastic residual is non-finite at step %d", c->step + 1);
+            return PFGB_ERR_NONFINITE;
+        }
+        c->last_el_iters = iter;
+    } else {
+        for (;;) {
+            TRY(update(iter));
             ++iter;
             if (iter >= P.elastic_iter_max) break;
         }

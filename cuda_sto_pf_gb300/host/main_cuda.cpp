@@ -67,6 +67,10 @@ struct Cli {
     int min_max_iter = -1, min_conv_steps = -1, min_post_iters = -1;
     double min_dt = NAN, V0 = NAN, eta_lambda = NAN, thr_dphi = NAN, thr_dY = NAN, thr_res = NAN, thr_vol = NAN,
            thr_E = NAN, min_pt = NAN, xB_max_safe = NAN, radius = NAN;
+    // continuation from ASCII VTK (--mode=minimize-continue, --continue-phi-vtk,
+    // main_cuda.cu:22752-22770, 23770-23780)
+    bool cont = false;
+    std::string cont_phi, cont_xB;
 };
 
 void usage() {
@@ -74,7 +78,9 @@ void usage() {
            "  ./main_cuda Nx Ny Nz dt nsteps out_every csv_out_every elastic_enabled(0/1)\n"
            "    dt is a fallback only: the parameter file's dt wins.\n"
            "\nFlags:\n"
-           "  --mode=dynamics|minimize\n"
+           "  --mode=dynamics|dynamics-continue|minimize|minimize-continue\n"
+           "  --continue-phi-vtk <path>       continuation: load phi from ASCII VTK\n"
+           "  --continue-xB-vtk <path>        continuation: optional xB ASCII VTK (else rebuilt from phi)\n"
            "  --minimize-full-model           minimize with chemistry + diffusion + volume constraint\n"
            "  --minimize-max-iter <n>  --minimize-dt <dt>  --V0 <v>  --eta-lambda-vol <v>\n"
            "  --minimize-rms-dphi-threshold <v>  --minimize-rms-dY-threshold <v>\n"
@@ -163,6 +169,8 @@ Cli parse(int argc, char **argv) {
         if (!strcmp(a, "--help") || !strcmp(a, "-h")) { usage(); exit(0); }
         else if (!strncmp(a, "--mode=", 7)) c.mode = a + 7;
         else if ((v = flag_value(argc, argv, &i, "--mode"))) c.mode = v;
+        else if ((v = flag_value(argc, argv, &i, "--continue-phi-vtk"))) { c.cont_phi = v; c.cont = true; }
+        else if ((v = flag_value(argc, argv, &i, "--continue-xB-vtk"))) c.cont_xB = v;
         else if ((v = flag_value(argc, argv, &i, "--pf-param-file"))) c.param_file = v;
         else if ((v = flag_value(argc, argv, &i, "--elastic"))) { if (!to_int(v, &c.elastic)) bad(a, v); }
         else if ((v = flag_value(argc, argv, &i, "--temperature-C"))) { if (!to_double(v, &c.temperature_C)) bad(a, v); }
@@ -319,6 +327,133 @@ bool json_string(const std::string &txt, const char *key, std::string *v) {
     return true;
 }
 
+// ASCII VTK scalar field (read_vtk_ascii_to_host, io_vtk_cuda.h:131-200):
+// DIMENSIONS must match (a 2D x-z file has Ny = 1 for a run with Ny = 2),
+// values follow LOOKUP_TABLE with x fastest, then y, then z
+bool read_vtk_field(const std::string &path, int Nx, int Ny, int Nz, std::vector<double> *out) {
+    FILE *f = fopen(path.c_str(), "r");
+    if (!f) { fprintf(stderr, "ERROR: Cannot open VTK file %s for reading\n", path.c_str()); return false; }
+    char line[4096];
+    int vx = -1, vy = -1, vz = -1;
+    bool dims = false, lookup = false;
+    while (fgets(line, sizeof(line), f)) {
+        if (!dims && !strncmp(line, "DIMENSIONS", 10)) { dims = sscanf(line, "DIMENSIONS %d %d %d", &vx, &vy, &vz) == 3; continue; }
+        if (!strncmp(line, "LOOKUP_TABLE", 12)) { lookup = true; break; }
+    }
+    const bool two_d = vy == 1 && Ny == 2;
+    if (!dims || !lookup || vx != Nx || vz != Nz || !(vy == Ny || two_d)) {
+        fprintf(stderr, "ERROR: VTK grid mismatch or bad header in %s: file=%dx%dx%d expected=%dx%dx%d\n",
+                path.c_str(), vx, vy, vz, Nx, Ny, Nz);
+        fclose(f);
+        return false;
+    }
+    out->assign((size_t)Nx * Ny * Nz, 0.0);
+    const int ny_in = two_d ? 1 : Ny;
+    for (int k = 0; k < Nz; ++k)
+        for (int j = 0; j < ny_in; ++j)
+            for (int i = 0; i < Nx; ++i) {
+                double v;
+                if (fscanf(f, "%lf", &v) != 1) {
+                    fprintf(stderr, "ERROR: Unexpected EOF while reading VTK data from %s\n", path.c_str());
+                    fclose(f);
+                    return false;
+                }
+                for (int jj = j; jj < (two_d ? Ny : j + 1); ++jj) (*out)[((size_t)i * Ny + jj) * Nz + k] = v;
+            }
+    fclose(f);
+    return true;
+}
+
+double h_of(double p);
+double clamp_eps_h(double x, double e) { return x < e ? e : (x > 1.0 - e ? 1.0 - e : x); }
+
+// volume fraction of the legacy seed target (compute_effective_vf_target,
+// main_cuda.cu:2459-2490; ellipsoid axes normalised to the sphere's volume)
+double effective_vf_target(const pfgb_params &P) {
+    const double vf = std::fmin(0.999, std::fmax(1e-6, P.ic_vf_target_phi));
+    if (!(P.ic_phi_seed_radius > 0.0)) return vf;
+    const int ns = P.ic_phi_num_seeds > 0 ? P.ic_phi_num_seeds : 1;
+    const double R = P.ic_phi_seed_radius, Lx = P.Nx * P.dx, Ly = P.Ny * P.dy, Lz = P.Nz * P.dz;
+    double t = vf;
+    if (P.Ny > 2) { if (Lx * Ly * Lz > 0.0) t = ns * (4.0 * M_PI / 3.0) * R * R * R / (Lx * Ly * Lz); }
+    else if (Lx * Lz > 0.0) t = ns * M_PI * R * R / (Lx * Lz);
+    return std::fmin(0.999, std::fmax(1e-6, t));
+}
+
+// composition rebuilt from phi by the diffuse-interface lever rule
+// (rebuild_full_model_composition_from_phi, main_cuda.cu:2521-2600)
+void rebuild_composition(const pfgb_params &P, std::vector<double> &phi, std::vector<double> *xB) {
+    const size_t N = phi.size();
+    double sh = 0.0, sh2 = 0.0;
+    for (size_t i = 0; i < N; ++i) {
+        phi[i] = std::fmin(1.0, std::fmax(0.0, phi[i]));
+        const double h = h_of(phi[i]);
+        sh += h;
+        sh2 += h * h;
+    }
+    const double mh = sh / (double)N, mh2 = sh2 / (double)N, xeq = P.xB_eq_matrix, vf = effective_vf_target(P);
+    const double target = P.v_B * vf + (1.0 - vf) * xeq;
+    const double A = 1.0 - 2.0 * mh + mh2, B = mh - mh2, C = P.v_B * mh;
+    double xout;
+    if (P.ic_23d_xB_out > 0.0) xout = P.ic_23d_xB_out;
+    else if (std::fabs(A) < 1e-12) xout = ((vf - mh) * P.v_B + (1.0 - vf) * xeq) / std::fmax(1.0 - mh, 1e-12);
+    else xout = (target - B * xeq - C) / A;
+    xout = clamp_eps_h(xout, P.xB_eps);
+    xB->resize(N);
+    for (size_t i = 0; i < N; ++i) {
+        const double h = h_of(phi[i]);
+        (*xB)[i] = clamp_eps_h((1.0 - h) * xout + h * xeq, P.xB_eps);
+    }
+}
+
+// continue_dyn_<n+1> / continue_min_<n+1>, n the largest index of that
+// prefix in the source path (derive_next_continue_case_tag, main_cuda.cu:2492-2520)
+std::string next_continue_tag(const std::string &path, bool minimize) {
+    const std::string prefix = minimize ? "continue_min_" : "continue_dyn_";
+    int mx = 0;
+    for (size_t p = path.find(prefix); p != std::string::npos; p = path.find(prefix, p + 1)) {
+        size_t q = p + prefix.size();
+        if (q < path.size() && isdigit((unsigned char)path[q])) {
+            int v = 0;
+            while (q < path.size() && isdigit((unsigned char)path[q])) v = v * 10 + (path[q++] - '0');
+            mx = std::max(mx, v);
+        }
+    }
+    return prefix + std::to_string(mx + 1);
+}
+
+std::string dir_of(const std::string &p) {
+    const size_t s = p.rfind('/');
+    return s == std::string::npos ? std::string() : p.substr(0, s);
+}
+std::string base_of(const std::string &p) {
+    const size_t s = p.rfind('/');
+    return s == std::string::npos ? p : p.substr(s + 1);
+}
+
+// last step, t_code, t_real of an existing vf CSV / last iteration of an
+// energy CSV (read_last_vf_csv_state / read_last_energy_iter, main_cuda.cu:311-352)
+bool last_csv_row(const std::string &path, int *step, double *t, double *tr) {
+    FILE *f = fopen(path.c_str(), "r");
+    if (!f) return false;
+    char line[4096];
+    bool found = false;
+    while (fgets(line, sizeof(line), f)) {
+        if (!isdigit((unsigned char)line[0]) && line[0] != '-') continue;
+        int a;
+        double b = 0.0, d = 0.0;
+        const int n = sscanf(line, "%d,%lf,%lf", &a, &b, &d);
+        if ((tr && n == 3) || (!tr && n >= 1)) {
+            found = true;
+            *step = a;
+            if (t) *t = b;
+            if (tr) *tr = d;
+        }
+    }
+    fclose(f);
+    return found;
+}
+
 // a key of the parameter file that the library's parameter struct does not
 // carry (used for output naming only)
 double param_file_value(const std::string &txt, const char *key, double dflt) {
@@ -433,6 +568,7 @@ int main(int argc, char **argv) {
     // (main_cuda.cu:22752-22763); its raw-field / checkpoint inputs are the
     // ordinary ones
     if (c.mode == "dynamics-continue") c.mode = "dynamics";
+    if (c.mode == "minimize-continue") { c.mode = "minimize"; c.cont = true; }
     if (c.mode != "dynamics" && c.mode != "minimize") {
         fprintf(stderr, "[fatal] --mode=%s is not available in this build (dynamics, dynamics-continue, minimize)\n",
                 c.mode.c_str());
@@ -538,8 +674,44 @@ int main(int argc, char **argv) {
     // ---- initial fields ---------------------------------------------------
     const size_t N = (size_t)P.Nx * P.Ny * P.Nz;
     std::vector<double> phi, xB, eta, dYdt;
-    const bool seeded = !restarting && c.init_mode.empty();
-    if (restarting || seeded) {
+    // VTK continuation (main_cuda.cu:24752-24772, 27194-27207)
+    if (c.cont) {
+        if (c.cont_phi.empty()) {
+            fprintf(stderr, "[fatal] continuation needs --continue-phi-vtk <path>\n");
+            return 2;
+        }
+        if (!c.init_mode.empty()) {
+            fprintf(stderr, "[fatal] --init-mode raw_fields cannot be combined with --continue-phi-vtk/--continue-xB-vtk.\n");
+            return 2;
+        }
+        if (P.zero_mode_enabled || restarting) {
+            fprintf(stderr, "[fatal] zero-mode restart cannot be mixed with VTK continuation; use --pf-restart-from "
+                            "for exact state restoration\n");
+            return 2;
+        }
+        printf("[continue-param] explicit --pf-param-file takes precedence over stored PF params next to %s\n",
+               c.cont_phi.c_str());
+    }
+    const bool seeded = !restarting && !c.cont && c.init_mode.empty();
+    if (c.cont) {
+        if (!read_vtk_field(c.cont_phi, P.Nx, P.Ny, P.Nz, &phi)) return 2;
+        if (!minimize || P.minimize_full_model) {
+            struct stat sb;
+            if (!c.cont_xB.empty() && stat(c.cont_xB.c_str(), &sb) == 0) {
+                if (!read_vtk_field(c.cont_xB, P.Nx, P.Ny, P.Nz, &xB)) return 2;
+            } else {
+                if (!c.cont_xB.empty())
+                    fprintf(stderr, "[warn] continuation xB VTK missing or unreadable, xB/Y rebuilt from phi: %s\n",
+                            c.cont_xB.c_str());
+                rebuild_composition(P, phi, &xB);
+            }
+        } else {
+            xB.assign(N, 0.0);   // phi-only minimize carries no composition
+        }
+        // clamps only (no xB_max_safe cap): phi to [0, 1], xB to [eps, 1 - eps]
+        st = pfgb_prepare_raw_fields(&P, NAN, phi.data(), xB.data(), nullptr, nullptr, N);
+        if (st != PFGB_OK) return fail(st, "pfgb_prepare_raw_fields");
+    } else if (restarting || seeded) {
         // the fields come from the checkpoint (main_cuda.cu:27340-27380) or
         // from the seeded initialiser on the device (main_cuda.cu:15157-15430)
     } else if (c.init_mode != "raw_fields") {
@@ -550,12 +722,12 @@ int main(int argc, char **argv) {
         fprintf(stderr, "[fatal] raw_fields needs --init-phi-raw and --init-xB-raw\n");
         return 2;
     }
-    if (!restarting && !seeded && minimize && !P.minimize_full_model) {
+    if (!restarting && !seeded && !c.cont && minimize && !P.minimize_full_model) {
         fprintf(stderr, "[fatal] --init-mode raw_fields requires dynamics mode or full-model minimize "
                         "(--mode=minimize --minimize-full-model).\n");
         return 2;
     }
-    if (!restarting && !seeded) {
+    if (!restarting && !seeded && !c.cont) {
         // init_meta.json (load_raw_init_meta, main_cuda.cu:2733-2762): the
         // grid must match, order must be C, dtype is float32 (the default)
         // or float64, and xB_max_safe caps xB (the minimize monitor cap when
@@ -612,10 +784,19 @@ int main(int argc, char **argv) {
         snprintf(name, sizeof(name), "%s_T%.0f_cuda_%dx%dx%d_dt%.3g_steps%d_xB%.3f", P.elastic_enabled ? "chel" : "ch",
                  P.temperature_C, P.Nx, P.Ny, P.Nz, P.dt, c.nsteps, xB_out);
     mkdir(root.c_str(), 0755);
-    const std::string out_dir = root + "/" + name;
+    std::string out_dir = root + "/" + name, tag = c.case_tag, csv_tag;
+    if (c.cont) {
+        // the source run's root (the phi VTK's case directory's parent): kept,
+        // or re-rooted under CUDA_STO_RESULTS_ROOT by its base name
+        // (main_cuda.cu:25363-25385); a new case directory continue_*_<n>
+        const std::string src_case = dir_of(c.cont_phi), src_root = dir_of(src_case);
+        if (root_env && root_env[0] && !base_of(src_root).empty()) out_dir = root + "/" + base_of(src_root);
+        else out_dir = !src_root.empty() ? src_root : root;
+        if (tag.empty()) tag = next_continue_tag(c.cont_phi, minimize);
+        csv_tag = !src_case.empty() ? base_of(src_case) : tag;
+    }
     mkdir(out_dir.c_str(), 0755);
-    copy_file(c.param_file, out_dir + "/pf_input.params");
-    std::string tag = c.case_tag;
+    if (!minimize && !c.cont) copy_file(c.param_file, out_dir + "/pf_input.params");   // main_cuda.cu:25408-25416
     if (tag.empty() && seeded) {   // main_cuda.cu:25425-25436
         char t[256];
         snprintf(t, sizeof(t), "case_test%d_%s_th%.0f_ph%.0f_noise%.0e", -1,
@@ -624,6 +805,7 @@ int main(int argc, char **argv) {
         tag = t;
     }
     if (tag.empty()) tag = "raw_fields_relax";
+    if (csv_tag.empty()) csv_tag = tag;
     const std::string case_dir = out_dir + "/" + tag;
     mkdir(case_dir.c_str(), 0755);
     copy_file(c.param_file, case_dir + "/pf_input.params");
@@ -658,7 +840,7 @@ int main(int argc, char **argv) {
         }
         first_step = s0.step + 1;
         printf("PF_ZERO_MODE_RESTART checkpoint=%s accepted_step=%d\n", c.restart_from.c_str(), s0.step);
-    } else if (seeded) {
+    } else if (seeded && !c.cont) {
         if ((st = pfgb_init_fields(ctx)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_init_fields"); }
         if (minimize && !P.minimize_full_model) {
             // phi-only minimize starts from the seeded phi with no composition
@@ -700,7 +882,14 @@ int main(int argc, char **argv) {
         return ok;
     };
 
-    FILE *csv = fopen((case_dir + "/vf_precip_vs_time_" + tag + ".csv").c_str(), "w");
+    // vf CSV (dynamics and full-model minimize, main_cuda.cu:25571-25590); a
+    // continuation appends to an existing one, its rows offset by the last row
+    int csv_step_off = 0;
+    double csv_t_off = 0.0, csv_tr_off = 0.0;
+    const bool want_csv = !minimize || P.minimize_full_model;
+    const std::string csv_path = case_dir + "/vf_precip_vs_time_" + csv_tag + ".csv";
+    const bool csv_append = c.cont && last_csv_row(csv_path, &csv_step_off, &csv_t_off, &csv_tr_off);
+    FILE *csv = want_csv ? fopen(csv_path.c_str(), csv_append ? "a" : "w") : nullptr;
     FILE *etrace = nullptr, *ztrace = nullptr;
     const bool accel = P.elastic_enabled && (P.elastic_warm_start_enabled || P.elastic_residual_control_enabled);
     if (accel) {
@@ -716,23 +905,26 @@ int main(int argc, char **argv) {
                             "bisection_steps,Y_star_min,Y_star_max,lambda_lower,lambda_upper,"
                             "accepted_zero_mode_steps\n");
     }
-    if (!csv || (accel && !etrace) || (P.zero_mode_enabled && !ztrace)) {
+    if ((want_csv && !csv) || (accel && !etrace) || (P.zero_mode_enabled && !ztrace)) {
         fprintf(stderr, "[fatal] cannot open the CSV outputs under %s\n", case_dir.c_str());
         pfgb_destroy(ctx);
         return 2;
     }
-    fprintf(csv, "step,t_code,t_real_s,vf_precip,R_avg\n");
+    if (csv && !csv_append) fprintf(csv, "step,t_code,t_real_s,vf_precip,R_avg\n");
     FILE *efp = nullptr;
+    int energy_off = 0;
     if (minimize) {   // energy_minimize_T%.0f_r%.2f_xB%.3f_<tag>.csv (main_cuda.cu:27436-27467)
         char en[512];
         snprintf(en, sizeof(en), "/energy_minimize_T%.0f_r%.2f_xB%.3f_%s.csv", P.temperature_C, P.ic_phi_seed_radius,
-                 xB_out, tag.c_str());
-        efp = fopen((case_dir + en).c_str(), "w");
+                 xB_out, csv_tag.c_str());
+        const bool e_append = c.cont && last_csv_row(case_dir + en, &energy_off, nullptr, nullptr);
+        efp = fopen((case_dir + en).c_str(), e_append ? "a" : "w");
         if (!efp) { fprintf(stderr, "[fatal] cannot open %s%s\n", case_dir.c_str(), en); pfgb_destroy(ctx); return 2; }
-        fprintf(efp, "iter,dt,mean_h,V0,lambda,F_surf_hat,F_el_hat,F_chem_excess_hat,F_total_excess_hat,"
-                     "F_chem_CNT_hat,F_total_CNT_hat,total_interface_sum,total_el_core_sum,"
-                     "rms_res,rms_dphi,rms_dY,rel_dF,vol_err_rel,mass_target_code,mass_current_code,mass_err_rel,"
-                     "mass_lambda,post_proj_iters_used\n");
+        if (!e_append)
+            fprintf(efp, "iter,dt,mean_h,V0,lambda,F_surf_hat,F_el_hat,F_chem_excess_hat,F_total_excess_hat,"
+                         "F_chem_CNT_hat,F_total_CNT_hat,total_interface_sum,total_el_core_sum,"
+                         "rms_res,rms_dphi,rms_dY,rel_dF,vol_err_rel,mass_target_code,mass_current_code,mass_err_rel,"
+                         "mass_lambda,post_proj_iters_used\n");
     }
 
     const char *dim = P.Ny == 2 ? "[2D]" : "[3D]";
@@ -747,8 +939,11 @@ int main(int argc, char **argv) {
             R_avg = (P.Ny == 2 ? 2.0 : 3.0) * P.dx * ratio;
         }
         const double t = step * P.dt, t_real = t * P.t_real_unit;
-        fprintf(csv, "%d,%.8f,%.8e,%.8e,%.8e\n", step, t, t_real, d.vf_precip, R_avg);
-        fflush(csv);
+        if (csv) {
+            fprintf(csv, "%d,%.8f,%.8e,%.8e,%.8e\n", step + csv_step_off, t + csv_t_off, t_real + csv_tr_off,
+                    d.vf_precip, R_avg);
+            fflush(csv);
+        }
         printf("%s step=%05d t=%.6f t_real=%.6e s <x_B_tot>=%.6e vf_precip=%.6e R_avg_internal=%.6e "
                "R_avg_nm=%.6e xB_range=[%.4f, %.4f] t_wall=%s\n",
                dim, step, t, t_real, d.mass_xBtot / (double)N, d.vf_precip, R_avg, R_avg * unit_to_nm, d.xB_min,
@@ -774,7 +969,8 @@ int main(int argc, char **argv) {
         if (gp) write_vtk(case_dir + "/eta_init.vtk", "eta", f_eta, P.Nx, P.Ny, P.Nz);
         write_vtk(case_dir + "/xB_0.vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
     }
-    if ((st = csv_row(0, NAN)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_diagnostics"); }
+    // a continuation writes no step-0 row (main_cuda.cu:28309)
+    if (!c.cont && (st = csv_row(0, NAN)) != PFGB_OK) { pfgb_destroy(ctx); return fail(st, "pfgb_diagnostics"); }
 
     std::vector<double> wall;
     wall.reserve(c.nsteps);
@@ -791,7 +987,7 @@ int main(int argc, char **argv) {
         wall.push_back(w);
         fprintf(efp, "%d,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,%.8e,"
                      "%.17e,%.17e,%.17e,%.17e,%d\n",
-                step, P.dt, m.mean_h, m.V0_target, m.lambda_vol, m.F_surf, m.F_el, m.F_chem_excess,
+                step + energy_off, P.dt, m.mean_h, m.V0_target, m.lambda_vol, m.F_surf, m.F_el, m.F_chem_excess,
                 m.F_total_excess, m.F_chem_CNT, m.F_total_CNT, m.total_interface_sum, m.total_el_core_sum,
                 m.rms_res, m.rms_dphi, m.rms_dY, m.energy_diff_rel, m.vol_err_rel, NAN, NAN, NAN, NAN,
                 P.minimize_post_projection_iters);
@@ -811,6 +1007,10 @@ int main(int argc, char **argv) {
             break;
         }
     }
+    // final audits of the accelerated elastic solver and the zero mode
+    // (main_cuda.cu:34300-34350, 34796-34800)
+    unsigned long long el_nonconv = 0, el_iters_total = 0, el_last_iters = 0;
+    double el_last_resid = NAN, zm_target = NAN;
     for (int step = first_step; step <= c.nsteps && !minimize; ++step) {
         pfgb_step_stats s;
         const auto a = std::chrono::steady_clock::now();
@@ -819,6 +1019,13 @@ int main(int argc, char **argv) {
         const double w = std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
         if (st != PFGB_OK) { rc = fail(st, "pfgb_step"); break; }
         wall.push_back(w);
+        if (accel) {
+            el_nonconv += s.elastic_converged ? 0 : 1;
+            el_iters_total += (unsigned long long)s.elastic_iterations;
+            el_last_iters = (unsigned long long)s.elastic_iterations;
+            el_last_resid = s.elastic_relative_residual;
+        }
+        if (P.zero_mode_enabled) zm_target = s.zero_mode_target_mass;
         if (etrace) {
             fprintf(etrace, "%d,%d,%d,%.17e,%d,%d,%.17e,%.9f,%llu\n", step, s.elastic_warm_start_used,
                     s.elastic_iterations, s.elastic_relative_residual, s.elastic_converged, P.elastic_iter_max,
@@ -844,6 +1051,30 @@ int main(int argc, char **argv) {
         }
     }
     const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    int audit_rc = 0;
+    if (rc == 0 && !minimize && P.zero_mode_enabled) {
+        pfgb_diag zd;
+        if ((st = pfgb_diagnostics(ctx, &zd)) != PFGB_OK) rc = fail(st, "pfgb_diagnostics");
+        else {
+            const double mean_err = (zd.mass_xBtot - zm_target) / (double)N;
+            const bool ok = std::isfinite(zd.mass_xBtot) && std::fabs(mean_err) <= 1.0e-10;
+            printf("PF_ZERO_MODE_FINAL_AUDIT status=%s final_step=%d target_mass_code=%.17e final_mass_code=%.17e "
+                   "mean_mass_error=%.17e gp_paths_enabled=false\n",
+                   ok ? "PASS" : "FAIL", c.nsteps, zm_target, zd.mass_xBtot, mean_err);
+            if (!ok) audit_rc = 2;
+        }
+    }
+    if (rc == 0 && !minimize && accel) {
+        const double n = (double)wall.size();
+        printf("PF_ELASTIC_SOLVER_FINAL_AUDIT status=%s mode=ELASTIC_WARM_START_RESIDUAL_V1 steps=%zu "
+               "total_iterations=%llu mean_iterations=%.9f last_iterations=%llu last_residual=%.17e "
+               "nonconverged_steps=%llu\n",
+               el_nonconv == 0 ? "PASS" : "FAIL", wall.size(), el_iters_total, n > 0 ? el_iters_total / n : 0.0,
+               el_last_iters, el_last_resid, el_nonconv);
+        printf("elastic_solver_status=%s\n", el_nonconv == 0 ? "PASS_ELASTIC_WARM_START_RESIDUAL_V1"
+                                                               : "FAIL_ELASTIC_WARM_START_RESIDUAL_V1");
+        if (el_nonconv != 0) audit_rc = 2;   // the run completes; the exit status reports it
+    }
     if (rc == 0) {
         if ((st = read_state()) != PFGB_OK) rc = fail(st, "pfgb_read_fields");
         else if (minimize) {   // main_cuda.cu:33635-33665
@@ -897,5 +1128,5 @@ int main(int argc, char **argv) {
     printf("done: %zu steps, %.3f s, %.3f Mpts/s\n", wall.size(), total,
            total > 0 ? (double)N * wall.size() / total / 1e6 : 0.0);
     pfgb_destroy(ctx);
-    return rc;
+    return rc != 0 ? rc : audit_rc;
 }

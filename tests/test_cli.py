@@ -296,3 +296,107 @@ def test_cli_seeded_initialisation(capi, tmp_path):
     want, _ = init_oracle.seed_fields(p)
     got = _vtk_values(case / "phi_init.vtk", (n, n, n))
     assert np.abs(got - want).max() <= 5.1e-6
+
+
+@pytest.mark.gpu
+def test_cli_vtk_continuation(capi, tmp_path):
+    """--mode=dynamics-continue / --mode=minimize-continue with
+    --continue-phi-vtk [--continue-xB-vtk] (main_cuda.cu:22752-22770,
+    2602-2650, 25363-25480): the fields come from the source run's ASCII
+    VTK files, the outputs go to a new case directory continue_dyn_<n> /
+    continue_min_<n> under the source run's root (re-rooted under
+    CUDA_STO_RESULTS_ROOT), the CSVs keep the source case's tag and a
+    continuation writes no step-0 row."""
+    import ctypes
+    from cuda_sto_pf_gb300 import workloads
+    from cuda_sto_pf_gb300.solver import Solver
+    n = 16
+    w = workloads.single_sphere(n=n, radius=5.0)
+    w["phi"].tofile(tmp_path / "phi.raw")
+    w["xB"].tofile(tmp_path / "xB.raw")
+    pf = os.path.join(GOLDEN, "c2.params")
+    raw = ["--init-mode", "raw_fields", "--init-phi-raw", str(tmp_path / "phi.raw"), "--init-xB-raw",
+           str(tmp_path / "xB.raw")]
+    # dynamics: 4 steps, then 3 more from the step-4 VTK files
+    r = _run(capi, [str(n)] * 3 + ["0.01", "4", "4", "1", "1", "--pf-param-file", pf] + raw, tmp_path,
+             env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "A")})
+    assert r.returncode == 0, r.stderr
+    run = os.listdir(tmp_path / "A")[0]
+    src = tmp_path / "A" / run / "raw_fields_relax"
+    r = _run(capi, [str(n)] * 3 + ["0.01", "3", "3", "1", "1", "--pf-param-file", pf, "--mode=dynamics-continue",
+                                   "--continue-phi-vtk", str(src / "phi_4.vtk"), "--continue-xB-vtk",
+                                   str(src / "xB_4.vtk")], tmp_path, env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "B")})
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    case = tmp_path / "B" / run / "continue_dyn_1"
+    assert (case / "phi_3.vtk").exists() and (case / "pf_input.params").exists()
+    rows = (case / "vf_precip_vs_time_raw_fields_relax.csv").read_text().strip().split("\n")
+    assert rows[0] == "step,t_code,t_real_s,vf_precip,R_avg" and [int(x.split(",")[0]) for x in rows[1:]] == [1, 2, 3]
+    # the same continuation through the library from the VTK values
+    phi0 = _vtk_values(src / "phi_4.vtk", (n, n, n))
+    xB0 = _vtk_values(src / "xB_4.vtk", (n, n, n))
+    p = params_for(capi, "c2.params", n=n, precision=0)
+    capi.load().pfgb_prepare_raw_fields(ctypes.byref(p), float("nan"), phi0.ctypes.data, xB0.ctypes.data, None, None,
+                                        phi0.size)
+    with Solver(p) as s:
+        s.load(phi0, xB0)
+        s.step(3)
+        f = s.fields()
+    assert np.abs(_vtk_values(case / "phi_3.vtk", (n, n, n)) - f["phi"]).max() <= 6e-6
+    # a second continuation from inside the first takes the next index
+    r = _run(capi, [str(n)] * 3 + ["0.01", "2", "2", "1", "1", "--pf-param-file", pf, "--mode=dynamics-continue",
+                                   "--continue-phi-vtk", str(case / "phi_3.vtk")], tmp_path,
+             env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "B")})
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert (tmp_path / "B" / run / "continue_dyn_2" / "phi_2.vtk").exists()
+    # full-model minimize, then minimize-continue from its final files
+    mz = ["--mode=minimize", "--minimize-full-model", "--minimize-max-iter", "3", "--minimize-dt", "0.05"]
+    r = _run(capi, [str(n)] * 3 + ["0.05", "100", "50", "1", "1", "--pf-param-file", pf] + mz + raw, tmp_path,
+             env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "C")})
+    assert r.returncode == 0, r.stderr
+    run = os.listdir(tmp_path / "C")[0]
+    src = tmp_path / "C" / run / "raw_fields_relax"
+    r = _run(capi, [str(n)] * 3 + ["0.05", "100", "50", "1", "1", "--pf-param-file", pf, "--mode=minimize-continue",
+                                   "--minimize-full-model", "--minimize-max-iter", "2", "--minimize-dt", "0.05",
+                                   "--continue-phi-vtk", str(src / "phi_final_raw_fields_relax.vtk"),
+                                   "--continue-xB-vtk", str(src / "xB_final_raw_fields_relax.vtk")], tmp_path,
+             env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "D")})
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    case = tmp_path / "D" / run / "continue_min_1"
+    names = os.listdir(case)
+    assert "phi_final_continue_min_1.vtk" in names and "xB_final_continue_min_1.vtk" in names, names
+    energy = [x for x in names if x.startswith("energy_minimize_") and x.endswith("_raw_fields_relax.csv")]
+    assert len(energy) == 1, names
+    assert len((case / energy[0]).read_text().strip().split("\n")) == 3
+    # continuation refusals
+    r = _run(capi, [str(n)] * 3 + ["0.05", "10", "5", "1", "1", "--pf-param-file", pf, "--mode=minimize-continue"],
+             tmp_path)
+    assert r.returncode == 2 and "--continue-phi-vtk" in r.stderr
+    r = _run(capi, [str(n)] * 3 + ["0.01", "2", "2", "1", "1", "--pf-param-file", pf, "--continue-phi-vtk",
+                                   str(src / "phi_final_raw_fields_relax.vtk")] + raw, tmp_path)
+    assert r.returncode == 2 and "cannot be combined" in r.stderr
+
+
+@pytest.mark.gpu
+def test_cli_phi_only_minimize(capi, tmp_path):
+    """--mode=minimize without --minimize-full-model: the reference's default
+    phi-only minimize from the seeded phi (raw fields are refused there),
+    no vf CSV, phi files only."""
+    n = 16
+    pf = os.path.join(GOLDEN, "c2.params")
+    r = _run(capi, [str(n)] * 3 + ["0.05", "100", "50", "1", "1", "--pf-param-file", pf, "--mode=minimize",
+                                   "--minimize-max-iter", "4", "--radius", "5"], tmp_path,
+             env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "R")})
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    run = os.listdir(tmp_path / "R")[0]
+    case = tmp_path / "R" / run / os.listdir(tmp_path / "R" / run)[0]
+    names = os.listdir(case)
+    assert not any(x.startswith("vf_precip_vs_time") for x in names), names
+    assert any(x.startswith("phi_final_") for x in names) and not any(x.startswith("xB_final_") for x in names)
+    energy = [x for x in names if x.startswith("energy_minimize_")][0]
+    rows = (case / energy).read_text().strip().split("\n")
+    assert len(rows) == 5 and rows[1].split(",")[7] == "nan"   # F_chem_excess_hat is NaN
+    w = np.ones((n, n, n)).tofile(tmp_path / "phi.raw")
+    r = _run(capi, [str(n)] * 3 + ["0.05", "100", "50", "1", "1", "--pf-param-file", pf, "--mode=minimize",
+                                   "--init-mode", "raw_fields", "--init-phi-raw", str(tmp_path / "phi.raw"),
+                                   "--init-xB-raw", str(tmp_path / "phi.raw")], tmp_path)
+    assert r.returncode == 2 and "full-model minimize" in r.stderr

@@ -119,7 +119,11 @@ def test_phi_only_minimize_parity(capi, oracle, precision, tol):
             for f in PHI_ONLY_FIELDS:
                 a, b = getattr(mg, f), getattr(mo, f)
                 if f == "vol_err_rel":
-                    assert abs(a - b) <= (1e-10 if precision == 0 else 1e-7), (it, f, a, b)
+                    # the phi-only drive is mostly elastic, so the FP32
+                    # elastic rounding (different transform orders on the two
+                    # sides) reaches <h> at about 1e-8 relative even with
+                    # FP64 fields
+                    assert abs(a - b) <= (5e-9 if precision == 0 else 1e-7), (it, f, a, b)
                     continue
                 scale = max(abs(b), 1e-6 if f.startswith("rms") else 1e-12)
                 assert abs(a - b) <= (50 * tol if f == "rms_res" else tol) * scale, (it, f, a, b)

@@ -182,18 +182,24 @@ def _compare(ref, ours, keys):
     return {k: rel_l2(ours[k], ref[k]) for k in keys}
 
 
-def _zero_mode_case(capi, ref_main, tmp_path, name, base, extra, fields, n, steps, xB_max_safe):
+def _zero_mode_case(capi, ref_main, tmp_path, name, base, extra, fields, n, steps, xB_max_safe, ref_rc=0):
     """Run the reference and this repository's main_cuda with one command
-    line, and the library in FP32; compare the checkpointed fields."""
+    line, and the library in FP32; compare the checkpointed fields.  ref_rc:
+    the reference's expected exit status (2 when its elastic solver misses
+    the tolerance on some step: the run completes, checkpoints included, and
+    its final audit fails, main_cuda.cu:34796-34800)."""
     d = str(tmp_path)
     paths = _write_inputs(os.path.join(d, "in"), fields, n, xB_max_safe)
     pf = _params_file(d, base, extra)
     ck_ref, ck_ours = os.path.join(d, "ref.ckpt"), os.path.join(d, "ours.ckpt")
     r = _run(ref_main, _argv(n, steps, steps, pf, paths, True, ck_ref), os.path.join(d, "R_ref"))
-    assert r.returncode == 0, "reference main_cuda failed:\n" + r.stdout[-3000:] + r.stderr[-3000:]
+    assert r.returncode == ref_rc, "reference main_cuda:\n" + r.stdout[-3000:] + r.stderr[-3000:]
     from cuda_sto_pf_gb300 import build
     o = _run(build.EXE, _argv(n, steps, steps, pf, paths, True, ck_ours), os.path.join(d, "R_ours"))
-    assert o.returncode == 0, o.stdout[-3000:] + o.stderr[-3000:]
+    if ref_rc == 0:
+        assert o.returncode == 0, o.stdout[-3000:] + o.stderr[-3000:]
+    else:   # judged below from the elastic trace
+        assert o.returncode in (0, 2), o.stdout[-3000:] + o.stderr[-3000:]
     ref = _read_ckpt(capi, ck_ref, n)
     cli = _read_ckpt(capi, ck_ours, n)
     f32, st32 = _library_fields(capi, base, n, extra, fields, xB_max_safe, steps, 1, True)
@@ -256,7 +262,8 @@ def _compare_outputs(cr, co, name, rec):
         assert er.shape[0] == eo.shape[0]
         rec["elastic_iters_ref"] = [int(x) for x in er[:, 2]]
         rec["elastic_iters_ours"] = [int(x) for x in eo[:, 2]]
-        assert np.abs(er[:, 2] - eo[:, 2]).max() <= 1, (name, rec)
+        if "tol1e-8" not in name:
+            assert np.abs(er[:, 2] - eo[:, 2]).max() <= 1, (name, rec)
 
 
 def test_c1_sphere_homogeneous_100_steps(capi, ref_main, tmp_path):
@@ -289,16 +296,35 @@ def test_c1_uncapped_composition_fails_closed_in_both(capi, ref_main, tmp_path):
     assert not os.path.exists(os.path.join(d, "ref.ckpt")) and not os.path.exists(os.path.join(d, "ours.ckpt"))
 
 
+def _c2_like_fields():
+    from cuda_sto_pf_gb300 import workloads
+    w = workloads.ellipsoid_population(n=64, count=8, eta_sites=0, seed=11)
+    return {"phi": w["phi"], "xB": w["xB"]}
+
+
 def test_two_phase_heterogeneous_elasticity(capi, ref_main, tmp_path):
     """C2's physics at 64^3 (two_phase, since the reference refuses the zero
     mode with gp_zone): 8 ellipsoids with log-normal radii, heterogeneous
-    stiffness S_p = C_Ag2Te - C_PbTe, elastic tolerance 1e-8 without the
-    fail-closed rule, 30 steps, the loader's default composition cap."""
-    from cuda_sto_pf_gb300 import workloads
-    w = workloads.ellipsoid_population(n=64, count=8, eta_sites=0, seed=11)
+    stiffness S_p = C_Ag2Te - C_PbTe, the reference's default elastic
+    tolerance 1e-6, 30 steps, the loader's default composition cap."""
+    _zero_mode_case(capi, ref_main, tmp_path, "c2_two_phase_64_30_tol1e-6", "c2.params", {}, _c2_like_fields(),
+                    64, 30, 0.07)
+
+
+def test_two_phase_heterogeneous_tolerance_1e8(capi, ref_main, tmp_path):
+    """The same case at C2's elastic tolerance 1e-8 without the fail-closed
+    rule.  The reference's iteration u <- Phi(u) with FP32 elastic fields
+    levels off near 5e-8 and runs every step into the 32-update cap: it
+    completes the run and exits 2 with its elastic audit FAIL.  This
+    repository's default increment form reaches 1e-8 on every step (audit
+    PASS, exit 0); the fields of both agree within the field tolerance."""
     extra = {"elastic_residual_tolerance": "1e-8", "elastic_fail_on_nonconvergence": "0"}
-    _zero_mode_case(capi, ref_main, tmp_path, "c2_two_phase_64_30", "c2.params", extra,
-                    {"phi": w["phi"], "xB": w["xB"]}, 64, 30, 0.07)
+    rec = _zero_mode_case(capi, ref_main, tmp_path, "c2_two_phase_64_30_tol1e-8", "c2.params", extra,
+                          _c2_like_fields(), 64, 30, 0.07, ref_rc=2)
+    # every reference step at the cap; ours converged on every warm step (the
+    # cold first step's increment is most of u and may meet the FP32 floor)
+    assert min(rec["elastic_iters_ref"]) == 32, rec["elastic_iters_ref"]
+    assert max(rec["elastic_iters_ours"][1:]) < 32, rec["elastic_iters_ours"]
 
 
 def test_gp_zone_heterogeneous_vtk(capi, ref_main, tmp_path):
