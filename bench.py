@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-chebyshev", action="store_true", help="the reference's plain elastic iteration")
     ap.add_argument("--no-extrapolate", action="store_true",
                     help="start each elastic solve from the previous solution (the reference's warm start)")
+    ap.add_argument("--fft-tensor-cores", type=int, default=None,
+                    help="1: the 41-point stage of the elastic y passes on the tensor cores (default: FFT_TENSOR_CORES)")
     ap.add_argument("--profile-json", default="")
     ap.add_argument("--fno-n", type=int, default=128)
     ap.add_argument("--fno-base", type=int, default=128, help="distinct generated microstructures")
@@ -82,6 +84,9 @@ CHEBYSHEV = 1
 # (same fixed point and stopping test, fewer iterations when the fields
 # move; --no-extrapolate: the reference's previous-solution start)
 EXTRAPOLATE = 1
+# the 41-point stage of the 246-point transforms on the tensor cores
+# (split-precision TF32); --fft-tensor-cores overrides
+FFT_TENSOR_CORES = 0
 
 
 def make_params(capi, n, precision, tol, shape=None, chebyshev=None):
@@ -96,6 +101,7 @@ def make_params(capi, n, precision, tol, shape=None, chebyshev=None):
     p.elastic_fail_on_nonconvergence = 0
     p.elastic_chebyshev = CHEBYSHEV if chebyshev is None else chebyshev
     p.elastic_warm_start_extrapolate = EXTRAPOLATE if chebyshev is None else 0
+    p.fft_tensor_cores = FFT_TENSOR_CORES if chebyshev is None else 0
     capi.finalize(p)
     return p
 
@@ -300,6 +306,9 @@ def compare_plain_fp64(args, capi, Solver, n, shape, fields, dev, stream, nsteps
 
 
 def run_ours(args):
+    global FFT_TENSOR_CORES
+    if args.fft_tensor_cores is not None:
+        FFT_TENSOR_CORES = args.fft_tensor_cores
     import torch
     ws, rank, local = dist_env()
     if ws > 1:
@@ -451,6 +460,8 @@ def run_ours(args):
                            else "plain (the reference's)",
                            "elastic_warm_start": "extrapolated from the last two solutions" if EXTRAPOLATE
                            else "previous solution (the reference's)",
+                           "dft41_stage": "tensor cores (tcgen05, split-precision TF32)" if FFT_TENSOR_CORES
+                           else "FP32 multiply-adds",
                            "l2": "inputs larger than L2 (working set > 1 GB at 246^3)",
                            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
                 "elastic_iters_per_step": sum(iters) / max(1, len(iters)),

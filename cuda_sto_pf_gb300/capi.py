@@ -48,7 +48,7 @@ class Params(Structure):
         ("elastic_residual_control_enabled", c_int32), ("elastic_iter_min", c_int32),
         ("elastic_iter_max", c_int32), ("elastic_fail_on_nonconvergence", c_int32),
         ("elastic_increment_form", c_int32), ("elastic_warm_start_extrapolate", c_int32),
-        ("elastic_chebyshev", c_int32), ("elastic_pad0", c_int32),
+        ("elastic_chebyshev", c_int32), ("fft_tensor_cores", c_int32),
         ("elastic_residual_tolerance", c_double), ("elastic_residual_absolute_floor", c_double),
         ("eps_iso_over_vB", c_double),
         ("eps00", c_double * 6), ("E0", c_double * 6),

@@ -26,6 +26,7 @@
 
 #include "fft.cuh"
 #include "fft246.cuh"
+#include "dft41_tc.cuh"
 #include "physics.cuh"
 
 const char *pfgb_error_buffer(void);
@@ -130,6 +131,11 @@ struct pfgb_ctx {
     // once the device has decided the solve), else null
     const double *skip = nullptr;
     int last_el_iters = 0;   // updates of the last solve: the first batch launched ahead
+    // tensor-core 41-point stage (fft_tensor_cores): its B table (hi | lo in
+    // the shared-memory layout of dft41_tc.cuh) and a device error word set
+    // when a bounded wait on the tensor core runs out
+    void *tc_btab = nullptr;
+    int *tc_err = nullptr;
 };
 
 // tag + algorithmic bytes of the next launch (set by the op-level wrappers)
@@ -1629,6 +1635,19 @@ k_zpass246(Grid3 g, const float2 *tw_g, Op op, const double *skip) {
 
 template <int DIR>
 static pfgb_status launch_y246(pfgb_ctx *c, const char *tag) {
+    if (c->tc_btab) {   // the 41-point stage on the tensor cores
+        const size_t smem = tc41::y_smem_bytes();
+        auto kern = k_y246tc<DIR>;
+        PFGB_CUDA_TRY(allow_smem(kern, smem));
+        AxisIO<float, 6, 6> io;
+        for (int i = 0; i < 6; ++i) { io.in[i] = (const float2 *)c->E[i]; io.out[i] = (float2 *)c->E[i]; }
+        dim3 grid((c->g.NzC + f246::TC - 1) / f246::TC, c->g.Nx);
+        ProfScope ps(c, {tag, 12.0 * (double)c->g.Nk * sizeof(float2)});
+        kern<<<grid, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][1], (const float4 *)c->tc_btab,
+                                                       io, c->skip, c->tc_err);
+        PFGB_CUDA_TRY(cudaGetLastError());
+        return PFGB_OK;
+    }
     const size_t smem = f246::axis_smem_bytes();
     auto kern = k_y246<DIR>;
     PFGB_CUDA_TRY(allow_smem(kern, smem));
@@ -1995,6 +2014,15 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
             batch = 2;
         }
         c->skip = nullptr;
+        if (c->tc_err) {   // a bounded wait of the tensor-core stage ran out
+            int te = 0;
+            PFGB_CUDA_TRY(cudaMemcpy(&te, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+            if (te) {
+                pfgb_set_error_msg("tensor-core 41-point stage: a wait for the MMA completion ran out at step %d",
+                                   c->step + 1);
+                return PFGB_ERR_TIMEOUT;
+            }
+        }
         iter = (int)c->hscal[DS_EL + 1];
         conv = c->hscal[DS_EL + 3] != 0.0;
         rel = c->hscal[3];
@@ -2364,7 +2392,7 @@ struct OpMinGradZ {
             d.mge[cell] = phi_rhs_phi_only<T, TE>(c, ec, p, e, sg);
         } else {
             const T xB = xB_of_Y<T>(c, d.Y[cell] + T(d.Yc));
-            d.mge[cell] = phi_rhs_sig<T, TE>(c, ec, p, T(0), xB, e, sg);
+            d.mge[cell] = phi_rhs_sig<T, TE>(c, ec, p, c.gp ? d.eta_old[cell] : T(0), xB, e, sg);
         }
         out[0] = p;
     }
@@ -2469,7 +2497,7 @@ k_min_energy(DevState<T, TE> d, PhysC c, ElasC<TE> ec, const T *phi, double g0, 
         const T xm = xB < T(c.xbcap) ? xB : T(c.xbcap);
         if (c.elastic) {
             TE e0[6];
-            eigenstrain<T, TE>(c, ec, p, T(0), clamp01(xm), false, e0);
+            eigenstrain<T, TE>(c, ec, p, c.gp ? d.eta_old[cell] : T(0), clamp01(xm), c.gp_el != 0, e0);
             double sd = 0.0;
 #pragma unroll
             for (int q = 0; q < 6; ++q)
@@ -2688,6 +2716,7 @@ static pfgb_status minimize_once(pfgb_ctx *c, pfgb_min_stats *ms) {
         DevState<T, TE> dy = d;
         dy.phi_old = pa;
         dy.phi_new = pb;
+        dy.eta_new = dy.eta_old;   // eta does not evolve in minimize (gp_zone)
         TRY((y_update<T, TE>(c, dy, &st)));
     }
     d = dev_state<T, TE>(c);   // same buffers, updated scalars
@@ -2846,6 +2875,36 @@ static pfgb_status upload_twiddles(pfgb_ctx *c, int axis, int n) {
     return PFGB_OK;
 }
 
+// B of the tensor-core 41-point stage (dft41_tc.cuh): B[n][j] for outputs
+// k = n + 1 and pairing index j, as TF32 high parts (round to nearest, ties
+// away, like cvt.rna) and the FP32 remainders, in the stage's shared-memory
+// byte layout: hi matrix, then lo matrix
+static uint32_t tf32_rna_bits(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    return (u + 0x1000u) & 0xFFFFE000u;
+}
+static pfgb_status upload_tc41_table(pfgb_ctx *c) {
+    std::vector<unsigned char> tab(2 * tc41::B_BYTES, 0);
+    for (int n = 0; n < tc41::NOUT; ++n)
+        for (int j = 0; j < tc41::K; ++j) {
+            const int k = n + 1;
+            const double v = j < 20 ? cos(2.0 * PFGB_PI * (double)(((j + 1) * k) % 41) / 41.0)
+                                    : sin(2.0 * PFGB_PI * (double)(((j - 19) * k) % 41) / 41.0);
+            const uint32_t hb = tf32_rna_bits((float)v);
+            float hi;
+            memcpy(&hi, &hb, 4);
+            const float lo = (float)(v - (double)hi);
+            memcpy(&tab[tc41::b_offset(n, j)], &hi, 4);
+            memcpy(&tab[tc41::B_BYTES + tc41::b_offset(n, j)], &lo, 4);
+        }
+    TRY(dalloc(c, &c->tc_btab, tab.size()));
+    TRY(dalloc(c, (void **)&c->tc_err, sizeof(int)));
+    PFGB_CUDA_TRY(cudaMemcpy(c->tc_btab, tab.data(), tab.size(), cudaMemcpyHostToDevice));
+    PFGB_CUDA_TRY(cudaMemset(c->tc_err, 0, sizeof(int)));
+    return PFGB_OK;
+}
+
 static pfgb_status make_ktab(pfgb_ctx *c) {
     const pfgb_params &P = c->p;
     auto wrap = [](int i, int n, double d) {
@@ -2966,8 +3025,9 @@ static pfgb_status validate(const pfgb_params *p) {
         return PFGB_ERR_INVALID;
     }
     if (p->mode == PFGB_MODE_MINIMIZE) {
-        if (p->model_mode != PFGB_MODEL_TWO_PHASE || p->zero_mode_enabled) {
-            pfgb_set_error_msg("minimize is built for two_phase with the zero mode off");
+        if ((p->model_mode != PFGB_MODEL_TWO_PHASE && !p->minimize_full_model) || p->zero_mode_enabled) {
+            pfgb_set_error_msg("minimize is built for the full model (two_phase or gp_zone) and the phi-only "
+                               "model (two_phase), with the zero mode off");
             return PFGB_ERR_UNSUPPORTED;
         }
         if (!(p->minimize_dt > 0)) {
@@ -3037,6 +3097,8 @@ static pfgb_status validate(const pfgb_params *p) {
 static void ctx_free(pfgb_ctx *c) {
     auto f = [](void *p) { if (p) cudaFree(p); };
     for (int a = 0; a < 2; ++a) for (int b = 0; b < 3; ++b) f(c->tw[a][b]);
+    f(c->tc_btab);
+    f(c->tc_err);
     f(c->kx); f(c->ky); f(c->kz); f(c->mx); f(c->my); f(c->mz);
     for (int i = 0; i < 2; ++i) f(c->phi[i]);
     f(c->eta[0]);
@@ -3266,6 +3328,7 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
     if (s == PFGB_OK) s = upload_twiddles(c, 0, pin->Nx);
     if (s == PFGB_OK) s = upload_twiddles(c, 1, pin->Ny);
     if (s == PFGB_OK) s = upload_twiddles(c, 2, pin->Nz);
+    if (s == PFGB_OK && pin->fft_tensor_cores && c->f246[1] && pin->elastic_enabled) s = upload_tc41_table(c);
     if (s == PFGB_OK) {
         cudaError_t e = cudaMallocHost((void **)&c->hscal, sizeof(double) * 64);
         if (e != cudaSuccess) { pfgb_set_error("cudaMallocHost", e, __FILE__, __LINE__); s = PFGB_ERR_CUDA; }

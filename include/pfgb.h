@@ -132,7 +132,14 @@ typedef struct pfgb_params {
        reference's iteration, in fewer iterations.  No counterpart key in the
        reference; default 0. */
     int32_t elastic_chebyshev;
-    int32_t elastic_pad0;
+    /* 1: the 41-point stage of the 246 = 6 x 41 transforms of the elastic
+       y passes runs on the tensor cores as a split-precision TF32
+       contraction (three terms, FP32 accumulation; tcgen05.mma with the
+       accumulators in tensor memory) instead of direct FP32 multiply-adds.
+       FP32 elastic fields, 246-long y axis with an even Nz/2+1.  No
+       counterpart key in the reference (its transforms are cuFFT's);
+       default 0. */
+    int32_t fft_tensor_cores;
     double elastic_residual_tolerance;
     double elastic_residual_absolute_floor;
     double eps_iso_over_vB;

@@ -1602,9 +1602,11 @@ static int minimize_iter(pfo_state *s, pfgb_min_stats *ms) {
     const double F_surf = total_interface / (double)s->N;
     double F_el = 0.0, total_el_core = 0.0;
     if (P->elastic_enabled) {   /* compute_gel_density_kernel, cuda_kernels.cu:1789-1850 */
+        /* the three-phase eigenstrain when GP elasticity is on (gp_zone) */
+        const int gp3 = s->gp && P->gp_elastic_enabled;
         RLOOP_BEGIN(s)
             double e0[6];
-            eigen_point(s, &ec, s->phi[idx], s->eta[idx], o_clamp01(s->xB[idx]), 0, e0);
+            eigen_point(s, &ec, s->phi[idx], s->eta[idx], o_clamp01(s->xB[idx]), gp3, e0);
             double sd = 0.0;
             for (int c = 0; c < 6; ++c) {
                 const double el = s->eps_r[c][idx] - e0[c];
@@ -1751,7 +1753,10 @@ static int minimize_iter(pfo_state *s, pfgb_min_stats *ms) {
 
 int pfo_minimize(pfo_state *s, int max_iter, int stop_on_convergence, pfgb_min_stats *ms) {
     const pfgb_params *P = &s->p;
-    if (P->mode != PFGB_MODE_MINIMIZE || s->gp || P->zero_mode_enabled)
+    /* gp_zone minimize: the same iteration with eta held fixed (eta evolves
+     * in dynamics only, main_cuda.cu:29948-30006) and the GP forms of the
+     * phi drive, the mu of the flux and the eigenstrain */
+    if (P->mode != PFGB_MODE_MINIMIZE || P->zero_mode_enabled || (s->gp && !P->minimize_full_model))
         return PFGB_ERR_UNSUPPORTED;
     for (int i = 0; i < max_iter; ++i) {
         int rc = minimize_iter(s, ms);

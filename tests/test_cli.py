@@ -349,7 +349,7 @@ def test_cli_vtk_continuation(capi, tmp_path):
     assert r.returncode == 0, r.stderr[-2000:]
     assert (tmp_path / "B" / run / "continue_dyn_2" / "phi_2.vtk").exists()
     # full-model minimize, then minimize-continue from its final files
-    mz = ["--mode=minimize", "--minimize-full-model", "--minimize-max-iter", "3", "--minimize-dt", "0.05"]
+    mz = ["--mode=minimize", "--minimize-full-model", "--minimize-max-iter", "3", "--minimize-dt", "0.05", "--V0", "0.05"]
     r = _run(capi, [str(n)] * 3 + ["0.05", "100", "50", "1", "1", "--pf-param-file", pf] + mz + raw, tmp_path,
              env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "C")})
     assert r.returncode == 0, r.stderr
@@ -357,7 +357,7 @@ def test_cli_vtk_continuation(capi, tmp_path):
     src = tmp_path / "C" / run / "raw_fields_relax"
     r = _run(capi, [str(n)] * 3 + ["0.05", "100", "50", "1", "1", "--pf-param-file", pf, "--mode=minimize-continue",
                                    "--minimize-full-model", "--minimize-max-iter", "2", "--minimize-dt", "0.05",
-                                   "--continue-phi-vtk", str(src / "phi_final_raw_fields_relax.vtk"),
+                                   "--V0", "0.05", "--continue-phi-vtk", str(src / "phi_final_raw_fields_relax.vtk"),
                                    "--continue-xB-vtk", str(src / "xB_final_raw_fields_relax.vtk")], tmp_path,
              env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "D")})
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
@@ -384,7 +384,7 @@ def test_cli_phi_only_minimize(capi, tmp_path):
     n = 16
     pf = os.path.join(GOLDEN, "c2.params")
     r = _run(capi, [str(n)] * 3 + ["0.05", "100", "50", "1", "1", "--pf-param-file", pf, "--mode=minimize",
-                                   "--minimize-max-iter", "4", "--radius", "5"], tmp_path,
+                                   "--minimize-max-iter", "4", "--radius", "5", "--V0", "0.05"], tmp_path,
              env={"CUDA_STO_RESULTS_ROOT": str(tmp_path / "R")})
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     run = os.listdir(tmp_path / "R")[0]

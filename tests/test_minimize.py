@@ -135,6 +135,42 @@ def test_phi_only_minimize_parity(capi, oracle, precision, tol):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(0, 1e-6), (1, 2e-5)])
+def test_gp_zone_minimize_parity(capi, oracle, precision, tol):
+    """Full-model minimize in gp_zone (GP elasticity on phi and eta): eta is
+    held fixed (it evolves in dynamics only), the phi drive, the flux mu and
+    the eigenstrain take their GP forms.  GPU against the oracle, iteration
+    by iteration."""
+    from cuda_sto_pf_gb300 import workloads
+    from cuda_sto_pf_gb300.solver import Solver
+    p, phi, xB = _case(capi, precision=precision, minimize_V0=0.1, model_mode=1, gp_elastic_enabled=1,
+                       gp_elastic_active_phi=1, gp_elastic_active_eta=1)
+    eta = workloads.ellipsoid_field(phi.shape, [np.array([5.0, 5.0, 5.0])], [np.full(3, 3.0)], [np.eye(3)],
+                                    p.ic_phi_iface_w)
+    o = oracle(p, threads=8)
+    o.load(phi, xB, eta)
+    mo, mg = capi.MinStats(), capi.MinStats()
+    with Solver(p) as s:
+        s.load(phi, xB, eta)
+        for it in range(5):
+            assert o.minimize(1, mo) == 0
+            s.minimize(1, mg)
+            for f in FIELDS:
+                a, b = getattr(mg, f), getattr(mo, f)
+                if f == "vol_err_rel":
+                    assert abs(a - b) <= (1e-9 if precision == 0 else 1e-7), (it, f, a, b)
+                    continue
+                scale = max(abs(b), 1e-6 if f.startswith("rms") else 1e-12)
+                assert abs(a - b) <= (50 * tol if f == "rms_res" else tol) * scale, (it, f, a, b)
+            assert abs(mg.elastic_iterations - mo.elastic_iterations) <= 1
+        fg = s.fields()
+    fo = o.fields()
+    for k in ("phi", "xB", "Y"):
+        assert rel_l2(fg[k], fo[k]) <= tol, k
+    assert rel_l2(fg["eta"], eta) == 0.0 or rel_l2(fg["eta"], eta) <= 1e-7   # eta unchanged
+
+
+@pytest.mark.gpu
 def test_minimize_stops_on_convergence(capi):
     from cuda_sto_pf_gb300.solver import Solver
     big = 1e30
