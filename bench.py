@@ -61,7 +61,14 @@ def parse():
     ap.add_argument("--fno-pairs", type=int, default=1024, help="training pairs (base x cube symmetries)")
     ap.add_argument("--fno-train-steps", type=int, default=6000)
     ap.add_argument("--fno-eval-steps", type=int, default=300)
-    ap.add_argument("--workload", default="c2", choices=["c2", "sweep", "fno", "fno-step"],
+    ap.add_argument("--particles", type=int, default=None,
+                    help="precipitate count (default: 60 scaled by the grid volume over 246^3)")
+    ap.add_argument("--median-radius", type=float, default=6.0, help="median precipitate radius in cells")
+    ap.add_argument("--eta-sites", type=int, default=None,
+                    help="GP-zone eta sites (default: 20 scaled by the grid volume over 246^3)")
+    ap.add_argument("--horizon-marks", default="8,25,50,100",
+                    help="horizon workload: step counts at which the fields are compared")
+    ap.add_argument("--workload", default="c2", choices=["c2", "sweep", "fno", "fno-step", "horizon"],
                     help="c2: the 246^3 dynamics step (default); sweep: the batched minimize sweep")
     ap.add_argument("--sweep-cases", type=int, default=48)
     ap.add_argument("--sweep-iters", type=int, default=500)
@@ -106,14 +113,18 @@ def make_params(capi, n, precision, tol, shape=None, chebyshev=None):
     return p
 
 
+# population of the generated microstructure (set from the command line)
+POPULATION = {"particles": None, "median_r": 6.0, "eta_sites": None}
+
+
 def make_fields(capi, p, n, seed=2468):
     from cuda_sto_pf_gb300 import workloads
     shape = (p.Nx, p.Ny, p.Nz)
     frac = shape[0] * shape[1] * shape[2] / 246.0 ** 3
-    count = max(1, int(round(60 * frac)))
-    sites = max(1, int(round(20 * frac)))
-    w = workloads.ellipsoid_population(n, count=count, eta_sites=sites, w=p.ic_phi_iface_w, seed=seed,
-                                       shape=shape)
+    count = POPULATION["particles"] or max(1, int(round(60 * frac)))
+    sites = POPULATION["eta_sites"] or max(1, int(round(20 * frac)))
+    w = workloads.ellipsoid_population(n, count=count, median_r=POPULATION["median_r"], eta_sites=sites,
+                                       w=p.ic_phi_iface_w, seed=seed, shape=shape)
     phi, xB, eta = w["phi"], w["xB"], w["eta"]
     # raw-field rules of the reference loader (xB capped at its default
     # xB_max_safe = 0.07)
@@ -305,6 +316,71 @@ def compare_plain_fp64(args, capi, Solver, n, shape, fields, dev, stream, nsteps
                     f"of phi, xB, eta and the 6 stress components"}
 
 
+def run_horizon(args):
+    """Field error of the chosen path (FP32 fields, Chebyshev increment
+    iteration, extrapolated start) against the plain FP64 form (FP64
+    fields, the reference's iteration) over a long horizon: both run the
+    workload from the same initial fields side by side; the relative L2
+    errors of phi, xB, eta and the six stress components are taken at
+    several step counts."""
+    import torch
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from cuda_sto_pf_gb300 import capi
+    from cuda_sto_pf_gb300.solver import Solver
+    capi.load(build_if_missing=True)
+    torch.cuda.set_device(local)
+    n = args.n
+    shape = tuple(int(x) for x in args.shape.split(",")) if args.shape else (n, n, n)
+    p32 = make_params(capi, n, "fp32", args.elastic_tol, shape)
+    p64 = make_params(capi, n, "fp64", args.elastic_tol, shape, chebyshev=0)
+    phi, xB, eta, npart, neta = make_fields(capi, p32, n)
+    marks = sorted(set(int(x) for x in args.horizon_marks.split(",")))
+    stream = torch.cuda.current_stream(local)
+    out = []
+    it32, it64, conv32, ms32, ms64 = [], [], 0, 0.0, 0.0
+    with Solver(p32, device=local) as s32, Solver(p64, device=local) as s64:
+        for s in (s32, s64):
+            s.set_stream(stream.cuda_stream)
+            s.load(phi, xB, eta)
+        done = 0
+        for m in marks:
+            for _ in range(m - done):
+                for s, its, tag in ((s32, it32, 32), (s64, it64, 64)):
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    st = s.step(1)
+                    e1.record(stream)
+                    e1.synchronize()
+                    its.append(st.elastic_iterations)
+                    if tag == 32:
+                        ms32 += e0.elapsed_time(e1)
+                        conv32 += st.elastic_converged
+                    else:
+                        ms64 += e0.elapsed_time(e1)
+            done = m
+            f32, f64 = s32.fields(), s64.fields()
+            err = {k: rel_l2(f32[k], f64[k]) for k in ("phi", "xB", "eta")}
+            err["sigma"] = rel_l2(s32.elastic()["sigma"], s64.elastic()["sigma"])
+            m32, m64 = s32.diagnostics().mass_xBtot, s64.diagnostics().mass_xBtot
+            err["mass_rel_fp32_vs_fp64"] = abs(m32 - m64) / m64
+            out.append({"after_steps": m, "field_rel_l2_vs_fp64": err})
+            print(json.dumps({"after_steps": m, **err}), file=sys.stderr, flush=True)
+    line = {"metric": "field rel. L2 of the chosen FP32 path vs the plain FP64 form over a long horizon",
+            "value": out[-1]["field_rel_l2_vs_fp64"]["xB"], "unit": "relative L2 (xB)", "n_gpus": 1,
+            "steps": marks[-1], "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded microstructure generator, reference raw-field rules)",
+            "config": {"workload": f"{'x'.join(map(str, shape))} gp_zone dynamics, {npart} ellipsoids + "
+                                   f"{neta} eta sites, heterogeneous elasticity, zero mode",
+                       "elastic_tol": args.elastic_tol, "dt": p32.dt},
+            "horizon": out,
+            "chosen": {"ms_per_step": ms32 / marks[-1], "elastic_iters_per_step": sum(it32) / len(it32),
+                       "elastic_converged_steps": conv32},
+            "plain_fp64": {"ms_per_step": ms64 / marks[-1], "elastic_iters_per_step": sum(it64) / len(it64)}}
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args):
     global FFT_TENSOR_CORES
     if args.fft_tensor_cores is not None:
@@ -361,6 +437,7 @@ def run_ours(args):
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
     launches = s.launches()
+    dev_bytes = int(capi.load().pfgb_device_bytes(s.ctx))
     # per-kernel CUDA-event timing on a separate pass (events bracket every launch)
     s.profile_enable(True)
     for _ in range(min(args.steps, 5)):
@@ -474,6 +551,7 @@ def run_ours(args):
                 # host round trips (residual reads, zero-mode scalars) and gaps
                 "kernel_busy_fraction": (total_ms / max(1, prof_steps)) / (ms_max / args.steps),
                 "wall_ms_per_step": 1e3 * wall / args.steps,
+                "device_bytes": dev_bytes,
                 "gpu_launches": launches,
                 "clocks": clk, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "vs_plain_fp64": plain,
                 "at_reference_default_tol": ref_tol}
@@ -717,8 +795,12 @@ def run_fno_step(args):
 def main():
     global CHEBYSHEV, EXTRAPOLATE
     args = parse()
+    POPULATION.update(particles=args.particles, median_r=args.median_radius, eta_sites=args.eta_sites)
     CHEBYSHEV = 0 if args.no_chebyshev else 1
     EXTRAPOLATE = 0 if args.no_extrapolate else 1
+    if args.workload == "horizon":
+        run_horizon(args)
+        return
     if args.workload == "sweep":
         run_sweep(args)
         return

@@ -192,6 +192,7 @@ EXPORTS = [
     ("pfgb_fft3d_r2c", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     ("pfgb_fft3d_c2r", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     ("pfgb_fft3d_r2c_noalloc", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    ("pfgb_fft_y246x6", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
     ("pfgb_fnv1a64", ctypes.c_uint64, [c_void_p, c_size_t, ctypes.c_uint64]),
     ("pfgb_parameter_fingerprint", ctypes.c_uint64, [POINTER(Params)]),
     ("pfgb_elastic_solver_fingerprint", ctypes.c_uint64, [POINTER(Params)]),

@@ -347,3 +347,40 @@ k_y246tc(Grid3 g, const float2 *tw_g, const float4 *btab, AxisIO<float, 6, 6> io
     __syncthreads();
     if (warp == 0) tc41::tmem_dealloc(tbase, tc41::TMEM_COLS);
 }
+
+namespace tc41 {
+// per-block set-up of the tensor-core stage, called by all threads before
+// the first transform: TMEM columns (warp 0), the completion barrier
+// (thread 0) and the B table copied into shared memory with 16-byte
+// cp.async (committed with the caller's group; after its cp.async wait the
+// caller calls ready())
+__device__ __forceinline__ void begin(uint32_t *tbase, uint64_t *mbar, float4 *bt, const float4 *btab) {
+    if ((threadIdx.x >> 5) == 0) tmem_alloc(tbase, TMEM_COLS);
+    if (threadIdx.x == 0) mbar_init(mbar);
+    for (int e = threadIdx.x; e < 2 * B_BYTES / 16; e += blockDim.x) {
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(bt + e);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(btab + e));
+    }
+}
+// the B table made visible to the tensor core, the TMEM base to every thread
+__device__ __forceinline__ Ctx ready(uint32_t *tbase, uint64_t *mbar, float4 *bt, int *err) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    fence_before();
+    __syncthreads();
+    fence_after();
+    return Ctx{*tbase, mbar, 0u, smem_u32(bt), smem_u32(bt) + B_BYTES, err};
+}
+__device__ __forceinline__ void end(uint32_t tmem) {
+    fence_before();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) tmem_dealloc(tmem, TMEM_COLS);
+}
+// one transform of the block's NL lines: the radix-6 stage on the CUDA
+// cores, the 41-point stage on the tensor cores
+template <int DIR, int PS, int LS>
+__device__ __forceinline__ void lines(float2 *buf, const float2 *tw, Ctx &c) {
+    f246::stage_a<DIR, PS, LS>(buf, tw);
+    __syncthreads();
+    stage_c<DIR, PS, LS>(buf, c);
+}
+}  // namespace tc41

@@ -136,6 +136,7 @@ struct pfgb_ctx {
     // when a bounded wait on the tensor core runs out
     void *tc_btab = nullptr;
     int *tc_err = nullptr;
+    bool tc_y = false, tc_x = false, tc_z = false;   // passes that use it
 };
 
 // tag + algorithmic bytes of the next launch (set by the op-level wrappers)
@@ -1113,6 +1114,8 @@ struct GreenArgs {
     TE gam, rho;
     double *partials;
     const double *skip;        // return at once when *skip != 0 (a finished solve)
+    const float4 *btab;        // tensor-core 41-point stage: its B table (null: FP32 FMAs)
+    int *tc_err;               // set when a bounded tensor-core wait runs out
     int resid;
     int mode;                  // 0 u <- Phi(u); 1 first increment step; 2 delta <- r0 + L delta
 };
@@ -1435,6 +1438,8 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
     A.rho = (TE)c->cheb_rho;
     A.partials = c->partials;
     A.skip = c->skip;
+    A.btab = (const float4 *)c->tc_btab;
+    A.tc_err = c->tc_err;
     A.resid = resid;
     A.mode = mode;
     dim3 grid((c->g.NzC + TK - 1) / TK, c->g.Ny);
@@ -1460,16 +1465,23 @@ static pfgb_status launch_green(pfgb_ctx *c, bool eigen, int resid, int *nblocks
 // same operations as k_x_green / k_zpass<OpHijZ> / the y OpCopy pass, with
 // f246::NL lines per block in one in-place shared buffer
 // ---------------------------------------------------------------------------
-template <bool EIGEN>
+// TCS: the 41-point stages on the tensor cores (dft41_tc.cuh): shared memory
+// B table | twiddles | line buffer without row padding
+template <bool EIGEN, bool TCS>
 __global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
 k_x_green246(GreenArgs<float> A) {
     if (A.skip && *A.skip != 0.0) return;
     using namespace f246;
     using T2 = float2;
     constexpr int TP = TC / 2;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    constexpr int PSX = TCS ? NL : PSTR;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t tc_mbar;
+    __shared__ uint32_t tc_tbase;
+    float4 *bt = reinterpret_cast<float4 *>(smem_raw);
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw + (TCS ? 2 * tc41::B_BYTES : 0));
     float2 *buf = tw + N;
+    if constexpr (TCS) tc41::begin(&tc_tbase, &tc_mbar, bt, A.btab);
     const int k0 = blockIdx.x * TC, j = blockIdx.y;
     const int kcnt = min(TC, A.g.NzC - k0);
     const long long base = (long long)j * A.g.NzC + k0;
@@ -1478,7 +1490,7 @@ k_x_green246(GreenArgs<float> A) {
         const int tp = e % TP, r = e / TP;
         const int q = r % N, s = r / N;
         const int t = 2 * tp;
-        float2 *dst = buf + q * PSTR + s * TC + t;
+        float2 *dst = buf + q * PSX + s * TC + t;
         const float2 *src = A.E[s] + base + q * es + t;
         if (t + 1 < kcnt) {
             const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
@@ -1491,8 +1503,14 @@ k_x_green246(GreenArgs<float> A) {
     cp_async_commit();
     load_twiddles(tw, A.tw);
     cp_async_wait_all();
-    __syncthreads();
-    lines<-1, PSTR, 1>(buf, tw);
+    tc41::Ctx tcx{};
+    if constexpr (TCS) {
+        tcx = tc41::ready(&tc_tbase, &tc_mbar, bt, A.tc_err);
+        tc41::lines<-1, PSX, 1>(buf, tw, tcx);
+    } else {
+        __syncthreads();
+        lines<-1, PSX, 1>(buf, tw);
+    }
     float rd = 0.f, rr = 0.f;
     // mode 2 (every iteration after the first of a step): the k-point's
     // r0 / delta / u0 / previous iterate are loaded as one batch first
@@ -1503,7 +1521,7 @@ k_x_green246(GreenArgs<float> A) {
         if (pre && l < kcnt) green_fetch<float>(A, base + q * es + l, cur);
         const int kk = min(k, A.g.NzC - 1);
         const float kv[3] = {float(A.kt.kx[q]), float(A.kt.ky[j]), float(A.kt.kz[kk])};
-        float2 *pt = buf + q * PSTR + l;
+        float2 *pt = buf + q * PSX + l;
         T2 x[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) x[c] = pt[c * TC];
@@ -1549,32 +1567,43 @@ k_x_green246(GreenArgs<float> A) {
             reinterpret_cast<AccSum2 *>(A.partials)[blockIdx.y * gridDim.x + blockIdx.x] = sacc;
     }
     __syncthreads();
-    lines<+1, PSTR, 1>(buf, tw);
+    if constexpr (TCS) tc41::lines<+1, PSX, 1>(buf, tw, tcx);
+    else lines<+1, PSX, 1>(buf, tw);
     for (int e = threadIdx.x; e < 6 * N * TP; e += blockDim.x) {
         const int tp = e % TP, r = e / TP;
         const int q = r % N, s = r / N;
         const int t = 2 * tp;
-        const float2 *srcs = buf + q * PSTR + s * TC + t;
+        const float2 *srcs = buf + q * PSX + s * TC + t;
         float2 *dst = A.E[s] + base + q * es + t;
         if (t + 1 < kcnt) *reinterpret_cast<float4 *>(dst) = *reinterpret_cast<const float4 *>(srcs);
         else if (t < kcnt) dst[0] = srcs[0];
     }
+    if constexpr (TCS) tc41::end(tcx.tmem);
 }
 
 // z pass with six fields in and six out (C2R -> op.point -> R2C), ZR rows
 // per block: the rows' three field pairs are the block's NL complex lines
-template <class Op>
+// TCS: the 41-point stages on the tensor cores (dft41_tc.cuh); shared
+// memory B table | twiddles | lines
+template <class Op, bool TCS>
 __global__ void __launch_bounds__(f246::THREADS, f246::BLOCKS_PER_SM)
-k_zpass246(Grid3 g, const float2 *tw_g, Op op, const double *skip) {
+k_zpass246(Grid3 g, const float2 *tw_g, Op op, const double *skip, const float4 *btab, int *tc_err) {
     if (skip && *skip != 0.0) return;
     using namespace f246;
     constexpr int R = ZR, NC = N / 2 + 1;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t tc_mbar;
+    __shared__ uint32_t tc_tbase;
+    float4 *bt = reinterpret_cast<float4 *>(smem_raw);
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw + (TCS ? 2 * tc41::B_BYTES : 0));
     float2 *buf = tw + N;
     const long long row0 = (long long)blockIdx.x * R;
     const long long nrows = (long long)g.Nx * g.Ny;
     const int rcnt = (int)min((long long)R, nrows - row0);
+    if constexpr (TCS) {
+        tc41::begin(&tc_tbase, &tc_mbar, bt, btab);
+        cp_async_commit();
+    }
     load_twiddles(tw, tw_g);
     // unrolled by two: two trips' spectral loads in flight together
 #pragma unroll 2
@@ -1596,8 +1625,15 @@ k_zpass246(Grid3 g, const float2 *tw_g, Op op, const double *skip) {
             if (k > 0 && 2 * k != N) line[N - k] = make_float2(Av.x + Bv.y, Bv.x - Av.y);
         }
     }
-    __syncthreads();
-    lines<+1, 1, N>(buf, tw);
+    tc41::Ctx tcx{};
+    if constexpr (TCS) {
+        cp_async_wait_all();
+        tcx = tc41::ready(&tc_tbase, &tc_mbar, bt, tc_err);
+        tc41::lines<+1, 1, N>(buf, tw, tcx);
+    } else {
+        __syncthreads();
+        lines<+1, 1, N>(buf, tw);
+    }
     typename Op::Acc acc = Op::Acc::identity();
     for (int e = threadIdx.x; e < rcnt * N; e += blockDim.x) {
         const int r = e / N, z = e - r * N;
@@ -1617,7 +1653,8 @@ k_zpass246(Grid3 g, const float2 *tw_g, Op op, const double *skip) {
         if (threadIdx.x == 0) op.finish(blockIdx.x, acc);
     }
     __syncthreads();
-    lines<-1, 1, N>(buf, tw);
+    if constexpr (TCS) tc41::lines<-1, 1, N>(buf, tw, tcx);
+    else lines<-1, 1, N>(buf, tw);
     for (int e = threadIdx.x; e < rcnt * NC; e += blockDim.x) {
         const int rr = e / NC, k = e - rr * NC;
         float2 v[6];
@@ -1631,11 +1668,12 @@ k_zpass246(Grid3 g, const float2 *tw_g, Op op, const double *skip) {
         }
         op.store_spec(row0 + rr, k, v);
     }
+    if constexpr (TCS) tc41::end(tcx.tmem);
 }
 
 template <int DIR>
 static pfgb_status launch_y246(pfgb_ctx *c, const char *tag) {
-    if (c->tc_btab) {   // the 41-point stage on the tensor cores
+    if (c->tc_y) {   // the 41-point stage on the tensor cores
         const size_t smem = tc41::y_smem_bytes();
         auto kern = k_y246tc<DIR>;
         PFGB_CUDA_TRY(allow_smem(kern, smem));
@@ -1676,19 +1714,23 @@ static pfgb_status launch_green246(pfgb_ctx *c, bool eigen, int resid, int *nblo
     A.rho = (float)c->cheb_rho;
     A.partials = c->partials;
     A.skip = c->skip;
+    A.btab = (const float4 *)c->tc_btab;
+    A.tc_err = c->tc_err;
     A.resid = resid;
     A.mode = mode;
     dim3 grid((c->g.NzC + f246::TC - 1) / f246::TC, c->g.Ny);
     ProfScope ps(c, {eigen ? "x_green_eigen" : "x_green_hij",
                      (double)(6 + 3 + 6 + green_extra(c, mode, resid)) * (double)c->g.Nk * sizeof(float2)});
-    if (eigen) {
-        auto kern = k_x_green246<true>;
-        PFGB_CUDA_TRY(allow_smem(kern, smem));
-        kern<<<grid, f246::THREADS, smem, c->stream>>>(A);
+    auto go = [&](auto kern, size_t sm) -> pfgb_status {
+        PFGB_CUDA_TRY(allow_smem(kern, sm));
+        kern<<<grid, f246::THREADS, sm, c->stream>>>(A);
+        return PFGB_OK;
+    };
+    if (c->tc_x) {   // the 41-point stages on the tensor cores
+        const size_t smem_tc = tc41::y_smem_bytes();
+        TRY(eigen ? go(k_x_green246<true, true>, smem_tc) : go(k_x_green246<false, true>, smem_tc));
     } else {
-        auto kern = k_x_green246<false>;
-        PFGB_CUDA_TRY(allow_smem(kern, smem));
-        kern<<<grid, f246::THREADS, smem, c->stream>>>(A);
+        TRY(eigen ? go(k_x_green246<true, false>, smem) : go(k_x_green246<false, false>, smem));
     }
     PFGB_CUDA_TRY(cudaGetLastError());
     *nblocks = grid.x * grid.y;
@@ -1698,12 +1740,21 @@ static pfgb_status launch_green246(pfgb_ctx *c, bool eigen, int resid, int *nblo
 template <class Op>
 static pfgb_status launch_z246(pfgb_ctx *c, Op op, const char *tag, double extra_bytes) {
     const size_t smem = f246::z_smem_bytes();
-    auto kern = k_zpass246<Op>;
-    PFGB_CUDA_TRY(allow_smem(kern, smem));
     const long long rows = (long long)c->g.Nx * c->g.Ny;
     const int nb = (int)((rows + f246::ZR - 1) / f246::ZR);
     ProfScope ps(c, {tag, 12.0 * (double)c->g.Nk * sizeof(float2) + extra_bytes});
-    kern<<<nb, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][2], op, c->skip);
+    if (c->tc_z) {   // the 41-point stages on the tensor cores
+        auto kern = k_zpass246<Op, true>;
+        const size_t smem_tc = 2 * tc41::B_BYTES + smem;
+        PFGB_CUDA_TRY(allow_smem(kern, smem_tc));
+        kern<<<nb, f246::THREADS, smem_tc, c->stream>>>(c->g, (const float2 *)c->tw[1][2], op, c->skip,
+                                                         (const float4 *)c->tc_btab, c->tc_err);
+    } else {
+        auto kern = k_zpass246<Op, false>;
+        PFGB_CUDA_TRY(allow_smem(kern, smem));
+        kern<<<nb, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][2], op, c->skip, nullptr,
+                                                     nullptr);
+    }
     PFGB_CUDA_TRY(cudaGetLastError());
     return PFGB_OK;
 }
@@ -3328,7 +3379,12 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
     if (s == PFGB_OK) s = upload_twiddles(c, 0, pin->Nx);
     if (s == PFGB_OK) s = upload_twiddles(c, 1, pin->Ny);
     if (s == PFGB_OK) s = upload_twiddles(c, 2, pin->Nz);
-    if (s == PFGB_OK && pin->fft_tensor_cores && c->f246[1] && pin->elastic_enabled) s = upload_tc41_table(c);
+    if (s == PFGB_OK && pin->elastic_enabled) {
+        c->tc_y = (pin->fft_tensor_cores & 1) && c->f246[1];
+        c->tc_x = (pin->fft_tensor_cores & 2) && c->f246[0];
+        c->tc_z = (pin->fft_tensor_cores & 4) && c->f246[2];
+        if (c->tc_y || c->tc_x || c->tc_z) s = upload_tc41_table(c);
+    }
     if (s == PFGB_OK) {
         cudaError_t e = cudaMallocHost((void **)&c->hscal, sizeof(double) * 64);
         if (e != cudaSuccess) { pfgb_set_error("cudaMallocHost", e, __FILE__, __LINE__); s = PFGB_ERR_CUDA; }
@@ -3940,6 +3996,37 @@ static pfgb_status check_transform_buffers(const void *in, const void *out) {
 }
 
 extern "C" {
+
+// the elastic iteration's y transform of six half spectra on the 246-point
+// engine (test / tooling entry point)
+pfgb_status pfgb_fft_y246x6(int tensor_cores, int dir, int Nx, int NzC, void *spec6, void *stream) {
+    if (!spec6 || (dir != -1 && dir != 1) || Nx < 1 || NzC < 2 || (NzC % 2) != 0 || NzC > PFGB_MAX_N) {
+        pfgb_set_error_msg("pfgb_fft_y246x6: dir must be -1 or +1, Nx >= 1 and NzC even in [2, %d]", PFGB_MAX_N);
+        return PFGB_ERR_INVALID;
+    }
+    TRY(check_transform_buffers(spec6, spec6));
+    pfgb_ctx c;
+    pfgb_status s = fft_ctx_init(&c, Nx, f246::N, 2 * (NzC - 1), stream);
+    c.g.NzC = NzC;
+    c.g.Nk = (long long)Nx * f246::N * NzC;
+    const size_t per = sizeof(float2) * (size_t)c.g.Nk;
+    for (int i = 0; i < 6; ++i) c.E[i] = (unsigned char *)spec6 + i * per;
+    if (s == PFGB_OK && tensor_cores) {
+        s = upload_tc41_table(&c);
+        c.tc_y = true;
+    }
+    if (s == PFGB_OK) s = dir < 0 ? launch_y246<-1>(&c, "y_fwd6") : launch_y246<+1>(&c, "y_inv6");
+    if (s == PFGB_OK && c.tc_err) {
+        int te = 0;
+        if (cudaMemcpyAsync(&te, c.tc_err, sizeof(int), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess ||
+            cudaStreamSynchronize(c.stream) != cudaSuccess) s = PFGB_ERR_CUDA;
+        else if (te) { pfgb_set_error_msg("tensor-core 41-point stage: a wait ran out"); s = PFGB_ERR_TIMEOUT; }
+    }
+    fft_ctx_free(&c);
+    if (c.tc_btab) cudaFree(c.tc_btab);
+    if (c.tc_err) cudaFree(c.tc_err);
+    return s;
+}
 
 pfgb_status pfgb_fft3d_r2c(int precision, int Nx, int Ny, int Nz, const void *in, void *out, void *stream) {
     TRY(check_transform_buffers(in, out));

@@ -132,11 +132,13 @@ typedef struct pfgb_params {
        reference's iteration, in fewer iterations.  No counterpart key in the
        reference; default 0. */
     int32_t elastic_chebyshev;
-    /* 1: the 41-point stage of the 246 = 6 x 41 transforms of the elastic
-       y passes runs on the tensor cores as a split-precision TF32
-       contraction (three terms, FP32 accumulation; tcgen05.mma with the
-       accumulators in tensor memory) instead of direct FP32 multiply-adds.
-       FP32 elastic fields, 246-long y axis with an even Nz/2+1.  No
+    /* Bit mask of the elastic-iteration passes whose 246 = 6 x 41
+       transforms run their 41-point stage on the tensor cores as a
+       split-precision TF32 contraction (three terms, FP32 accumulation;
+       tcgen05.mma with the accumulators in tensor memory) instead of direct
+       FP32 multiply-adds: 1 the y passes, 2 the x (Green's operator) pass,
+       4 the z (h_ij) pass.  A bit applies where that axis is 246 long (x and
+       y also with an even Nz/2+1) and the elastic fields are FP32.  No
        counterpart key in the reference (its transforms are cuFFT's);
        default 0. */
     int32_t fft_tensor_cores;
@@ -426,6 +428,15 @@ pfgb_status pfgb_fft3d_r2c(int precision, int Nx, int Ny, int Nz,
                            const void *d_in, void *d_out, void *cuda_stream);
 pfgb_status pfgb_fft3d_c2r(int precision, int Nx, int Ny, int Nz,
                            const void *d_in, void *d_out, void *cuda_stream);
+
+/* The elastic iteration's y-axis transform of six half spectra, in place,
+ * on the 246 = 6 x 41 engine (test / tooling; no reference counterpart,
+ * its transforms are cuFFT's): d_spec6 holds six arrays of Nx x 246 x NzC
+ * interleaved complex float one after another (NzC even, 16-byte aligned),
+ * dir -1 forward (exp(-i k.x)), +1 inverse, unnormalised.  tensor_cores != 0
+ * runs the 41-point stage on the tensor cores (split-precision TF32), as
+ * fft_tensor_cores bit 1 does in the solver. */
+pfgb_status pfgb_fft_y246x6(int tensor_cores, int dir, int Nx, int NzC, void *d_spec6, void *cuda_stream);
 
 /* --- allocation-free forward transform -------------------------------- */
 /* No counterpart in the reference (its transforms go through cuFFT plans

@@ -40,3 +40,26 @@ def test_fft_rejects_bad_size(capi):
     lib = capi.load()
     assert lib.pfgb_fft3d_r2c(0, 0, 4, 4, 1, 1, None) == 1
     assert lib.pfgb_fft3d_r2c(0, 4, 4, 4, None, 1, None) == 1
+
+
+@pytest.mark.parametrize("tc", [0, 1], ids=["fma", "tensor-cores"])
+@pytest.mark.parametrize("direction", [-1, 1])
+def test_y246_lines_against_numpy(capi, tc, direction):
+    """The elastic y transform of six spectra on the 246 = 6 x 41 engine,
+    with the 41-point stage as FP32 multiply-adds or on the tensor cores
+    (split-precision TF32), against numpy: within 3e-6 x log2(246) of the
+    largest output."""
+    import torch
+    nx, nzc = 5, 10
+    rng = np.random.default_rng(41 + tc)
+    x = rng.standard_normal((6, nx, 246, nzc)) + 1j * rng.standard_normal((6, nx, 246, nzc))
+    ref = np.fft.fft(x, axis=2) if direction < 0 else np.fft.ifft(x, axis=2) * 246
+    d = torch.tensor(np.stack([x.real, x.imag], axis=-1), dtype=torch.float32, device="cuda").contiguous()
+    s = torch.cuda.current_stream().cuda_stream
+    lib = capi.load()
+    assert lib.pfgb_fft_y246x6(tc, direction, nx, nzc, d.data_ptr(), s) == 0, lib.pfgb_last_error(None)
+    torch.cuda.synchronize()
+    got = d.cpu().numpy().astype(np.float64)
+    got = got[..., 0] + 1j * got[..., 1]
+    err = np.abs(got - ref).max()
+    assert err <= 3e-6 * np.log2(246) * np.abs(ref).max(), err
