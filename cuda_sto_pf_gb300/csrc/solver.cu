@@ -1691,7 +1691,7 @@ static pfgb_status launch_y246(pfgb_ctx *c, const char *tag) {
     PFGB_CUDA_TRY(allow_smem(kern, smem));
     AxisIO<float, 6, 6> io;
     for (int i = 0; i < 6; ++i) { io.in[i] = (const float2 *)c->E[i]; io.out[i] = (float2 *)c->E[i]; }
-    dim3 grid((c->g.NzC + f246::TC - 1) / f246::TC, c->g.Nx);
+    dim3 grid((c->g.NzC + f246::YC - 1) / f246::YC, c->g.Nx, 6 / f246::YS);
     ProfScope ps(c, {tag, 12.0 * (double)c->g.Nk * sizeof(float2)});
     kern<<<grid, f246::THREADS, smem, c->stream>>>(c->g, (const float2 *)c->tw[1][1], io, c->skip);
     PFGB_CUDA_TRY(cudaGetLastError());
