@@ -36,7 +36,7 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INC
               "--expt-relaxed-constexpr"] + ARCH
 
 CU_SOURCES = ["solver.cu", "params.cu", "paramfile.cpp", "batch.cpp", "fno.cu", "checkpoint.cpp", "init.cu"]
-HEADERS = ["common.cuh", "dft41_tc.cuh", "fft.cuh", "fft246.cuh", "physics.cuh", "rader41.cuh"]
+HEADERS = ["common.cuh", "dfexp.cuh", "dfloat.cuh", "dft41_tc.cuh", "fft.cuh", "fft246.cuh", "physics.cuh", "rader41.cuh"]
 
 
 def _newer(target: str, deps: list[str]) -> bool:

@@ -73,7 +73,7 @@ class Params(Structure):
         ("minimize_rms_dphi_threshold", c_double), ("minimize_rms_dY_threshold", c_double),
         ("minimize_energy_diff_rel_threshold", c_double), ("minimize_rms_res_threshold", c_double),
         ("minimize_vol_err_rel_threshold", c_double),
-        ("pf_params_schema_version", c_int32), ("pad1", c_int32),
+        ("pf_params_schema_version", c_int32), ("zero_mode_fp64_cells", c_int32),
         ("t_real_unit", c_double),
         ("ic_vf_init_phi", c_double), ("ic_vf_target_phi", c_double), ("ic_phi_iface_w", c_double),
         ("gamma_Jm2", c_double), ("lambda_sm_m", c_double), ("Vm_alpha_0_phys_m3mol", c_double),

@@ -103,6 +103,7 @@ const DKey kInts[] = {
     DK("elastic_warm_start_extrapolate", elastic_warm_start_extrapolate),
     DK("elastic_warm_start_source", elastic_warm_start_source),
     DK("elastic_chebyshev", elastic_chebyshev), DK("fft_tensor_cores", fft_tensor_cores),
+    DK("zero_mode_fp64_cells", zero_mode_fp64_cells),
     DK("enable_Y_rhs_previous_time_level", enable_Y_rhs_previous_time_level),
     DK("disable_Y_rhs_gamma_term", disable_Y_rhs_gamma_term),
     DK("gp_elastic_enabled", gp_elastic_enabled), DK("gp_elastic_active_eta", gp_elastic_active_eta),

@@ -24,6 +24,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "dfloat.cuh"
 #include "fft.cuh"
 #include "fft246.cuh"
 #include "dft41_tc.cuh"
@@ -872,11 +873,11 @@ struct OpYFinalZ {
         const T Yold = p.Y;
         T y = in[0];
         if (!c.zm) {
-            // Y_normalize_and_clamp_kernel (:2554-2572), Y_cap = Y_clip
-            T yt = y + T(d.Yc);
-            if (yt > T(c.Yclip)) yt = T(c.Yclip);
-            if (yt < T(-c.Yclip)) yt = T(-c.Yclip);
-            y = yt - T(d.Yc);
+            // Y_normalize_and_clamp_kernel (:2554-2572), Y_cap = Y_clip, with
+            // the bounds moved to the stored frame (no round trip through Y + Yc)
+            const T hi = T(c.Yclip - d.Yc), lo = T(-c.Yclip - d.Yc);
+            if (y > hi) y = hi;
+            if (y < lo) y = lo;
         }
         d.Y[cell] = y;
         d.Yprev[cell] = Yold;
@@ -961,6 +962,67 @@ __global__ void k_zm_eval(const T *Y, const T *phi, long long N, double Yc, doub
     }
 #pragma unroll
     for (int q = 0; q < NL; ++q) { m[q] += double(cm[q]); dd[q] += double(cd[q]); }
+#pragma unroll
+    for (int q = 0; q < NL; ++q) {
+        AccSum2 s{m[q], dd[q]};
+        block_reduce_acc(s);
+        if (threadIdx.x == 0) reinterpret_cast<AccSum2 *>(partials)[q * gridDim.x + blockIdx.x] = s;
+        __syncthreads();
+    }
+}
+
+// The exact evaluation of the FP32-field path in double-float arithmetic
+// (dfloat.cuh): per cell h(phi), 1 - h, sigmoid(Y* + Yc + l) and the mass
+// term (1 - h) s + h v_B on the FP32 pipe, summed in double-float over
+// chunks of 16 cells of a thread, the chunks in FP64 and the blocks in FP64.
+// A cell's term carries a relative error of a few 2^-48 and the chunk sums
+// about 2^-44, so the total stays within about 1e-13 relative of the FP64
+// evaluation (k_zm_eval<T, double>), under the 1e-12 the mass ledger holds.
+// The derivative feeds only the Newton steps and is summed in float chunks.
+template <int NL>
+__global__ void k_zm_eval_df(const float *Y, const float *phi, long long N, double Yc, double vB,
+                             const double *lam, double *partials) {
+    __shared__ float2 tab[64];
+    if (threadIdx.x < 64) tab[threadIdx.x] = dfexp::kExp2Tab[threadIdx.x];
+    __syncthreads();
+    dfl c[NL], cm[NL];
+    double m[NL], dd[NL];
+    float cd[NL];
+#pragma unroll
+    for (int q = 0; q < NL; ++q) {
+        c[q] = df_from_double(Yc + lam[q]);
+        cm[q] = dfl{0.f, 0.f};
+        m[q] = 0.0; dd[q] = 0.0; cd[q] = 0.f;
+    }
+    const dfl vb = df_from_double(vB);
+    int cnt = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float p = phi[i];
+        // h = p^3 (10 + p (6 p - 15)), p exact
+        dfl t = df_add_f(df_two_prod(6.0f, p), -15.0f);
+        t = df_add_f(df_mul_f(t, p), 10.0f);
+        const dfl h = df_mul(df_mul_f(df_two_prod(p, p), p), t);
+        const dfl a = df_add_f(df_neg(h), 1.0f);
+        const dfl hv = df_mul(h, vb);
+        const float y = Y[i];
+#pragma unroll
+        for (int q = 0; q < NL; ++q) {
+            const dfl sg = df_sigmoid(df_add_f(c[q], y), tab);
+            cm[q] = df_add(cm[q], df_add(df_mul(a, sg), hv));
+            cd[q] = fmaf(a.hi * sg.hi, 1.0f - sg.hi, cd[q]);
+        }
+        if (++cnt == 16) {
+#pragma unroll
+            for (int q = 0; q < NL; ++q) {
+                m[q] += df_to_double(cm[q]); dd[q] += (double)cd[q];
+                cm[q] = dfl{0.f, 0.f}; cd[q] = 0.f;
+            }
+            cnt = 0;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NL; ++q) { m[q] += df_to_double(cm[q]); dd[q] += (double)cd[q]; }
 #pragma unroll
     for (int q = 0; q < NL; ++q) {
         AccSum2 s{m[q], dd[q]};
@@ -2159,15 +2221,24 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     const double target = c->target_mass;
     const double tol = P.zero_mode_tolerance_relative * std::max(std::fabs(target), 1.0);
     const long long N = c->g.N;
-    const int eb = 304;
     auto direct = [&](const double *lams, int nl, double *mass, double *der, bool exact = true) -> pfgb_status {
         if (nl < 1 || nl > 2) return fail("internal: 1 or 2 trial multipliers per evaluation");
         PFGB_CUDA_TRY(cudaMemcpyAsync(c->dscal + DS_EV, lams, sizeof(double) * nl, cudaMemcpyHostToDevice, c->stream));
+        // FP32 fields: the exact evaluation in double-float unless
+        // zero_mode_fp64_cells asks for FP64 per cell; that kernel is an
+        // arithmetic chain per cell and takes 8 blocks per SM, the others 2
+        const bool dfe = sizeof(T) == 4 && exact && !P.zero_mode_fp64_cells;
+        const int eb = dfe ? 1216 : 304;
         {
             ProfScope ps(c, {"zero_mode_eval", (double)N * 2.0 * sizeof(T)});
             const T *Yp = (const T *)c->Y, *ph = (const T *)c->phi[1 - c->cur];
             const double *lp = c->dscal + DS_EV;
-            if (exact && nl == 2) k_zm_eval<T, double, 2><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
+            if constexpr (sizeof(T) == 4) {
+                if (dfe && nl == 2) k_zm_eval_df<2><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
+                else if (dfe) k_zm_eval_df<1><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
+            }
+            if (dfe) {
+            } else if (exact && nl == 2) k_zm_eval<T, double, 2><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
             else if (exact) k_zm_eval<T, double, 1><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
             else if (nl == 2) k_zm_eval<T, T, 2><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
             else k_zm_eval<T, T, 1><<<eb, 256, 0, c->stream>>>(Yp, ph, N, c->Yc, P.v_B, lp, c->partials);
@@ -3210,6 +3281,53 @@ __global__ void k_load_state(const double *phi, const double *xB, const double *
     }
 }
 
+// FP32 fields hold the logit composition relative to its mean: Y* = Y - Yc
+// with Yc = mean(Y) in FP64.  The Y update is linear in Y with the constant
+// mode passed through unchanged, and every evaluation adds Yc back, so the
+// shift changes no result in exact arithmetic; the float transforms of Y then
+// carry roundoff in proportion to the spread of Y rather than to its mean
+// (the logit of a dilute composition, about -3.5), and the stored Y* has the
+// finer ulp of a centred value.  Y* is rounded once from the double logit
+// (xB given) or the double Y (checkpoint restart).
+template <typename T>
+__global__ void k_sum_field(const T *f, long long N, double *partials) {
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x)
+        acc += (double)f[i];
+    AccSum1 s{acc};
+    block_reduce_acc(s);
+    if (threadIdx.x == 0) reinterpret_cast<AccSum1 *>(partials)[blockIdx.x] = s;
+}
+
+__global__ void k_center_logit(const double *xB, const double *Y, float *Y_o, long long N, double eps, double Yclip,
+                               double shift) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double y = Y ? Y[i] : logit_clip(xB[i], eps, Yclip);
+        Y_o[i] = (float)(y - shift);
+    }
+}
+
+// sets Yc to the mean of the loaded Y and stores Y - Yc (FP32 fields)
+static pfgb_status center_logit(pfgb_ctx *c, const double *xB, const double *Y) {
+    const int nb = 304;
+    k_sum_field<float><<<nb, 256, 0, c->stream>>>((const float *)c->Y, c->g.N, c->partials);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    TRY(reduce_to<AccSum1>(c, nb, DS_ZM));
+    TRY(sync_read(c, DS_ZM, 1));
+    const double m = c->hscal[DS_ZM] / (double)c->g.N;
+    if (!std::isfinite(m)) {
+        pfgb_set_error_msg("non-finite mean of the loaded logit composition");
+        return PFGB_ERR_INVALID;
+    }
+    k_center_logit<<<nb, 256, 0, c->stream>>>(xB, Y, (float *)c->Y, c->g.N, c->p.xB_eps, c->p.Y_clip, m);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    c->Yc = m;
+    c->Yc_prev = m;
+    return PFGB_OK;
+}
+
 template <typename T>
 static pfgb_status load_device(pfgb_ctx *c, const double *phi, const double *xB, const double *eta,
                                const double *dYdt, bool keep_history) {
@@ -3225,11 +3343,15 @@ static pfgb_status load_device(pfgb_ctx *c, const double *phi, const double *xB,
                                                          c->p.xB_eps, c->p.Y_clip, c->p.v_B, c->partials);
     PFGB_CUDA_TRY(cudaGetLastError());
     c->Yc = 0.0;
+    c->Yc_prev = 0.0;
     c->dYoff = 0.0;
+    if (!keep) {
+        TRY(reduce_to<AccSum1>(c, nb, DS_ZM));
+        TRY(sync_read(c, DS_ZM, 1));
+        c->target_mass = c->hscal[DS_ZM];
+    }
+    if constexpr (sizeof(T) == 4) TRY(center_logit(c, xB, nullptr));
     if (keep) return PFGB_OK;
-    TRY(reduce_to<AccSum1>(c, nb, DS_ZM));
-    TRY(sync_read(c, DS_ZM, 1));
-    c->target_mass = c->hscal[DS_ZM];
     for (int i = 0; i < 6; ++i) PFGB_CUDA_TRY(cudaMemsetAsync(c->eps[i], 0, sizeof(float) * c->g.N, c->stream));
     c->warm_valid = 0;
     c->warm_count = 0;
@@ -3814,7 +3936,9 @@ pfgb_status pfgb_checkpoint_restore(pfgb_ctx *c, const char *path, const char *i
     for (int i = 0; i < 6; ++i) PFGB_CUDA_TRY(cudaMemsetAsync(c->eps[i], 0, sizeof(float) * N, c->stream));
     PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->Yc = 0.0;
+    c->Yc_prev = 0.0;
     c->dYoff = 0.0;
+    if (c->p.precision != PFGB_PREC_FP64) TRY(center_logit(c, nullptr, d + N));
     c->target_mass = st.target_mass_code;
     c->zm_lambda = st.last_lambda;
     c->zm_residual = st.last_residual_code;

@@ -202,7 +202,10 @@ typedef struct pfgb_params {
     /* provenance keys required in the parameter file (main_cuda.cu:1089-1146),
        used for output naming / physical time, not by the time step */
     int32_t pf_params_schema_version;
-    int32_t pad1;
+    /* zero-mode exact evaluations of an FP32-field run: 0 (default) in
+       double-float arithmetic per cell (about 48 bits, FP32 pipe) with FP64
+       sums; 1 in FP64 per cell.  FP64-field runs always evaluate in FP64. */
+    int32_t zero_mode_fp64_cells;
     double t_real_unit;
     double ic_vf_init_phi, ic_vf_target_phi, ic_phi_iface_w;
     double gamma_Jm2, lambda_sm_m, Vm_alpha_0_phys_m3mol;

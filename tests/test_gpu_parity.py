@@ -99,6 +99,33 @@ def test_zero_mode_conserves_mass(capi, prec):
             assert abs(d.mass_xBtot - target) <= 1e-12 * max(1.0, abs(target)), (d.mass_xBtot, target)
 
 
+@pytest.mark.parametrize("n", [32, 64])
+def test_zero_mode_double_float_evaluation(capi, n):
+    """FP32 fields: the zero mode's exact evaluations in double-float
+    arithmetic (the default) against FP64 per cell (zero_mode_fp64_cells = 1):
+    the same multipliers to 1e-10, the same fields to 1e-6, and both ledgers at
+    the reference's 1e-12."""
+    from cuda_sto_pf_gb300.solver import Solver
+    out = []
+    for fp64_cells in (0, 1):
+        p = params_for(capi, "c2.params", n=n, zero_mode_enabled=1, precision=1, zero_mode_fp64_cells=fp64_cells)
+        phi, xB, _ = _inputs(capi, p, n, False, seed=21)
+        lams = []
+        with Solver(p) as s:
+            s.load(phi, xB)
+            for _ in range(5):
+                st = s.step(1)
+                lams.append(st.zero_mode_lambda)
+                d = s.diagnostics()
+                assert abs(d.mass_xBtot - st.zero_mode_target_mass) <= 1e-12 * max(1.0, abs(st.zero_mode_target_mass))
+            out.append((lams, s.fields()))
+    (l0, f0), (l1, f1) = out
+    for a, b in zip(l0, l1):
+        assert abs(a - b) <= 1e-10 * max(1.0, abs(b)), (a, b)
+    for k in ("phi", "xB", "Y"):
+        assert rel_l2(f0[k], f1[k]) <= 1e-6, k
+
+
 def test_deterministic(capi):
     from cuda_sto_pf_gb300.solver import Solver
     p = params_for(capi, "c2.params", n=24, zero_mode_enabled=1, precision=1)
