@@ -18,7 +18,7 @@ c_float_p = POINTER(ctypes.c_float)
 PREC_FP64, PREC_FP32 = 0, 1
 MODEL_TWO_PHASE, MODEL_GP_ZONE = 0, 1
 MODE_DYNAMICS, MODE_MINIMIZE = 0, 1
-Y_LAGGED_RHS, Y_STORAGE_EXACT, Y_X_TRANSPORT_SPLIT = 0, 1, 2
+Y_LAGGED_RHS, Y_STORAGE_EXACT, Y_X_TRANSPORT_SPLIT, Y_Q_TRANSPORT_SPLIT = 0, 1, 2, 3
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device out of memory",
           4: "elastic solver did not converge", 5: "zero-mode mass solve rejected the step",
@@ -96,6 +96,7 @@ class StepStats(Structure):
         ("zero_mode_newton_steps", c_int32), ("zero_mode_bisection_steps", c_int32),
         ("zero_mode_lambda", c_double), ("zero_mode_residual", c_double),
         ("zero_mode_target_mass", c_double), ("mean_DY", c_double),
+        ("q_phase_rejected", c_int32), ("q_redistributed_cells", c_int32),
     ]
 
 

@@ -306,6 +306,7 @@ uint64_t pfgb_parameter_fingerprint(const pfgb_params *p) {
     add(flags, sizeof(flags));
     const char *ymode = p->pf_y_update_mode == PFGB_Y_STORAGE_EXACT      ? "storage_exact"
                         : p->pf_y_update_mode == PFGB_Y_X_TRANSPORT_SPLIT ? "x_transport_projection_split"
+                        : p->pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT ? "q_transport_projection_split"
                                                                            : kYUpdateLagged;
     for (const char *s : {kCompositionLegacy, ymode, kExplicitContextV1, kReactionTangentV1})
         add(s, std::strlen(s) + 1);

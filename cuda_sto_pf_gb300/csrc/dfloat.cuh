@@ -68,8 +68,11 @@ __device__ __forceinline__ dfl df_from_double(double v) {
 // 2^(j/64) from the double-float table, times 2^k (exact).
 // tab: dfexp::kExp2Tab staged in shared memory
 __device__ __forceinline__ dfl df_exp_neg(dfl w, const float2 *tab) {
-    const int N = __float2int_rn(w.hi * dfexp::kInvL64);   // -3694 .. 0
-    const float fN = (float)N;
+    // N = nearest integer to w.hi * 64/ln2 (-3694 .. 0) by the 1.5 * 2^23
+    // shift: its float bits hold N, so no float <-> int conversion is issued
+    const float tN = fmaf(w.hi, dfexp::kInvL64, 12582912.0f);
+    const float fN = tN - 12582912.0f;
+    const int N = __float_as_int(tN) - 0x4B400000;
     // w.hi - N C1 is exact (N C1 has 24 bits and is within a factor 2 of w.hi)
     dfl r = df_two_sum(fmaf(-fN, dfexp::kC1, w.hi), w.lo);
     r = df_add(r, df_neg(df_two_prod(fN, dfexp::kC2)));

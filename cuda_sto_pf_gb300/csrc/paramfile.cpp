@@ -222,8 +222,10 @@ extern "C" pfgb_status pfgb_params_set(pfgb_params *p, const char *key, const ch
             p->pf_y_update_mode = PFGB_Y_X_TRANSPORT_SPLIT;
             return PFGB_OK;
         }
-        // q_transport_projection_split is valid there but not built here:
-        // refused rather than run as another update
+        if (!strcmp(value, "q_transport_projection_split")) {
+            p->pf_y_update_mode = PFGB_Y_Q_TRANSPORT_SPLIT;
+            return PFGB_OK;
+        }
         return PFGB_ERR_INVALID;
     }
     if (!strcmp(key, "model_mode")) {

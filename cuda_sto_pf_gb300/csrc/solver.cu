@@ -51,6 +51,7 @@ struct DevState {
     KTab kt;
     T *phi_old, *phi_new, *eta_old, *eta_new, *Y, *dYdt;
     T *Yprev;           // Y_f at the start of the step (the elastic solve's Y)
+    T *q, *qb, *divr;   // q split: matrix storage (1 - h) x, its value before transport, div J
     TE *sig[6];         // stored stress of the elastic solve (minimize only, else null)
     T *mge, *mlap;      // minimize: explicit phi drive and Lap(phi)
     TE *eps[6];
@@ -83,6 +84,8 @@ struct pfgb_ctx {
     unsigned char *mx = nullptr, *my = nullptr, *mz = nullptr;
     void *phi[2] = {nullptr, nullptr}, *eta[2] = {nullptr, nullptr}, *Y = nullptr, *dYdt = nullptr;
     void *Yprev = nullptr;   // Y_f of the last step's start, for the stress export
+    void *q = nullptr, *qb = nullptr, *divr = nullptr;   // q split state (pf_y_update_mode q)
+    int q_rejected = 0, q_redistributed = 0;             // of the last step
     int cur = 0, ecur = 0;
     void *S[4] = {nullptr, nullptr, nullptr, nullptr};
     void *eps[6] = {}, *E[6] = {}, *U[3] = {};
@@ -682,7 +685,12 @@ struct OpFluxZ {
         const T pn = p.pn, pp = p.pp;
         const T phiY = (c.zm || c.prev_level) ? pn : pp;
         const T xBp = sigmoid_clip(Yv, T(c.Yclip), T(c.xBeps));
-        const T M = mobility<T>(c, phiY, p.eta, xBp);
+        // q split: the matrix channel alone, (1 - h) M_alpha with G_alpha at
+        // h = 0 (compute_flux_single_component_q_kernel, cuda_kernels.cu:2014-2037)
+        const T M = qmob ? (T(1) - pf_h(clamp01(phiY))) *
+                               stabilized_meff<T>(T(c.Da), gamma_thermo<T>(c.tc, xBp, T(0), T(c.Vm0), T(c.dVm),
+                                                                            T(c.Vmc)))
+                         : mobility<T>(c, phiY, p.eta, xBp);
         out[0] = M * g[0];
         out[1] = M * g[1];
         out[2] = M * g[2];
@@ -707,7 +715,8 @@ struct OpFluxZ {
         out[3] = src;
         out[4] = Yf;
     }
-    int no_src = 0;   // storage_exact: the divergence of J alone
+    int no_src = 0;   // storage_exact and the splits: the divergence of J alone
+    int qmob = 0;     // q split: the matrix-channel mobility
     __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
         const long long o = row * d.g.NzC + k;
         const T kz = T(d.kt.kz[k]);
@@ -849,6 +858,111 @@ struct OpXSplitFinalZ {
         d.dYdt[cell] = (yn - Yold) / T(c.dt);
     }
     __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
+};
+
+// ---------------------------------------------------------------------------
+// q_transport_projection_split (main_cuda.cu:27781-27783): the matrix storage
+// q = (1 - h) x of the conserved composition is the evolved coordinate.
+// Tolerances as the reference's calls: feasibility and bound 1e-12.
+// ---------------------------------------------------------------------------
+constexpr double kQTol = 1.0e-12;
+
+// the bounded context x = q / (1 - h) -> Y (the tail of
+// q_normalize_validate_and_reconstruct_kernel and
+// q_explicit_transport_and_reconstruct_kernel, cuda_kernels.cu:3032-3105);
+// xprev: the current composition, kept where there is no matrix storage
+template <typename T, typename PC>
+__device__ __forceinline__ T q_context_y(const PC &c, T q, T alpha, T xprev) {
+    const T eps = T(c.xBeps), yc = T(c.Yclip);
+    T x = alpha > T(1e-14) ? q / alpha : xprev;
+    x = fmin(fmax(x, eps), one_minus_eps(eps));
+    const T y = logit_clip(x, eps, yc);
+    return fmin(fmax(y, -yc), yc);
+}
+
+// q = (1 - h) x of the loaded raw fields (initialize_q_alpha_kernel, :2975-2984)
+template <typename T>
+__global__ void k_q_load(const double *phi, const double *xB, T *q, long long N) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x)
+        q[i] = T((1.0 - pf_h(clamp01(phi[i]))) * xB[i]);
+}
+
+// q = (1 - h(phi)) x(Y) (sync_q_from_phi_xB_kernel, :3107-3116; also the
+// rebuild after a rejected phase substep).  dydt: the end of the step, where
+// dY/dt = (Y - Y^n) / dt is also taken (update_dY_dt_prev_kernel), after a
+// redistribution may have moved Y
+template <typename T, typename TE>
+__global__ void k_q_sync(DevState<T, TE> d, PhysCT<T> c, const T *phi, int dydt) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.g.N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const T x = sigmoid_clip(d.Y[i] + T(d.Yc), T(c.Yclip), T(c.xBeps));
+        d.q[i] = (T(1) - pf_h(clamp01(phi[i]))) * x;
+        if (dydt) d.dYdt[i] = (d.Y[i] - d.Yprev[i]) / T(c.dt);
+    }
+}
+
+// the phase substep's storage transfer q -= (h^{n+1} - h^n) v_B
+// (apply_local_phase_storage_transfer_q_kernel, :2989-3019): infeasible cells
+// keep q and are counted (block partials); Y of the step's start is kept in
+// Yprev for dY/dt
+template <typename T, typename TE>
+__global__ void k_q_phase(DevState<T, TE> d, PhysCT<T> c) {
+    double bad = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.g.N;
+         i += (long long)gridDim.x * blockDim.x) {
+        d.Yprev[i] = d.Y[i];
+        const T ho = pf_h(clamp01(d.phi_old[i])), hn = pf_h(clamp01(d.phi_new[i]));
+        const T an = T(1) - hn;
+        const T qn = d.q[i] - (hn - ho) * T(c.vB);
+        if (!isfinite(qn) || qn < T(-kQTol) || qn > an + T(kQTol)) { bad += 1.0; continue; }
+        d.q[i] = fmin(fmax(qn, T(0)), an);
+    }
+    AccSum1 s{bad};
+    block_reduce_acc(s);
+    if (threadIdx.x == 0) reinterpret_cast<AccSum1 *>(d.partials)[blockIdx.x] = s;
+}
+
+// q_normalize_validate_and_reconstruct_kernel with invN = 1 (:3032-3069)
+template <typename T, typename TE>
+__global__ void k_q_reconstruct(DevState<T, TE> d, PhysCT<T> c, const T *phi) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.g.N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const T alpha = T(1) - pf_h(clamp01(phi[i]));
+        T q = d.q[i];
+        q = isfinite(q) ? fmin(fmax(q, T(0)), alpha) : T(0);
+        d.q[i] = q;
+        const T xprev = sigmoid_clip(d.Y[i] + T(d.Yc), T(c.Yclip), T(c.xBeps));
+        d.Y[i] = q_context_y<T>(c, q, alpha, xprev) - T(d.Yc);
+    }
+}
+
+// final z pass of the q split: div J to real space, the explicit transport
+// q + dt div J bounded to [0, 1 - h] with the out-of-bounds cells counted
+// (q_explicit_transport_and_reconstruct_kernel, :3071-3105), Y from the new
+// context, dY/dt against the step's start.  q and div J before the update
+// are kept for the local redistribution.
+template <typename T, typename TE>
+struct OpQTransportZ {
+    using Acc = AccSum1;
+    DevState<T, TE> d; PhysCT<T> c; const cplx_t<T> *src;
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * d.g.NzC + k]; }
+    __device__ void point(long long cell, const T *in, T *, Acc &acc) const {
+        const T divJ = in[0];
+        const T alpha = T(1) - pf_h(clamp01(d.phi_new[cell]));
+        const T q0 = d.q[cell];
+        d.qb[cell] = q0;
+        d.divr[cell] = divJ;
+        const T qt = q0 + T(c.dt) * divJ;
+        if (!isfinite(qt) || qt < T(-kQTol) || qt > alpha + T(kQTol)) acc.s += 1.0;
+        const T q = isfinite(qt) ? fmin(fmax(qt, T(0)), alpha) : T(0);
+        d.q[cell] = q;
+        const T xprev = sigmoid_clip(d.Y[cell] + T(d.Yc), T(c.Yclip), T(c.xBeps));
+        const T yn = q_context_y<T>(c, q, alpha, xprev) - T(d.Yc);
+        d.Y[cell] = yn;
+        d.dYdt[cell] = (yn - d.Yprev[cell]) / T(c.dt);
+    }
+    __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
+    __device__ void finish(int b, const Acc &a) const { reinterpret_cast<Acc *>(d.partials)[b] = a; }
 };
 
 // (6) final z pass: store Y_f, dY/dt, and the zero-mode statistics
@@ -1835,6 +1949,9 @@ static DevState<T, TE> dev_state(pfgb_ctx *c) {
     d.eta_new = (T *)c->eta[1 - c->ecur];
     d.Y = (T *)c->Y;
     d.Yprev = (T *)c->Yprev;
+    d.q = (T *)c->q;
+    d.qb = (T *)c->qb;
+    d.divr = (T *)c->divr;
     for (int i = 0; i < 6; ++i) d.sig[i] = (TE *)c->sig[i];
     d.mge = (T *)c->mge;
     d.mlap = (T *)c->mlap;
@@ -2355,6 +2472,124 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     return PFGB_OK;
 }
 
+// the local redistribution of the q split's out-of-bounds transport, on
+// the host as in the reference (q_transport_conservative_local_redistribution,
+// main_cuda.cu:22362-22456): every cell's trial q0 + dt div J is bounded to
+// [0, 1 - h]; in cell order each cell's excess (deficit) goes to the cells of
+// growing Chebyshev shells around it, radius 1 to 8, periodic, in the order
+// of the offsets (di, dj, dk) from -r to r, within their capacity 1 - h - q
+// (storage q).  Fails when an amount stays unresolved beyond the tolerance.
+static bool q_redistribute_host(int Nx, int Ny, int Nz, const std::vector<double> &q0, const std::vector<double> &divJ,
+                                const std::vector<double> &phi, double dt, std::vector<double> &q, int *violating,
+                                double *unresolved_out) {
+    const size_t N = (size_t)Nx * Ny * Nz;
+    const int R = 8;
+    std::vector<double> alpha(N), res(N);
+    q.assign(N, 0.0);
+    int nv = 0;
+    for (size_t i = 0; i < N; ++i) {
+        alpha[i] = 1.0 - pf_h(clamp01(phi[i]));
+        const double trial = q0[i] + dt * divJ[i];
+        const double b = std::fmin(std::fmax(trial, 0.0), alpha[i]);
+        q[i] = b;
+        res[i] = trial - b;
+        if (!std::isfinite(trial) || std::fabs(res[i]) > kQTol) ++nv;
+    }
+    double unresolved = 0.0;
+    for (size_t i = 0; i < N; ++i) {
+        double amt = res[i];
+        if (!std::isfinite(amt)) { unresolved = INFINITY; continue; }
+        if (std::fabs(amt) <= kQTol) continue;
+        const int k0 = (int)(i % Nz), j0 = (int)((i / Nz) % Ny), i0 = (int)(i / ((size_t)Nz * Ny));
+        for (int r = 1; r <= R && std::fabs(amt) > kQTol; ++r)
+            for (int di = -r; di <= r && std::fabs(amt) > kQTol; ++di)
+                for (int dj = -r; dj <= r && std::fabs(amt) > kQTol; ++dj)
+                    for (int dk = -r; dk <= r && std::fabs(amt) > kQTol; ++dk) {
+                        if (std::max(std::max(std::abs(di), std::abs(dj)), std::abs(dk)) != r) continue;
+                        const size_t n = ((size_t)((i0 + di + Nx) % Nx) * Ny + (size_t)((j0 + dj + Ny) % Ny)) * Nz +
+                                         (size_t)((k0 + dk + Nz) % Nz);
+                        if (amt > 0.0) {
+                            const double cap = alpha[n] - q[n];
+                            if (cap <= 0.0) continue;
+                            const double mv = std::fmin(amt, cap);
+                            q[n] += mv;
+                            amt -= mv;
+                        } else {
+                            const double av = q[n];
+                            if (av <= 0.0) continue;
+                            const double mv = std::fmin(-amt, av);
+                            q[n] -= mv;
+                            amt += mv;
+                        }
+                    }
+        unresolved += std::fabs(amt);
+    }
+    *violating = nv;
+    *unresolved_out = unresolved;
+    return std::isfinite(unresolved) && unresolved <= kQTol * std::max(1.0, (double)nv);
+}
+
+// the q split's phase substep (main_cuda.cu:30241-30277): the storage transfer;
+// where it is infeasible anywhere, the whole phi substep is rejected (phi
+// returns to phi^n and q is rebuilt from it); then the bounded context
+template <typename T, typename TE>
+static pfgb_status q_phase(pfgb_ctx *c, const DevState<T, TE> &d, const PhysCT<T> &pc) {
+    const int nb = 304;
+    k_q_phase<T, TE><<<nb, 256, 0, c->stream>>>(d, pc);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    TRY(reduce_to<AccSum1>(c, nb, DS_ZM));
+    TRY(sync_read(c, DS_ZM, 1));
+    c->q_rejected = c->hscal[DS_ZM] > 0.5;
+    if (c->q_rejected) {
+        PFGB_CUDA_TRY(cudaMemcpyAsync(d.phi_new, d.phi_old, sizeof(T) * (size_t)c->g.N, cudaMemcpyDeviceToDevice,
+                                      c->stream));
+        k_q_sync<T, TE><<<nb, 256, 0, c->stream>>>(d, pc, d.phi_new, 0);
+        PFGB_CUDA_TRY(cudaGetLastError());
+    }
+    k_q_reconstruct<T, TE><<<nb, 256, 0, c->stream>>>(d, pc, d.phi_new);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    return PFGB_OK;
+}
+
+// the q split's composition update after the flux divergence
+// (main_cuda.cu:30648-30707, 31227-31229): explicit transport in the final z
+// pass; where a cell left its bounds, the host redistribution and the bounded
+// context; then q from the new composition
+template <typename T, typename TE>
+static pfgb_status q_transport(pfgb_ctx *c, const DevState<T, TE> &d, const PhysCT<T> &pc, double Nf) {
+    int nbq = 0;
+    TRY((launch_z<T, 1, 0>(c, OpQTransportZ<T, TE>{d, pc, d.S[0]}, "z_q_transport", 7.0 * Nf * sizeof(T), &nbq)));
+    TRY(reduce_to<AccSum1>(c, nbq, DS_ZM));
+    TRY(sync_read(c, DS_ZM, 1));
+    c->q_redistributed = 0;
+    const int nb = 304;
+    if (c->hscal[DS_ZM] > 0.5) {
+        const size_t N = (size_t)c->g.N;
+        std::vector<T> hq(N), hd(N), hp(N);
+        PFGB_CUDA_TRY(cudaMemcpyAsync(hq.data(), d.qb, sizeof(T) * N, cudaMemcpyDeviceToHost, c->stream));
+        PFGB_CUDA_TRY(cudaMemcpyAsync(hd.data(), d.divr, sizeof(T) * N, cudaMemcpyDeviceToHost, c->stream));
+        PFGB_CUDA_TRY(cudaMemcpyAsync(hp.data(), d.phi_new, sizeof(T) * N, cudaMemcpyDeviceToHost, c->stream));
+        PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));
+        std::vector<double> q0(hq.begin(), hq.end()), dj(hd.begin(), hd.end()), ph(hp.begin(), hp.end()), qa;
+        int nv = 0;
+        double unresolved = 0.0;
+        if (!q_redistribute_host(c->g.Nx, c->g.Ny, c->g.Nz, q0, dj, ph, c->p.dt, qa, &nv, &unresolved)) {
+            pfgb_set_error_msg("q transport step rejected at step %d: %d cells out of bounds, unresolved mass %.17e",
+                               c->step + 1, nv, unresolved);
+            return PFGB_ERR_NONCONVERGED;
+        }
+        std::vector<T> hqa(qa.begin(), qa.end());
+        PFGB_CUDA_TRY(cudaMemcpyAsync(d.q, hqa.data(), sizeof(T) * N, cudaMemcpyHostToDevice, c->stream));
+        k_q_reconstruct<T, TE><<<nb, 256, 0, c->stream>>>(d, pc, d.phi_new);
+        PFGB_CUDA_TRY(cudaGetLastError());
+        PFGB_CUDA_TRY(cudaStreamSynchronize(c->stream));   // hqa is read by the copy
+        c->q_redistributed = nv;
+    }
+    k_q_sync<T, TE><<<nb, 256, 0, c->stream>>>(d, pc, d.phi_new, c->q_redistributed ? 1 : 0);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    return PFGB_OK;
+}
+
 // Y (composition) update: mu -> flux -> semi-implicit update -> dY/dt and
 // the zero mode (main_cuda.cu:30280-30800, 31618-31623).  d.phi_old = phi^n,
 // d.phi_new = phi^{n+1}; Y and the stored strain are those of the step start.
@@ -2384,8 +2619,10 @@ static pfgb_status y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_sta
         TRY((launch_axis<T, 3, 3, +1, 0>(c, 1, io, OpCopy<T, 3>{}, "y_inv3")));
     }
     const bool storage_exact = P.pf_y_update_mode == PFGB_Y_STORAGE_EXACT;
-    const bool divj_real = storage_exact || P.pf_y_update_mode == PFGB_Y_X_TRANSPORT_SPLIT;
-    TRY((launch_z<T, 3, 5>(c, OpFluxZ<T, TE>{d, pc, divj_real ? 1 : 0}, "z_flux", (4.0 + pc.gp) * Nf * sizeof(T))));
+    const bool qsplit = P.pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT;
+    const bool divj_real = storage_exact || qsplit || P.pf_y_update_mode == PFGB_Y_X_TRANSPORT_SPLIT;
+    TRY((launch_z<T, 3, 5>(c, OpFluxZ<T, TE>{d, pc, divj_real ? 1 : 0, qsplit ? 1 : 0}, "z_flux",
+                           (4.0 + pc.gp) * Nf * sizeof(T))));
     if (divj_real) {
         {
             AxisIO<T, 4, 3> io;
@@ -2403,6 +2640,8 @@ static pfgb_status y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_sta
         if (storage_exact) {
             TRY((launch_z<T, 1, 0>(c, OpStorageExactZ<T, TE>{d, pc, d.S[0], P.gp_h_alpha_eps}, "z_storage_exact",
                                    5.0 * Nf * sizeof(T))));
+        } else if (qsplit) {
+            TRY((q_transport<T, TE>(c, d, pc, Nf)));
         } else {
             const double mDx = P.D_alpha * P.pf_composition_stabilizer_Dalpha_multiplier;
             TRY((launch_z<T, 1, 2>(c, OpXSplitSrcZ<T, TE>{d, pc, P.pf_matrix_storage_floor}, "z_xsplit_src",
@@ -2483,7 +2722,15 @@ static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
         TRY((launch_z<T, 1, 0>(c, OpACStoreZ<T, TE>{d.S[0], d.eta_new, c->g.NzC, T(0), T(1)}, "z_ac_store", Nf * sizeof(T))));
     }
 
+    // q split: the phase substep's storage transfer
+    c->q_rejected = 0;
+    if (P.pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT) TRY((q_phase<T, TE>(c, d, pc)));
+
     TRY((y_update<T, TE>(c, d, st)));
+    if (st) {
+        st->q_phase_rejected = c->q_rejected;
+        st->q_redistributed_cells = c->q_redistributed;
+    }
     c->cur = 1 - c->cur;
     if (pc.gp) c->ecur = 1 - c->ecur;
     c->step++;
@@ -2952,7 +3199,10 @@ static void build_physc(pfgb_ctx *c) {
     // phi_elastic_coupling_enabled (main_cuda.cu:24868)
     k.coupling = P.elastic_enabled && (!k.gp_el || P.gp_elastic_active_phi);
     k.zm = P.zero_mode_enabled;
-    k.prev_level = P.enable_Y_rhs_previous_time_level;
+    // the q split evaluates mu and J at phi^{n+1} whatever the previous-level
+    // switch says (phi_for_Y_explicit, main_cuda.cu:30286-30291); the switch
+    // acts on nothing else there
+    k.prev_level = P.enable_Y_rhs_previous_time_level && P.pf_y_update_mode != PFGB_Y_Q_TRANSPORT_SPLIT;
     k.disable_gamma = P.disable_Y_rhs_gamma_term;
     k.xb_raw = P.zero_mode_enabled;
     k.xbcap = 2.0;
@@ -3177,9 +3427,9 @@ static pfgb_status validate(const pfgb_params *p) {
             return PFGB_ERR_UNSUPPORTED;
         }
     }
-    if (p->pf_y_update_mode < PFGB_Y_LAGGED_RHS || p->pf_y_update_mode > PFGB_Y_X_TRANSPORT_SPLIT) {
-        pfgb_set_error_msg("pf_y_update_mode: lagged_rhs, storage_exact or x_transport_projection_split (the q "
-                           "split is not built)");
+    if (p->pf_y_update_mode < PFGB_Y_LAGGED_RHS || p->pf_y_update_mode > PFGB_Y_Q_TRANSPORT_SPLIT) {
+        pfgb_set_error_msg("pf_y_update_mode: lagged_rhs, storage_exact, x_transport_projection_split or "
+                           "q_transport_projection_split");
         return PFGB_ERR_UNSUPPORTED;
     }
     if (p->pf_y_update_mode == PFGB_Y_X_TRANSPORT_SPLIT &&
@@ -3199,12 +3449,12 @@ static pfgb_status validate(const pfgb_params *p) {
         return PFGB_ERR_UNSUPPORTED;
     }
     // the zero mode and minimize refuse every mode but lagged_rhs
-    // (main_cuda.cu:24600-24612, 24692-24702); storage_exact and the x split
-    // without the GP storage coupling are the two_phase paths
-    // (main_cuda.cu:30564-30566, 30627-30628)
+    // (main_cuda.cu:24600-24612, 24692-24702); storage_exact and the x and q
+    // splits without the GP storage coupling are the two_phase paths
+    // (main_cuda.cu:27781-27783, 30564-30566, 30627-30628)
     if (p->pf_y_update_mode != PFGB_Y_LAGGED_RHS &&
         (p->zero_mode_enabled || p->model_mode != PFGB_MODEL_TWO_PHASE || p->mode != PFGB_MODE_DYNAMICS)) {
-        pfgb_set_error_msg("pf_y_update_mode storage_exact / x_transport_projection_split: two_phase dynamics with "
+        pfgb_set_error_msg("pf_y_update_mode storage_exact / x_ or q_transport_projection_split: two_phase dynamics with "
                            "the zero mode off (the zero mode owns lagged_rhs; the GP storage-coupled modes are not "
                            "built)");
         return PFGB_ERR_UNSUPPORTED;
@@ -3226,6 +3476,7 @@ static void ctx_free(pfgb_ctx *c) {
     f(c->eta[0]);
     if (c->eta[1] != c->eta[0]) f(c->eta[1]);
     f(c->Y); f(c->Yprev); f(c->dYdt);
+    f(c->q); f(c->qb); f(c->divr);
     for (int i = 0; i < 4; ++i) f(c->S[i]);
     for (int i = 0; i < 6; ++i) { f(c->eps[i]); f(c->E[i]); }
     for (int i = 0; i < 3; ++i) f(c->U[i]);
@@ -3351,6 +3602,10 @@ static pfgb_status load_device(pfgb_ctx *c, const double *phi, const double *xB,
         c->target_mass = c->hscal[DS_ZM];
     }
     if constexpr (sizeof(T) == 4) TRY(center_logit(c, xB, nullptr));
+    if (c->q) {   // q split: q = (1 - h) x of the loaded fields (main_cuda.cu:28051-28053)
+        k_q_load<T><<<nb, 256, 0, c->stream>>>(phi, xB, (T *)c->q, c->g.N);
+        PFGB_CUDA_TRY(cudaGetLastError());
+    }
     if (keep) return PFGB_OK;
     for (int i = 0; i < 6; ++i) PFGB_CUDA_TRY(cudaMemsetAsync(c->eps[i], 0, sizeof(float) * c->g.N, c->stream));
     c->warm_valid = 0;
@@ -3468,6 +3723,11 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
     A_(&c->Y, rs * N);
     A_(&c->Yprev, rs * N);
     A_(&c->dYdt, rs * N);
+    if (pin->pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT) {
+        A_(&c->q, rs * N);
+        A_(&c->qb, rs * N);
+        A_(&c->divr, rs * N);
+    }
     for (int i = 0; i < 4; ++i) { A_(&c->S[i], 2 * rs * Nk); }
     for (int i = 0; i < 6; ++i) { A_(&c->eps[i], sizeof(float) * N); }
     if (pin->elastic_enabled) {

@@ -592,7 +592,9 @@ int main(int argc, char **argv) {
     if (c.pos_Nx > 0) P.Nx = c.pos_Nx;
     if (c.pos_Ny > 0) P.Ny = c.pos_Ny;
     if (c.pos_Nz > 0) P.Nz = c.pos_Nz;
-    if (c.pos_elastic >= 0) P.elastic_enabled = c.pos_elastic ? 1 : 0;
+    // the positional elastic switch is a default the parameter file may
+    // override (it is set before the file is read, main_cuda.cu:22534-22540);
+    // the --elastic flag is read after it and wins
     if (c.elastic >= 0) P.elastic_enabled = c.elastic ? 1 : 0;
     if (std::isfinite(c.temperature_C)) P.temperature_C = c.temperature_C;
     if (!c.zero_mode.empty()) {
@@ -1019,6 +1021,14 @@ int main(int argc, char **argv) {
         const double w = std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
         if (st != PFGB_OK) { rc = fail(st, "pfgb_step"); break; }
         wall.push_back(w);
+        if (P.pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT) {
+            // the q split's events, as the reference prints them (main_cuda.cu:30262-30266, 30701-30706)
+            if (s.q_phase_rejected)
+                printf("PF_Q_PHASE_SUBSTEP_REJECTED step=%d policy=rollback_entire_phi_substep\n", step);
+            if (s.q_redistributed_cells)
+                printf("PF_Q_TRANSPORT_LOCAL_REDISTRIBUTION step=%d violating_cells=%d global_mass_loss=0\n", step,
+                       s.q_redistributed_cells);
+        }
         if (accel) {
             el_nonconv += s.elastic_converged ? 0 : 1;
             el_iters_total += (unsigned long long)s.elastic_iterations;

@@ -78,7 +78,7 @@ enum { PFGB_MODEL_TWO_PHASE = 0, PFGB_MODEL_GP_ZONE = 1 };
 /* mode (pf_params.h: 0=dynamics, 1=minimize) */
 enum { PFGB_MODE_DYNAMICS = 0, PFGB_MODE_MINIMIZE = 1 };
 /* pf_y_update_mode (pf_params.h:345) */
-enum { PFGB_Y_LAGGED_RHS = 0, PFGB_Y_STORAGE_EXACT = 1, PFGB_Y_X_TRANSPORT_SPLIT = 2 };
+enum { PFGB_Y_LAGGED_RHS = 0, PFGB_Y_STORAGE_EXACT = 1, PFGB_Y_X_TRANSPORT_SPLIT = 2, PFGB_Y_Q_TRANSPORT_SPLIT = 3 };
 
 /*
  * Stiffness tensors are the 21 independent Voigt entries in the reference's
@@ -161,7 +161,15 @@ typedef struct pfgb_params {
        or PFGB_Y_X_TRANSPORT_SPLIT (two_phase, zero mode off: x_alpha advanced
        semi-implicitly with the source div J / (1 - h) where 1 - h is at least
        pf_matrix_storage_floor, stabilised by D_alpha times
-       pf_composition_stabilizer_Dalpha_multiplier, main_cuda.cu:30564-30676) */
+       pf_composition_stabilizer_Dalpha_multiplier, main_cuda.cu:30564-30676);
+       or PFGB_Y_Q_TRANSPORT_SPLIT (two_phase dynamics, zero mode off: the
+       matrix storage q = (1 - h) x_alpha is the conserved coordinate; a local
+       phase transfer q -= dh v_B after the phi update (the phi substep is
+       rejected where it would leave [0, 1 - h]), explicit transport
+       q += dt div J with the matrix-channel mobility (1 - h) M_alpha, a
+       sequential local redistribution where transport leaves the bounds, and
+       x_alpha = q / (1 - h); main_cuda.cu:27781-27783, 30241-30277,
+       30648-30707, 22362-22456, cuda_kernels.cu:2014-2037, 2975-3116) */
     int32_t pf_y_update_mode;
     int32_t pad_y;
     double gp_h_alpha_eps;
@@ -264,6 +272,11 @@ typedef struct pfgb_step_stats {
     double zero_mode_residual;
     double zero_mode_target_mass;
     double mean_DY;
+    /* q_transport_projection_split: the step's phase substep was rejected
+       (infeasible local storage transfer, phi kept), and the cells whose
+       transport left [0, 1 - h] and went through the local redistribution */
+    int32_t q_phase_rejected;
+    int32_t q_redistributed_cells;
 } pfgb_step_stats;
 
 /* Minimize iteration statistics (energy_minimize.csv row and the stopping

@@ -242,6 +242,8 @@ struct pfo_state {
     double *phi, *eta, *Y, *xB, *dYdt;
     double *phi_n, *eta_prev, *Y_n, *xB_prev;
     double *rhs, *mu, *scr, *divJ, *lapY, *mass_t, *der_t;
+    double *q, *q_before;   /* q_transport_projection_split: matrix storage (1 - h) x */
+    int q_rejected, q_redistributed;
     cpx *phi_k, *rhs_k, *mu_k, *divJ_k, *Y_k, *scr_k, *eta_k;
     /* elastic */
     double *eps_r[6], *sig_r[6];
@@ -294,7 +296,7 @@ pfo_state *pfo_create(const pfgb_params *pin) {
     const size_t rb = sizeof(double) * s->N, kb = sizeof(cpx) * s->Nk;
     double **rf_[] = {&s->phi, &s->eta, &s->Y, &s->xB, &s->dYdt, &s->phi_n, &s->eta_prev,
                       &s->Y_n, &s->xB_prev, &s->rhs, &s->mu, &s->scr, &s->divJ, &s->lapY,
-                      &s->mass_t, &s->der_t};
+                      &s->mass_t, &s->der_t, &s->q, &s->q_before};
     for (size_t i = 0; i < sizeof(rf_) / sizeof(rf_[0]); ++i) *rf_[i] = (double *)xalloc(rb);
     cpx **kf_[] = {&s->phi_k, &s->rhs_k, &s->mu_k, &s->divJ_k, &s->Y_k, &s->scr_k, &s->eta_k};
     for (size_t i = 0; i < sizeof(kf_) / sizeof(kf_[0]); ++i) *kf_[i] = (cpx *)xalloc(kb);
@@ -342,7 +344,8 @@ pfo_state *pfo_create(const pfgb_params *pin) {
 void pfo_destroy(pfo_state *s) {
     if (!s) return;
     double *rr[] = {s->phi, s->eta, s->Y, s->xB, s->dYdt, s->phi_n, s->eta_prev, s->Y_n,
-                    s->xB_prev, s->rhs, s->mu, s->scr, s->divJ, s->lapY, s->mass_t, s->der_t};
+                    s->xB_prev, s->rhs, s->mu, s->scr, s->divJ, s->lapY, s->mass_t, s->der_t, s->q,
+                    s->q_before};
     for (size_t i = 0; i < sizeof(rr) / sizeof(rr[0]); ++i) free(rr[i]);
     cpx *kk[] = {s->phi_k, s->rhs_k, s->mu_k, s->divJ_k, s->Y_k, s->scr_k, s->eta_k};
     for (size_t i = 0; i < sizeof(kk) / sizeof(kk[0]); ++i) free(kk[i]);
@@ -1102,6 +1105,13 @@ static void flux_field(pfo_state *s, const double *phiY, const double *etaY) {
                                 P->Vm_compound, T, sc, cv);
             double Ma = o_meff(P->D_alpha, Ga);
             M = ha * Ma + hg * P->gp_M_GP + hb * P->gp_M_beta;
+        } else if (P->pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT) {
+            /* compute_flux_single_component_q_kernel, :2014-2037: the matrix
+             * channel alone, (1 - h) M_alpha with G_alpha at h = 0 */
+            double a = 1.0 - o_h(o_clamp01(phiY[idx]));
+            double Ga = o_gamma(s->xB_prev[idx], 0.0, P->Vm_alpha_0, P->dVm_alpha_dxB,
+                                P->Vm_compound, T, sc, cv);
+            M = a * o_meff(P->D_alpha, Ga);
         } else {       /* compute_flux_single_component_kernel, :1985 */
             double h = o_h(phiY[idx]);
             double Dm = o_Dmix(h, P->D_alpha, P->D_compound);
@@ -1173,6 +1183,193 @@ void pfo_test_xsplit_final(pfo_state *s, double dt, const double *x, const doubl
     xsplit_final(s, dt);
     memcpy(Y, s->Y, b);
     memcpy(xB, s->xB, b);
+}
+
+/* q_transport_projection_split (main_cuda.cu:27781-27783): the matrix
+ * storage q = (1 - h) x of the conserved composition is the evolved
+ * coordinate.  Bounds and tolerances as the reference's calls: feasibility
+ * and bound tolerance 1e-12, redistribution radius 8. */
+#define Q_TOL 1.0e-12
+
+/* initialize_q_alpha_kernel / sync_q_from_phi_xB_kernel, cuda_kernels.cu:2975-2984, 3107-3116 */
+static void q_from_phi_xB(pfo_state *s) {
+    RLOOP_BEGIN(s)
+        s->q[idx] = (1.0 - o_h(o_clamp01(s->phi[idx]))) * s->xB[idx];
+    RLOOP_END
+}
+
+/* the bounded context x = q / (1 - h) -> Y -> x (the tail shared by
+ * q_normalize_validate_and_reconstruct_kernel :3032-3069 and
+ * q_explicit_transport_and_reconstruct_kernel :3071-3105) */
+static void q_context(pfo_state *s, size_t idx, double q, double alpha) {
+    const pfgb_params *P = &s->p;
+    double x = s->xB[idx];
+    if (alpha > 1.0e-14) x = q / alpha;
+    x = fmin(fmax(x, P->xB_eps), 1.0 - P->xB_eps);
+    double y = o_logit(x, P->xB_eps, P->Y_clip);
+    y = fmin(fmax(y, -P->Y_clip), P->Y_clip);
+    s->xB[idx] = o_sigmoid(y, P->Y_clip, P->xB_eps);
+    s->Y[idx] = y;
+}
+
+/* q_normalize_validate_and_reconstruct_kernel with invN = 1, :3032-3069 */
+static void q_reconstruct(pfo_state *s) {
+    RLOOP_BEGIN(s)
+        const double alpha = 1.0 - o_h(o_clamp01(s->phi[idx]));
+        double q = s->q[idx];
+        q = isfinite(q) ? fmin(fmax(q, 0.0), alpha) : 0.0;
+        s->q[idx] = q;
+        q_context(s, idx, q, alpha);
+    RLOOP_END
+}
+
+/* the phase substep's storage transfer q -= (h_new - h_old) v_B
+ * (apply_local_phase_storage_transfer_q_kernel, :2989-3019); where it is
+ * infeasible anywhere the whole phi substep is rejected: phi returns to
+ * phi^n and q is rebuilt from it (main_cuda.cu:30241-30266).  Then the
+ * context is refreshed (:30271-30274). */
+static long long q_phase_cells(pfo_state *s) {
+    const pfgb_params *P = &s->p;
+    long long bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+    for (long long i = 0; i < (long long)s->N; ++i) {
+        const double ho = o_h(o_clamp01(s->phi_n[i])), hn = o_h(o_clamp01(s->phi[i]));
+        const double an = 1.0 - hn;
+        const double qn = s->q[i] - (hn - ho) * P->v_B;
+        if (!isfinite(qn) || qn < -Q_TOL || qn > an + Q_TOL) { ++bad; continue; }
+        s->q[i] = fmin(fmax(qn, 0.0), an);
+    }
+    return bad;
+}
+static void q_phase(pfo_state *s) {
+    const long long bad = q_phase_cells(s);
+    s->q_rejected = bad > 0;
+    if (bad) {
+        memcpy(s->phi, s->phi_n, sizeof(double) * s->N);
+        q_from_phi_xB(s);
+    }
+    q_reconstruct(s);
+}
+
+/* the host's local redistribution of out-of-bounds transport
+ * (q_transport_conservative_local_redistribution, main_cuda.cu:22362-22456):
+ * each cell's trial q + dt divJ is bounded to [0, 1 - h]; in cell order the
+ * excess (or deficit) goes to the cells of growing Chebyshev shells around
+ * it, up to radius 8, within their capacity (1 - h - q) or storage (q).
+ * Returns 0 when an amount stays unresolved beyond the tolerance. */
+static int q_redistribute(pfo_state *s, double dt, int *violating) {
+    const int Nx = s->Nx, Ny = s->Ny, Nz = s->Nz, R = 8;
+    double *alpha = s->mass_t, *res = s->der_t;
+    int nv = 0;
+    for (size_t i = 0; i < s->N; ++i) {
+        alpha[i] = 1.0 - o_h(o_clamp01(s->phi[i]));
+        const double trial = s->q_before[i] + dt * s->divJ[i];
+        const double b = fmin(fmax(trial, 0.0), alpha[i]);
+        s->q[i] = b;
+        res[i] = trial - b;
+        if (!isfinite(trial) || fabs(res[i]) > Q_TOL) ++nv;
+    }
+    double unresolved = 0.0;
+    for (size_t i = 0; i < s->N; ++i) {
+        double amt = res[i];
+        if (!isfinite(amt)) { unresolved = INFINITY; continue; }
+        if (fabs(amt) <= Q_TOL) continue;
+        const int k0 = (int)(i % Nz), j0 = (int)((i / Nz) % Ny), i0 = (int)(i / ((size_t)Nz * Ny));
+        for (int r = 1; r <= R && fabs(amt) > Q_TOL; ++r)
+            for (int di = -r; di <= r && fabs(amt) > Q_TOL; ++di)
+                for (int dj = -r; dj <= r && fabs(amt) > Q_TOL; ++dj)
+                    for (int dk = -r; dk <= r && fabs(amt) > Q_TOL; ++dk) {
+                        const int m = abs(di) > abs(dj) ? abs(di) : abs(dj);
+                        if ((m > abs(dk) ? m : abs(dk)) != r) continue;
+                        const size_t n = ((size_t)((i0 + di + Nx) % Nx) * Ny + (size_t)((j0 + dj + Ny) % Ny)) * Nz +
+                                         (size_t)((k0 + dk + Nz) % Nz);
+                        if (amt > 0.0) {
+                            const double cap = alpha[n] - s->q[n];
+                            if (cap <= 0.0) continue;
+                            const double mv = fmin(amt, cap);
+                            s->q[n] += mv;
+                            amt -= mv;
+                        } else {
+                            const double av = s->q[n];
+                            if (av <= 0.0) continue;
+                            const double mv = fmin(-amt, av);
+                            s->q[n] -= mv;
+                            amt += mv;
+                        }
+                    }
+        unresolved += fabs(amt);
+    }
+    *violating = nv;
+    return isfinite(unresolved) && unresolved <= Q_TOL * fmax(1.0, (double)nv);
+}
+
+/* the composition update of the q split from divJ (real, normalised):
+ * q_explicit_transport_and_reconstruct_kernel (:3071-3105), the local
+ * redistribution and q_normalize_validate_and_reconstruct_kernel when a cell
+ * left its bounds (main_cuda.cu:30648-30707), sync_q_from_phi_xB_kernel
+ * (:31227-31229) and update_dY_dt_prev_kernel */
+static long long q_transport_cells(pfo_state *s, double dt) {
+    long long viol = 0;
+#pragma omp parallel for schedule(static) reduction(+ : viol)
+    for (long long i = 0; i < (long long)s->N; ++i) {
+        const double alpha = 1.0 - o_h(o_clamp01(s->phi[i]));
+        const double qt = s->q[i] + dt * s->divJ[i];
+        if (!isfinite(qt) || qt < -Q_TOL || qt > alpha + Q_TOL) ++viol;
+        const double q = isfinite(qt) ? fmin(fmax(qt, 0.0), alpha) : 0.0;
+        s->q[i] = q;
+        q_context(s, (size_t)i, q, alpha);
+    }
+    return viol;
+}
+static int q_transport(pfo_state *s, double dt) {
+    memcpy(s->q_before, s->q, sizeof(double) * s->N);
+    const long long viol = q_transport_cells(s, dt);
+    s->q_redistributed = 0;
+    if (viol) {
+        int nv = 0;
+        if (!q_redistribute(s, dt, &nv)) return PFGB_ERR_NONCONVERGED;
+        s->q_redistributed = nv;
+        q_reconstruct(s);
+    }
+    q_from_phi_xB(s);
+    RLOOP_BEGIN(s) s->dYdt[idx] = (s->Y[idx] - s->Y_n[idx]) / dt; RLOOP_END
+    return PFGB_OK;
+}
+
+/* test hooks (the pinning tests) for the q split's per-cell functions */
+long long pfo_test_q_phase(pfo_state *s, const double *phi_new, const double *phi_old, const double *q_in,
+                           double *q_out) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->phi, phi_new, b);
+    memcpy(s->phi_n, phi_old, b);
+    memcpy(s->q, q_in, b);
+    const long long bad = q_phase_cells(s);
+    memcpy(q_out, s->q, b);
+    return bad;
+}
+long long pfo_test_q_transport(pfo_state *s, double dt, const double *q_in, const double *divJ, const double *phi,
+                               const double *xB_in, double *q_out, double *xB_out, double *Y_out) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->q, q_in, b);
+    memcpy(s->divJ, divJ, b);
+    memcpy(s->phi, phi, b);
+    memcpy(s->xB, xB_in, b);
+    const long long viol = q_transport_cells(s, dt);
+    memcpy(q_out, s->q, b);
+    memcpy(xB_out, s->xB, b);
+    memcpy(Y_out, s->Y, b);
+    return viol;
+}
+void pfo_test_q_reconstruct(pfo_state *s, const double *q_in, const double *phi, const double *xB_in, double *q_out,
+                            double *xB_out, double *Y_out) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->q, q_in, b);
+    memcpy(s->phi, phi, b);
+    memcpy(s->xB, xB_in, b);
+    q_reconstruct(s);
+    memcpy(q_out, s->q, b);
+    memcpy(xB_out, s->xB, b);
+    memcpy(Y_out, s->Y, b);
 }
 
 /* test hook (the pinning tests): the 2/3 dealias rule on a given half
@@ -1279,7 +1476,9 @@ void pfo_test_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ,
 static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
     pfgb_params *P = &s->p;
     const int zm = P->zero_mode_enabled;
-    const double *phiY = zm ? s->phi_n : (P->enable_Y_rhs_previous_time_level ? s->phi_n : s->phi);
+    const int qm = P->pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT;
+    /* phi_for_Y_explicit, main_cuda.cu:30286-30291 */
+    const double *phiY = zm ? s->phi_n : (qm || !P->enable_Y_rhs_previous_time_level ? s->phi : s->phi_n);
     const double *etaY = s->eta;
     mu_field(s, phiY, etaY);
     fwd(s, s->mu, s->mu_k); dealias(s, s->mu_k);
@@ -1322,6 +1521,15 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
             st->mean_DY = dsum(s->mass_t, s->N) / (double)s->N;
         }
         return PFGB_OK;
+    }
+    if (qm) {
+        /* q_transport_projection_split, main_cuda.cu:30648-30707 */
+        int rc = q_transport(s, dt);
+        if (st) {
+            st->mean_DY = P->D_alpha * P->pf_composition_stabilizer_Dalpha_multiplier;
+            st->q_redistributed_cells = s->q_redistributed;
+        }
+        return rc;
     }
     if (P->pf_y_update_mode == PFGB_Y_X_TRANSPORT_SPLIT) {
         /* x_transport_projection_split, main_cuda.cu:30564-30593 and
@@ -1464,6 +1672,11 @@ static int step_once(pfo_state *s, pfgb_step_stats *st) {
             s->eta[idx] = v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
         RLOOP_END
     }
+
+    /* q split: the phase substep's storage transfer, main_cuda.cu:30241-30277 */
+    s->q_rejected = 0;
+    if (P->pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT) q_phase(s);
+    if (st) st->q_phase_rejected = s->q_rejected;
 
     int rc = y_update(s, st, dt);
     if (rc != PFGB_OK) return rc;
@@ -1783,6 +1996,7 @@ int pfo_load_fields(pfo_state *s, const double *phi, const double *xB, const dou
         s->mass_t[idx] = (1.0 - h) * s->xB[idx] + P->v_B * h;
     RLOOP_END
     s->target_mass = dsum(s->mass_t, s->N);
+    q_from_phi_xB(s);   /* initialize_q_alpha_kernel, main_cuda.cu:28051-28053 */
     for (int c = 0; c < 6; ++c) {
         memset(s->sig_r[c], 0, sizeof(double) * s->N);
         memset(s->eps_r[c], 0, sizeof(double) * s->N);

@@ -54,6 +54,12 @@ void pfo_test_xsplit_source(pfo_state *s, double mDx, const double *divJ, const 
 void pfo_test_xsplit_final(pfo_state *s, double dt, const double *x, const double *xB_old, double *Y, double *xB);
 void pfo_test_flux(pfo_state *s, const double *g, const double *phiY, const double *etaY, const double *xB_prev,
                    double *J);
+long long pfo_test_q_phase(pfo_state *s, const double *phi_new, const double *phi_old, const double *q_in,
+                           double *q_out);
+long long pfo_test_q_transport(pfo_state *s, double dt, const double *q_in, const double *divJ, const double *phi,
+                               const double *xB_in, double *q_out, double *xB_out, double *Y_out);
+void pfo_test_q_reconstruct(pfo_state *s, const double *q_in, const double *phi, const double *xB_in, double *q_out,
+                            double *xB_out, double *Y_out);
 void pfo_test_storage_exact(pfo_state *s, double dt, const double *divJ, const double *phi_new,
                             const double *phi_old, const double *Y_old, double *Y, double *xB);
 void pfo_test_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ, const double *phi_new,

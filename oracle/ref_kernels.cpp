@@ -213,6 +213,34 @@ void refk_xsplit_final(const double *x, double *xB, double *Y, int n, const doub
     REF_LAUNCH(n, xB_normalize_clamp_and_logit_kernel(const_cast<double *>(x), xB, Y, 1.0, d[0], d[1], d[2], n));
 }
 
+// q_transport_projection_split kernels over n cells; stats: PF_Q_STATS_COUNT
+// doubles (the caller zeroes them and sets PF_Q_MIN_ALPHA to 1).
+int refk_q_stats_layout(int *infeasible, int *violations) {
+    *infeasible = PF_Q_INFEASIBLE_PHASE_COUNT;
+    *violations = PF_Q_TRANSPORT_BOUND_VIOLATION_COUNT;
+    return PF_Q_STATS_COUNT;
+}
+// apply_local_phase_storage_transfer_q_kernel (feasibility tolerance 1e-12)
+void refk_q_phase(const double *phi_new, const double *phi_old, double *q, double vB, double *stats, int n) {
+    REF_LAUNCH(n, apply_local_phase_storage_transfer_q_kernel(phi_new, phi_old, q, vB, 1.0e-12, stats, n));
+}
+// q_explicit_transport_and_reconstruct_kernel.  d: dt, xB_eps, Y_clip, Y_upper_cap
+void refk_q_transport(double *q, const double *divJ, const double *phi, double *xB, double *Y, int n,
+                      const double *d, double *stats) {
+    REF_LAUNCH(n, q_explicit_transport_and_reconstruct_kernel(q, divJ, phi, xB, Y, d[0], d[1], d[2], d[3], 1.0e-12,
+                                                              stats, n));
+}
+// q_normalize_validate_and_reconstruct_kernel in place, invN = 1.  d: xB_eps, Y_clip, Y_upper_cap
+void refk_q_reconstruct(double *q, const double *phi, double *xB, double *Y, int n, const double *d,
+                        double *stats) {
+    REF_LAUNCH(n, q_normalize_validate_and_reconstruct_kernel(q, q, phi, xB, Y, 1.0, d[0], d[1], d[2], 1.0e-12,
+                                                              stats, n));
+}
+// compute_flux_single_component_q_kernel.  d as refk_flux
+void refk_flux_q(const double *g, const double *phi, const double *xB_prev, double *J, int n, const double *d) {
+    REF_LAUNCH(n, compute_flux_single_component_q_kernel(g, phi, xB_prev, J, d[0], d[2], d[3], d[4], d[5], d[6], n));
+}
+
 // dealias_23_kernel on a half spectrum of an Nx x Ny x Nz grid, in place
 void refk_dealias(cuDoubleComplex *k, int Nx, int Ny, int Nz, double dx, double dy, double dz) {
     const int NzC = Nz / 2 + 1, nk = Nx * Ny * NzC;

@@ -105,13 +105,15 @@ def test_y_update_mode_key(capi, tmp_path):
     p = capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = storage_exact\ngp_h_alpha_eps = 1e-6\n"))
     assert p.pf_y_update_mode == capi.Y_STORAGE_EXACT and p.gp_h_alpha_eps == 1e-6
     assert capi.default_params().pf_y_update_mode == capi.Y_LAGGED_RHS
-    # the q split is refused, not silently replaced
     p = capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = x_transport_projection_split\n"
                                      "pf_matrix_storage_floor = 0.2\n"))
     assert p.pf_y_update_mode == capi.Y_X_TRANSPORT_SPLIT and p.pf_matrix_storage_floor == 0.2
     assert p.pf_composition_stabilizer_Dalpha_multiplier == 10.0
+    p = capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = q_transport_projection_split\n"))
+    assert p.pf_y_update_mode == capi.Y_Q_TRANSPORT_SPLIT
+    # an unknown mode is refused, not silently replaced
     with pytest.raises(capi.PfgbError) as e:
-        capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = q_transport_projection_split\n"))
+        capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = q_transport\n"))
     assert "pf_y_update_mode" in str(e.value)
 
 
@@ -154,7 +156,10 @@ def test_create_rejects_bad_grid_without_touching_gpu(capi):
                                   dict(pf_y_update_mode=1, zero_mode_enabled=1),
                                   dict(pf_y_update_mode=2, mode=1),
                                   dict(pf_y_update_mode=2, pf_matrix_storage_floor=0.0),
-                                  dict(pf_y_update_mode=3)])
+                                  dict(pf_y_update_mode=3, zero_mode_enabled=1),
+                                  dict(pf_y_update_mode=3, mode=1),
+                                  dict(pf_y_update_mode=3, model_mode=1),
+                                  dict(pf_y_update_mode=4)])
 def test_create_refuses_unbuilt_or_invalid_composition_paths(capi, over):
     """Refused by the parameter check before any device work."""
     p = capi.load_params_file(os.path.join(GOLDEN, "c2.params"))

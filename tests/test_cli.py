@@ -64,9 +64,9 @@ def test_cli_rejects_bad_inputs(capi, tmp_path):
     r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf,
                     "--pf-zero-mode", "PF_CONSERVED_Y_ZERO_MODE_V1", "--pf-checkpoint-every", "1"], tmp_path)
     assert r.returncode == 2 and "--pf-checkpoint-path" in r.stderr
-    # a Y update mode that is not built
+    # a Y update mode that does not exist
     r = _run(capi, ["16", "16", "16", "0.01", "2", "1", "1", "1", "--pf-param-file", pf,
-                    "--pf_y_update_mode", "q_transport_projection_split"], tmp_path)
+                    "--pf_y_update_mode", "q_transport"], tmp_path)
     assert r.returncode == 2 and "pf_y_update_mode" in r.stderr
     # malformed parameter file
     pbad = tmp_path / "bad.params"

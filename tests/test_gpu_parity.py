@@ -451,10 +451,87 @@ def test_storage_exact_clipped_cells_one_step(capi, oracle):
     assert rel_l2(fg["xB"], fo["xB"]) <= 1e-6
     assert rel_l2(fg["Y"], fo["Y"]) <= 2e-5
 
-@pytest.mark.parametrize("mode", ["storage_exact", "x_split"])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_q_transport_split_parity(capi, oracle, prec):
+    """pf_y_update_mode=q_transport_projection_split (the matrix storage
+    q = (1 - h) x evolved by explicit transport, two_phase, zero mode off)
+    against the oracle over 8 steps of a low-amplitude seed at dt = 1e-4,
+    inside the explicit limit: no phase rejection, no redistribution, and the
+    B ledger sum(q + h v_B) conserved (FP64: 1e-12)."""
+    from cuda_sto_pf_gb300.solver import Solver
+    n, steps = 32, 8
+    p = params_for(capi, "c2.params", n=n, precision=prec, pf_y_update_mode=capi.Y_Q_TRANSPORT_SPLIT, dt=1e-4)
+    phi, xB = _diffuse_seed(capi, p, n)
+    o = oracle(p, threads=4)
+    o.load(phi, xB)
+    so = capi.StepStats()
+    assert o.step(steps, so) == 0
+    with Solver(p) as s:
+        s.load(phi, xB)
+        d0 = s.diagnostics()
+        sg = s.step(steps)
+        fg = s.fields()
+        d1 = s.diagnostics()
+    fo = o.fields()
+    for k in ("phi", "xB", "Y"):
+        assert rel_l2(fg[k], fo[k]) <= TOL[prec], (k, rel_l2(fg[k], fo[k]))
+    assert rel_l2(fg["dYdt"], fo["dYdt"]) <= (1e-5 if prec == 0 else 1e-3)
+    assert sg.q_phase_rejected == so.q_phase_rejected == 0
+    assert sg.q_redistributed_cells == so.q_redistributed_cells == 0
+    assert sg.mean_DY == so.mean_DY == p.D_alpha * p.pf_composition_stabilizer_Dalpha_multiplier
+    assert abs(d1.mass_xBtot - d0.mass_xBtot) <= (1e-12 if prec == 0 else 2e-6) * d0.mass_xBtot
+    # the lagged form moves along another path
+    p2 = params_for(capi, "c2.params", n=n, precision=prec, dt=1e-4)
+    with Solver(p2) as s:
+        s.load(phi, xB)
+        s.step(steps)
+        assert rel_l2(s.fields()["xB"], fg["xB"]) > 10 * TOL[prec]
+
+
+def test_q_transport_split_bounds(capi, oracle):
+    """The q split's bound handling on a sharp particle at dt = 1e-3 (FP64),
+    step by step against the oracle: step 1 sends about 160 cells through
+    the host's local redistribution; step 2 rejects the phase substep (an
+    infeasible storage transfer) and redistributes about 11,700 cells; step 3
+    leaves an amount unresolved and fails in both (the reference's
+    PF_Q_TRANSPORT_STEP_REJECTED).  dt = 1e-3 is past the explicit
+    transport's limit (D_alpha dt / dx^2 = 0.625), which amplifies every
+    difference between the two programs: with the FP32 elastic solve on, its
+    round-off alone moves x by up to 3e-3 in interface cells after one step,
+    so the case runs without elasticity, where the two agree to round-off."""
+    from cuda_sto_pf_gb300.solver import Solver
+    n = 32
+    p = params_for(capi, "c2.params", n=n, precision=0, pf_y_update_mode=capi.Y_Q_TRANSPORT_SPLIT, dt=1e-3,
+                   elastic_enabled=0)
+    phi, xB, _ = _inputs(capi, p, n, False, seed=23)
+    o = oracle(p, threads=4)
+    o.load(phi, xB)
+    with Solver(p) as s:
+        s.load(phi, xB)
+        for step in (1, 2):
+            so = capi.StepStats()
+            assert o.step(1, so) == 0
+            sg = s.step(1)
+            fg, fo = s.fields(), o.fields()
+            print("step", step, "rejected", sg.q_phase_rejected, so.q_phase_rejected, "redistributed",
+                  sg.q_redistributed_cells, so.q_redistributed_cells,
+                  {k: f"{rel_l2(fg[k], fo[k]):.2e}" for k in ("phi", "xB", "Y")})
+            assert sg.q_phase_rejected == so.q_phase_rejected == (1 if step == 2 else 0)
+            assert so.q_redistributed_cells > 100
+            assert abs(sg.q_redistributed_cells - so.q_redistributed_cells) <= max(2, so.q_redistributed_cells // 200)
+            for k in ("phi", "xB", "Y", "dYdt"):
+                assert rel_l2(fg[k], fo[k]) <= (1e-9 if step == 1 else 1e-7), (step, k, rel_l2(fg[k], fo[k]))
+        assert o.step(1, capi.StepStats()) == 4      # PFGB_ERR_NONCONVERGED
+        with pytest.raises(capi.PfgbError) as e:
+            s.step(1)
+        assert "q transport step rejected" in str(e.value)
+
+
+@pytest.mark.parametrize("mode", ["storage_exact", "x_split", "q_split"])
 def test_composition_modes_refuse_the_zero_mode(capi, mode):
     from cuda_sto_pf_gb300.solver import Solver
-    m = capi.Y_STORAGE_EXACT if mode == "storage_exact" else capi.Y_X_TRANSPORT_SPLIT
+    m = {"storage_exact": capi.Y_STORAGE_EXACT, "x_split": capi.Y_X_TRANSPORT_SPLIT,
+         "q_split": capi.Y_Q_TRANSPORT_SPLIT}[mode]
     p = params_for(capi, "c2.params", n=16, pf_y_update_mode=m, zero_mode_enabled=1)
     with pytest.raises(capi.PfgbError):
         Solver(p)

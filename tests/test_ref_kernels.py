@@ -338,3 +338,93 @@ def test_dealias_matches_reference_kernel(capi, shape):
     o.L.pfo_test_dealias(o.s, _ptr(got))
     assert 0 < (ref == 0).sum() < ref.size
     assert np.array_equal(got, ref)
+
+
+def test_q_split_functions_match_reference_kernels(capi):
+    """The q split's per-cell functions against the reference's kernels: the
+    phase storage transfer (feasible and infeasible cells), the explicit
+    transport with its bound check (cells inside, below and above [0, 1 - h],
+    a non-finite divergence), the bounded reconstruction (out-of-range and
+    non-finite q, cells without matrix storage) and the matrix-channel flux."""
+    L = _refk()
+    L.refk_q_stats_layout.argtypes = [ip, ip]
+    L.refk_q_phase.argtypes = [dp, dp, dp, ctypes.c_double, dp, ctypes.c_int]
+    L.refk_q_transport.argtypes = [dp, dp, dp, dp, dp, ctypes.c_int, dp, dp]
+    L.refk_q_reconstruct.argtypes = [dp, dp, dp, dp, ctypes.c_int, dp, dp]
+    L.refk_flux_q.argtypes = [dp, dp, dp, dp, ctypes.c_int, dp]
+    n = 8                      # N = 512: the oracle's 1/N scaling is exact
+    p = params_for(capi, "c2.params", n=n, pf_y_update_mode=capi.Y_Q_TRANSPORT_SPLIT)
+    N = n ** 3
+    rng = np.random.default_rng(131)
+    i_inf, i_viol = ctypes.c_int(), ctypes.c_int()
+    ns = L.refk_q_stats_layout(ctypes.byref(i_inf), ctypes.byref(i_viol))
+
+    def stats():
+        st = np.zeros(ns)
+        st[7] = 1.0            # PF_Q_MIN_ALPHA starts at 1, as the reference initialises it
+        return st
+
+    def h(v):
+        v = np.clip(v, 0.0, 1.0)
+        return v ** 3 * (6 * v ** 2 - 15 * v + 10)
+
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_q_phase.restype = ctypes.c_longlong
+    o.L.pfo_test_q_phase.argtypes = [ctypes.c_void_p, dp, dp, dp, dp]
+    o.L.pfo_test_q_transport.restype = ctypes.c_longlong
+    o.L.pfo_test_q_transport.argtypes = [ctypes.c_void_p, ctypes.c_double, dp, dp, dp, dp, dp, dp, dp]
+    o.L.pfo_test_q_reconstruct.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp, dp]
+
+    # phase transfer
+    phi_old = rng.uniform(-0.05, 1.05, N)
+    phi_new = np.clip(phi_old + rng.normal(0.0, 0.2, N), -0.05, 1.05)
+    xB = rng.uniform(1e-3, 0.3, N)
+    q_in = (1.0 - h(phi_old)) * xB
+    rq = q_in.copy()
+    st = stats()
+    L.refk_q_phase(_ptr(phi_new), _ptr(phi_old), _ptr(rq), p.v_B, _ptr(st), N)
+    gq = np.zeros(N)
+    bad = o.L.pfo_test_q_phase(o.s, _ptr(phi_new), _ptr(phi_old), _ptr(q_in), _ptr(gq))
+    assert 0 < bad < N and bad == int(round(st[i_inf.value]))
+    assert np.abs(gq - rq).max() <= 1e-15
+
+    # explicit transport and reconstruction
+    phi = rng.uniform(-0.05, 1.05, N)
+    phi[:6] = 1.0                      # no matrix storage: x keeps its previous value
+    alpha = 1.0 - h(phi)
+    q0 = alpha * rng.uniform(1e-3, 0.3, N)
+    divJ = rng.normal(0.0, 2.0, N)
+    divJ[7] = np.nan
+    xB0 = rng.uniform(1e-3, 0.3, N)
+    d = np.array([p.dt, p.xB_eps, p.Y_clip, p.Y_clip])
+    rq, rx, rY = q0.copy(), xB0.copy(), np.zeros(N)
+    st = stats()
+    L.refk_q_transport(_ptr(rq), _ptr(divJ), _ptr(phi), _ptr(rx), _ptr(rY), N, _ptr(d), _ptr(st))
+    gq, gx, gY = np.zeros(N), np.zeros(N), np.zeros(N)
+    viol = o.L.pfo_test_q_transport(o.s, p.dt, _ptr(q0), _ptr(divJ), _ptr(phi), _ptr(xB0), _ptr(gq), _ptr(gx),
+                                    _ptr(gY))
+    assert 0 < viol < N and viol == int(round(st[i_viol.value]))
+    assert np.abs(gq - rq).max() <= 1e-15
+    assert np.abs(gx - rx).max() <= 1e-15
+    assert np.abs(gY - rY).max() <= 1e-12 * np.abs(rY).max()
+
+    qr = q0 + rng.normal(0.0, 0.05, N)
+    qr[:3] = [np.nan, -1.0, 2.0]
+    rq, rx, rY = qr.copy(), xB0.copy(), np.zeros(N)
+    L.refk_q_reconstruct(_ptr(rq), _ptr(phi), _ptr(rx), _ptr(rY), N, _ptr(d[1:]), _ptr(stats()))
+    o.L.pfo_test_q_reconstruct(o.s, _ptr(qr), _ptr(phi), _ptr(xB0), _ptr(gq), _ptr(gx), _ptr(gY))
+    assert np.abs(gq - rq).max() <= 1e-15
+    assert np.abs(gx - rx).max() <= 1e-15
+    assert np.abs(gY - rY).max() <= 1e-12 * np.abs(rY).max()
+
+    # the matrix-channel flux
+    g = rng.normal(0.0, 1.0, N)
+    L.refk_set_convex(p.thermo_convex_extrapolation_enabled)
+    dfl = np.array([p.D_alpha, p.D_compound, p.Vm_alpha_0, p.dVm_alpha_dxB, p.Vm_compound, p.temperature_K,
+                    p.mu_reference_scale, p.gp_M_GP, p.gp_M_beta])
+    ref = np.zeros(N)
+    L.refk_flux_q(_ptr(g), _ptr(phi), _ptr(xB0), _ptr(ref), N, _ptr(dfl))
+    o.L.pfo_test_flux.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp]
+    got = np.zeros(N)
+    o.L.pfo_test_flux(o.s, _ptr(g), _ptr(phi), _ptr(phi), _ptr(xB0), _ptr(got))
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()

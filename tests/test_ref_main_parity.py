@@ -365,3 +365,79 @@ def test_gp_zone_heterogeneous_vtk(capi, ref_main, tmp_path):
         if "maxabs" in k:
             # 5e-6 of VTK rounding plus 1e-5 of the field scale (all in [0, 1])
             assert v <= 1.5e-5, (k, rec)
+
+
+def _q_events(text):
+    """(step, kind, cells) of the q split's event lines in a program's stdout"""
+    ev = []
+    for line in text.split("\n"):
+        if line.startswith("PF_Q_PHASE_SUBSTEP_REJECTED"):
+            ev.append((int(line.split("step=")[1].split()[0]), "rejected", 0))
+        elif line.startswith("PF_Q_TRANSPORT_LOCAL_REDISTRIBUTION"):
+            ev.append((int(line.split("step=")[1].split()[0]), "redistributed",
+                       int(line.split("violating_cells=")[1].split()[0])))
+    return ev
+
+
+@pytest.mark.parametrize("case", ["diffuse", "bounds"])
+def test_q_transport_split_vtk(capi, ref_main, tmp_path, case):
+    """pf_y_update_mode=q_transport_projection_split against the reference
+    program (two_phase, no zero mode: the reference refuses it with the
+    composition modes).  diffuse: a low-amplitude seed at dt = 1e-4 for 10
+    steps, inside the explicit transport's limit.  bounds: a sharp particle
+    at dt = 1e-3 for 2 steps, without elasticity: the host's local
+    redistribution on both steps and a rejected phase substep on the second
+    (the step is past the explicit transport's limit, which would amplify
+    the FP32 elastic solve's round-off into the composition).  The two
+    programs' output files and CSV rows, their PF_Q_* event lines (cell
+    counts within a few cells at the bounds), and the last phi and xB VTK
+    files against the library's FP64 fields."""
+    from cuda_sto_pf_gb300 import build, workloads
+    n = 32
+    p0 = params_for(capi, "c2.params", n=n)
+    rng = np.random.default_rng(23)
+    if case == "diffuse":
+        dt, steps, every = "1e-4", 10, 4
+        phi = 0.35 * workloads.ellipsoid_field((n, n, n), [np.full(3, n / 2.0)], [np.array([7.0, 6.0, 5.0])],
+                                               [workloads.random_rotation(rng)], p0.ic_phi_iface_w)
+        xB = 0.03 + 1e-3 * rng.standard_normal(phi.shape)
+    else:
+        dt, steps, every = "1e-3", 2, 2
+        phi = workloads.ellipsoid_field((n, n, n), [np.full(3, n / 2.0)], [np.array([7.0, 6.0, 5.0])],
+                                        [workloads.random_rotation(rng)], p0.ic_phi_iface_w)
+        xB = workloads.composition(phi, rng)
+    fields = {"phi": phi, "xB": xB}
+    extra = {"pf_y_update_mode": "q_transport_projection_split", "dt": dt}
+    if case == "bounds":
+        extra["elastic_enabled"] = "0"
+    d = str(tmp_path)
+    paths = _write_inputs(os.path.join(d, "in"), fields, n, 0.07)
+    pf = _params_file(d, "c2.params", extra)
+    argv = _argv(n, steps, every, pf, paths, False, None)
+    argv[3] = dt
+    argv[6] = "1"
+    r = _run(ref_main, argv, os.path.join(d, "R_ref"))
+    assert r.returncode == 0, "reference main_cuda failed:\n" + r.stdout[-3000:] + r.stderr[-3000:]
+    o = _run(build.EXE, argv, os.path.join(d, "R_ours"))
+    assert o.returncode == 0, o.stdout[-3000:] + o.stderr[-3000:]
+    cr, co = _case_dir(os.path.join(d, "R_ref")), _case_dir(os.path.join(d, "R_ours"))
+    rec = {"n": n, "steps": steps, "dt": dt}
+    _compare_outputs(cr, co, "q_split_" + case, rec)
+    er, eo = _q_events(r.stdout), _q_events(o.stdout)
+    rec["events_ref"], rec["events_ours"] = er, eo
+    assert [e[:2] for e in er] == [e[:2] for e in eo], rec
+    for a, b in zip(er, eo):
+        assert abs(a[2] - b[2]) <= max(2, a[2] // 200), rec
+    if case == "bounds":
+        assert ("rejected" in [e[1] for e in er]) and any(e[1] == "redistributed" for e in er), rec
+    f, _ = _library_fields(capi, "c2.params", n, extra, fields, 0.07, steps, 0, False)
+    last = steps // every + 1
+    for k in ("phi", "xB"):
+        ref = _vtk(os.path.join(cr, f"{k}_{last}.vtk"), n)
+        cli = _vtk(os.path.join(co, f"{k}_{last}.vtk"), n)
+        rec[f"{k}_maxabs_lib_fp64"] = float(np.abs(f[k] - ref).max())
+        rec[f"{k}_maxabs_cli"] = float(np.abs(cli - ref).max())
+    _report("q_split_" + case, rec)
+    for k, v in rec.items():
+        if "maxabs" in k:
+            assert v <= 1.5e-5, (k, rec)
