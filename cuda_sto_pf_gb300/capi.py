@@ -19,6 +19,8 @@ PREC_FP64, PREC_FP32 = 0, 1
 MODEL_TWO_PHASE, MODEL_GP_ZONE = 0, 1
 MODE_DYNAMICS, MODE_MINIMIZE = 0, 1
 Y_LAGGED_RHS, Y_STORAGE_EXACT, Y_X_TRANSPORT_SPLIT, Y_Q_TRANSPORT_SPLIT = 0, 1, 2, 3
+COMPOSITION_LEGACY, COMPOSITION_CTOT, COMPOSITION_QALPHA = 0, 1, 2
+CONS_FLUX_PAIRWISE_LIMITED, CONS_FLUX_BACKWARD_EULER = 0, 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device out of memory",
           4: "elastic solver did not converge", 5: "zero-mode mass solve rejected the step",
@@ -84,6 +86,10 @@ class Params(Structure):
         ("init_tilt_theta_deg", c_double), ("init_tilt_phi_deg", c_double),
         ("init_center_shift_x", c_double), ("init_center_shift_y", c_double), ("init_center_shift_z", c_double),
         ("init_phi_noise_amp", c_double), ("init_phi_noise_seed", ctypes.c_uint64), ("seed", ctypes.c_uint64),
+        ("pf_composition_mode", c_int32), ("pf_conservative_flux_strategy", c_int32),
+        ("pf_conservative_bound_tol", c_double), ("pf_conservative_mass_tol", c_double),
+        ("pf_conservative_beta_support_eps", c_double), ("pf_conservative_max_subcycles", c_int32),
+        ("pad_cons", c_int32),
         ("temperature_K", c_double), ("mu0_compound", c_double), ("xB_eq_matrix", c_double),
     ]
 
@@ -97,6 +103,7 @@ class StepStats(Structure):
         ("zero_mode_lambda", c_double), ("zero_mode_residual", c_double),
         ("zero_mode_target_mass", c_double), ("mean_DY", c_double),
         ("q_phase_rejected", c_int32), ("q_redistributed_cells", c_int32),
+        ("cons_limited_faces", c_int32), ("cons_phase_constrained", c_int32),
     ]
 
 

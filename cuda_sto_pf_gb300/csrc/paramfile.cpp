@@ -90,6 +90,9 @@ const DKey kDoubles[] = {
     DK("init_center_shift_y", init_center_shift_y), DK("init_center_shift_z", init_center_shift_z),
     DK("init_phi_noise_amp", init_phi_noise_amp), DK("gp_h_alpha_eps", gp_h_alpha_eps),
     DK("pf_matrix_storage_floor", pf_matrix_storage_floor),
+    DK("pf_conservative_bound_tol", pf_conservative_bound_tol),
+    DK("pf_conservative_mass_tol", pf_conservative_mass_tol),
+    DK("pf_conservative_beta_support_eps", pf_conservative_beta_support_eps),
     DK("pf_composition_stabilizer_Dalpha_multiplier", pf_composition_stabilizer_Dalpha_multiplier),
 };
 const DKey kInts[] = {
@@ -104,6 +107,7 @@ const DKey kInts[] = {
     DK("elastic_warm_start_source", elastic_warm_start_source),
     DK("elastic_chebyshev", elastic_chebyshev), DK("fft_tensor_cores", fft_tensor_cores),
     DK("zero_mode_fp64_cells", zero_mode_fp64_cells),
+    DK("pf_conservative_max_subcycles", pf_conservative_max_subcycles),
     DK("enable_Y_rhs_previous_time_level", enable_Y_rhs_previous_time_level),
     DK("disable_Y_rhs_gamma_term", disable_Y_rhs_gamma_term),
     DK("gp_elastic_enabled", gp_elastic_enabled), DK("gp_elastic_active_eta", gp_elastic_active_eta),
@@ -123,7 +127,7 @@ const DKey kInts[] = {
 // 16137, 16424): any other value is refused, not ignored
 struct Selector { const char *key, *allowed; };
 const Selector kSelectors[] = {
-    {"pf_composition_mode", "legacy"},         {"y_update_mass_projection_enabled", "0"},
+    {"y_update_mass_projection_enabled", "0"},
     {"enable_Y_rhs_picard", "0"},              {"enable_gp_assisted_beta_nucleation", "0"},
     {"gp_nuc_enabled", "0"},                   {"diagnostic_rsmd_enabled", "0"},
 };
@@ -228,6 +232,26 @@ extern "C" pfgb_status pfgb_params_set(pfgb_params *p, const char *key, const ch
         }
         return PFGB_ERR_INVALID;
     }
+    if (!strcmp(key, "pf_composition_mode")) {   // pf_params.h:349, checked at main_cuda.cu:1697-1703
+        if (!strcmp(value, "legacy")) { p->pf_composition_mode = PFGB_COMPOSITION_LEGACY; return PFGB_OK; }
+        if (!strcmp(value, "ctot_conservative_split")) { p->pf_composition_mode = PFGB_COMPOSITION_CTOT; return PFGB_OK; }
+        if (!strcmp(value, "qalpha_conservative_local_transaction")) {
+            p->pf_composition_mode = PFGB_COMPOSITION_QALPHA;
+            return PFGB_OK;
+        }
+        return PFGB_ERR_INVALID;
+    }
+    if (!strcmp(key, "pf_conservative_flux_strategy")) {   // pf_params.h:350, main_cuda.cu:1705-1710
+        if (!strcmp(value, "pairwise_limited")) {
+            p->pf_conservative_flux_strategy = PFGB_CONS_FLUX_PAIRWISE_LIMITED;
+            return PFGB_OK;
+        }
+        if (!strcmp(value, "pairwise_backward_euler")) {
+            p->pf_conservative_flux_strategy = PFGB_CONS_FLUX_BACKWARD_EULER;
+            return PFGB_OK;
+        }
+        return PFGB_ERR_INVALID;
+    }
     if (!strcmp(key, "model_mode")) {
         if (!strcmp(value, "two_phase")) { p->model_mode = PFGB_MODEL_TWO_PHASE; return PFGB_OK; }
         if (!strcmp(value, "gp_zone")) { p->model_mode = PFGB_MODEL_GP_ZONE; return PFGB_OK; }
@@ -272,7 +296,7 @@ extern "C" pfgb_status pfgb_params_load_file(pfgb_params *p, const char *path, c
         trim(val);
         pfgb_status st = pfgb_params_set(p, key.c_str(), val.c_str());
         if (st == PFGB_ERR_INVALID) {
-            bool selector = !strcmp(key.c_str(), "pf_y_update_mode");
+            bool selector = false;
             for (const Selector &sel : kSelectors) selector = selector || key == sel.key;
             if (selector)
                 seterr(errbuf, errlen, "%s:%d %s=%s selects a path that is not built", path, line_no, key.c_str(),

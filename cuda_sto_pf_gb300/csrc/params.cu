@@ -111,6 +111,12 @@ void pfgb_params_default(pfgb_params *p) {
     p->pf_y_update_mode = PFGB_Y_LAGGED_RHS;
     p->gp_h_alpha_eps = 1.0e-8;   // main_cuda.cu:16187
     p->pf_matrix_storage_floor = 0.1;                      // main_cuda.cu:16116
+    p->pf_composition_mode = PFGB_COMPOSITION_LEGACY;      // main_cuda.cu:16108-16114
+    p->pf_conservative_flux_strategy = PFGB_CONS_FLUX_PAIRWISE_LIMITED;
+    p->pf_conservative_bound_tol = 1.0e-12;
+    p->pf_conservative_mass_tol = 1.0e-10;
+    p->pf_conservative_beta_support_eps = 1.0e-10;
+    p->pf_conservative_max_subcycles = 64;
     p->pf_composition_stabilizer_Dalpha_multiplier = 10.0; // main_cuda.cu:16117
     p->gp_barrier_only_mode = 1;                           // main_cuda.cu:15823
     p->enable_legacy_gp_storage_coupling = 0;              // main_cuda.cu:15824

@@ -86,6 +86,8 @@ struct pfgb_ctx {
     void *Yprev = nullptr;   // Y_f of the last step's start, for the stress export
     void *q = nullptr, *qb = nullptr, *divr = nullptr;   // q split state (pf_y_update_mode q)
     int q_rejected = 0, q_redistributed = 0;             // of the last step
+    double *cstore = nullptr, *cmu = nullptr;            // conservative modes: storage and mu (FP64)
+    int cons_limited = 0, cons_constrained = 0;          // of the last step
     int cur = 0, ecur = 0;
     void *S[4] = {nullptr, nullptr, nullptr, nullptr};
     void *eps[6] = {}, *E[6] = {}, *U[3] = {};
@@ -964,6 +966,195 @@ struct OpQTransportZ {
     __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
     __device__ void finish(int b, const Acc &a) const { reinterpret_cast<Acc *>(d.partials)[b] = a; }
 };
+
+// ---------------------------------------------------------------------------
+// PF-only conservative composition modes (pf_composition_mode,
+// main_cuda.cu:27784-27792; kernels cuda_kernels.cu:3117-3288): the storage
+// C = q + h v_B (ctot) or q = (1 - h) x (qalpha) in FP64 on the cell grid,
+// moved by limited pairwise face transfers.  FP64 throughout (the storage
+// sums must stay conserved); the fields keep their precision.
+// ---------------------------------------------------------------------------
+// h^-1 by 60 bisections on [0, 1] (h_inverse_bisection_device, :85-97)
+__device__ __forceinline__ double h_inverse_bisect(double target) {
+    if (target <= 0.0) return 0.0;
+    if (target >= 1.0) return 1.0;
+    double lo = 0.0, hi = 1.0;
+    for (int it = 0; it < 60; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (pf_h(mid) < target) lo = mid; else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+// x from the storage, the equilibrium composition where the matrix vanishes
+// or x is not finite, bounded; its logit (the shared tail of
+// reconstruct_conservative_context_kernel and
+// constrain_phase_and_reconstruct_conservative_kernel)
+__device__ __forceinline__ double cons_y(double q, double alpha, double beta_eps, double xeq, double eps,
+                                        double yclip, bool *nonfinite) {
+    double x = xeq;
+    if (alpha > beta_eps) x = q / alpha;
+    if (!isfinite(x)) { x = xeq; *nonfinite = true; }
+    x = fmin(fmax(x, eps), 1.0 - eps);
+    return logit_clip(x, eps, yclip);
+}
+
+struct ConsArgs {
+    int ctot, be;
+    double vB, beta_eps, xeq, eps, yclip, tol, dt, Da;
+};
+static ConsArgs cons_args(const pfgb_ctx *c) {
+    const pfgb_params &P = c->p;
+    ConsArgs a;
+    a.ctot = P.pf_composition_mode == PFGB_COMPOSITION_CTOT;
+    a.be = P.pf_conservative_flux_strategy == PFGB_CONS_FLUX_BACKWARD_EULER;
+    a.vB = P.v_B;
+    a.beta_eps = P.pf_conservative_beta_support_eps;
+    a.xeq = P.xB_eq_matrix;
+    a.eps = P.xB_eps;
+    a.yclip = P.Y_clip;
+    a.tol = P.pf_conservative_bound_tol;
+    a.dt = P.dt;
+    a.Da = P.D_alpha;
+    return a;
+}
+
+// initialize_conservative_storage_kernel (:3123-3132), from the loaded fields
+__global__ void k_cons_load(const double *phi, const double *xB, double *cst, long long N, int ctot, double vB) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        const double h = pf_h(clamp01(phi[i]));
+        const double q = (1.0 - h) * clamp01(xB[i]);
+        cst[i] = ctot ? q + h * vB : q;
+    }
+}
+
+// reconstruct_conservative_context_kernel (:3134-3159) at phi
+template <typename T, typename TE>
+__global__ void k_cons_context(DevState<T, TE> d, ConsArgs a, const double *cst, const T *phi) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.g.N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double h = pf_h(clamp01(double(phi[i])));
+        const double alpha = fmax(1.0 - h, 0.0);
+        const double q = a.ctot ? cst[i] - h * a.vB : cst[i];
+        bool nf = false;
+        d.Y[i] = T(cons_y(q, alpha, a.beta_eps, a.xeq, a.eps, a.yclip, &nf) - d.Yc);
+    }
+}
+
+// compute_mu_x_kernel (:1266-1324) at phi^n in real space, FP64, with the
+// stress stored by the last elastic solve
+template <typename T, typename TE>
+__global__ void k_cons_mu(DevState<T, TE> d, PhysC c, double *mu) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.g.N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double xB = sigmoid_clip(double(d.Y[i]) + d.Yc, c.Yclip, c.xBeps);
+        double offA, offB;
+        thermo_mu_off<double>(c.tc, xB, offA, offB);
+        const double h = pf_h(double(d.phi_old[i]));
+        const double cb = c_xB_phi<double>(xB, c.Vm0, c.dVm, c.Vmc, h);
+        const double muA = c.tc.GA_s + offA, muB = c.tc.GB_s + offB;
+        const double mt = (1.0 - h) * (muA * (1.0 - xB) + muB * xB) + h * c.mu0;
+        double m = cb * ((c.dG + offB - offA) - cb * mt * c.dVm);
+        if (c.elastic && d.sig[0]) m += -c.eiv * (double(d.sig[0][i]) + double(d.sig[1][i]) + double(d.sig[2][i]));
+        mu[i] = m;
+    }
+}
+
+// one checkerboard sweep of the pairwise face transfer
+// (pairwise_conservative_face_sweep_kernel, :3161-3237): the face between
+// each cell of the given coordinate parity and its + neighbour (periodic);
+// mobilities (1 - h) M_alpha joined harmonically; dt M (mu_i - mu_j) / dx^2,
+// damped in the backward-Euler strategy; limited by both cells' storage
+// bounds.  Every cell lies on one face of a sweep, so the faces run in
+// parallel.  The limited faces are counted (block partials).
+template <typename T, typename TE>
+__global__ void k_cons_sweep(DevState<T, TE> d, PhysC c, ConsArgs a, double *cst, const double *mu, int axis,
+                             int parity, double spacing) {
+    double lim = 0.0;
+    const int Nx = d.g.Nx, Ny = d.g.Ny, Nz = d.g.Nz;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < d.g.N;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(idx % Nz), t = (int)(idx / Nz), j = t % Ny, i = t / Ny;
+        const int coord = axis == 0 ? i : (axis == 1 ? j : k);
+        if ((coord & 1) != parity) continue;
+        int ni = i, nj = j, nk = k;
+        if (axis == 0) ni = i + 1 == Nx ? 0 : i + 1;
+        else if (axis == 1) nj = j + 1 == Ny ? 0 : j + 1;
+        else nk = k + 1 == Nz ? 0 : k + 1;
+        const long long n = ((long long)ni * Ny + nj) * Nz + nk;
+        const double hi = pf_h(clamp01(double(d.phi_old[idx]))), hj = pf_h(clamp01(double(d.phi_old[n])));
+        const double ai = fmax(1.0 - hi, 0.0), aj = fmax(1.0 - hj, 0.0);
+        const double xi = fmin(fmax(sigmoid_clip(double(d.Y[idx]) + d.Yc, c.Yclip, c.xBeps), 1e-12), 1.0 - 1e-12);
+        const double xj = fmin(fmax(sigmoid_clip(double(d.Y[n]) + d.Yc, c.Yclip, c.xBeps), 1e-12), 1.0 - 1e-12);
+        const double Gi = gamma_thermo<double>(c.tc, xi, 0.0, c.Vm0, c.dVm, c.Vmc);
+        const double Gj = gamma_thermo<double>(c.tc, xj, 0.0, c.Vm0, c.dVm, c.Vmc);
+        const double Mi = ai * stabilized_meff<double>(a.Da, Gi), Mj = aj * stabilized_meff<double>(a.Da, Gj);
+        const double Mf = (Mi > 0.0 && Mj > 0.0) ? 2.0 * Mi * Mj / (Mi + Mj) : 0.0;
+        const double inv2 = 1.0 / (spacing * spacing);
+        double tr = a.dt * Mf * (mu[idx] - mu[n]) * inv2;
+        if (a.be && Mf > 0.0) {
+            const double di = Gi / fmax(ai, 1.0e-14), dj = Gj / fmax(aj, 1.0e-14);
+            tr /= 1.0 + a.dt * Mf * inv2 * fmax(di + dj, 0.0);
+        }
+        const double si = cst[idx], sj = cst[n];
+        const double loi = a.ctot ? hi * a.vB : 0.0, loj = a.ctot ? hj * a.vB : 0.0;
+        const double upi = a.ctot ? hi * a.vB + ai : ai, upj = a.ctot ? hj * a.vB + aj : aj;
+        const double raw = tr;
+        if (tr >= 0.0) {
+            tr = fmin(tr, fmax(si - loi, 0.0));
+            tr = fmin(tr, fmax(upj - sj, 0.0));
+        } else {
+            const double mag = fmin(-tr, fmax(sj - loj, 0.0));
+            tr = -fmin(mag, fmax(upi - si, 0.0));
+        }
+        if (fabs(tr - raw) > a.tol) lim += 1.0;
+        cst[idx] = si - tr;
+        cst[n] = sj + tr;
+    }
+    AccSum1 s{lim};
+    block_reduce_acc(s);
+    if (threadIdx.x == 0) reinterpret_cast<AccSum1 *>(d.partials)[blockIdx.x] = s;
+}
+
+// constrain_phase_and_reconstruct_conservative_kernel (:3239-3288) on the
+// new phi: h capped at C / v_B (phi by bisection); a cell whose storage would
+// leave its bounds keeps phi^n (counted: the step is rejected); qalpha stores
+// q for the new h; the context.  Partials: rejected and capped cells.
+template <typename T, typename TE>
+__global__ void k_cons_constrain(DevState<T, TE> d, ConsArgs a, double *cst) {
+    double bad = 0.0, capped = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < d.g.N;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double po = clamp01(double(d.phi_old[i]));
+        const double ho = pf_h(po);
+        const double C = a.ctot ? cst[i] : cst[i] + ho * a.vB;
+        double phi = clamp01(double(d.phi_new[i]));
+        double h = pf_h(phi);
+        const double hmax = a.vB > 0.0 ? fmin(fmax(C / a.vB, 0.0), 1.0) : 1.0;
+        if (h > hmax + a.tol) {
+            phi = h_inverse_bisect(hmax);
+            h = pf_h(phi);
+            capped += 1.0;
+        }
+        double alpha = fmax(1.0 - h, 0.0);
+        double q = C - h * a.vB;
+        if (!isfinite(q) || q < -a.tol || q > alpha + a.tol) {
+            bad += 1.0;
+            phi = po;
+            h = ho;
+            alpha = fmax(1.0 - h, 0.0);
+            q = C - h * a.vB;
+        }
+        d.phi_new[i] = T(phi);
+        if (!a.ctot) cst[i] = q;
+        bool nf = false;
+        d.Y[i] = T(cons_y(q, alpha, a.beta_eps, a.xeq, a.eps, a.yclip, &nf) - d.Yc);
+        if (nf) bad += 1.0;
+    }
+    AccSum2 s{bad, capped};
+    block_reduce_acc(s);
+    if (threadIdx.x == 0) reinterpret_cast<AccSum2 *>(d.partials)[blockIdx.x] = s;
+}
 
 // (6) final z pass: store Y_f, dY/dt, and the zero-mode statistics
 template <typename T, typename TE>
@@ -2472,6 +2663,55 @@ static pfgb_status zero_mode(pfgb_ctx *c, int nb_final, pfgb_step_stats *st) {
     return PFGB_OK;
 }
 
+// the conservative modes' transport, before the step's elastic solve
+// (main_cuda.cu:28486-28545): the context at phi^n, mu there, the six
+// checkerboard sweeps (x, y, z; parity 0 then 1; their limited-face counts
+// into DS_EV .. DS_EV + 5), the context again
+template <typename T, typename TE>
+static pfgb_status cons_transport(pfgb_ctx *c) {
+    const pfgb_params &P = c->p;
+    DevState<T, TE> d = dev_state<T, TE>(c);
+    const ConsArgs a = cons_args(c);
+    const int nb = 304;
+    k_cons_context<T, TE><<<nb, 256, 0, c->stream>>>(d, a, c->cstore, d.phi_old);
+    k_cons_mu<T, TE><<<nb, 256, 0, c->stream>>>(d, c->pc, c->cmu);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    const double sp[3] = {P.dx, P.dy, P.dz};
+    for (int ax = 0; ax < 3; ++ax)
+        for (int par = 0; par < 2; ++par) {
+            k_cons_sweep<T, TE><<<nb, 256, 0, c->stream>>>(d, c->pc, a, c->cstore, c->cmu, ax, par, sp[ax]);
+            PFGB_CUDA_TRY(cudaGetLastError());
+            TRY(reduce_to<AccSum1>(c, nb, DS_EV + 2 * ax + par));
+        }
+    k_cons_context<T, TE><<<nb, 256, 0, c->stream>>>(d, a, c->cstore, d.phi_old);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    return PFGB_OK;
+}
+
+// the storage constraint on the new phi (main_cuda.cu:29859-29871): a cell
+// that would leave its storage bounds, or a non-finite context, rejects the
+// step (the reference's PF_CONSERVATIVE_STEP_REJECTED)
+template <typename T, typename TE>
+static pfgb_status cons_constrain(pfgb_ctx *c, const DevState<T, TE> &d) {
+    const int nb = 304;
+    k_cons_constrain<T, TE><<<nb, 256, 0, c->stream>>>(d, cons_args(c), c->cstore);
+    PFGB_CUDA_TRY(cudaGetLastError());
+    TRY(reduce_to<AccSum2>(c, nb, DS_BR));
+    TRY(sync_read(c, DS_BR, 2));
+    const double bad = c->hscal[DS_BR], capped = c->hscal[DS_BR + 1];
+    TRY(sync_read(c, DS_EV, 6));
+    double lim = 0.0;
+    for (int i = 0; i < 6; ++i) lim += c->hscal[DS_EV + i];
+    c->cons_limited = (int)(lim + 0.5);
+    c->cons_constrained = (int)(capped + 0.5);
+    if (bad > 0.5) {
+        pfgb_set_error_msg("conservative composition step rejected at step %d: %.0f cells out of their storage "
+                           "bounds or not finite", c->step + 1, bad);
+        return PFGB_ERR_NONCONVERGED;
+    }
+    return PFGB_OK;
+}
+
 // the local redistribution of the q split's out-of-bounds transport, on
 // the host as in the reference (q_transport_conservative_local_redistribution,
 // main_cuda.cu:22362-22456): every cell's trial q0 + dt div J is bounded to
@@ -2698,6 +2938,10 @@ static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
     const PhysCT<T> pc = phys_as<T>(c->pc);
     const ElasC<TE> ec = elas_consts<TE>(c);
     c->Yc_prev = c->Yc;
+    // conservative composition modes: the transport before the elastic solve
+    const bool cons = P.pf_composition_mode != PFGB_COMPOSITION_LEGACY;
+    c->cons_limited = c->cons_constrained = 0;
+    if (cons) TRY((cons_transport<T, TE>(c)));
     if (P.elastic_enabled) TRY((elastic_solve<T, TE>(c, st)));
     DevState<T, TE> d = dev_state<T, TE>(c);
     const KTab kt = d.kt;
@@ -2712,6 +2956,7 @@ static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
     TRY((launch_axis<T, 1, 1, -1, +1>(c, 2, io1, OpACFilterX<T>{kt, P.L_phi * P.dt * P.kappa_phi, invN}, "x_ac_filter")));
     TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
     TRY((launch_z<T, 1, 0>(c, OpACStoreZ<T, TE>{d.S[0], d.phi_new, c->g.NzC, T(-1e-6), T(1.0 + 1e-6)}, "z_ac_store", Nf * sizeof(T))));
+    if (cons) TRY((cons_constrain<T, TE>(c, d)));
 
     // ---- eta (GP zone) ----
     if (pc.gp) {
@@ -2726,10 +2971,14 @@ static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
     c->q_rejected = 0;
     if (P.pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT) TRY((q_phase<T, TE>(c, d, pc)));
 
-    TRY((y_update<T, TE>(c, d, st)));
+    // the conservative modes carry the composition in their storage: no Y
+    // update and no dY/dt update (main_cuda.cu:30283-30284)
+    if (!cons) TRY((y_update<T, TE>(c, d, st)));
     if (st) {
         st->q_phase_rejected = c->q_rejected;
         st->q_redistributed_cells = c->q_redistributed;
+        st->cons_limited_faces = c->cons_limited;
+        st->cons_phase_constrained = c->cons_constrained;
     }
     c->cur = 1 - c->cur;
     if (pc.gp) c->ecur = 1 - c->ecur;
@@ -3459,6 +3708,33 @@ static pfgb_status validate(const pfgb_params *p) {
                            "built)");
         return PFGB_ERR_UNSUPPORTED;
     }
+    // PF-only conservative composition modes (main_cuda.cu:1697-1775, 24600-24612,
+    // 24691-24702, 28487-28491)
+    if (p->pf_composition_mode < PFGB_COMPOSITION_LEGACY || p->pf_composition_mode > PFGB_COMPOSITION_QALPHA ||
+        p->pf_conservative_flux_strategy < PFGB_CONS_FLUX_PAIRWISE_LIMITED ||
+        p->pf_conservative_flux_strategy > PFGB_CONS_FLUX_BACKWARD_EULER) {
+        pfgb_set_error_msg("pf_composition_mode: legacy, ctot_conservative_split or "
+                           "qalpha_conservative_local_transaction; pf_conservative_flux_strategy: pairwise_limited "
+                           "or pairwise_backward_euler");
+        return PFGB_ERR_INVALID;
+    }
+    if (p->pf_composition_mode != PFGB_COMPOSITION_LEGACY) {
+        if (!(p->pf_conservative_bound_tol > 0.0) || !(p->pf_conservative_mass_tol > 0.0) ||
+            !(p->pf_conservative_beta_support_eps > 0.0) || p->pf_conservative_max_subcycles < 1) {
+            pfgb_set_error_msg("invalid PF conservative solver controls");
+            return PFGB_ERR_INVALID;
+        }
+        if (p->model_mode != PFGB_MODEL_TWO_PHASE || p->zero_mode_enabled || p->mode != PFGB_MODE_DYNAMICS ||
+            p->pf_y_update_mode != PFGB_Y_LAGGED_RHS) {
+            pfgb_set_error_msg("conservative PF composition modes are PF-only two_phase dynamics with the zero mode "
+                               "off and pf_y_update_mode lagged_rhs");
+            return PFGB_ERR_UNSUPPORTED;
+        }
+        if ((p->Nx & 1) || (p->Ny & 1) || (p->Nz & 1)) {
+            pfgb_set_error_msg("shared-face checkerboard solver requires even periodic dimensions");
+            return PFGB_ERR_INVALID;
+        }
+    }
     if (p->elastic_warm_start_source < 0 || p->elastic_warm_start_source > 3) {
         pfgb_set_error_msg("elastic_warm_start_source must be 0, 1, 2 or 3");
         return PFGB_ERR_INVALID;
@@ -3477,6 +3753,7 @@ static void ctx_free(pfgb_ctx *c) {
     if (c->eta[1] != c->eta[0]) f(c->eta[1]);
     f(c->Y); f(c->Yprev); f(c->dYdt);
     f(c->q); f(c->qb); f(c->divr);
+    f(c->cstore); f(c->cmu);
     for (int i = 0; i < 4; ++i) f(c->S[i]);
     for (int i = 0; i < 6; ++i) { f(c->eps[i]); f(c->E[i]); }
     for (int i = 0; i < 3; ++i) f(c->U[i]);
@@ -3605,6 +3882,14 @@ static pfgb_status load_device(pfgb_ctx *c, const double *phi, const double *xB,
     if (c->q) {   // q split: q = (1 - h) x of the loaded fields (main_cuda.cu:28051-28053)
         k_q_load<T><<<nb, 256, 0, c->stream>>>(phi, xB, (T *)c->q, c->g.N);
         PFGB_CUDA_TRY(cudaGetLastError());
+    }
+    if (c->cstore) {   // conservative modes: the storage of the loaded fields (main_cuda.cu:28054-28058)
+        k_cons_load<<<nb, 256, 0, c->stream>>>(phi, xB, c->cstore, c->g.N,
+                                               c->p.pf_composition_mode == PFGB_COMPOSITION_CTOT, c->p.v_B);
+        PFGB_CUDA_TRY(cudaGetLastError());
+        if (c->sig[0] && !keep)
+            for (int i = 0; i < 6; ++i)
+                PFGB_CUDA_TRY(cudaMemsetAsync(c->sig[i], 0, sizeof(float) * c->g.N, c->stream));
     }
     if (keep) return PFGB_OK;
     for (int i = 0; i < 6; ++i) PFGB_CUDA_TRY(cudaMemsetAsync(c->eps[i], 0, sizeof(float) * c->g.N, c->stream));
@@ -3748,8 +4033,17 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
             for (int i = 0; i < 3; ++i) { A_(&c->Uprev[i], sizeof(float2) * Nk); }
         }
     }
-    if (pin->mode == PFGB_MODE_MINIMIZE) {
+    if (pin->pf_composition_mode != PFGB_COMPOSITION_LEGACY) {
+        A_(&c->cstore, sizeof(double) * N);
+        A_(&c->cmu, sizeof(double) * N);
+    }
+    // the stored stress: minimize, and the conservative modes, whose transport
+    // runs before the step's elastic solve on the last solve's stress
+    if (pin->mode == PFGB_MODE_MINIMIZE ||
+        (pin->pf_composition_mode != PFGB_COMPOSITION_LEGACY && pin->elastic_enabled)) {
         for (int i = 0; i < 6; ++i) { A_(&c->sig[i], sizeof(float) * N); }
+    }
+    if (pin->mode == PFGB_MODE_MINIMIZE) {
         A_(&c->mge, rs * N);
         A_(&c->mlap, rs * N);
     }

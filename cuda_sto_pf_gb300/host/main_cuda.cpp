@@ -232,8 +232,15 @@ Cli parse(int argc, char **argv) {
         else if ((v = flag_value(argc, argv, &i, "--minimize-xB-max-safe"))) { if (!to_double(v, &c.xB_max_safe)) bad(a, v); }
         else if ((v = flag_value(argc, argv, &i, "--radius"))) { if (!to_double(v, &c.radius) || c.radius < 0) bad(a, v); }
         else if ((v = flag_value(argc, argv, &i, "--radius-phys-nm"))) { if (!to_double(v, &c.radius_nm) || c.radius_nm < 0) bad(a, v); }
-        else if ((v = flag_value(argc, argv, &i, "--pf_y_update_mode")))   // main_cuda.cu:23411
+        else if ((v = flag_value(argc, argv, &i, "--pf_y_update_mode")) ||
+                 (v = flag_value(argc, argv, &i, "--pf-y-update-mode")))   // main_cuda.cu:23410-23414
             c.param_sets.push_back({"pf_y_update_mode", v});
+        else if ((v = flag_value(argc, argv, &i, "--pf_composition_mode")) ||
+                 (v = flag_value(argc, argv, &i, "--pf-composition-mode")))   // main_cuda.cu:23415-23419
+            c.param_sets.push_back({"pf_composition_mode", v});
+        else if ((v = flag_value(argc, argv, &i, "--pf_conservative_flux_strategy")) ||
+                 (v = flag_value(argc, argv, &i, "--pf-conservative-flux-strategy")))   // main_cuda.cu:23420-23425
+            c.param_sets.push_back({"pf_conservative_flux_strategy", v});
         else if ((v = flag_value(argc, argv, &i, "--init-shape"))) {
             if (!strcmp(v, "sphere")) c.param_sets.push_back({"init_shape_mode", "0"});
             else if (!strcmp(v, "ellipsoid")) c.param_sets.push_back({"init_shape_mode", "1"});

@@ -79,6 +79,8 @@ enum { PFGB_MODEL_TWO_PHASE = 0, PFGB_MODEL_GP_ZONE = 1 };
 enum { PFGB_MODE_DYNAMICS = 0, PFGB_MODE_MINIMIZE = 1 };
 /* pf_y_update_mode (pf_params.h:345) */
 enum { PFGB_Y_LAGGED_RHS = 0, PFGB_Y_STORAGE_EXACT = 1, PFGB_Y_X_TRANSPORT_SPLIT = 2, PFGB_Y_Q_TRANSPORT_SPLIT = 3 };
+enum { PFGB_COMPOSITION_LEGACY = 0, PFGB_COMPOSITION_CTOT = 1, PFGB_COMPOSITION_QALPHA = 2 };
+enum { PFGB_CONS_FLUX_PAIRWISE_LIMITED = 0, PFGB_CONS_FLUX_BACKWARD_EULER = 1 };
 
 /*
  * Stiffness tensors are the 21 independent Voigt entries in the reference's
@@ -251,6 +253,24 @@ typedef struct pfgb_params {
     double init_phi_noise_amp;
     uint64_t init_phi_noise_seed;
     uint64_t seed;
+    /* PF-only conservative composition modes (pf_composition_mode,
+       main_cuda.cu:27784-27792, 28486-28545, 29859-29880, kernels
+       cuda_kernels.cu:3117-3288; two_phase dynamics, zero mode off, even
+       grid axes): the conserved storage C = q + h v_B (ctot_conservative_split)
+       or q = (1 - h) x (qalpha_conservative_local_transaction) is moved by a
+       limited pairwise face transfer of the matrix-channel flux on the cell
+       grid (six checkerboard sweeps per step, before the elastic solve; the
+       backward-Euler damped variant with pf_conservative_flux_strategy =
+       PFGB_CONS_FLUX_BACKWARD_EULER), and the phi update is constrained to
+       h <= C / v_B; the spectral Y update is not run.  mass_tol and
+       max_subcycles are validated as the reference does and not used. */
+    int32_t pf_composition_mode;              /* PFGB_COMPOSITION_*        */
+    int32_t pf_conservative_flux_strategy;    /* PFGB_CONS_FLUX_*          */
+    double pf_conservative_bound_tol;
+    double pf_conservative_mass_tol;
+    double pf_conservative_beta_support_eps;
+    int32_t pf_conservative_max_subcycles;
+    int32_t pad_cons;
     /* derived by pfgb_params_finalize (pfparams_refresh_thermo) */
     double temperature_K;
     double mu0_compound;
@@ -277,6 +297,10 @@ typedef struct pfgb_step_stats {
        transport left [0, 1 - h] and went through the local redistribution */
     int32_t q_phase_rejected;
     int32_t q_redistributed_cells;
+    /* conservative composition modes: faces whose transfer the storage
+       bounds limited, and cells whose phi update the storage constrained */
+    int32_t cons_limited_faces;
+    int32_t cons_phase_constrained;
 } pfgb_step_stats;
 
 /* Minimize iteration statistics (energy_minimize.csv row and the stopping

@@ -244,6 +244,8 @@ struct pfo_state {
     double *rhs, *mu, *scr, *divJ, *lapY, *mass_t, *der_t;
     double *q, *q_before;   /* q_transport_projection_split: matrix storage (1 - h) x */
     int q_rejected, q_redistributed;
+    double *cstore;         /* conservative composition modes: C = q + h v_B or q */
+    long long cons_limited, cons_constrained;
     cpx *phi_k, *rhs_k, *mu_k, *divJ_k, *Y_k, *scr_k, *eta_k;
     /* elastic */
     double *eps_r[6], *sig_r[6];
@@ -296,7 +298,7 @@ pfo_state *pfo_create(const pfgb_params *pin) {
     const size_t rb = sizeof(double) * s->N, kb = sizeof(cpx) * s->Nk;
     double **rf_[] = {&s->phi, &s->eta, &s->Y, &s->xB, &s->dYdt, &s->phi_n, &s->eta_prev,
                       &s->Y_n, &s->xB_prev, &s->rhs, &s->mu, &s->scr, &s->divJ, &s->lapY,
-                      &s->mass_t, &s->der_t, &s->q, &s->q_before};
+                      &s->mass_t, &s->der_t, &s->q, &s->q_before, &s->cstore};
     for (size_t i = 0; i < sizeof(rf_) / sizeof(rf_[0]); ++i) *rf_[i] = (double *)xalloc(rb);
     cpx **kf_[] = {&s->phi_k, &s->rhs_k, &s->mu_k, &s->divJ_k, &s->Y_k, &s->scr_k, &s->eta_k};
     for (size_t i = 0; i < sizeof(kf_) / sizeof(kf_[0]); ++i) *kf_[i] = (cpx *)xalloc(kb);
@@ -345,7 +347,7 @@ void pfo_destroy(pfo_state *s) {
     if (!s) return;
     double *rr[] = {s->phi, s->eta, s->Y, s->xB, s->dYdt, s->phi_n, s->eta_prev, s->Y_n,
                     s->xB_prev, s->rhs, s->mu, s->scr, s->divJ, s->lapY, s->mass_t, s->der_t, s->q,
-                    s->q_before};
+                    s->q_before, s->cstore};
     for (size_t i = 0; i < sizeof(rr) / sizeof(rr[0]); ++i) free(rr[i]);
     cpx *kk[] = {s->phi_k, s->rhs_k, s->mu_k, s->divJ_k, s->Y_k, s->scr_k, s->eta_k};
     for (size_t i = 0; i < sizeof(kk) / sizeof(kk[0]); ++i) free(kk[i]);
@@ -1336,6 +1338,220 @@ static int q_transport(pfo_state *s, double dt) {
     return PFGB_OK;
 }
 
+static void mu_field(pfo_state *s, const double *phiY, const double *etaY);
+
+/* PF-only conservative composition modes (pf_composition_mode,
+ * main_cuda.cu:27784-27792): the storage C = q + h v_B (ctot) or q (qalpha)
+ * moved by limited pairwise face transfers; kernels cuda_kernels.cu:3117-3288 */
+
+/* h^-1 by 60 bisections on [0, 1] (h_inverse_bisection_device, :85-97) */
+static double h_inverse_bisect(double target) {
+    if (target <= 0.0) return 0.0;
+    if (target >= 1.0) return 1.0;
+    double lo = 0.0, hi = 1.0;
+    for (int it = 0; it < 60; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (o_h(mid) < target) lo = mid; else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+/* initialize_conservative_storage_kernel, :3123-3132 */
+static void cons_init(pfo_state *s) {
+    const pfgb_params *P = &s->p;
+    const int ctot = P->pf_composition_mode == PFGB_COMPOSITION_CTOT;
+    RLOOP_BEGIN(s)
+        const double h = o_h(o_clamp01(s->phi[idx]));
+        const double q = (1.0 - h) * o_clamp01(s->xB[idx]);
+        s->cstore[idx] = ctot ? q + h * P->v_B : q;
+    RLOOP_END
+}
+
+/* the matrix composition of a cell from its storage: x = q / (1 - h), the
+ * equilibrium composition where the matrix vanishes or x is not finite,
+ * bounded to [eps, 1 - eps], and its logit (the tail shared by
+ * reconstruct_conservative_context_kernel :3134-3159 and
+ * constrain_phase_and_reconstruct_conservative_kernel :3239-3288) */
+static void cons_x(pfo_state *s, size_t idx, double q, double alpha) {
+    const pfgb_params *P = &s->p;
+    double x = P->xB_eq_matrix;
+    if (alpha > P->pf_conservative_beta_support_eps) x = q / alpha;
+    if (!isfinite(x)) x = P->xB_eq_matrix;
+    x = fmin(fmax(x, P->xB_eps), 1.0 - P->xB_eps);
+    s->xB[idx] = x;
+    s->Y[idx] = o_logit(x, P->xB_eps, P->Y_clip);
+}
+
+/* reconstruct_conservative_context_kernel, :3134-3159 */
+static void cons_context(pfo_state *s, const double *phi) {
+    const pfgb_params *P = &s->p;
+    const int ctot = P->pf_composition_mode == PFGB_COMPOSITION_CTOT;
+    RLOOP_BEGIN(s)
+        const double h = o_h(o_clamp01(phi[idx]));
+        const double alpha = fmax(1.0 - h, 0.0);
+        const double q = ctot ? s->cstore[idx] - h * P->v_B : s->cstore[idx];
+        cons_x(s, idx, q, alpha);
+    RLOOP_END
+}
+
+/* one checkerboard sweep of the pairwise face transfer along an axis: the
+ * face between each cell of the given coordinate parity and its + neighbour
+ * (periodic), matrix-channel mobilities (1 - h) M_alpha joined harmonically,
+ * transfer dt M (mu_i - mu_j) / dx^2 (damped by the backward-Euler factor
+ * 1 + dt M / dx^2 max(G_i / a_i + G_j / a_j, 0)), limited by both cells'
+ * storage bounds [h v_B, h v_B + (1 - h)] (ctot) or [0, 1 - h] (qalpha)
+ * (pairwise_conservative_face_sweep_kernel, :3161-3237).  Every cell is on one
+ * face of a sweep, so the faces are independent. */
+static long long cons_sweep(pfo_state *s, int axis, int parity, double spacing) {
+    const pfgb_params *P = &s->p;
+    const int ctot = P->pf_composition_mode == PFGB_COMPOSITION_CTOT;
+    const int be = P->pf_conservative_flux_strategy == PFGB_CONS_FLUX_BACKWARD_EULER;
+    const double T = P->temperature_K, sc = P->mu_reference_scale, dt = P->dt;
+    const int cv = P->thermo_convex_extrapolation_enabled;
+    const int Nx = s->Nx, Ny = s->Ny, Nz = s->Nz;
+    long long limited = 0;
+#pragma omp parallel for schedule(static) reduction(+ : limited)
+    for (long long idx = 0; idx < (long long)s->N; ++idx) {
+        const int k = (int)(idx % Nz), t = (int)(idx / Nz), j = t % Ny, i = t / Ny;
+        const int coord = axis == 0 ? i : (axis == 1 ? j : k);
+        if ((coord & 1) != parity) continue;
+        int ni = i, nj = j, nk = k;
+        if (axis == 0) ni = i + 1 == Nx ? 0 : i + 1;
+        else if (axis == 1) nj = j + 1 == Ny ? 0 : j + 1;
+        else nk = k + 1 == Nz ? 0 : k + 1;
+        const size_t n = ((size_t)ni * Ny + nj) * Nz + nk;
+        const double hi = o_h(o_clamp01(s->phi_n[idx])), hj = o_h(o_clamp01(s->phi_n[n]));
+        const double ai = fmax(1.0 - hi, 0.0), aj = fmax(1.0 - hj, 0.0);
+        const double xi = fmin(fmax(s->xB[idx], 1e-12), 1.0 - 1e-12), xj = fmin(fmax(s->xB[n], 1e-12), 1.0 - 1e-12);
+        const double Gi = o_gamma(xi, 0.0, P->Vm_alpha_0, P->dVm_alpha_dxB, P->Vm_compound, T, sc, cv);
+        const double Gj = o_gamma(xj, 0.0, P->Vm_alpha_0, P->dVm_alpha_dxB, P->Vm_compound, T, sc, cv);
+        const double Mi = ai * o_meff(P->D_alpha, Gi), Mj = aj * o_meff(P->D_alpha, Gj);
+        const double Mf = (Mi > 0.0 && Mj > 0.0) ? 2.0 * Mi * Mj / (Mi + Mj) : 0.0;
+        const double inv2 = 1.0 / (spacing * spacing);
+        double tr = dt * Mf * (s->mu[idx] - s->mu[n]) * inv2;
+        if (be && Mf > 0.0) {
+            const double di = Gi / fmax(ai, 1.0e-14), dj = Gj / fmax(aj, 1.0e-14);
+            tr /= 1.0 + dt * Mf * inv2 * fmax(di + dj, 0.0);
+        }
+        const double si = s->cstore[idx], sj = s->cstore[n];
+        const double loi = ctot ? hi * P->v_B : 0.0, loj = ctot ? hj * P->v_B : 0.0;
+        const double upi = ctot ? hi * P->v_B + ai : ai, upj = ctot ? hj * P->v_B + aj : aj;
+        const double raw = tr;
+        if (tr >= 0.0) {
+            tr = fmin(tr, fmax(si - loi, 0.0));
+            tr = fmin(tr, fmax(upj - sj, 0.0));
+        } else {
+            const double mag = fmin(-tr, fmax(sj - loj, 0.0));
+            tr = -fmin(mag, fmax(upi - si, 0.0));
+        }
+        if (fabs(tr - raw) > P->pf_conservative_bound_tol) ++limited;
+        s->cstore[idx] = si - tr;
+        s->cstore[n] = sj + tr;
+    }
+    return limited;
+}
+
+/* the storage constraint on the new phi and the context from it
+ * (constrain_phase_and_reconstruct_conservative_kernel, :3239-3288): h is
+ * capped at C / v_B (phi by bisection); a cell whose storage would leave its
+ * bounds keeps phi^n and is counted (the host rejects the step); qalpha
+ * stores q for the new h.  Returns the rejected cells; *constrained: the
+ * capped ones. */
+static long long cons_constrain(pfo_state *s, long long *constrained) {
+    const pfgb_params *P = &s->p;
+    const int ctot = P->pf_composition_mode == PFGB_COMPOSITION_CTOT;
+    const double tol = P->pf_conservative_bound_tol, vB = P->v_B;
+    long long bad = 0, capped = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad, capped)
+    for (long long i = 0; i < (long long)s->N; ++i) {
+        const double po = o_clamp01(s->phi_n[i]);
+        const double ho = o_h(po);
+        const double C = ctot ? s->cstore[i] : s->cstore[i] + ho * vB;
+        double phi = o_clamp01(s->phi[i]);
+        double h = o_h(phi);
+        const double hmax = vB > 0.0 ? fmin(fmax(C / vB, 0.0), 1.0) : 1.0;
+        if (h > hmax + tol) {
+            phi = h_inverse_bisect(hmax);
+            h = o_h(phi);
+            ++capped;
+        }
+        double alpha = fmax(1.0 - h, 0.0);
+        double q = C - h * vB;
+        if (!isfinite(q) || q < -tol || q > alpha + tol) {
+            ++bad;
+            phi = po;
+            h = ho;
+            alpha = fmax(1.0 - h, 0.0);
+            q = C - h * vB;
+        }
+        s->phi[i] = phi;
+        if (!ctot) s->cstore[i] = q;
+        double x = P->xB_eq_matrix;
+        if (alpha > P->pf_conservative_beta_support_eps) x = q / alpha;
+        if (!isfinite(x)) { x = P->xB_eq_matrix; ++bad; }
+        x = fmin(fmax(x, P->xB_eps), 1.0 - P->xB_eps);
+        s->xB[i] = x;
+        s->Y[i] = o_logit(x, P->xB_eps, P->Y_clip);
+    }
+    *constrained = capped;
+    return bad;
+}
+
+/* the transport half of a conservative step, before the elastic solve
+ * (main_cuda.cu:28486-28545): context at phi^n, mu there, the six sweeps
+ * (x, y, z; parity 0 then 1), the context again */
+static void cons_transport(pfo_state *s) {
+    const pfgb_params *P = &s->p;
+    cons_context(s, s->phi_n);
+    mu_field(s, s->phi_n, s->eta);
+    const double sp[3] = {P->dx, P->dy, P->dz};
+    long long lim = 0;
+    for (int a = 0; a < 3; ++a)
+        for (int par = 0; par < 2; ++par) lim += cons_sweep(s, a, par, sp[a]);
+    s->cons_limited = lim;
+    cons_context(s, s->phi_n);
+}
+
+/* test hooks (the pinning tests) for the conservative modes' functions */
+void pfo_test_cons_init(pfo_state *s, const double *phi, const double *xB, double *storage) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->phi, phi, b);
+    memcpy(s->xB, xB, b);
+    cons_init(s);
+    memcpy(storage, s->cstore, b);
+}
+void pfo_test_cons_context(pfo_state *s, const double *storage, const double *phi, double *xB, double *Y) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->cstore, storage, b);
+    cons_context(s, phi);
+    memcpy(xB, s->xB, b);
+    memcpy(Y, s->Y, b);
+}
+long long pfo_test_cons_sweep(pfo_state *s, double *storage, const double *mu, const double *phi, const double *xB,
+                              int axis, int parity, double spacing) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->cstore, storage, b);
+    memcpy(s->mu, mu, b);
+    memcpy(s->phi_n, phi, b);
+    memcpy(s->xB, xB, b);
+    const long long lim = cons_sweep(s, axis, parity, spacing);
+    memcpy(storage, s->cstore, b);
+    return lim;
+}
+long long pfo_test_cons_constrain(pfo_state *s, double *phi_new, const double *phi_old, double *storage, double *xB,
+                                  double *Y, long long *capped) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->phi, phi_new, b);
+    memcpy(s->phi_n, phi_old, b);
+    memcpy(s->cstore, storage, b);
+    const long long bad = cons_constrain(s, capped);
+    memcpy(phi_new, s->phi, b);
+    memcpy(storage, s->cstore, b);
+    memcpy(xB, s->xB, b);
+    memcpy(Y, s->Y, b);
+    return bad;
+}
+
 /* test hooks (the pinning tests) for the q split's per-cell functions */
 long long pfo_test_q_phase(pfo_state *s, const double *phi_new, const double *phi_old, const double *q_in,
                            double *q_out) {
@@ -1643,6 +1859,10 @@ static int step_once(pfo_state *s, pfgb_step_stats *st) {
 
     const int gp_el = s->gp && P->gp_elastic_enabled;
     const int coupling = P->elastic_enabled && (!gp_el || P->gp_elastic_active_phi);
+    /* conservative composition modes: the transport before the elastic solve */
+    const int cons = P->pf_composition_mode != PFGB_COMPOSITION_LEGACY;
+    s->cons_limited = s->cons_constrained = 0;
+    if (cons) cons_transport(s);
     if (P->elastic_enabled) {
         int rc = elastic_solve(s, st);
         if (rc != PFGB_OK) return rc;
@@ -1652,6 +1872,13 @@ static int step_once(pfo_state *s, pfgb_step_stats *st) {
     fwd(s, s->phi, s->phi_k); dealias(s, s->phi_k);
     phi_rhs(s, coupling);
     phi_si_update(s, dt);
+    if (cons) {   /* the storage constraint, :29859-29880 (a rejected cell fails the step) */
+        long long capped = 0;
+        const long long bad = cons_constrain(s, &capped);
+        s->cons_constrained = capped;
+        if (st) { st->cons_limited_faces = (int)s->cons_limited; st->cons_phase_constrained = (int)capped; }
+        if (bad) return PFGB_ERR_NONCONVERGED;
+    }
 
     /* eta update (gp_zone), :29948-30006 */
     if (s->gp) {
@@ -1678,7 +1905,9 @@ static int step_once(pfo_state *s, pfgb_step_stats *st) {
     if (P->pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT) q_phase(s);
     if (st) st->q_phase_rejected = s->q_rejected;
 
-    int rc = y_update(s, st, dt);
+    /* the conservative modes carry the composition in their storage: no Y
+     * update and no dY/dt update (main_cuda.cu:30283-30284) */
+    int rc = cons ? PFGB_OK : y_update(s, st, dt);
     if (rc != PFGB_OK) return rc;
     s->step++;
     return PFGB_OK;
@@ -1997,6 +2226,7 @@ int pfo_load_fields(pfo_state *s, const double *phi, const double *xB, const dou
     RLOOP_END
     s->target_mass = dsum(s->mass_t, s->N);
     q_from_phi_xB(s);   /* initialize_q_alpha_kernel, main_cuda.cu:28051-28053 */
+    cons_init(s);       /* initialize_conservative_storage_kernel, main_cuda.cu:28054-28058 */
     for (int c = 0; c < 6; ++c) {
         memset(s->sig_r[c], 0, sizeof(double) * s->N);
         memset(s->eps_r[c], 0, sizeof(double) * s->N);

@@ -54,6 +54,12 @@ void pfo_test_xsplit_source(pfo_state *s, double mDx, const double *divJ, const 
 void pfo_test_xsplit_final(pfo_state *s, double dt, const double *x, const double *xB_old, double *Y, double *xB);
 void pfo_test_flux(pfo_state *s, const double *g, const double *phiY, const double *etaY, const double *xB_prev,
                    double *J);
+void pfo_test_cons_init(pfo_state *s, const double *phi, const double *xB, double *storage);
+void pfo_test_cons_context(pfo_state *s, const double *storage, const double *phi, double *xB, double *Y);
+long long pfo_test_cons_sweep(pfo_state *s, double *storage, const double *mu, const double *phi, const double *xB,
+                              int axis, int parity, double spacing);
+long long pfo_test_cons_constrain(pfo_state *s, double *phi_new, const double *phi_old, double *storage, double *xB,
+                                  double *Y, long long *capped);
 long long pfo_test_q_phase(pfo_state *s, const double *phi_new, const double *phi_old, const double *q_in,
                            double *q_out);
 long long pfo_test_q_transport(pfo_state *s, double dt, const double *q_in, const double *divJ, const double *phi,

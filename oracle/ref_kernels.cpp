@@ -241,6 +241,39 @@ void refk_flux_q(const double *g, const double *phi, const double *xB_prev, doub
     REF_LAUNCH(n, compute_flux_single_component_q_kernel(g, phi, xB_prev, J, d[0], d[2], d[3], d[4], d[5], d[6], n));
 }
 
+// the conservative composition modes' kernels over an Nx x Ny x Nz grid;
+// stats: PF_CONS_STATS_COUNT doubles, zeroed by the caller
+int refk_cons_stats_layout(int *limited, int *constrained, int *violations, int *nonfinite) {
+    *limited = PF_CONS_LIMITED_FACE_COUNT;
+    *constrained = PF_CONS_PHASE_CONSTRAINT_COUNT;
+    *violations = PF_CONS_BOUND_VIOLATION_COUNT;
+    *nonfinite = PF_CONS_NONFINITE_COUNT;
+    return PF_CONS_STATS_COUNT;
+}
+void refk_cons_init(const double *phi, const double *xB, double *storage, double vB, int ctot, int n) {
+    REF_LAUNCH(n, initialize_conservative_storage_kernel(phi, xB, storage, vB, ctot, n));
+}
+// d: T_K, v_B, beta_support_eps, xB_eps, Y_clip
+void refk_cons_context(const double *storage, const double *phi, double *xB, double *Y, int ctot, int n,
+                       const double *d, double *stats) {
+    REF_LAUNCH(n, reconstruct_conservative_context_kernel(storage, phi, xB, Y, d[0], d[1], ctot, d[2], d[3], d[4],
+                                                          stats, n));
+}
+// d: spacing, dt, D_alpha, Vm_alpha_0, dVm_alpha_dxB, Vm_compound, T_K, mu_reference_scale, v_B, bound_tol
+void refk_cons_sweep(double *storage, const double *mu, const double *phi, const double *xB, int Nx, int Ny, int Nz,
+                     int axis, int parity, int ctot, int be, const double *d, double *stats) {
+    const int n = Nx * Ny * Nz;
+    REF_LAUNCH(n, pairwise_conservative_face_sweep_kernel(storage, mu, phi, xB, Nx, Ny, Nz, axis, parity, d[0], d[1],
+                                                          d[2], d[3], d[4], d[5], d[6], d[7], d[8], ctot, be, d[9],
+                                                          stats, n));
+}
+// d: T_K, v_B, beta_support_eps, xB_eps, Y_clip, bound_tol
+void refk_cons_constrain(double *phi_new, const double *phi_old, double *storage, double *xB, double *Y, int ctot,
+                         int n, const double *d, double *stats) {
+    REF_LAUNCH(n, constrain_phase_and_reconstruct_conservative_kernel(phi_new, phi_old, storage, xB, Y, d[0], d[1],
+                                                                      ctot, d[2], d[3], d[4], d[5], stats, n));
+}
+
 // dealias_23_kernel on a half spectrum of an Nx x Ny x Nz grid, in place
 void refk_dealias(cuDoubleComplex *k, int Nx, int Ny, int Nz, double dx, double dy, double dz) {
     const int NzC = Nz / 2 + 1, nk = Nx * Ny * NzC;

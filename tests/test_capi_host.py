@@ -78,8 +78,7 @@ def test_unknown_key_warns_and_is_ignored(capi, tmp_path, capfd):
     assert "unknown key ignored: not_a_key" in capfd.readouterr().err
 
 
-@pytest.mark.parametrize("line", ["pf_composition_mode = ctot_conservative_split",
-                                  "y_update_mass_projection_enabled = 1", "enable_Y_rhs_picard = 1",
+@pytest.mark.parametrize("line", ["y_update_mass_projection_enabled = 1", "enable_Y_rhs_picard = 1",
                                   "gp_nuc_enabled = 1", "diagnostic_rsmd_enabled = 1",
                                   "enable_gp_assisted_beta_nucleation = 1"])
 def test_unbuilt_path_selectors_are_refused(capi, tmp_path, line):
@@ -89,8 +88,7 @@ def test_unbuilt_path_selectors_are_refused(capi, tmp_path, line):
     assert "not built" in str(e.value)
     # the default value is accepted
     key = line.split("=")[0].strip()
-    default = "legacy" if key == "pf_composition_mode" else "0"
-    capi.load_params_file(_write(tmp_path, base + "\n%s = %s\n" % (key, default)))
+    capi.load_params_file(_write(tmp_path, base + "\n%s = 0\n" % key))
 
 
 def test_gp_storage_coupling_keys(capi, tmp_path):
@@ -115,6 +113,22 @@ def test_y_update_mode_key(capi, tmp_path):
     with pytest.raises(capi.PfgbError) as e:
         capi.load_params_file(_write(tmp_path, base + "\npf_y_update_mode = q_transport\n"))
     assert "pf_y_update_mode" in str(e.value)
+
+
+def test_composition_mode_keys(capi, tmp_path):
+    base = open(os.path.join(GOLDEN, "c1.params")).read()
+    p = capi.load_params_file(_write(tmp_path, base + "\npf_composition_mode = qalpha_conservative_local_transaction\n"
+                                     "pf_conservative_flux_strategy = pairwise_backward_euler\n"
+                                     "pf_conservative_bound_tol = 1e-11\npf_conservative_max_subcycles = 8\n"))
+    assert p.pf_composition_mode == capi.COMPOSITION_QALPHA
+    assert p.pf_conservative_flux_strategy == capi.CONS_FLUX_BACKWARD_EULER
+    assert p.pf_conservative_bound_tol == 1e-11 and p.pf_conservative_max_subcycles == 8
+    d = capi.default_params()
+    assert d.pf_composition_mode == capi.COMPOSITION_LEGACY
+    assert (d.pf_conservative_bound_tol, d.pf_conservative_mass_tol, d.pf_conservative_beta_support_eps,
+            d.pf_conservative_max_subcycles) == (1e-12, 1e-10, 1e-10, 64)
+    with pytest.raises(capi.PfgbError):
+        capi.load_params_file(_write(tmp_path, base + "\npf_composition_mode = ctot\n"))
 
 
 def test_finalize_matches_oracle(capi, oracle):
@@ -159,7 +173,14 @@ def test_create_rejects_bad_grid_without_touching_gpu(capi):
                                   dict(pf_y_update_mode=3, zero_mode_enabled=1),
                                   dict(pf_y_update_mode=3, mode=1),
                                   dict(pf_y_update_mode=3, model_mode=1),
-                                  dict(pf_y_update_mode=4)])
+                                  dict(pf_y_update_mode=4),
+                                  dict(pf_composition_mode=1, zero_mode_enabled=1),
+                                  dict(pf_composition_mode=2, model_mode=1),
+                                  dict(pf_composition_mode=1, mode=1),
+                                  dict(pf_composition_mode=1, pf_y_update_mode=1),
+                                  dict(pf_composition_mode=2, Nz=15),
+                                  dict(pf_composition_mode=1, pf_conservative_bound_tol=0.0),
+                                  dict(pf_composition_mode=3)])
 def test_create_refuses_unbuilt_or_invalid_composition_paths(capi, over):
     """Refused by the parameter check before any device work."""
     p = capi.load_params_file(os.path.join(GOLDEN, "c2.params"))

@@ -428,3 +428,92 @@ def test_q_split_functions_match_reference_kernels(capi):
     got = np.zeros(N)
     o.L.pfo_test_flux(o.s, _ptr(g), _ptr(phi), _ptr(phi), _ptr(xB0), _ptr(got))
     assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("ctot", [1, 0])
+def test_conservative_functions_match_reference_kernels(capi, ctot):
+    """The conservative composition modes' per-cell functions against the
+    reference's kernels (ctot_conservative_split and
+    qalpha_conservative_local_transaction): the storage from (phi, x), the
+    context from the storage (matrix and beta cells), the six checkerboard
+    face sweeps in both flux strategies (limited faces included), and the
+    phase constraint (capped cells and cells that keep phi^n)."""
+    L = _refk()
+    L.refk_cons_stats_layout.argtypes = [ip, ip, ip, ip]
+    L.refk_cons_init.argtypes = [dp, dp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+    L.refk_cons_context.argtypes = [dp, dp, dp, dp, ctypes.c_int, ctypes.c_int, dp, dp]
+    L.refk_cons_sweep.argtypes = [dp, dp, dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp]
+    L.refk_cons_constrain.argtypes = [dp, dp, dp, dp, dp, ctypes.c_int, ctypes.c_int, dp, dp]
+    n = 8
+    mode = capi.COMPOSITION_CTOT if ctot else capi.COMPOSITION_QALPHA
+    p = params_for(capi, "c2.params", n=n, pf_composition_mode=mode)
+    N = n ** 3
+    rng = np.random.default_rng(141 + ctot)
+    li, lc, lv, lnf = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    ns = L.refk_cons_stats_layout(ctypes.byref(li), ctypes.byref(lc), ctypes.byref(lv), ctypes.byref(lnf))
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_cons_init.argtypes = [ctypes.c_void_p, dp, dp, dp]
+    o.L.pfo_test_cons_context.argtypes = [ctypes.c_void_p, dp, dp, dp, dp]
+    o.L.pfo_test_cons_sweep.restype = ctypes.c_longlong
+    o.L.pfo_test_cons_sweep.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+    o.L.pfo_test_cons_constrain.restype = ctypes.c_longlong
+    o.L.pfo_test_cons_constrain.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp, ctypes.POINTER(ctypes.c_longlong)]
+
+    phi = rng.uniform(-0.05, 1.05, N)
+    phi[:5] = 1.0                              # beta cells: the equilibrium context
+    xB = rng.uniform(1e-3, 0.3, N)
+    rs, gs = np.zeros(N), np.zeros(N)
+    L.refk_cons_init(_ptr(phi), _ptr(xB), _ptr(rs), p.v_B, ctot, N)
+    o.L.pfo_test_cons_init(o.s, _ptr(phi), _ptr(xB), _ptr(gs))
+    assert np.abs(gs - rs).max() <= 1e-15
+
+    dctx = np.array([p.temperature_K, p.v_B, p.pf_conservative_beta_support_eps, p.xB_eps, p.Y_clip])
+    rx, rY, gx, gY = np.zeros(N), np.zeros(N), np.zeros(N), np.zeros(N)
+    L.refk_cons_context(_ptr(rs), _ptr(phi), _ptr(rx), _ptr(rY), ctot, N, _ptr(dctx), _ptr(np.zeros(ns)))
+    o.L.pfo_test_cons_context(o.s, _ptr(rs), _ptr(phi), _ptr(gx), _ptr(gY))
+    assert np.abs(gx - rx).max() <= 1e-15
+    assert np.abs(gY - rY).max() <= 1e-12 * np.abs(rY).max()
+
+    mu = rng.normal(0.0, 2.0, N)
+    L.refk_set_convex(p.thermo_convex_extrapolation_enabled)
+    import oracle_py
+    dt = 5.0 * p.dt                            # large enough that some faces hit the storage bounds
+    for be in (0, 1):
+        rsw, gsw = rs.copy(), rs.copy()
+        st = np.zeros(ns)
+        ob = oracle_py.Oracle(params_for(capi, "c2.params", n=n, pf_composition_mode=mode, dt=dt,
+                                         pf_conservative_flux_strategy=be), threads=1)
+        ob.L.pfo_test_cons_sweep.restype = ctypes.c_longlong
+        ob.L.pfo_test_cons_sweep.argtypes = o.L.pfo_test_cons_sweep.argtypes
+        glim = 0
+        for axis, sp in ((0, p.dx), (1, p.dy), (2, p.dz)):
+            for par in (0, 1):
+                d = np.array([sp, dt, p.D_alpha, p.Vm_alpha_0, p.dVm_alpha_dxB, p.Vm_compound, p.temperature_K,
+                              p.mu_reference_scale, p.v_B, p.pf_conservative_bound_tol])
+                L.refk_cons_sweep(_ptr(rsw), _ptr(mu), _ptr(phi), _ptr(rx), n, n, n, axis, par, ctot, be, _ptr(d),
+                                  _ptr(st))
+                glim += ob.L.pfo_test_cons_sweep(ob.s, _ptr(gsw), _ptr(mu), _ptr(phi), _ptr(rx), axis, par, sp)
+        assert glim == int(round(st[li.value])) and (be == 1 or glim > 0)
+        assert np.abs(gsw - rsw).max() <= 1e-15
+        # the sweeps move storage between cells: its sum is unchanged
+        assert abs(rsw.sum() - rs.sum()) <= 1e-12 * abs(rs.sum())
+
+    # the phase constraint
+    phi_old = np.clip(phi, 0.0, 1.0)
+    phi_new = np.clip(phi_old + rng.normal(0.0, 0.3, N), -0.05, 1.05)
+    dcon = np.array([p.temperature_K, p.v_B, p.pf_conservative_beta_support_eps, p.xB_eps, p.Y_clip,
+                     p.pf_conservative_bound_tol])
+    rphi, rst, rx2, rY2 = phi_new.copy(), rsw.copy(), np.zeros(N), np.zeros(N)
+    st = np.zeros(ns)
+    L.refk_cons_constrain(_ptr(rphi), _ptr(phi_old), _ptr(rst), _ptr(rx2), _ptr(rY2), ctot, N, _ptr(dcon), _ptr(st))
+    gphi, gst, gx2, gY2 = phi_new.copy(), rsw.copy(), np.zeros(N), np.zeros(N)
+    capped = ctypes.c_longlong()
+    bad = o.L.pfo_test_cons_constrain(o.s, _ptr(gphi), _ptr(phi_old), _ptr(gst), _ptr(gx2), _ptr(gY2),
+                                      ctypes.byref(capped))
+    assert capped.value == int(round(st[lc.value])) and capped.value > 0
+    assert bad == int(round(st[lv.value] + st[lnf.value]))
+    assert np.abs(gphi - rphi).max() <= 1e-15
+    assert np.abs(gst - rst).max() <= 1e-15
+    assert np.abs(gx2 - rx2).max() <= 1e-15
+    assert np.abs(gY2 - rY2).max() <= 1e-12 * np.abs(rY2).max()

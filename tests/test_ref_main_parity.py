@@ -431,13 +431,58 @@ def test_q_transport_split_vtk(capi, ref_main, tmp_path, case):
     if case == "bounds":
         assert ("rejected" in [e[1] for e in er]) and any(e[1] == "redistributed" for e in er), rec
     f, _ = _library_fields(capi, "c2.params", n, extra, fields, 0.07, steps, 0, False)
-    last = steps // every + 1
+    last = steps if steps % every == 0 else steps // every + 1
     for k in ("phi", "xB"):
         ref = _vtk(os.path.join(cr, f"{k}_{last}.vtk"), n)
         cli = _vtk(os.path.join(co, f"{k}_{last}.vtk"), n)
         rec[f"{k}_maxabs_lib_fp64"] = float(np.abs(f[k] - ref).max())
         rec[f"{k}_maxabs_cli"] = float(np.abs(cli - ref).max())
     _report("q_split_" + case, rec)
+    for k, v in rec.items():
+        if "maxabs" in k:
+            assert v <= 1.5e-5, (k, rec)
+
+
+@pytest.mark.parametrize("mode,strategy", [("ctot_conservative_split", "pairwise_limited"),
+                                           ("qalpha_conservative_local_transaction", "pairwise_backward_euler")])
+def test_conservative_composition_vtk(capi, ref_main, tmp_path, mode, strategy):
+    """pf_composition_mode ctot / qalpha against the reference program: a
+    sharp particle at the file's dt for 4 steps without elasticity (the
+    limiter and the phase constraint are branches that the FP32 elastic
+    solve's round-off would move cells across): the two programs' output
+    files and CSV rows, and the last phi and xB VTK files against the
+    library's FP64 fields."""
+    from cuda_sto_pf_gb300 import build, workloads
+    n, steps, every = 32, 4, 2
+    p0 = params_for(capi, "c2.params", n=n)
+    rng = np.random.default_rng(23)
+    phi = workloads.ellipsoid_field((n, n, n), [np.full(3, n / 2.0)], [np.array([7.0, 6.0, 5.0])],
+                                    [workloads.random_rotation(rng)], p0.ic_phi_iface_w)
+    xB = workloads.composition(phi, rng)
+    fields = {"phi": phi, "xB": xB}
+    extra = {"pf_composition_mode": mode, "pf_conservative_flux_strategy": strategy, "elastic_enabled": "0"}
+    d = str(tmp_path)
+    paths = _write_inputs(os.path.join(d, "in"), fields, n, 0.07)
+    pf = _params_file(d, "c2.params", extra)
+    argv = _argv(n, steps, every, pf, paths, False, None)
+    argv[6] = "1"
+    r = _run(ref_main, argv, os.path.join(d, "R_ref"))
+    assert r.returncode == 0, "reference main_cuda failed:\n" + r.stdout[-3000:] + r.stderr[-3000:]
+    o = _run(build.EXE, argv, os.path.join(d, "R_ours"))
+    assert o.returncode == 0, o.stdout[-3000:] + o.stderr[-3000:]
+    cr, co = _case_dir(os.path.join(d, "R_ref")), _case_dir(os.path.join(d, "R_ours"))
+    rec = {"n": n, "steps": steps, "mode": mode, "strategy": strategy}
+    _compare_outputs(cr, co, "conservative_" + mode, rec)
+    f, _ = _library_fields(capi, "c2.params", n, extra, fields, 0.07, steps, 0, False)
+    # on the schedule a file carries its step number; an off-schedule last
+    # step is numbered steps // every + 1 (main_cuda.cu:33815-33840)
+    last = steps if steps % every == 0 else steps // every + 1
+    for k in ("phi", "xB"):
+        ref = _vtk(os.path.join(cr, f"{k}_{last}.vtk"), n)
+        cli = _vtk(os.path.join(co, f"{k}_{last}.vtk"), n)
+        rec[f"{k}_maxabs_lib_fp64"] = float(np.abs(f[k] - ref).max())
+        rec[f"{k}_maxabs_cli"] = float(np.abs(cli - ref).max())
+    _report("conservative_" + mode, rec)
     for k, v in rec.items():
         if "maxabs" in k:
             assert v <= 1.5e-5, (k, rec)
