@@ -21,6 +21,8 @@ MODE_DYNAMICS, MODE_MINIMIZE = 0, 1
 Y_LAGGED_RHS, Y_STORAGE_EXACT, Y_X_TRANSPORT_SPLIT, Y_Q_TRANSPORT_SPLIT = 0, 1, 2, 3
 COMPOSITION_LEGACY, COMPOSITION_CTOT, COMPOSITION_QALPHA = 0, 1, 2
 CONS_FLUX_PAIRWISE_LIMITED, CONS_FLUX_BACKWARD_EULER = 0, 1
+GP_Y_OLD_RHS, GP_Y_PICARD_STORAGE, GP_Y_STORAGE_EXACT, GP_Y_CONSERVATIVE_RHS = 0, 1, 2, 3
+GP_ETA_LIMITER_OFF, GP_ETA_LIMITER_LOCAL_CLIP = 0, 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "device out of memory",
           4: "elastic solver did not converge", 5: "zero-mode mass solve rejected the step",
@@ -89,7 +91,8 @@ class Params(Structure):
         ("pf_composition_mode", c_int32), ("pf_conservative_flux_strategy", c_int32),
         ("pf_conservative_bound_tol", c_double), ("pf_conservative_mass_tol", c_double),
         ("pf_conservative_beta_support_eps", c_double), ("pf_conservative_max_subcycles", c_int32),
-        ("pad_cons", c_int32),
+        ("gp_y_update_mode", c_int32), ("gp_eta_mass_limiter", c_int32), ("gp_y_picard_iters", c_int32),
+        ("gp_limiter_flux_from_xn", c_int32), ("pad_gp", c_int32),
         ("temperature_K", c_double), ("mu0_compound", c_double), ("xB_eq_matrix", c_double),
     ]
 
@@ -104,6 +107,7 @@ class StepStats(Structure):
         ("zero_mode_target_mass", c_double), ("mean_DY", c_double),
         ("q_phase_rejected", c_int32), ("q_redistributed_cells", c_int32),
         ("cons_limited_faces", c_int32), ("cons_phase_constrained", c_int32),
+        ("gp_eta_limited_cells", c_int32), ("pad_stats", c_int32),
     ]
 
 

@@ -108,6 +108,7 @@ const DKey kInts[] = {
     DK("elastic_chebyshev", elastic_chebyshev), DK("fft_tensor_cores", fft_tensor_cores),
     DK("zero_mode_fp64_cells", zero_mode_fp64_cells),
     DK("pf_conservative_max_subcycles", pf_conservative_max_subcycles),
+    DK("gp_y_picard_iters", gp_y_picard_iters), DK("gp_limiter_flux_from_xn", gp_limiter_flux_from_xn),
     DK("enable_Y_rhs_previous_time_level", enable_Y_rhs_previous_time_level),
     DK("disable_Y_rhs_gamma_term", disable_Y_rhs_gamma_term),
     DK("gp_elastic_enabled", gp_elastic_enabled), DK("gp_elastic_active_eta", gp_elastic_active_eta),
@@ -230,6 +231,18 @@ extern "C" pfgb_status pfgb_params_set(pfgb_params *p, const char *key, const ch
             p->pf_y_update_mode = PFGB_Y_Q_TRANSPORT_SPLIT;
             return PFGB_OK;
         }
+        return PFGB_ERR_INVALID;
+    }
+    if (!strcmp(key, "gp_y_update_mode")) {   // main_cuda.cu:22254-22263
+        if (!strcmp(value, "old_rhs")) { p->gp_y_update_mode = PFGB_GP_Y_OLD_RHS; return PFGB_OK; }
+        if (!strcmp(value, "conservative_y_rhs")) { p->gp_y_update_mode = PFGB_GP_Y_CONSERVATIVE_RHS; return PFGB_OK; }
+        if (!strcmp(value, "picard_storage")) { p->gp_y_update_mode = PFGB_GP_Y_PICARD_STORAGE; return PFGB_OK; }
+        if (!strcmp(value, "storage_exact")) { p->gp_y_update_mode = PFGB_GP_Y_STORAGE_EXACT; return PFGB_OK; }
+        return PFGB_ERR_INVALID;
+    }
+    if (!strcmp(key, "gp_eta_mass_limiter")) {   // main_cuda.cu:22244-22252 (off or local_clip)
+        if (!strcmp(value, "off")) { p->gp_eta_mass_limiter = PFGB_GP_ETA_LIMITER_OFF; return PFGB_OK; }
+        if (!strcmp(value, "local_clip")) { p->gp_eta_mass_limiter = PFGB_GP_ETA_LIMITER_LOCAL_CLIP; return PFGB_OK; }
         return PFGB_ERR_INVALID;
     }
     if (!strcmp(key, "pf_composition_mode")) {   // pf_params.h:349, checked at main_cuda.cu:1697-1703

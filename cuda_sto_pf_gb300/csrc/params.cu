@@ -120,6 +120,9 @@ void pfgb_params_default(pfgb_params *p) {
     p->pf_composition_stabilizer_Dalpha_multiplier = 10.0; // main_cuda.cu:16117
     p->gp_barrier_only_mode = 1;                           // main_cuda.cu:15823
     p->enable_legacy_gp_storage_coupling = 0;              // main_cuda.cu:15824
+    p->gp_y_update_mode = PFGB_GP_Y_OLD_RHS;               // main_cuda.cu:16188-16190
+    p->gp_eta_mass_limiter = PFGB_GP_ETA_LIMITER_OFF;
+    p->gp_y_picard_iters = 3;
     p->elastic_residual_tolerance = 1.0e-6;
     p->elastic_residual_absolute_floor = 1.0e-30;
     p->eps_iso_over_vB = -1.0;

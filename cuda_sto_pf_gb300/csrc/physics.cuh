@@ -42,6 +42,10 @@ struct PhysCT {
     R gp_Cg;           // offA(xg)(1-xg) + offB(xg) xg - delta_g0
     int gp, gp_el, act_eta, act_phi;
     int coupling, elastic, zm, prev_level, disable_gamma, xb_raw;
+    // GP storage coupling: 0 off; 1 old_rhs (h_alpha floored at haeps in the
+    // gamma term); 2 conservative_y_rhs; 3 a storage point update
+    int gpy;
+    R haeps;           // gp_h_alpha_eps
     // upper cap on the composition seen by the eigenstrain of the elastic
     // solve and the stress (minimize_xB_max_safe once the minimize monitor
     // has clamped xB; above 1 = inactive)
@@ -69,6 +73,7 @@ PhysCT<R> phys_as(const PhysC &c) {
     o.gp = c.gp; o.gp_el = c.gp_el; o.act_eta = c.act_eta; o.act_phi = c.act_phi;
     o.coupling = c.coupling; o.elastic = c.elastic; o.zm = c.zm; o.prev_level = c.prev_level;
     o.disable_gamma = c.disable_gamma; o.xb_raw = c.xb_raw;
+    o.gpy = c.gpy; o.haeps = R(c.haeps);
     o.xbcap = R(c.xbcap); o.dx = R(c.dx); o.dy = R(c.dy); o.dz = R(c.dz);
     o.tc = thermo_as<R>(c.tc);
     return o;

@@ -86,6 +86,7 @@ struct pfgb_ctx {
     void *Yprev = nullptr;   // Y_f of the last step's start, for the stress export
     void *q = nullptr, *qb = nullptr, *divr = nullptr;   // q split state (pf_y_update_mode q)
     int q_rejected = 0, q_redistributed = 0;             // of the last step
+    int gp_limited = 0;                                  // GP eta limiter: cells limited in the last step
     double *cstore = nullptr, *cmu = nullptr;            // conservative modes: storage and mu (FP64)
     int cons_limited = 0, cons_constrained = 0;          // of the last step
     int cur = 0, ecur = 0;
@@ -578,7 +579,9 @@ struct OpACStoreZ {   // z pass consumer: clamp and store the new order paramete
 // ===========================================================================
 // (1) chemical potential mu (compute_mu_x_kernel :1266-1324 / compute_mu_C_gp
 // :1326-1366) and sum of D_mix(h) xB (1-xB) (reduce_sum_DY_kernel :3870).
-template <typename T, typename TE>
+// GPC: the GP storage coupling's <DY> (a separate instance, so the other
+// paths carry none of its code)
+template <typename T, typename TE, bool GPC = false>
 struct OpMuR2C {
     using Acc = AccSum1;
     DevState<T, TE> d; PhysCT<T> c; ElasC<TE> ec;
@@ -600,7 +603,7 @@ struct OpMuR2C {
         fetch(cell, p);
         point_with(cell, p, in, out, acc);
     }
-    __device__ void point_with(long long, const Pre &p, const T *, T *out, Acc &acc) const {
+    __device__ void point_with(long long cell, const Pre &p, const T *, T *out, Acc &acc) const {
         const T Yv = p.Y + T(d.Yc);
         const T phiY = p.pn;
         const T xB = sigmoid_clip(Yv, T(c.Yclip), T(c.xBeps));
@@ -625,6 +628,14 @@ struct OpMuR2C {
             mu += -T(c.eiv) * (T(s[0]) + T(s[1]) + T(s[2]));
         }
         out[0] = mu;
+        if constexpr (GPC) {
+            // reduce_sum_DY_gp_kernel (:3923-3955): h_alpha D_alpha x (1 - x)
+            // at eta_for_Y_explicit (main_cuda.cu:30292)
+            const T hp = pf_h(phiY), he = pf_h(c.prev_level ? d.eta_old[cell] : d.eta_new[cell]);
+            const T xs = sigmoid_clip(Yv, T(20), T(1e-12));
+            acc.s += double((T(1) - hp) * (T(1) - he) * T(c.Da) * (xs * (T(1) - xs)));
+            return;
+        }
         const T h = pf_h(phiY);
         const T Dm = (T(1) - h) * T(c.Da) + h * T(c.Dc);
         T x = sigmoid_raw(Yv);
@@ -658,7 +669,9 @@ struct OpGradX {
 // source T = term_h + term_gamma of the Y right-hand side
 // (compute_Y_rhs_kernel :2185-2266 / _sm_tangent_n_ :2268-2359) and Y^n,
 // then R2C.  The spectral side combines i kz J_z - T into one array.
-template <typename T, typename TE>
+// GPC: the GP storage coupling's source and the limiter's second flux (a
+// separate instance, so the other paths carry none of their code)
+template <typename T, typename TE, bool GPC = false>
 struct OpFluxZ {
     using Acc = NoAcc;
     DevState<T, TE> d; PhysCT<T> c;
@@ -681,7 +694,7 @@ struct OpFluxZ {
         fetch(cell, p);
         point_with(cell, p, g, out, acc);
     }
-    __device__ void point_with(long long, const Pre &p, const T *g, T *out, Acc &) const {
+    __device__ void point_with(long long cell, const Pre &p, const T *g, T *out, Acc &) const {
         const T Yf = p.Y;
         const T Yv = Yf + T(d.Yc);
         const T pn = p.pn, pp = p.pp;
@@ -689,10 +702,22 @@ struct OpFluxZ {
         const T xBp = sigmoid_clip(Yv, T(c.Yclip), T(c.xBeps));
         // q split: the matrix channel alone, (1 - h) M_alpha with G_alpha at
         // h = 0 (compute_flux_single_component_q_kernel, cuda_kernels.cu:2014-2037)
-        const T M = qmob ? (T(1) - pf_h(clamp01(phiY))) *
-                               stabilized_meff<T>(T(c.Da), gamma_thermo<T>(c.tc, xBp, T(0), T(c.Vm0), T(c.dVm),
-                                                                            T(c.Vmc)))
-                         : mobility<T>(c, phiY, p.eta, xBp);
+        T M;
+        if (GPC && xmob) {
+            // the GP mobility at the composition held in xmob, in FP64 as the
+            // reference evaluates it (compute_flux_single_component_gp_kernel,
+            // cuda_kernels.cu:2039-2071; outside [0, 1] its difference quotient
+            // is not finite and the mobility takes its cap)
+            const double hb = pf_h(double(phiY)), he = pf_h(double(p.eta));
+            const double Ga = gamma_thermo<double>(tcd, double(xmob[cell]), 0.0, md[0], md[1], md[2]);
+            const double Ma = stabilized_meff<double>(md[3], Ga);
+            M = T((1.0 - hb) * (1.0 - he) * Ma + (1.0 - hb) * he * md[4] + hb * md[5]);
+        } else {
+            M = qmob ? (T(1) - pf_h(clamp01(phiY))) *
+                           stabilized_meff<T>(T(c.Da), gamma_thermo<T>(c.tc, xBp, T(0), T(c.Vm0), T(c.dVm),
+                                                                        T(c.Vmc)))
+                     : mobility<T>(c, phiY, p.eta, xBp);
+        }
         out[0] = M * g[0];
         out[1] = M * g[1];
         out[2] = M * g[2];
@@ -703,7 +728,19 @@ struct OpFluxZ {
         const T dYdt = p.dydt + T(d.dYoff);
         const T dt = T(c.dt);
         T src;
-        if (c.zm) {
+        if (GPC) {
+            // GP storage source and gamma term (compute_Y_rhs_gp_kernel
+            // :2361-2430; conservative_y_rhs :2432-2527 without the floor)
+            const T hpn = pf_h(pp), hen = pf_h(p.eta), hpo = pf_h(pn), heo = pf_h(d.eta_old[cell]);
+            const T hgn = (T(1) - hpn) * hen, hgo = (T(1) - hpo) * heo;
+            const T han = (T(1) - hpn) * (T(1) - hen), hao = (T(1) - hpo) * (T(1) - heo);
+            const T xs = sigmoid_clip(Yv, T(20), T(1e-12));
+            const T qd = xs * (T(1) - xs);
+            const T ss = ((hgn - hgo) / dt) * (T(c.gpxB) - xs) + ((hpn - hpo) / dt) * (T(1) - xs);
+            const T hx = c.prev_level ? hao : han;
+            const T gl = (c.gpy == 2 ? hx : (hx > T(c.haeps) ? hx : T(c.haeps))) * qd - T(1);
+            src = ss + (c.disable_gamma ? T(0) : gl * dYdt);
+        } else if (c.zm) {
             const T th = pf_hp(pn) * ((pp - pn) / dt) * (T(c.vB) - x);
             const T gl = (T(1) - pf_h(pn)) * ld - T(1);
             src = th + gl * dYdt;
@@ -719,6 +756,13 @@ struct OpFluxZ {
     }
     int no_src = 0;   // storage_exact and the splits: the divergence of J alone
     int qmob = 0;     // q split: the matrix-channel mobility
+    // GP eta limiter, second flux: the mobility's composition read from this
+    // array (the reference's aliased buffer, see gp_y_update), with the FP64
+    // thermodynamic constants and Vm_alpha_0, dVm_alpha_dxB, Vm_compound,
+    // D_alpha, gp_M_GP, gp_M_beta in md
+    const T *xmob = nullptr;
+    ThermoConstT<double> tcd{};
+    double md[6] = {0, 0, 0, 0, 0, 0};
     __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
         const long long o = row * d.g.NzC + k;
         const T kz = T(d.kt.kz[k]);
@@ -985,6 +1029,181 @@ __device__ __forceinline__ double h_inverse_bisect(double target) {
     }
     return 0.5 * (lo + hi);
 }
+
+// ---------------------------------------------------------------------------
+// GP storage coupling (gp_zone with gp_barrier_only_mode = 0 or
+// enable_legacy_gp_storage_coupling = 1): the conserved composition is
+// xBtot_gp = h_alpha x + h_GP x_GP + h_beta, with h_beta = h(phi),
+// h_GP = (1 - h(phi)) h(eta), h_alpha = (1 - h(phi)) (1 - h(eta))
+// (phase_fractions_gp, phase_functions.h:27-42)
+// ---------------------------------------------------------------------------
+// the matrix composition recovered from a storage target and whether it lies
+// in [x_min, x_max] (gp_recovered_xB_valid_device, cuda_kernels.cu:1100-1120)
+template <typename T>
+__device__ __forceinline__ bool gp_recovered_valid(T tot, T hb, T A, T hg, T xg, T xmin, T xmax, T eh) {
+    if (!isfinite(tot) || !isfinite(hb) || !isfinite(A) || !isfinite(hg)) return false;
+    if (A < T(0) || hg < T(0) || hg > A) return false;
+    const T ha = A - hg;
+    if (!(ha >= eh)) return false;
+    const T num = tot - hg * xg - hb;
+    if (!isfinite(num)) return false;
+    const T x = num / ha;
+    if (!isfinite(x)) return false;
+    return x >= xmin && x <= xmax;
+}
+
+// the largest GP fraction in [0, min(h_GP, A)] that keeps the recovered
+// composition valid, by 80 bisections (gp_limited_hGP_device, :1122-1149)
+template <typename T>
+__device__ __forceinline__ T gp_limited_hgp(T tot, T hb, T A, T hg_tent, T xg, T xmin, T xmax, T eh) {
+    if (!isfinite(tot) || !isfinite(hb) || !isfinite(A) || !isfinite(hg_tent)) return T(0);
+    const T hi0 = fmin(fmax(hg_tent, T(0)), fmax(A, T(0)));
+    if (gp_recovered_valid(tot, hb, A, hi0, xg, xmin, xmax, eh)) return hi0;
+    T lo = T(0), hi = hi0;
+    for (int it = 0; it < 80; ++it) {
+        const T mid = T(0.5) * (lo + hi);
+        if (gp_recovered_valid(tot, hb, A, mid, xg, xmin, xmax, eh)) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// z pass on div J after the flux (main_cuda.cu:30449-30503): the eta
+// feasibility pass (gp_eta_feasibility_and_limiter_kernel, :1151-1250):
+// eta^{n+1} clamped to [0, 1]; with the local_clip limiter, where the
+// storage target xBtot_gp^n + dt div J admits no matrix composition in
+// [xB_eps, 1 - xB_eps] under the tentative GP fraction, the fraction is
+// lowered to the largest feasible one and eta follows by inverting h.
+// stage 0: the pass alone (the limiter runs it again on a new div J);
+// (with keep_div it also keeps div J in divr, the composition of the second
+// flux's mobility as the reference computes it);
+// stage 1: then the storage point update of Y, gp_storage_exact_Y_update_kernel
+// (:2746-2857) or gp_y_picard_iters sweeps of gp_picard_storage_Y_update_kernel
+// (:3290-3370) from the guess Y^n; stage 2: then div J kept in divr for the
+// right-hand side pass.  Partials: limited cells and <DY> (reduce_sum_DY_gp_kernel,
+// :3923-3955, with the final eta).
+template <typename T, typename TE>
+struct OpGPEtaZ {
+    using Acc = AccSum2;
+    DevState<T, TE> d; PhysCT<T> c; const cplx_t<T> *src;
+    int limiter, stage, picard, iters; double invN;
+    int keep_div = 0;   // stage 0: div J kept in divr as well
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const { v[0] = src[row * d.g.NzC + k]; }
+    __device__ void point(long long cell, const T *in, T *, Acc &acc) const {
+        const T one = T(1), dt = T(c.dt), xg = T(c.gpxB), eh = T(c.haeps);
+        const T eps = T(c.xBeps), xmax = one_minus_eps(eps), yc = T(c.Yclip);
+        const T dJ = in[0];
+        const T Yf = d.Y[cell];
+        const T Yn = Yf + T(d.Yc);
+        const T pn = d.phi_new[cell], po = d.phi_old[cell], eo = d.eta_old[cell];
+        const T et = clamp01(d.eta_new[cell]);
+        // feasibility on the clamped fields, x^n the composition of Y^n
+        const T xo = sigmoid_clip(Yn, yc, eps);
+        const T hpo_c = pf_h(clamp01(po));
+        const T hgo_c = (one - hpo_c) * pf_h(clamp01(eo));
+        const T hpn_c = pf_h(clamp01(pn));
+        const T A = fmax(one - hpn_c, T(0));
+        const T hg_tent = A * pf_h(et);
+        const T target = (xo + hgo_c * (xg - xo) + hpo_c * (one - xo)) + dt * dJ;
+        T ef = et;
+        if (limiter && A > eh && hg_tent > T(0) &&
+            !gp_recovered_valid(target, hpn_c, A, hg_tent, xg, eps, xmax, eh)) {
+            const T hgf = gp_limited_hgp(target, hpn_c, A, hg_tent, xg, eps, xmax, eh);
+            const T allowed = clamp01(hgf / fmax(A, eh));
+            ef = T(h_inverse_bisect(double(allowed)));
+            if (!isfinite(ef)) ef = T(0);
+            ef = clamp01(ef);
+            if (fabs(et - ef) > T(0)) acc.a += 1.0;
+        }
+        d.eta_new[cell] = ef;
+        if (stage == 0) {
+            if (keep_div) d.divr[cell] = dJ;
+            return;
+        }
+        {   // <DY> at phi_for_Y_explicit, eta_for_Y_explicit (main_cuda.cu:30286-30292)
+            const T hp = pf_h(c.prev_level ? po : pn), he = pf_h(c.prev_level ? eo : ef);
+            const T xs = sigmoid_clip(Yn, T(20), T(1e-12));
+            acc.b += double((one - hp) * (one - he) * T(c.Da) * (xs * (one - xs))) * invN;
+        }
+        if (stage == 2) { d.divr[cell] = dJ; return; }
+        // the storage update on the fields as stored (not clamped)
+        const T hpo = pf_h(po), heo = pf_h(eo), hpn = pf_h(pn), hen = pf_h(ef);
+        const T hgo = (one - hpo) * heo;
+        const T hgn = (one - hpn) * hen, han = (one - hpn) * (one - hen);
+        const T So = hgo * (xg - xo) + hpo * (one - xo);
+        T y;
+        if (!picard) {
+            const T tot = xo + So + dt * dJ;
+            if (!isfinite(tot)) {
+                y = Yn;
+            } else {
+                T xu = xo;
+                if (!(han < eh)) xu = (tot - hgn * xg - hpn) / han;
+                if (!isfinite(xu)) xu = xo;
+                y = logit_clip(xu, eps, yc);
+            }
+        } else {
+            const bool small = han < fmax(eps, T(1.0e-8));
+            y = Yn;
+            for (int it = 0; it < iters; ++it) {
+                const T xs = sigmoid_clip(y, yc, eps);
+                T xu = xo;
+                if (!small) xu = xo + dt * (dJ - ((hgn * (xg - xs) + hpn * (one - xs)) - So) / dt);
+                y = logit_clip(xu, eps, yc);
+            }
+        }
+        const T yn = y - T(d.Yc);
+        d.Y[cell] = yn;
+        d.Yprev[cell] = Yf;
+        d.dYdt[cell] = (yn - Yf) / dt;
+    }
+    __device__ void store_spec(long long, int, const cplx_t<T> *) const {}
+    __device__ void finish(int b, const Acc &a) const { reinterpret_cast<Acc *>(d.partials)[b] = a; }
+};
+
+// R2C z pass of the limited-eta right-hand side: R = div J - S - gamma dY/dt
+// from the div J kept by OpGPEtaZ (compute_Y_rhs_gp_kernel :2361-2430 /
+// compute_Y_rhs_gp_conservative_kernel :2432-2527 less the Laplacian term,
+// which the x pass applies), and Y^n
+template <typename T, typename TE>
+struct OpGPRhsZ {
+    using Acc = NoAcc;
+    DevState<T, TE> d; PhysCT<T> c;
+    __device__ void load_spec(long long, int, cplx_t<T> *) const {}
+    __device__ void point(long long cell, const T *, T *out, Acc &) const {
+        const T one = T(1), dt = T(c.dt);
+        const T Yf = d.Y[cell];
+        const T pn = d.phi_new[cell], po = d.phi_old[cell];
+        const T hpn = pf_h(pn), hen = pf_h(d.eta_new[cell]), hpo = pf_h(po), heo = pf_h(d.eta_old[cell]);
+        const T hgn = (one - hpn) * hen, hgo = (one - hpo) * heo;
+        const T han = (one - hpn) * (one - hen), hao = (one - hpo) * (one - heo);
+        const T xs = sigmoid_clip(Yf + T(d.Yc), T(20), T(1e-12));
+        const T ss = ((hgn - hgo) / dt) * (T(c.gpxB) - xs) + ((hpn - hpo) / dt) * (one - xs);
+        const T hx = c.prev_level ? hao : han;
+        const T gl = (c.gpy == 2 ? hx : (hx > T(c.haeps) ? hx : T(c.haeps))) * (xs * (one - xs)) - one;
+        const T dYdt = d.dYdt[cell] + T(d.dYoff);
+        out[0] = d.divr[cell] - ss - (c.disable_gamma ? T(0) : gl * dYdt);
+        out[1] = Yf;
+    }
+    __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
+        const long long o = row * d.g.NzC + k;
+        d.S[0][o] = v[0];
+        d.S[1][o] = v[1];
+    }
+};
+
+// x pass of that update: Y_k = mask [Y^n_k + dt R_k / (1 + dt <DY> k^2)] / N
+// (Y_semi_implicit_update_kernel with rhs = R - <DY> Lap Y^n, exact algebra)
+template <typename T>
+struct OpYUpdRX {
+    static constexpr bool kInplace = false;
+    KTab kt; double dt, invN; const double *meanDY;
+    __device__ void apply(int i, int j, int k, const cplx_t<T> *in, cplx_t<T> *out) const {
+        using T2 = cplx_t<T>;
+        if (kt.cut(i, j, k)) { out[0] = mk2<T2>(T(0), T(0)); return; }
+        const T a = T(dt / (1.0 + dt * (*meanDY) * kt.k2(i, j, k)));
+        out[0] = cscale(cadd(in[1], cscale(in[0], a)), T(invN));
+    }
+};
 
 // x from the storage, the equilibrium composition where the matrix vanishes
 // or x is not finite, bounded; its logit (the shared tail of
@@ -2833,6 +3052,97 @@ static pfgb_status q_transport(pfgb_ctx *c, const DevState<T, TE> &d, const Phys
 // Y (composition) update: mu -> flux -> semi-implicit update -> dY/dt and
 // the zero mode (main_cuda.cu:30280-30800, 31618-31623).  d.phi_old = phi^n,
 // d.phi_new = phi^{n+1}; Y and the stored strain are those of the step start.
+// the GP storage-coupled Y update through div J in real space: the storage
+// point updates (gp_y_update_mode storage_exact / picard_storage) and the
+// local_clip eta limiter (main_cuda.cu:30449-30503, 30587-30591,
+// 30734-30760, 30912-30952).  Entered with the gradient of mu in real space
+// (S[0..2]).  With the limiter the flux and div J are formed again with the
+// limited eta and the feasibility pass runs on them once more; the
+// right-hand side update then uses that div J and the final eta.  The
+// reference keeps x^n for the mobility in the buffer of div J (d_xB_prev_r =
+// d_divJ_r, main_cuda.cu:27858), so its second flux evaluates the mobility
+// at the first pass's div J; that is reproduced unless
+// gp_limiter_flux_from_xn = 1, which takes x^n.
+template <typename T, typename TE>
+static pfgb_status gp_y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_stats *st) {
+    const pfgb_params &P = c->p;
+    const PhysCT<T> pc = phys_as<T>(c->pc);
+    const ElasC<TE> ec = elas_consts<TE>(c);
+    const KTab kt = d.kt;
+    const double invN = 1.0 / (double)c->g.N;
+    const double Nf = (double)c->g.N;
+    AxisIO<T, 1, 1> io1;
+    io1.in[0] = d.S[0]; io1.out[0] = d.S[0];
+    const bool direct = pc.gpy == 3;
+    const int lim = P.gp_eta_mass_limiter == PFGB_GP_ETA_LIMITER_LOCAL_CLIP;
+    const int picard = P.gp_y_update_mode == PFGB_GP_Y_PICARD_STORAGE;
+    const int iters = P.gp_y_picard_iters > 0 ? P.gp_y_picard_iters : 1;
+    const int passes = lim ? 2 : 1;
+    const bool alias = lim && !P.gp_limiter_flux_from_xn;
+    for (int pass = 0; pass < passes; ++pass) {
+        if (pass == 1) {   // mu is unchanged; its gradient again for the new flux
+            TRY((launch_z<T, 0, 1>(c, OpMuR2C<T, TE, true>{d, pc, ec}, "z_mu", 4.0 * Nf * sizeof(T))));
+            TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
+            AxisIO<T, 1, 3> iog;
+            iog.in[0] = d.S[0];
+            iog.out[0] = d.S[0]; iog.out[1] = d.S[1]; iog.out[2] = d.S[2];
+            TRY((launch_axis<T, 1, 3, -1, +1>(c, 2, iog, OpGradX<T>{kt, invN}, "x_grad")));
+            AxisIO<T, 3, 3> io3;
+            for (int i = 0; i < 3; ++i) { io3.in[i] = d.S[i]; io3.out[i] = d.S[i]; }
+            TRY((launch_axis<T, 3, 3, +1, 0>(c, 1, io3, OpCopy<T, 3>{}, "y_inv3")));
+        }
+        OpFluxZ<T, TE, true> fx{d, pc, 1, 0};
+        if (pass == 1 && alias) {
+            fx.xmob = d.divr;
+            fx.tcd = c->pc.tc;
+            const double md[6] = {P.Vm_alpha_0, P.dVm_alpha_dxB, P.Vm_compound, P.D_alpha, P.gp_M_GP, P.gp_M_beta};
+            for (int i = 0; i < 6; ++i) fx.md[i] = md[i];
+        }
+        TRY((launch_z<T, 3, 5>(c, fx, "z_flux", 5.0 * Nf * sizeof(T))));
+        {
+            AxisIO<T, 4, 3> io;
+            for (int i = 0; i < 4; ++i) io.in[i] = d.S[i];
+            io.out[0] = d.S[0]; io.out[1] = d.S[1]; io.out[2] = d.S[3];
+            TRY((launch_axis<T, 4, 3, -1, 0>(c, 1, io, OpYCombY<T>{kt}, "y_ycomb")));
+        }
+        {
+            AxisIO<T, 2, 1> io;
+            io.in[0] = d.S[0]; io.in[1] = d.S[1];
+            io.out[0] = d.S[0];
+            TRY((launch_axis<T, 2, 1, -1, +1>(c, 2, io, OpDivX<T>{kt, invN}, "x_div")));
+        }
+        TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+        const int stage = (pass + 1 < passes) ? 0 : (direct ? 1 : 2);
+        int nb = 0;
+        OpGPEtaZ<T, TE> ge{d, pc, d.S[0], lim, stage, picard, iters, invN};
+        ge.keep_div = stage == 0 && alias;
+        TRY((launch_z<T, 1, 0>(c, ge, "z_gp_eta", (stage == 1 ? 9.0 : 7.0) * Nf * sizeof(T), &nb)));
+        TRY(reduce_to<AccSum2>(c, nb, DS_BR + 2 * pass));
+    }
+    const double *meanDY = c->dscal + DS_BR + 2 * (passes - 1) + 1;
+    if (!direct) {
+        TRY((launch_z<T, 0, 2>(c, OpGPRhsZ<T, TE>{d, pc}, "z_gp_rhs", 8.0 * Nf * sizeof(T))));
+        AxisIO<T, 2, 2> io2;
+        for (int i = 0; i < 2; ++i) { io2.in[i] = d.S[i]; io2.out[i] = d.S[i]; }
+        TRY((launch_axis<T, 2, 2, -1, 0>(c, 1, io2, OpCopy<T, 2>{}, "y_fwd2")));
+        AxisIO<T, 2, 1> iox;
+        iox.in[0] = d.S[0]; iox.in[1] = d.S[1];
+        iox.out[0] = d.S[0];
+        TRY((launch_axis<T, 2, 1, -1, +1>(c, 2, iox, OpYUpdRX<T>{kt, P.dt, invN, meanDY}, "x_y_update")));
+        TRY((launch_axis<T, 1, 1, +1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_inv1")));
+        int nbf = 0;
+        TRY((launch_z<T, 1, 0>(c, OpYFinalZ<T, TE>{d, pc, d.S[0]}, "z_y_final", 4.0 * Nf * sizeof(T), &nbf)));
+    }
+    c->dYoff = 0.0;
+    c->gp_limited = 0;
+    if (st) {
+        TRY(sync_read(c, DS_BR, 4));
+        c->gp_limited = (int)(c->hscal[DS_BR] + (lim ? c->hscal[DS_BR + 2] : 0.0) + 0.5);
+        st->mean_DY = c->hscal[DS_BR + 2 * (passes - 1) + 1];
+    }
+    return PFGB_OK;
+}
+
 template <typename T, typename TE>
 static pfgb_status y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_stats *st) {
     const pfgb_params &P = c->p;
@@ -2844,7 +3154,11 @@ static pfgb_status y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_sta
     AxisIO<T, 1, 1> io1;
     io1.in[0] = d.S[0]; io1.out[0] = d.S[0];
     int nb = 0;
-    TRY((launch_z<T, 0, 1>(c, OpMuR2C<T, TE>{d, pc, ec}, "z_mu", (3.0 + pc.gp) * Nf * sizeof(T) + (pc.elastic ? 6.0 : 0.0) * Nf * sizeof(TE), &nb)));
+    const double mu_bytes = (3.0 + pc.gp) * Nf * sizeof(T) + (pc.elastic ? 6.0 : 0.0) * Nf * sizeof(TE);
+    if (pc.gpy)
+        TRY((launch_z<T, 0, 1>(c, OpMuR2C<T, TE, true>{d, pc, ec}, "z_mu", mu_bytes + Nf * sizeof(T), &nb)));
+    else
+        TRY((launch_z<T, 0, 1>(c, OpMuR2C<T, TE>{d, pc, ec}, "z_mu", mu_bytes, &nb)));
     TRY(reduce_to<AccSum1>(c, nb, DS_MEAN_DY, invN));
     TRY((launch_axis<T, 1, 1, -1, 0>(c, 1, io1, OpCopy<T, 1>{}, "y_fwd1")));
     {
@@ -2858,11 +3172,17 @@ static pfgb_status y_update(pfgb_ctx *c, const DevState<T, TE> &d, pfgb_step_sta
         for (int i = 0; i < 3; ++i) { io.in[i] = d.S[i]; io.out[i] = d.S[i]; }
         TRY((launch_axis<T, 3, 3, +1, 0>(c, 1, io, OpCopy<T, 3>{}, "y_inv3")));
     }
+    // GP storage coupling with a storage point update or the eta limiter
+    if (pc.gpy == 3 || (pc.gpy && P.gp_eta_mass_limiter == PFGB_GP_ETA_LIMITER_LOCAL_CLIP))
+        return gp_y_update<T, TE>(c, d, st);
     const bool storage_exact = P.pf_y_update_mode == PFGB_Y_STORAGE_EXACT;
     const bool qsplit = P.pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT;
     const bool divj_real = storage_exact || qsplit || P.pf_y_update_mode == PFGB_Y_X_TRANSPORT_SPLIT;
-    TRY((launch_z<T, 3, 5>(c, OpFluxZ<T, TE>{d, pc, divj_real ? 1 : 0, qsplit ? 1 : 0}, "z_flux",
-                           (4.0 + pc.gp) * Nf * sizeof(T))));
+    if (pc.gpy)
+        TRY((launch_z<T, 3, 5>(c, OpFluxZ<T, TE, true>{d, pc, 0, 0}, "z_flux", 6.0 * Nf * sizeof(T))));
+    else
+        TRY((launch_z<T, 3, 5>(c, OpFluxZ<T, TE>{d, pc, divj_real ? 1 : 0, qsplit ? 1 : 0}, "z_flux",
+                               (4.0 + pc.gp) * Nf * sizeof(T))));
     if (divj_real) {
         {
             AxisIO<T, 4, 3> io;
@@ -2978,6 +3298,7 @@ static pfgb_status step_once(pfgb_ctx *c, pfgb_step_stats *st) {
         st->q_phase_rejected = c->q_rejected;
         st->q_redistributed_cells = c->q_redistributed;
         st->cons_limited_faces = c->cons_limited;
+        st->gp_eta_limited_cells = c->gp_limited;
         st->cons_phase_constrained = c->cons_constrained;
     }
     c->cur = 1 - c->cur;
@@ -3454,6 +3775,10 @@ static void build_physc(pfgb_ctx *c) {
     k.prev_level = P.enable_Y_rhs_previous_time_level && P.pf_y_update_mode != PFGB_Y_Q_TRANSPORT_SPLIT;
     k.disable_gamma = P.disable_Y_rhs_gamma_term;
     k.xb_raw = P.zero_mode_enabled;
+    // gp_storage_coupling_enabled (main_cuda.cu:16767-16772)
+    if (k.gp && (P.enable_legacy_gp_storage_coupling || !P.gp_barrier_only_mode))
+        k.gpy = P.gp_y_update_mode == PFGB_GP_Y_OLD_RHS ? 1 : (P.gp_y_update_mode == PFGB_GP_Y_CONSERVATIVE_RHS ? 2 : 3);
+    k.haeps = P.gp_h_alpha_eps;
     k.xbcap = 2.0;
     k.dx = P.dx; k.dy = P.dy; k.dz = P.dz;
     pfgb_thermo_const(P.temperature_K, P.mu_reference_scale, P.thermo_convex_extrapolation_enabled, &k.tc);
@@ -3690,10 +4015,19 @@ static pfgb_status validate(const pfgb_params *p) {
                            "pf_composition_stabilizer_Dalpha_multiplier finite and > 0");
         return PFGB_ERR_INVALID;
     }
-    if (p->model_mode == PFGB_MODEL_GP_ZONE && (p->enable_legacy_gp_storage_coupling || !p->gp_barrier_only_mode)) {
-        // gp_storage_coupling_enabled (main_cuda.cu:16767-16772) selects the
-        // storage-coupled Y path and the eta feasibility limiter
-        pfgb_set_error_msg("gp_zone with the GP storage coupling (gp_barrier_only_mode=0 or "
+    if (p->gp_y_update_mode < PFGB_GP_Y_OLD_RHS || p->gp_y_update_mode > PFGB_GP_Y_CONSERVATIVE_RHS ||
+        (p->gp_eta_mass_limiter != PFGB_GP_ETA_LIMITER_OFF &&
+         p->gp_eta_mass_limiter != PFGB_GP_ETA_LIMITER_LOCAL_CLIP)) {
+        // main_cuda.cu:1218-1225
+        pfgb_set_error_msg("gp_y_update_mode: old_rhs, conservative_y_rhs, picard_storage or storage_exact; "
+                           "gp_eta_mass_limiter: off or local_clip");
+        return PFGB_ERR_INVALID;
+    }
+    if (p->model_mode == PFGB_MODEL_GP_ZONE && (p->enable_legacy_gp_storage_coupling || !p->gp_barrier_only_mode) &&
+        p->mode != PFGB_MODE_DYNAMICS) {
+        // gp_storage_coupling_enabled (main_cuda.cu:16767-16772): the
+        // storage-coupled Y update is built for dynamics
+        pfgb_set_error_msg("gp_zone minimize with the GP storage coupling (gp_barrier_only_mode=0 or "
                            "enable_legacy_gp_storage_coupling=1) is not built");
         return PFGB_ERR_UNSUPPORTED;
     }
@@ -4012,6 +4346,8 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
         A_(&c->q, rs * N);
         A_(&c->qb, rs * N);
         A_(&c->divr, rs * N);
+    } else if (c->pc.gpy && pin->gp_eta_mass_limiter == PFGB_GP_ETA_LIMITER_LOCAL_CLIP) {
+        A_(&c->divr, rs * N);   // the limiter's div J (second flux, right-hand side pass)
     }
     for (int i = 0; i < 4; ++i) { A_(&c->S[i], 2 * rs * Nk); }
     for (int i = 0; i < 6; ++i) { A_(&c->eps[i], sizeof(float) * N); }
@@ -4543,8 +4879,8 @@ struct AccDiag {
 };
 
 template <typename T>
-__global__ void k_diag(const T *phi, const T *Y, long long N, double Yc, int raw, double Yclip, double eps,
-                       double vB, AccDiag *part) {
+__global__ void k_diag(const T *phi, const T *Y, const T *eta, long long N, double Yc, int raw, double Yclip,
+                       double eps, double vB, double xgp, AccDiag *part) {
     AccDiag a = AccDiag::identity();
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
          i += (long long)gridDim.x * blockDim.x) {
@@ -4553,7 +4889,12 @@ __global__ void k_diag(const T *phi, const T *Y, long long N, double Yc, int raw
         const double x = raw ? sigmoid_raw(y) : sigmoid_clip(y, Yclip, eps);
         const double h = pf_h(p);
         a.vf += pf_h(clamp01(p));             // reduce_sum_h_kernel (:5580)
-        a.mass += (1.0 - h) * x + vB * h;      // reduce_sum_xBtot_kernel (:3792)
+        if (eta) {                             // GP storage coupling: reduce_sum_xBtot_gp_kernel (:3830)
+            const double he = pf_h(double(eta[i]));
+            a.mass += (1.0 - h) * (1.0 - he) * x + (1.0 - h) * he * xgp + h;
+        } else {
+            a.mass += (1.0 - h) * x + vB * h;  // reduce_sum_xBtot_kernel (:3792)
+        }
         a.xb += x;
         a.nin += p > 0.5 ? 1.0 : 0.0;                 // reduce_sum_N_in_N_if_kernel (:3746)
         a.nif += (p > 0.12 && p < 0.88) ? 1.0 : 0.0;
@@ -4571,12 +4912,16 @@ pfgb_status pfgb_diagnostics(pfgb_ctx *c, pfgb_diag *out) {
     PFGB_CUDA_TRY(cudaSetDevice(c->device));
     const int nb = 304;
     const int raw = c->p.zero_mode_enabled && c->step > 0;
+    // the model's xBtot (gpu_reduce_sum_model_xBtot, main_cuda.cu:21215-21224)
+    void *eta = c->pc.gpy ? c->eta[c->ecur] : nullptr;
     if (c->p.precision == PFGB_PREC_FP64)
-        k_diag<double><<<nb, 256, 0, c->stream>>>((double *)c->phi[c->cur], (double *)c->Y, c->g.N, c->Yc, raw,
-                                                  c->p.Y_clip, c->p.xB_eps, c->p.v_B, (AccDiag *)c->partials);
+        k_diag<double><<<nb, 256, 0, c->stream>>>((double *)c->phi[c->cur], (double *)c->Y, (const double *)eta,
+                                                  c->g.N, c->Yc, raw, c->p.Y_clip, c->p.xB_eps, c->p.v_B,
+                                                  c->p.gp_xB_fixed, (AccDiag *)c->partials);
     else
-        k_diag<float><<<nb, 256, 0, c->stream>>>((float *)c->phi[c->cur], (float *)c->Y, c->g.N, c->Yc, raw,
-                                                 c->p.Y_clip, c->p.xB_eps, c->p.v_B, (AccDiag *)c->partials);
+        k_diag<float><<<nb, 256, 0, c->stream>>>((float *)c->phi[c->cur], (float *)c->Y, (const float *)eta,
+                                                 c->g.N, c->Yc, raw, c->p.Y_clip, c->p.xB_eps, c->p.v_B,
+                                                 c->p.gp_xB_fixed, (AccDiag *)c->partials);
     PFGB_CUDA_TRY(cudaGetLastError());
     TRY(reduce_to<AccDiag>(c, nb, 24));
     TRY(sync_read(c, 24, 9));

@@ -238,6 +238,13 @@ Cli parse(int argc, char **argv) {
         else if ((v = flag_value(argc, argv, &i, "--pf_composition_mode")) ||
                  (v = flag_value(argc, argv, &i, "--pf-composition-mode")))   // main_cuda.cu:23415-23419
             c.param_sets.push_back({"pf_composition_mode", v});
+        else if ((v = flag_value(argc, argv, &i, "--gp-y-update-mode")) ||
+                 (v = flag_value(argc, argv, &i, "--gp_y_update_mode")))   // main_cuda.cu:24156-24166
+            c.param_sets.push_back({"gp_y_update_mode", v});
+        else if ((v = flag_value(argc, argv, &i, "--gp-barrier-only-mode")))   // main_cuda.cu:24293-24296
+            c.param_sets.push_back({"gp_barrier_only_mode", v});
+        else if ((v = flag_value(argc, argv, &i, "--enable-legacy-gp-storage-coupling")))   // :24297-24300
+            c.param_sets.push_back({"enable_legacy_gp_storage_coupling", v});
         else if ((v = flag_value(argc, argv, &i, "--pf_conservative_flux_strategy")) ||
                  (v = flag_value(argc, argv, &i, "--pf-conservative-flux-strategy")))   // main_cuda.cu:23420-23425
             c.param_sets.push_back({"pf_conservative_flux_strategy", v});
@@ -819,6 +826,12 @@ int main(int argc, char **argv) {
     mkdir(case_dir.c_str(), 0755);
     copy_file(c.param_file, case_dir + "/pf_input.params");
     const bool gp = P.model_mode == PFGB_MODEL_GP_ZONE;
+    // gp_storage_coupling_enabled (main_cuda.cu:16767-16772): the outputs carry
+    // xBtot_gp = h_alpha x + h_GP x_GP + h_beta (xBtot_output_stem,
+    // xBtot_vtk_field_name, main_cuda.cu:16774-16780)
+    const bool gpc = gp && (P.enable_legacy_gp_storage_coupling || !P.gp_barrier_only_mode);
+    const std::string xbt_stem = gpc ? "/xBtot_gp" : "/xBtot";
+    const char *xbt_name = gpc ? "xBtot_gp" : "xB_tot";
     printf("output_dir=%s\ncase_output_dir=%s\n", out_dir.c_str(), case_dir.c_str());
 
     // ---- solver -----------------------------------------------------------
@@ -872,13 +885,19 @@ int main(int argc, char **argv) {
         return pfgb_read_fields(ctx, f_phi.data(), f_xB.data(), nullptr, gp ? f_eta.data() : nullptr, nullptr);
     };
     auto vtk_set = [&](const char *suffix, int step) -> bool {
+        // launch_compute_model_xBtot_kernel (main_cuda.cu:19855-19866)
         for (size_t i = 0; i < N; ++i) {
             const double h = h_of(f_phi[i]);
-            f_xBtot[i] = (1.0 - h) * f_xB[i] + h * P.v_B;
+            if (gpc) {
+                const double he = h_of(f_eta[i]);
+                f_xBtot[i] = (1.0 - h) * (1.0 - he) * f_xB[i] + (1.0 - h) * he * P.gp_xB_fixed + h;
+            } else {
+                f_xBtot[i] = (1.0 - h) * f_xB[i] + h * P.v_B;
+            }
         }
         // the fields of one output set are written in parallel
         struct Job { std::string path; const char *name; const std::vector<double> *v; bool ok; };
-        std::vector<Job> jobs = {{case_dir + "/xBtot" + suffix + ".vtk", "xB_tot", &f_xBtot, false},
+        std::vector<Job> jobs = {{case_dir + xbt_stem + suffix + ".vtk", xbt_name, &f_xBtot, false},
                                  {case_dir + "/xB" + suffix + ".vtk", "xB", &f_xB, false},
                                  {case_dir + "/phi" + suffix + ".vtk", "phi", &f_phi, false}};
         if (gp) jobs.push_back({case_dir + "/eta" + suffix + ".vtk", "eta", &f_eta, false});
@@ -968,11 +987,19 @@ int main(int argc, char **argv) {
         write_vtk(case_dir + "/phi_init_" + tag + ".vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
         if (P.minimize_full_model) write_vtk(case_dir + "/xB_init_" + tag + ".vtk", "xB", f_xB, P.Nx, P.Ny, P.Nz);
     } else {
+        // recompute_host_xBtot_field (main_cuda.cu:19147-19170)
         for (size_t i = 0; i < N; ++i) {
-            const double h = h_of(f_phi[i]);
-            f_xBtot[i] = (1.0 - h) * f_xB[i] + h * P.v_B;
+            const double pc = std::min(std::max(f_phi[i], 0.0), 1.0);
+            const double h = h_of(pc);
+            const double x = std::min(std::max(f_xB[i], P.xB_eps), 1.0 - P.xB_eps);
+            if (gpc) {
+                const double he = h_of(std::min(std::max(f_eta[i], 0.0), 1.0));
+                f_xBtot[i] = (1.0 - h) * (1.0 - he) * x + (1.0 - h) * he * P.gp_xB_fixed + h;
+            } else {
+                f_xBtot[i] = (1.0 - h) * x + h;   // the host form adds h_beta alone
+            }
         }
-        write_vtk(case_dir + "/xBtot_0.vtk", "xB_tot", f_xBtot, P.Nx, P.Ny, P.Nz);
+        write_vtk(case_dir + xbt_stem + "_0.vtk", xbt_name, f_xBtot, P.Nx, P.Ny, P.Nz);
         if (gp) write_vtk(case_dir + "/xBtot_gp_init.vtk", "xBtot_gp", f_xBtot, P.Nx, P.Ny, P.Nz);
         write_vtk(case_dir + "/phi_init.vtk", "phi", f_phi, P.Nx, P.Ny, P.Nz);
         if (gp) write_vtk(case_dir + "/eta_init.vtk", "eta", f_eta, P.Nx, P.Ny, P.Nz);

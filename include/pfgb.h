@@ -81,6 +81,9 @@ enum { PFGB_MODE_DYNAMICS = 0, PFGB_MODE_MINIMIZE = 1 };
 enum { PFGB_Y_LAGGED_RHS = 0, PFGB_Y_STORAGE_EXACT = 1, PFGB_Y_X_TRANSPORT_SPLIT = 2, PFGB_Y_Q_TRANSPORT_SPLIT = 3 };
 enum { PFGB_COMPOSITION_LEGACY = 0, PFGB_COMPOSITION_CTOT = 1, PFGB_COMPOSITION_QALPHA = 2 };
 enum { PFGB_CONS_FLUX_PAIRWISE_LIMITED = 0, PFGB_CONS_FLUX_BACKWARD_EULER = 1 };
+/* gp_y_update_mode (gp_y_update_mode_code, main_cuda.cu:16786-16793) */
+enum { PFGB_GP_Y_OLD_RHS = 0, PFGB_GP_Y_PICARD_STORAGE = 1, PFGB_GP_Y_STORAGE_EXACT = 2, PFGB_GP_Y_CONSERVATIVE_RHS = 3 };
+enum { PFGB_GP_ETA_LIMITER_OFF = 0, PFGB_GP_ETA_LIMITER_LOCAL_CLIP = 1 };
 
 /*
  * Stiffness tensors are the 21 independent Voigt entries in the reference's
@@ -178,8 +181,10 @@ typedef struct pfgb_params {
     double pf_matrix_storage_floor;
     double pf_composition_stabilizer_Dalpha_multiplier;
     /* GP storage coupling switches (gp_storage_coupling_enabled,
-       main_cuda.cu:16767-16772; defaults 1 and 0).  The storage-coupled gp_zone
-       path is not built: pfgb_create refuses gp_zone with coupling on. */
+       main_cuda.cu:16767-16772; defaults 1 and 0): gp_zone with
+       gp_barrier_only_mode = 0 or enable_legacy_gp_storage_coupling = 1
+       conserves xBtot_gp = h_alpha x + h_GP gp_xB_fixed + h_beta; the Y
+       update then follows gp_y_update_mode and gp_eta_mass_limiter below. */
     int32_t gp_barrier_only_mode;
     int32_t enable_legacy_gp_storage_coupling;
     /* zero mode (PF_CONSERVED_Y_ZERO_MODE_V1) */
@@ -270,7 +275,31 @@ typedef struct pfgb_params {
     double pf_conservative_mass_tol;
     double pf_conservative_beta_support_eps;
     int32_t pf_conservative_max_subcycles;
-    int32_t pad_cons;
+    /* GP storage coupling (gp_zone dynamics with the coupling on,
+       main_cuda.cu:30449-30560, 30587-30628, 30734-30760, 30912-30952):
+       gp_y_update_mode PFGB_GP_Y_OLD_RHS (default; the semi-implicit Y update
+       with the GP storage source, compute_Y_rhs_gp_kernel,
+       cuda_kernels.cu:2361-2430, its h_alpha floored at gp_h_alpha_eps),
+       PFGB_GP_Y_CONSERVATIVE_RHS (the same without the floor,
+       compute_Y_rhs_gp_conservative_kernel, :2432-2527),
+       PFGB_GP_Y_STORAGE_EXACT (the point update of xBtot_gp solved for x,
+       gp_storage_exact_Y_update_kernel, :2746-2857) or
+       PFGB_GP_Y_PICARD_STORAGE (gp_y_picard_iters fixed-point sweeps of the
+       storage update, gp_picard_storage_Y_update_kernel, :3290-3370);
+       gp_eta_mass_limiter PFGB_GP_ETA_LIMITER_LOCAL_CLIP caps the GP
+       fraction where the recovered matrix composition would leave
+       [xB_eps, 1 - xB_eps] (gp_eta_feasibility_and_limiter_kernel,
+       :1151-1250), default off. */
+    int32_t gp_y_update_mode;
+    int32_t gp_eta_mass_limiter;
+    int32_t gp_y_picard_iters;
+    /* the composition of the mobility in the limiter's second flux: 0
+       (default) as the reference computes it, where the buffer of x^n
+       (d_xB_prev_r) is the buffer of div J (main_cuda.cu:27858) and so holds
+       the first pass's div J by then; 1 = x^n.  No counterpart key in the
+       reference. */
+    int32_t gp_limiter_flux_from_xn;
+    int32_t pad_gp;
     /* derived by pfgb_params_finalize (pfparams_refresh_thermo) */
     double temperature_K;
     double mu0_compound;
@@ -301,6 +330,10 @@ typedef struct pfgb_step_stats {
        bounds limited, and cells whose phi update the storage constrained */
     int32_t cons_limited_faces;
     int32_t cons_phase_constrained;
+    /* GP storage coupling with the local_clip limiter: cells whose eta the
+       limiter lowered (both limiter passes of the step) */
+    int32_t gp_eta_limited_cells;
+    int32_t pad_stats;
 } pfgb_step_stats;
 
 /* Minimize iteration statistics (energy_minimize.csv row and the stopping
@@ -340,7 +373,8 @@ typedef struct pfgb_case {
 /* Scalar diagnostics of the current state (CSV row, mass ledger). */
 typedef struct pfgb_diag {
     double vf_precip;      /* <h(phi)>, gpu_compute_vf_from_h            */
-    double mass_xBtot;     /* sum((1-h) xB + h v_B)                      */
+    double mass_xBtot;     /* sum((1-h) xB + h v_B); with the GP storage
+                              coupling sum(h_alpha xB + h_GP x_GP + h_beta) */
     double mean_xB;
     double phi_min, phi_max;
     double xB_min, xB_max;

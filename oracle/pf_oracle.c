@@ -241,6 +241,8 @@ struct pfo_state {
     /* fields */
     double *phi, *eta, *Y, *xB, *dYdt;
     double *phi_n, *eta_prev, *Y_n, *xB_prev;
+    double *xB_gp_old;      /* GP storage coupling: x^n of the feasibility pass */
+    double gp_mean_DY;      /* GP storage coupling: <DY> of the step */
     double *rhs, *mu, *scr, *divJ, *lapY, *mass_t, *der_t;
     double *q, *q_before;   /* q_transport_projection_split: matrix storage (1 - h) x */
     int q_rejected, q_redistributed;
@@ -298,7 +300,7 @@ pfo_state *pfo_create(const pfgb_params *pin) {
     const size_t rb = sizeof(double) * s->N, kb = sizeof(cpx) * s->Nk;
     double **rf_[] = {&s->phi, &s->eta, &s->Y, &s->xB, &s->dYdt, &s->phi_n, &s->eta_prev,
                       &s->Y_n, &s->xB_prev, &s->rhs, &s->mu, &s->scr, &s->divJ, &s->lapY,
-                      &s->mass_t, &s->der_t, &s->q, &s->q_before, &s->cstore};
+                      &s->mass_t, &s->der_t, &s->q, &s->q_before, &s->cstore, &s->xB_gp_old};
     for (size_t i = 0; i < sizeof(rf_) / sizeof(rf_[0]); ++i) *rf_[i] = (double *)xalloc(rb);
     cpx **kf_[] = {&s->phi_k, &s->rhs_k, &s->mu_k, &s->divJ_k, &s->Y_k, &s->scr_k, &s->eta_k};
     for (size_t i = 0; i < sizeof(kf_) / sizeof(kf_[0]); ++i) *kf_[i] = (cpx *)xalloc(kb);
@@ -347,7 +349,7 @@ void pfo_destroy(pfo_state *s) {
     if (!s) return;
     double *rr[] = {s->phi, s->eta, s->Y, s->xB, s->dYdt, s->phi_n, s->eta_prev, s->Y_n,
                     s->xB_prev, s->rhs, s->mu, s->scr, s->divJ, s->lapY, s->mass_t, s->der_t, s->q,
-                    s->q_before, s->cstore};
+                    s->q_before, s->cstore, s->xB_gp_old};
     for (size_t i = 0; i < sizeof(rr) / sizeof(rr[0]); ++i) free(rr[i]);
     cpx *kk[] = {s->phi_k, s->rhs_k, s->mu_k, s->divJ_k, s->Y_k, s->scr_k, s->eta_k};
     for (size_t i = 0; i < sizeof(kk) / sizeof(kk[0]); ++i) free(kk[i]);
@@ -1627,11 +1629,208 @@ static void mu_field(pfo_state *s, const double *phiY, const double *etaY) {
     RLOOP_END
 }
 
+/* ------------------------------------------------------------------ */
+/* GP storage coupling (gp_zone with gp_barrier_only_mode = 0 or       */
+/* enable_legacy_gp_storage_coupling = 1, gp_storage_coupling_enabled, */
+/* main_cuda.cu:16767-16772): the conserved composition is             */
+/* xBtot_gp = h_alpha x + h_GP x_GP + h_beta                           */
+/* ------------------------------------------------------------------ */
+static int gp_coupled(const pfo_state *s) {
+    return s->gp && (s->p.enable_legacy_gp_storage_coupling || !s->p.gp_barrier_only_mode);
+}
+
+/* phase_fractions_gp, phase_functions.h:27-42 (phi and eta as given) */
+static void o_gpfrac(double phi, double eta, double *ha, double *hg, double *hb) {
+    const double hp = o_h(phi), he = o_h(eta);
+    *hb = hp;
+    *hg = (1.0 - hp) * he;
+    *ha = (1.0 - hp) * (1.0 - he);
+}
+
+/* the matrix composition recovered from a storage target, and whether it
+ * lies in [x_min, x_max] (gp_recovered_xB_valid_device, cuda_kernels.cu:1100-1120) */
+static int gp_recovered_valid(double tot, double hb, double A, double hg, double xg, double xmin, double xmax,
+                              double eps_h, double *xr) {
+    if (!isfinite(tot) || !isfinite(hb) || !isfinite(A) || !isfinite(hg)) return 0;
+    if (A < 0.0) return 0;
+    if (hg < 0.0 || hg > A) return 0;
+    const double ha = A - hg;
+    if (!(ha >= eps_h)) return 0;
+    const double num = tot - hg * xg - hb;
+    if (!isfinite(num)) return 0;
+    const double x = num / ha;
+    if (!isfinite(x)) return 0;
+    if (xr) *xr = x;
+    return x >= xmin && x <= xmax;
+}
+
+/* the largest GP fraction in [0, min(h_GP, A)] whose recovered composition
+ * is valid, by 80 bisections (gp_limited_hGP_device, :1122-1149) */
+static double gp_limited_hgp(double tot, double hb, double A, double hg_tent, double xg, double xmin, double xmax,
+                             double eps_h) {
+    if (!isfinite(tot) || !isfinite(hb) || !isfinite(A) || !isfinite(hg_tent)) return 0.0;
+    const double hi0 = fmin(fmax(hg_tent, 0.0), fmax(A, 0.0));
+    double xr = 0.0;
+    if (gp_recovered_valid(tot, hb, A, hi0, xg, xmin, xmax, eps_h, &xr)) return hi0;
+    double lo = 0.0, hi = hi0;
+    for (int it = 0; it < 80; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (gp_recovered_valid(tot, hb, A, mid, xg, xmin, xmax, eps_h, &xr)) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+/* the eta feasibility check after the flux (gp_eta_feasibility_and_limiter_kernel,
+ * :1151-1250): eta clamped to [0, 1]; with the local_clip limiter, where the
+ * storage target xBtot_gp^n + dt divJ cannot be met by a matrix composition
+ * in [xB_eps, 1 - xB_eps] under the tentative GP fraction, the GP fraction is
+ * lowered to the largest feasible one and eta follows by inverting h.  x^n is
+ * the composition of Y^n (s->xB_gp_old).  Returns the limited cells. */
+static long long gp_eta_feasibility(pfo_state *s, double dt, int limiter) {
+    const pfgb_params *P = &s->p;
+    const double xmin = P->xB_eps, xmax = 1.0 - P->xB_eps, eps_h = P->gp_h_alpha_eps, xg = P->gp_xB_fixed;
+    long long limited = 0;
+#pragma omp parallel for schedule(static) reduction(+ : limited)
+    for (long long i = 0; i < (long long)s->N; ++i) {
+        const double et = o_clamp01(s->eta[i]);
+        const double pnew = o_clamp01(s->phi[i]), pold = o_clamp01(s->phi_n[i]);
+        const double xo = o_clamp_eps(s->xB_gp_old[i], xmin);
+        double hao, hgo, hbo;
+        o_gpfrac(pold, o_clamp01(s->eta_prev[i]), &hao, &hgo, &hbo);
+        const double hpn = o_h(pnew);
+        const double A = fmax(1.0 - hpn, 0.0);
+        const double hg_tent = A * o_h(et);
+        const double tot_old = xo + hgo * (xg - xo) + hbo * (1.0 - xo);
+        const double target = tot_old + dt * s->divJ[i];
+        double xr = 0.0;
+        const int valid = gp_recovered_valid(target, hpn, A, hg_tent, xg, xmin, xmax, eps_h, &xr);
+        double ef = et;
+        if (limiter && A > eps_h && hg_tent > 0.0 && !valid) {
+            const double hgf = gp_limited_hgp(target, hpn, A, hg_tent, xg, xmin, xmax, eps_h);
+            double allowed = o_clamp01(hgf / fmax(A, eps_h));
+            ef = h_inverse_bisect(allowed);
+            if (!isfinite(ef)) ef = 0.0;
+            ef = o_clamp01(ef);
+            if (fabs(et - ef) > 0.0) ++limited;
+        }
+        s->eta[i] = ef;
+    }
+    return limited;
+}
+
+/* the storage-consistent point updates of Y (gp_y_update_mode storage_exact,
+ * gp_storage_exact_Y_update_kernel :2746-2857, and picard_storage,
+ * gp_picard_storage_Y_update_kernel :3290-3370, repeated gp_y_picard_iters
+ * times from the guess Y^n); the fractions at (phi^n, eta^n) and
+ * (phi^{n+1}, eta^{n+1}); Y capped at +-Y_clip */
+static void gp_storage_update(pfo_state *s, double dt) {
+    const pfgb_params *P = &s->p;
+    const double eps = P->xB_eps, Yc = P->Y_clip, xg = P->gp_xB_fixed;
+    const int picard = P->gp_y_update_mode == PFGB_GP_Y_PICARD_STORAGE;
+    const int iters = P->gp_y_picard_iters > 0 ? P->gp_y_picard_iters : 1;
+    RLOOP_BEGIN(s)
+        double hao, hgo, hbo, han, hgn, hbn;
+        o_gpfrac(s->phi_n[idx], s->eta_prev[idx], &hao, &hgo, &hbo);
+        o_gpfrac(s->phi[idx], s->eta[idx], &han, &hgn, &hbn);
+        const double xo = o_sigmoid(s->Y_n[idx], Yc, eps);
+        const double So = hgo * (xg - xo) + hbo * (1.0 - xo);
+        if (!picard) {
+            const double target = xo + So + dt * s->divJ[idx];
+            if (!isfinite(target)) {
+                s->Y[idx] = s->Y_n[idx];
+                s->xB[idx] = xo;
+            } else {
+                double xu = xo;
+                if (!(han < P->gp_h_alpha_eps)) xu = (target - hgn * xg - hbn) / han;
+                if (!isfinite(xu)) xu = xo;
+                double xf = xu;
+                if (xf < eps) xf = eps;
+                if (xf > 1.0 - eps) xf = 1.0 - eps;
+                double y = o_logit(xf, eps, Yc);
+                if (y > Yc) y = Yc;
+                if (y < -Yc) y = -Yc;
+                s->Y[idx] = y;
+                s->xB[idx] = o_sigmoid(y, Yc, eps);
+            }
+        } else {
+            const int small = han < fmax(eps, 1.0e-8);
+            double yg = s->Y[idx];
+            for (int it = 0; it < iters; ++it) {
+                const double xgs = o_sigmoid(yg, Yc, eps);
+                double xu = xo;
+                if (!small) {
+                    const double Sg = hgn * (xg - xgs) + hbn * (1.0 - xgs);
+                    xu = xo + dt * (s->divJ[idx] - (Sg - So) / dt);
+                }
+                double xf = xu;
+                if (xf < eps) xf = eps;
+                if (xf > 1.0 - eps) xf = 1.0 - eps;
+                double y = o_logit(xf, eps, Yc);
+                if (y > Yc) y = Yc;
+                if (y < -Yc) y = -Yc;
+                yg = y;
+            }
+            s->Y[idx] = yg;
+            s->xB[idx] = o_sigmoid(yg, Yc, eps);
+        }
+    RLOOP_END
+}
+
+/* sum of h_alpha D_alpha x (1 - x) over the cells (reduce_sum_DY_gp_kernel,
+ * :3923-3955), the fractions at the given phi and eta */
+static double gp_sum_DY(pfo_state *s, const double *phiY, const double *etaY) {
+    const pfgb_params *P = &s->p;
+    RLOOP_BEGIN(s)
+        double ha, hg, hb;
+        o_gpfrac(phiY[idx], etaY[idx], &ha, &hg, &hb);
+        const double x = o_sigmoid(s->Y[idx], 20.0, 1e-12);
+        s->mass_t[idx] = ha * P->D_alpha * (x * (1.0 - x));
+    RLOOP_END
+    return dsum(s->mass_t, s->N);
+}
+
+/* test hooks (the pinning tests) for the GP storage coupling's functions;
+ * inputs are copied into the state, outputs read back */
+void pfo_test_gp_storage(pfo_state *s, double dt, const double *divJ, const double *phi_new, const double *phi_old,
+                         const double *eta_new, const double *eta_old, const double *Y_old, const double *Y_guess,
+                         double *Y, double *xB) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->divJ, divJ, b);
+    memcpy(s->phi, phi_new, b);
+    memcpy(s->phi_n, phi_old, b);
+    memcpy(s->eta, eta_new, b);
+    memcpy(s->eta_prev, eta_old, b);
+    memcpy(s->Y_n, Y_old, b);
+    memcpy(s->Y, Y_guess, b);
+    gp_storage_update(s, dt);
+    memcpy(Y, s->Y, b);
+    memcpy(xB, s->xB, b);
+}
+long long pfo_test_gp_eta_feasibility(pfo_state *s, double dt, int limiter, double *eta, const double *eta_old,
+                                      const double *phi_new, const double *phi_old, const double *xB_old,
+                                      const double *divJ) {
+    const size_t b = sizeof(double) * s->N;
+    memcpy(s->eta, eta, b);
+    memcpy(s->eta_prev, eta_old, b);
+    memcpy(s->phi, phi_new, b);
+    memcpy(s->phi_n, phi_old, b);
+    memcpy(s->xB_gp_old, xB_old, b);
+    memcpy(s->divJ, divJ, b);
+    const long long n = gp_eta_feasibility(s, dt, limiter);
+    memcpy(eta, s->eta, b);
+    return n;
+}
+double pfo_test_gp_sum_dy(pfo_state *s, const double *phiY, const double *etaY, const double *Y) {
+    memcpy(s->Y, Y, sizeof(double) * s->N);
+    return gp_sum_DY(s, phiY, etaY);
+}
+
 /* the lagged Y right-hand side (compute_Y_rhs_kernel, :2185-2266; zero mode:
  * compute_Y_rhs_sm_tangent_n_kernel, :2268-2359) from divJ, lapY and Y^n */
 static void y_rhs_field(pfo_state *s, double dt, double mean_DY) {
     pfgb_params *P = &s->p;
     const int zm = P->zero_mode_enabled;
+    const int gpc = gp_coupled(s);
     RLOOP_BEGIN(s)
         double Yv = s->Y[idx];
         double x = o_sigmoid_raw(Yv);
@@ -1640,7 +1839,21 @@ static void y_rhs_field(pfo_state *s, double dt, double mean_DY) {
         double ld = x * (1.0 - x);
         double dYdt = s->dYdt[idx];
         double f;
-        if (zm) {   /* compute_Y_rhs_sm_tangent_n_kernel, :2268-2359 */
+        if (gpc) {  /* compute_Y_rhs_gp_kernel :2361-2430 / _conservative_ :2432-2527 */
+            double han, hgn, hbn, hao, hgo, hbo;
+            o_gpfrac(s->phi[idx], s->eta[idx], &han, &hgn, &hbn);
+            o_gpfrac(s->phi_n[idx], s->eta_prev[idx], &hao, &hgo, &hbo);
+            const double dhg = (hgn - hgo) / dt, dhb = (hbn - hbo) / dt;
+            const double xs = o_sigmoid(Yv, 20.0, 1e-12);
+            const double q = xs * (1.0 - xs);
+            const double ss = dhg * (P->gp_xB_fixed - xs) + dhb * (1.0 - xs);
+            const double hx = P->enable_Y_rhs_previous_time_level ? hao : han;
+            const double gl = P->gp_y_update_mode == PFGB_GP_Y_CONSERVATIVE_RHS ? hx * q - 1.0
+                                                                             : fmax(hx, P->gp_h_alpha_eps) * q - 1.0;
+            const double tg = P->disable_Y_rhs_gamma_term ? 0.0 : gl * dYdt;
+            const double tl = mean_DY * s->lapY[idx];
+            f = s->divJ[idx] - ss - tl - tg;
+        } else if (zm) {   /* compute_Y_rhs_sm_tangent_n_kernel, :2268-2359 */
             double pn = s->phi_n[idx], pp = s->phi[idx];
             double hn = o_h(pn), hpn = o_hp(pn);
             double th = hpn * ((pp - pn) / dt) * (P->v_B - x);
@@ -1671,6 +1884,13 @@ void pfo_test_mu(pfo_state *s, const double *Y, const double *phiY, const double
     memcpy(xB, s->xB, b);
     memcpy(mu, s->mu, b);
 }
+void pfo_test_gp_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ, const double *phi_new,
+                       const double *phi_old, const double *eta_new, const double *eta_old, const double *lapY,
+                       const double *Y, const double *dYdt, double *out) {
+    memcpy(s->eta, eta_new, sizeof(double) * s->N);
+    memcpy(s->eta_prev, eta_old, sizeof(double) * s->N);
+    pfo_test_y_rhs(s, dt, mean_DY, divJ, phi_new, phi_old, lapY, Y, dYdt, out);
+}
 void pfo_test_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ, const double *phi_new,
                     const double *phi_old, const double *lapY, const double *Y, const double *dYdt, double *out) {
     const size_t b = sizeof(double) * s->N;
@@ -1684,22 +1904,11 @@ void pfo_test_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ,
     memcpy(out, s->rhs, b);
 }
 
-/* ------------------------------------------------------------------ */
-/* one dynamics step — main_cuda.cu:28427-31623                        */
-/* ------------------------------------------------------------------ */
-/* Y (composition) update and dY/dt history, main_cuda.cu:30280-30800 and
- * 31618-31623; fields at entry: phi = phi^{n+1}, phi_n = phi^n, Y = Y^n. */
-static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
-    pfgb_params *P = &s->p;
-    const int zm = P->zero_mode_enabled;
-    const int qm = P->pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT;
-    /* phi_for_Y_explicit, main_cuda.cu:30286-30291 */
-    const double *phiY = zm ? s->phi_n : (qm || !P->enable_Y_rhs_previous_time_level ? s->phi : s->phi_n);
-    const double *etaY = s->eta;
-    mu_field(s, phiY, etaY);
-    fwd(s, s->mu, s->mu_k); dealias(s, s->mu_k);
+/* divJ from the dealiased transform of mu in s->mu_k: per axis the
+ * gradient, the flux J_a = M d_a mu at the mobility of phiY, etaY and x^n,
+ * and the accumulated divergence (main_cuda.cu:30366-30440) */
+static void divj_field(pfo_state *s, const double *phiY, const double *etaY) {
     memset(s->divJ_k, 0, sizeof(cpx) * s->Nk);
-    memcpy(s->xB_prev, s->xB, sizeof(double) * s->N);
     for (int a = 0; a < 3; ++a) {
         KLOOP_BEGIN(s)   /* compute_gradient_single_component_k_kernel, :1887 */
             double ka = a == 0 ? s->kx[ii_] : (a == 1 ? s->ky[jj_] : s->kz[kk_]);
@@ -1721,6 +1930,52 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
     dealias(s, s->divJ_k);
     inv(s, s->divJ_k, s->divJ);
     RLOOP_BEGIN(s) s->divJ[idx] *= s->invN; RLOOP_END
+}
+
+/* ------------------------------------------------------------------ */
+/* one dynamics step — main_cuda.cu:28427-31623                        */
+/* ------------------------------------------------------------------ */
+/* Y (composition) update and dY/dt history, main_cuda.cu:30280-30800 and
+ * 31618-31623; fields at entry: phi = phi^{n+1}, phi_n = phi^n, Y = Y^n. */
+static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
+    pfgb_params *P = &s->p;
+    const int zm = P->zero_mode_enabled;
+    const int qm = P->pf_y_update_mode == PFGB_Y_Q_TRANSPORT_SPLIT;
+    /* phi_for_Y_explicit, main_cuda.cu:30286-30291 */
+    const double *phiY = zm ? s->phi_n : (qm || !P->enable_Y_rhs_previous_time_level ? s->phi : s->phi_n);
+    const double *etaY = s->eta;
+    const int gpc = gp_coupled(s);
+    mu_field(s, phiY, etaY);
+    fwd(s, s->mu, s->mu_k); dealias(s, s->mu_k);
+    memcpy(s->xB_prev, s->xB, sizeof(double) * s->N);
+    if (gpc) memcpy(s->xB_gp_old, s->xB, sizeof(double) * s->N);
+    divj_field(s, phiY, etaY);
+    if (gpc) {
+        /* main_cuda.cu:30449-30503: the feasibility pass; with the local_clip
+         * limiter the flux and divJ again with the limited eta, and the pass
+         * once more on them.  The reference keeps x^n for the mobility in the
+         * buffer of div J (d_xB_prev_r = d_divJ_r, main_cuda.cu:27858), so its
+         * second flux evaluates the mobility at the first pass's div J;
+         * gp_limiter_flux_from_xn = 1 takes x^n instead. */
+        const int lim = P->gp_eta_mass_limiter == PFGB_GP_ETA_LIMITER_LOCAL_CLIP;
+        long long nl = gp_eta_feasibility(s, dt, lim);
+        if (lim) {
+            if (!P->gp_limiter_flux_from_xn) memcpy(s->xB_prev, s->divJ, sizeof(double) * s->N);
+            divj_field(s, phiY, etaY);
+            nl += gp_eta_feasibility(s, dt, lim);
+        }
+        if (st) st->gp_eta_limited_cells = (int32_t)nl;
+        /* eta_for_Y_explicit, main_cuda.cu:30292; global_sum_DY, :30587-30591 */
+        const double *etaD = P->enable_Y_rhs_previous_time_level ? s->eta_prev : s->eta;
+        const double mean_gp = gp_sum_DY(s, phiY, etaD) / (double)s->N;
+        if (P->gp_y_update_mode == PFGB_GP_Y_STORAGE_EXACT || P->gp_y_update_mode == PFGB_GP_Y_PICARD_STORAGE) {
+            gp_storage_update(s, dt);   /* main_cuda.cu:30927-30951 */
+            RLOOP_BEGIN(s) s->dYdt[idx] = (s->Y[idx] - s->Y_n[idx]) / dt; RLOOP_END
+            if (st) st->mean_DY = mean_gp;
+            return PFGB_OK;
+        }
+        s->gp_mean_DY = mean_gp;
+    }
     if (P->pf_y_update_mode == PFGB_Y_STORAGE_EXACT) {
         /* two_phase_storage_exact_Y_update_kernel, cuda_kernels.cu:2859-2921:
          * C^n + dt divJ solved for x_alpha with h^{n+1}; x^n kept where the
@@ -1785,7 +2040,7 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
     dealias(s, s->Y_k);
     inv(s, s->Y_k, s->lapY);
     RLOOP_BEGIN(s) s->lapY[idx] *= s->invN; RLOOP_END
-    /* mean_DY, reduce_sum_DY_kernel :3870 */
+    /* mean_DY, reduce_sum_DY_kernel :3870 (GP coupling: reduce_sum_DY_gp_kernel) */
     RLOOP_BEGIN(s)
         double h = o_h(phiY[idx]);
         double Dm = o_Dmix(h, P->D_alpha, P->D_compound);
@@ -1794,7 +2049,7 @@ static int y_update(pfo_state *s, pfgb_step_stats *st, double dt) {
         if (x > 1.0 - 1e-12) x = 1.0 - 1e-12;
         s->mass_t[idx] = Dm * x * (1.0 - x);
     RLOOP_END
-    const double mean_DY = dsum(s->mass_t, s->N) / (double)s->N;
+    const double mean_DY = gpc ? s->gp_mean_DY : dsum(s->mass_t, s->N) / (double)s->N;
     if (st) st->mean_DY = mean_DY;
     /* Y^n in k space (stored in divJ_k like the reference) */
     fwd(s, s->Y_n, s->divJ_k); dealias(s, s->divJ_k);
@@ -2279,7 +2534,13 @@ int pfo_diagnostics(const pfo_state *s, pfgb_diag *d) {
         double h = o_h(o_clamp01(s->phi[i]));
         t[i] = h;
         double hh = o_h(s->phi[i]);
-        u[i] = (1.0 - hh) * s->xB[i] + P->v_B * hh;
+        if (gp_coupled(s)) {   /* reduce_sum_xBtot_gp_kernel, cuda_kernels.cu:3830-3860 */
+            double ha, hg, hb;
+            o_gpfrac(s->phi[i], s->eta[i], &ha, &hg, &hb);
+            u[i] = ha * s->xB[i] + hg * P->gp_xB_fixed + hb;
+        } else {
+            u[i] = (1.0 - hh) * s->xB[i] + P->v_B * hh;
+        }
         /* reduce_sum_N_in_N_if_kernel, cuda_kernels.cu:3746-3786 */
         w[i] = s->phi[i] > 0.5 ? 1.0 : 0.0;
         f[i] = (s->phi[i] > 0.12 && s->phi[i] < 0.88) ? 1.0 : 0.0;

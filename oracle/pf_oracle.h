@@ -14,10 +14,13 @@
  * Parity pinning: the thermodynamics and phase functions are checked against
  * the reference's own thermo_utils.h / phase_functions.h compiled on the
  * host (oracle/build_ref.sh -> oracle/_ref/libpfref.so) and against golden
- * vectors generated from them (tests/golden/).  The step as a whole is pinned
- * by known-answer tests (Fourier-mode decay, homogeneous Eshelby field,
- * exact mass conservation); the reference has no CPU time step and ships no
- * golden fields, so whole-step parity with main_cuda itself is unpinned.
+ * vectors generated from them (tests/golden/), and the per-cell kernels of
+ * the step against the reference's own cuda_kernels.cu built for the host
+ * (oracle/ref_kernels.cpp -> oracle/_ref/librefk.so).  The step as a whole
+ * is pinned by known-answer tests (Fourier-mode decay, homogeneous Eshelby
+ * field, exact mass conservation) and, through the CUDA library it checks,
+ * against the reference main_cuda rebuilt from its sources
+ * (tests/test_ref_main_parity.py).
  */
 #ifndef PF_ORACLE_H
 #define PF_ORACLE_H
@@ -70,6 +73,19 @@ void pfo_test_storage_exact(pfo_state *s, double dt, const double *divJ, const d
                             const double *phi_old, const double *Y_old, double *Y, double *xB);
 void pfo_test_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ, const double *phi_new,
                     const double *phi_old, const double *lapY, const double *Y, const double *dYdt, double *out);
+/* GP storage coupling: the right-hand side with the GP storage source, the
+ * storage point updates (Y_guess the Picard start), the eta feasibility pass
+ * (returns the limited cells) and the <DY> sum */
+void pfo_test_gp_y_rhs(pfo_state *s, double dt, double mean_DY, const double *divJ, const double *phi_new,
+                       const double *phi_old, const double *eta_new, const double *eta_old, const double *lapY,
+                       const double *Y, const double *dYdt, double *out);
+void pfo_test_gp_storage(pfo_state *s, double dt, const double *divJ, const double *phi_new, const double *phi_old,
+                         const double *eta_new, const double *eta_old, const double *Y_old, const double *Y_guess,
+                         double *Y, double *xB);
+long long pfo_test_gp_eta_feasibility(pfo_state *s, double dt, int limiter, double *eta, const double *eta_old,
+                                      const double *phi_new, const double *phi_old, const double *xB_old,
+                                      const double *divJ);
+double pfo_test_gp_sum_dy(pfo_state *s, const double *phiY, const double *etaY, const double *Y);
 /* minimize iterations (mode = minimize, full model, two_phase, zero mode off) */
 int pfo_minimize(pfo_state *s, int max_iter, int stop_on_convergence, pfgb_min_stats *stats);
 int pfo_read_fields(const pfo_state *s, double *phi, double *xB, double *Y,

@@ -275,6 +275,58 @@ void refk_cons_constrain(double *phi_new, const double *phi_old, double *storage
 }
 
 // dealias_23_kernel on a half spectrum of an Nx x Ny x Nz grid, in place
+// GP storage coupling.  compute_Y_rhs_gp_kernel (conservative = 0) or
+// compute_Y_rhs_gp_conservative_kernel (1) over n cells.  d: dt, gp_xB_fixed,
+// mean_DY, gp_h_alpha_eps; i: use_previous_time_level, disable_gamma_term.
+void refk_gp_y_rhs(int conservative, const double *divJ, const double *phi, const double *phi_prev,
+                   const double *eta, const double *eta_prev, const double *lapY, const double *Y,
+                   const double *dYdt, double *rhs, int n, const double *d, const int *i) {
+    if (conservative)
+        REF_LAUNCH(n, compute_Y_rhs_gp_conservative_kernel(divJ, phi, phi_prev, eta, eta_prev, lapY, Y, dYdt, rhs,
+                                                           d[0], d[1], d[2], n, i[0], i[1], nullptr));
+    else
+        REF_LAUNCH(n, compute_Y_rhs_gp_kernel(divJ, phi, phi_prev, eta, eta_prev, lapY, Y, dYdt, rhs, d[0], d[1],
+                                              d[2], d[3], n, i[0], i[1], nullptr));
+}
+
+// gp_storage_exact_Y_update_kernel (picard = 0) or iters sweeps of
+// gp_picard_storage_Y_update_kernel (Y holds the guess on entry).  d: dt,
+// gp_xB_fixed, Y_clip, Y_upper_cap, xB_eps, gp_h_alpha_eps.
+void refk_gp_storage(int picard, int iters, const double *divJ, const double *phi_new, const double *phi_old,
+                     const double *eta_new, const double *eta_old, const double *Y_old, double *Y, double *xB,
+                     int n, const double *d) {
+    if (!picard) {
+        REF_LAUNCH(n, gp_storage_exact_Y_update_kernel(divJ, phi_new, phi_old, eta_new, eta_old, Y_old, Y, xB,
+                                                       d[0], d[1], d[2], d[3], d[4], d[5], 0, nullptr, n));
+        return;
+    }
+    for (int it = 0; it < iters; ++it)
+        REF_LAUNCH(n, gp_picard_storage_Y_update_kernel(divJ, phi_new, phi_old, eta_new, eta_old, Y_old, Y, xB,
+                                                        d[0], d[1], d[2], d[3], d[4], nullptr, n));
+}
+
+// gp_eta_feasibility_and_limiter_kernel over n cells (eta in place); the
+// limited-cell count is returned.  d: dt, gp_xB_fixed, xB_min, xB_max,
+// gp_h_alpha_eps.
+double refk_gp_eta_feasibility(double *eta, const double *eta_old, const double *phi_new, const double *phi_old,
+                               const double *xB_old, const double *divJ, int limiter, int n, const double *d) {
+    double stats[GP_ETA_FEAS_STATS_COUNT] = {0.0};
+    REF_LAUNCH(n, gp_eta_feasibility_and_limiter_kernel(eta, eta_old, phi_new, phi_old, xB_old, divJ, d[0], d[1],
+                                                        d[2], d[3], d[4], limiter, stats, n));
+    return stats[GP_ETA_FEAS_LIMITER_COUNT];
+}
+
+// reduce_sum_DY_gp_kernel with one-thread blocks: the per-cell terms
+// h_alpha D_alpha x (1 - x) in out
+void refk_gp_dy_terms(const double *Y, const double *phi, const double *eta, double *out, double D_alpha, int n) {
+    REF_LAUNCH(n, reduce_sum_DY_gp_kernel(Y, phi, eta, out, D_alpha, n));
+}
+
+// reduce_sum_xBtot_gp_kernel with one-thread blocks: the per-cell xBtot_gp
+void refk_gp_xbtot_terms(const double *phi, const double *eta, const double *xB, double *out, double xgp, int n) {
+    REF_LAUNCH(n, reduce_sum_xBtot_gp_kernel(phi, eta, xB, out, xgp, n));
+}
+
 void refk_dealias(cuDoubleComplex *k, int Nx, int Ny, int Nz, double dx, double dy, double dz) {
     const int NzC = Nz / 2 + 1, nk = Nx * Ny * NzC;
     REF_LAUNCH(nk, dealias_23_kernel(k, Nx, Ny, Nz, NzC, dx, dy, dz, nk));

@@ -95,7 +95,19 @@ def test_gp_storage_coupling_keys(capi, tmp_path):
     base = open(os.path.join(GOLDEN, "c2.params")).read()
     p = capi.load_params_file(_write(tmp_path, base + "\ngp_barrier_only_mode = 0\n"))
     assert p.gp_barrier_only_mode == 0 and p.enable_legacy_gp_storage_coupling == 0
-    assert capi.default_params().gp_barrier_only_mode == 1
+    d = capi.default_params()
+    assert d.gp_barrier_only_mode == 1
+    assert (d.gp_y_update_mode, d.gp_eta_mass_limiter, d.gp_y_picard_iters) == (capi.GP_Y_OLD_RHS,
+                                                                                capi.GP_ETA_LIMITER_OFF, 3)
+    for text, mode in (("old_rhs", capi.GP_Y_OLD_RHS), ("conservative_y_rhs", capi.GP_Y_CONSERVATIVE_RHS),
+                       ("picard_storage", capi.GP_Y_PICARD_STORAGE), ("storage_exact", capi.GP_Y_STORAGE_EXACT)):
+        p = capi.load_params_file(_write(tmp_path, base + "\ngp_y_update_mode = %s\n"
+                                         "gp_eta_mass_limiter = local_clip\ngp_y_picard_iters = 5\n" % text))
+        assert (p.gp_y_update_mode, p.gp_eta_mass_limiter, p.gp_y_picard_iters) == (mode,
+                                                                                    capi.GP_ETA_LIMITER_LOCAL_CLIP, 5)
+    for line in ("gp_y_update_mode = explicit", "gp_eta_mass_limiter = hard"):
+        with pytest.raises(capi.PfgbError):
+            capi.load_params_file(_write(tmp_path, base + "\n" + line + "\n"))
 
 
 def test_y_update_mode_key(capi, tmp_path):
@@ -165,8 +177,10 @@ def test_create_rejects_bad_grid_without_touching_gpu(capi):
     assert capi.load().pfgb_create(ctypes.byref(p), 0, ctypes.byref(ctx)) == 1
 
 
-@pytest.mark.parametrize("over", [dict(model_mode=1, gp_barrier_only_mode=0),
-                                  dict(model_mode=1, enable_legacy_gp_storage_coupling=1),
+@pytest.mark.parametrize("over", [dict(model_mode=1, gp_barrier_only_mode=0, mode=1),
+                                  dict(model_mode=1, enable_legacy_gp_storage_coupling=1, mode=1),
+                                  dict(model_mode=1, gp_barrier_only_mode=0, gp_y_update_mode=4),
+                                  dict(model_mode=1, gp_barrier_only_mode=0, gp_eta_mass_limiter=2),
                                   dict(pf_y_update_mode=1, zero_mode_enabled=1),
                                   dict(pf_y_update_mode=2, mode=1),
                                   dict(pf_y_update_mode=2, pf_matrix_storage_floor=0.0),

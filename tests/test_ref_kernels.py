@@ -517,3 +517,145 @@ def test_conservative_functions_match_reference_kernels(capi, ctot):
     assert np.abs(gst - rst).max() <= 1e-15
     assert np.abs(gx2 - rx2).max() <= 1e-15
     assert np.abs(gY2 - rY2).max() <= 1e-12 * np.abs(rY2).max()
+
+
+@pytest.mark.parametrize("mode", ["old_rhs", "conservative_y_rhs"])
+def test_gp_coupled_y_rhs_matches_reference_kernel(capi, mode):
+    """The GP storage-coupled Y right-hand side (GP and beta storage source,
+    the gamma term with h_alpha floored at gp_h_alpha_eps in old_rhs, not in
+    conservative_y_rhs), both time levels of the gamma term, and the <DY>
+    terms h_alpha D_alpha x (1 - x)."""
+    L = _refk()
+    L.refk_gp_y_rhs.argtypes = [ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int, dp, ip]
+    L.refk_gp_dy_terms.argtypes = [dp, dp, dp, dp, ctypes.c_double, ctypes.c_int]
+    n = 8
+    N = n ** 3
+    rng = np.random.default_rng(151)
+    cons = mode == "conservative_y_rhs"
+    for prev in (0, 1):
+        p = params_for(capi, "c2.params", n=n, model_mode=1, gp_barrier_only_mode=0,
+                       gp_y_update_mode=capi.GP_Y_CONSERVATIVE_RHS if cons else capi.GP_Y_OLD_RHS,
+                       enable_Y_rhs_previous_time_level=prev)
+        phi = rng.uniform(-1e-6, 1.0, N)
+        phi_old = np.clip(phi + rng.normal(0.0, 0.05, N), 0.0, 1.0)
+        eta = rng.uniform(0.0, 1.0, N)
+        eta[:40] = 1.0                 # no matrix left: the h_alpha floor acts
+        eta_old = np.clip(eta + rng.normal(0.0, 0.05, N), 0.0, 1.0)
+        Y = rng.uniform(-25.0, 5.0, N)  # beyond the clip at 20 of the source
+        lap = rng.normal(0.0, 3.0, N)
+        divJ = rng.normal(0.0, 2.0, N)
+        dYdt = rng.normal(0.0, 5.0, N)
+        mdy = 0.37
+        ref = np.zeros(N)
+        d = np.array([p.dt, p.gp_xB_fixed, mdy, p.gp_h_alpha_eps])
+        iv = (ctypes.c_int * 2)(prev, p.disable_Y_rhs_gamma_term)
+        L.refk_gp_y_rhs(int(cons), _ptr(divJ), _ptr(phi), _ptr(phi_old), _ptr(eta), _ptr(eta_old), _ptr(lap),
+                        _ptr(Y), _ptr(dYdt), _ptr(ref), N, _ptr(d), iv)
+        o = _oracle_state(capi, p)
+        o.L.pfo_test_gp_y_rhs.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double] + [dp] * 9
+        got = np.zeros(N)
+        o.L.pfo_test_gp_y_rhs(o.s, p.dt, mdy, _ptr(divJ), _ptr(phi), _ptr(phi_old), _ptr(eta), _ptr(eta_old),
+                              _ptr(lap), _ptr(Y), _ptr(dYdt), _ptr(got))
+        assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max(), (mode, prev)
+        # <DY>: the per-cell terms of the reference's reduction, summed
+        terms = np.zeros(N)
+        L.refk_gp_dy_terms(_ptr(Y), _ptr(phi), _ptr(eta), _ptr(terms), p.D_alpha, N)
+        o.L.pfo_test_gp_sum_dy.restype = ctypes.c_double
+        o.L.pfo_test_gp_sum_dy.argtypes = [ctypes.c_void_p, dp, dp, dp]
+        s = o.L.pfo_test_gp_sum_dy(o.s, _ptr(phi), _ptr(eta), _ptr(Y))
+        assert abs(s - terms.sum()) <= 1e-13 * abs(terms.sum())
+
+
+@pytest.mark.parametrize("mode", ["storage_exact", "picard_storage"])
+def test_gp_storage_update_matches_reference_kernel(capi, mode):
+    """The GP storage point updates of Y: storage_exact (cells without matrix,
+    non-finite and out-of-range solutions, the clip) and three Picard sweeps
+    of picard_storage from the guess Y^n."""
+    L = _refk()
+    L.refk_gp_storage.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int, dp]
+    n = 8
+    N = n ** 3
+    pic = mode == "picard_storage"
+    p = params_for(capi, "c2.params", n=n, model_mode=1, gp_barrier_only_mode=0,
+                   gp_y_update_mode=capi.GP_Y_PICARD_STORAGE if pic else capi.GP_Y_STORAGE_EXACT)
+    rng = np.random.default_rng(161 + pic)
+    phi_new = rng.uniform(0.0, 1.0, N)
+    phi_old = np.clip(phi_new + rng.normal(0.0, 0.05, N), 0.0, 1.0)
+    eta_new = rng.uniform(0.0, 1.0, N)
+    eta_old = np.clip(eta_new + rng.normal(0.0, 0.05, N), 0.0, 1.0)
+    phi_new[:20] = 1.0                      # no matrix storage left
+    Y_old = rng.uniform(-6.0, 0.5, N)
+    divJ = rng.normal(0.0, 2.0, N)
+    divJ[20] = np.inf                        # non-finite target: Y^n kept
+    d = np.array([p.dt, p.gp_xB_fixed, p.Y_clip, p.Y_clip, p.xB_eps, p.gp_h_alpha_eps])
+    rY, rx = Y_old.copy(), np.zeros(N)
+    L.refk_gp_storage(int(pic), p.gp_y_picard_iters, _ptr(divJ), _ptr(phi_new), _ptr(phi_old), _ptr(eta_new),
+                      _ptr(eta_old), _ptr(Y_old), _ptr(rY), _ptr(rx), N, _ptr(d))
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_gp_storage.argtypes = [ctypes.c_void_p, ctypes.c_double] + [dp] * 9
+    gY, gx = np.zeros(N), np.zeros(N)
+    o.L.pfo_test_gp_storage(o.s, p.dt, _ptr(divJ), _ptr(phi_new), _ptr(phi_old), _ptr(eta_new), _ptr(eta_old),
+                            _ptr(Y_old), _ptr(Y_old), _ptr(gY), _ptr(gx))
+    fin = np.isfinite(rY)
+    assert fin.all() and np.isfinite(gY).all()
+    assert np.abs(gY - rY).max() <= 1e-12 * np.abs(rY).max(), mode
+    assert np.abs(gx - rx).max() <= 1e-14
+    assert (np.abs(gY - Y_old) < 1e-12).sum() >= 1 and (np.abs(gY - Y_old) > 1e-6).sum() > N // 2
+
+
+def test_gp_eta_feasibility_matches_reference_kernel(capi):
+    """The eta feasibility pass: eta clamped to [0, 1] without the limiter;
+    with local_clip the GP fraction lowered (bisection on h_GP, eta by
+    inverting h) where the storage target admits no matrix composition in
+    [xB_eps, 1 - xB_eps]; the limited-cell count."""
+    L = _refk()
+    L.refk_gp_eta_feasibility.restype = ctypes.c_double
+    L.refk_gp_eta_feasibility.argtypes = [dp, dp, dp, dp, dp, dp, ctypes.c_int, ctypes.c_int, dp]
+    n = 8
+    N = n ** 3
+    p = params_for(capi, "c2.params", n=n, model_mode=1, gp_barrier_only_mode=0,
+                   gp_eta_mass_limiter=capi.GP_ETA_LIMITER_LOCAL_CLIP)
+    rng = np.random.default_rng(171)
+    eta_old = rng.uniform(0.0, 1.0, N)
+    eta = np.clip(eta_old + rng.normal(0.0, 0.3, N), -0.1, 1.1)
+    phi_old = rng.uniform(0.0, 1.0, N)
+    phi_new = np.clip(phi_old + rng.normal(0.0, 0.05, N), 0.0, 1.0)
+    xB_old = rng.uniform(1e-4, 0.2, N)
+    divJ = rng.normal(0.0, 50.0, N)
+    d = np.array([p.dt, p.gp_xB_fixed, p.xB_eps, 1.0 - p.xB_eps, p.gp_h_alpha_eps])
+    o = _oracle_state(capi, p)
+    o.L.pfo_test_gp_eta_feasibility.restype = ctypes.c_longlong
+    o.L.pfo_test_gp_eta_feasibility.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int] + [dp] * 6
+    for lim in (0, 1):
+        re, ge = eta.copy(), eta.copy()
+        nr = L.refk_gp_eta_feasibility(_ptr(re), _ptr(eta_old), _ptr(phi_new), _ptr(phi_old), _ptr(xB_old),
+                                       _ptr(divJ), lim, N, _ptr(d))
+        ng = o.L.pfo_test_gp_eta_feasibility(o.s, p.dt, lim, _ptr(ge), _ptr(eta_old), _ptr(phi_new),
+                                             _ptr(phi_old), _ptr(xB_old), _ptr(divJ))
+        assert int(nr) == ng
+        assert np.array_equal(re, ge), lim
+        if lim:
+            assert ng > 10
+        else:
+            assert ng == 0 and np.array_equal(ge, np.clip(eta, 0.0, 1.0))
+
+
+def test_gp_xbtot_matches_reference_kernel(capi):
+    """The coupled mass ledger xBtot_gp = h_alpha x + h_GP x_GP + h_beta of
+    the diagnostics against the reference's reduction terms."""
+    L = _refk()
+    L.refk_gp_xbtot_terms.argtypes = [dp, dp, dp, dp, ctypes.c_double, ctypes.c_int]
+    n = 8
+    N = n ** 3
+    p = params_for(capi, "c2.params", n=n, model_mode=1, gp_barrier_only_mode=0)
+    rng = np.random.default_rng(181)
+    phi = rng.uniform(0.0, 1.0, N)
+    eta = rng.uniform(0.0, 1.0, N)
+    xB = rng.uniform(1e-3, 0.3, N)
+    terms = np.zeros(N)
+    L.refk_gp_xbtot_terms(_ptr(phi), _ptr(eta), _ptr(xB), _ptr(terms), p.gp_xB_fixed, N)
+    o = _oracle_state(capi, p)
+    o.load(phi, xB, eta)
+    dg = o.diagnostics(capi.Diag)
+    # the oracle's xB is the clipped sigmoid of the loaded logit: xB to rounding
+    assert abs(dg.mass_xBtot - terms.sum()) <= 1e-12 * terms.sum()
