@@ -77,6 +77,9 @@ def parse():
     ap.add_argument("--sweep-cases", type=int, default=48)
     ap.add_argument("--sweep-iters", type=int, default=500)
     ap.add_argument("--sweep-concurrency", type=int, default=8)
+    ap.add_argument("--sweep-autotune", type=int, default=0, choices=[0, 1],
+                    help="tile autotuner of the generic engine (fft_autotune) in the sweep; the rule's tiles are "
+                         "within 3%% of the tuned ones under the sweep's sharing, and tuning costs about 4 s")
     return ap.parse_args()
 
 
@@ -603,6 +606,7 @@ def run_sweep(args):
         p.minimize_dt = 0.05
         p.minimize_V0 = 0.1
         p.precision = capi.PREC_FP32
+        p.fft_autotune = args.sweep_autotune
         for k in range(6):
             p.eps00[k] = c["eps00"][k]
         capi.finalize(p)
@@ -631,6 +635,7 @@ def run_sweep(args):
             "config": {"workload": f"{len(specs)} minimize cases, grids 64^3-160^3, sphere/oblate seeds, "
                                    f"8 eigenstrain rotations, {args.sweep_iters} iterations, dt 0.05, V0 0.1, "
                                    f"full model", "concurrency": args.sweep_concurrency,
+                       "fft_autotune": args.sweep_autotune,
                        "l2": "per-case working sets 0.2-1 GB, above L2"},
             "e2e": {"value": v, "unit": "cell-iterations/s",
                     "h2d_bytes_per_step": 2 * 8 * sum(c["n"] ** 3 for c in specs) / args.sweep_iters,
@@ -639,6 +644,7 @@ def run_sweep(args):
                             "one call, so this equals value"},
             "cases_ok": ok, "status": rc,
             "case_seconds": [round(arr[i].seconds, 3) for i in range(len(specs))],
+            "tiles": capi.tile_report().splitlines() if args.sweep_autotune else [],
             "roofline": None, "cpu_baseline": None}
     print(json.dumps(line), flush=True)
 

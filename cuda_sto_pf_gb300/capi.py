@@ -52,7 +52,7 @@ class Params(Structure):
         ("elastic_residual_control_enabled", c_int32), ("elastic_iter_min", c_int32),
         ("elastic_iter_max", c_int32), ("elastic_fail_on_nonconvergence", c_int32),
         ("elastic_increment_form", c_int32), ("elastic_warm_start_extrapolate", c_int32),
-        ("elastic_chebyshev", c_int32), ("fft_tensor_cores", c_int32),
+        ("elastic_chebyshev", c_int32), ("fft_tensor_cores", c_int32), ("fft_autotune", c_int32), ("pad_fft", c_int32),
         ("elastic_residual_tolerance", c_double), ("elastic_residual_absolute_floor", c_double),
         ("eps_iso_over_vB", c_double),
         ("eps00", c_double * 6), ("E0", c_double * 6),
@@ -205,6 +205,8 @@ EXPORTS = [
     ("pfgb_fft3d_c2r", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     ("pfgb_fft3d_r2c_noalloc", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     ("pfgb_fft_y246x6", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
+    ("pfgb_tile_report", ctypes.c_size_t, [ctypes.c_char_p, ctypes.c_size_t]),
+    ("pfgb_set_tune_copies", None, [c_int]),
     ("pfgb_fnv1a64", ctypes.c_uint64, [c_void_p, c_size_t, ctypes.c_uint64]),
     ("pfgb_parameter_fingerprint", ctypes.c_uint64, [POINTER(Params)]),
     ("pfgb_elastic_solver_fingerprint", ctypes.c_uint64, [POINTER(Params)]),
@@ -280,6 +282,15 @@ def default_params() -> Params:
     p = Params()
     load().pfgb_params_default(ctypes.byref(p))
     return p
+
+
+def tile_report() -> str:
+    """The generic engine's autotuned tiles in this process (fft_autotune)."""
+    L = load()
+    n = L.pfgb_tile_report(None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    L.pfgb_tile_report(buf, n + 1)
+    return buf.value.decode()
 
 
 def load_params_file(path: str, p: Params | None = None) -> Params:

@@ -37,10 +37,40 @@ pfgb_status run_case(pfgb_case *cs, int device) {
     return st;
 }
 
+// with fft_autotune, one iteration of the first case of each distinct grid
+// on this thread before the pool starts: the tiles are then timed on an
+// otherwise idle device, and the cases find them chosen
+void pretune(pfgb_case *cases, int ncases, int device) {
+    std::vector<int> seen;
+    for (int i = 0; i < ncases; ++i) {
+        const pfgb_params &p = cases[i].params;
+        if (!p.fft_autotune) continue;
+        const int key[5] = {p.Nx, p.Ny, p.Nz, p.precision, p.model_mode};
+        bool dup = false;
+        for (size_t j = 0; j + 5 <= seen.size() && !dup; j += 5)
+            dup = !memcmp(&seen[j], key, sizeof(key));
+        if (dup) continue;
+        seen.insert(seen.end(), key, key + 5);
+        pfgb_ctx *ctx = nullptr;
+        if (pfgb_create(&p, device, &ctx) != PFGB_OK) continue;
+        if (pfgb_load_fields(ctx, cases[i].phi, cases[i].xB, cases[i].eta, nullptr) == PFGB_OK) {
+            pfgb_min_stats st;
+            pfgb_minimize(ctx, 1, 0, &st);
+            pfgb_sync(ctx);
+        }
+        pfgb_destroy(ctx);
+    }
+}
+
 }  // namespace
 
 extern "C" pfgb_status pfgb_batch_minimize(pfgb_case *cases, int ncases, int device, int concurrency) {
     if (!cases || ncases < 0 || concurrency < 1) return PFGB_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return PFGB_ERR_CUDA;
+    const int nt0 = concurrency < ncases ? concurrency : (ncases > 0 ? ncases : 1);
+    pfgb_set_tune_copies(nt0);   // the tiles are chosen for nt0 cases sharing the device
+    pretune(cases, ncases, device);
+    pfgb_set_tune_copies(1);
     std::atomic<int> next(0);
     auto worker = [&]() {
         if (cudaSetDevice(device) != cudaSuccess) return;

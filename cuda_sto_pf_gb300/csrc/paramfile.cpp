@@ -106,6 +106,7 @@ const DKey kInts[] = {
     DK("elastic_warm_start_extrapolate", elastic_warm_start_extrapolate),
     DK("elastic_warm_start_source", elastic_warm_start_source),
     DK("elastic_chebyshev", elastic_chebyshev), DK("fft_tensor_cores", fft_tensor_cores),
+    DK("fft_autotune", fft_autotune),
     DK("zero_mode_fp64_cells", zero_mode_fp64_cells),
     DK("pf_conservative_max_subcycles", pf_conservative_max_subcycles),
     DK("gp_y_picard_iters", gp_y_picard_iters), DK("gp_limiter_flux_from_xn", gp_limiter_flux_from_xn),

@@ -228,6 +228,245 @@ static const cplx_t<T> *twp(const pfgb_ctx *c, int axis) {
     return (const cplx_t<T> *)c->tw[sizeof(T) == 8 ? 0 : 1][axis];
 }
 
+// ---------------------------------------------------------------------------
+// tile autotuner of the generic engine (fft_autotune = 1): the columns per
+// block of an x or y pass (TK, a power of two) and the rows per block of a z
+// pass (R) are timed over their candidates on first use, and the fastest is
+// kept per kernel, grid shape and device for the life of the process (a
+// sweep of many cases tunes each grid size once).  An axis pass is timed as
+// itself on scratch arrays (its ops are pure functions of their inputs); a
+// z pass, whose ops write the step's fields, through a copy op with the
+// same field counts.  Two threads may tune the same key at once; the first
+// result stored stands.  pfgb_batch_minimize tunes each distinct grid on
+// one thread before its workers start, on an otherwise idle device.
+// ---------------------------------------------------------------------------
+struct TileKey {
+    int dev;
+    const void *kern;
+    long long a, b, c;
+    bool operator<(const TileKey &o) const {
+        if (dev != o.dev) return dev < o.dev;
+        if (kern != o.kern) return kern < o.kern;
+        if (a != o.a) return a < o.a;
+        if (b != o.b) return b < o.b;
+        return c < o.c;
+    }
+};
+struct TileRec { int tile, rule; float t_ms, t_rule_ms; std::string tag; long long a, b, c; };
+static std::mutex g_tile_mu;
+static std::map<TileKey, TileRec> g_tiles;
+
+// zeroed scratch arrays of `bytes` each, stream-ordered (no device-wide
+// synchronisation while other contexts run), freed with the object
+struct TuneScratch {
+    std::vector<void *> p;
+    cudaStream_t s;
+    bool ok = true;
+    TuneScratch(int n, size_t bytes, cudaStream_t st) : s(st) {
+        for (int i = 0; i < n && ok; ++i) {
+            void *q = nullptr;
+            ok = cudaMallocAsync(&q, bytes, s) == cudaSuccess;
+            if (ok) ok = cudaMemsetAsync(q, 0, bytes, s) == cudaSuccess;
+            p.push_back(q);
+        }
+    }
+    ~TuneScratch() {
+        for (void *q : p)
+            if (q) cudaFreeAsync(q, s);
+    }
+};
+
+// the number of copies of a candidate timed together: the concurrency of
+// the caller's cases (pfgb_batch_minimize sets it while it tunes), so the
+// choice is the one with the best throughput on a device the cases share
+static std::atomic<int> g_tune_copies(1);
+
+// one warm-up round, then the best of three (ms per round); a round is one
+// launch on each of the given streams, forked from and joined to the
+// first; infinity if a launch fails
+template <typename F>
+static float time_launch(const std::vector<cudaStream_t> &ss, F &&launch) {
+    const int k = (int)ss.size();
+    std::vector<cudaEvent_t> ev(k + 1, nullptr);
+    float best = INFINITY;
+    bool ok = true;
+    for (auto &e : ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDefault) == cudaSuccess;
+    auto round = [&](bool timed) {
+        if (timed) cudaEventRecord(ev[0], ss[0]);
+        else cudaEventRecord(ev[k], ss[0]);
+        for (int i = 1; i < k; ++i) cudaStreamWaitEvent(ss[i], timed ? ev[0] : ev[k], 0);
+        for (int i = 0; i < k; ++i) launch(i);
+        for (int i = 1; i < k; ++i) {
+            cudaEventRecord(ev[i], ss[i]);
+            cudaStreamWaitEvent(ss[0], ev[i], 0);
+        }
+        cudaEventRecord(ev[k], ss[0]);
+    };
+    if (ok) {
+        round(false);
+        if (cudaGetLastError() == cudaSuccess) {
+            for (int r = 0; r < 3; ++r) {
+                round(true);
+                if (cudaEventSynchronize(ev[k]) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+                    best = INFINITY;
+                    break;
+                }
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, ev[0], ev[k]);
+                best = std::min(best, ms);
+            }
+        }
+    }
+    for (auto &e : ev)
+        if (e) cudaEventDestroy(e);
+    return best;
+}
+
+// the context's stream and g_tune_copies - 1 more, each with its own
+// scratch arrays
+struct TuneStreams {
+    std::vector<cudaStream_t> ss;
+    std::vector<TuneScratch *> sc;
+    bool ok = true;
+    TuneStreams(cudaStream_t s0, int narr, size_t bytes) {
+        const int k = std::max(1, std::min(16, g_tune_copies.load()));
+        for (int i = 0; i < k && ok; ++i) {
+            cudaStream_t s = s0;
+            if (i > 0) ok = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess;
+            if (!ok) break;
+            ss.push_back(s);
+            sc.push_back(new TuneScratch(narr, bytes, s));
+            ok = sc.back()->ok;
+        }
+    }
+    ~TuneStreams() {
+        for (TuneScratch *t : sc) delete t;
+        if (!ss.empty()) cudaStreamSynchronize(ss[0]);
+        for (size_t i = 1; i < ss.size(); ++i) {
+            cudaStreamSynchronize(ss[i]);
+            cudaStreamDestroy(ss[i]);
+        }
+    }
+};
+
+
+
+// copy op of a z pass with NFI fields in and NFO out, for timing its tiles
+template <typename T, int NFI, int NFO>
+struct OpTuneZ {
+    using Acc = NoAcc;
+    const cplx_t<T> *src[NFI > 0 ? NFI : 1];
+    cplx_t<T> *dst[NFO > 0 ? NFO : 1];
+    int NzC;
+    __device__ void load_spec(long long row, int k, cplx_t<T> *v) const {
+#pragma unroll
+        for (int f = 0; f < NFI; ++f) v[f] = src[f][row * NzC + k];
+    }
+    __device__ void point(long long, const T *in, T *out, Acc &) const {
+#pragma unroll
+        for (int f = 0; f < NFO; ++f) out[f] = NFI > 0 ? in[f % (NFI > 0 ? NFI : 1)] : T(0);
+    }
+    __device__ void store_spec(long long row, int k, const cplx_t<T> *v) const {
+#pragma unroll
+        for (int f = 0; f < NFO; ++f) dst[f][row * NzC + k] = v[f];
+    }
+};
+
+template <typename T, int NIN, int NOUT, int DIN, int DOUT, class Op>
+static int tuned_tk(pfgb_ctx *c, int axis, const AxisPlan &pl, const Op &op, int rule, const char *tag) {
+    using T2 = cplx_t<T>;
+    auto kern = k_axis_pass<T, NIN, NOUT, DIN, DOUT, Op>;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int gy = axis == 1 ? c->g.Nx : c->g.Ny;
+    const TileKey key{dev, (const void *)kern, pl.n, c->g.NzC, gy};
+    {
+        std::lock_guard<std::mutex> lk(g_tile_mu);
+        auto it = g_tiles.find(key);
+        if (it != g_tiles.end()) return it->second.tile;
+    }
+    constexpr int NW = axis_width<NIN, NOUT>();
+    const int n = pl.n;
+    auto bytes = [&](int tk) { return ((size_t)n + 2 * (size_t)n * (NW * tk + 1)) * sizeof(T2); };
+    TileRec rec{rule, rule, INFINITY, INFINITY, tag, n, c->g.NzC, gy};
+    {
+        TuneStreams ts(c->stream, NIN + NOUT, (size_t)c->g.Nk * sizeof(T2));
+        if (ts.ok) {
+            std::vector<AxisIO<T, NIN, NOUT>> io(ts.ss.size());
+            for (size_t i = 0; i < io.size(); ++i) {
+                for (int a = 0; a < NIN; ++a) io[i].in[a] = (const T2 *)ts.sc[i]->p[a];
+                for (int b = 0; b < NOUT; ++b) io[i].out[b] = (T2 *)ts.sc[i]->p[NIN + b];
+            }
+            for (int tk = 1; tk <= 32; tk <<= 1) {
+                if (tk > 1 && tk / 2 >= c->g.NzC) break;
+                const size_t smem = bytes(tk);
+                if (smem > kSmemWide || allow_smem(kern, smem) != cudaSuccess) break;
+                const dim3 grid((c->g.NzC + tk - 1) / tk, gy);
+                const T2 *tw = twp<T>(c, axis == 1 ? 1 : 0);
+                const float t = time_launch(ts.ss, [&](int i) {
+                    kern<<<grid, 256, smem, ts.ss[i]>>>(c->g, axis, pl, tw, tk, io[i], op, nullptr);
+                });
+                if (tk == rule) rec.t_rule_ms = t;
+                if (t < rec.t_ms) { rec.t_ms = t; rec.tile = tk; }
+            }
+        }
+    }
+    cudaGetLastError();   // a candidate that could not launch is not chosen
+    std::lock_guard<std::mutex> lk(g_tile_mu);
+    return g_tiles.emplace(key, rec).first->second.tile;   // the first thread's choice stands
+}
+
+// shared memory of a generic z pass of R rows of length n
+template <typename T, int NFI, int NFO>
+static size_t zpass_bytes(int R, int n) {
+    int PI_ = NFI > 0 ? (R * NFI + 1) / 2 : 0, PO_ = NFO > 0 ? (R * NFO + 1) / 2 : 0;
+    if (NFI == NFO) PO_ = 0;   // in-place pointwise stage
+    return ((size_t)n + 2 * (size_t)PI_ * n + 2 * (size_t)PO_ * n) * sizeof(cplx_t<T>);
+}
+
+template <typename T, int NFI, int NFO>
+static int tuned_r(pfgb_ctx *c, int rule, size_t (*bytes)(int, int), const char *tag) {
+    using T2 = cplx_t<T>;
+    using OpT = OpTuneZ<T, NFI, NFO>;
+    auto kern = k_zpass<T, NFI, NFO, OpT>;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const long long rows = (long long)c->g.Nx * c->g.Ny;
+    const TileKey key{dev, (const void *)kern, c->g.Nz, rows, 0};
+    {
+        std::lock_guard<std::mutex> lk(g_tile_mu);
+        auto it = g_tiles.find(key);
+        if (it != g_tiles.end()) return it->second.tile;
+    }
+    TileRec rec{rule, rule, INFINITY, INFINITY, tag, c->g.Nz, rows, 0};
+    {
+        TuneStreams ts(c->stream, NFI + NFO, (size_t)c->g.Nk * sizeof(T2));
+        if (ts.ok) {
+            std::vector<OpT> op(ts.ss.size());
+            for (size_t i = 0; i < op.size(); ++i) {
+                for (int f = 0; f < NFI; ++f) op[i].src[f] = (const T2 *)ts.sc[i]->p[f];
+                for (int f = 0; f < NFO; ++f) op[i].dst[f] = (T2 *)ts.sc[i]->p[NFI + f];
+                op[i].NzC = c->g.NzC;
+            }
+            for (int r = 2; r <= 128; r <<= 1) {
+                if (r / 2 >= rows) break;
+                const size_t smem = bytes(r, c->g.Nz);
+                if (smem > kSmemWide || allow_smem(kern, smem) != cudaSuccess) break;
+                const int nb = (int)((rows + r - 1) / r);
+                const T2 *tw = twp<T>(c, 2);
+                const float t = time_launch(ts.ss, [&](int i) {
+                    kern<<<nb, 256, smem, ts.ss[i]>>>(c->g, c->plz, tw, r, op[i], nullptr);
+                });
+                if (r == rule) rec.t_rule_ms = t;
+                if (t < rec.t_ms) { rec.t_ms = t; rec.tile = r; }
+            }
+        }
+    }
+    cudaGetLastError();
+    std::lock_guard<std::mutex> lk(g_tile_mu);
+    return g_tiles.emplace(key, rec).first->second.tile;
+}
+
 template <typename T, int NIN, int NOUT, int DIN, int DOUT, class Op>
 static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, Op op, const char *tag) {
     using T2 = cplx_t<T>;
@@ -254,6 +493,7 @@ static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, O
     while (TK > 1 && bytes(TK) > kSmemBudget) TK >>= 1;
     if (TK < 4 && sizeof(T) == 4 && bytes(4) <= kSmemWide) TK = 4;
     while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
+    if (c->p.fft_autotune) TK = tuned_tk<T, NIN, NOUT, DIN, DOUT, Op>(c, axis, pl, op, TK, tag);
     const size_t smem = bytes(TK);
     auto kern = k_axis_pass<T, NIN, NOUT, DIN, DOUT, Op>;
     PFGB_CUDA_TRY(allow_smem(kern, smem));
@@ -391,15 +631,12 @@ static pfgb_status launch_z(pfgb_ctx *c, Op op, const char *tag, double extra_by
             return PFGB_OK;
         }
     }
-    auto bytes = [&](int R) {
-        int PI_ = NFI > 0 ? (R * NFI + 1) / 2 : 0, PO_ = NFO > 0 ? (R * NFO + 1) / 2 : 0;
-        if (NFI == NFO) PO_ = 0;   // in-place pointwise stage
-        return ((size_t)n + 2 * (size_t)PI_ * n + 2 * (size_t)PO_ * n) * sizeof(T2);
-    };
+    auto bytes = [&](int R) { return zpass_bytes<T, NFI, NFO>(R, n); };
     int R = 64;
     while (R > 2 && bytes(R) > kSmemBudget) R >>= 1;
     const long long rows = (long long)c->g.Nx * c->g.Ny;
     while (R > 2 && R / 2 >= rows) R >>= 1;
+    if (c->p.fft_autotune) R = tuned_r<T, NFI, NFO>(c, R, &zpass_bytes<T, NFI, NFO>, tag);
     const size_t smem = bytes(R);
     auto kern = k_zpass<T, NFI, NFO, Op>;
     PFGB_CUDA_TRY(allow_smem(kern, smem));
@@ -5022,6 +5259,28 @@ extern "C" {
 
 // the elastic iteration's y transform of six half spectra on the 246-point
 // engine (test / tooling entry point)
+void pfgb_set_tune_copies(int copies) { g_tune_copies.store(copies < 1 ? 1 : (copies > 16 ? 16 : copies)); }
+
+size_t pfgb_tile_report(char *buf, size_t len) {
+    std::string out;
+    {
+        std::lock_guard<std::mutex> lk(g_tile_mu);
+        for (const auto &kv : g_tiles) {
+            const TileRec &r = kv.second;
+            char line[256];
+            snprintf(line, sizeof(line), "%s n=%lld extents=%lld,%lld tile=%d %.4f ms rule=%d %.4f ms\n",
+                     r.tag.c_str(), r.a, r.b, r.c, r.tile, (double)r.t_ms, r.rule, (double)r.t_rule_ms);
+            out += line;
+        }
+    }
+    if (buf && len) {
+        const size_t m = std::min(len - 1, out.size());
+        memcpy(buf, out.data(), m);
+        buf[m] = '\0';
+    }
+    return out.size();
+}
+
 pfgb_status pfgb_fft_y246x6(int tensor_cores, int dir, int Nx, int NzC, void *spec6, void *stream) {
     if (!spec6 || (dir != -1 && dir != 1) || Nx < 1 || NzC < 2 || (NzC % 2) != 0 || NzC > PFGB_MAX_N) {
         pfgb_set_error_msg("pfgb_fft_y246x6: dir must be -1 or +1, Nx >= 1 and NzC even in [2, %d]", PFGB_MAX_N);

@@ -147,6 +147,15 @@ typedef struct pfgb_params {
        counterpart key in the reference (its transforms are cuFFT's);
        default 0. */
     int32_t fft_tensor_cores;
+    /* 1: the generic transform engine (axes other than 246 long) times its
+       tile candidates on first use, per kernel, grid shape and device, and
+       keeps the fastest for the life of the process: the columns per block
+       of the x and y passes and the rows per block of the z passes
+       (pfgb_tile_report lists them).  0 (default): the fixed rule, the
+       largest tile within 112 KiB of shared memory.  No counterpart key in
+       the reference. */
+    int32_t fft_autotune;
+    int32_t pad_fft;
     double elastic_residual_tolerance;
     double elastic_residual_absolute_floor;
     double eps_iso_over_vB;
@@ -511,6 +520,17 @@ pfgb_status pfgb_fft3d_c2r(int precision, int Nx, int Ny, int Nz,
  * runs the 41-point stage on the tensor cores (split-precision TF32), as
  * fft_tensor_cores bit 1 does in the solver. */
 pfgb_status pfgb_fft_y246x6(int tensor_cores, int dir, int Nx, int NzC, void *d_spec6, void *cuda_stream);
+
+/* The tiles the autotuner (fft_autotune) has chosen in this process, one
+ * line each: the pass, the axis length and grid extents, the chosen tile
+ * and its time, and the fixed rule's tile and time.  Writes at most len
+ * bytes (NUL-terminated) and returns the length of the full report. */
+size_t pfgb_tile_report(char *buf, size_t len);
+/* How many copies of a tile candidate the autotuner times at once, each on
+ * its own stream and arrays (1 to 16; default 1): the number of cases that
+ * will share the device, so that tiles are chosen for throughput under that
+ * sharing.  pfgb_batch_minimize sets it to its concurrency while it tunes. */
+void pfgb_set_tune_copies(int copies);
 
 /* --- allocation-free forward transform -------------------------------- */
 /* No counterpart in the reference (its transforms go through cuFFT plans

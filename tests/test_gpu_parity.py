@@ -749,3 +749,31 @@ def test_gp_storage_coupling_parity(capi, oracle, case, prec):
     dO = o.diagnostics(capi.Diag)
     mtol = (1e-4 if prec == 0 else 1e-3) if wild else (1e-8 if prec == 0 else (1e-3 if ill else 1e-5))
     assert abs(dg.mass_xBtot - dO.mass_xBtot) <= mtol * dO.mass_xBtot
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [0, 1])
+def test_autotuned_tiles_give_the_same_step(capi, prec):
+    """fft_autotune = 1 on the generic engine (48^3): the tiles timed and
+    chosen per pass, the step's fields equal to the fixed rule's up to the
+    order of the block reductions (1e-12 FP64, 1e-6 FP32), and the report
+    lists every tuned pass with a tile no slower than the rule's."""
+    from cuda_sto_pf_gb300.solver import Solver
+    n, steps = 48, 3
+    out = []
+    for tune in (0, 1):
+        p = params_for(capi, "c2.params", n=n, precision=prec, fft_autotune=tune)
+        phi, xB, _ = _inputs(capi, p, n, False, seed=31)
+        with Solver(p) as s:
+            s.load(phi, xB)
+            s.step(steps)
+            out.append(s.fields())
+    for k in ("phi", "xB", "Y"):
+        assert rel_l2(out[1][k], out[0][k]) <= (1e-12 if prec == 0 else 1e-6), k
+    rep = capi.tile_report().splitlines()
+    print("\n".join(rep))
+    assert sum(1 for l in rep if " n=48 " in l) >= 4   # several passes of the 48^3 grid were tuned
+    for l in rep:
+        t = float(l.split(" tile=")[1].split()[1])
+        tr = float(l.split(" rule=")[1].split()[1])
+        assert t <= tr * 1.0001 or tr != tr, l   # the rule is a candidate (nan: outside the candidates)
