@@ -107,6 +107,7 @@ struct pfgb_ctx {
     void *Dkm[3] = {nullptr, nullptr, nullptr};
     double cheb_gam = 1.0, cheb_sig = 0.0, cheb_rho = 1.0;
     void *Uprev[3] = {nullptr, nullptr, nullptr};   // extrapolated warm start: u of the step before
+    void *Uprev2[3] = {nullptr, nullptr, nullptr};  // quadratic extrapolation: u two steps before
     int warm_count = 0;
     // learned start (elastic_warm_start_source 1, 2) and training pairs
     pfgb_fno *fno = nullptr;
@@ -2640,17 +2641,26 @@ __global__ void k_add_increment(cplx_t<TE> *u0, cplx_t<TE> *u1, cplx_t<TE> *u2, 
     }
 }
 
+// the warm start from the last solutions: mode 1 u0 = 2 u^n - u^{n-1},
+// mode 2 u0 = 3 u^n - 3 u^{n-1} + u^{n-2}, 0 u^n; u^n and u^{n-1} kept in
+// p and q (q may be null) for the next step
 template <typename TE>
-__global__ void k_extrapolate_u(cplx_t<TE> *u0, cplx_t<TE> *u1, cplx_t<TE> *u2, cplx_t<TE> *p0, cplx_t<TE> *p1,
-                                cplx_t<TE> *p2, long long n, int extrapolate) {
+struct ExtrapArgs { cplx_t<TE> *u[3], *p[3], *q[3]; };
+template <typename TE>
+__global__ void k_extrapolate_u(ExtrapArgs<TE> a, long long n, int mode) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        cplx_t<TE> *u[3] = {u0, u1, u2}, *p[3] = {p0, p1, p2};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const cplx_t<TE> un = u[c][i];
-            if (extrapolate) u[c][i] = mk2<cplx_t<TE>>(TE(2) * un.x - p[c][i].x, TE(2) * un.y - p[c][i].y);
-            p[c][i] = un;
+            const cplx_t<TE> un = a.u[c][i], up = a.p[c][i];
+            if (mode == 2) {
+                const cplx_t<TE> uq = a.q[c][i];
+                a.u[c][i] = mk2<cplx_t<TE>>(TE(3) * un.x - TE(3) * up.x + uq.x, TE(3) * un.y - TE(3) * up.y + uq.y);
+            } else if (mode == 1) {
+                a.u[c][i] = mk2<cplx_t<TE>>(TE(2) * un.x - up.x, TE(2) * un.y - up.y);
+            }
+            if (a.q[c]) a.q[c][i] = up;
+            a.p[c][i] = un;
         }
     }
 }
@@ -2822,11 +2832,18 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     if (use_model) TRY((model_start<T, TE>(c)));
     if (warm_used || use_model) {
         if (warm_used && c->Uprev[0]) {
-            // u0 = 2 u^n - u^{n-1} once both exist; keep u^n for the next step
-            ProfScope ps(c, {"extrapolate_u", 12.0 * (double)c->g.Nk * sizeof(T2e)});
-            k_extrapolate_u<TE><<<1216, 256, 0, c->stream>>>((T2e *)c->U[0], (T2e *)c->U[1], (T2e *)c->U[2],
-                                                             (T2e *)c->Uprev[0], (T2e *)c->Uprev[1],
-                                                             (T2e *)c->Uprev[2], c->g.Nk, c->warm_count >= 2);
+            // u0 = 2 u^n - u^{n-1} once both exist, or 3 u^n - 3 u^{n-1} +
+            // u^{n-2} once three exist (extrapolate = 2); keep u^n (and u^{n-1})
+            const bool quad = c->Uprev2[0] != nullptr;
+            const int mode = (quad && c->warm_count >= 3) ? 2 : (c->warm_count >= 2 ? 1 : 0);
+            ProfScope ps(c, {"extrapolate_u", (quad ? 18.0 : 12.0) * (double)c->g.Nk * sizeof(T2e)});
+            ExtrapArgs<TE> a;
+            for (int i = 0; i < 3; ++i) {
+                a.u[i] = (T2e *)c->U[i];
+                a.p[i] = (T2e *)c->Uprev[i];
+                a.q[i] = (T2e *)c->Uprev2[i];
+            }
+            k_extrapolate_u<TE><<<1216, 256, 0, c->stream>>>(a, c->g.Nk, mode);
             PFGB_CUDA_TRY(cudaGetLastError());
         }
         AxisIO<TE, 3, 6> io;
@@ -4310,6 +4327,10 @@ static pfgb_status validate(const pfgb_params *p) {
         pfgb_set_error_msg("elastic_warm_start_source must be 0, 1, 2 or 3");
         return PFGB_ERR_INVALID;
     }
+    if (p->elastic_warm_start_extrapolate < 0 || p->elastic_warm_start_extrapolate > 2) {
+        pfgb_set_error_msg("elastic_warm_start_extrapolate must be 0 (u^n), 1 (linear) or 2 (quadratic)");
+        return PFGB_ERR_INVALID;
+    }
     return PFGB_OK;
 }
 
@@ -4330,7 +4351,7 @@ static void ctx_free(pfgb_ctx *c) {
     for (int i = 0; i < 3; ++i) f(c->U[i]);
     f(c->partials); f(c->dscal); f(c->stage);
     for (int i = 0; i < 6; ++i) f(c->sig[i]);
-    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); f(c->Dkm[i]); f(c->Uprev[i]); }
+    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); f(c->Dkm[i]); f(c->Uprev[i]); f(c->Uprev2[i]); }
     f(c->mge); f(c->mlap);
     f(c->fno_in); f(c->fno_out);
     for (int i = 0; i < 3; ++i) f(c->Uhom[i]);
@@ -4604,6 +4625,8 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
         if (pin->elastic_warm_start_extrapolate &&
             (pin->elastic_warm_start_enabled || pin->elastic_residual_control_enabled)) {
             for (int i = 0; i < 3; ++i) { A_(&c->Uprev[i], sizeof(float2) * Nk); }
+            if (pin->elastic_warm_start_extrapolate == 2)
+                for (int i = 0; i < 3; ++i) { A_(&c->Uprev2[i], sizeof(float2) * Nk); }
         }
     }
     if (pin->pf_composition_mode != PFGB_COMPOSITION_LEGACY) {

@@ -254,6 +254,7 @@ struct pfo_state {
     cpx *eps_k[6], *u_k[3], *u_next[3];
     cpx *r_k[3], *d_k[3];   /* increment form: r0 = Phi(u0) - u0 and delta */
     cpx *u_prev[3];         /* extrapolated warm start: u of the step before */
+    cpx *u_prev2[3];        /* quadratic extrapolation: u two steps before */
     cpx *dm_k[3];           /* Chebyshev semi-iteration: the iterate before delta */
     int cheb;               /* elastic_chebyshev with the increment form */
     double cheb_gam, cheb_sig;
@@ -315,6 +316,7 @@ pfo_state *pfo_create(const pfgb_params *pin) {
         s->r_k[c] = (cpx *)xalloc(kb);
         s->d_k[c] = (cpx *)xalloc(kb);
         s->u_prev[c] = (cpx *)xalloc(kb);
+        s->u_prev2[c] = (cpx *)xalloc(kb);
         s->dm_k[c] = (cpx *)xalloc(kb);
     }
     if (pin->elastic_chebyshev && pin->elastic_increment_form) {
@@ -355,7 +357,7 @@ void pfo_destroy(pfo_state *s) {
     for (size_t i = 0; i < sizeof(kk) / sizeof(kk[0]); ++i) free(kk[i]);
     for (int c = 0; c < 6; ++c) { free(s->eps_r[c]); free(s->sig_r[c]); free(s->eps_k[c]); }
     for (int c = 0; c < 3; ++c) {
-        free(s->u_k[c]); free(s->u_next[c]); free(s->r_k[c]); free(s->d_k[c]); free(s->u_prev[c]); free(s->dm_k[c]);
+        free(s->u_k[c]); free(s->u_next[c]); free(s->r_k[c]); free(s->d_k[c]); free(s->u_prev[c]); free(s->u_prev2[c]); free(s->dm_k[c]);
     }
     free(s->kx); free(s->ky); free(s->kz); free(s->mx); free(s->my); free(s->mz);
     free(s->mlap); free(s->mg);
@@ -677,14 +679,23 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
     }
 
     if (warm_used && P->elastic_warm_start_extrapolate) {
-        /* u0 = 2 u^n - u^{n-1} once both exist; keep u^n for the next step */
+        /* u0 = 2 u^n - u^{n-1} once both exist, or (extrapolate = 2)
+         * 3 u^n - 3 u^{n-1} + u^{n-2} once three exist; keep u^n and u^{n-1}
+         * for the next step */
+        const int quad = P->elastic_warm_start_extrapolate == 2 && s->warm_count >= 3;
+        const int lin = !quad && s->warm_count >= 2;
         KLOOP_BEGIN(s)
             for (int c = 0; c < 3; ++c) {
-                const cpx un = s->u_k[c][idx];
-                if (s->warm_count >= 2) {
-                    s->u_k[c][idx].re = rf(s, 2.0 * un.re - s->u_prev[c][idx].re);
-                    s->u_k[c][idx].im = rf(s, 2.0 * un.im - s->u_prev[c][idx].im);
+                const cpx un = s->u_k[c][idx], up = s->u_prev[c][idx];
+                if (quad) {
+                    const cpx uq = s->u_prev2[c][idx];
+                    s->u_k[c][idx].re = rf(s, 3.0 * un.re - 3.0 * up.re + uq.re);
+                    s->u_k[c][idx].im = rf(s, 3.0 * un.im - 3.0 * up.im + uq.im);
+                } else if (lin) {
+                    s->u_k[c][idx].re = rf(s, 2.0 * un.re - up.re);
+                    s->u_k[c][idx].im = rf(s, 2.0 * un.im - up.im);
                 }
+                s->u_prev2[c][idx] = up;
                 s->u_prev[c][idx] = un;
             }
         KLOOP_END

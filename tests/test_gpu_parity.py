@@ -306,18 +306,20 @@ def test_increment_form_matches_reference_form(capi, oracle, prec):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-def test_extrapolated_warm_start_parity(capi, oracle, prec):
+@pytest.mark.parametrize("order", [1, 2])
+def test_extrapolated_warm_start_parity(capi, oracle, prec, order):
     """elastic_warm_start_extrapolate = 1: from the third step the fixed point
-    starts at 2 u^n - u^{n-1}; GPU against the oracle doing the same."""
+    starts at 2 u^n - u^{n-1}; = 2: from the fourth at 3 u^n - 3 u^{n-1} +
+    u^{n-2}.  GPU against the oracle doing the same."""
     from cuda_sto_pf_gb300.solver import Solver
-    p = params_for(capi, "c2.params", n=32, precision=prec, elastic_warm_start_extrapolate=1)
+    p = params_for(capi, "c2.params", n=32, precision=prec, elastic_warm_start_extrapolate=order)
     phi, xB, _ = _inputs(capi, p, 32, False, seed=17)
     o = oracle(p, threads=4)
     o.load(phi, xB)
     so, sg = capi.StepStats(), None
     with Solver(p) as s:
         s.load(phi, xB)
-        for k in range(5):
+        for k in range(6):
             assert o.step(1, so) == 0
             sg = s.step(1)
             assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1, k
