@@ -106,8 +106,9 @@ struct pfgb_ctx {
     // the spectral bounds [a, b] of the linear part; rho of the next update
     void *Dkm[3] = {nullptr, nullptr, nullptr};
     double cheb_gam = 1.0, cheb_sig = 0.0, cheb_rho = 1.0;
-    void *Uprev[3] = {nullptr, nullptr, nullptr};   // extrapolated warm start: u of the step before
-    void *Uprev2[3] = {nullptr, nullptr, nullptr};  // quadratic extrapolation: u two steps before
+    // extrapolated warm start: u of the 1 to 4 steps before (as many levels
+    // as the extrapolation order)
+    void *Uhist[4][3] = {};
     int warm_count = 0;
     // learned start (elastic_warm_start_source 1, 2) and training pairs
     pfgb_fno *fno = nullptr;
@@ -2641,26 +2642,35 @@ __global__ void k_add_increment(cplx_t<TE> *u0, cplx_t<TE> *u1, cplx_t<TE> *u2, 
     }
 }
 
-// the warm start from the last solutions: mode 1 u0 = 2 u^n - u^{n-1},
-// mode 2 u0 = 3 u^n - 3 u^{n-1} + u^{n-2}, 0 u^n; u^n and u^{n-1} kept in
-// p and q (q may be null) for the next step
+// the warm start from the last solutions: the polynomial extrapolation of
+// order m (0: u^n; 1: 2 u^n - u^{n-1}; 2: 3 u^n - 3 u^{n-1} + u^{n-2};
+// 3: 4 u^n - 6 u^{n-1} + 4 u^{n-2} - u^{n-3}; 4: 5, -10, 10, -5, 1), in
+// FP64 arithmetic; the nh history levels h[0..nh-1] (u^{n-1}, ...) shift by
+// one, u^n entering
 template <typename TE>
-struct ExtrapArgs { cplx_t<TE> *u[3], *p[3], *q[3]; };
+struct ExtrapArgs { cplx_t<TE> *u[3], *h[4][3]; };
 template <typename TE>
-__global__ void k_extrapolate_u(ExtrapArgs<TE> a, long long n, int mode) {
+__global__ void k_extrapolate_u(ExtrapArgs<TE> a, long long n, int m, int nh) {
+    const double cf[5][5] = {{1, 0, 0, 0, 0}, {2, -1, 0, 0, 0}, {3, -3, 1, 0, 0}, {4, -6, 4, -1, 0},
+                             {5, -10, 10, -5, 1}};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const cplx_t<TE> un = a.u[c][i], up = a.p[c][i];
-            if (mode == 2) {
-                const cplx_t<TE> uq = a.q[c][i];
-                a.u[c][i] = mk2<cplx_t<TE>>(TE(3) * un.x - TE(3) * up.x + uq.x, TE(3) * un.y - TE(3) * up.y + uq.y);
-            } else if (mode == 1) {
-                a.u[c][i] = mk2<cplx_t<TE>>(TE(2) * un.x - up.x, TE(2) * un.y - up.y);
+            cplx_t<TE> v[5];
+            v[0] = a.u[c][i];
+#pragma unroll
+            for (int l = 0; l < 4; ++l) v[l + 1] = l < nh ? a.h[l][c][i] : v[0];
+            if (m >= 1) {
+                double re = 0.0, im = 0.0;
+#pragma unroll
+                for (int l = 0; l < 5; ++l)
+                    if (l <= m) { re += cf[m][l] * double(v[l].x); im += cf[m][l] * double(v[l].y); }
+                a.u[c][i] = mk2<cplx_t<TE>>(TE(re), TE(im));
             }
-            if (a.q[c]) a.q[c][i] = up;
-            a.p[c][i] = un;
+#pragma unroll
+            for (int l = 3; l >= 0; --l)
+                if (l < nh) a.h[l][c][i] = v[l];
         }
     }
 }
@@ -2831,19 +2841,18 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     }
     if (use_model) TRY((model_start<T, TE>(c)));
     if (warm_used || use_model) {
-        if (warm_used && c->Uprev[0]) {
-            // u0 = 2 u^n - u^{n-1} once both exist, or 3 u^n - 3 u^{n-1} +
-            // u^{n-2} once three exist (extrapolate = 2); keep u^n (and u^{n-1})
-            const bool quad = c->Uprev2[0] != nullptr;
-            const int mode = (quad && c->warm_count >= 3) ? 2 : (c->warm_count >= 2 ? 1 : 0);
-            ProfScope ps(c, {"extrapolate_u", (quad ? 18.0 : 12.0) * (double)c->g.Nk * sizeof(T2e)});
+        if (warm_used && c->Uhist[0][0]) {
+            // u0 extrapolated through the last m + 1 solutions, m the order
+            // or fewer while the history fills; the history shifts by one
+            const int nh = P.elastic_warm_start_extrapolate;
+            const int m = std::min(nh, c->warm_count - 1);
+            ProfScope ps(c, {"extrapolate_u", (2.0 + 2.0 * nh) * 3.0 * (double)c->g.Nk * sizeof(T2e)});
             ExtrapArgs<TE> a;
             for (int i = 0; i < 3; ++i) {
                 a.u[i] = (T2e *)c->U[i];
-                a.p[i] = (T2e *)c->Uprev[i];
-                a.q[i] = (T2e *)c->Uprev2[i];
+                for (int l = 0; l < 4; ++l) a.h[l][i] = (T2e *)c->Uhist[l][i];
             }
-            k_extrapolate_u<TE><<<1216, 256, 0, c->stream>>>(a, c->g.Nk, mode);
+            k_extrapolate_u<TE><<<1216, 256, 0, c->stream>>>(a, c->g.Nk, m, nh);
             PFGB_CUDA_TRY(cudaGetLastError());
         }
         AxisIO<TE, 3, 6> io;
@@ -4327,8 +4336,8 @@ static pfgb_status validate(const pfgb_params *p) {
         pfgb_set_error_msg("elastic_warm_start_source must be 0, 1, 2 or 3");
         return PFGB_ERR_INVALID;
     }
-    if (p->elastic_warm_start_extrapolate < 0 || p->elastic_warm_start_extrapolate > 2) {
-        pfgb_set_error_msg("elastic_warm_start_extrapolate must be 0 (u^n), 1 (linear) or 2 (quadratic)");
+    if (p->elastic_warm_start_extrapolate < 0 || p->elastic_warm_start_extrapolate > 4) {
+        pfgb_set_error_msg("elastic_warm_start_extrapolate must be 0 (u^n) or the order 1 to 4");
         return PFGB_ERR_INVALID;
     }
     return PFGB_OK;
@@ -4351,7 +4360,7 @@ static void ctx_free(pfgb_ctx *c) {
     for (int i = 0; i < 3; ++i) f(c->U[i]);
     f(c->partials); f(c->dscal); f(c->stage);
     for (int i = 0; i < 6; ++i) f(c->sig[i]);
-    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); f(c->Dkm[i]); f(c->Uprev[i]); f(c->Uprev2[i]); }
+    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); f(c->Dkm[i]); for (int l = 0; l < 4; ++l) f(c->Uhist[l][i]); }
     f(c->mge); f(c->mlap);
     f(c->fno_in); f(c->fno_out);
     for (int i = 0; i < 3; ++i) f(c->Uhom[i]);
@@ -4624,9 +4633,8 @@ pfgb_status pfgb_create(const pfgb_params *pin, int device, pfgb_ctx **out) {
         }
         if (pin->elastic_warm_start_extrapolate &&
             (pin->elastic_warm_start_enabled || pin->elastic_residual_control_enabled)) {
-            for (int i = 0; i < 3; ++i) { A_(&c->Uprev[i], sizeof(float2) * Nk); }
-            if (pin->elastic_warm_start_extrapolate == 2)
-                for (int i = 0; i < 3; ++i) { A_(&c->Uprev2[i], sizeof(float2) * Nk); }
+            for (int l = 0; l < pin->elastic_warm_start_extrapolate; ++l)
+                for (int i = 0; i < 3; ++i) { A_(&c->Uhist[l][i], sizeof(float2) * Nk); }
         }
     }
     if (pin->pf_composition_mode != PFGB_COMPOSITION_LEGACY) {

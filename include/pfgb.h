@@ -126,8 +126,9 @@ typedef struct pfgb_params {
        the linear extrapolation 2 u^n - u^{n-1} instead of u^n (the
        reference's warm start, main_cuda.cu:28795-28807); it converges to the
        same tolerance from a guess accurate to O(dt^2).  2: once three exist,
-       the quadratic 3 u^n - 3 u^{n-1} + u^{n-2}, accurate to O(dt^3).
-       Default 0. */
+       the quadratic 3 u^n - 3 u^{n-1} + u^{n-2}, accurate to O(dt^3); 3:
+       once four exist, the cubic 4 u^n - 6 u^{n-1} + 4 u^{n-2} - u^{n-3};
+       4: once five exist, the quartic (5, -10, 10, -5, 1).  Default 0. */
     int32_t elastic_warm_start_extrapolate;
     /* 1: Chebyshev semi-iteration of the increment fixed point (with
        elastic_increment_form).  The linear part L = -Gamma0 (h dC) is

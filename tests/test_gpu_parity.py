@@ -306,11 +306,12 @@ def test_increment_form_matches_reference_form(capi, oracle, prec):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
 def test_extrapolated_warm_start_parity(capi, oracle, prec, order):
     """elastic_warm_start_extrapolate = 1: from the third step the fixed point
     starts at 2 u^n - u^{n-1}; = 2: from the fourth at 3 u^n - 3 u^{n-1} +
-    u^{n-2}.  GPU against the oracle doing the same."""
+    u^{n-2}; = 3: from the fifth at 4 u^n - 6 u^{n-1} + 4 u^{n-2} - u^{n-3};
+    = 4: from the sixth at the quartic.  GPU against the oracle doing the same."""
     from cuda_sto_pf_gb300.solver import Solver
     p = params_for(capi, "c2.params", n=32, precision=prec, elastic_warm_start_extrapolate=order)
     phi, xB, _ = _inputs(capi, p, 32, False, seed=17)
@@ -319,7 +320,7 @@ def test_extrapolated_warm_start_parity(capi, oracle, prec, order):
     so, sg = capi.StepStats(), None
     with Solver(p) as s:
         s.load(phi, xB)
-        for k in range(6):
+        for k in range(7):
             assert o.step(1, so) == 0
             sg = s.step(1)
             assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1, k
