@@ -2643,34 +2643,41 @@ __global__ void k_add_increment(cplx_t<TE> *u0, cplx_t<TE> *u1, cplx_t<TE> *u2, 
 }
 
 // the warm start from the last solutions: the polynomial extrapolation of
-// order m (0: u^n; 1: 2 u^n - u^{n-1}; 2: 3 u^n - 3 u^{n-1} + u^{n-2};
-// 3: 4 u^n - 6 u^{n-1} + 4 u^{n-2} - u^{n-3}; 4: 5, -10, 10, -5, 1), in
-// FP64 arithmetic; the nh history levels h[0..nh-1] (u^{n-1}, ...) shift by
-// one, u^n entering
+// order m through u^n and the history h[0..m-1] = u^{n-1}, ..., u^{n-m}
+// (1: 2 u^n - u^{n-1}; 2: 3 u^n - 3 u^{n-1} + u^{n-2}; 3: 4, -6, 4, -1;
+// 4: 5, -10, 10, -5, 1), formed as u^n plus its backward differences
+// (nabla u^n + nabla^2 u^n + ... + nabla^m u^n): the differences of
+// neighbouring solutions are small and nearly exact in the field type, so
+// the sum loses less than the binomial form would.  u^n is also written to
+// `slot`, the history level that becomes u^{n-1} (the host rotates the
+// levels' pointers instead of copying them).
 template <typename TE>
-struct ExtrapArgs { cplx_t<TE> *u[3], *h[4][3]; };
+struct ExtrapArgs { cplx_t<TE> *u[3], *h[4][3], *slot[3]; };
 template <typename TE>
-__global__ void k_extrapolate_u(ExtrapArgs<TE> a, long long n, int m, int nh) {
-    const double cf[5][5] = {{1, 0, 0, 0, 0}, {2, -1, 0, 0, 0}, {3, -3, 1, 0, 0}, {4, -6, 4, -1, 0},
-                             {5, -10, 10, -5, 1}};
+__global__ void k_extrapolate_u(ExtrapArgs<TE> a, long long n, int m) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            cplx_t<TE> v[5];
-            v[0] = a.u[c][i];
+            cplx_t<TE> d[5];
+            d[0] = a.u[c][i];
 #pragma unroll
-            for (int l = 0; l < 4; ++l) v[l + 1] = l < nh ? a.h[l][c][i] : v[0];
+            for (int l = 0; l < 4; ++l)
+                if (l < m) d[l + 1] = a.h[l][c][i];
+            a.slot[c][i] = d[0];
             if (m >= 1) {
-                double re = 0.0, im = 0.0;
+                // d[j] <- nabla^j u^n, level by level
+                cplx_t<TE> sum = d[0];
 #pragma unroll
-                for (int l = 0; l < 5; ++l)
-                    if (l <= m) { re += cf[m][l] * double(v[l].x); im += cf[m][l] * double(v[l].y); }
-                a.u[c][i] = mk2<cplx_t<TE>>(TE(re), TE(im));
+                for (int k = 1; k <= 4; ++k) {
+                    if (k > m) break;
+#pragma unroll
+                    for (int l = 4; l >= 1; --l)
+                        if (l >= k && l <= m) d[l] = mk2<cplx_t<TE>>(d[l - 1].x - d[l].x, d[l - 1].y - d[l].y);
+                    sum = mk2<cplx_t<TE>>(sum.x + d[k].x, sum.y + d[k].y);
+                }
+                a.u[c][i] = sum;
             }
-#pragma unroll
-            for (int l = 3; l >= 0; --l)
-                if (l < nh) a.h[l][c][i] = v[l];
         }
     }
 }
@@ -2843,17 +2850,24 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     if (warm_used || use_model) {
         if (warm_used && c->Uhist[0][0]) {
             // u0 extrapolated through the last m + 1 solutions, m the order
-            // or fewer while the history fills; the history shifts by one
+            // or fewer while the history fills; u^n goes into the oldest
+            // level, which the pointer rotation below makes u^{n-1}
             const int nh = P.elastic_warm_start_extrapolate;
             const int m = std::min(nh, c->warm_count - 1);
-            ProfScope ps(c, {"extrapolate_u", (2.0 + 2.0 * nh) * 3.0 * (double)c->g.Nk * sizeof(T2e)});
+            ProfScope ps(c, {"extrapolate_u", (3.0 + (double)std::max(m, 0)) * 3.0 * (double)c->g.Nk * sizeof(T2e)});
             ExtrapArgs<TE> a;
             for (int i = 0; i < 3; ++i) {
                 a.u[i] = (T2e *)c->U[i];
                 for (int l = 0; l < 4; ++l) a.h[l][i] = (T2e *)c->Uhist[l][i];
+                a.slot[i] = (T2e *)c->Uhist[nh - 1][i];
             }
-            k_extrapolate_u<TE><<<1216, 256, 0, c->stream>>>(a, c->g.Nk, m, nh);
+            k_extrapolate_u<TE><<<1216, 256, 0, c->stream>>>(a, c->g.Nk, std::max(m, 0));
             PFGB_CUDA_TRY(cudaGetLastError());
+            for (int i = 0; i < 3; ++i) {
+                void *oldest = c->Uhist[nh - 1][i];
+                for (int l = nh - 1; l > 0; --l) c->Uhist[l][i] = c->Uhist[l - 1][i];
+                c->Uhist[0][i] = oldest;
+            }
         }
         AxisIO<TE, 3, 6> io;
         for (int i = 0; i < 3; ++i) io.in[i] = (const T2e *)c->U[i];
