@@ -92,7 +92,7 @@ class Params(Structure):
         ("pf_conservative_bound_tol", c_double), ("pf_conservative_mass_tol", c_double),
         ("pf_conservative_beta_support_eps", c_double), ("pf_conservative_max_subcycles", c_int32),
         ("gp_y_update_mode", c_int32), ("gp_eta_mass_limiter", c_int32), ("gp_y_picard_iters", c_int32),
-        ("gp_limiter_flux_from_xn", c_int32), ("pad_gp", c_int32),
+        ("gp_limiter_flux_from_xn", c_int32), ("y_update_mass_projection_enabled", c_int32),
         ("temperature_K", c_double), ("mu0_compound", c_double), ("xB_eq_matrix", c_double),
     ]
 

@@ -110,6 +110,7 @@ const DKey kInts[] = {
     DK("zero_mode_fp64_cells", zero_mode_fp64_cells),
     DK("pf_conservative_max_subcycles", pf_conservative_max_subcycles),
     DK("gp_y_picard_iters", gp_y_picard_iters), DK("gp_limiter_flux_from_xn", gp_limiter_flux_from_xn),
+    DK("y_update_mass_projection_enabled", y_update_mass_projection_enabled),
     DK("enable_Y_rhs_previous_time_level", enable_Y_rhs_previous_time_level),
     DK("disable_Y_rhs_gamma_term", disable_Y_rhs_gamma_term),
     DK("gp_elastic_enabled", gp_elastic_enabled), DK("gp_elastic_active_eta", gp_elastic_active_eta),
@@ -129,7 +130,6 @@ const DKey kInts[] = {
 // 16137, 16424): any other value is refused, not ignored
 struct Selector { const char *key, *allowed; };
 const Selector kSelectors[] = {
-    {"y_update_mass_projection_enabled", "0"},
     {"enable_Y_rhs_picard", "0"},              {"enable_gp_assisted_beta_nucleation", "0"},
     {"gp_nuc_enabled", "0"},                   {"diagnostic_rsmd_enabled", "0"},
 };

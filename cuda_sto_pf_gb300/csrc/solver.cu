@@ -4350,6 +4350,13 @@ static pfgb_status validate(const pfgb_params *p) {
         pfgb_set_error_msg("elastic_warm_start_source must be 0, 1, 2 or 3");
         return PFGB_ERR_INVALID;
     }
+    if (p->y_update_mass_projection_enabled &&
+        (p->pf_composition_mode != PFGB_COMPOSITION_LEGACY || p->zero_mode_enabled)) {
+        // main_cuda.cu:1719-1727 and 24691-24704
+        pfgb_set_error_msg("y_update_mass_projection_enabled is refused with the conservative composition modes "
+                           "and the zero mode");
+        return PFGB_ERR_INVALID;
+    }
     if (p->elastic_warm_start_extrapolate < 0 || p->elastic_warm_start_extrapolate > 4) {
         pfgb_set_error_msg("elastic_warm_start_extrapolate must be 0 (u^n) or the order 1 to 4");
         return PFGB_ERR_INVALID;

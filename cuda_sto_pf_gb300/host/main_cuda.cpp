@@ -241,6 +241,8 @@ Cli parse(int argc, char **argv) {
         else if ((v = flag_value(argc, argv, &i, "--gp-y-update-mode")) ||
                  (v = flag_value(argc, argv, &i, "--gp_y_update_mode")))   // main_cuda.cu:24156-24166
             c.param_sets.push_back({"gp_y_update_mode", v});
+        else if ((v = flag_value(argc, argv, &i, "--y-update-mass-projection-enabled")))   // main_cuda.cu:24218-24221
+            c.param_sets.push_back({"y_update_mass_projection_enabled", v});
         else if ((v = flag_value(argc, argv, &i, "--gp-barrier-only-mode")))   // main_cuda.cu:24293-24296
             c.param_sets.push_back({"gp_barrier_only_mode", v});
         else if ((v = flag_value(argc, argv, &i, "--enable-legacy-gp-storage-coupling")))   // :24297-24300

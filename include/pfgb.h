@@ -311,7 +311,14 @@ typedef struct pfgb_params {
        the first pass's div J by then; 1 = x^n.  No counterpart key in the
        reference. */
     int32_t gp_limiter_flux_from_xn;
-    int32_t pad_gp;
+    /* y_update_mass_projection_enabled (main_cuda.cu:31085-31140): the
+       reference arms its global shift of Y only after a GP-to-beta
+       conversion event (main_cuda.cu:30079-30084, not on this path) or in
+       the q split, where its target, captured only on such events, stays 0,
+       the bracket fails and the shift is 0.  So on this path 1 changes
+       nothing; it is refused, as in the reference, with the conservative
+       composition modes and the zero mode (main_cuda.cu:1719-1727, 24691-24704). */
+    int32_t y_update_mass_projection_enabled;
     /* derived by pfgb_params_finalize (pfparams_refresh_thermo) */
     double temperature_K;
     double mu0_compound;

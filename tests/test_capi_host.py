@@ -78,7 +78,7 @@ def test_unknown_key_warns_and_is_ignored(capi, tmp_path, capfd):
     assert "unknown key ignored: not_a_key" in capfd.readouterr().err
 
 
-@pytest.mark.parametrize("line", ["y_update_mass_projection_enabled = 1", "enable_Y_rhs_picard = 1",
+@pytest.mark.parametrize("line", ["enable_Y_rhs_picard = 1",
                                   "gp_nuc_enabled = 1", "diagnostic_rsmd_enabled = 1",
                                   "enable_gp_assisted_beta_nucleation = 1"])
 def test_unbuilt_path_selectors_are_refused(capi, tmp_path, line):
@@ -89,6 +89,23 @@ def test_unbuilt_path_selectors_are_refused(capi, tmp_path, line):
     # the default value is accepted
     key = line.split("=")[0].strip()
     capi.load_params_file(_write(tmp_path, base + "\n%s = 0\n" % key))
+
+
+def test_mass_projection_key(capi, tmp_path):
+    """y_update_mass_projection_enabled = 1 is accepted (on this path the
+    reference's projection never arms) and refused, as in the reference,
+    with the zero mode and the conservative composition modes."""
+    base = open(os.path.join(GOLDEN, "c2.params")).read()
+    p = capi.load_params_file(_write(tmp_path, base + "\ny_update_mass_projection_enabled = 1\n"))
+    assert p.y_update_mass_projection_enabled == 1
+    for over in (dict(zero_mode_enabled=1), dict(pf_composition_mode=1)):
+        q = capi.load_params_file(_write(tmp_path, base + "\ny_update_mass_projection_enabled = 1\n"))
+        for k, v in over.items():
+            setattr(q, k, v)
+        capi.finalize(q)
+        ctx = ctypes.c_void_p()
+        assert capi.load().pfgb_create(ctypes.byref(q), 0, ctypes.byref(ctx)) == 1
+        assert not ctx.value
 
 
 def test_gp_storage_coupling_keys(capi, tmp_path):
