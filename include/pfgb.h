@@ -315,8 +315,9 @@ typedef struct pfgb_params {
        reference arms its global shift of Y only after a GP-to-beta
        conversion event (main_cuda.cu:30079-30084, not on this path) or in
        the q split, where its target, captured only on such events, stays 0,
-       the bracket fails and the shift is 0.  So on this path 1 changes
-       nothing; it is refused, as in the reference, with the conservative
+       the bracket fails and the shift is 0 (x recomputed from Y, a
+       rounding-level change).  So on this path 1 changes nothing beyond
+       rounding; it is refused, as in the reference, with the conservative
        composition modes and the zero mode (main_cuda.cu:1719-1727, 24691-24704). */
     int32_t y_update_mass_projection_enabled;
     /* derived by pfgb_params_finalize (pfparams_refresh_thermo) */
