@@ -211,14 +211,15 @@ def test_bench_configuration_246_axes(capi, oracle, shape, tc):
     """The elastic configuration the benchmark times, on the 6 x 41 engine:
     FP32 fields, gp_zone, zero mode, heterogeneous S_p, tolerance 1e-8
     without the fail-closed rule, the Chebyshev semi-iteration of the
-    increment and the extrapolated warm start (bench.py make_params).  Six
-    steps against the oracle doing the same, step by step: iterations within
-    one, every warm step converged below 1e-8 on both sides (a warm step at
-    the cap fails), fields within the FP32 tolerance."""
+    increment and the warm start extrapolated to fourth order (bench.py
+    make_params).  Eight steps against the oracle doing the same (the fourth
+    order from the sixth), step by step: iterations within one, every warm
+    step converged below 1e-8 on both sides (a warm step at the cap fails),
+    fields within the FP32 tolerance."""
     from cuda_sto_pf_gb300.solver import Solver
     p = params_for(capi, "c2.params", n=16, zero_mode_enabled=1, model_mode=1, precision=1,
                    elastic_residual_tolerance=1e-8, elastic_fail_on_nonconvergence=0, elastic_chebyshev=1,
-                   elastic_warm_start_extrapolate=1, fft_tensor_cores=tc)
+                   elastic_warm_start_extrapolate=4, fft_tensor_cores=tc)
     p.Nx, p.Ny, p.Nz = shape
     phi, xB, eta = _inputs(capi, p, 16, True, seed=23, shape=shape)
     o = oracle(p, threads=8)
@@ -226,7 +227,7 @@ def test_bench_configuration_246_axes(capi, oracle, shape, tc):
     so = capi.StepStats()
     with Solver(p) as s:
         s.load(phi, xB, eta)
-        for k in range(6):
+        for k in range(8):
             assert o.step(1, so) == 0
             sg = s.step(1)
             # the cold first step: its increment is most of u, and with FP32
