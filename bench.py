@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--no-chebyshev", action="store_true", help="the reference's plain elastic iteration")
     ap.add_argument("--no-extrapolate", action="store_true",
                     help="start each elastic solve from the previous solution (the reference's warm start)")
-    ap.add_argument("--extrapolate-order", type=int, default=None, choices=[1, 2, 3, 4],
+    ap.add_argument("--extrapolate-order", type=int, default=None, choices=[1, 2, 3, 4, 5],
                     help="order of the extrapolated warm start (default: EXTRAPOLATE)")
     ap.add_argument("--fft-tensor-cores", type=int, default=None,
                     help="1: the 41-point stage of the elastic y passes on the tensor cores (default: FFT_TENSOR_CORES)")
@@ -96,13 +96,13 @@ def dist_env():
 # (--no-chebyshev: the reference's plain iteration); the CPU reference arm
 # and the plain FP64 comparison always run the reference's iteration
 CHEBYSHEV = 1
-# the elastic warm start extrapolated to fourth order from the last five
+# the elastic warm start extrapolated to fifth order from the last six
 # solutions (same fixed point and stopping test, fewer iterations when the
-# fields move: 8.66 iterations per step over 100 steps at 246^3 against
+# fields move: 8.14 iterations per step over 100 steps at 246^3 against
 # 11.1 with the linear form, fields against plain FP64 unchanged);
-# --extrapolate-order 1..3: lower orders; --no-extrapolate: the reference's
+# --extrapolate-order 1..4: lower orders; --no-extrapolate: the reference's
 # previous-solution start
-EXTRAPOLATE = 4
+EXTRAPOLATE = 5
 # the 41-point stage of the 246-point transforms on the tensor cores
 # (split-precision TF32); --fft-tensor-cores overrides
 FFT_TENSOR_CORES = 0
@@ -566,7 +566,8 @@ def run_ours(args):
                                                   1: "extrapolated linearly from the last two solutions",
                                                   2: "extrapolated quadratically from the last three solutions",
                                                   3: "extrapolated cubically from the last four solutions",
-                                                  4: "extrapolated to fourth order from the last five solutions"
+                                                  4: "extrapolated to fourth order from the last five solutions",
+                                                  5: "extrapolated to fifth order from the last six solutions"
                                                   }[EXTRAPOLATE],
                            "dft41_stage": "tensor cores (tcgen05, split-precision TF32)" if FFT_TENSOR_CORES
                            else "FP32 multiply-adds",

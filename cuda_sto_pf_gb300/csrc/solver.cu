@@ -106,9 +106,9 @@ struct pfgb_ctx {
     // the spectral bounds [a, b] of the linear part; rho of the next update
     void *Dkm[3] = {nullptr, nullptr, nullptr};
     double cheb_gam = 1.0, cheb_sig = 0.0, cheb_rho = 1.0;
-    // extrapolated warm start: u of the 1 to 4 steps before (as many levels
+    // extrapolated warm start: u of the 1 to 5 steps before (as many levels
     // as the extrapolation order)
-    void *Uhist[4][3] = {};
+    void *Uhist[5][3] = {};
     int warm_count = 0;
     // learned start (elastic_warm_start_source 1, 2) and training pairs
     pfgb_fno *fno = nullptr;
@@ -2645,34 +2645,35 @@ __global__ void k_add_increment(cplx_t<TE> *u0, cplx_t<TE> *u1, cplx_t<TE> *u2, 
 // the warm start from the last solutions: the polynomial extrapolation of
 // order m through u^n and the history h[0..m-1] = u^{n-1}, ..., u^{n-m}
 // (1: 2 u^n - u^{n-1}; 2: 3 u^n - 3 u^{n-1} + u^{n-2}; 3: 4, -6, 4, -1;
-// 4: 5, -10, 10, -5, 1), formed as u^n plus its backward differences
+// 4: 5, -10, 10, -5, 1; 5: 6, -15, 20, -15, 6, -1), formed as u^n plus its
+// backward differences
 // (nabla u^n + nabla^2 u^n + ... + nabla^m u^n): the differences of
 // neighbouring solutions are small and nearly exact in the field type, so
 // the sum loses less than the binomial form would.  u^n is also written to
 // `slot`, the history level that becomes u^{n-1} (the host rotates the
 // levels' pointers instead of copying them).
 template <typename TE>
-struct ExtrapArgs { cplx_t<TE> *u[3], *h[4][3], *slot[3]; };
+struct ExtrapArgs { cplx_t<TE> *u[3], *h[5][3], *slot[3]; };
 template <typename TE>
 __global__ void k_extrapolate_u(ExtrapArgs<TE> a, long long n, int m) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            cplx_t<TE> d[5];
+            cplx_t<TE> d[6];
             d[0] = a.u[c][i];
 #pragma unroll
-            for (int l = 0; l < 4; ++l)
+            for (int l = 0; l < 5; ++l)
                 if (l < m) d[l + 1] = a.h[l][c][i];
             a.slot[c][i] = d[0];
             if (m >= 1) {
                 // d[j] <- nabla^j u^n, level by level
                 cplx_t<TE> sum = d[0];
 #pragma unroll
-                for (int k = 1; k <= 4; ++k) {
+                for (int k = 1; k <= 5; ++k) {
                     if (k > m) break;
 #pragma unroll
-                    for (int l = 4; l >= 1; --l)
+                    for (int l = 5; l >= 1; --l)
                         if (l >= k && l <= m) d[l] = mk2<cplx_t<TE>>(d[l - 1].x - d[l].x, d[l - 1].y - d[l].y);
                     sum = mk2<cplx_t<TE>>(sum.x + d[k].x, sum.y + d[k].y);
                 }
@@ -2858,7 +2859,7 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
             ExtrapArgs<TE> a;
             for (int i = 0; i < 3; ++i) {
                 a.u[i] = (T2e *)c->U[i];
-                for (int l = 0; l < 4; ++l) a.h[l][i] = (T2e *)c->Uhist[l][i];
+                for (int l = 0; l < 5; ++l) a.h[l][i] = (T2e *)c->Uhist[l][i];
                 a.slot[i] = (T2e *)c->Uhist[nh - 1][i];
             }
             k_extrapolate_u<TE><<<1216, 256, 0, c->stream>>>(a, c->g.Nk, std::max(m, 0));
@@ -4357,8 +4358,8 @@ static pfgb_status validate(const pfgb_params *p) {
                            "and the zero mode");
         return PFGB_ERR_INVALID;
     }
-    if (p->elastic_warm_start_extrapolate < 0 || p->elastic_warm_start_extrapolate > 4) {
-        pfgb_set_error_msg("elastic_warm_start_extrapolate must be 0 (u^n) or the order 1 to 4");
+    if (p->elastic_warm_start_extrapolate < 0 || p->elastic_warm_start_extrapolate > 5) {
+        pfgb_set_error_msg("elastic_warm_start_extrapolate must be 0 (u^n) or the order 1 to 5");
         return PFGB_ERR_INVALID;
     }
     return PFGB_OK;
@@ -4381,7 +4382,7 @@ static void ctx_free(pfgb_ctx *c) {
     for (int i = 0; i < 3; ++i) f(c->U[i]);
     f(c->partials); f(c->dscal); f(c->stage);
     for (int i = 0; i < 6; ++i) f(c->sig[i]);
-    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); f(c->Dkm[i]); for (int l = 0; l < 4; ++l) f(c->Uhist[l][i]); }
+    for (int i = 0; i < 3; ++i) { f(c->Rk[i]); f(c->Dk[i]); f(c->Dkm[i]); for (int l = 0; l < 5; ++l) f(c->Uhist[l][i]); }
     f(c->mge); f(c->mlap);
     f(c->fno_in); f(c->fno_out);
     for (int i = 0; i < 3; ++i) f(c->Uhom[i]);

@@ -128,7 +128,8 @@ typedef struct pfgb_params {
        same tolerance from a guess accurate to O(dt^2).  2: once three exist,
        the quadratic 3 u^n - 3 u^{n-1} + u^{n-2}, accurate to O(dt^3); 3:
        once four exist, the cubic 4 u^n - 6 u^{n-1} + 4 u^{n-2} - u^{n-3};
-       4: once five exist, the quartic (5, -10, 10, -5, 1).  Default 0. */
+       4: once five exist, the quartic (5, -10, 10, -5, 1); 5: once six
+       exist, the quintic (6, -15, 20, -15, 6, -1).  Default 0. */
     int32_t elastic_warm_start_extrapolate;
     /* 1: Chebyshev semi-iteration of the increment fixed point (with
        elastic_increment_form).  The linear part L = -Gamma0 (h dC) is

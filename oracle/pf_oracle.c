@@ -256,7 +256,8 @@ struct pfo_state {
     cpx *u_prev[3];         /* extrapolated warm start: u of the step before */
     cpx *u_prev2[3];        /* order 2 and 3: u two steps before */
     cpx *u_prev3[3];        /* order 3 and 4: u three steps before */
-    cpx *u_prev4[3];        /* order 4: u four steps before */
+    cpx *u_prev4[3];        /* order 4 and 5: u four steps before */
+    cpx *u_prev5[3];        /* order 5: u five steps before */
     cpx *dm_k[3];           /* Chebyshev semi-iteration: the iterate before delta */
     int cheb;               /* elastic_chebyshev with the increment form */
     double cheb_gam, cheb_sig;
@@ -321,6 +322,7 @@ pfo_state *pfo_create(const pfgb_params *pin) {
         s->u_prev2[c] = (cpx *)xalloc(kb);
         s->u_prev3[c] = (cpx *)xalloc(kb);
         s->u_prev4[c] = (cpx *)xalloc(kb);
+        s->u_prev5[c] = (cpx *)xalloc(kb);
         s->dm_k[c] = (cpx *)xalloc(kb);
     }
     if (pin->elastic_chebyshev && pin->elastic_increment_form) {
@@ -361,7 +363,7 @@ void pfo_destroy(pfo_state *s) {
     for (size_t i = 0; i < sizeof(kk) / sizeof(kk[0]); ++i) free(kk[i]);
     for (int c = 0; c < 6; ++c) { free(s->eps_r[c]); free(s->sig_r[c]); free(s->eps_k[c]); }
     for (int c = 0; c < 3; ++c) {
-        free(s->u_k[c]); free(s->u_next[c]); free(s->r_k[c]); free(s->d_k[c]); free(s->u_prev[c]); free(s->u_prev2[c]); free(s->u_prev3[c]); free(s->u_prev4[c]); free(s->dm_k[c]);
+        free(s->u_k[c]); free(s->u_next[c]); free(s->r_k[c]); free(s->d_k[c]); free(s->u_prev[c]); free(s->u_prev2[c]); free(s->u_prev3[c]); free(s->u_prev4[c]); free(s->u_prev5[c]); free(s->dm_k[c]);
     }
     free(s->kx); free(s->ky); free(s->kz); free(s->mx); free(s->my); free(s->mz);
     free(s->mlap); free(s->mg);
@@ -688,24 +690,26 @@ static int elastic_solve(pfo_state *s, pfgb_step_stats *st) {
          * 2 u^n - u^{n-1}; 3 u^n - 3 u^{n-1} + u^{n-2};
          * 4 u^n - 6 u^{n-1} + 4 u^{n-2} - u^{n-3};
          * 5 u^n - 10 u^{n-1} + 10 u^{n-2} - 5 u^{n-3} + u^{n-4};
-         * the history shifts by one */
+         * 6, -15, 20, -15, 6, -1; the history shifts by one */
         int m = P->elastic_warm_start_extrapolate;
         if (m > s->warm_count - 1) m = s->warm_count - 1;
-        static const double cf[5][5] = {{1, 0, 0, 0, 0}, {2, -1, 0, 0, 0}, {3, -3, 1, 0, 0}, {4, -6, 4, -1, 0},
-                                        {5, -10, 10, -5, 1}};
+        static const double cf[6][6] = {{1, 0, 0, 0, 0, 0}, {2, -1, 0, 0, 0, 0}, {3, -3, 1, 0, 0, 0},
+                                        {4, -6, 4, -1, 0, 0}, {5, -10, 10, -5, 1, 0}, {6, -15, 20, -15, 6, -1}};
         const double *w = cf[m < 0 ? 0 : m];
         KLOOP_BEGIN(s)
             for (int c = 0; c < 3; ++c) {
                 const cpx h0 = s->u_k[c][idx], h1 = s->u_prev[c][idx], h2 = s->u_prev2[c][idx],
-                          h3 = s->u_prev3[c][idx], h4 = s->u_prev4[c][idx];
+                          h3 = s->u_prev3[c][idx], h4 = s->u_prev4[c][idx], h5 = s->u_prev5[c][idx];
                 if (m >= 1) {
                     double re = w[0] * h0.re + w[1] * h1.re, im = w[0] * h0.im + w[1] * h1.im;
                     if (m >= 2) { re += w[2] * h2.re; im += w[2] * h2.im; }
                     if (m >= 3) { re += w[3] * h3.re; im += w[3] * h3.im; }
                     if (m >= 4) { re += w[4] * h4.re; im += w[4] * h4.im; }
+                    if (m >= 5) { re += w[5] * h5.re; im += w[5] * h5.im; }
                     s->u_k[c][idx].re = rf(s, re);
                     s->u_k[c][idx].im = rf(s, im);
                 }
+                s->u_prev5[c][idx] = h4;
                 s->u_prev4[c][idx] = h3;
                 s->u_prev3[c][idx] = h2;
                 s->u_prev2[c][idx] = h1;

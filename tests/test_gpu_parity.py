@@ -211,15 +211,15 @@ def test_bench_configuration_246_axes(capi, oracle, shape, tc):
     """The elastic configuration the benchmark times, on the 6 x 41 engine:
     FP32 fields, gp_zone, zero mode, heterogeneous S_p, tolerance 1e-8
     without the fail-closed rule, the Chebyshev semi-iteration of the
-    increment and the warm start extrapolated to fourth order (bench.py
-    make_params).  Eight steps against the oracle doing the same (the fourth
-    order from the sixth), step by step: iterations within one, every warm
+    increment and the warm start extrapolated to fifth order (bench.py
+    make_params).  Nine steps against the oracle doing the same (the fifth
+    order from the seventh), step by step: iterations within one, every warm
     step converged below 1e-8 on both sides (a warm step at the cap fails),
     fields within the FP32 tolerance."""
     from cuda_sto_pf_gb300.solver import Solver
     p = params_for(capi, "c2.params", n=16, zero_mode_enabled=1, model_mode=1, precision=1,
                    elastic_residual_tolerance=1e-8, elastic_fail_on_nonconvergence=0, elastic_chebyshev=1,
-                   elastic_warm_start_extrapolate=4, fft_tensor_cores=tc)
+                   elastic_warm_start_extrapolate=5, fft_tensor_cores=tc)
     p.Nx, p.Ny, p.Nz = shape
     phi, xB, eta = _inputs(capi, p, 16, True, seed=23, shape=shape)
     o = oracle(p, threads=8)
@@ -227,7 +227,7 @@ def test_bench_configuration_246_axes(capi, oracle, shape, tc):
     so = capi.StepStats()
     with Solver(p) as s:
         s.load(phi, xB, eta)
-        for k in range(8):
+        for k in range(9):
             assert o.step(1, so) == 0
             sg = s.step(1)
             # the cold first step: its increment is most of u, and with FP32
@@ -307,12 +307,13 @@ def test_increment_form_matches_reference_form(capi, oracle, prec):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("order", [1, 2, 3, 4])
+@pytest.mark.parametrize("order", [1, 2, 3, 4, 5])
 def test_extrapolated_warm_start_parity(capi, oracle, prec, order):
     """elastic_warm_start_extrapolate = 1: from the third step the fixed point
     starts at 2 u^n - u^{n-1}; = 2: from the fourth at 3 u^n - 3 u^{n-1} +
     u^{n-2}; = 3: from the fifth at 4 u^n - 6 u^{n-1} + 4 u^{n-2} - u^{n-3};
-    = 4: from the sixth at the quartic.  GPU against the oracle doing the same."""
+    = 4 and 5: from the sixth and seventh at the quartic and quintic.  GPU
+    against the oracle doing the same."""
     from cuda_sto_pf_gb300.solver import Solver
     p = params_for(capi, "c2.params", n=32, precision=prec, elastic_warm_start_extrapolate=order)
     phi, xB, _ = _inputs(capi, p, 32, False, seed=17)
@@ -321,7 +322,7 @@ def test_extrapolated_warm_start_parity(capi, oracle, prec, order):
     so, sg = capi.StepStats(), None
     with Solver(p) as s:
         s.load(phi, xB)
-        for k in range(7):
+        for k in range(8):
             assert o.step(1, so) == 0
             sg = s.step(1)
             assert abs(sg.elastic_iterations - so.elastic_iterations) <= 1, k
