@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <type_traits>
@@ -264,6 +265,8 @@ struct TuneScratch {
     std::vector<void *> p;
     cudaStream_t s;
     bool ok = true;
+    TuneScratch(const TuneScratch &) = delete;
+    TuneScratch &operator=(const TuneScratch &) = delete;
     TuneScratch(int n, size_t bytes, cudaStream_t st) : s(st) {
         for (int i = 0; i < n && ok; ++i) {
             void *q = nullptr;
@@ -328,7 +331,7 @@ static float time_launch(const std::vector<cudaStream_t> &ss, F &&launch) {
 // scratch arrays
 struct TuneStreams {
     std::vector<cudaStream_t> ss;
-    std::vector<TuneScratch *> sc;
+    std::vector<std::unique_ptr<TuneScratch>> sc;
     bool ok = true;
     TuneStreams(cudaStream_t s0, int narr, size_t bytes) {
         const int k = std::max(1, std::min(16, g_tune_copies.load()));
@@ -337,12 +340,14 @@ struct TuneStreams {
             if (i > 0) ok = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess;
             if (!ok) break;
             ss.push_back(s);
-            sc.push_back(new TuneScratch(narr, bytes, s));
+            sc.push_back(std::make_unique<TuneScratch>(narr, bytes, s));
             ok = sc.back()->ok;
         }
     }
+    TuneStreams(const TuneStreams &) = delete;
+    TuneStreams &operator=(const TuneStreams &) = delete;
     ~TuneStreams() {
-        for (TuneScratch *t : sc) delete t;
+        sc.clear();   // stream-ordered frees first
         if (!ss.empty()) cudaStreamSynchronize(ss[0]);
         for (size_t i = 1; i < ss.size(); ++i) {
             cudaStreamSynchronize(ss[i]);
