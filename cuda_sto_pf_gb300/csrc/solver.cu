@@ -2908,16 +2908,19 @@ static pfgb_status elastic_solve(pfgb_ctx *c, pfgb_step_stats *st) {
     if (accel) {
         // The residual test runs on the device (k_resid_step) and the host
         // launches the updates in batches, reading the status once per
-        // batch: the first batch is one update short of the last solve's
-        // count, later ones two.  Updates launched past the stopping point
-        // return at once (c->skip); the Chebyshev buffer swaps they made on
-        // the host are undone below.
+        // batch: the first batch is the last solve's count (with the
+        // extrapolated start the count moves by one at most from step to
+        // step, so one read usually ends the solve), later ones two.
+        // Updates launched past the stopping point return at once
+        // (c->skip): an unneeded update costs its empty launches, a second
+        // batch a host round trip.  The Chebyshev buffer swaps the host made
+        // for updates that returned at once are undone below.
         struct SkipGuard { pfgb_ctx *c; ~SkipGuard() { c->skip = nullptr; } } guard{c};
         k_el_status_reset<<<1, 32, 0, c->stream>>>(c->dscal);
         PFGB_CUDA_TRY(cudaGetLastError());
         c->skip = c->dscal + DS_EL;
         const int imax = std::max(1, P.elastic_iter_max);
-        int batch = c->last_el_iters > 1 ? c->last_el_iters - 1 : 4;
+        int batch = c->last_el_iters > 1 ? c->last_el_iters : 4;
         batch = std::max(1, std::min(std::max(batch, P.elastic_iter_min), imax));
         int launched = 0;
         for (;;) {
