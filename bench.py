@@ -55,6 +55,9 @@ def parse():
                     help="start each elastic solve from the previous solution (the reference's warm start)")
     ap.add_argument("--extrapolate-order", type=int, default=None, choices=[1, 2, 3, 4, 5],
                     help="order of the extrapolated warm start (default: EXTRAPOLATE)")
+    ap.add_argument("--fft-autotune", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="bits of the generic engine's tile autotuner (grids whose axes are not 246 long): "
+                         "1 the x / y passes, 2 the z passes")
     ap.add_argument("--fft-tensor-cores", type=int, default=None,
                     help="1: the 41-point stage of the elastic y passes on the tensor cores (default: FFT_TENSOR_CORES)")
     ap.add_argument("--profile-json", default="")
@@ -79,7 +82,7 @@ def parse():
     ap.add_argument("--sweep-cases", type=int, default=48)
     ap.add_argument("--sweep-iters", type=int, default=500)
     ap.add_argument("--sweep-concurrency", type=int, default=8)
-    ap.add_argument("--sweep-autotune", type=int, default=0, choices=[0, 1],
+    ap.add_argument("--sweep-autotune", type=int, default=0, choices=[0, 1, 2, 3],
                     help="tile autotuner of the generic engine (fft_autotune) in the sweep; the rule's tiles are "
                          "within 3%% of the tuned ones under the sweep's sharing, and tuning costs about 4 s")
     return ap.parse_args()
@@ -106,6 +109,8 @@ EXTRAPOLATE = 5
 # the 41-point stage of the 246-point transforms on the tensor cores
 # (split-precision TF32); --fft-tensor-cores overrides
 FFT_TENSOR_CORES = 0
+# the generic engine's tile autotuner (--fft-autotune); off by default
+FFT_AUTOTUNE = 0
 
 
 def make_params(capi, n, precision, tol, shape=None, chebyshev=None):
@@ -121,6 +126,7 @@ def make_params(capi, n, precision, tol, shape=None, chebyshev=None):
     p.elastic_chebyshev = CHEBYSHEV if chebyshev is None else chebyshev
     p.elastic_warm_start_extrapolate = EXTRAPOLATE if chebyshev is None else 0
     p.fft_tensor_cores = FFT_TENSOR_CORES if chebyshev is None else 0
+    p.fft_autotune = FFT_AUTOTUNE
     capi.finalize(p)
     return p
 
@@ -569,6 +575,7 @@ def run_ours(args):
                                                   4: "extrapolated to fourth order from the last five solutions",
                                                   5: "extrapolated to fifth order from the last six solutions"
                                                   }[EXTRAPOLATE],
+                           "fft_autotune": FFT_AUTOTUNE,
                            "dft41_stage": "tensor cores (tcgen05, split-precision TF32)" if FFT_TENSOR_CORES
                            else "FP32 multiply-adds",
                            "l2": "inputs larger than L2 (working set > 1 GB at 246^3)",
@@ -585,6 +592,7 @@ def run_ours(args):
                 "wall_ms_per_step": 1e3 * wall / args.steps,
                 "device_bytes": dev_bytes,
                 "gpu_launches": launches,
+                "tiles": capi.tile_report().splitlines() if FFT_AUTOTUNE else [],
                 "clocks": clk, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "vs_plain_fp64": plain,
                 "at_reference_default_tol": ref_tol}
         print(json.dumps(line), flush=True)
@@ -828,10 +836,11 @@ def run_fno_step(args):
 
 
 def main():
-    global CHEBYSHEV, EXTRAPOLATE
+    global CHEBYSHEV, EXTRAPOLATE, FFT_AUTOTUNE
     args = parse()
     POPULATION.update(particles=args.particles, median_r=args.median_radius, eta_sites=args.eta_sites)
     CHEBYSHEV = 0 if args.no_chebyshev else 1
+    FFT_AUTOTUNE = args.fft_autotune
     if args.no_extrapolate:
         EXTRAPOLATE = 0
     elif args.extrapolate_order:

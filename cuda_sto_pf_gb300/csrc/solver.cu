@@ -500,7 +500,7 @@ static pfgb_status launch_axis(pfgb_ctx *c, int axis, AxisIO<T, NIN, NOUT> io, O
     while (TK > 1 && bytes(TK) > kSmemBudget) TK >>= 1;
     if (TK < 4 && sizeof(T) == 4 && bytes(4) <= kSmemWide) TK = 4;
     while (TK > 1 && TK / 2 >= c->g.NzC) TK >>= 1;
-    if (c->p.fft_autotune) TK = tuned_tk<T, NIN, NOUT, DIN, DOUT, Op>(c, axis, pl, op, TK, tag);
+    if (c->p.fft_autotune & 1) TK = tuned_tk<T, NIN, NOUT, DIN, DOUT, Op>(c, axis, pl, op, TK, tag);
     const size_t smem = bytes(TK);
     auto kern = k_axis_pass<T, NIN, NOUT, DIN, DOUT, Op>;
     PFGB_CUDA_TRY(allow_smem(kern, smem));
@@ -643,7 +643,7 @@ static pfgb_status launch_z(pfgb_ctx *c, Op op, const char *tag, double extra_by
     while (R > 2 && bytes(R) > kSmemBudget) R >>= 1;
     const long long rows = (long long)c->g.Nx * c->g.Ny;
     while (R > 2 && R / 2 >= rows) R >>= 1;
-    if (c->p.fft_autotune) R = tuned_r<T, NFI, NFO>(c, R, &zpass_bytes<T, NFI, NFO>, tag);
+    if (c->p.fft_autotune & 2) R = tuned_r<T, NFI, NFO>(c, R, &zpass_bytes<T, NFI, NFO>, tag);
     const size_t smem = bytes(R);
     auto kern = k_zpass<T, NFI, NFO, Op>;
     PFGB_CUDA_TRY(allow_smem(kern, smem));

@@ -151,13 +151,14 @@ typedef struct pfgb_params {
        counterpart key in the reference (its transforms are cuFFT's);
        default 0. */
     int32_t fft_tensor_cores;
-    /* 1: the generic transform engine (axes other than 246 long) times its
-       tile candidates on first use, per kernel, grid shape and device, and
-       keeps the fastest for the life of the process: the columns per block
-       of the x and y passes and the rows per block of the z passes
-       (pfgb_tile_report lists them).  0 (default): the fixed rule, the
-       largest tile within 112 KiB of shared memory.  No counterpart key in
-       the reference. */
+    /* Bits: the generic transform engine (axes other than 246 long) times
+       its tile candidates on first use, per kernel, grid shape and device,
+       and keeps the fastest for the life of the process: 1 the columns per
+       block of the x and y passes (timed as themselves), 2 the rows per
+       block of the z passes (timed through a copy op with the same field
+       counts); pfgb_tile_report lists them.  0 (default): the fixed rule,
+       the largest tile within 112 KiB of shared memory.  No counterpart key
+       in the reference. */
     int32_t fft_autotune;
     int32_t pad_fft;
     double elastic_residual_tolerance;

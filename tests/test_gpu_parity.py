@@ -759,14 +759,14 @@ def test_gp_storage_coupling_parity(capi, oracle, case, prec):
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", [0, 1])
 def test_autotuned_tiles_give_the_same_step(capi, prec):
-    """fft_autotune = 1 on the generic engine (48^3): the tiles timed and
+    """fft_autotune = 3 (x / y and z passes) on the generic engine (48^3): the tiles timed and
     chosen per pass, the step's fields equal to the fixed rule's up to the
     order of the block reductions (1e-12 FP64, 1e-6 FP32), and the report
     lists every tuned pass with a tile no slower than the rule's."""
     from cuda_sto_pf_gb300.solver import Solver
     n, steps = 48, 3
     out = []
-    for tune in (0, 1):
+    for tune in (0, 3):
         p = params_for(capi, "c2.params", n=n, precision=prec, fft_autotune=tune)
         phi, xB, _ = _inputs(capi, p, n, False, seed=31)
         with Solver(p) as s:
