@@ -100,8 +100,8 @@ def _run(exe, argv, results):
     env = dict(os.environ, CUDA_STO_RESULTS_ROOT=results)
     r = subprocess.run([exe, *argv], capture_output=True, text=True, timeout=1200, env=env,
                        cwd=os.path.dirname(results))
-    out = os.path.join(REPO, "gpurun_out")
-    if os.path.isdir(out):
+    out = os.environ.get("PFGB_TEST_LOG_DIR", "")
+    if out and os.path.isdir(out):
         tag = os.path.basename(os.path.dirname(results)) + "_" + os.path.basename(results)
         with open(os.path.join(out, f"ref_main_{tag}.log"), "w") as f:
             f.write(" ".join(argv) + f"\nrc={r.returncode}\n" + r.stdout[-20000:] + "\n---- stderr\n" +
@@ -140,8 +140,10 @@ def _case_dir(results):
 
 
 def _report(name, rec):
-    out = os.path.join(REPO, "gpurun_out")
-    if os.path.isdir(out):
+    """One JSON line per case in $PFGB_TEST_LOG_DIR/ref_main_parity.jsonl
+    (when that directory is set and exists)."""
+    out = os.environ.get("PFGB_TEST_LOG_DIR", "")
+    if out and os.path.isdir(out):
         with open(os.path.join(out, "ref_main_parity.jsonl"), "a") as f:
             f.write(json.dumps({"case": name, **rec}) + "\n")
 
