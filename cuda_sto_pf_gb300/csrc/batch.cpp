@@ -38,7 +38,7 @@ pfgb_status run_case(pfgb_case *cs, int device) {
 }
 
 // with fft_autotune, one iteration of the first case of each distinct grid
-// on this thread before the pool starts: the tiles are then timed on an
+// on this thread before the worker threads start: the tiles are then timed on an
 // otherwise idle device, and the cases find them chosen
 void pretune(pfgb_case *cases, int ncases, int device) {
     std::vector<int> seen;

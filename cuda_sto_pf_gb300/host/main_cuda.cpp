@@ -586,7 +586,7 @@ int main(int argc, char **argv) {
     if (c.mode == "dynamics-continue") c.mode = "dynamics";
     if (c.mode == "minimize-continue") { c.mode = "minimize"; c.cont = true; }
     if (c.mode != "dynamics" && c.mode != "minimize") {
-        fprintf(stderr, "[fatal] --mode=%s is not available in this build (dynamics, dynamics-continue, minimize)\n",
+        fprintf(stderr, "[fatal] --mode=%s is not available in this program (dynamics, dynamics-continue, minimize)\n",
                 c.mode.c_str());
         return 2;
     }

@@ -12,7 +12,7 @@ conventions the CUDA path uses, so that parity rests on:
 - numpy.fft for the truncated spectral convolution, and
 - central finite differences of this float64 forward for the gradients.
 
-It is the checker for the CUDA kernels, never the thing measured or shipped.
+It is the oracle for the CUDA kernels, never the thing measured or shipped.
 
 Model (width W = 32, hidden H = 64, IN = 8 inputs, OUT = 3 outputs):
 

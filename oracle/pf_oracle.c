@@ -1,7 +1,7 @@
 /*
  * pf_oracle.c — CPU FP64 restatement of the CUDA_STO_PF dynamics step.
  *
- * TEST INFRASTRUCTURE (the checker).  Only tests/, __graft_entry__.smoke()
+ * TEST INFRASTRUCTURE (the oracle).  Only tests/, __graft_entry__.smoke()
  * and bench.py's cpu_baseline leg use it; the shipped library never does.
  *
  * Each function cites the reference code it restates.  All arithmetic is

@@ -1,7 +1,7 @@
 /*
  * pf_oracle.h — CPU FP64 restatement of the CUDA_STO_PF time step.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker for the CUDA library in
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle for the CUDA library in
  * cuda_sto_pf_gb300/: tests, __graft_entry__.smoke() and bench.py's CPU
  * baseline leg may call it; the product path never does.
  *
